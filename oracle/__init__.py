@@ -1,0 +1,195 @@
+"""TEST INFRASTRUCTURE: ctypes front end of the CPU oracle (oracle/ikarus_oracle.cpp).
+
+The oracle restates the reference's FP64 CPU algorithm for the Newton-Raphson / LoadControl
+hot path.  Only tests/, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use it,
+and only as the checker or the reported CPU baseline; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+EAS_NONE, EAS_GL, EAS_H, EAS_HT = 0, 1, 2, 3
+DBC_RAW, DBC_REDUCED, DBC_FULL = 0, 1, 2
+SOLVER_BANDED_LDLT, SOLVER_CG_JACOBI = 0, 1
+ERRORS = {-1: "ARG", -2: "NOT_IMPLEMENTED", -3: "NONPOSITIVE_DETC", -4: "SINGULAR", -5: "NOT_CONVERGED"}
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, what=""):
+        super().__init__(f"oracle {what} failed: {ERRORS.get(code, code)}")
+        self.code = code
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = C.CDLL(_LIB_PATH)
+        dp, ip, up, lp = (C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint8), C.POINTER(C.c_int64))
+        vp = C.c_void_p
+        L.orc_problem_create.restype = vp
+        L.orc_problem_create.argtypes = [C.c_int, dp, C.c_int, ip, C.c_double, C.c_double, C.c_int, C.c_int]
+        L.orc_problem_destroy.argtypes = [vp]
+        L.orc_set_dirichlet.argtypes = [vp, up]
+        L.orc_add_neumann.argtypes = [vp, C.c_int, ip, ip, dp]
+        L.orc_add_point_loads.argtypes = [vp, C.c_int, ip, dp]
+        L.orc_set_faithful_moduli.argtypes = [vp, C.c_int]
+        L.orc_get_alpha.argtypes = [vp, dp]
+        L.orc_set_alpha.argtypes = [vp, dp]
+        L.orc_element_vector.argtypes = [vp, C.c_int, dp, C.c_double, dp]
+        L.orc_element_matrix.argtypes = [vp, C.c_int, dp, C.c_double, dp]
+        L.orc_element_energy.argtypes = [vp, C.c_int, dp, C.c_double, dp]
+        L.orc_update_state.argtypes = [vp, dp, C.c_double, dp]
+        L.orc_assemble_vector.argtypes = [vp, dp, C.c_double, C.c_int, dp]
+        L.orc_pattern_nnz.restype = C.c_int64
+        L.orc_pattern_nnz.argtypes = [vp, C.c_int]
+        L.orc_reduced_size.argtypes = [vp]
+        L.orc_assemble_matrix_csc.argtypes = [vp, dp, C.c_double, C.c_int, lp, ip, dp]
+        L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, dp, dp, ip, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(C.POINTER(t)) if a is not None else None
+
+
+def _check(code, what):
+    if code != 0:
+        raise OracleError(code, what)
+
+
+class OracleProblem:
+    """One mesh + NeoHooke material + EAS choice, with Dirichlet flags and dead loads."""
+
+    def __init__(self, coords, conn, lam, mu, eas_kind=EAS_NONE, n_alpha=0):
+        self.coords = np.ascontiguousarray(coords, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int32)
+        self.n_nodes, self.n_elems = self.coords.shape[0], self.conn.shape[0]
+        self.n_dofs = 3 * self.n_nodes
+        self.n_alpha = n_alpha
+        L = lib()
+        self.h = L.orc_problem_create(self.n_nodes, _p(self.coords, C.c_double), self.n_elems,
+                                      _p(self.conn, C.c_int32), lam, mu, eas_kind, n_alpha)
+        if not self.h:
+            raise OracleError(-1, "create")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_problem_destroy(self.h)
+            self.h = None
+
+    def set_dirichlet(self, fixed):
+        f = np.ascontiguousarray(fixed, dtype=np.uint8)
+        _check(lib().orc_set_dirichlet(self.h, _p(f, C.c_uint8)), "set_dirichlet")
+
+    def add_neumann(self, face_elem, face_local, traction):
+        fe = np.ascontiguousarray(face_elem, dtype=np.int32)
+        fl = np.ascontiguousarray(face_local, dtype=np.int32)
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(traction, dtype=np.float64), (len(fe), 3)))
+        _check(lib().orc_add_neumann(self.h, len(fe), _p(fe, C.c_int32), _p(fl, C.c_int32), _p(t, C.c_double)),
+               "add_neumann")
+
+    def add_point_loads(self, dofs, values):
+        d = np.ascontiguousarray(dofs, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        _check(lib().orc_add_point_loads(self.h, len(d), _p(d, C.c_int32), _p(v, C.c_double)), "add_point_loads")
+
+    def set_faithful_moduli(self, on=True):
+        _check(lib().orc_set_faithful_moduli(self.h, int(on)), "faithful")
+
+    @property
+    def alpha(self):
+        a = np.zeros(self.n_elems * self.n_alpha)
+        if a.size:
+            _check(lib().orc_get_alpha(self.h, _p(a, C.c_double)), "get_alpha")
+        return a.reshape(self.n_elems, self.n_alpha)
+
+    @alpha.setter
+    def alpha(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+        _check(lib().orc_set_alpha(self.h, _p(a, C.c_double)), "set_alpha")
+
+    def _u(self, u):
+        return np.ascontiguousarray(u if u is not None else np.zeros(self.n_dofs), dtype=np.float64)
+
+    def element_vector(self, e, u=None, lam=0.0):
+        u = self._u(u)
+        out = np.zeros(24)
+        _check(lib().orc_element_vector(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_vector")
+        return out
+
+    def element_matrix(self, e, u=None, lam=0.0):
+        u = self._u(u)
+        out = np.zeros(576)
+        _check(lib().orc_element_matrix(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_matrix")
+        return out.reshape(24, 24).T.copy()  # stored column-major
+
+    def element_energy(self, e, u=None, lam=0.0):
+        u = self._u(u)
+        out = np.zeros(1)
+        _check(lib().orc_element_energy(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_energy")
+        return float(out[0])
+
+    def update_state(self, u, correction, lam=0.0):
+        u = self._u(u)
+        c = np.ascontiguousarray(correction, dtype=np.float64)
+        _check(lib().orc_update_state(self.h, _p(u, C.c_double), lam, _p(c, C.c_double)), "update_state")
+
+    def reduced_size(self):
+        return lib().orc_reduced_size(self.h)
+
+    def assemble_vector(self, u=None, lam=0.0, dbc=DBC_FULL):
+        u = self._u(u)
+        n = self.reduced_size() if dbc == DBC_REDUCED else self.n_dofs
+        out = np.zeros(n)
+        _check(lib().orc_assemble_vector(self.h, _p(u, C.c_double), lam, dbc, _p(out, C.c_double)), "assemble_vector")
+        return out
+
+    def assemble_matrix_csc(self, u=None, lam=0.0, dbc=DBC_FULL):
+        """Returns (col_ptr int64, row_idx int32, values float64, n)."""
+        u = self._u(u)
+        n = self.reduced_size() if dbc == DBC_REDUCED else self.n_dofs
+        nnz = lib().orc_pattern_nnz(self.h, dbc)
+        cp = np.zeros(n + 1, dtype=np.int64)
+        ri = np.zeros(nnz, dtype=np.int32)
+        v = np.zeros(nnz)
+        _check(lib().orc_assemble_matrix_csc(self.h, _p(u, C.c_double), lam, dbc, _p(cp, C.c_int64),
+                                             _p(ri, C.c_int32), _p(v, C.c_double)), "assemble_matrix")
+        return cp, ri, v, n
+
+    def assemble_matrix_dense(self, u=None, lam=0.0, dbc=DBC_FULL):
+        cp, ri, v, n = self.assemble_matrix_csc(u, lam, dbc)
+        A = np.zeros((n, n))
+        for c in range(n):
+            A[ri[cp[c]:cp[c + 1]], c] = v[cp[c]:cp[c + 1]]
+        return A
+
+    def load_control(self, steps, t_begin=0.0, t_end=1.0, tol=1e-10, tol_mode=0, max_iter=20,
+                     solver=SOLVER_BANDED_LDLT, cg_rtol=1e-12, u0=None, lam0=0.0, allow_failure=False):
+        u = self._u(u0).copy()
+        lam = np.array([lam0])
+        its = np.zeros(steps + 1, dtype=np.int32)
+        rn = np.zeros(steps + 1)
+        ns, tot = C.c_int(0), C.c_int(0)
+        code = lib().orc_load_control(self.h, steps, t_begin, t_end, tol, tol_mode, max_iter, solver, cg_rtol,
+                                      _p(u, C.c_double), _p(lam, C.c_double), _p(its, C.c_int32), _p(rn, C.c_double),
+                                      C.byref(ns), C.byref(tot))
+        if code != 0 and not (allow_failure and code == -5):
+            raise OracleError(code, "load_control")
+        return dict(u=u, lam=float(lam[0]), iterations=its[: ns.value], res_norms=rn[: ns.value],
+                    total_iterations=tot.value, success=(code == 0))

@@ -1,0 +1,1032 @@
+// ikarus_oracle.cpp -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
+//
+// CPU FP64 restatement of the reference (ikarus-project/ikarus v0.4.9) hot path for 3D Q1 hexahedra.
+// It is the parity checker for the GPU product and the reported CPU baseline; nothing in the
+// product links it.  Every routine names the reference lines it restates.  The reference's
+// third-party arithmetic (dune-localfefunctions' Green-Lagrange strain, B-operator and geometric
+// stiffness; Dune Q1 geometry and Gauss rules; Eigen's setFromTriplets) is restated from the
+// mathematics those call sites document; parity of that part is pinned by the reference's
+// end-to-end cantilever goldens (tests/src/testcantileverbeamEAS.cpp:60-96) and by
+// finite-difference consistency checks in tests/.
+#include "ikarus_oracle.h"
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+namespace {
+
+constexpr int NN = 8;    // nodes per hexahedron
+constexpr int ND = 24;   // dofs per hexahedron
+constexpr int MAXA = 21; // largest EAS parameter count in 3D (E21)
+
+// Voigt index pairs in the reference order 11,22,33,23,13,12 (tensorutils.hh:180-202).
+constexpr int VA[6] = {0, 1, 2, 1, 0, 0};
+constexpr int VB[6] = {0, 1, 2, 2, 2, 1};
+inline int voigt(int i, int j) {
+  if (i == j) return i;
+  if (i + j == 3) return 3;  // (1,2)
+  if (i + j == 2) return 4;  // (0,2)
+  return 5;                  // (0,1)
+}
+
+struct M3 {
+  double a[3][3];
+};
+
+inline double det3(const double m[3][3]) {
+  return m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+         m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+}
+inline void inv3(const double m[3][3], double r[3][3], double* detOut = nullptr) {
+  const double d = det3(m);
+  const double id = 1.0 / d;
+  r[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]) * id;
+  r[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) * id;
+  r[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) * id;
+  r[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) * id;
+  r[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) * id;
+  r[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) * id;
+  r[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]) * id;
+  r[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) * id;
+  r[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) * id;
+  if (detOut) *detOut = d;
+}
+
+// Dense LU with partial pivoting on an n x n row-major matrix; solves for nrhs columns of B (row-major n x nrhs).
+// Stands in for Eigen's D.inverse() (enhancedassumedstrains.hh:243, 294, 344).
+bool lu_solve(int n, std::vector<double> A, double* B, int nrhs) {
+  std::vector<int> piv(n);
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    double best = std::fabs(A[k * n + k]);
+    for (int i = k + 1; i < n; ++i)
+      if (std::fabs(A[i * n + k]) > best) best = std::fabs(A[i * n + k]), p = i;
+    if (best == 0.0) return false;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) std::swap(A[k * n + j], A[p * n + j]);
+      for (int j = 0; j < nrhs; ++j) std::swap(B[k * nrhs + j], B[p * nrhs + j]);
+    }
+    const double pv = A[k * n + k];
+    for (int i = k + 1; i < n; ++i) {
+      const double f = A[i * n + k] / pv;
+      if (f == 0.0) continue;
+      for (int j = k + 1; j < n; ++j) A[i * n + j] -= f * A[k * n + j];
+      for (int j = 0; j < nrhs; ++j) B[i * nrhs + j] -= f * B[k * nrhs + j];
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    for (int j = 0; j < nrhs; ++j) {
+      double s = B[k * nrhs + j];
+      for (int i = k + 1; i < n; ++i) s -= A[k * n + i] * B[i * nrhs + j];
+      B[k * nrhs + j] = s / A[k * n + k];
+    }
+  }
+  return true;
+}
+
+// Q1 shape functions on the reference cube [0,1]^3 with Dune's vertex numbering:
+// vertex v sits at (v&1, (v>>1)&1, (v>>2)&1).
+void shape_values(const double xi[3], double N[NN]) {
+  for (int v = 0; v < NN; ++v) {
+    double p = 1.0;
+    for (int d = 0; d < 3; ++d) p *= ((v >> d) & 1) ? xi[d] : 1.0 - xi[d];
+    N[v] = p;
+  }
+}
+void shape_gradients(const double xi[3], double dN[NN][3]) {
+  for (int v = 0; v < NN; ++v) {
+    double f[3], df[3];
+    for (int d = 0; d < 3; ++d) {
+      const bool b = (v >> d) & 1;
+      f[d] = b ? xi[d] : 1.0 - xi[d];
+      df[d] = b ? 1.0 : -1.0;
+    }
+    dN[v][0] = df[0] * f[1] * f[2];
+    dN[v][1] = f[0] * df[1] * f[2];
+    dN[v][2] = f[0] * f[1] * df[2];
+  }
+}
+
+// Trilinear geometry at xi: J[i][j] = dx_i/dxi_j, detJ, dN/dX = J^{-T} dN/dxi.
+struct Geo {
+  double J[3][3], Jinv[3][3], detJ, dNdX[NN][3];
+};
+void geometry(const double X[NN][3], const double xi[3], Geo& g) {
+  double dN[NN][3];
+  shape_gradients(xi, dN);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0;
+      for (int v = 0; v < NN; ++v) s += X[v][i] * dN[v][j];
+      g.J[i][j] = s;
+    }
+  inv3(g.J, g.Jinv, &g.detJ);
+  for (int v = 0; v < NN; ++v)
+    for (int k = 0; k < 3; ++k) g.dNdX[v][k] = dN[v][0] * g.Jinv[0][k] + dN[v][1] * g.Jinv[1][k] + dN[v][2] * g.Jinv[2][k];
+}
+
+// 2x2x2 Gauss-Legendre rule on [0,1]^3 (defaultQuadratureRule(element, 2*order), nonlinearelastic.hh:124).
+struct Rule {
+  double xi[8][3];
+  double w[8];
+};
+const Rule& gauss2() {
+  static Rule r = [] {
+    Rule q{};
+    const double a = 0.5 - 0.5 / std::sqrt(3.0), b = 0.5 + 0.5 / std::sqrt(3.0);
+    const double p[2] = {a, b};
+    int k = 0;
+    for (int z = 0; z < 2; ++z)
+      for (int y = 0; y < 2; ++y)
+        for (int x = 0; x < 2; ++x, ++k) {
+          q.xi[k][0] = p[x];
+          q.xi[k][1] = p[y];
+          q.xi[k][2] = p[z];
+          q.w[k] = 0.125;
+        }
+    return q;
+  }();
+  return r;
+}
+
+// NeoHooke on C = 2E + I (neohooke.hh:78-142, strainconversions.hh:93-97, interface.hh:211-242).
+struct MatState {
+  double S[6];      // PK2 in Voigt [S11,S22,S33,S23,S13,S12]
+  double C6[6][6];  // material tangent in Voigt
+  double psi;       // stored energy
+  bool ok;
+};
+void neohooke(double lam, double mu, const double Ev[6], MatState& m, bool wantTangent = true) {
+  double C[3][3];
+  for (int i = 0; i < 3; ++i) C[i][i] = 2.0 * Ev[i] + 1.0;
+  C[1][2] = C[2][1] = Ev[3];
+  C[0][2] = C[2][0] = Ev[4];
+  C[0][1] = C[1][0] = Ev[5];
+  double Ci[3][3], detC;
+  inv3(C, Ci, &detC);
+  m.ok = detC > 1e-10;  // checkPositiveOrAbort with FloatCmp::le(det, 0, 1e-10)
+  const double lnJ = std::log(std::sqrt(detC));
+  const double trC = C[0][0] + C[1][1] + C[2][2];
+  m.psi = mu / 2.0 * (trC - 3.0 - 2.0 * lnJ) + lam / 2.0 * lnJ * lnJ;
+  for (int v = 0; v < 6; ++v) {
+    const int i = VA[v], j = VB[v];
+    m.S[v] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+  }
+  if (!wantTangent) return;
+  const double c = mu - lam * lnJ;
+  for (int r = 0; r < 6; ++r)
+    for (int s = 0; s < 6; ++s) {
+      const int i = VA[r], j = VB[r], k = VA[s], l = VB[s];
+      m.C6[r][s] = lam * Ci[i][j] * Ci[k][l] + c * (Ci[i][k] * Ci[j][l] + Ci[i][l] * Ci[j][k]);
+    }
+}
+
+// Green-Lagrange strain of a displacement gradient, Voigt with doubled shears
+// (dune-localfefunctions greenLagrangeStrains; easfunctions/displacementgradient.hh:86-87).
+void gl_strain(const double H[3][3], double Ev[6]) {
+  double E[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double hh = 0;
+      for (int k = 0; k < 3; ++k) hh += H[k][i] * H[k][j];
+      E[i][j] = 0.5 * (H[i][j] + H[j][i] + hh);
+    }
+  for (int v = 0; v < 6; ++v) Ev[v] = (v < 3 ? 1.0 : 2.0) * E[VA[v]][VB[v]];
+}
+
+// B-operator row layout of the Green-Lagrange strain variation w.r.t. node displacement
+// (easfunctions/displacementgradient.hh:129-146): g_k = F e_k, dN = nodal gradient.
+void bop(const double F[3][3], const double dN[3], double B[6][3]) {
+  for (int a = 0; a < 3; ++a) {
+    const double g0 = F[a][0], g1 = F[a][1], g2 = F[a][2];
+    B[0][a] = dN[0] * g0;
+    B[1][a] = dN[1] * g1;
+    B[2][a] = dN[2] * g2;
+    B[3][a] = dN[2] * g1 + dN[1] * g2;
+    B[4][a] = dN[2] * g0 + dN[0] * g2;
+    B[5][a] = dN[1] * g0 + dN[0] * g1;
+  }
+}
+
+// Strain transformation matrix of tensorutils.hh:438-465 written from its defining rule:
+// T[(a,b)][(c,d)] = (a==b ? 1/2 : 1) * (Jt[a][c] Jt[b][d] + Jt[b][c] Jt[a][d]) with Jt = J^T.
+void transformation_matrix(const double J[3][3], double T[6][6]) {
+  for (int r = 0; r < 6; ++r)
+    for (int s = 0; s < 6; ++s) {
+      const int a = VA[r], b = VB[r], c = VA[s], d = VB[s];
+      const double v = J[c][a] * J[d][b] + J[c][b] * J[d][a];
+      T[r][s] = (a == b) ? 0.5 * v : v;
+    }
+}
+
+// E9 / E21 ansatz before transformation (easvariants/linearandglstrains.hh:252-327):
+// each entry is (row, column, product of the listed (2 xi_k - 1) factors).
+struct AnsatzEntry {
+  int row, col, f1, f2;  // f2 = -1 for a single factor
+};
+constexpr AnsatzEntry kE21[] = {
+    {0, 0, 0, -1},  {1, 1, 1, -1},  {2, 2, 2, -1},  {3, 3, 1, -1},  {3, 4, 2, -1},  {4, 5, 0, -1},
+    {4, 6, 2, -1},  {5, 7, 0, -1},  {5, 8, 1, -1},  {3, 9, 0, 1},   {3, 10, 0, 2},  {4, 11, 0, 1},
+    {4, 12, 1, 2},  {5, 13, 0, 2},  {5, 14, 1, 2},  {0, 15, 0, 1},  {0, 16, 0, 2},  {1, 17, 0, 1},
+    {1, 18, 1, 2},  {2, 19, 0, 2},  {2, 20, 1, 2}};
+
+}  // namespace
+
+struct orc_problem {
+  int nn = 0, ne = 0;
+  std::vector<double> X;      // nn*3
+  std::vector<int32_t> conn;  // ne*8
+  double lam = 0, mu = 0;
+  int eas = 0, na = 0;
+  bool faithful = false;
+  std::vector<uint8_t> fixed;   // n dofs
+  std::vector<double> alpha;    // ne*na
+  // Neumann faces grouped per element
+  std::vector<std::vector<std::pair<int, std::array<double, 3>>>> faces;
+  std::vector<int32_t> pl_dof;
+  std::vector<double> pl_val;
+  // pattern caches
+  std::vector<std::vector<int32_t>> nodeAdj;
+  int ndof() const { return 3 * nn; }
+};
+
+namespace {
+
+struct ElemOut {
+  double f[ND];
+  double K[ND][ND];
+  double D[MAXA * MAXA];
+  double L[MAXA * ND];
+  double Rt[MAXA];
+  double energy;
+  bool ok;
+};
+
+void gather(const orc_problem& p, int e, const double* u, double X[NN][3], double ue[NN][3]) {
+  for (int v = 0; v < NN; ++v) {
+    const int n = p.conn[8 * e + v];
+    for (int c = 0; c < 3; ++c) {
+      X[v][c] = p.X[3 * n + c];
+      ue[v][c] = u ? u[3 * n + c] : 0.0;
+    }
+  }
+}
+
+// Enhanced-strain element at the current (u, alpha): internal force, tangent, D, L, R~ and energy.
+// Restates NonLinearElastic::calculate{Vector,Matrix}Impl (nonlinearelastic.hh:375-430) and
+// EnhancedAssumedStrains::calculate{Vector,Matrix}Impl / calculateDAndLMatrix / calculateRtilde
+// (enhancedassumedstrains.hh:258-434) with the strain functions of easfunctions/*.hh.
+void element_internal(const orc_problem& p, int e, const double* u, bool wantK, ElemOut& out) {
+  double X[NN][3], ue[NN][3];
+  gather(p, e, u, X, ue);
+  const int na = p.na;
+  const int kind = na > 0 ? p.eas : ORC_EAS_NONE;
+  const double* al = na > 0 ? &p.alpha[(size_t)e * na] : nullptr;
+  std::memset(&out, 0, sizeof(out));
+  out.ok = true;
+
+  // centre data (helperfunctions.hh:19-36, displacementgradienttransposed.hh:336-369)
+  Geo g0;
+  const double xc[3] = {0.5, 0.5, 0.5};
+  geometry(X, xc, g0);
+  double T0inv[6][6] = {};
+  if (kind == ORC_EAS_GL) {
+    double T[6][6];
+    transformation_matrix(g0.J, T);
+    std::vector<double> A(36), B(36, 0.0);
+    for (int r = 0; r < 6; ++r)
+      for (int s = 0; s < 6; ++s) A[r * 6 + s] = T[r][s] * g0.detJ;
+    for (int r = 0; r < 6; ++r) B[r * 6 + r] = 1.0;
+    lu_solve(6, A, B.data(), 6);
+    for (int r = 0; r < 6; ++r)
+      for (int s = 0; s < 6; ++s) T0inv[r][s] = B[r * 6 + s];
+  }
+  double JIT0[3][3];  // jacobianInverseTransposed at the centre = J0^{-T}
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) JIT0[i][j] = g0.Jinv[j][i];
+  double Fc0[3][3];  // compatible deformation gradient at the centre (H9T)
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = (i == j) ? 1.0 : 0.0;
+      for (int v = 0; v < NN; ++v) s += ue[v][i] * g0.dNdX[v][j];
+      Fc0[i][j] = s;
+    }
+
+  const Rule& R = gauss2();
+  for (int q = 0; q < 8; ++q) {
+    Geo g;
+    geometry(X, R.xi[q], g);
+    const double wdJ = R.w[q] * g.detJ;
+    double Hc[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double s = 0;
+        for (int v = 0; v < NN; ++v) s += ue[v][i] * g.dNdX[v][j];
+        Hc[i][j] = s;
+      }
+
+    // EAS ansatz at this Gauss point
+    double M[6][MAXA] = {};      // GL: E~ = M alpha
+    double Hp[MAXA][3][3] = {};  // H, HT: enhancement matrices (transformed)
+    if (kind == ORC_EAS_GL) {
+      double M0[6][MAXA] = {};
+      for (int k = 0; k < na; ++k) {
+        const AnsatzEntry& a = kE21[k];
+        double v = 2.0 * R.xi[q][a.f1] - 1.0;
+        if (a.f2 >= 0) v *= 2.0 * R.xi[q][a.f2] - 1.0;
+        M0[a.row][a.col] = v;
+      }
+      for (int r = 0; r < 6; ++r)
+        for (int k = 0; k < na; ++k) {
+          double s = 0;
+          for (int t = 0; t < 6; ++t) s += T0inv[r][t] * M0[t][k];
+          M[r][k] = s / g.detJ;
+        }
+    } else if (kind == ORC_EAS_H || kind == ORC_EAS_HT) {
+      // H9 (easvariants/displacementgradient.hh:136-161): mode p = 3r+c has entry (r,c) = 2 xi_c - 1,
+      // transformed by (detJ0/detJ) J0^{-T} H J0^{-1} (helperfunctions.hh:27-36).
+      const double sc = g0.detJ / g.detJ;
+      for (int pm = 0; pm < na; ++pm) {
+        const int r = pm / 3, c = pm % 3;
+        const double val = 2.0 * R.xi[q][c] - 1.0;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) Hp[pm][i][j] = sc * JIT0[i][r] * val * JIT0[j][c];
+      }
+    }
+
+    // displacement gradient actually used, F, modified nodal gradients
+    double H[3][3];
+    std::memcpy(H, Hc, sizeof(H));
+    double Ht[3][3] = {};  // sum_p alpha_p H_p
+    if (kind == ORC_EAS_H || kind == ORC_EAS_HT) {
+      for (int pm = 0; pm < na; ++pm)
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) Ht[i][j] += Hp[pm][i][j] * al[pm];
+      if (kind == ORC_EAS_H) {
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) H[i][j] += Ht[i][j];
+      } else {  // H = Hc + Fc0 Ht^T (displacementgradienttransposed.hh:353-368)
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            double s = 0;
+            for (int k = 0; k < 3; ++k) s += Fc0[i][k] * Ht[j][k];
+            H[i][j] += s;
+          }
+      }
+    }
+    double F[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) F[i][j] = H[i][j] + (i == j ? 1.0 : 0.0);
+    double Ev[6];
+    gl_strain(H, Ev);
+    if (kind == ORC_EAS_GL)
+      for (int r = 0; r < 6; ++r)
+        for (int k = 0; k < na; ++k) Ev[r] += M[r][k] * al[k];
+
+    MatState m;
+    neohooke(p.lam, p.mu, Ev, m, true);
+    if (!m.ok) out.ok = false;
+    out.energy += m.psi * wdJ;
+    double Smat[3][3];
+    for (int v = 0; v < 6; ++v) Smat[VA[v]][VB[v]] = Smat[VB[v]][VA[v]] = m.S[v];
+
+    // nodal gradients entering B and kg (HT modifies them: displacementgradienttransposed.hh:126-140)
+    double dN[NN][3];
+    for (int v = 0; v < NN; ++v)
+      for (int k = 0; k < 3; ++k) {
+        dN[v][k] = g.dNdX[v][k];
+        if (kind == ORC_EAS_HT)
+          dN[v][k] += Ht[k][0] * g0.dNdX[v][0] + Ht[k][1] * g0.dNdX[v][1] + Ht[k][2] * g0.dNdX[v][2];
+      }
+    double B[NN][6][3];
+    for (int v = 0; v < NN; ++v) bop(F, dN[v], B[v]);
+
+    // internal forces f_I += B_I^T S w detJ (nonlinearelastic.hh:335-342)
+    for (int v = 0; v < NN; ++v)
+      for (int a = 0; a < 3; ++a) {
+        double s = 0;
+        for (int r = 0; r < 6; ++r) s += B[v][r][a] * m.S[r];
+        out.f[3 * v + a] += s * wdJ;
+      }
+
+    if (wantK) {
+      // K_IJ += (B_I^T C B_J + kg_IJ) w detJ (nonlinearelastic.hh:294-322, 387-398)
+      for (int I = 0; I < NN; ++I)
+        for (int Jn = 0; Jn < NN; ++Jn) {
+          MatState mm;
+          const MatState* mp = &m;
+          if (p.faithful) {  // the reference evaluates the moduli inside the (i,j) loop
+            neohooke(p.lam, p.mu, Ev, mm, true);
+            mp = &mm;
+          }
+          double CB[6][3];
+          for (int r = 0; r < 6; ++r)
+            for (int b = 0; b < 3; ++b) {
+              double s = 0;
+              for (int t = 0; t < 6; ++t) s += mp->C6[r][t] * B[Jn][t][b];
+              CB[r][b] = s;
+            }
+          double kg = 0;
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) kg += dN[I][i] * Smat[i][j] * dN[Jn][j];
+          for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+              double s = 0;
+              for (int r = 0; r < 6; ++r) s += B[I][r][a] * CB[r][b];
+              if (a == b) s += kg;
+              out.K[3 * I + a][3 * Jn + b] += s * wdJ;
+            }
+        }
+    }
+
+    if (na > 0) {
+      // E_alpha (6 x na)
+      double Ea[6][MAXA] = {};
+      double Haux[MAXA][3][3];  // H~_p used by H / HT
+      if (kind == ORC_EAS_GL) {
+        std::memcpy(Ea, M, sizeof(Ea));
+      } else {
+        for (int pm = 0; pm < na; ++pm) {
+          if (kind == ORC_EAS_H) {
+            std::memcpy(Haux[pm], Hp[pm], sizeof(Haux[pm]));
+          } else {  // Fc0 H_p^T (displacementgradienttransposed.hh:155-158)
+            for (int i = 0; i < 3; ++i)
+              for (int j = 0; j < 3; ++j) {
+                double s = 0;
+                for (int k = 0; k < 3; ++k) s += Fc0[i][k] * Hp[pm][j][k];
+                Haux[pm][i][j] = s;
+              }
+          }
+          // M(v,p) = sym(F^T Haux_p) in Voigt (displacementgradient.hh:153-166)
+          const double(*h)[3] = Haux[pm];
+          auto col_dot = [&](int ci, int gj) { return h[0][ci] * F[0][gj] + h[1][ci] * F[1][gj] + h[2][ci] * F[2][gj]; };
+          Ea[0][pm] = col_dot(0, 0);
+          Ea[1][pm] = col_dot(1, 1);
+          Ea[2][pm] = col_dot(2, 2);
+          Ea[3][pm] = col_dot(2, 1) + col_dot(1, 2);
+          Ea[4][pm] = col_dot(2, 0) + col_dot(0, 2);
+          Ea[5][pm] = col_dot(1, 0) + col_dot(0, 1);
+        }
+      }
+      // C Ea
+      double CEa[6][MAXA];
+      for (int r = 0; r < 6; ++r)
+        for (int k = 0; k < na; ++k) {
+          double s = 0;
+          for (int t = 0; t < 6; ++t) s += m.C6[r][t] * Ea[t][k];
+          CEa[r][k] = s;
+        }
+      // D += (Ea^T C Ea + E_aa) w detJ (enhancedassumedstrains.hh:400)
+      for (int a = 0; a < na; ++a)
+        for (int b = 0; b < na; ++b) {
+          double s = 0;
+          for (int r = 0; r < 6; ++r) s += Ea[r][a] * CEa[r][b];
+          if (kind != ORC_EAS_GL) {  // E_aa (displacementgradient.hh:213-230)
+            double kgab = 0;
+            for (int i = 0; i < 3; ++i)
+              for (int j = 0; j < 3; ++j) {
+                const double sij = 0.5 * Smat[i][j];
+                double c1 = 0, c2 = 0;
+                for (int k = 0; k < 3; ++k) {
+                  c1 += Haux[a][k][i] * Haux[b][k][j];
+                  c2 += Haux[a][k][j] * Haux[b][k][i];
+                }
+                kgab += sij * (c1 + c2);
+              }
+            s += kgab;
+          }
+          out.D[a * na + b] += s * wdJ;
+        }
+      // R~ += Ea^T S w detJ (enhancedassumedstrains.hh:428)
+      for (int a = 0; a < na; ++a) {
+        double s = 0;
+        for (int r = 0; r < 6; ++r) s += Ea[r][a] * m.S[r];
+        out.Rt[a] += s * wdJ;
+      }
+      // L(:, 3I..3I+2) += (Ea^T C B_I + E_ad) w detJ (enhancedassumedstrains.hh:401-408)
+      for (int I = 0; I < NN; ++I)
+        for (int a = 0; a < na; ++a)
+          for (int b = 0; b < 3; ++b) {
+            double s = 0;
+            for (int r = 0; r < 6; ++r) s += CEa[r][a] * B[I][r][b];
+            if (kind == ORC_EAS_H) {  // displacementgradient.hh:231-254
+              double kad = 0;
+              for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                  kad += 0.5 * Smat[i][j] * (Haux[a][b][i] * g.dNdX[I][j] + Haux[a][b][j] * g.dNdX[I][i]);
+              s += kad;
+            } else if (kind == ORC_EAS_HT) {  // displacementgradienttransposed.hh:272-319
+              double hv[3];  // H_a dN0_I
+              for (int i = 0; i < 3; ++i)
+                hv[i] = Hp[a][i][0] * g0.dNdX[I][0] + Hp[a][i][1] * g0.dNdX[I][1] + Hp[a][i][2] * g0.dNdX[I][2];
+              double kad = 0;
+              for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j)
+                  kad += 0.5 * Smat[i][j] *
+                         (Haux[a][b][i] * dN[I][j] + Haux[a][b][j] * dN[I][i] + hv[i] * F[b][j] + hv[j] * F[b][i]);
+              s += kad;
+            }
+            out.L[a * ND + 3 * I + b] += s * wdJ;
+          }
+    }
+  }
+}
+
+// Dead traction on the element's Neumann faces, 1-point rule (loads/traction.hh:105-138).
+void element_traction(const orc_problem& p, int e, double lambda, double f[ND], const double* u, double* energy) {
+  if (p.faces.empty() || p.faces[e].empty()) return;
+  double X[NN][3], ue[NN][3];
+  gather(p, e, u, X, ue);
+  for (const auto& fc : p.faces[e]) {
+    const int lf = fc.first;
+    const int d = lf / 2;
+    double xi[3] = {0.5, 0.5, 0.5};
+    xi[d] = (lf % 2) ? 1.0 : 0.0;
+    double N[NN], dN[NN][3];
+    shape_values(xi, N);
+    shape_gradients(xi, dN);
+    int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+    double a[3], b[3];
+    for (int c = 0; c < 3; ++c) {
+      a[c] = b[c] = 0;
+      for (int v = 0; v < NN; ++v) a[c] += X[v][c] * dN[v][t1], b[c] += X[v][c] * dN[v][t2];
+    }
+    const double cr[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    const double dA = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    const double t[3] = {lambda * fc.second[0], lambda * fc.second[1], lambda * fc.second[2]};
+    if (f)
+      for (int v = 0; v < NN; ++v)
+        for (int c = 0; c < 3; ++c) f[3 * v + c] -= N[v] * t[c] * 1.0 * dA;
+    if (energy) {
+      double uv[3] = {0, 0, 0};
+      for (int v = 0; v < NN; ++v)
+        for (int c = 0; c < 3; ++c) uv[c] += N[v] * ue[v][c];
+      *energy -= (t[0] * uv[0] + t[1] * uv[1] + t[2] * uv[2]) * dA;
+    }
+  }
+}
+
+// Condensed element vector / matrix (enhancedassumedstrains.hh:291-296, 336-345).
+int element_vector(const orc_problem& p, int e, const double* u, double lambda, double out[ND]) {
+  ElemOut eo;
+  element_internal(p, e, u, false, eo);
+  if (!eo.ok) return ORC_ERR_NONPOSITIVE_DETC;
+  std::memcpy(out, eo.f, sizeof(eo.f));
+  const int na = p.na;
+  if (na > 0) {
+    std::vector<double> Dm(eo.D, eo.D + na * na), y(eo.Rt, eo.Rt + na);
+    if (!lu_solve(na, Dm, y.data(), 1)) return ORC_ERR_SINGULAR;
+    for (int k = 0; k < ND; ++k) {
+      double s = 0;
+      for (int a = 0; a < na; ++a) s += eo.L[a * ND + k] * y[a];
+      out[k] -= s;
+    }
+  }
+  element_traction(p, e, lambda, out, nullptr, nullptr);
+  return ORC_OK;
+}
+
+int element_matrix(const orc_problem& p, int e, const double* u, double K[ND][ND]) {
+  static thread_local ElemOut eo;
+  element_internal(p, e, u, true, eo);
+  if (!eo.ok) return ORC_ERR_NONPOSITIVE_DETC;
+  std::memcpy(K, eo.K, sizeof(eo.K));
+  const int na = p.na;
+  if (na > 0) {
+    std::vector<double> Dm(eo.D, eo.D + na * na), Y(eo.L, eo.L + na * ND);
+    if (!lu_solve(na, Dm, Y.data(), ND)) return ORC_ERR_SINGULAR;
+    for (int r = 0; r < ND; ++r)
+      for (int c = r; c < ND; ++c) {
+        double s = 0;
+        for (int a = 0; a < na; ++a) s += eo.L[a * ND + r] * Y[a * ND + c];
+        K[r][c] -= s;
+      }
+    for (int r = 0; r < ND; ++r)
+      for (int c = 0; c < r; ++c) K[r][c] = K[c][r];
+  }
+  return ORC_OK;
+}
+
+// sparsity: node adjacency (nodes sharing an element), sorted
+void build_adjacency(orc_problem& p) {
+  if (!p.nodeAdj.empty()) return;
+  p.nodeAdj.assign(p.nn, {});
+  for (int e = 0; e < p.ne; ++e)
+    for (int a = 0; a < NN; ++a)
+      for (int b = 0; b < NN; ++b) p.nodeAdj[p.conn[8 * e + a]].push_back(p.conn[8 * e + b]);
+  for (auto& v : p.nodeAdj) {
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+  }
+}
+
+std::vector<int32_t> constraints_below(const orc_problem& p) {
+  // FlatAssemblerBase ctor (assembler/interface.hh:50-62)
+  std::vector<int32_t> cb(p.ndof());
+  int32_t c = 0;
+  for (int i = 0; i < p.ndof(); ++i) {
+    cb[i] = c;
+    if (p.fixed[i]) ++c;
+  }
+  return cb;
+}
+
+struct CSC {
+  int n = 0;
+  std::vector<int64_t> cp;
+  std::vector<int32_t> ri;
+  std::vector<double> v;
+};
+
+// createOccupationPattern / createReducedOccupationPattern + setFromTriplets (simpleassemblers.inl:206-251):
+// column-major, row indices sorted, duplicates merged.
+void build_pattern(orc_problem& p, int dbc, CSC& A) {
+  build_adjacency(p);
+  const bool red = dbc == ORC_DBC_REDUCED;
+  auto cb = constraints_below(p);
+  const int n = red ? p.ndof() - (p.ndof() ? cb[p.ndof() - 1] + p.fixed[p.ndof() - 1] : 0) : p.ndof();
+  A.n = n;
+  A.cp.assign(n + 1, 0);
+  A.ri.clear();
+  for (int J = 0; J < p.nn; ++J)
+    for (int b = 0; b < 3; ++b) {
+      const int gc = 3 * J + b;
+      if (red && p.fixed[gc]) continue;
+      for (int I : p.nodeAdj[J])
+        for (int a = 0; a < 3; ++a) {
+          const int gr = 3 * I + a;
+          if (red && p.fixed[gr]) continue;
+          A.ri.push_back(red ? gr - cb[gr] : gr);
+        }
+      const int col = red ? gc - cb[gc] : gc;
+      A.cp[col + 1] = (int64_t)A.ri.size();
+    }
+  A.v.assign(A.ri.size(), 0.0);
+}
+
+int64_t linear_index(const CSC& A, int r, int c) {
+  const int32_t* b = A.ri.data() + A.cp[c];
+  const int32_t* e = A.ri.data() + A.cp[c + 1];
+  const int32_t* it = std::lower_bound(b, e, r);
+  return (int64_t)(it - A.ri.data());
+}
+
+int assemble_matrix(orc_problem& p, const double* u, int dbc, CSC& A) {
+  build_pattern(p, dbc, A);
+  auto cb = constraints_below(p);
+  static thread_local double K[ND][ND];
+  for (int e = 0; e < p.ne; ++e) {
+    int st = element_matrix(p, e, u, K);
+    if (st) return st;
+    int dofs[ND];
+    for (int v = 0; v < NN; ++v)
+      for (int c = 0; c < 3; ++c) dofs[3 * v + c] = 3 * p.conn[8 * e + v] + c;
+    // column-major scatter through linear indices (simpleassemblers.inl:120-137, 253-265)
+    for (int c = 0; c < ND; ++c)
+      for (int r = 0; r < ND; ++r) {
+        int gr = dofs[r], gc = dofs[c];
+        if (dbc == ORC_DBC_REDUCED) {
+          if (p.fixed[gr] || p.fixed[gc]) continue;
+          gr -= cb[gr];
+          gc -= cb[gc];
+        }
+        A.v[linear_index(A, gr, gc)] += K[r][c];
+      }
+  }
+  if (dbc == ORC_DBC_FULL) {  // simpleassemblers.inl:159-167 (explicit zeros stay stored)
+    for (int c = 0; c < A.n; ++c)
+      for (int64_t k = A.cp[c]; k < A.cp[c + 1]; ++k) {
+        const int r = A.ri[k];
+        if (p.fixed[c] || p.fixed[r]) A.v[k] = (r == c) ? 1.0 : 0.0;
+      }
+  }
+  return ORC_OK;
+}
+
+int assemble_vector(orc_problem& p, const double* u, double lambda, int dbc, std::vector<double>& out) {
+  auto cb = constraints_below(p);
+  const int n = p.ndof();
+  std::vector<double> full(n, 0.0);
+  double fe[ND];
+  for (int e = 0; e < p.ne; ++e) {
+    int st = element_vector(p, e, u, lambda, fe);
+    if (st) return st;
+    for (int v = 0; v < NN; ++v)
+      for (int c = 0; c < 3; ++c) full[3 * p.conn[8 * e + v] + c] += fe[3 * v + c];
+  }
+  if (dbc == ORC_DBC_REDUCED) {
+    out.assign(n - (n ? cb[n - 1] + p.fixed[n - 1] : 0), 0.0);
+    for (int i = 0; i < n; ++i)
+      if (!p.fixed[i]) out[i - cb[i]] = full[i];
+    for (size_t k = 0; k < p.pl_dof.size(); ++k)
+      if (!p.fixed[p.pl_dof[k]]) out[p.pl_dof[k] - cb[p.pl_dof[k]]] += lambda * p.pl_val[k];
+  } else {
+    if (dbc == ORC_DBC_FULL)
+      for (int i = 0; i < n; ++i)
+        if (p.fixed[i]) full[i] = 0.0;
+    for (size_t k = 0; k < p.pl_dof.size(); ++k) full[p.pl_dof[k]] += lambda * p.pl_val[k];
+    out.swap(full);
+  }
+  return ORC_OK;
+}
+
+// Banded LDL^T (no pivoting) for the symmetric Full-DBC tangent; stands in for the reference's
+// sparse direct solvers (UmfPackLU / SimplicialLDLT).
+bool banded_ldlt_solve(const CSC& A, const std::vector<double>& b, std::vector<double>& x) {
+  const int n = A.n;
+  int bw = 0;
+  for (int c = 0; c < n; ++c)
+    for (int64_t k = A.cp[c]; k < A.cp[c + 1]; ++k) bw = std::max(bw, std::abs(A.ri[k] - c));
+  const int w = bw + 1;
+  // lower band storage: Lb[i*w + (i-j)] for j in [i-bw, i]
+  std::vector<double> Lb((size_t)n * w, 0.0);
+  for (int c = 0; c < n; ++c)
+    for (int64_t k = A.cp[c]; k < A.cp[c + 1]; ++k) {
+      const int r = A.ri[k];
+      if (r >= c) Lb[(size_t)r * w + (r - c)] = A.v[k];
+    }
+  std::vector<double> d(n);
+  for (int j = 0; j < n; ++j) {
+    double dj = Lb[(size_t)j * w];
+    const int k0 = std::max(0, j - bw);
+    for (int k = k0; k < j; ++k) {
+      const double l = Lb[(size_t)j * w + (j - k)];
+      dj -= l * l * d[k];
+    }
+    if (dj == 0.0 || !std::isfinite(dj)) return false;
+    d[j] = dj;
+    const int iend = std::min(n - 1, j + bw);
+    for (int i = j + 1; i <= iend; ++i) {
+      double s = Lb[(size_t)i * w + (i - j)];
+      const int kk0 = std::max(k0, i - bw);
+      for (int k = kk0; k < j; ++k) s -= Lb[(size_t)i * w + (i - k)] * Lb[(size_t)j * w + (j - k)] * d[k];
+      Lb[(size_t)i * w + (i - j)] = s / dj;
+    }
+  }
+  x = b;
+  for (int i = 0; i < n; ++i) {
+    double s = x[i];
+    for (int k = std::max(0, i - bw); k < i; ++k) s -= Lb[(size_t)i * w + (i - k)] * x[k];
+    x[i] = s;
+  }
+  for (int i = 0; i < n; ++i) x[i] /= d[i];
+  for (int i = n - 1; i >= 0; --i) {
+    double s = x[i];
+    for (int k = i + 1; k <= std::min(n - 1, i + bw); ++k) s -= Lb[(size_t)k * w + (k - i)] * x[k];
+    x[i] = s;
+  }
+  return true;
+}
+
+// Jacobi-preconditioned CG (the reference's si_ConjugateGradient: Eigen ConjugateGradient with its
+// default diagonal preconditioner, linearsolver.cpp:23-25), relative tolerance on ||r||/||b||.
+bool cg_jacobi_solve(const CSC& A, const std::vector<double>& b, std::vector<double>& x, double rtol, int maxit) {
+  const int n = A.n;
+  std::vector<double> diag(n, 1.0), r(b), z(n), pv(n), q(n);
+  for (int c = 0; c < n; ++c)
+    for (int64_t k = A.cp[c]; k < A.cp[c + 1]; ++k)
+      if (A.ri[k] == c && A.v[k] != 0.0) diag[c] = A.v[k];
+  x.assign(n, 0.0);
+  double bn = 0;
+  for (double v : b) bn += v * v;
+  bn = std::sqrt(bn);
+  if (bn == 0) return true;
+  for (int i = 0; i < n; ++i) z[i] = r[i] / diag[i];
+  pv = z;
+  double rz = 0;
+  for (int i = 0; i < n; ++i) rz += r[i] * z[i];
+  for (int it = 0; it < maxit; ++it) {
+    std::fill(q.begin(), q.end(), 0.0);
+    for (int c = 0; c < n; ++c) {  // symmetric: q = A p
+      const double pc = pv[c];
+      for (int64_t k = A.cp[c]; k < A.cp[c + 1]; ++k) q[A.ri[k]] += A.v[k] * pc;
+    }
+    double pq = 0;
+    for (int i = 0; i < n; ++i) pq += pv[i] * q[i];
+    const double al = rz / pq;
+    double rn = 0;
+    for (int i = 0; i < n; ++i) {
+      x[i] += al * pv[i];
+      r[i] -= al * q[i];
+      rn += r[i] * r[i];
+    }
+    if (std::sqrt(rn) <= rtol * bn) return true;
+    double rzn = 0;
+    for (int i = 0; i < n; ++i) {
+      z[i] = r[i] / diag[i];
+      rzn += r[i] * z[i];
+    }
+    const double be = rzn / rz;
+    rz = rzn;
+    for (int i = 0; i < n; ++i) pv[i] = z[i] + be * pv[i];
+  }
+  return false;
+}
+
+// EAS internal-state update at the old displacement (enhancedassumedstrains.hh:225-248).
+int update_state(orc_problem& p, const double* u, const double* corr) {
+  if (p.na == 0) return ORC_OK;
+  const int na = p.na;
+  std::vector<double> newAlpha(p.alpha);
+  for (int e = 0; e < p.ne; ++e) {
+    ElemOut eo;
+    element_internal(p, e, u, false, eo);
+    if (!eo.ok) return ORC_ERR_NONPOSITIVE_DETC;
+    std::vector<double> rhs(na);
+    for (int a = 0; a < na; ++a) {
+      double s = eo.Rt[a];
+      for (int v = 0; v < NN; ++v)
+        for (int c = 0; c < 3; ++c) s += eo.L[a * ND + 3 * v + c] * corr[3 * p.conn[8 * e + v] + c];
+      rhs[a] = s;
+    }
+    std::vector<double> Dm(eo.D, eo.D + na * na);
+    if (!lu_solve(na, Dm, rhs.data(), 1)) return ORC_ERR_SINGULAR;
+    for (int a = 0; a < na; ++a) newAlpha[(size_t)e * na + a] -= rhs[a];
+  }
+  p.alpha.swap(newAlpha);
+  return ORC_OK;
+}
+
+double norm2(const std::vector<double>& v) {
+  double s = 0;
+  for (double x : v) s += x * x;
+  return std::sqrt(s);
+}
+
+}  // namespace
+
+extern "C" {
+
+orc_problem* orc_problem_create(int n_nodes, const double* coords, int n_elems, const int32_t* conn, double lambda,
+                                double mu, int eas_kind, int n_alpha) {
+  if (n_nodes <= 0 || n_elems <= 0 || !coords || !conn) return nullptr;
+  if (eas_kind < 0 || eas_kind > 3) return nullptr;
+  if (n_alpha != 0) {
+    if (eas_kind == ORC_EAS_NONE) return nullptr;
+    if (eas_kind == ORC_EAS_GL && n_alpha != 9 && n_alpha != 21) return nullptr;
+    if ((eas_kind == ORC_EAS_H || eas_kind == ORC_EAS_HT) && n_alpha != 9) return nullptr;
+  }
+  auto* p = new orc_problem;
+  p->nn = n_nodes;
+  p->ne = n_elems;
+  p->X.assign(coords, coords + 3 * (size_t)n_nodes);
+  p->conn.assign(conn, conn + 8 * (size_t)n_elems);
+  p->lam = lambda;
+  p->mu = mu;
+  p->eas = eas_kind;
+  p->na = n_alpha;
+  p->fixed.assign(3 * (size_t)n_nodes, 0);
+  p->alpha.assign((size_t)n_elems * n_alpha, 0.0);
+  return p;
+}
+void orc_problem_destroy(orc_problem* p) { delete p; }
+int orc_set_dirichlet(orc_problem* p, const uint8_t* f) {
+  if (!p || !f) return ORC_ERR_ARG;
+  for (int i = 0; i < p->ndof(); ++i) p->fixed[i] = f[i] ? 1 : 0;
+  return ORC_OK;
+}
+int orc_add_neumann(orc_problem* p, int nf, const int32_t* fe, const int32_t* fl, const double* t) {
+  if (!p || nf < 0) return ORC_ERR_ARG;
+  if (p->faces.empty()) p->faces.assign(p->ne, {});
+  for (int k = 0; k < nf; ++k) {
+    if (fe[k] < 0 || fe[k] >= p->ne || fl[k] < 0 || fl[k] > 5) return ORC_ERR_ARG;
+    p->faces[fe[k]].push_back({fl[k], {t[3 * k], t[3 * k + 1], t[3 * k + 2]}});
+  }
+  return ORC_OK;
+}
+int orc_add_point_loads(orc_problem* p, int n, const int32_t* dofs, const double* vals) {
+  if (!p || n < 0) return ORC_ERR_ARG;
+  for (int k = 0; k < n; ++k) {
+    if (dofs[k] < 0 || dofs[k] >= p->ndof()) return ORC_ERR_ARG;
+    p->pl_dof.push_back(dofs[k]);
+    p->pl_val.push_back(vals[k]);
+  }
+  return ORC_OK;
+}
+int orc_set_faithful_moduli(orc_problem* p, int on) {
+  if (!p) return ORC_ERR_ARG;
+  p->faithful = on != 0;
+  return ORC_OK;
+}
+int orc_get_alpha(const orc_problem* p, double* a) {
+  if (!p || !a) return ORC_ERR_ARG;
+  std::copy(p->alpha.begin(), p->alpha.end(), a);
+  return ORC_OK;
+}
+int orc_set_alpha(orc_problem* p, const double* a) {
+  if (!p || !a) return ORC_ERR_ARG;
+  std::copy(a, a + p->alpha.size(), p->alpha.begin());
+  return ORC_OK;
+}
+int orc_element_vector(orc_problem* p, int e, const double* u, double lambda, double* out) {
+  if (!p || e < 0 || e >= p->ne || !out) return ORC_ERR_ARG;
+  return element_vector(*p, e, u, lambda, out);
+}
+int orc_element_matrix(orc_problem* p, int e, const double* u, double lambda, double* out) {
+  (void)lambda;
+  if (!p || e < 0 || e >= p->ne || !out) return ORC_ERR_ARG;
+  static thread_local double K[ND][ND];
+  int st = element_matrix(*p, e, u, K);
+  if (st) return st;
+  for (int c = 0; c < ND; ++c)
+    for (int r = 0; r < ND; ++r) out[c * ND + r] = K[r][c];
+  return ORC_OK;
+}
+int orc_element_energy(orc_problem* p, int e, const double* u, double lambda, double* energy) {
+  if (!p || e < 0 || e >= p->ne || !energy) return ORC_ERR_ARG;
+  if (p->na > 0) return ORC_ERR_NOT_IMPLEMENTED;  // enhancedassumedstrains.hh:305-309
+  ElemOut eo;
+  element_internal(*p, e, u, false, eo);
+  if (!eo.ok) return ORC_ERR_NONPOSITIVE_DETC;
+  double en = eo.energy;
+  element_traction(*p, e, lambda, nullptr, u, &en);
+  *energy = en;
+  return ORC_OK;
+}
+int orc_update_state(orc_problem* p, const double* u, double lambda, const double* corr) {
+  (void)lambda;
+  if (!p || !corr) return ORC_ERR_ARG;
+  return update_state(*p, u, corr);
+}
+int orc_assemble_vector(orc_problem* p, const double* u, double lambda, int dbc, double* out) {
+  if (!p || !out || dbc < 0 || dbc > 2) return ORC_ERR_ARG;
+  std::vector<double> v;
+  int st = assemble_vector(*p, u, lambda, dbc, v);
+  if (st) return st;
+  std::copy(v.begin(), v.end(), out);
+  return ORC_OK;
+}
+int64_t orc_pattern_nnz(orc_problem* p, int dbc) {
+  if (!p || dbc < 0 || dbc > 2) return ORC_ERR_ARG;
+  CSC A;
+  build_pattern(*p, dbc, A);
+  return (int64_t)A.ri.size();
+}
+int orc_reduced_size(orc_problem* p) {
+  if (!p) return ORC_ERR_ARG;
+  int c = 0;
+  for (auto f : p->fixed) c += f;
+  return p->ndof() - c;
+}
+int orc_assemble_matrix_csc(orc_problem* p, const double* u, double lambda, int dbc, int64_t* cp, int32_t* ri,
+                            double* v) {
+  (void)lambda;
+  if (!p || dbc < 0 || dbc > 2) return ORC_ERR_ARG;
+  CSC A;
+  int st = assemble_matrix(*p, u, dbc, A);
+  if (st) return st;
+  if (cp) std::copy(A.cp.begin(), A.cp.end(), cp);
+  if (ri) std::copy(A.ri.begin(), A.ri.end(), ri);
+  if (v) std::copy(A.v.begin(), A.v.end(), v);
+  return ORC_OK;
+}
+
+int orc_load_control(orc_problem* p, int steps, double t0, double t1, double tol, int tol_mode, int max_iter,
+                     int solver, double cg_rtol, double* u, double* lambda, int32_t* iterations, double* res_norms,
+                     int* n_solves, int* total_iterations) {
+  if (!p || !u || !lambda || steps <= 0) return ORC_ERR_ARG;
+  const int n = p->ndof();
+  std::vector<double> x(u, u + n), R, dx;
+  const double step = (t1 - t0) / steps;  // loadcontrol.hh:77
+  int total = 0, solves = 0;
+  CSC K;
+  for (int s = 0; s <= steps; ++s) {
+    if (s > 0) *lambda += step;  // LoadControl::predictor (loadcontrol.inl:54-57)
+    int st = assemble_vector(*p, x.data(), *lambda, ORC_DBC_FULL, R);
+    if (st) return st;
+    double rn = norm2(R);
+    const double thr = tol_mode == 1 ? tol * rn : tol;
+    int it = 0;
+    while (rn > thr && it < max_iter) {  // newtonraphson.hh:219
+      st = assemble_matrix(*p, x.data(), ORC_DBC_FULL, K);
+      if (st) return st;
+      std::vector<double> b(n);
+      for (int i = 0; i < n; ++i) b[i] = -R[i];
+      bool ok = solver == ORC_SOLVER_CG_JACOBI ? cg_jacobi_solve(K, b, dx, cg_rtol, 20 * n)
+                                               : banded_ldlt_solve(K, b, dx);
+      if (!ok) return ORC_ERR_SINGULAR;
+      st = update_state(*p, x.data(), dx.data());  // CORRECTION_UPDATED before x += dx (newtonraphson.hh:230-233)
+      if (st) return st;
+      for (int i = 0; i < n; ++i) x[i] += dx[i];
+      st = assemble_vector(*p, x.data(), *lambda, ORC_DBC_FULL, R);
+      if (st) return st;
+      rn = norm2(R);
+      ++it;
+    }
+    if (iterations) iterations[s] = it;
+    if (res_norms) res_norms[s] = rn;
+    total += it;
+    ++solves;
+    if (n_solves) *n_solves = solves;
+    if (total_iterations) *total_iterations = total;
+    std::copy(x.begin(), x.end(), u);
+    if (it == max_iter) return ORC_ERR_NOT_CONVERGED;  // success = (iter != maxIter)
+  }
+  return ORC_OK;
+}
+
+}  // extern "C"

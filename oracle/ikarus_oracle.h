@@ -1,0 +1,88 @@
+/*
+ * ikarus_oracle.h -- TEST INFRASTRUCTURE, NOT PRODUCT CODE.
+ *
+ * C interface of the CPU oracle: a plain-C++ FP64 restatement of the reference
+ * (ikarus-project/ikarus v0.4.9) nonlinear-mechanics hot path for Q1 hexahedra:
+ * NeoHooke material, displacement-based and EAS elements (GL-E9/E21, H9, H9T),
+ * dead Neumann tractions, the flat sparse assembler with Raw/Full/Reduced
+ * Dirichlet handling, a direct solve, Newton-Raphson and LoadControl.
+ *
+ * Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * load this library, and only as the checker / reported CPU baseline.
+ * The GPU product (ikarus_gb300/) never links or calls it.
+ *
+ * All functions return 0 on success and a negative status on failure
+ * (see ORC_* below).  Dof numbering is the reference's FlatInterleaved one:
+ * global dof = 3*node + component.  Element-local dofs are node-major:
+ * local k = 3*i + c (ikarus/finiteelements/fehelper.hh:145-153).
+ */
+#ifndef IKARUS_ORACLE_H
+#define IKARUS_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  ORC_OK = 0,
+  ORC_ERR_ARG = -1,
+  ORC_ERR_NOT_IMPLEMENTED = -2,  /* mirrors DUNE_THROW(NotImplemented) */
+  ORC_ERR_NONPOSITIVE_DETC = -3, /* mirrors checkPositiveOrAbort (materialhelpers.hh:119-126) */
+  ORC_ERR_SINGULAR = -4,
+  ORC_ERR_NOT_CONVERGED = -5
+};
+
+/* EAS kinds: 0 = none (NonLinearElastic), 1 = Green-Lagrange (E9/E21),
+ * 2 = displacement gradient (H9), 3 = displacement gradient transposed (H9T). */
+enum { ORC_EAS_NONE = 0, ORC_EAS_GL = 1, ORC_EAS_H = 2, ORC_EAS_HT = 3 };
+/* DBCOption (ikarus/assembler/dirichletbcenforcement.hh:8) */
+enum { ORC_DBC_RAW = 0, ORC_DBC_REDUCED = 1, ORC_DBC_FULL = 2 };
+/* linear solvers of the oracle */
+enum { ORC_SOLVER_BANDED_LDLT = 0, ORC_SOLVER_CG_JACOBI = 1 };
+
+typedef struct orc_problem orc_problem;
+
+orc_problem* orc_problem_create(int n_nodes, const double* coords, int n_elems, const int32_t* conn,
+                                double lambda, double mu, int eas_kind, int n_alpha);
+void orc_problem_destroy(orc_problem* p);
+int orc_set_dirichlet(orc_problem* p, const uint8_t* fixed_dofs);
+/* Dead Neumann load on element faces (Dune face numbering: 2d -> xi_d = 0, 2d+1 -> xi_d = 1).
+ * traction: 3 values per face = t(X_face_center, lambda = 1); the applied load is lambda * t. */
+int orc_add_neumann(orc_problem* p, int n_faces, const int32_t* face_elem, const int32_t* face_local,
+                    const double* traction);
+/* Manipulator-style point loads: after the Dirichlet treatment, R[dof] += lambda * value. */
+int orc_add_point_loads(orc_problem* p, int n, const int32_t* dofs, const double* values);
+/* When set, the tangent moduli are recomputed for every (i,j) node pair of every Gauss point,
+ * as the reference does (nonlinearelastic.hh:318 called from :395).  Results are identical. */
+int orc_set_faithful_moduli(orc_problem* p, int on);
+
+int orc_get_alpha(const orc_problem* p, double* alpha);
+int orc_set_alpha(orc_problem* p, const double* alpha);
+
+/* element level (calculateVector / calculateMatrix / calculateScalar) */
+int orc_element_vector(orc_problem* p, int e, const double* u, double lambda, double* out24);
+int orc_element_matrix(orc_problem* p, int e, const double* u, double lambda, double* out576_colmajor);
+int orc_element_energy(orc_problem* p, int e, const double* u, double lambda, double* energy);
+int orc_update_state(orc_problem* p, const double* u, double lambda, const double* correction);
+
+/* assembler */
+int orc_assemble_vector(orc_problem* p, const double* u, double lambda, int dbc, double* out);
+/* returns nnz; pass NULL arrays to query sizes.  CSC: col_ptr (ncols+1), row_idx (nnz), values (nnz) */
+int64_t orc_pattern_nnz(orc_problem* p, int dbc);
+int orc_assemble_matrix_csc(orc_problem* p, const double* u, double lambda, int dbc, int64_t* col_ptr,
+                            int32_t* row_idx, double* values);
+int orc_reduced_size(orc_problem* p);
+
+/* Newton-Raphson (newtonraphson.hh:193-257) under LoadControl (loadcontrol.inl:17-52).
+ * tol_mode 0: absolute ||R|| <= tol (reference default); 1: ||R|| <= tol * ||R at step start||.
+ * u (in/out, n dofs), lambda0 in *lambda (in/out).
+ * iterations[steps+1], res_norms[steps+1]: per solve (index 0 = initial equilibrium solve).
+ * Returns ORC_OK, or ORC_ERR_NOT_CONVERGED with the number of completed solves in *n_solves. */
+int orc_load_control(orc_problem* p, int load_steps, double t_begin, double t_end, double tol, int tol_mode,
+                     int max_iter, int solver, double cg_rtol, double* u, double* lambda, int32_t* iterations,
+                     double* res_norms, int* n_solves, int* total_iterations);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
