@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark: time to ||R||/||R0|| < 1e-8 on every load step of one load path (20 LoadControl steps) on the
+128x32x32 jittered Q1 Neo-Hooke cantilever (131072 elements, 421443 dofs), mixed-precision form
+(FP32 tangent / FP32 block-Jacobi CG, FP64 residual, Eisenstat-Walker inexact Newton) against the plain FP64
+GPU form (FP64 tangent, FP64 block-Jacobi CG to 1e-10), plus the roofline of the dominant kernel (the CG SpMV).
+
+A step = one complete load path from the undeformed state.  `value` is device time per load path with the
+inputs resident in HBM; `e2e` adds the host->device copy of the initial displacement and the device->host
+copy of the converged displacement, through the public API.  Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time to ||R||/||R0||<1e-8 per load path (mixed vs plain FP64 GPU)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--load-steps", type=int, default=20)
+    ap.add_argument("--plain-runs", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--small", action="store_true", help="32x8x8 mesh (profiling runs)")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.rows, self.proc, self.gpu = [], None, gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------------------------------------
+def solver_settings(ikr, mixed: bool):
+    if mixed:
+        return ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                              linear_rtol_min=1e-5, linear_max_iter=200000)
+    return ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, linear_rtol=1e-10, linear_max_iter=400000)
+
+
+class Form:
+    """One solution form (mixed or plain) on the GPU: element set, assembler, solver objects, requirements."""
+
+    def __init__(self, ikr, problems, p, mixed):
+        self.ikr = ikr
+        self.fes, self.asm = problems.build_gpu(p, precision=1 if mixed else 0)
+        self.ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
+        self.nr = ikr.NewtonRaphson(self.asm, ikr.NewtonRaphsonConfig(solver_settings(ikr, mixed), self.ls))
+        self.lc = ikr.LoadControl(self.nr, p.load_steps, (0.0, p.t_end))
+        self.req = ikr.FERequirements(self.fes)
+        self.req0 = ikr.FERequirements(self.fes)  # undeformed state, load factor 0 (device resident)
+        self.asm.bind(self.req, ikr.DBCOption.Full)
+
+    def run_device(self):
+        self.req.assign(self.req0)
+        return self.lc.run(self.req)
+
+
+def make_events(torch, stream_ptr):
+    st = torch.cuda.ExternalStream(stream_ptr)
+    return st, torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def spmv_bytes(asm, n_nodes, value_bytes):
+    """Algorithmic bytes of one fused CG SpMV launch: values + column indices + row pointers of the 3x3-block
+    matrix, and the four dof vectors it streams (z, p_old read; p_new, q written)."""
+    rp, col = asm.block_pattern()
+    nb = len(col)
+    n = 3 * n_nodes
+    return nb * (9 * value_bytes + 4) + 4 * (n_nodes + 1) + 4 * n * value_bytes, nb
+
+
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+
+    import ikarus_gb300 as ikr
+    from ikarus_gb300 import problems
+
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    p = problems.cantilever(32, 8, 8, jitter=0.1, seed=2024, load_steps=args.load_steps, tol=1e-8, relative=True) \
+        if args.small else problems.config2(load_steps=args.load_steps)
+    n_nodes = p.mesh.n_nodes
+    mixed = Form(ikr, problems, p, mixed=True)
+    stream, ev0, ev1 = make_events(torch, mixed.fes.stream())
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up
+    for _ in range(args.warmup):
+        info = mixed.run_device()
+        assert info.success, "mixed-precision load path failed"
+    barrier()
+
+    # timed: device-resident inputs
+    times, infos = [], []
+    launches0 = ikr.kernel_launches()
+    mixed.ls.profile(True)
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            mixed.req.assign(mixed.req0)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            info = mixed.lc.run(mixed.req)
+            ev1.record(stream)
+            ev1.synchronize()
+            times.append(ev0.elapsed_time(ev1) / 1e3)
+            infos.append(info)
+    spmv_ms, spmv_n = mixed.ls.profile_read()
+    mixed.ls.profile(False)
+    launches = (ikr.kernel_launches() - launches0) // max(1, args.steps)
+    assert all(i.success for i in infos)
+    t_mixed = sum(times) / len(times)
+    if world > 1:
+        t = torch.tensor([t_mixed], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_mixed = float(t.item())
+
+    # e2e: public API with host buffers (h2d initial displacement, d2h converged displacement)
+    u0 = np.zeros(p.n_dofs)
+    e2e = []
+    for _ in range(min(args.steps, 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        mixed.req.insertGlobalSolution(u0)
+        mixed.req.insertParameter(0.0)
+        info = mixed.lc.run(mixed.req)
+        u = mixed.req.globalSolution()
+        e2e.append(time.perf_counter() - t0)
+        assert info.success and np.isfinite(u).all()
+    t_e2e = sum(e2e) / len(e2e)
+
+    # plain FP64 form of the same method
+    del flush
+    plain = Form(ikr, problems, p, mixed=False)
+    pstream, pev0, pev1 = make_events(torch, plain.fes.stream())
+    plain_times, plain_infos = [], []
+    for _ in range(args.plain_runs):
+        plain.req.assign(plain.req0)
+        torch.cuda.synchronize()
+        pev0.record(pstream)
+        pinfo = plain.lc.run(plain.req)
+        pev1.record(pstream)
+        pev1.synchronize()
+        plain_times.append(pev0.elapsed_time(pev1) / 1e3)
+        plain_infos.append(pinfo)
+    t_plain = sum(plain_times) / len(plain_times)
+    u_plain = plain.req.globalSolution()
+    u_mixed = mixed.req.globalSolution()
+    rel_diff = float(np.abs(u_mixed - u_plain).max() / np.abs(u_plain).max())
+
+    # roofline of the dominant kernel (the fused CG SpMV, FP32 in the mixed form)
+    bpl, nb = spmv_bytes(mixed.asm, n_nodes, 4)
+    avg_s = spmv_ms / max(spmv_n, 1) / 1e3
+    pk = peaks()
+    peak = pk["hbm_gbs"] if pk else 6800.0
+    achieved = bpl / avg_s / 1e9 if avg_s > 0 else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "spmv_fp32_dram_traffic.json")
+    if os.path.exists(tf) and not args.small:
+        try:
+            traffic = json.load(open(tf)).get("bytes_per_launch_config2")
+        except (OSError, ValueError):
+            traffic = None
+
+    info0 = infos[-1]
+    newton = [s.iterations for s in info0.solverInfos]
+    out = {
+        "metric": METRIC,
+        "value": round(t_mixed, 4),
+        "unit": "s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(t_mixed * 1e3, 2),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 tangent/CG + fp64 residual (mixed); fp64 (plain)",
+        "data": "synthetic (seeded jittered mesh, the configuration's shapes; no dataset involved)",
+        "config": {"workload": p.name, "elements": p.mesh.n_elems, "nodes": n_nodes, "dofs": p.n_dofs,
+                   "load_steps": p.load_steps, "tolerance": "||R||/||R0|| < 1e-8 every load step",
+                   "material": "NeoHooke E=1000 nu=0.3", "parallelism": f"replicas x{world}",
+                   "l2": "256 MB buffer written between timed load paths; working set > L2"},
+        "plain_fp64": {"s_per_load_path": round(t_plain, 4), "newton_iterations": plain_infos[-1].totalIterations,
+                       "cg_iterations": plain_infos[-1].totalLinearIterations},
+        "mixed": {"newton_iterations": info0.totalIterations, "cg_iterations": info0.totalLinearIterations,
+                  "newton_per_step": newton, "max_rel_diff_vs_plain": rel_diff},
+        "speedup_vs_plain_fp64": round(t_plain / t_mixed, 3),
+        "e2e": {"value": round(t_e2e, 4), "unit": "s", "h2d_bytes_per_step": 8 * p.n_dofs,
+                "d2h_bytes_per_step": 8 * p.n_dofs},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "pcg_spmv_kernel<float>", "achieved": round(achieved, 1) if achieved
+                     else None, "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": bpl, "avg_launch_us": round(avg_s * 1e6, 3),
+                     "launches": spmv_n, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback"},
+        "clocks": clocks.summary(),
+    }
+    return out, p
+
+
+# ---------------------------------------------------------------------------------------------------------
+def cpu_sample(plain_newton, plain_cg, steps=1, warmup=0):
+    """Oracle (1 thread) on the 64x16x16 cantilever: one residual + tangent assembly (reference-faithful
+    per-(i,j) moduli evaluation) and 50 Jacobi-CG iterations; scaled per element and per nonzero to the
+    128x32x32 mesh and to the Newton / CG iteration counts of the plain FP64 GPU run."""
+    import numpy as np
+
+    import oracle
+    from ikarus_gb300 import problems
+
+    small = problems.cantilever(64, 16, 16, jitter=0.1, seed=2024)
+    big_elems = 128 * 32 * 32
+    big_nnz = 9 * (3 * 129 - 2) * (3 * 33 - 2) * (3 * 33 - 2)
+    o = oracle.from_problem(small, faithful=True)
+    u = np.zeros(small.n_dofs)
+    vals = []
+    for k in range(warmup + steps):
+        t0 = time.perf_counter()
+        o.assemble_vector(u, 0.05)
+        t1 = time.perf_counter()
+        cp, ri, v, n = o.assemble_matrix_csc(u, 0.05)
+        t2 = time.perf_counter()
+        # 50 Jacobi-CG iterations as a vectorised-free scalar loop would be slow in Python: time the CSC SpMV
+        import scipy.sparse as sp
+        A = sp.csc_matrix((v, ri, cp), shape=(n, n))
+        x = np.ones(n)
+        t3 = time.perf_counter()
+        for _ in range(50):
+            y = A @ x
+            x = y / np.abs(y).max()
+        t4 = time.perf_counter()
+        t_res = (t1 - t0) * big_elems / small.mesh.n_elems
+        t_mat = (t2 - t1) * big_elems / small.mesh.n_elems
+        t_it = (t4 - t3) / 50 * big_nnz / len(v)
+        est = plain_newton * (t_res + t_mat) + plain_cg * t_it
+        if k >= warmup:
+            vals.append(est)
+    return sum(vals) / len(vals), dict(t_residual_s=t_res, t_tangent_s=t_mat, t_cg_iteration_s=t_it)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # the reference's CPU implementation of the path: the oracle port (the reference cannot be built here)
+        newton, cg = 100, 100000  # counts of the plain FP64 GPU run, overwritten when a bench record exists
+        rec = os.path.join(ROOT, "profiles", "bench_counts.json")
+        if os.path.exists(rec):
+            try:
+                d = json.load(open(rec))
+                newton, cg = d["plain_newton_iterations"], d["plain_cg_iterations"]
+            except (OSError, ValueError, KeyError):
+                pass
+        vals = []
+        for k in range(args.warmup + args.steps):
+            v, parts = cpu_sample(newton, cg)
+            if k >= args.warmup:
+                vals.append(v)
+        val = sum(vals) / len(vals)
+        sample = ("oracle port, 1 thread: R+K assembly and 50 CG SpMVs on the 64x16x16 cantilever, scaled to the "
+                  "128x32x32 mesh and to the plain FP64 GPU run's Newton/CG counts")
+        print(json.dumps({"metric": METRIC, "value": round(val, 2), "unit": "s", "impl": "reference", "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+                          "config": {"workload": "cantilever_128x32x32_jittered", "load_steps": args.load_steps},
+                          "cpu_baseline": {"value": round(val, 2), "unit": "s", "cores": 1, "kind": "port",
+                                           "sample": sample, **{k: round(x, 6) for k, x in parts.items()}},
+                          "e2e": {"value": round(val, 2), "unit": "s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    out, p = run_ours(args, rank, world)
+    if rank == 0:
+        os.makedirs(os.path.join(ROOT, "profiles"), exist_ok=True)
+        if not args.no_cpu_baseline and not args.small:
+            v, parts = cpu_sample(out["plain_fp64"]["newton_iterations"], out["plain_fp64"]["cg_iterations"])
+            out["cpu_baseline"] = {"value": round(v, 2), "unit": "s", "cores": 1, "kind": "port",
+                                   "sample": "oracle port, 1 thread: one R+K assembly (reference-faithful moduli) "
+                                             "and 50 CSC SpMVs on the 64x16x16 cantilever, scaled per element and "
+                                             "per nonzero to 128x32x32 and to the plain FP64 run's Newton/CG counts",
+                                   **{k: round(x, 6) for k, x in parts.items()}}
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,644 @@
+"""GB300-native Newton-Raphson / LoadControl path for Q1 hexahedral Neo-Hookean solids.
+
+Python front end over the C ABI of ``include/ikarus_gb300.h`` (``ikarus_gb300/_build/libikarus_gb300.so``),
+with the reference's names (ikarus-project/ikarus v0.4.9): finite elements with ``calculateVector`` /
+``calculateMatrix`` / ``calculateScalar``, ``FERequirements``, ``SparseFlatAssembler`` with ``DBCOption``,
+``LinearSolver``, ``NewtonRaphson`` and ``LoadControl`` with observers.  All arithmetic runs in the CUDA
+library on the GPU; there is no CPU path, and every call fails loudly when the library or a GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import mesh  # noqa: F401  (re-export)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libikarus_gb300.so")
+_lib = None
+
+
+class IkarusError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{_STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_STATUS = {-1: "ARG", -2: "NOT_IMPLEMENTED", -3: "INVALID_STATE", -4: "NONPOSITIVE_DETC", -5: "NOT_CONVERGED",
+           -6: "CG_BREAKDOWN", -7: "CUDA", -8: "SINGULAR", -9: "NO_DEVICE"}
+
+
+class DBCOption(enum.IntEnum):  # ikarus/assembler/dirichletbcenforcement.hh:8
+    Raw = 0
+    Reduced = 1
+    Full = 2
+
+
+class VectorAffordance(enum.IntEnum):  # ikarus/finiteelements/ferequirements.hh:35-89
+    noAffordance = 0
+    forces = 1
+
+
+class MatrixAffordance(enum.IntEnum):
+    noAffordance = 0
+    stiffness = 1
+
+
+class ScalarAffordance(enum.IntEnum):
+    noAffordance = 0
+    mechanicalPotentialEnergy = 1
+
+
+class EAS(enum.IntEnum):  # strain measure enhanced by the EAS skill (strainenhancements/easfunctions/)
+    none = 0
+    GreenLagrangeStrain = 1
+    DisplacementGradient = 2
+    DisplacementGradientTransposed = 3
+
+
+class SolverTypeTag(enum.IntEnum):  # ikarus/solver/linearsolver/linearsolver.hh:28-31 (+ device solvers)
+    none = 0
+    si_ConjugateGradient = 1
+    gpu_PCG_BlockJacobi = 100
+
+
+class Precision(enum.IntEnum):
+    fp64 = 0
+    fp32 = 1
+
+
+class NonLinearSolverMessages(enum.IntEnum):  # ikarus/utils/broadcaster/broadcastermessages.hh:23-24
+    INIT = 0
+    ITERATION_STARTED = 1
+    ITERATION_ENDED = 2
+    RESIDUALNORM_UPDATED = 3
+    CORRECTIONNORM_UPDATED = 4
+    CORRECTION_UPDATED = 5
+    SOLUTION_CHANGED = 6
+    FINISHED_SUCESSFULLY = 7
+
+
+class ControlMessages(enum.IntEnum):  # broadcastermessages.hh:18
+    CONTROL_STARTED = 0
+    CONTROL_ENDED = 1
+    STEP_STARTED = 2
+    STEP_ENDED = 3
+    SOLUTION_CHANGED = 4
+
+
+class _NRSettings(C.Structure):
+    _fields_ = [("tol", C.c_double), ("max_iter", C.c_int32), ("min_iter", C.c_int32), ("tol_mode", C.c_int32),
+                ("forcing", C.c_int32), ("linear_rtol", C.c_double), ("linear_rtol_min", C.c_double),
+                ("linear_max_iter", C.c_int32), ("refinements", C.c_int32)]
+
+
+class _NRInfo(C.Structure):
+    _fields_ = [("success", C.c_int32), ("residual_norm", C.c_double), ("correction_norm", C.c_double),
+                ("iterations", C.c_int32), ("linear_iterations", C.c_int64)]
+
+
+class _NRState(C.Structure):
+    _fields_ = [("domain", C.c_void_p), ("residual_norm", C.c_double), ("correction_norm", C.c_double),
+                ("iterations", C.c_int32), ("load_factor", C.c_double)]
+
+
+class _ControlState(C.Structure):
+    _fields_ = [("domain", C.c_void_p), ("load_step", C.c_int32), ("step_size", C.c_double),
+                ("load_factor", C.c_double)]
+
+
+class _ControlInfo(C.Structure):
+    _fields_ = [("success", C.c_int32), ("total_iterations", C.c_int32), ("n_solver_infos", C.c_int32),
+                ("total_linear_iterations", C.c_int64)]
+
+
+_NR_OBS = C.CFUNCTYPE(None, C.c_int32, C.POINTER(_NRState), C.c_void_p)
+_CTRL_OBS = C.CFUNCTYPE(None, C.c_int32, C.POINTER(_ControlState), C.c_void_p)
+
+# exported entry points and their ctypes signatures (kept in sync with include/ikarus_gb300.h)
+_vp, _dp, _ip, _i64p, _u8p = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64), \
+    C.POINTER(C.c_uint8)
+_I, _D, _L = C.c_int32, C.c_double, C.c_int64
+SIGNATURES = {
+    "ikr_version": ([], C.c_int),
+    "ikr_last_error": ([C.c_char_p, _I], C.c_int),
+    "ikr_kernel_launches": ([], C.c_int64),
+    "ikr_fes_create": ([C.POINTER(_vp), _I, _dp, _I, _ip, _D, _D, _I, _I], C.c_int),
+    "ikr_fes_add_neumann": ([_vp, _I, _ip, _ip, _dp], C.c_int),
+    "ikr_fes_destroy": ([_vp], C.c_int),
+    "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
+    "ikr_fes_get_alpha": ([_vp, _dp], C.c_int),
+    "ikr_fes_set_alpha": ([_vp, _dp], C.c_int),
+    "ikr_fe_calculate_vector": ([_vp, _vp, _I, _I, _I, _dp], C.c_int),
+    "ikr_fe_calculate_matrix": ([_vp, _vp, _I, _I, _I, _dp], C.c_int),
+    "ikr_fe_calculate_scalar": ([_vp, _vp, _I, _I, _I, _dp], C.c_int),
+    "ikr_fe_update_state": ([_vp, _vp, _dp, _I], C.c_int),
+    "ikr_req_create": ([C.POINTER(_vp), _vp], C.c_int),
+    "ikr_req_destroy": ([_vp], C.c_int),
+    "ikr_req_insert_global_solution": ([_vp, _dp], C.c_int),
+    "ikr_req_global_solution": ([_vp, _dp], C.c_int),
+    "ikr_req_insert_parameter": ([_vp, _D], C.c_int),
+    "ikr_req_parameter": ([_vp, _dp], C.c_int),
+    "ikr_req_solution_device": ([_vp, C.POINTER(_dp)], C.c_int),
+    "ikr_req_copy": ([_vp, _vp], C.c_int),
+    "ikr_assembler_create": ([C.POINTER(_vp), _vp, _u8p, _I], C.c_int),
+    "ikr_assembler_destroy": ([_vp], C.c_int),
+    "ikr_assembler_add_point_loads": ([_vp, _I, _ip, _dp], C.c_int),
+    "ikr_assembler_bind": ([_vp, _vp, _I], C.c_int),
+    "ikr_assembler_size": ([_vp, _ip], C.c_int),
+    "ikr_assembler_reduced_size": ([_vp, _ip], C.c_int),
+    "ikr_assembler_constraints_below": ([_vp, _ip], C.c_int),
+    "ikr_assembler_vector": ([_vp, _vp, _I, _I, _dp], C.c_int),
+    "ikr_assembler_matrix": ([_vp, _vp, _I, _I], C.c_int),
+    "ikr_assembler_matrix_nnz": ([_vp, _I, _i64p], C.c_int),
+    "ikr_assembler_export_csc": ([_vp, _I, _i64p, _ip, _dp], C.c_int),
+    "ikr_assembler_block_pattern": ([_vp, _ip, _i64p, _ip, _ip], C.c_int),
+    "ikr_assembler_vector_norm": ([_vp, _dp], C.c_int),
+    "ikr_linear_solver_create": ([C.POINTER(_vp), _I], C.c_int),
+    "ikr_linear_solver_destroy": ([_vp], C.c_int),
+    "ikr_linear_solver_set_tolerance": ([_vp, _D, _I], C.c_int),
+    "ikr_linear_solver_analyze_pattern": ([_vp, _vp], C.c_int),
+    "ikr_linear_solver_factorize": ([_vp, _vp], C.c_int),
+    "ikr_linear_solver_solve": ([_vp, _vp, _dp, _dp], C.c_int),
+    "ikr_linear_solver_last_info": ([_vp, _ip, _dp], C.c_int),
+    "ikr_linear_solver_profile": ([_vp, _I], C.c_int),
+    "ikr_linear_solver_profile_read": ([_vp, _dp, _i64p], C.c_int),
+    "ikr_fes_stream": ([_vp, C.POINTER(_vp)], C.c_int),
+    "ikr_nr_settings_default": ([C.POINTER(_NRSettings)], C.c_int),
+    "ikr_newton_create": ([C.POINTER(_vp), _vp, _vp, C.POINTER(_NRSettings)], C.c_int),
+    "ikr_newton_destroy": ([_vp], C.c_int),
+    "ikr_newton_subscribe": ([_vp, _NR_OBS, _vp], C.c_int),
+    "ikr_newton_subscribe_fe_state": ([_vp, _I], C.c_int),
+    "ikr_newton_solve": ([_vp, _vp, _D, C.POINTER(_NRInfo)], C.c_int),
+    "ikr_load_control_create": ([C.POINTER(_vp), _vp, _I, _D, _D], C.c_int),
+    "ikr_load_control_destroy": ([_vp], C.c_int),
+    "ikr_load_control_subscribe": ([_vp, _CTRL_OBS, _vp], C.c_int),
+    "ikr_load_control_run": ([_vp, _vp, C.POINTER(_ControlInfo), C.POINTER(_NRInfo), _I], C.c_int),
+}
+
+
+def lib():
+    """The loaded CUDA library; raises if it was not built (there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"CUDA library missing: {LIB_PATH} (run __graft_entry__.build())")
+        L = C.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+    return _lib
+
+
+def _err(code, what=""):
+    if code != 0:
+        buf = C.create_string_buffer(512)
+        lib().ikr_last_error(buf, 512)
+        raise IkarusError(code, f"{what}: {buf.value.decode(errors='replace')}")
+
+
+def _ptr(a, t=C.c_double):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def kernel_launches() -> int:
+    return int(lib().ikr_kernel_launches())
+
+
+# ---- materials --------------------------------------------------------------------------------------------
+def toLamesFirstParameterAndShearModulus(emodul: float, nu: float):
+    """(E, nu) -> (lambda, mu) (ikarus/finiteelements/physicshelper.hh:81-85, 123-127, 276-280)."""
+    lam = float("inf") if nu == 0.5 else emodul * nu / ((1.0 + nu) * (1.0 - 2.0 * nu))
+    return lam, emodul / (2.0 * (1.0 + nu))
+
+
+@dataclass
+class NeoHooke:
+    """Compressible Neo-Hooke law on C (materials/hyperelastic/neohooke.hh:37-208)."""
+    lambda_: float
+    mu: float
+
+    @classmethod
+    def from_E_nu(cls, E, nu):
+        return cls(*toLamesFirstParameterAndShearModulus(E, nu))
+
+
+# ---- finite elements -------------------------------------------------------------------------------------
+class FiniteElements:
+    """All elements of one Q1 hexahedral mesh with skills nonLinearElastic(NeoHooke) [+ eas<ES>(n)]
+    [+ neumannBoundaryLoad], bound to their grid elements (the reference's ``std::vector<FE>``)."""
+
+    def __init__(self, coords, conn, material: NeoHooke, eas: EAS = EAS.none, n_eas: int = 0):
+        self.coords = np.ascontiguousarray(coords, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int32)
+        self.n_nodes, self.n_elems = self.coords.shape[0], self.conn.shape[0]
+        self.n_dofs = 3 * self.n_nodes
+        self.n_eas = int(n_eas)
+        self.material = material
+        h = C.c_void_p()
+        _err(lib().ikr_fes_create(C.byref(h), self.n_nodes, _ptr(self.coords), self.n_elems,
+                                  _ptr(self.conn, C.c_int32), material.lambda_, material.mu, int(eas), self.n_eas),
+             "fes_create")
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_fes_destroy(self.h)
+            self.h = None
+
+    def add_neumann(self, face_elem, face_local, traction):
+        """neumannBoundaryLoad: traction per face (n_faces x 3, value at the face centre, load factor 1)."""
+        fe = np.ascontiguousarray(face_elem, dtype=np.int32)
+        fl = np.ascontiguousarray(face_local, dtype=np.int32)
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(traction, dtype=np.float64), (len(fe), 3)))
+        _err(lib().ikr_fes_add_neumann(self.h, len(fe), _ptr(fe, C.c_int32), _ptr(fl, C.c_int32), _ptr(t)),
+             "add_neumann")
+
+    def num_colours(self):
+        n = C.c_int32()
+        _err(lib().ikr_fes_num_colours(self.h, C.byref(n)))
+        return n.value
+
+    def stream(self) -> int:
+        """Address of the cudaStream_t the library issues this element set's work on."""
+        s = C.c_void_p()
+        _err(lib().ikr_fes_stream(self.h, C.byref(s)))
+        return int(s.value or 0)
+
+    @property
+    def alpha(self):
+        a = np.zeros((self.n_elems, self.n_eas))
+        if a.size:
+            _err(lib().ikr_fes_get_alpha(self.h, _ptr(a)), "get_alpha")
+        return a
+
+    @alpha.setter
+    def alpha(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        _err(lib().ikr_fes_set_alpha(self.h, _ptr(a)), "set_alpha")
+
+
+class FERequirements:
+    """Displacement (device-resident FP64) and load factor (ferequirements.hh:222-407)."""
+
+    def __init__(self, fes: FiniteElements, u=None, load_factor: float = 0.0):
+        self.fes = fes
+        h = C.c_void_p()
+        _err(lib().ikr_req_create(C.byref(h), fes.h), "req_create")
+        self.h = h
+        if u is not None:
+            self.insertGlobalSolution(u)
+        self.insertParameter(load_factor)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_req_destroy(self.h)
+            self.h = None
+
+    def insertGlobalSolution(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        if u.size != self.fes.n_dofs:
+            raise ValueError("solution size mismatch")
+        _err(lib().ikr_req_insert_global_solution(self.h, _ptr(u)), "insertGlobalSolution")
+
+    def globalSolution(self):
+        u = np.zeros(self.fes.n_dofs)
+        _err(lib().ikr_req_global_solution(self.h, _ptr(u)), "globalSolution")
+        return u
+
+    def insertParameter(self, lf: float):
+        _err(lib().ikr_req_insert_parameter(self.h, float(lf)), "insertParameter")
+
+    def parameter(self) -> float:
+        v = C.c_double()
+        _err(lib().ikr_req_parameter(self.h, C.byref(v)), "parameter")
+        return v.value
+
+    def assign(self, other: "FERequirements"):
+        """Deep copy of another requirement's solution and load factor, device to device."""
+        _err(lib().ikr_req_copy(self.h, other.h), "copy")
+
+
+def calculateVector(fes: FiniteElements, req: FERequirements, affordance=VectorAffordance.forces, elements=None):
+    """Element force vectors (n x 24) of the given element range (mixin.hh:137-140)."""
+    e0, e1 = elements if elements is not None else (0, fes.n_elems)
+    out = np.zeros((e1 - e0, 24))
+    _err(lib().ikr_fe_calculate_vector(fes.h, req.h, int(affordance), e0, e1, _ptr(out)), "calculateVector")
+    return out
+
+
+def calculateMatrix(fes: FiniteElements, req: FERequirements, affordance=MatrixAffordance.stiffness, elements=None):
+    """Element stiffness matrices (n x 24 x 24) of the given element range (mixin.hh:149-152)."""
+    e0, e1 = elements if elements is not None else (0, fes.n_elems)
+    out = np.zeros((e1 - e0, 576))
+    _err(lib().ikr_fe_calculate_matrix(fes.h, req.h, int(affordance), e0, e1, _ptr(out)), "calculateMatrix")
+    return out.reshape(-1, 24, 24).transpose(0, 2, 1).copy()  # stored column-major
+
+
+def calculateScalar(fes: FiniteElements, req: FERequirements,
+                    affordance=ScalarAffordance.mechanicalPotentialEnergy, elements=None):
+    e0, e1 = elements if elements is not None else (0, fes.n_elems)
+    out = np.zeros(e1 - e0)
+    _err(lib().ikr_fe_calculate_scalar(fes.h, req.h, int(affordance), e0, e1, _ptr(out)), "calculateScalar")
+    return out
+
+
+def updateState(fes: FiniteElements, req: FERequirements, correction):
+    c = np.ascontiguousarray(correction, dtype=np.float64)
+    _err(lib().ikr_fe_update_state(fes.h, req.h, _ptr(c), c.size), "updateState")
+
+
+# ---- assembler -------------------------------------------------------------------------------------------
+class SparseFlatAssembler:
+    """SparseFlatAssembler (simpleassemblers.hh:108-177) with Dirichlet flags and manipulator point loads."""
+
+    def __init__(self, fes: FiniteElements, fixed_dofs, precision: Precision = Precision.fp64):
+        self.fes = fes
+        fixed = np.ascontiguousarray(fixed_dofs, dtype=np.uint8)
+        if fixed.size != fes.n_dofs:
+            raise ValueError("Dirichlet flag size mismatch")
+        self.fixed = fixed
+        self.precision = Precision(precision)
+        h = C.c_void_p()
+        _err(lib().ikr_assembler_create(C.byref(h), fes.h, _ptr(fixed, C.c_uint8), int(precision)), "assembler")
+        self.h = h
+        self._req = None
+        self._dbc = DBCOption.Full
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_assembler_destroy(self.h)
+            self.h = None
+
+    def bind(self, req: FERequirements, dbc: DBCOption = DBCOption.Full):
+        _err(lib().ikr_assembler_bind(self.h, req.h, int(dbc)), "bind")
+        self._req, self._dbc = req, DBCOption(dbc)
+
+    def dBCOption(self):
+        return self._dbc
+
+    def add_point_loads(self, dofs, values):
+        """AssemblerManipulator vector hook: vec[dof] += load_factor * value after the Dirichlet treatment."""
+        d = np.ascontiguousarray(dofs, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        _err(lib().ikr_assembler_add_point_loads(self.h, len(d), _ptr(d, C.c_int32), _ptr(v)), "point loads")
+
+    def size(self):
+        return self.fes.n_dofs
+
+    def reducedSize(self):
+        n = C.c_int32()
+        _err(lib().ikr_assembler_reduced_size(self.h, C.byref(n)))
+        return n.value
+
+    def constraintsBelow(self):
+        out = np.zeros(self.size(), dtype=np.int32)
+        _err(lib().ikr_assembler_constraints_below(self.h, _ptr(out, C.c_int32)))
+        return out
+
+    def isConstrained(self, i):
+        return bool(self.fixed[i])
+
+    def createFullVector(self, reduced):
+        full = np.zeros(self.size())
+        full[self.fixed == 0] = reduced
+        return full
+
+    def createReducedVector(self, full):
+        return np.asarray(full)[self.fixed == 0].copy()
+
+    def _args(self, req, dbc):
+        req = req if req is not None else self._req
+        if req is None:
+            raise IkarusError(-3, "assembler not bound")
+        return req, DBCOption(self._dbc if dbc is None else dbc)
+
+    def vector(self, req=None, affordance=VectorAffordance.forces, dbc=None):
+        req, dbc = self._args(req, dbc)
+        n = self.reducedSize() if dbc == DBCOption.Reduced else self.size()
+        out = np.zeros(n)
+        _err(lib().ikr_assembler_vector(self.h, req.h, int(affordance), int(dbc), _ptr(out)), "vector")
+        return out
+
+    def matrix(self, req=None, affordance=MatrixAffordance.stiffness, dbc=None, export=True):
+        """Assembles on the device; returns the scalar CSC (scipy) unless export=False."""
+        req, dbc = self._args(req, dbc)
+        _err(lib().ikr_assembler_matrix(self.h, req.h, int(affordance), int(dbc)), "matrix")
+        return self.export_csc(dbc) if export else None
+
+    def export_csc(self, dbc=None):
+        import scipy.sparse as sp
+        dbc = DBCOption(self._dbc if dbc is None else dbc)
+        nnz = C.c_int64()
+        _err(lib().ikr_assembler_matrix_nnz(self.h, int(dbc), C.byref(nnz)), "nnz")
+        n = self.reducedSize() if dbc == DBCOption.Reduced else self.size()
+        cp = np.zeros(n + 1, dtype=np.int64)
+        ri = np.zeros(nnz.value, dtype=np.int32)
+        v = np.zeros(nnz.value)
+        _err(lib().ikr_assembler_export_csc(self.h, int(dbc), _ptr(cp, C.c_int64), _ptr(ri, C.c_int32), _ptr(v)),
+             "export")
+        return sp.csc_matrix((v, ri, cp), shape=(n, n))
+
+    def pattern_csc(self, dbc=DBCOption.Full):
+        nnz = C.c_int64()
+        _err(lib().ikr_assembler_matrix_nnz(self.h, int(dbc), C.byref(nnz)), "nnz")
+        n = self.reducedSize() if dbc == DBCOption.Reduced else self.size()
+        cp = np.zeros(n + 1, dtype=np.int64)
+        ri = np.zeros(nnz.value, dtype=np.int32)
+        _err(lib().ikr_assembler_export_csc(self.h, int(dbc), _ptr(cp, C.c_int64), _ptr(ri, C.c_int32), None),
+             "pattern")
+        return cp, ri
+
+    def block_pattern(self):
+        nr, nb = C.c_int32(), C.c_int64()
+        _err(lib().ikr_assembler_block_pattern(self.h, C.byref(nr), C.byref(nb), None, None))
+        rp = np.zeros(nr.value + 1, dtype=np.int32)
+        col = np.zeros(nb.value, dtype=np.int32)
+        _err(lib().ikr_assembler_block_pattern(self.h, None, None, _ptr(rp, C.c_int32), _ptr(col, C.c_int32)))
+        return rp, col
+
+    def vector_norm(self):
+        v = C.c_double()
+        _err(lib().ikr_assembler_vector_norm(self.h, C.byref(v)))
+        return v.value
+
+
+# ---- solvers ---------------------------------------------------------------------------------------------
+class LinearSolver:
+    """LinearSolver facade (linearsolver.hh:49-233) over the device CG solvers."""
+
+    def __init__(self, tag: SolverTypeTag = SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-10, max_iter=100000):
+        h = C.c_void_p()
+        _err(lib().ikr_linear_solver_create(C.byref(h), int(tag)), "linear solver")
+        self.h = h
+        self.tag = tag
+        self.setTolerance(rtol, max_iter)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_linear_solver_destroy(self.h)
+            self.h = None
+
+    def setTolerance(self, rtol, max_iter=100000):
+        _err(lib().ikr_linear_solver_set_tolerance(self.h, rtol, max_iter))
+        self.rtol, self.max_iter = rtol, max_iter
+
+    def analyzePattern(self, assembler: SparseFlatAssembler):
+        _err(lib().ikr_linear_solver_analyze_pattern(self.h, assembler.h), "analyzePattern")
+
+    def factorize(self, assembler: SparseFlatAssembler):
+        _err(lib().ikr_linear_solver_factorize(self.h, assembler.h), "factorize")
+
+    def compute(self, assembler: SparseFlatAssembler):
+        self.analyzePattern(assembler)
+        self.factorize(assembler)
+
+    def solve(self, assembler: SparseFlatAssembler, b):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros_like(b)
+        _err(lib().ikr_linear_solver_solve(self.h, assembler.h, _ptr(x), _ptr(b)), "solve")
+        return x
+
+    def last_info(self):
+        it, rel = C.c_int32(), C.c_double()
+        _err(lib().ikr_linear_solver_last_info(self.h, C.byref(it), C.byref(rel)))
+        return it.value, rel.value
+
+    def profile(self, on=True):
+        """Bracket every CG SpMV with device events (inside the CUDA graphs); resets the counters."""
+        _err(lib().ikr_linear_solver_profile(self.h, int(on)))
+
+    def profile_read(self):
+        """(summed SpMV device time in ms, SpMV launches) since profiling was switched on."""
+        ms, n = C.c_double(), C.c_int64()
+        _err(lib().ikr_linear_solver_profile_read(self.h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+
+@dataclass
+class NRSettings:
+    """NRSettings (newtonraphson.hh:27-32) plus the inexact-Newton controls of this library."""
+    tol: float = 1e-8
+    maxIter: int = 20
+    minIter: int = 0
+    relative: bool = False        # ||R|| <= tol * ||R0|| instead of the reference's absolute test
+    eisenstat_walker: bool = False
+    linear_rtol: float = 1e-10
+    linear_rtol_min: float = 1e-12
+    linear_max_iter: int = 100000
+    refinements: int = 0
+
+    def _c(self):
+        return _NRSettings(self.tol, self.maxIter, self.minIter, int(self.relative), int(self.eisenstat_walker),
+                           self.linear_rtol, self.linear_rtol_min, self.linear_max_iter, self.refinements)
+
+
+@dataclass
+class NonLinearSolverInformation:  # solverinfos.hh:20-32
+    success: bool = False
+    residualNorm: float = float("inf")
+    correctionNorm: float = float("inf")
+    iterations: int = -1
+    linearIterations: int = 0
+
+    def __bool__(self):
+        return self.success
+
+    @classmethod
+    def _from(cls, c: _NRInfo):
+        return cls(bool(c.success), c.residual_norm, c.correction_norm, c.iterations, c.linear_iterations)
+
+
+@dataclass
+class NewtonRaphsonConfig:  # newtonraphson.hh:38-70
+    parameters: NRSettings = field(default_factory=NRSettings)
+    linearSolver: LinearSolver = None
+
+
+class NewtonRaphson:
+    """NewtonRaphson (newtonraphson.hh:193-257), a broadcaster of NonLinearSolverMessages."""
+
+    def __init__(self, assembler: SparseFlatAssembler, config: NewtonRaphsonConfig):
+        self.assembler = assembler
+        self.config = config
+        self.linearSolver = config.linearSolver or LinearSolver()
+        st = config.parameters._c()
+        h = C.c_void_p()
+        _err(lib().ikr_newton_create(C.byref(h), assembler.h, self.linearSolver.h, C.byref(st)), "newton")
+        self.h = h
+        self._cbs = []
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_newton_destroy(self.h)
+            self.h = None
+
+    def subscribe(self, fn):
+        """fn(message: NonLinearSolverMessages, state: dict)"""
+        def tramp(msg, st, _user):
+            s = st.contents
+            fn(NonLinearSolverMessages(msg), dict(residualNorm=s.residual_norm, correctionNorm=s.correction_norm,
+                                                  iterations=s.iterations, loadFactor=s.load_factor))
+        cb = _NR_OBS(tramp)
+        self._cbs.append(cb)
+        _err(lib().ikr_newton_subscribe(self.h, cb, None), "subscribe")
+
+    def subscribe_fe_state(self, on=True):
+        _err(lib().ikr_newton_subscribe_fe_state(self.h, int(on)))
+
+    def solve(self, req: FERequirements, stepSize: float = 0.0) -> NonLinearSolverInformation:
+        info = _NRInfo()
+        _err(lib().ikr_newton_solve(self.h, req.h, stepSize, C.byref(info)), "NewtonRaphson::solve")
+        return NonLinearSolverInformation._from(info)
+
+
+@dataclass
+class ControlInformation:  # controlinfos.hh:22-32
+    success: bool = False
+    solverInfos: list = field(default_factory=list)
+    totalIterations: int = 0
+    totalLinearIterations: int = 0
+    name: str = "Load Control"
+
+
+class LoadControl:
+    """LoadControl (loadcontrol.hh:58-113); creating it subscribes the element state update to the solver
+    as ControlRoutineFactory::create does (controlroutinefactory.hh:38-48)."""
+
+    def __init__(self, nonLinearSolver: NewtonRaphson, loadSteps: int, tbeginEnd=(0.0, 1.0)):
+        self.nonLinearSolver = nonLinearSolver
+        self.loadSteps = loadSteps
+        h = C.c_void_p()
+        _err(lib().ikr_load_control_create(C.byref(h), nonLinearSolver.h, loadSteps, tbeginEnd[0], tbeginEnd[1]),
+             "load control")
+        self.h = h
+        self._cbs = []
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_load_control_destroy(self.h)
+            self.h = None
+
+    def subscribe(self, fn):
+        """fn(message: ControlMessages, state: dict)"""
+        def tramp(msg, st, _user):
+            s = st.contents
+            fn(ControlMessages(msg), dict(loadStep=s.load_step, stepSize=s.step_size, loadFactor=s.load_factor))
+        cb = _CTRL_OBS(tramp)
+        self._cbs.append(cb)
+        _err(lib().ikr_load_control_subscribe(self.h, cb, None), "subscribe")
+
+    def run(self, req: FERequirements) -> ControlInformation:
+        cap = self.loadSteps + 1
+        infos = (_NRInfo * cap)()
+        ci = _ControlInfo()
+        _err(lib().ikr_load_control_run(self.h, req.h, C.byref(ci), infos, cap), "LoadControl::run")
+        return ControlInformation(bool(ci.success), [NonLinearSolverInformation._from(infos[i])
+                                                     for i in range(min(ci.n_solver_infos, cap))],
+                                  ci.total_iterations, ci.total_linear_iterations)

@@ -1,0 +1,308 @@
+// Element kernels for 3D Q1 hexahedra with the compressible Neo-Hooke law (sm_103a).
+//
+// Reference path: NonLinearElastic::calculateVectorImpl / calculateMatrixImpl
+// (ikarus/finiteelements/mechanics/nonlinearelastic.hh:375-430) with NeoHookeT
+// (materials/hyperelastic/neohooke.hh:78-142) and dead tractions (loads/traction.hh:105-138).
+//
+// Work decomposition: 8 lanes per element (lane = element node I), 32 elements per 256-thread block.
+// Per Gauss point the lanes reduce J = sum_I X_I (x) dN_I/dxi and H = sum_I u_I (x) grad N_I with warp
+// butterflies, so every lane holds F, F^{-1}, ln J.  The Neo-Hooke first elasticity tensor contracted with
+// two shape-function gradients needs only g_I = F^{-T} grad N_I:
+//   K_IJ = w [ mu (grad N_I . grad N_J) I + lambda g_I (x) g_J + (mu - lambda ln J) g_J (x) g_I ]
+// which equals the reference's B_I^T C B_J + kg_IJ (nonlinearelastic.hh:294-322) exactly in real arithmetic,
+// and the internal force f_I = w [ mu F grad N_I + (lambda ln J - mu) g_I ] equals B_I^T S w.
+// Lane I owns the node blocks (I, I+d mod 8), d = 0..4, and writes d = 1..3 also transposed, so each of the
+// 64 blocks is produced once and the element matrix is exactly symmetric.
+// Assembly is a plain read-modify-write into the BSR values through the precomputed element-to-block slot map;
+// the host launches one colour class at a time (no two elements of a class share a node), so the summation
+// order is fixed and repeated runs are bit-identical.
+#include <cmath>
+#include <type_traits>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace ikr {
+
+namespace {
+
+constexpr int kElemsPerBlock = 32;
+
+template <typename KT, int MODE>
+__global__ void __launch_bounds__(256) disp_element_kernel(ElemArgs a, const int32_t* __restrict__ list, int n_list,
+                                                           int e_base) {
+  constexpr bool WANT_R = MODE & kWantR;
+  constexpr bool WANT_K = MODE & kWantK;
+  constexpr bool WANT_E = MODE & kWantEnergy;
+  constexpr bool ELEM_OUT = MODE & kElemOut;
+  static_assert(!(WANT_R || WANT_E) || std::is_same<KT, double>::value, "residual and energy are FP64");
+  __shared__ KT sh[kElemsPerBlock][8][6];
+
+  const int lane = threadIdx.x & 31;
+  const int sub = threadIdx.x & 7;
+  const int es = threadIdx.x >> 3;
+  const int li = blockIdx.x * kElemsPerBlock + es;
+  const bool active = li < n_list;
+  const int lic = active ? li : n_list - 1;
+  const int e = list ? list[lic] : e_base + lic;
+  const int ne = a.n_elems;
+  const int node = a.conn[sub * ne + e];
+
+  double Xd[3], Ud[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    Xd[c] = a.X[3 * node + c];
+    Ud[c] = a.u ? a.u[3 * node + c] : 0.0;
+  }
+  // coordinates and displacements relative to the element's first corner keep FP32 geometry accurate
+  KT dX[3], dU[3];
+  const int src = lane & ~7;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const double x0 = __shfl_sync(0xffffffffu, Xd[c], src);
+    const double u0 = __shfl_sync(0xffffffffu, Ud[c], src);
+    dX[c] = KT(Xd[c] - x0);
+    dU[c] = KT(Ud[c] - u0);
+  }
+  const KT lam = KT(a.lam), mu = KT(a.mu);
+
+  KT Kacc[5][3][3];
+  if (WANT_K) {
+#pragma unroll
+    for (int d = 0; d < 5; ++d)
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Kacc[d][i][j] = KT(0);
+  }
+  double f[3] = {0.0, 0.0, 0.0};
+  double psi = 0.0;
+  int bad = 0;
+
+#pragma unroll 1
+  for (int q = 0; q < 8; ++q) {
+    KT dxi[3];
+    ref_gradient_at_gp<KT>(sub, q, dxi);
+    KT J[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) J[i][j] = sum8(dX[i] * dxi[j]);
+    KT Ji[3][3];
+    const KT detJ = inv3(J, Ji);
+    KT dN[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dN[k] = dxi[0] * Ji[0][k] + dxi[1] * Ji[1][k] + dxi[2] * Ji[2][k];
+    KT F[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) F[i][j] = sum8(dU[i] * dN[j]) + (i == j ? KT(1) : KT(0));
+    KT Fi[3][3];
+    const KT detF = inv3(F, Fi);
+    // det C = det(F)^2 must exceed 1e-10 (checkPositiveOrAbort); NaN fails the test as well
+    if (!(detF * detF > KT(1e-10)) || !(detF > KT(0))) bad |= kStatusNonPositiveDetC;
+    const KT lnJ = log(detF);
+    const KT w = KT(kGaussW) * detJ;
+    KT g[3];  // F^{-T} grad N_I
+#pragma unroll
+    for (int k = 0; k < 3; ++k) g[k] = Fi[0][k] * dN[0] + Fi[1][k] * dN[1] + Fi[2][k] * dN[2];
+
+    if (WANT_R) {
+      // P = mu (F - F^{-T}) + lambda ln J F^{-T}: written with F - F^{-T} so the undeformed state gives an
+      // exactly zero internal force (no FMA rounding residue), as the reference's S = 0 does
+      const KT ll = lam * lnJ;
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const KT Pd = (F[i][0] - Fi[0][i]) * dN[0] + (F[i][1] - Fi[1][i]) * dN[1] + (F[i][2] - Fi[2][i]) * dN[2];
+        f[i] += double(w * (mu * Pd + ll * g[i]));
+      }
+    }
+    if (WANT_E && sub == 0) {
+      KT trC = 0;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) trC += F[i][j] * F[i][j];
+      psi += double(w * (mu / KT(2) * (trC - KT(3) - KT(2) * lnJ) + lam / KT(2) * lnJ * lnJ));
+    }
+    if (WANT_K) {
+      const KT c = mu - lam * lnJ;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        sh[es][sub][k] = dN[k];
+        sh[es][sub][3 + k] = g[k];
+      }
+      __syncwarp();
+#pragma unroll
+      for (int d = 0; d < 5; ++d) {
+        const int Jn = (sub + d) & 7;
+        KT dNJ[3], gJ[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          dNJ[k] = sh[es][Jn][k];
+          gJ[k] = sh[es][Jn][3 + k];
+        }
+        const KT dd = w * mu * (dN[0] * dNJ[0] + dN[1] * dNJ[1] + dN[2] * dNJ[2]);
+        const KT wl = w * lam, wc = w * c;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            Kacc[d][i][j] += wl * g[i] * gJ[j] + wc * gJ[i] * g[j] + (i == j ? dd : KT(0));
+      }
+      __syncwarp();
+    }
+  }
+
+  const uint8_t fmaskI = a.node_fixed ? a.node_fixed[node] : uint8_t(0);
+  if (WANT_R || WANT_E) {
+    if (a.trac_idx) {
+      const int t = a.trac_idx[e];
+      if (t >= 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const double tv = a.trac[24 * t + 3 * sub + c];
+          f[c] -= a.load_factor * tv;
+          if (WANT_E) psi -= a.load_factor * tv * Ud[c];
+        }
+      }
+    }
+  }
+  double psi_tot = 0.0;
+  if (WANT_E) psi_tot = sum8(psi);  // last warp-wide operation: inactive lanes may leave after it
+
+  if (!active) return;
+  if (bad && a.status) atomicOr(a.status, bad);
+  if (WANT_E && ELEM_OUT && sub == 0) a.elem_energy[li] = psi_tot;
+  if (WANT_R) {
+    if (ELEM_OUT) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) a.elem_vec[24 * (size_t)li + 3 * sub + c] = f[c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        if (!((fmaskI >> c) & 1)) a.R[3 * node + c] += f[c];
+    }
+  }
+  if (WANT_K) {
+    if (ELEM_OUT) {
+      double* out = a.elem_mat + 576 * (size_t)li;
+#pragma unroll
+      for (int d = 0; d < 5; ++d) {
+        const int Jn = (sub + d) & 7;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            out[(3 * Jn + j) * 24 + 3 * sub + i] = double(Kacc[d][i][j]);
+            if (d >= 1 && d <= 3) out[(3 * sub + i) * 24 + 3 * Jn + j] = double(Kacc[d][i][j]);
+          }
+      }
+    } else {
+      KT* val = static_cast<KT*>(a.Kval);
+#pragma unroll
+      for (int d = 0; d < 5; ++d) {
+        const int Jn = (sub + d) & 7;
+        const uint8_t fmaskJ = a.node_fixed ? a.node_fixed[a.conn[Jn * ne + e]] : uint8_t(0);
+        const int64_t s1 = a.slot[(size_t)(sub * 8 + Jn) * ne + e];
+        KT* b1 = val + 9 * s1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[3 * i + j] += Kacc[d][i][j];
+        if (d >= 1 && d <= 3) {
+          const int64_t s2 = a.slot[(size_t)(Jn * 8 + sub) * ne + e];
+          KT* b2 = val + 9 * s2;
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[3 * j + i] += Kacc[d][i][j];
+        }
+      }
+    }
+  }
+}
+
+// Dead traction at load factor 1 on the element's Neumann faces, 1-point rule per face
+// (loads/traction.hh:122-135: quadrature order = order() = 1 -> the face centre, weight 1):
+// trac[slot][3v+c] = sum_faces N_v(centre) t_c dA.  One thread per loaded element, faces in input order.
+__global__ void traction_kernel(const double* __restrict__ X, const int32_t* __restrict__ conn, int ne, int n_slots,
+                                const int32_t* __restrict__ slot_elem, const int32_t* __restrict__ face_ptr,
+                                const int32_t* __restrict__ face_local, const double* __restrict__ t,
+                                double* __restrict__ trac) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_slots) return;
+  const int e = slot_elem[s];
+  double acc[24];
+  for (int k = 0; k < 24; ++k) acc[k] = 0.0;
+  double Xe[8][3];
+  for (int v = 0; v < 8; ++v) {
+    const int n = conn[v * ne + e];
+    for (int c = 0; c < 3; ++c) Xe[v][c] = X[3 * n + c];
+  }
+  for (int k = face_ptr[s]; k < face_ptr[s + 1]; ++k) {
+    const int lf = face_local[k];
+    const int d = lf >> 1, side = lf & 1;
+    const int t1 = (d == 0) ? 1 : 0, t2 = (d == 2) ? 1 : 2;
+    double a1[3] = {0, 0, 0}, a2[3] = {0, 0, 0};
+    for (int v = 0; v < 8; ++v) {
+      if (((v >> d) & 1) != side) continue;
+      const double s1 = ((v >> t1) & 1) ? 0.5 : -0.5;
+      const double s2 = ((v >> t2) & 1) ? 0.5 : -0.5;
+      for (int c = 0; c < 3; ++c) {
+        a1[c] += Xe[v][c] * s1;
+        a2[c] += Xe[v][c] * s2;
+      }
+    }
+    const double cr0 = a1[1] * a2[2] - a1[2] * a2[1];
+    const double cr1 = a1[2] * a2[0] - a1[0] * a2[2];
+    const double cr2 = a1[0] * a2[1] - a1[1] * a2[0];
+    const double dA = sqrt(cr0 * cr0 + cr1 * cr1 + cr2 * cr2);
+    for (int v = 0; v < 8; ++v) {
+      if (((v >> d) & 1) != side) continue;
+      for (int c = 0; c < 3; ++c) acc[3 * v + c] += 0.25 * t[3 * k + c] * 1.0 * dA;
+    }
+  }
+  for (int k = 0; k < 24; ++k) trac[24 * (size_t)s + k] = acc[k];
+}
+
+template <typename KT, int MODE>
+void launch_disp_t(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
+  const int blocks = (n_list + kElemsPerBlock - 1) / kElemsPerBlock;
+  disp_element_kernel<KT, MODE><<<blocks, 256, 0, s>>>(a, list, n_list, e_base);
+}
+
+}  // namespace
+
+void launch_disp_element(const ElemArgs& a, int mode, bool fp32_tangent, const int32_t* list, int n_list, int e_base,
+                         cudaStream_t s) {
+  if (n_list <= 0) return;
+  switch (mode) {
+    case kWantR: launch_disp_t<double, kWantR>(a, list, n_list, e_base, s); break;
+    case kWantR | kWantK: launch_disp_t<double, kWantR | kWantK>(a, list, n_list, e_base, s); break;
+    case kWantK:
+      if (fp32_tangent) launch_disp_t<float, kWantK>(a, list, n_list, e_base, s);
+      else launch_disp_t<double, kWantK>(a, list, n_list, e_base, s);
+      break;
+    case kWantR | kElemOut: launch_disp_t<double, kWantR | kElemOut>(a, list, n_list, e_base, s); break;
+    case kWantK | kElemOut:
+      if (fp32_tangent) launch_disp_t<float, kWantK | kElemOut>(a, list, n_list, e_base, s);
+      else launch_disp_t<double, kWantK | kElemOut>(a, list, n_list, e_base, s);
+      break;
+    case kWantEnergy | kElemOut: launch_disp_t<double, kWantEnergy | kElemOut>(a, list, n_list, e_base, s); break;
+    default: break;
+  }
+}
+
+void launch_traction_loads(const double* X, const int32_t* conn, int n_elems, int n_slots, const int32_t* slot_elem,
+                           const int32_t* face_ptr, const int32_t* face_local, const double* traction, double* trac,
+                           cudaStream_t s) {
+  if (n_slots <= 0) return;
+  traction_kernel<<<(n_slots + 127) / 128, 128, 0, s>>>(X, conn, n_elems, n_slots, slot_elem, face_ptr, face_local,
+                                                          traction, trac);
+}
+
+}  // namespace ikr

@@ -1,0 +1,118 @@
+"""Workload definitions: the cantilever and block problems the reference's tests and the benchmark configs use.
+
+A ``Problem`` is plain data (mesh, NeoHooke parameters, EAS choice, Dirichlet flags, dead face tractions,
+manipulator point loads, load stepping), so the same definition feeds the GPU path and the CPU oracle.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .mesh import (HexMesh, boundary_faces, face_centers, fixed_dofs_where, jitter_interior, structured_hex_grid,
+                   vertex_at)
+
+
+def lame(E, nu):
+    """(E, nu) -> (lambda, mu) (ikarus/finiteelements/physicshelper.hh:81-85, 123-127)."""
+    return E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu)), E / (2.0 * (1.0 + nu))
+
+
+@dataclass
+class Problem:
+    name: str
+    mesh: HexMesh
+    lam: float
+    mu: float
+    eas: int = 0
+    n_eas: int = 0
+    fixed: np.ndarray = None
+    face_elem: np.ndarray = None
+    face_local: np.ndarray = None
+    face_traction: np.ndarray = None  # per face, load factor 1
+    pl_dofs: np.ndarray = None
+    pl_values: np.ndarray = None
+    load_steps: int = 10
+    t_end: float = 1.0
+    tol: float = 1e-10
+    relative: bool = False
+
+    @property
+    def n_dofs(self):
+        return self.mesh.n_dofs
+
+
+def cantilever_golden(eas: int, n_eas: int, nx=10, ny=1, nz=1) -> Problem:
+    """tests/src/testcantileverbeam.hh:42-198 in 3D: YaspGrid 10x1x1 on (10, 2, 2), E = 100, nu = 0.3, clamped at
+    x = 0, manipulator point loads R[y-dof] += lambda at the vertices (10,2,2) and (10,2,0), 20 load steps,
+    ||R|| < 1e-10 (testcantileverbeamEAS.cpp:60-124)."""
+    L, h = 10.0, 2.0
+    m = structured_hex_grid(nx, ny, nz, (L, h, h))
+    lam, mu = lame(100.0, 0.3)
+    fixed = fixed_dofs_where(m, lambda X: np.abs(X[:, 0]) < 1e-8)
+    dofs = np.array([3 * vertex_at(m, (L, h, h)) + 1, 3 * vertex_at(m, (L, h, 0.0)) + 1], dtype=np.int32)
+    return Problem(f"cantilever_golden_eas{eas}_{n_eas}", m, lam, mu, eas, n_eas, fixed, pl_dofs=dofs,
+                   pl_values=np.ones(2), load_steps=20, tol=1e-10)
+
+
+def cantilever(nx, ny, nz, L=10.0, E=1000.0, nu=0.3, jitter=0.0, seed=0, load_steps=10, traction=(0.0, 0.0, -1.0),
+               eas=0, n_eas=0, tol=1e-10, relative=False) -> Problem:
+    """Cantilever [0,L]x[0,1]x[0,1] clamped at x = 0 with a uniform dead traction on the face x = L."""
+    m = structured_hex_grid(nx, ny, nz, (L, 1.0, 1.0))
+    if jitter > 0:
+        m = jitter_interior(m, jitter, seed)
+    lam, mu = lame(E, nu)
+    fixed = fixed_dofs_where(m, lambda X: np.abs(X[:, 0]) < 1e-8)
+    fe, fl = boundary_faces(m, "x+")
+    t = np.tile(np.asarray(traction, dtype=np.float64), (len(fe), 1))
+    return Problem(f"cantilever_{nx}x{ny}x{nz}", m, lam, mu, eas, n_eas, fixed, fe, fl, t, load_steps=load_steps,
+                   tol=tol, relative=relative)
+
+
+def config1() -> Problem:
+    """16x4x4 Q1 cantilever, E = 1000, nu = 0.3, traction (0,0,-1) on x = 10, 10 steps, ||R|| < 1e-10."""
+    return cantilever(16, 4, 4, load_steps=10, tol=1e-10)
+
+
+def config2(seed=2024, load_steps=20) -> Problem:
+    """128x32x32 Q1 cantilever (131072 elements, 421443 dofs), interior vertices jittered by U(-0.1h, 0.1h),
+    20 load steps, ||R||/||R0|| < 1e-8 per load step."""
+    p = cantilever(128, 32, 32, jitter=0.1, seed=seed, load_steps=load_steps, tol=1e-8, relative=True)
+    p.name = "cantilever_128x32x32_jittered"
+    return p
+
+
+def eas_block(nx=64, ny=64, nz=16, nu=0.4999, E=1000.0, pressure=50.0, load_steps=25, eas=1, n_eas=9) -> Problem:
+    """Block [0,1]x[0,1]x[0,0.25], bottom face clamped, dead normal pressure on the centred 0.5 x 0.5 top patch,
+    9-parameter EAS (nearly incompressible when nu = 0.4999)."""
+    m = structured_hex_grid(nx, ny, nz, (1.0, 1.0, 0.25))
+    lam, mu = lame(E, nu)
+    fixed = fixed_dofs_where(m, lambda X: np.abs(X[:, 2]) < 1e-12)
+    fe, fl = boundary_faces(m, "z+")
+    c = face_centers(m, fe, fl)
+    sel = (c[:, 0] > 0.25) & (c[:, 0] < 0.75) & (c[:, 1] > 0.25) & (c[:, 1] < 0.75)
+    fe, fl = fe[sel], fl[sel]
+    t = np.tile(np.array([0.0, 0.0, -pressure]), (len(fe), 1))
+    return Problem(f"eas_block_{nx}x{ny}x{nz}", m, lam, mu, eas, n_eas, fixed, fe, fl, t, load_steps=load_steps,
+                   tol=1e-8, relative=True)
+
+
+def single_element(offsets=None, E=1000.0, nu=0.3, eas=0, n_eas=0) -> Problem:
+    """One hexahedron on the unit cube, corners moved by ``offsets`` (8 x 3) as in tests/src/testcommon.hh."""
+    m = structured_hex_grid(1, 1, 1, (1.0, 1.0, 1.0))
+    if offsets is not None:
+        m.coords = m.coords + np.asarray(offsets, dtype=np.float64)
+    lam, mu = lame(E, nu)
+    return Problem("single_element", m, lam, mu, eas, n_eas, np.zeros(24, dtype=np.uint8))
+
+
+def build_gpu(p: Problem, precision=0):
+    """GPU objects for a problem: (FiniteElements, SparseFlatAssembler)."""
+    from . import FiniteElements, NeoHooke, Precision, SparseFlatAssembler
+    fes = FiniteElements(p.mesh.coords, p.mesh.conn, NeoHooke(p.lam, p.mu), p.eas, p.n_eas)
+    if p.face_elem is not None and len(p.face_elem):
+        fes.add_neumann(p.face_elem, p.face_local, p.face_traction)
+    asm = SparseFlatAssembler(fes, p.fixed, Precision(precision))
+    if p.pl_dofs is not None:
+        asm.add_point_loads(p.pl_dofs, p.pl_values)
+    return fes, asm

@@ -1,0 +1,232 @@
+/*
+ * ikarus_gb300.h -- C ABI of the GB300-native Newton-Raphson / LoadControl path for Q1 hexahedral
+ * Neo-Hookean solids (displacement-based and enhanced-assumed-strain), mirroring ikarus-project/ikarus v0.4.9.
+ *
+ * Plain pointers and sizes only.  Every function returns IKR_OK (0) or a negative IKR_ERR_* status; the
+ * message of the last failure on the calling thread is available from ikr_last_error().  No function
+ * throws or aborts.  Arrays passed in are host arrays and are copied; device storage belongs to the
+ * library.  Handles are not thread-safe: use one handle set per host thread (or lock externally).
+ *
+ * Numbering: dof = 3 * node + component (FlatInterleaved, ikarus/utils/flatprebasis.hh:57-76).
+ * Element corners in Dune reference-cube order (vertex v at (v&1, v>>1&1, v>>2&1)).
+ * Element-local dofs are node-major (local k = 3*i + c, ikarus/finiteelements/fehelper.hh:145-153).
+ * Element matrices are returned column-major (Eigen default, fetraits.hh:79-86).
+ */
+#ifndef IKARUS_GB300_H
+#define IKARUS_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (replace DUNE_THROW / abort(); SURVEY error conventions) ---------------------------- */
+enum {
+  IKR_OK = 0,
+  IKR_ERR_ARG = -1,
+  IKR_ERR_NOT_IMPLEMENTED = -2,   /* DUNE_THROW(Dune::NotImplemented), e.g. enhancedassumedstrains.hh:231-235 */
+  IKR_ERR_INVALID_STATE = -3,     /* DUNE_THROW(Dune::InvalidStateException), e.g. assembler/interface.hh:187-193 */
+  IKR_ERR_NONPOSITIVE_DETC = -4,  /* checkPositiveOrAbort, materials/materialhelpers.hh:119-126 (aborts there) */
+  IKR_ERR_NOT_CONVERGED = -5,
+  IKR_ERR_CG_BREAKDOWN = -6,
+  IKR_ERR_CUDA = -7,
+  IKR_ERR_SINGULAR = -8,
+  IKR_ERR_NO_DEVICE = -9
+};
+
+/* ---- enums with the reference's values ------------------------------------------------------------------ */
+/* DBCOption, ikarus/assembler/dirichletbcenforcement.hh:8 */
+enum { IKR_DBC_RAW = 0, IKR_DBC_REDUCED = 1, IKR_DBC_FULL = 2 };
+/* VectorAffordance / MatrixAffordance / ScalarAffordance, ikarus/finiteelements/ferequirements.hh:35-89 */
+enum { IKR_VEC_NO_AFFORDANCE = 0, IKR_VEC_FORCES = 1 };
+enum { IKR_MAT_NO_AFFORDANCE = 0, IKR_MAT_STIFFNESS = 1 };
+enum { IKR_SCALAR_NO_AFFORDANCE = 0, IKR_SCALAR_MECHANICAL_POTENTIAL_ENERGY = 1 };
+/* strain measure enhanced by EAS: none (NonLinearElastic only), EAS::GreenLagrangeStrain,
+ * EAS::DisplacementGradient, EAS::DisplacementGradientTransposed (strainenhancements/easfunctions/) */
+enum { IKR_EAS_NONE = 0, IKR_EAS_GREEN_LAGRANGE = 1, IKR_EAS_DISPLACEMENT_GRADIENT = 2,
+       IKR_EAS_DISPLACEMENT_GRADIENT_TRANSPOSED = 3 };
+/* SolverTypeTag (ikarus/solver/linearsolver/linearsolver.hh:28-31) keeps its values; the device solvers
+ * of this library are added after it.  si_ConjugateGradient maps to device CG with point-Jacobi
+ * preconditioning (Eigen's default diagonal preconditioner); the sparse direct tags are not provided. */
+enum {
+  IKR_SOLVER_NONE = 0,
+  IKR_SOLVER_SI_CONJUGATE_GRADIENT = 1,
+  IKR_SOLVER_GPU_PCG_BLOCK_JACOBI = 100,  /* FP64 or FP32 CG, 3x3 block-Jacobi, precision of the assembled K */
+};
+/* precision of the assembled tangent */
+enum { IKR_PRECISION_FP64 = 0, IKR_PRECISION_FP32 = 1 };
+/* messages, ikarus/utils/broadcaster/broadcastermessages.hh:18,23-24 (spelling of the reference kept) */
+enum { IKR_CONTROL_STARTED = 0, IKR_CONTROL_ENDED, IKR_STEP_STARTED, IKR_STEP_ENDED, IKR_CONTROL_SOLUTION_CHANGED };
+enum { IKR_NLS_INIT = 0, IKR_NLS_ITERATION_STARTED, IKR_NLS_ITERATION_ENDED, IKR_NLS_RESIDUALNORM_UPDATED,
+       IKR_NLS_CORRECTIONNORM_UPDATED, IKR_NLS_CORRECTION_UPDATED, IKR_NLS_SOLUTION_CHANGED,
+       IKR_NLS_FINISHED_SUCESSFULLY };
+
+typedef struct ikr_fes_s* ikr_fes;   /* the bound finite elements of one mesh (the reference's std::vector<FE>) */
+typedef struct ikr_req_s* ikr_req;   /* FERequirements: displacement (device, FP64) + load factor */
+typedef struct ikr_asm_s* ikr_asm;   /* SparseFlatAssembler (+ AssemblerManipulator point loads) */
+typedef struct ikr_ls_s* ikr_ls;     /* LinearSolver */
+typedef struct ikr_nr_s* ikr_nr;     /* NewtonRaphson */
+typedef struct ikr_lc_s* ikr_lc;     /* LoadControl */
+
+/* ---- library ---------------------------------------------------------------------------------------------- */
+int ikr_version(void);
+/* copies the last error message of this thread (NUL-terminated, truncated to len) */
+int ikr_last_error(char* buf, int32_t len);
+/* number of kernels this library has launched (for launch-count reporting) */
+int64_t ikr_kernel_launches(void);
+
+/* ---- finite elements ----------------------------------------------------------------------------------------
+ * Replaces: for (ge : elements(gridView)) { fes.emplace_back(makeFE(basis, skills(nonLinearElastic(NeoHooke(
+ * {lambda, mu})), eas<ES>(n_alpha)))); fes.back().bind(ge); }  (fefactory.hh:67-72, febase.hh:77-161,
+ * nonlinearelastic.hh:439-444, enhancedassumedstrains.hh:443-448, materials/hyperelastic/neohooke.hh:37-208).
+ * conn: n_elems x 8 corner node ids (row-major), coords: n_nodes x 3. */
+int ikr_fes_create(ikr_fes* out, int32_t n_nodes, const double* coords, int32_t n_elems, const int32_t* conn,
+                   double lambda, double mu, int32_t eas_kind, int32_t n_alpha);
+/* Replaces skills(neumannBoundaryLoad(patch, f)) (loads/traction.hh:21-33, 105-138): dead traction
+ * lambda * t on each listed face (Dune face numbering 2d: xi_d = 0, 2d+1: xi_d = 1), t given per face as the
+ * value of f at the face's single quadrature point (the face centre; rule order = order() = 1). */
+int ikr_fes_add_neumann(ikr_fes fes, int32_t n_faces, const int32_t* face_elem, const int32_t* face_local,
+                        const double* traction);
+int ikr_fes_destroy(ikr_fes fes);
+int ikr_fes_num_colours(ikr_fes fes, int32_t* n_colours);
+/* EAS internal variables alpha_ (enhancedassumedstrains.hh:207, 364): n_elems x n_alpha, row-major */
+int ikr_fes_get_alpha(ikr_fes fes, double* alpha);
+int ikr_fes_set_alpha(ikr_fes fes, const double* alpha);
+
+/* ---- element level: calculateVector / calculateMatrix / calculateScalar (mixin.hh:126-152) and
+ * updateState (mixin.hh:284-287), batched over the element range [e_begin, e_end).  Results are written
+ * (not added) to out: 24 (vector), 576 column-major (matrix) or 1 (scalar) values per element. ---------- */
+int ikr_fe_calculate_vector(ikr_fes fes, ikr_req req, int32_t affordance, int32_t e_begin, int32_t e_end,
+                            double* out);
+int ikr_fe_calculate_matrix(ikr_fes fes, ikr_req req, int32_t affordance, int32_t e_begin, int32_t e_end,
+                            double* out);
+int ikr_fe_calculate_scalar(ikr_fes fes, ikr_req req, int32_t affordance, int32_t e_begin, int32_t e_end,
+                            double* out);
+/* EAS::updateStateImpl (enhancedassumedstrains.hh:225-248) on every element; correction has n dofs (a
+ * reduced-size correction returns IKR_ERR_NOT_IMPLEMENTED like the reference). */
+int ikr_fe_update_state(ikr_fes fes, ikr_req req, const double* correction, int32_t correction_size);
+
+/* ---- FERequirements (ferequirements.hh:222-407) -------------------------------------------------------- */
+int ikr_req_create(ikr_req* out, ikr_fes fes);
+int ikr_req_destroy(ikr_req req);
+int ikr_req_insert_global_solution(ikr_req req, const double* u);  /* copies n dofs to the device */
+int ikr_req_global_solution(ikr_req req, double* u);               /* copies n dofs to the host */
+int ikr_req_insert_parameter(ikr_req req, double load_factor);
+int ikr_req_parameter(ikr_req req, double* load_factor);
+/* device address of the displacement (valid for the lifetime of req) */
+int ikr_req_solution_device(ikr_req req, double** dptr);
+/* deep copy of solution and load factor, device to device (the FERequirements copy constructor,
+ * ferequirements.hh:222-407); both requirements must belong to the same element set */
+int ikr_req_copy(ikr_req dst, ikr_req src);
+
+/* ---- SparseFlatAssembler (simpleassemblers.hh:108-177, assembler/interface.hh:28-266) --------------------
+ * fixed: n dofs, 1 = constrained (DirichletValues flags, dirichletvalues.hh:110-131, 187-194).
+ * precision: IKR_PRECISION_FP64 or IKR_PRECISION_FP32 for the stored tangent. */
+int ikr_assembler_create(ikr_asm* out, ikr_fes fes, const uint8_t* fixed, int32_t precision);
+int ikr_assembler_destroy(ikr_asm a);
+/* AssemblerManipulator vector hook (assemblermanipulatorbuildingblocks.hh:94-121) of the form
+ * vec[dof] += load_factor * value, applied after the Dirichlet treatment. */
+int ikr_assembler_add_point_loads(ikr_asm a, int32_t n, const int32_t* dofs, const double* values);
+int ikr_assembler_bind(ikr_asm a, ikr_req req, int32_t dbc_option);                    /* interface.hh:150-175 */
+int ikr_assembler_size(ikr_asm a, int32_t* size);
+int ikr_assembler_reduced_size(ikr_asm a, int32_t* size);
+int ikr_assembler_constraints_below(ikr_asm a, int32_t* out);   /* n dofs, interface.hh:50-62 */
+/* vector(req, affordance, dbc) (interface.hh:355-365): assembles on the device; out (host, may be NULL)
+ * receives size() or reducedSize() values. */
+int ikr_assembler_vector(ikr_asm a, ikr_req req, int32_t affordance, int32_t dbc_option, double* out);
+/* matrix(req, affordance, dbc) (interface.hh:430-440): assembles the 3x3-block CSR on the device. */
+int ikr_assembler_matrix(ikr_asm a, ikr_req req, int32_t affordance, int32_t dbc_option);
+/* scalar CSC export of the last assembled matrix for the given option (parity with Eigen's column-major
+ * SparseMatrix): col_ptr (cols+1), row_idx (nnz), values (nnz); pass NULLs to query nnz. */
+int ikr_assembler_matrix_nnz(ikr_asm a, int32_t dbc_option, int64_t* nnz);
+int ikr_assembler_export_csc(ikr_asm a, int32_t dbc_option, int64_t* col_ptr, int32_t* row_idx, double* values);
+/* the block pattern itself: row_ptr (n_nodes+1), col (n_blocks) */
+int ikr_assembler_block_pattern(ikr_asm a, int32_t* n_rows, int64_t* n_blocks, int32_t* row_ptr, int32_t* col);
+/* ||R|| of the last assembled vector (FP64, deterministic device reduction) */
+int ikr_assembler_vector_norm(ikr_asm a, double* norm);
+
+/* ---- LinearSolver (linearsolver.hh:49-233) --------------------------------------------------------------- */
+int ikr_linear_solver_create(ikr_ls* out, int32_t solver_type_tag);
+int ikr_linear_solver_destroy(ikr_ls ls);
+int ikr_linear_solver_set_tolerance(ikr_ls ls, double rtol, int32_t max_iter);
+int ikr_linear_solver_analyze_pattern(ikr_ls ls, ikr_asm a);
+int ikr_linear_solver_factorize(ikr_ls ls, ikr_asm a);       /* builds the preconditioner from the device K */
+/* solve(x, b) with host arrays of size() (Full option system) */
+int ikr_linear_solver_solve(ikr_ls ls, ikr_asm a, double* x, const double* b);
+/* iterations and achieved relative residual of the last solve */
+int ikr_linear_solver_last_info(ikr_ls ls, int32_t* iterations, double* rel_residual);
+/* Measurement hooks (no reference counterpart): with profiling on, every CG SpMV launch is bracketed by
+ * device events inside the CUDA graphs; read returns the summed SpMV device time and the launch count
+ * since profiling was switched on. */
+int ikr_linear_solver_profile(ikr_ls ls, int32_t on);
+int ikr_linear_solver_profile_read(ikr_ls ls, double* spmv_ms_total, int64_t* spmv_launches);
+/* the CUDA stream (cudaStream_t) all work on this element set is issued on */
+int ikr_fes_stream(ikr_fes fes, void** stream);
+
+/* ---- NewtonRaphson (newtonraphson.hh:27-303, nonlinearsolverfactory.hh:110-122) -------------------------- */
+typedef struct ikr_nr_settings {
+  double tol;          /* NRSettings::tol (default 1e-8) */
+  int32_t max_iter;    /* NRSettings::maxIter (default 20) */
+  int32_t min_iter;    /* NRSettings::minIter (default 0) */
+  /* additions of this library (defaults reproduce the reference) */
+  int32_t tol_mode;    /* 0: ||R|| <= tol (reference); 1: ||R|| <= tol * ||R at solve start|| */
+  int32_t forcing;     /* 0: fixed linear tolerance; 1: Eisenstat-Walker inexact Newton */
+  double linear_rtol;  /* fixed linear relative tolerance (forcing = 0) / upper bound (forcing = 1) */
+  double linear_rtol_min;
+  int32_t linear_max_iter;
+  int32_t refinements; /* FP64 iterative-refinement sweeps around an FP32 solve (0 = none) */
+} ikr_nr_settings;
+typedef struct ikr_nr_info {   /* NonLinearSolverInformation (solverinfos.hh:20-32) */
+  int32_t success;
+  double residual_norm;
+  double correction_norm;
+  int32_t iterations;
+  int64_t linear_iterations;   /* addition: CG iterations spent in this solve */
+} ikr_nr_info;
+typedef struct ikr_nr_state {  /* NonlinearSolverState (nonlinearsolverstate.hh:22-31) */
+  ikr_req domain;
+  double residual_norm;
+  double correction_norm;
+  int32_t iterations;
+  double load_factor;
+} ikr_nr_state;
+typedef void (*ikr_nr_observer)(int32_t message, const ikr_nr_state* state, void* user);
+
+int ikr_nr_settings_default(ikr_nr_settings* s);
+int ikr_newton_create(ikr_nr* out, ikr_asm a, ikr_ls ls, const ikr_nr_settings* settings);
+int ikr_newton_destroy(ikr_nr nr);
+/* Broadcaster::subscribe (broadcaster.hh:24-78) for NonLinearSolverMessages */
+int ikr_newton_subscribe(ikr_nr nr, ikr_nr_observer cb, void* user);
+/* the EAS skill's subscription (enhancedassumedstrains.hh:350-359): update alpha on CORRECTION_UPDATED */
+int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on);
+/* solve(x, stepSize) (newtonraphson.hh:193-257) */
+int ikr_newton_solve(ikr_nr nr, ikr_req req, double step_size, ikr_nr_info* info);
+
+/* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
+typedef struct ikr_control_state {   /* ControlRoutineState (controlroutinestate.hh:21-31) */
+  ikr_req domain;
+  int32_t load_step;
+  double step_size;
+  double load_factor;
+} ikr_control_state;
+typedef void (*ikr_control_observer)(int32_t message, const ikr_control_state* state, void* user);
+typedef struct ikr_control_info {    /* ControlInformation (controlinfos.hh:22-32) */
+  int32_t success;
+  int32_t total_iterations;
+  int32_t n_solver_infos;
+  int64_t total_linear_iterations;
+} ikr_control_info;
+/* ControlRoutineFactory::create(LoadControlConfig{load_steps, t_begin, t_end}, nr, assembler): also
+ * subscribes the elements' state update to the Newton solver. */
+int ikr_load_control_create(ikr_lc* out, ikr_nr nr, int32_t load_steps, double t_begin, double t_end);
+int ikr_load_control_destroy(ikr_lc lc);
+int ikr_load_control_subscribe(ikr_lc lc, ikr_control_observer cb, void* user);
+/* run(req): info plus per-solve NonLinearSolverInformation (capacity entries; index 0 = the initial
+ * equilibrium solve at the starting load factor). */
+int ikr_load_control_run(ikr_lc lc, ikr_req req, ikr_control_info* info, ikr_nr_info* solver_infos,
+                         int32_t capacity);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -73,6 +73,19 @@ def _check(code, what):
         raise OracleError(code, what)
 
 
+def from_problem(p, faithful=False):
+    """Oracle twin of an ``ikarus_gb300.problems.Problem`` definition (plain data, no GPU objects)."""
+    o = OracleProblem(p.mesh.coords, p.mesh.conn, p.lam, p.mu, p.eas if p.n_eas else EAS_NONE, p.n_eas)
+    o.set_dirichlet(p.fixed)
+    if p.face_elem is not None and len(p.face_elem):
+        o.add_neumann(p.face_elem, p.face_local, p.face_traction)
+    if p.pl_dofs is not None:
+        o.add_point_loads(p.pl_dofs, p.pl_values)
+    if faithful:
+        o.set_faithful_moduli(True)
+    return o
+
+
 class OracleProblem:
     """One mesh + NeoHooke material + EAS choice, with Dirichlet flags and dead loads."""
 

@@ -1,0 +1,51 @@
+"""Generates tests/golden/reference_goldens.json from the reference's own test sources (read as text).
+
+Run in a container where the reference is mounted at /root/reference; the JSON it writes is committed so
+the tests never read the reference at run time.
+
+Sources:
+  tests/src/testcantileverbeamEAS.cpp:60-96   3D cantilever (NR + LoadControl + SparseFlatAssembler + EAS):
+                                               (total Newton iterations, max |d|) per enhanced strain & material
+  tests/src/testcantileverbeamEAS.cpp:101     material parameters (E = 100, nu = 0.3)
+  tests/src/testcantileverbeam.hh:42-53, 96-151  mesh 10x1x1 on (L, h, h) = (10, 2, 2), tol 1e-10, 20 steps
+  tests/src/testcommon.hh:199-207             fixed corner distortion of the single-element tests
+"""
+import json
+import os
+import re
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
+
+
+def main():
+    src = open(os.path.join(REF, "tests/src/testcantileverbeamEAS.cpp")).read()
+    body = src[src.index("cantileverBeamResults3D"):]
+    body = body[: body.index("int main")]
+    goldens = {}
+    for es_block in re.split(r"std::same_as<ES, EAS::", body)[1:]:
+        es = es_block.split(">")[0]
+        for mat, it, md in re.findall(r"is_same_v<MAT, ([^>]+(?:>[^>]*>)*?)>\)\s*\{\s*return std::make_pair\((\d+), ([0-9.e+-]+)\)", es_block):
+            goldens.setdefault(es, {})[mat.strip()] = {"iterations": int(it), "max_disp": float(md)}
+    common = open(os.path.join(REF, "tests/src/testcommon.hh")).read()
+    blk = common[common.index("if constexpr (gridDim == 3)", common.index("fixedDistorted")):]
+    blk = blk[: blk.index("} else")]
+    offsets = [[float(x) for x in m] for m in re.findall(r"push_back\(\{([-0-9.]+), ([-0-9.]+), ([-0-9.]+)\}\)", blk)]
+    data = {
+        "source": "ikarus-project/ikarus tests/src/testcantileverbeamEAS.cpp:60-96, testcantileverbeam.hh:42-198, "
+                  "testcommon.hh:199-207",
+        "cantilever_3d": {"L": 10.0, "h": 2.0, "elements": [10, 1, 1], "E": 100.0, "nu": 0.3, "load_steps": 20,
+                          "tol": 1e-10, "point_load_nodes": [[10.0, 2.0, 2.0], [10.0, 2.0, 0.0]],
+                          "eas_parameters": {"GreenLagrangeStrain": 21, "DisplacementGradient": 9,
+                                             "DisplacementGradientTransposed": 9},
+                          "results": goldens},
+        "fixed_distortion_3d": offsets,
+    }
+    with open(OUT, "w") as f:
+        json.dump(data, f, indent=1)
+    print(OUT)
+
+
+if __name__ == "__main__":
+    main()

