@@ -384,9 +384,11 @@ struct ikr_ls_s {
       cudaGraph_t g = nullptr;
       CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < chunk_len; ++k) {
-        if (profile) CK(cudaEventRecord(pev[gi][2 * k], s));
+        // cudaEventRecordExternal turns the records into event-record nodes of the graph (a plain record
+        // during capture would only become an internal dependency)
+        if (profile) CK(cudaEventRecordWithFlags(pev[gi][2 * k], s, cudaEventRecordExternal));
         ikr::launch_pcg_spmv(A, w, k & 1, s);
-        if (profile) CK(cudaEventRecord(pev[gi][2 * k + 1], s));
+        if (profile) CK(cudaEventRecordWithFlags(pev[gi][2 * k + 1], s, cudaEventRecordExternal));
         ikr::launch_pcg_update(A, w, k & 1, s);
       }
       CK(cudaStreamEndCapture(s, &g));
