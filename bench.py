@@ -89,6 +89,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def log(msg):
+    print(msg, file=sys.stderr, flush=True)
+
+
 def peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -158,7 +162,10 @@ def run_ours(args, rank, world):
 
     # warm-up
     for _ in range(args.warmup):
+        t0 = time.perf_counter()
         info = mixed.run_device()
+        log(f"warmup mixed: {time.perf_counter() - t0:.3f} s, newton {info.totalIterations}, "
+            f"cg {info.totalLinearIterations}, ok {info.success}")
         assert info.success, "mixed-precision load path failed"
     barrier()
 
@@ -217,6 +224,7 @@ def run_ours(args, rank, world):
         pev1.synchronize()
         plain_times.append(pev0.elapsed_time(pev1) / 1e3)
         plain_infos.append(pinfo)
+        log(f"plain fp64: {plain_times[-1]:.3f} s, newton {pinfo.totalIterations}, cg {pinfo.totalLinearIterations}")
     t_plain = sum(plain_times) / len(plain_times)
     u_plain = plain.req.globalSolution()
     u_mixed = mixed.req.globalSolution()

@@ -261,3 +261,21 @@ def test_config1_mixed_precision_reaches_fp64_tolerance(ikr):
     for si in info.solverInfos[1:]:
         assert si.success
     assert rel_err(req.globalSolution(), ref["u"]) <= 1e-6
+
+
+@pytest.mark.parametrize("es", ["GreenLagrangeStrain", "DisplacementGradient", "DisplacementGradientTransposed"])
+def test_cpp_facade_cantilever_goldens(ikr, es, tmp_path):
+    """The reference's cantilever test written in C++ against include/ikarus_gb300.hpp (tests/cpp/)."""
+    import subprocess
+    from ikarus_gb300 import build
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    exe = str(tmp_path / "cantilever_eas")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(root, "include"),
+                    os.path.join(root, "tests", "cpp", "cantilever_eas.cpp"), "-L" + build.OUT, "-likarus_gb300",
+                    "-Wl,-rpath," + build.OUT, "-o", exe], check=True)
+    g = GOLD["cantilever_3d"]
+    want = g["results"][es]["NeoHooke"]
+    kind = {"GreenLagrangeStrain": 1, "DisplacementGradient": 2, "DisplacementGradientTransposed": 3}[es]
+    r = subprocess.run([exe, str(kind), str(g["eas_parameters"][es]), str(want["iterations"]), repr(want["max_disp"])],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
