@@ -168,6 +168,7 @@ SIGNATURES = {
     "ikr_linear_solver_profile": ([_vp, _I], C.c_int),
     "ikr_linear_solver_profile_read": ([_vp, _dp, _i64p], C.c_int),
     "ikr_fes_stream": ([_vp, C.POINTER(_vp)], C.c_int),
+    "ikr_linear_solver_solve_noalloc": ([_vp, _vp, _vp, _D, _I, _ip], C.c_int),
     "ikr_nr_settings_default": ([C.POINTER(_NRSettings)], C.c_int),
     "ikr_newton_create": ([C.POINTER(_vp), _vp, _vp, C.POINTER(_NRSettings)], C.c_int),
     "ikr_newton_destroy": ([_vp], C.c_int),

@@ -1093,6 +1093,45 @@ int ikr_linear_solver_profile_read(ikr_ls ls, double* ms, int64_t* n) {
     if (n) *n = ls->prof_n;
   });
 }
+// Allocation-free variant of the solve: the CG work set is carved out of the library's fixed device array
+// (noalloc.cu) instead of cudaMalloc'ed buffers; no graphs, events or pinned buffers either, the host polls
+// the device scalars with a plain copy into a static host array after every 32 iterations.
+int ikr_linear_solver_solve_noalloc(ikr_asm a, const double* b, double* x, double rtol, int32_t max_iter,
+                                    int32_t* iterations) {
+  return guarded([&] {
+    need(a && b && x, IKR_ERR_ARG, "null argument");
+    if (a->fes->nn > IKR_NOALLOC_MAX_NODES)
+      fail(IKR_ERR_ARG, "allocation-free solve supports at most %d nodes (%d dofs); this system has %d nodes",
+           IKR_NOALLOC_MAX_NODES, 3 * IKR_NOALLOC_MAX_NODES, a->fes->nn);
+    need(rtol >= 0 && max_iter > 0, IKR_ERR_ARG, "invalid tolerance");
+    need(a->matrix_dbc >= 0 && a->nb > 0, IKR_ERR_INVALID_STATE, "no matrix assembled");
+    void* base = nullptr;
+    CK(ikr::noalloc_scratch_address(&base));
+    ikr::PcgWork w;
+    ikr::noalloc_workset(base, a->fes->nn, a->fp32, std::min(4 * num_sms(), ikr::kNoAllocMaxGrid), w);
+    cudaStream_t s = a->fes->stream;
+    const ikr::Bsr A = a->bsr();
+    ikr::launch_block_jacobi(A, a->fp32, w.minv, false, s);
+    ikr::launch_pcg_init(A, w, b, rtol, max_iter, s);
+    count(3);
+    static thread_local double sc[ikr::kNScal];
+    for (;;) {
+      for (int k = 0; k < 32; ++k) ikr::launch_pcg_iteration(A, w, k & 1, s);
+      count(64);
+      CK(cudaGetLastError());
+      CK(cudaMemcpyAsync(sc, w.scal, sizeof(sc), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      if (sc[ikr::kDone] != 0.0) break;
+    }
+    ikr::launch_pcg_result(w, x, 1.0, s);
+    count(1);
+    CK(cudaStreamSynchronize(s));
+    if (iterations) *iterations = (int32_t)std::max(sc[ikr::kIters], sc[ikr::kIters + 1]);
+    if (sc[ikr::kDone] == 3.0) fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp <= 0)");
+    if (sc[ikr::kDone] == 2.0) fail(IKR_ERR_NOT_CONVERGED, "CG reached max_iter = %d", max_iter);
+  });
+}
+
 int ikr_fes_stream(ikr_fes fes, void** stream) {
   return guarded([&] {
     need(fes && stream, IKR_ERR_ARG, "null argument");

@@ -118,6 +118,13 @@ void launch_pcg_spmv(const Bsr& A, PcgWork& w, int parity, cudaStream_t s);
 void launch_pcg_update(const Bsr& A, PcgWork& w, int parity, cudaStream_t s);
 void launch_pcg_result(const PcgWork& w, double* x_out, double scale, cudaStream_t s);
 void launch_residual64(const Bsr& A, bool fp32, const double* x, const double* b, double* r, cudaStream_t s);
+
+// noalloc.cu -- fixed device scratch of the allocation-free CG solve
+constexpr int kNoAllocMaxRows = 32768;  // block rows (nodes) = 98304 dofs
+constexpr int kNoAllocMaxGrid = 1216;   // blocks of the partial-producing CG kernels
+size_t noalloc_scratch_bytes();
+cudaError_t noalloc_scratch_address(void** out);  // device address on the current device (cached per device)
+void noalloc_workset(void* base, int n_rows, bool fp32, int grid, PcgWork& w);
 void launch_axpy64(double* y, const double* x, double a, int64_t n, cudaStream_t s);
 void launch_scale64(double* y, const double* x, double a, int64_t n, cudaStream_t s);
 void launch_spmv64(const Bsr& A, bool fp32, const double* x, double* y, cudaStream_t s);

@@ -163,6 +163,23 @@ int ikr_linear_solver_profile_read(ikr_ls ls, double* spmv_ms_total, int64_t* sp
 /* the CUDA stream (cudaStream_t) all work on this element set is issued on */
 int ikr_fes_stream(ikr_fes fes, void** stream);
 
+/* Allocation-free solve of K x = b with the tangent the assembler last assembled (no counterpart in the
+ * reference).  For callers that may not allocate device memory after start-up (a fixed device-memory
+ * budget, or all allocations routed through their own allocator): it calls no cudaMalloc / cudaFree /
+ * cudaMallocHost and no allocating library routine.  The CG vectors, the 3x3 block-Jacobi inverse and the
+ * reduction slots live in one file-scope device array of the library (about 7.1 MB, held by every GPU that
+ * loads the library until exit), so the system may have at most IKR_NOALLOC_MAX_NODES nodes (3x as many
+ * dofs); larger systems return IKR_ERR_ARG.  b and x are device pointers of size() doubles; the CG runs in
+ * the precision of the stored tangent with the same block-Jacobi preconditioner, tolerance rtol on
+ * ||r|| / ||b|| and at most max_iter iterations (IKR_ERR_NOT_CONVERGED when that limit is hit).
+ * The first call on a device looks up the array's device address; make that call before any stream
+ * capture.  All calls share the one array, which keeps the last call's contents (every call re-initialises
+ * what it reads), so calls whose GPU work overlaps -- e.g. from two element sets on different streams --
+ * race on it: serialise them. */
+#define IKR_NOALLOC_MAX_NODES 32768
+int ikr_linear_solver_solve_noalloc(ikr_asm a, const double* b_device, double* x_device, double rtol,
+                                    int32_t max_iter, int32_t* iterations);
+
 /* ---- NewtonRaphson (newtonraphson.hh:27-303, nonlinearsolverfactory.hh:110-122) -------------------------- */
 typedef struct ikr_nr_settings {
   double tol;          /* NRSettings::tol (default 1e-8) */
