@@ -37,6 +37,19 @@ def parse():
     ap.add_argument("--plain-runs", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="32x8x8 mesh (profiling runs)")
+    ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
+                    help="2: 128x32x32 cantilever (default, the headline); 3: 512 batched cantilevers; "
+                         "4: learned predictor on 64x16x16; 5: nearly incompressible EAS block")
+    ap.add_argument("--train-paths", type=int, default=200, help="config 4: training load paths")
+    ap.add_argument("--eval-paths", type=int, default=20, help="config 4: held-out load paths")
+    ap.add_argument("--no-graphs", action="store_true", help="launch CG kernels one by one (for profilers)")
+    ap.add_argument("--eas-size", default="64,64,16", help="config 5: elements per direction")
+    ap.add_argument("--eas-steps", type=int, default=25, help="config 5: load steps")
+    ap.add_argument("--eas-predictor", type=int, default=1, help="config 5: 0 none, 1 previous increment")
+    ap.add_argument("--spmv-kinds", default="-1", help="--spmv-only: comma-separated kind[:keep] SpMV choices")
+    ap.add_argument("--spmv-only", type=int, default=0,
+                    help="assemble the 128x32x32 tangent once (FP32) and run this many CG iterations, then exit "
+                         "(the case the SpMV ncu captures run)")
     return ap.parse_args()
 
 
@@ -172,7 +185,6 @@ def run_ours(args, rank, world):
     # timed: device-resident inputs
     times, infos = [], []
     launches0 = ikr.kernel_launches()
-    mixed.ls.profile(True)
     with ClockSampler(0) as clocks:
         for _ in range(args.steps):
             flush.zero_()
@@ -185,9 +197,16 @@ def run_ours(args, rank, world):
             ev1.synchronize()
             times.append(ev0.elapsed_time(ev1) / 1e3)
             infos.append(info)
+    launches = (ikr.kernel_launches() - launches0) // max(1, args.steps)
+    # one more (untimed) load path with device events around every CG SpMV inside the graphs: the dominant
+    # kernel's average duration for the roofline (the event nodes would perturb the timed region)
+    mixed.ls.profile(True)
+    flush.zero_()
+    torch.cuda.synchronize()
+    pinfo = mixed.run_device()
+    assert pinfo.success
     spmv_ms, spmv_n = mixed.ls.profile_read()
     mixed.ls.profile(False)
-    launches = (ikr.kernel_launches() - launches0) // max(1, args.steps)
     assert all(i.success for i in infos)
     t_mixed = sum(times) / len(times)
     if world > 1:
@@ -212,6 +231,9 @@ def run_ours(args, rank, world):
 
     # plain FP64 form of the same method
     del flush
+    if args.plain_runs <= 0:
+        return finish(args, p, world, t_mixed, t_e2e, None, None, infos, launches, mixed, n_nodes, spmv_ms, spmv_n,
+                      clocks, None), p
     plain = Form(ikr, problems, p, mixed=False)
     pstream, pev0, pev1 = make_events(torch, plain.fes.stream())
     plain_times, plain_infos = [], []
@@ -229,6 +251,12 @@ def run_ours(args, rank, world):
     u_plain = plain.req.globalSolution()
     u_mixed = mixed.req.globalSolution()
     rel_diff = float(np.abs(u_mixed - u_plain).max() / np.abs(u_plain).max())
+    return finish(args, p, world, t_mixed, t_e2e, t_plain, plain_infos[-1], infos, launches, mixed, n_nodes, spmv_ms,
+                  spmv_n, clocks, rel_diff), p
+
+
+def finish(args, p, world, t_mixed, t_e2e, t_plain, plain_info, infos, launches, mixed, n_nodes, spmv_ms, spmv_n,
+           clocks, rel_diff):
 
     # roofline of the dominant kernel (the fused CG SpMV, FP32 in the mixed form)
     bpl, nb = spmv_bytes(mixed.asm, n_nodes, 4)
@@ -263,11 +291,12 @@ def run_ours(args, rank, world):
                    "load_steps": p.load_steps, "tolerance": "||R||/||R0|| < 1e-8 every load step",
                    "material": "NeoHooke E=1000 nu=0.3", "parallelism": f"replicas x{world}",
                    "l2": "256 MB buffer written between timed load paths; working set > L2"},
-        "plain_fp64": {"s_per_load_path": round(t_plain, 4), "newton_iterations": plain_infos[-1].totalIterations,
-                       "cg_iterations": plain_infos[-1].totalLinearIterations},
+        "plain_fp64": None if t_plain is None else
+        {"s_per_load_path": round(t_plain, 4), "newton_iterations": plain_info.totalIterations,
+         "cg_iterations": plain_info.totalLinearIterations},
         "mixed": {"newton_iterations": info0.totalIterations, "cg_iterations": info0.totalLinearIterations,
                   "newton_per_step": newton, "max_rel_diff_vs_plain": rel_diff},
-        "speedup_vs_plain_fp64": round(t_plain / t_mixed, 3),
+        "speedup_vs_plain_fp64": None if t_plain is None else round(t_plain / t_mixed, 3),
         "e2e": {"value": round(t_e2e, 4), "unit": "s", "h2d_bytes_per_step": 8 * p.n_dofs,
                 "d2h_bytes_per_step": 8 * p.n_dofs},
         "gpu_launches": int(launches),
@@ -277,7 +306,7 @@ def run_ours(args, rank, world):
                      "launches": spmv_n, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback"},
         "clocks": clocks.summary(),
     }
-    return out, p
+    return out
 
 
 # ---------------------------------------------------------------------------------------------------------
@@ -320,6 +349,236 @@ def cpu_sample(plain_newton, plain_cg, steps=1, warmup=0):
     return sum(vals) / len(vals), dict(t_residual_s=t_res, t_tangent_s=t_mat, t_cg_iteration_s=t_it)
 
 
+def run_spmv_only(args):
+    """Tangent of the 128x32x32 cantilever at the undeformed state (FP32) and a fixed number of CG iterations on
+    its external-load right-hand side, once per SpMV kernel choice in --spmv-kinds ("kind:keep" items, -1 =
+    tuned): the workload of the SpMV ncu captures and of the kernel comparison."""
+    import numpy as np
+
+    import ikarus_gb300 as ikr
+    from ikarus_gb300 import problems
+
+    p = problems.config2(load_steps=20)
+    fes, asm = problems.build_gpu(p, precision=1)
+    req = ikr.FERequirements(fes, None, 0.05)
+    asm.matrix(req, dbc=ikr.DBCOption.Full, export=False)
+    b = -asm.vector(req, dbc=ikr.DBCOption.Full)
+    bpl, nb = spmv_bytes(asm, p.mesh.n_nodes, 4)
+    out = {"n_blocks": nb, "dofs": p.n_dofs, "graphs": not args.no_graphs, "spmv_bytes": bpl, "runs": []}
+    for item in args.spmv_kinds.split(","):
+        kind, _, keep = item.partition(":")
+        ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-30, max_iter=args.spmv_only)
+        ls.set_launch(use_graphs=not args.no_graphs)
+        ls.set_kernel(int(kind), float(keep) if keep else (0.0 if int(kind) >= 0 else -1.0))
+        ls.compute(asm)
+        k_used, keep_used, tuned_us = ls.kernel_info()
+        rec = {"kind": k_used, "keep": keep_used, "tuned_us_per_iteration": round(tuned_us, 3)}
+        for profiled in (False, True):
+            ls.profile(profiled)
+            t0 = time.perf_counter()
+            try:
+                ls.solve(asm, b)
+            except ikr.IkarusError as e:  # the iteration limit is the point of this mode
+                if e.code != -5 and "NOT_CONVERGED" not in str(e):
+                    log(f"solve: {e}")
+            wall = time.perf_counter() - t0
+            it, rel = ls.last_info()
+            rec["plain_us_per_iteration" if not profiled else "profiled_us_per_iteration"] = round(
+                wall / max(it, 1) * 1e6, 2)
+            if profiled:
+                ms, n = ls.profile_read()
+                rec["spmv_us"] = round(ms / max(n, 1) * 1e3, 3)
+                rec["spmv_gbs"] = round(bpl / (ms / max(n, 1) / 1e3) / 1e9, 1) if ms > 0 else None
+                rec["iterations"] = it
+        ls.profile(False)
+        out["runs"].append(rec)
+        log(f"spmv-only: {rec}")
+        del ls
+    print(json.dumps(out))
+    return 0
+
+
+def run_batched(args):
+    """512 independent cantilevers (random grids, lengths, materials, tip tractions), 10 load steps, every
+    instance to ||R||/||R0|| < 1e-8 on every step: mixed form (FP32 tangent, one batched FP32 CG launch per Newton
+    iteration, FP64 residual) against the plain FP64 form of the same batched method."""
+    import numpy as np
+    import torch
+
+    import ikarus_gb300 as ikr
+    from ikarus_gb300 import problems
+
+    bp = problems.batched_cantilevers(512, seed=7, load_steps=10)
+    out = {"metric": "time to ||R||/||R0||<1e-8 on every load step for all 512 instances", "unit": "s",
+           "higher_is_better": False, "config": {"workload": bp.name, "elements": bp.mesh.n_elems,
+                                                  "dofs": bp.n_dofs, "instances": 512, "load_steps": 10}}
+    for mixed in (True, False):
+        fes, asm = problems.build_gpu_batched(bp, precision=1 if mixed else 0)
+        st = ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, eisenstat_walker=mixed,
+                            linear_rtol=1e-2 if mixed else 1e-10, linear_rtol_min=1e-6, linear_max_iter=20000)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+        lc = ikr.LoadControl(nr, bp.load_steps)
+        req, req0 = ikr.FERequirements(fes), ikr.FERequirements(fes)
+        stream, ev0, ev1 = make_events(torch, fes.stream())
+        times = []
+        for k in range(args.warmup + args.steps):
+            req.assign(req0)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            info = lc.run(req)
+            ev1.record(stream)
+            ev1.synchronize()
+            if k >= args.warmup:
+                times.append(ev0.elapsed_time(ev1) / 1e3)
+            log(f"batched {'mixed' if mixed else 'plain'}: {times[-1] if times else ev0.elapsed_time(ev1) / 1e3:.3f} s"
+                f" success {info.success} newton {info.totalIterations} cg {info.totalLinearIterations}")
+        its, rn, conv = nr.instance_info()
+        key = "mixed" if mixed else "plain_fp64"
+        out[key] = {"s": round(sum(times) / len(times), 4), "success": bool(info.success),
+                    "newton_iterations_batch": info.totalIterations, "cg_iterations_sum": info.totalLinearIterations,
+                    "instances_converged_last_step": int(conv.sum())}
+        del lc, nr, asm, fes
+    out["value"] = out["mixed"]["s"]
+    out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 3)
+    out["instances_per_s"] = round(512 / out["mixed"]["s"], 2)
+    print(json.dumps(out))
+
+
+def run_learned(args):
+    """Learned Newton predictor on the 64x16x16 cantilever: load paths with random top pressure
+    p(x) = sum a_k sin(k pi x / L) and tip traction; trained on --train-paths paths solved by the method without
+    predictor, evaluated on --eval-paths held-out paths (Newton iterations and time to ||R||/||R0|| < 1e-8 on
+    every step) against no predictor and against the previous-increment extrapolation."""
+    import numpy as np
+    import torch
+
+    import ikarus_gb300 as ikr
+    from ikarus_gb300 import problems
+
+    p = problems.learned_cantilever(64, 16, 16, load_steps=20)
+    fes, asm = problems.build_gpu(p, precision=1)
+    st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                        linear_rtol_min=1e-5, linear_max_iter=200000)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver()))
+    lc = ikr.LoadControl(nr, p.load_steps)
+    req = ikr.FERequirements(fes)
+    stream, ev0, ev1 = make_events(torch, fes.stream())
+    pred = ikr.LearnedPredictor(fes, n_params=9, n_modes=64, width=256, depth=4,
+                                capacity=args.train_paths * p.load_steps, seed=1)
+    rng = np.random.default_rng(2025)
+
+    def run(theta, kind, record=False):
+        fes.clear_neumann()
+        fes.add_neumann(*problems.learned_loads(p, theta))
+        req.insertGlobalSolution(np.zeros(p.n_dofs))
+        req.insertParameter(0.0)
+        lc.set_predictor(kind, pred if (kind == 2 or record) else None, theta, record)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        info = lc.run(req)
+        ev1.record(stream)
+        ev1.synchronize()
+        return info, ev0.elapsed_time(ev1) / 1e3, lc.predictor_stats()
+
+    t0 = time.perf_counter()
+    for i in range(args.train_paths):
+        info, _, _ = run(problems.sample_load_parameters(rng), 0, record=True)
+        if not info.success:
+            log(f"training path {i} did not converge")
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss, energy = pred.fit(epochs=300, batch=128, lr=1e-3)
+    t_fit = time.perf_counter() - t0
+    log(f"training data {t_data:.1f} s, fit {t_fit:.1f} s, loss {loss:.3e}, POD energy {energy:.6f}")
+    res = {k: {"newton": 0, "cg": 0, "s": 0.0, "failed": 0} for k in ("none", "previous_increment", "learned")}
+    kept = [0, 0]
+    for j in range(args.eval_paths):
+        theta = problems.sample_load_parameters(rng)
+        for kind, name in ((0, "none"), (1, "previous_increment"), (2, "learned")):
+            info, t, (acc, rej) = run(theta, kind)
+            r = res[name]
+            r["newton"] += info.totalIterations
+            r["cg"] += info.totalLinearIterations
+            r["s"] += t
+            r["failed"] += 0 if info.success else 1
+            if kind == 2:
+                kept[0] += acc
+                kept[1] += rej
+    for r in res.values():
+        r["s"] = round(r["s"] / args.eval_paths, 4)
+    out = {"metric": "Newton iterations and time per held-out load path to ||R||/||R0||<1e-8 (learned predictor)",
+           "config": {"workload": p.name, "dofs": p.n_dofs, "load_steps": p.load_steps, "train_paths":
+                      args.train_paths, "eval_paths": args.eval_paths, "pod_modes": 64, "mlp": "4 x 256 GELU, BF16 "
+                      "weights, FP32 accumulation"},
+           "training": {"data_s": round(t_data, 2), "fit_s": round(t_fit, 2), "loss": loss, "pod_energy": energy},
+           "results": res, "learned_predictions_kept": kept[0], "learned_predictions_rejected": kept[1],
+           "newton_saving_vs_none": round(1 - res["learned"]["newton"] / max(1, res["none"]["newton"]), 4),
+           "time_saving_vs_none": round(1 - res["learned"]["s"] / max(1e-9, res["none"]["s"]), 4)}
+    print(json.dumps(out))
+
+
+def run_eas(args):
+    """Nearly incompressible EAS block (64x64x16, 9-parameter GL EAS, nu = 0.4999, pressure 0 -> 50 on the centred
+    top patch, 25 load steps), every step to ||R||/||R0|| < 1e-8: plain FP64 form against the mixed form (FP32
+    global tangent and CG with FP64 iterative refinement, FP64 EAS condensation and residual), with the
+    per-step error of the mixed displacements against the plain ones."""
+    import numpy as np
+    import torch
+
+    import ikarus_gb300 as ikr
+    from ikarus_gb300 import problems
+
+    nx, ny, nz = (int(v) for v in args.eas_size.split(","))
+    p = problems.eas_block(nx, ny, nz, load_steps=args.eas_steps)
+    out = {"metric": "time to ||R||/||R0||<1e-8 on every load step (nearly incompressible EAS block)", "unit": "s",
+           "higher_is_better": False,
+           "config": {"workload": p.name, "elements": p.mesh.n_elems, "dofs": p.n_dofs, "load_steps": p.load_steps,
+                      "eas": "GreenLagrange E9", "nu": 0.4999, "predictor": args.eas_predictor}}
+    per_step = {}
+    for mixed in (False, True):
+        fes, asm = problems.build_gpu(p, precision=1 if mixed else 0)
+        if mixed:
+            st = ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                                linear_rtol_min=1e-5, linear_max_iter=400000, refinements=1)
+        else:
+            st = ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, linear_rtol=1e-10, linear_max_iter=1000000)
+        ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ls))
+        lc = ikr.LoadControl(nr, p.load_steps)
+        if args.eas_predictor:
+            lc.set_predictor(1)
+        req = ikr.FERequirements(fes)
+        us = []
+
+        def obs(msg, state, req=req, us=us):
+            if msg == ikr.ControlMessages.STEP_ENDED:
+                us.append(req.globalSolution())
+
+        lc.subscribe(obs)
+        stream, ev0, ev1 = make_events(torch, fes.stream())
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        info = lc.run(req)
+        ev1.record(stream)
+        ev1.synchronize()
+        t = ev0.elapsed_time(ev1) / 1e3  # includes the observer's per-step downloads
+        key = "mixed" if mixed else "plain_fp64"
+        out[key] = {"s": round(t, 3), "success": bool(info.success), "newton_iterations": info.totalIterations,
+                    "cg_iterations": info.totalLinearIterations,
+                    "newton_per_step": [si.iterations for si in info.solverInfos], "spmv_kernel": ls.kernel_info()[:2]}
+        per_step[key] = us
+        log(f"eas {key}: {t:.2f} s success {info.success} newton {info.totalIterations} "
+            f"cg {info.totalLinearIterations}")
+        del lc, nr, ls, asm, fes
+    if len(per_step["mixed"]) == len(per_step["plain_fp64"]):
+        out["mixed"]["max_rel_diff_vs_plain_per_step"] = [
+            float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+            for a, b in zip(per_step["mixed"], per_step["plain_fp64"])]
+    out["value"] = out["mixed"]["s"]
+    out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 3)
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -356,10 +615,17 @@ def main():
                           "e2e": {"value": round(val, 2), "unit": "s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}))
         return
+    if args.spmv_only:
+        return run_spmv_only(args)
+    if args.config == 3:
+        return run_batched(args)
+    if args.config == 4:
+        return run_learned(args)
+    if args.config == 5:
+        return run_eas(args)
     out, p = run_ours(args, rank, world)
     if rank == 0:
-        os.makedirs(os.path.join(ROOT, "profiles"), exist_ok=True)
-        if not args.no_cpu_baseline and not args.small:
+        if not args.no_cpu_baseline and not args.small and out["plain_fp64"]:
             v, parts = cpu_sample(out["plain_fp64"]["newton_iterations"], out["plain_fp64"]["cg_iterations"])
             out["cpu_baseline"] = {"value": round(v, 2), "unit": "s", "cores": 1, "kind": "port",
                                    "sample": "oracle port, 1 thread: one R+K assembly (reference-faithful moduli) "

@@ -29,7 +29,7 @@ class IkarusError(RuntimeError):
 
 
 _STATUS = {-1: "ARG", -2: "NOT_IMPLEMENTED", -3: "INVALID_STATE", -4: "NONPOSITIVE_DETC", -5: "NOT_CONVERGED",
-           -6: "CG_BREAKDOWN", -7: "CUDA", -8: "SINGULAR", -9: "NO_DEVICE"}
+           -6: "CG_BREAKDOWN", -7: "CUDA", -8: "SINGULAR", -9: "NO_DEVICE", -10: "TIMEOUT"}
 
 
 class DBCOption(enum.IntEnum):  # ikarus/assembler/dirichletbcenforcement.hh:8
@@ -64,6 +64,7 @@ class SolverTypeTag(enum.IntEnum):  # ikarus/solver/linearsolver/linearsolver.hh
     none = 0
     si_ConjugateGradient = 1
     gpu_PCG_BlockJacobi = 100
+    gpu_PCG_Batched = 101
 
 
 class Precision(enum.IntEnum):
@@ -123,6 +124,7 @@ _CTRL_OBS = C.CFUNCTYPE(None, C.c_int32, C.POINTER(_ControlState), C.c_void_p)
 _vp, _dp, _ip, _i64p, _u8p = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_int64), \
     C.POINTER(C.c_uint8)
 _I, _D, _L = C.c_int32, C.c_double, C.c_int64
+_fp = C.POINTER(C.c_float)
 SIGNATURES = {
     "ikr_version": ([], C.c_int),
     "ikr_last_error": ([C.c_char_p, _I], C.c_int),
@@ -130,6 +132,10 @@ SIGNATURES = {
     "ikr_fes_create": ([C.POINTER(_vp), _I, _dp, _I, _ip, _D, _D, _I, _I], C.c_int),
     "ikr_fes_add_neumann": ([_vp, _I, _ip, _ip, _dp], C.c_int),
     "ikr_fes_destroy": ([_vp], C.c_int),
+    "ikr_fes_clear_neumann": ([_vp], C.c_int),
+    "ikr_fes_set_element_materials": ([_vp, _dp, _dp], C.c_int),
+    "ikr_fes_set_instances": ([_vp, _I, _ip], C.c_int),
+    "ikr_newton_instance_info": ([_vp, _ip, _dp, _ip], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_get_alpha": ([_vp, _dp], C.c_int),
     "ikr_fes_set_alpha": ([_vp, _dp], C.c_int),
@@ -167,6 +173,9 @@ SIGNATURES = {
     "ikr_linear_solver_last_info": ([_vp, _ip, _dp], C.c_int),
     "ikr_linear_solver_profile": ([_vp, _I], C.c_int),
     "ikr_linear_solver_profile_read": ([_vp, _dp, _i64p], C.c_int),
+    "ikr_linear_solver_set_launch": ([_vp, _I, _I], C.c_int),
+    "ikr_linear_solver_set_kernel": ([_vp, _I, _D], C.c_int),
+    "ikr_linear_solver_kernel_info": ([_vp, _ip, _dp, _dp], C.c_int),
     "ikr_fes_stream": ([_vp, C.POINTER(_vp)], C.c_int),
     "ikr_linear_solver_solve_noalloc": ([_vp, _vp, _vp, _D, _I, _ip], C.c_int),
     "ikr_nr_settings_default": ([C.POINTER(_NRSettings)], C.c_int),
@@ -179,6 +188,23 @@ SIGNATURES = {
     "ikr_load_control_destroy": ([_vp], C.c_int),
     "ikr_load_control_subscribe": ([_vp, _CTRL_OBS, _vp], C.c_int),
     "ikr_load_control_run": ([_vp, _vp, C.POINTER(_ControlInfo), C.POINTER(_NRInfo), _I], C.c_int),
+    "ikr_load_control_set_predictor": ([_vp, _I, _vp, _dp, _I], C.c_int),
+    "ikr_load_control_predictor_stats": ([_vp, _ip, _ip], C.c_int),
+    "ikr_load_control_predictor_history": ([_vp, _I, _dp, _ip], C.c_int),
+    "ikr_load_control_set_predictor_gate": ([_vp, _I, _I], C.c_int),
+    "ikr_load_control_predictor_gate_cg": ([_vp, _i64p], C.c_int),
+    "ikr_predictor_create": ([C.POINTER(_vp), _vp, _I, _I, _I, _I, _L, C.c_uint64], C.c_int),
+    "ikr_predictor_destroy": ([_vp], C.c_int),
+    "ikr_predictor_num_snapshots": ([_vp, _i64p], C.c_int),
+    "ikr_predictor_fit": ([_vp, _I, _I, C.c_float, C.POINTER(C.c_float), _dp], C.c_int),
+    "ikr_mlp_create": ([C.POINTER(_vp), _I, _I, _I, _I, C.c_uint64], C.c_int),
+    "ikr_mlp_destroy": ([_vp], C.c_int),
+    "ikr_mlp_num_params": ([_vp, _i64p], C.c_int),
+    "ikr_mlp_get_params": ([_vp, _fp], C.c_int),
+    "ikr_mlp_set_params": ([_vp, _fp], C.c_int),
+    "ikr_mlp_forward": ([_vp, _I, _fp, _fp], C.c_int),
+    "ikr_mlp_loss_grad": ([_vp, _I, _fp, _fp, _fp, _fp], C.c_int),
+    "ikr_mlp_train": ([_vp, _I, _fp, _fp, _I, _I, C.c_float, C.c_uint64, _fp], C.c_int),
 }
 
 
@@ -260,6 +286,21 @@ class FiniteElements:
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(traction, dtype=np.float64), (len(fe), 3)))
         _err(lib().ikr_fes_add_neumann(self.h, len(fe), _ptr(fe, C.c_int32), _ptr(fl, C.c_int32), _ptr(t)),
              "add_neumann")
+
+    def clear_neumann(self):
+        _err(lib().ikr_fes_clear_neumann(self.h), "clear_neumann")
+
+    def set_element_materials(self, lam, mu):
+        """Per-element NeoHooke Lame parameters."""
+        lam = np.ascontiguousarray(lam, dtype=np.float64)
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        _err(lib().ikr_fes_set_element_materials(self.h, _ptr(lam), _ptr(mu)), "set_element_materials")
+
+    def set_instances(self, node_offsets):
+        """Independent problems on contiguous node ranges (batched Newton / CG with gpu_PCG_Batched)."""
+        off = np.ascontiguousarray(node_offsets, dtype=np.int32)
+        self.n_instances = len(off) - 1
+        _err(lib().ikr_fes_set_instances(self.h, self.n_instances, _ptr(off, C.c_int32)), "set_instances")
 
     def num_colours(self):
         n = C.c_int32()
@@ -515,6 +556,20 @@ class LinearSolver:
         """Bracket every CG SpMV with device events (inside the CUDA graphs); resets the counters."""
         _err(lib().ikr_linear_solver_profile(self.h, int(on)))
 
+    def set_launch(self, use_graphs=True, chunk_len=16):
+        """CG iterations per host poll, issued as CUDA graphs or kernel by kernel."""
+        _err(lib().ikr_linear_solver_set_launch(self.h, int(use_graphs), int(chunk_len)))
+
+    def set_kernel(self, spmv_kind=-1, l2_keep_fraction=-1.0):
+        """SpMV kernel (0 direct, 1..4 staged, -1 autotune) and L2 keep fraction (-1 autotune)."""
+        _err(lib().ikr_linear_solver_set_kernel(self.h, int(spmv_kind), float(l2_keep_fraction)))
+
+    def kernel_info(self):
+        """(spmv kind, L2 keep fraction, tuned SpMV microseconds per launch)."""
+        k, f, us = C.c_int32(), C.c_double(), C.c_double()
+        _err(lib().ikr_linear_solver_kernel_info(self.h, C.byref(k), C.byref(f), C.byref(us)))
+        return k.value, f.value, us.value
+
     def profile_read(self):
         """(summed SpMV device time in ms, SpMV launches) since profiling was switched on."""
         ms, n = C.c_double(), C.c_int64()
@@ -593,6 +648,15 @@ class NewtonRaphson:
     def subscribe_fe_state(self, on=True):
         _err(lib().ikr_newton_subscribe_fe_state(self.h, int(on)))
 
+    def instance_info(self):
+        """(iterations, residual norms, converged) per instance of the last batched solve."""
+        n = self.assembler.fes.n_instances
+        it = np.zeros(n, dtype=np.int32)
+        rn = np.zeros(n)
+        cv = np.zeros(n, dtype=np.int32)
+        _err(lib().ikr_newton_instance_info(self.h, _ptr(it, C.c_int32), _ptr(rn), _ptr(cv, C.c_int32)))
+        return it, rn, cv.astype(bool)
+
     def solve(self, req: FERequirements, stepSize: float = 0.0) -> NonLinearSolverInformation:
         info = _NRInfo()
         _err(lib().ikr_newton_solve(self.h, req.h, stepSize, C.byref(info)), "NewtonRaphson::solve")
@@ -635,6 +699,35 @@ class LoadControl:
         self._cbs.append(cb)
         _err(lib().ikr_load_control_subscribe(self.h, cb, None), "subscribe")
 
+    def set_predictor(self, kind: int = 0, predictor: "LearnedPredictor" = None, params=None, record=False):
+        """Newton predictor of every load step: 0 none (reference), 1 previous increment, 2 learned.
+        Predictions are kept only when their FP64 residual is below the unpredicted one."""
+        par = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
+        _err(lib().ikr_load_control_set_predictor(self.h, int(kind), predictor.h if predictor else None,
+                                                  _ptr(par) if par is not None else None, int(record)), "predictor")
+
+    def predictor_stats(self):
+        a, r = C.c_int32(), C.c_int32()
+        _err(lib().ikr_load_control_predictor_stats(self.h, C.byref(a), C.byref(r)))
+        return a.value, r.value
+
+    def set_predictor_gate(self, gate=0, relax_iters=30):
+        """0: FP64 residual at the candidates; 1: after one truncated Newton step from each; 2: ungated."""
+        _err(lib().ikr_load_control_set_predictor_gate(self.h, int(gate), int(relax_iters)))
+
+    def predictor_gate_cg(self):
+        n = C.c_int64()
+        _err(lib().ikr_load_control_predictor_gate_cg(self.h, C.byref(n)))
+        return n.value
+
+    def predictor_history(self):
+        """Per load step of the last run: (step, |R| unpredicted, |R| full prediction, s*, |R| at s*, s kept)."""
+        n = C.c_int32()
+        _err(lib().ikr_load_control_predictor_history(self.h, 0, None, C.byref(n)))
+        out = np.zeros((max(n.value, 1), 6))
+        _err(lib().ikr_load_control_predictor_history(self.h, n.value, _ptr(out), C.byref(n)))
+        return out[:n.value]
+
     def run(self, req: FERequirements) -> ControlInformation:
         cap = self.loadSteps + 1
         infos = (_NRInfo * cap)()
@@ -643,3 +736,83 @@ class LoadControl:
         return ControlInformation(bool(ci.success), [NonLinearSolverInformation._from(infos[i])
                                                      for i in range(min(ci.n_solver_infos, cap))],
                                   ci.total_iterations, ci.total_linear_iterations)
+
+
+# ---- learned Newton predictor ------------------------------------------------------------------------------
+class MLP:
+    """Dense network with GELU hidden layers, BF16 weights and FP32 accumulation, trained on the GPU."""
+
+    def __init__(self, n_in, width, depth, n_out, seed=0):
+        h = C.c_void_p()
+        _err(lib().ikr_mlp_create(C.byref(h), n_in, width, depth, n_out, seed), "mlp")
+        self.h, self.n_in, self.width, self.depth, self.n_out = h, n_in, width, depth, n_out
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_mlp_destroy(self.h)
+            self.h = None
+
+    def num_params(self):
+        n = C.c_int64()
+        _err(lib().ikr_mlp_num_params(self.h, C.byref(n)))
+        return n.value
+
+    @property
+    def params(self):
+        out = np.zeros(self.num_params(), dtype=np.float32)
+        _err(lib().ikr_mlp_get_params(self.h, _ptr(out, C.c_float)))
+        return out
+
+    @params.setter
+    def params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _err(lib().ikr_mlp_set_params(self.h, _ptr(p, C.c_float)))
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros((x.shape[0], self.n_out), dtype=np.float32)
+        _err(lib().ikr_mlp_forward(self.h, x.shape[0], _ptr(x, C.c_float), _ptr(y, C.c_float)), "forward")
+        return y
+
+    def loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = C.c_float()
+        g = np.zeros(self.num_params(), dtype=np.float32)
+        _err(lib().ikr_mlp_loss_grad(self.h, x.shape[0], _ptr(x, C.c_float), _ptr(t, C.c_float), C.byref(loss),
+                                     _ptr(g, C.c_float)), "loss_grad")
+        return loss.value, g
+
+    def train(self, x, t, epochs, batch, lr, seed=0):
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(t, dtype=np.float32)
+        loss = C.c_float()
+        _err(lib().ikr_mlp_train(self.h, x.shape[0], _ptr(x, C.c_float), _ptr(t, C.c_float), epochs, batch, lr, seed,
+                                 C.byref(loss)), "train")
+        return loss.value
+
+
+class LearnedPredictor:
+    """POD basis of converged displacement increments + MLP over [load parameters, load factor, POD coordinates
+    of the previous two increments] predicting the next increment (trained on the GPU)."""
+
+    def __init__(self, fes: FiniteElements, n_params, n_modes=64, width=256, depth=4, capacity=4096, seed=0):
+        h = C.c_void_p()
+        _err(lib().ikr_predictor_create(C.byref(h), fes.h, n_params, n_modes, width, depth, capacity, seed),
+             "predictor")
+        self.h, self.fes, self.n_params = h, fes, n_params
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_predictor_destroy(self.h)
+            self.h = None
+
+    def num_snapshots(self):
+        n = C.c_int64()
+        _err(lib().ikr_predictor_num_snapshots(self.h, C.byref(n)))
+        return n.value
+
+    def fit(self, epochs=300, batch=128, lr=1e-3):
+        loss, energy = C.c_float(), C.c_double()
+        _err(lib().ikr_predictor_fit(self.h, epochs, batch, lr, C.byref(loss), C.byref(energy)), "fit")
+        return loss.value, energy.value

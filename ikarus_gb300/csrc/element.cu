@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(256) disp_element_kernel(ElemArgs a, const int
     dX[c] = KT(Xd[c] - x0);
     dU[c] = KT(Ud[c] - u0);
   }
-  const KT lam = KT(a.lam), mu = KT(a.mu);
+  const KT lam = KT(a.lam_e ? a.lam_e[e] : a.lam), mu = KT(a.mu_e ? a.mu_e[e] : a.mu);
 
   KT Kacc[5][3][3];
   if (WANT_K) {
@@ -206,20 +206,20 @@ __global__ void __launch_bounds__(256) disp_element_kernel(ElemArgs a, const int
         const int Jn = (sub + d) & 7;
         const uint8_t fmaskJ = a.node_fixed ? a.node_fixed[a.conn[Jn * ne + e]] : uint8_t(0);
         const int64_t s1 = a.slot[(size_t)(sub * 8 + Jn) * ne + e];
-        KT* b1 = val + 9 * s1;
+        KT* b1 = val + block_entry(s1, 0);  // entries of a block are 32 apart
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int j = 0; j < 3; ++j)
-            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[3 * i + j] += Kacc[d][i][j];
+            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[32 * (3 * i + j)] += Kacc[d][i][j];
         if (d >= 1 && d <= 3) {
           const int64_t s2 = a.slot[(size_t)(Jn * 8 + sub) * ne + e];
-          KT* b2 = val + 9 * s2;
+          KT* b2 = val + block_entry(s2, 0);
 #pragma unroll
           for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j)
-              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[3 * j + i] += Kacc[d][i][j];
+              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[32 * (3 * j + i)] += Kacc[d][i][j];
         }
       }
     }

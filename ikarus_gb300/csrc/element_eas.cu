@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(EasCfg<NA>::EPB * 8) eas_element_kernel(ElemAr
   }
   __syncwarp();
 
-  const double lam = a.lam, mu = a.mu;
+  const double lam = a.lam_e ? a.lam_e[e] : a.lam, mu = a.mu_e ? a.mu_e[e] : a.mu;
   double f[3] = {0, 0, 0};
   double Kacc[5][3][3];
 #pragma unroll
@@ -588,19 +588,19 @@ __global__ void __launch_bounds__(EasCfg<NA>::EPB * 8) eas_element_kernel(ElemAr
       for (int d = 0; d < 5; ++d) {
         const int Jn = (sub + d) & 7;
         const uint8_t fmaskJ = a.node_fixed ? a.node_fixed[a.conn[Jn * ne + e]] : uint8_t(0);
-        KT* b1 = val + 9 * (int64_t)a.slot[(size_t)(sub * 8 + Jn) * ne + e];
+        KT* b1 = val + block_entry(a.slot[(size_t)(sub * 8 + Jn) * ne + e], 0);  // entries 32 apart
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int j = 0; j < 3; ++j)
-            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[3 * i + j] += KT(Kacc[d][i][j]);
+            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[32 * (3 * i + j)] += KT(Kacc[d][i][j]);
         if (d >= 1 && d <= 3) {
-          KT* b2 = val + 9 * (int64_t)a.slot[(size_t)(Jn * 8 + sub) * ne + e];
+          KT* b2 = val + block_entry(a.slot[(size_t)(Jn * 8 + sub) * ne + e], 0);
 #pragma unroll
           for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j)
-              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[3 * j + i] += KT(Kacc[d][i][j]);
+              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[32 * (3 * j + i)] += KT(Kacc[d][i][j]);
         }
       }
     }

@@ -1,506 +1,12 @@
 // Host layer of the GB300-native Newton-Raphson / LoadControl path: the C ABI of include/ikarus_gb300.h.
-// One CUDA stream per finite-element set; every object built on that set (requirements, assembler,
-// solver, Newton, LoadControl) issues its work on it.  Kernels live in element.cu, sparse.cu, solver.cu.
-#include <cuda_runtime.h>
-
-#include <algorithm>
-#include <array>
-#include <atomic>
-#include <cmath>
-#include <cstdarg>
-#include <cstdio>
-#include <cstring>
-#include <map>
-#include <memory>
-#include <numeric>
-#include <stdexcept>
-#include <string>
-#include <vector>
-
-#include "../../include/ikarus_gb300.h"
-#include "kernels.h"
-
-namespace {
-
+// Kernels live in element.cu, element_eas.cu, sparse.cu, solver.cu; shared internals in host_internal.h.
+#include "host_internal.h"
+// ------------------------------------------------------------------------------------------------------------
+namespace ikr_host {
 thread_local std::string g_last_error;
 std::atomic<int64_t> g_launches{0};
+}  // namespace ikr_host
 
-struct IkrError : std::runtime_error {
-  int code;
-  IkrError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
-};
-
-[[noreturn]] void fail(int code, const char* fmt, ...) {
-  char buf[512];
-  va_list ap;
-  va_start(ap, fmt);
-  vsnprintf(buf, sizeof(buf), fmt, ap);
-  va_end(ap);
-  throw IkrError(code, buf);
-}
-
-void cuda_check(cudaError_t e, const char* what) {
-  if (e != cudaSuccess) fail(IKR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-}
-#define CK(x) cuda_check((x), #x)
-
-void count(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
-
-template <typename F>
-int guarded(F&& f) {
-  try {
-    f();
-    return IKR_OK;
-  } catch (const IkrError& e) {
-    g_last_error = e.what();
-    return e.code;
-  } catch (const std::bad_alloc&) {
-    g_last_error = "host allocation failed";
-    return IKR_ERR_ARG;
-  } catch (const std::exception& e) {
-    g_last_error = e.what();
-    return IKR_ERR_ARG;
-  }
-}
-
-// device buffer
-template <typename T>
-struct DBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  DBuf() = default;
-  DBuf(const DBuf&) = delete;
-  DBuf& operator=(const DBuf&) = delete;
-  ~DBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  void alloc(size_t count) {
-    if (count == n && p) return;
-    release();
-    if (count == 0) return;
-    CK(cudaMalloc(&p, count * sizeof(T)));
-    n = count;
-  }
-  void upload(const T* h, size_t count, cudaStream_t s) {
-    alloc(count);
-    if (count) CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
-  }
-  void download(T* h, size_t count, cudaStream_t s) const {
-    if (count) CK(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
-  }
-};
-
-int num_sms() {
-  static int sms = [] {
-    int dev = 0, v = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return 152;
-    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 152;
-    return v > 0 ? v : 152;
-  }();
-  return sms;
-}
-
-}  // namespace
-
-// ------------------------------------------------------------------------------------------------------------
-struct ikr_fes_s {
-  int nn = 0, ne = 0, na = 0, eas = 0;
-  double lam = 0, mu = 0;
-  cudaStream_t stream = nullptr;
-  std::vector<int32_t> conn_h;  // row-major n_elems x 8
-  DBuf<double> X;
-  DBuf<int32_t> conn;  // corner-major
-  DBuf<double> alpha;  // n_alpha x n_elems
-  DBuf<double> eas_geo;
-  DBuf<double> eas_y, eas_Y;
-  uint64_t eas_cache_key = 0;  // (req id, solution version, alpha version) hash of the cached D^{-1}R~, D^{-1}L
-  uint64_t alpha_version = 1;
-  // colours
-  std::vector<int32_t> colour_ptr;
-  DBuf<int32_t> colour_elems;
-  // Neumann faces
-  std::vector<std::vector<std::pair<int, std::array<double, 3>>>> faces;
-  DBuf<int32_t> trac_idx;
-  DBuf<double> trac;
-  bool trac_dirty = false;
-  DBuf<int> status;
-  DBuf<double> scratch_out;  // element-level outputs
-
-  ~ikr_fes_s() {
-    if (stream) cudaStreamDestroy(stream);
-  }
-
-  ikr::ElemArgs args() const {
-    ikr::ElemArgs a;
-    a.n_nodes = nn;
-    a.n_elems = ne;
-    a.X = X.p;
-    a.conn = conn.p;
-    a.lam = lam;
-    a.mu = mu;
-    a.eas_kind = na > 0 ? eas : 0;
-    a.n_alpha = na;
-    a.alpha = alpha.p;
-    a.eas_geo = eas_geo.p;
-    a.eas_y = eas_y.p;
-    a.eas_Y = eas_Y.p;
-    a.trac_idx = trac_idx.n ? trac_idx.p : nullptr;
-    a.trac = trac.p;
-    a.status = status.p;
-    return a;
-  }
-
-  void refresh_tractions() {
-    if (!trac_dirty) return;
-    std::vector<int32_t> idx(ne, -1), slot_elem, face_ptr{0}, face_local;
-    std::vector<double> t;
-    for (int e = 0; e < ne; ++e) {
-      if (faces[e].empty()) continue;
-      idx[e] = (int32_t)slot_elem.size();
-      slot_elem.push_back(e);
-      for (auto& f : faces[e]) {
-        face_local.push_back(f.first);
-        t.insert(t.end(), f.second.begin(), f.second.end());
-      }
-      face_ptr.push_back((int32_t)face_local.size());
-    }
-    trac_idx.upload(idx.data(), idx.size(), stream);
-    DBuf<int32_t> d_se, d_fp, d_fl;
-    DBuf<double> d_t;
-    d_se.upload(slot_elem.data(), slot_elem.size(), stream);
-    d_fp.upload(face_ptr.data(), face_ptr.size(), stream);
-    d_fl.upload(face_local.data(), face_local.size(), stream);
-    d_t.upload(t.data(), t.size(), stream);
-    trac.alloc(std::max<size_t>(1, 24 * slot_elem.size()));
-    ikr::launch_traction_loads(X.p, conn.p, ne, (int)slot_elem.size(), d_se.p, d_fp.p, d_fl.p, d_t.p, trac.p, stream);
-    count(1);
-    CK(cudaStreamSynchronize(stream));
-    trac_dirty = false;
-  }
-
-  void check_status() {
-    int h = 0;
-    CK(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
-    if (h) {
-      CK(cudaMemsetAsync(status.p, 0, sizeof(int), stream));
-      if (h & ikr::kStatusNonPositiveDetC)
-        fail(IKR_ERR_NONPOSITIVE_DETC, "Determinant of right Cauchy Green tensor C must be greater than zero");
-      if (h & ikr::kStatusSingularD) fail(IKR_ERR_SINGULAR, "EAS matrix D is singular");
-      if (h & ikr::kStatusPatternOverflow) fail(IKR_ERR_ARG, "a node couples with more than 128 nodes");
-      fail(IKR_ERR_ARG, "device status %d", h);
-    }
-  }
-
-  void launch_elements(const ikr::ElemArgs& a, int mode, bool fp32, const int32_t* list, int n, int base) {
-    if (na > 0) ikr::launch_eas_element(a, mode, fp32, list, n, base, stream);
-    else ikr::launch_disp_element(a, mode, fp32, list, n, base, stream);
-    count(1);
-  }
-  // one launch per colour class: deterministic scatter without atomics
-  void launch_coloured(const ikr::ElemArgs& a, int mode, bool fp32) {
-    for (size_t c = 0; c + 1 < colour_ptr.size(); ++c) {
-      const int n = colour_ptr[c + 1] - colour_ptr[c];
-      launch_elements(a, mode, fp32, colour_elems.p + colour_ptr[c], n, 0);
-    }
-  }
-};
-
-struct ikr_req_s {
-  ikr_fes fes = nullptr;
-  DBuf<double> u;
-  double lambda = 0.0;
-  uint64_t id = 0;
-  uint64_t version = 1;
-};
-
-struct ikr_asm_s {
-  ikr_fes fes = nullptr;
-  int n = 0, nred = 0;
-  bool fp32 = false;
-  std::vector<uint8_t> fixed_h;
-  std::vector<int32_t> cb_h;
-  DBuf<uint8_t> node_fixed;
-  // pattern
-  int64_t nb = 0;
-  DBuf<int32_t> row_ptr, col, diag, slot;
-  std::vector<int32_t> row_ptr_h, col_h;
-  DBuf<double> val64;
-  DBuf<float> val32;
-  int matrix_dbc = -1;  // option of the last assembled matrix
-  // vector
-  DBuf<double> R;
-  int vector_dbc = -1;
-  DBuf<int32_t> pl_dof;
-  DBuf<double> pl_val;
-  std::map<int32_t, double> pl_h;
-  DBuf<double> norm_part, norm_out;
-  ikr_req bound_req = nullptr;
-  int bound_dbc = IKR_DBC_FULL;
-
-  ikr::Bsr bsr() const {
-    ikr::Bsr b;
-    b.n_rows = fes->nn;
-    b.n_blocks = nb;
-    b.row_ptr = row_ptr.p;
-    b.col = col.p;
-    b.diag = diag.p;
-    b.val = fp32 ? (const void*)val32.p : (const void*)val64.p;
-    return b;
-  }
-  void* values() { return fp32 ? (void*)val32.p : (void*)val64.p; }
-
-  void build_pattern() {
-    ikr_fes f = fes;
-    cudaStream_t s = f->stream;
-    DBuf<int32_t> cnt, ne_ptr, cursor, ne_elems, rcnt;
-    cnt.alloc(f->nn);
-    ne_ptr.alloc(f->nn + 1);
-    cursor.alloc(f->nn);
-    ne_elems.alloc(8LL * f->ne);
-    ikr::launch_node_elem_count(f->conn.p, f->ne, f->nn, cnt.p, s);
-    ikr::launch_exclusive_scan(cnt.p, ne_ptr.p, f->nn, s);
-    ikr::launch_node_elem_fill(f->conn.p, f->ne, ne_ptr.p, cursor.p, ne_elems.p, f->nn, s);
-    rcnt.alloc(f->nn);
-    ikr::launch_row_build(f->conn.p, f->ne, f->nn, ne_ptr.p, ne_elems.p, nullptr, rcnt.p, false, f->status.p, s);
-    row_ptr.alloc(f->nn + 1);
-    ikr::launch_exclusive_scan(rcnt.p, row_ptr.p, f->nn, s);
-    count(7);
-    int32_t total = 0;
-    CK(cudaMemcpyAsync(&total, row_ptr.p + f->nn, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    f->check_status();
-    nb = total;
-    col.alloc(nb);
-    ikr::launch_row_build(f->conn.p, f->ne, f->nn, ne_ptr.p, ne_elems.p, row_ptr.p, col.p, true, f->status.p, s);
-    slot.alloc(64LL * f->ne);
-    diag.alloc(f->nn);
-    ikr::launch_slot_map(f->conn.p, f->ne, row_ptr.p, col.p, slot.p, diag.p, f->nn, s);
-    count(3);
-    row_ptr_h.resize(f->nn + 1);
-    col_h.resize(nb);
-    row_ptr.download(row_ptr_h.data(), row_ptr_h.size(), s);
-    col.download(col_h.data(), col_h.size(), s);
-    CK(cudaStreamSynchronize(s));
-    f->check_status();
-    if (fp32) val32.alloc(9 * nb);
-    else val64.alloc(9 * nb);
-  }
-};
-
-struct ikr_ls_s {
-  int tag = IKR_SOLVER_GPU_PCG_BLOCK_JACOBI;
-  double rtol = 1e-10;
-  int max_iter = 100000;
-  ikr_asm asm_ = nullptr;
-  bool fp32 = false;
-  ikr::PcgWork w;
-  DBuf<double> dx, dp, dq, dmv, pa, pb, scal;
-  DBuf<float> fx, fp, fq, fmv;
-  DBuf<double> dz, dr, dp1;
-  DBuf<float> fz, fr, fp1;
-  double* scal_h = nullptr;
-  cudaEvent_t ev[2] = {nullptr, nullptr};
-  // CG iterations are launched as CUDA graphs of chunk_len iterations.  In profiling mode two graphs
-  // alternate, each with its own event-record nodes around every SpMV, so the SpMV device time of the
-  // chunk that just finished can be read while the next one runs.
-  cudaGraphExec_t chunk[2] = {nullptr, nullptr};
-  int chunk_len = 16;
-  bool profile = false;
-  std::vector<cudaEvent_t> pev[2];
-  double prof_ms = 0.0;
-  int64_t prof_n = 0;
-  int last_iters = 0;
-  double last_rel = 0.0;
-  bool factorized = false;
-  DBuf<double> b64, x64, r64, c64;  // refinement work
-
-  ~ikr_ls_s() {
-    drop_graphs();
-    for (auto& e : ev)
-      if (e) cudaEventDestroy(e);
-    for (auto& v : pev)
-      for (auto e : v) cudaEventDestroy(e);
-    if (scal_h) cudaFreeHost(scal_h);
-  }
-
-  void drop_graphs() {
-    for (auto& g : chunk)
-      if (g) {
-        cudaGraphExecDestroy(g);
-        g = nullptr;
-      }
-  }
-
-  void set_profile(bool on) {
-    if (on != profile) drop_graphs();
-    profile = on;
-    prof_ms = 0.0;
-    prof_n = 0;
-  }
-
-  void setup(ikr_asm a) {
-    if (asm_ == a && w.n_rows == a->fes->nn && fp32 == a->fp32 && w.grid) return;
-    drop_graphs();
-    asm_ = a;
-    fp32 = a->fp32;
-    const int nr = a->fes->nn;
-    const size_t n = 3 * (size_t)nr;
-    w = ikr::PcgWork{};
-    w.n_rows = nr;
-    w.fp32 = fp32;
-    w.grid = 4 * num_sms();
-    if (fp32) {
-      fx.alloc(n), fr.alloc(n), fz.alloc(n), fp.alloc(n), fp1.alloc(n), fq.alloc(n), fmv.alloc(9 * (size_t)nr);
-      w.x = fx.p, w.r = fr.p, w.z = fz.p, w.p0 = fp.p, w.p1 = fp1.p, w.q = fq.p, w.minv = fmv.p;
-    } else {
-      dx.alloc(n), dr.alloc(n), dz.alloc(n), dp.alloc(n), dp1.alloc(n), dq.alloc(n), dmv.alloc(9 * (size_t)nr);
-      w.x = dx.p, w.r = dr.p, w.z = dz.p, w.p0 = dp.p, w.p1 = dp1.p, w.q = dq.p, w.minv = dmv.p;
-    }
-    pa.alloc(w.grid);
-    pb.alloc(2 * (size_t)w.grid);
-    scal.alloc(ikr::kNScal);
-    w.part_a = pa.p;
-    w.part_b = pb.p;
-    w.scal = scal.p;
-    if (!scal_h) CK(cudaMallocHost(&scal_h, sizeof(double) * 2 * ikr::kNScal));
-    for (auto& e : ev)
-      if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    b64.alloc(n), x64.alloc(n), r64.alloc(n), c64.alloc(n);
-  }
-
-  void build_chunk(cudaStream_t s) {
-    const int ng = profile ? 2 : 1;
-    const ikr::Bsr A = asm_->bsr();
-    for (int gi = 0; gi < ng; ++gi) {
-      if (chunk[gi]) continue;
-      if (profile && pev[gi].empty()) {
-        pev[gi].resize(2 * chunk_len);
-        for (auto& e : pev[gi]) CK(cudaEventCreate(&e));
-      }
-      cudaGraph_t g = nullptr;
-      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < chunk_len; ++k) {
-        // cudaEventRecordExternal turns the records into event-record nodes of the graph (a plain record
-        // during capture would only become an internal dependency)
-        if (profile) CK(cudaEventRecordWithFlags(pev[gi][2 * k], s, cudaEventRecordExternal));
-        ikr::launch_pcg_spmv(A, w, k & 1, s);
-        if (profile) CK(cudaEventRecordWithFlags(pev[gi][2 * k + 1], s, cudaEventRecordExternal));
-        ikr::launch_pcg_update(A, w, k & 1, s);
-      }
-      CK(cudaStreamEndCapture(s, &g));
-      CK(cudaGraphInstantiate(&chunk[gi], g, 0));
-      cudaGraphDestroy(g);
-    }
-  }
-  // SpMV device time of the first `working` iterations of a finished profiled chunk
-  void read_profile(int gi, int working) {
-    for (int k = 0; k < working && k < chunk_len; ++k) {
-      float ms = 0.f;
-      CK(cudaEventElapsedTime(&ms, pev[gi][2 * k], pev[gi][2 * k + 1]));
-      prof_ms += ms;
-      ++prof_n;
-    }
-  }
-
-  void factorize(ikr_asm a) {
-    setup(a);
-    ikr::launch_block_jacobi(a->bsr(), fp32, w.minv, tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT, a->fes->stream);
-    count(1);
-    factorized = true;
-  }
-
-  // x = K^{-1} b on the device (FP64 in / out); returns CG iterations
-  int solve_device(ikr_asm a, const double* b, double* x, double rt, int maxit) {
-    if (!factorized || asm_ != a) fail(IKR_ERR_INVALID_STATE, "linear solver not factorized for this assembler");
-    cudaStream_t s = a->fes->stream;
-    const ikr::Bsr A = a->bsr();
-    build_chunk(s);
-    ikr::launch_pcg_init(A, w, b, rt, maxit, s);
-    count(2);
-    // Chunks of CG iterations are launched one ahead of the host check: once the device flags
-    // convergence the chunk in flight returns at entry, so polling never stalls the GPU.
-    constexpr int NS = ikr::kNScal;
-    auto graph = [&](int k) { return chunk[profile ? (k & 1) : 0]; };
-    auto iters_in = [&](int slot) {
-      return (int)std::max(scal_h[NS * slot + ikr::kIters], scal_h[NS * slot + ikr::kIters + 1]);
-    };
-    int k = 0, prev_iters = 0;
-    CK(cudaGraphLaunch(graph(0), s));
-    count(2 * chunk_len);
-    CK(cudaMemcpyAsync(scal_h, scal.p, sizeof(double) * NS, cudaMemcpyDeviceToHost, s));
-    CK(cudaEventRecord(ev[0], s));
-    for (;;) {
-      ++k;
-      CK(cudaGraphLaunch(graph(k), s));
-      count(2 * chunk_len);
-      CK(cudaMemcpyAsync(scal_h + NS * (k & 1), scal.p, sizeof(double) * NS, cudaMemcpyDeviceToHost, s));
-      CK(cudaEventRecord(ev[k & 1], s));
-      CK(cudaEventSynchronize(ev[(k - 1) & 1]));
-      if (profile) {
-        const int it = iters_in((k - 1) & 1);
-        read_profile((k - 1) & 1, it - prev_iters);
-        prev_iters = it;
-      }
-      if (scal_h[NS * ((k - 1) & 1) + ikr::kDone] != 0.0) break;
-    }
-    CK(cudaStreamSynchronize(s));
-    const double* sc = scal_h + NS * (k & 1);  // state after the last (no-op) chunk
-    const double done = sc[ikr::kDone];
-    last_iters = (int)std::max(sc[ikr::kIters], sc[ikr::kIters + 1]);
-    last_rel = sc[ikr::kBB] > 0 ? std::sqrt(sc[ikr::kRR] / sc[ikr::kBB]) : 0.0;
-    ikr::launch_pcg_result(w, x, 1.0, s);
-    count(1);
-    if (done == 3.0) fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp <= 0) after %d iterations", last_iters);
-    return last_iters;
-  }
-
-  // x = K^{-1} b with optional FP64 iterative refinement around the (possibly FP32) CG
-  int64_t solve(ikr_asm a, const double* b, double* x, double rt, int maxit, int refinements) {
-    int64_t its = solve_device(a, b, x, rt, maxit);
-    if (refinements <= 0) return its;
-    cudaStream_t s = a->fes->stream;
-    const int64_t n = 3LL * a->fes->nn;
-    for (int k = 0; k < refinements; ++k) {
-      ikr::launch_residual64(a->bsr(), fp32, x, b, r64.p, s);  // r = b - K x in FP64 accumulation
-      its += solve_device(a, r64.p, c64.p, rt, maxit);
-      ikr::launch_axpy64(x, c64.p, 1.0, n, s);
-      count(2);
-    }
-    return its;
-  }
-};
-
-struct Observer {
-  ikr_nr_observer cb;
-  void* user;
-};
-struct ControlObserver {
-  ikr_control_observer cb;
-  void* user;
-};
-
-struct ikr_nr_s {
-  ikr_asm asm_ = nullptr;
-  ikr_ls ls = nullptr;
-  ikr_nr_settings st{};
-  std::vector<Observer> obs;
-  bool fe_state = false;
-  DBuf<double> corr, rhs;
-  DBuf<double> nrm_part, nrm_out;
-};
-
-struct ikr_lc_s {
-  ikr_nr nr = nullptr;
-  int steps = 1;
-  double t0 = 0, t1 = 1;
-  std::vector<ControlObserver> obs;
-};
-
-// ------------------------------------------------------------------------------------------------------------
 namespace {
 
 std::atomic<uint64_t> g_req_ids{1};
@@ -540,10 +46,25 @@ void greedy_colouring(ikr_fes f) {
   f->colour_elems.upload(list.data(), list.size(), f->stream);
 }
 
+}  // namespace
+
+namespace ikr_host {
+
 double device_norm(ikr_fes f, const double* x, int64_t n, DBuf<double>& part, DBuf<double>& out) {
   part.alloc(1024);
   out.alloc(1);
   ikr::launch_norm2(x, n, part.p, out.p, f->stream);
+  count(2);
+  double h = 0;
+  CK(cudaMemcpyAsync(&h, out.p, sizeof(double), cudaMemcpyDeviceToHost, f->stream));
+  CK(cudaStreamSynchronize(f->stream));
+  return h;
+}
+
+double device_dot(ikr_fes f, const double* x, const double* y, int64_t n, DBuf<double>& part, DBuf<double>& out) {
+  part.alloc(1024);
+  out.alloc(1);
+  ikr::launch_dot(x, y, n, part.p, out.p, f->stream);
   count(2);
   double h = 0;
   CK(cudaMemcpyAsync(&h, out.p, sizeof(double), cudaMemcpyDeviceToHost, f->stream));
@@ -580,7 +101,7 @@ void assemble_matrix(ikr_asm a, ikr_req r, int dbc) {
   ikr_fes f = a->fes;
   if (!a->nb) a->build_pattern();
   const uint8_t* nf = (dbc == IKR_DBC_RAW) ? nullptr : a->node_fixed.p;
-  ikr::launch_bsr_reset(a->values(), a->fp32, a->nb, a->diag.p, nf, f->nn, f->stream);
+  ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
   count(nf ? 1 : 0);
   ikr::ElemArgs args = f->args();
   args.u = r->u.p;
@@ -619,7 +140,7 @@ void update_state(ikr_fes f, ikr_req r, const double* corr_dev) {
   f->alpha_version++;
 }
 
-}  // namespace
+}  // namespace ikr_host
 
 // ------------------------------------------------------------------------------------------------------------
 extern "C" {
@@ -695,6 +216,59 @@ int ikr_fes_add_neumann(ikr_fes fes, int32_t n_faces, const int32_t* face_elem, 
   });
 }
 
+int ikr_fes_clear_neumann(ikr_fes fes) {
+  return guarded([&] {
+    need(fes, IKR_ERR_ARG, "null argument");
+    fes->faces.clear();
+    fes->trac_idx.release();
+    fes->trac.release();
+    fes->trac_dirty = false;
+  });
+}
+int ikr_fes_set_element_materials(ikr_fes fes, const double* lambda, const double* mu) {
+  return guarded([&] {
+    need(fes && lambda && mu, IKR_ERR_ARG, "null argument");
+    fes->lam_e.upload(lambda, fes->ne, fes->stream);
+    fes->mu_e.upload(mu, fes->ne, fes->stream);
+    CK(cudaStreamSynchronize(fes->stream));
+  });
+}
+int ikr_fes_set_instances(ikr_fes fes, int32_t n_inst, const int32_t* node_off) {
+  return guarded([&] {
+    need(fes && n_inst > 0 && node_off, IKR_ERR_ARG, "invalid instance partition");
+    need(node_off[0] == 0 && node_off[n_inst] == fes->nn, IKR_ERR_ARG, "instance offsets must cover all nodes");
+    std::vector<int32_t> inst_of(fes->nn);
+    for (int i = 0; i < n_inst; ++i) {
+      need(node_off[i + 1] > node_off[i], IKR_ERR_ARG, "empty instance");
+      for (int k = node_off[i]; k < node_off[i + 1]; ++k) inst_of[k] = i;
+    }
+    for (int e = 0; e < fes->ne; ++e)  // instances must be independent: no element spans two of them
+      for (int v = 1; v < 8; ++v)
+        need(inst_of[fes->conn_h[8 * e + v]] == inst_of[fes->conn_h[8 * e]], IKR_ERR_ARG,
+             "an element connects two instances");
+    std::vector<int32_t> order(n_inst);
+    for (int i = 0; i < n_inst; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+      return node_off[a + 1] - node_off[a] > node_off[b + 1] - node_off[b];  // largest first
+    });
+    fes->n_inst = n_inst;
+    fes->inst_off_h.assign(node_off, node_off + n_inst + 1);
+    fes->inst_off.upload(node_off, n_inst + 1, fes->stream);
+    fes->inst_order.upload(order.data(), order.size(), fes->stream);
+    CK(cudaStreamSynchronize(fes->stream));
+  });
+}
+int ikr_newton_instance_info(ikr_nr nr, int32_t* iterations, double* residual_norms, int32_t* converged) {
+  return guarded([&] {
+    need(nr, IKR_ERR_ARG, "null argument");
+    const size_t ni = nr->inst_iters.size();
+    for (size_t i = 0; i < ni; ++i) {
+      if (iterations) iterations[i] = nr->inst_iters[i];
+      if (residual_norms) residual_norms[i] = nr->inst_res[i];
+      if (converged) converged[i] = nr->inst_conv[i];
+    }
+  });
+}
 int ikr_fes_destroy(ikr_fes fes) {
   return guarded([&] {
     if (fes) cudaStreamSynchronize(fes->stream);
@@ -954,7 +528,7 @@ static void export_csc(ikr_asm a, int dbc, int64_t* cp, int32_t* ri, double* v, 
   const int nn = a->fes->nn;
   std::vector<double> val;
   if (v) {
-    val.resize(9 * (size_t)a->nb);
+    val.resize(9 * (size_t)a->npad);
     if (a->fp32) {
       std::vector<float> f(val.size());
       a->val32.download(f.data(), f.size(), a->fes->stream);
@@ -972,7 +546,7 @@ static void export_csc(ikr_asm a, int dbc, int64_t* cp, int32_t* ri, double* v, 
   auto block_of = [&](int I, int J) -> int64_t {
     auto b = cl.begin() + rp[I], e = cl.begin() + rp[I + 1];
     auto it = std::lower_bound(b, e, J);
-    return it - cl.begin();
+    return a->block_id(I, it - cl.begin());
   };
   int64_t nnz = 0;
   int col_out = 0;
@@ -987,7 +561,7 @@ static void export_csc(ikr_asm a, int dbc, int64_t* cp, int32_t* ri, double* v, 
           const int gr = 3 * I + aa;
           if (reduced && a->fixed_h[gr]) continue;
           if (ri) ri[nnz] = reduced ? gr - a->cb_h[gr] : gr;
-          if (v) v[nnz] = val[9 * block_of(I, J) + 3 * aa + b];
+          if (v) v[nnz] = val[ikr::block_entry(block_of(I, J), 3 * aa + b)];
           ++nnz;
         }
       }
@@ -1031,8 +605,9 @@ int ikr_assembler_block_pattern(ikr_asm a, int32_t* n_rows, int64_t* n_blocks, i
 int ikr_linear_solver_create(ikr_ls* out, int32_t tag) {
   return guarded([&] {
     need(out, IKR_ERR_ARG, "null argument");
-    need(tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI || tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT, IKR_ERR_NOT_IMPLEMENTED,
-         "this SolverTypeTag has no device implementation");
+    need(tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI || tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT ||
+             tag == IKR_SOLVER_GPU_PCG_BATCHED,
+         IKR_ERR_NOT_IMPLEMENTED, "this SolverTypeTag has no device implementation");
     auto l = std::make_unique<ikr_ls_s>();
     l->tag = tag;
     *out = l.release();
@@ -1093,6 +668,27 @@ int ikr_linear_solver_profile_read(ikr_ls ls, double* ms, int64_t* n) {
     if (n) *n = ls->prof_n;
   });
 }
+int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_len) {
+  return guarded([&] {
+    need(ls && chunk_len >= 1 && chunk_len <= 256, IKR_ERR_ARG, "invalid launch shape");
+    ls->set_launch(use_graphs != 0, chunk_len);
+  });
+}
+int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t kind, double keep) {
+  return guarded([&] {
+    need(ls && kind >= -1 && kind <= ikr::spmv_staged_variants() && (keep == -1.0 || (keep >= 0.0 && keep < 1.0)),
+         IKR_ERR_ARG, "invalid SpMV kernel choice");
+    ls->set_kernel(kind, keep);
+  });
+}
+int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* kind, double* keep, double* us) {
+  return guarded([&] {
+    need(ls, IKR_ERR_ARG, "null argument");
+    if (kind) *kind = ls->w.spmv_kind;
+    if (keep) *keep = ls->keep_frac;
+    if (us) *us = ls->tuned_us;
+  });
+}
 // Allocation-free variant of the solve: the CG work set is carved out of the library's fixed device array
 // (noalloc.cu) instead of cudaMalloc'ed buffers; no graphs, events or pinned buffers either, the host polls
 // the device scalars with a plain copy into a static host array after every 32 iterations.
@@ -1126,8 +722,8 @@ int ikr_linear_solver_solve_noalloc(ikr_asm a, const double* b, double* x, doubl
     ikr::launch_pcg_result(w, x, 1.0, s);
     count(1);
     CK(cudaStreamSynchronize(s));
-    if (iterations) *iterations = (int32_t)std::max(sc[ikr::kIters], sc[ikr::kIters + 1]);
-    if (sc[ikr::kDone] == 3.0) fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp <= 0)");
+    if (iterations) *iterations = (int32_t)sc[ikr::kIters];
+    if (sc[ikr::kDone] == 3.0) fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp zero or not finite)");
     if (sc[ikr::kDone] == 2.0) fail(IKR_ERR_NOT_CONVERGED, "CG reached max_iter = %d", max_iter);
   });
 }
@@ -1181,8 +777,104 @@ int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on) {
   });
 }
 
-static void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info) {
+}  // extern "C"
+
+namespace ikr_host {
+// Newton-Raphson over independent instances: every instance runs its own Newton iteration and relative
+// convergence test; one assembly and one batched CG launch (CTA per instance) serve all still-active instances.
+static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
+  ikr_asm a = nr->asm_;
+  ikr_fes f = a->fes;
+  cudaStream_t s = f->stream;
+  const ikr_nr_settings& st = nr->st;
+  const int ni = f->n_inst;
+  const int64_t n = a->n;
+  nr->corr.alloc(n);
+  nr->rhs.alloc(n);
+  nr->inst_norm.alloc(ni);
+  nr->inst_rtol.alloc(ni);
+  nr->inst_active.alloc(ni);
+  nr->inst_cg_iters.alloc(ni);
+  nr->inst_cg_res.alloc(ni);
+  std::vector<double> rn(ni), r0(ni), rprev(ni), thr(ni), eta(ni);
+  std::vector<uint8_t> act(ni);
+  std::vector<int32_t> cgit(ni);
+  nr->inst_iters.assign(ni, 0);
+  nr->inst_conv.assign(ni, 0);
+  auto norms = [&]() {
+    ikr::launch_instance_norms(a->R.p, ni, f->inst_off.p, nr->inst_norm.p, s);
+    count(1);
+    nr->inst_norm.download(rn.data(), ni, s);
+    CK(cudaStreamSynchronize(s));
+  };
+  assemble_vector(a, r, IKR_DBC_FULL);
+  norms();
+  r0 = rn;
+  for (int i = 0; i < ni; ++i) {
+    thr[i] = st.tol_mode == 1 ? st.tol * r0[i] : st.tol;
+    act[i] = rn[i] > thr[i];
+  }
+  if (!a->nb) a->build_pattern();
+  nr->ls->setup(a);
+  int iter = 0;
+  int64_t lin = 0;
+  auto any = [&] { return std::any_of(act.begin(), act.end(), [](uint8_t v) { return v != 0; }); };
+  while ((any() && iter < st.max_iter) || iter < st.min_iter) {
+    assemble_matrix(a, r, IKR_DBC_FULL);
+    nr->ls->factorize(a);
+    for (int i = 0; i < ni; ++i) {
+      double e = st.linear_rtol;
+      if (st.forcing == 1 && nr->inst_iters[i] > 0) {
+        e = std::min(st.linear_rtol, 0.9 * (rn[i] / rprev[i]) * (rn[i] / rprev[i]));
+        e = std::max(e, 0.5 * thr[i] / std::max(rn[i], 1e-300));
+        e = std::min(std::max(e, st.linear_rtol_min), st.linear_rtol);
+      }
+      eta[i] = e;
+    }
+    nr->inst_rtol.upload(eta.data(), ni, s);
+    nr->inst_active.upload(act.data(), ni, s);
+    ikr::launch_scale64(nr->rhs.p, a->R.p, -1.0, n, s);
+    ikr::PcgWork& w = nr->ls->w;
+    ikr::launch_batched_pcg(a->bsr(), a->fp32, w.minv, nr->rhs.p, nr->corr.p, ni, f->inst_off.p, f->inst_order.p,
+                            nr->inst_active.p, w.x, w.r, w.z, w.p0, w.q, nr->inst_rtol.p, st.linear_max_iter,
+                            nr->inst_cg_iters.p, nr->inst_cg_res.p, s);
+    count(2);
+    nr->inst_cg_iters.download(cgit.data(), ni, s);
+    ikr::launch_axpy64(r->u.p, nr->corr.p, 1.0, n, s);
+    count(1);
+    r->version++;
+    for (int i = 0; i < ni; ++i) rprev[i] = rn[i];
+    assemble_vector(a, r, IKR_DBC_FULL);
+    norms();
+    for (int i = 0; i < ni; ++i) {
+      lin += cgit[i];
+      if (act[i]) nr->inst_iters[i]++;
+      act[i] = rn[i] > thr[i] && std::isfinite(rn[i]);
+    }
+    ++iter;
+  }
+  bool ok = true;
+  for (int i = 0; i < ni; ++i) {
+    nr->inst_conv[i] = rn[i] <= thr[i];
+    ok = ok && nr->inst_conv[i];
+  }
+  nr->inst_res = rn;
+  ikr_nr_info inf{};
+  inf.success = ok ? 1 : 0;
+  inf.residual_norm = *std::max_element(rn.begin(), rn.end());
+  inf.correction_norm = 0.0;
+  inf.iterations = iter;
+  inf.linear_iterations = lin;
+  if (info) *info = inf;
+}
+
+void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double ref_norm) {
   (void)step_size;
+  if (nr->asm_->fes->n_inst > 0 && nr->ls->tag == IKR_SOLVER_GPU_PCG_BATCHED) {
+    need(nr->asm_->fes->na == 0, IKR_ERR_NOT_IMPLEMENTED, "the batched solve supports displacement-based elements");
+    nr_solve_batched(nr, r, info);
+    return;
+  }
   ikr_asm a = nr->asm_;
   ikr_fes f = a->fes;
   need(r->fes == f, IKR_ERR_ARG, "requirement of another element set");
@@ -1207,7 +899,7 @@ static void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info) 
   assemble_vector(a, r, IKR_DBC_FULL);
   double rnorm = device_norm(f, a->R.p, n, nr->nrm_part, nr->nrm_out);
   inf.residual_norm = rnorm;
-  const double thr = st.tol_mode == 1 ? st.tol * rnorm : st.tol;
+  const double thr = st.tol_mode == 1 ? st.tol * (ref_norm > 0.0 ? ref_norm : rnorm) : st.tol;
   bool k_valid = false;
   if (!a->nb) a->build_pattern();
   nr->ls->setup(a);
@@ -1258,6 +950,9 @@ static void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info) 
   if (inf.success) notify(IKR_NLS_FINISHED_SUCESSFULLY);
   if (info) *info = inf;
 }
+}  // namespace ikr_host
+
+extern "C" {
 
 int ikr_newton_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info) {
   return guarded([&] {
@@ -1315,11 +1010,14 @@ int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_in
     if (ni.success) {
       cs.step_size = step;
       bool ok = true;
+      predictor_begin(lc, r);
       for (int ls = 0; ls < lc->steps; ++ls) {
         cs.load_step = ls;
         notify(IKR_STEP_STARTED);
         r->lambda += step;  // LoadControl::predictor (loadcontrol.inl:54-57)
-        nr_solve(lc->nr, r, step, &ni);
+        const double ref = predictor_apply(lc, r, ls);  // optional displacement prediction, FP64-gated
+        nr_solve(lc->nr, r, step, &ni, ref);
+        predictor_end_step(lc, r, ls);
         record(ni);
         if (!ni.success) {
           ok = false;

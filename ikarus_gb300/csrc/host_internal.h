@@ -1,0 +1,688 @@
+// Internals of the host layer shared by host.cpp (finite elements, assembler, solver, Newton, LoadControl)
+// and predictor.cpp (learned Newton predictor).  One CUDA stream per finite-element set; every object built on
+// that set (requirements, assembler, solver, Newton, LoadControl, predictor) issues its work on it.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ikarus_gb300.h"
+#include "kernels.h"
+
+namespace ikr_host {
+
+extern thread_local std::string g_last_error;
+extern std::atomic<int64_t> g_launches;
+
+struct IkrError : std::runtime_error {
+  int code;
+  IkrError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] inline void fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  throw IkrError(code, buf);
+}
+
+inline void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) fail(IKR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+#define CK(x) cuda_check((x), #x)
+
+inline void count(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+template <typename F>
+int guarded(F&& f) {
+  try {
+    f();
+    return IKR_OK;
+  } catch (const IkrError& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return IKR_ERR_ARG;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return IKR_ERR_ARG;
+  }
+}
+
+// device buffer
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count == n && p) return;
+    release();
+    if (count == 0) return;
+    CK(cudaMalloc(&p, count * sizeof(T)));
+    n = count;
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) CK(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void download(T* h, size_t count, cudaStream_t s) const {
+    if (count) CK(cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
+};
+
+inline int num_sms() {
+  static int sms = [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 152;
+    return v > 0 ? v : 152;
+  }();
+  return sms;
+}
+
+}  // namespace ikr_host
+using namespace ikr_host;
+
+// ------------------------------------------------------------------------------------------------------------
+struct ikr_fes_s {
+  int nn = 0, ne = 0, na = 0, eas = 0;
+  double lam = 0, mu = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<int32_t> conn_h;  // row-major n_elems x 8
+  DBuf<double> X;
+  DBuf<int32_t> conn;  // corner-major
+  DBuf<double> alpha;  // n_alpha x n_elems
+  DBuf<double> eas_geo;
+  DBuf<double> eas_y, eas_Y;
+  uint64_t eas_cache_key = 0;  // (req id, solution version, alpha version) hash of the cached D^{-1}R~, D^{-1}L
+  uint64_t alpha_version = 1;
+  // colours
+  std::vector<int32_t> colour_ptr;
+  DBuf<int32_t> colour_elems;
+  // Neumann faces
+  std::vector<std::vector<std::pair<int, std::array<double, 3>>>> faces;
+  DBuf<int32_t> trac_idx;
+  DBuf<double> trac;
+  bool trac_dirty = false;
+  DBuf<int> status;
+  DBuf<double> scratch_out;  // element-level outputs
+  DBuf<double> lam_e, mu_e;  // per-element Lame parameters (empty: lam / mu everywhere)
+  // independent instances: disjoint contiguous node ranges [inst_off[i], inst_off[i+1])
+  int n_inst = 0;
+  std::vector<int32_t> inst_off_h;
+  DBuf<int32_t> inst_off, inst_order;
+
+  ~ikr_fes_s() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  ikr::ElemArgs args() const {
+    ikr::ElemArgs a;
+    a.n_nodes = nn;
+    a.n_elems = ne;
+    a.X = X.p;
+    a.conn = conn.p;
+    a.lam = lam;
+    a.mu = mu;
+    a.eas_kind = na > 0 ? eas : 0;
+    a.n_alpha = na;
+    a.alpha = alpha.p;
+    a.eas_geo = eas_geo.p;
+    a.eas_y = eas_y.p;
+    a.eas_Y = eas_Y.p;
+    a.trac_idx = trac_idx.n ? trac_idx.p : nullptr;
+    a.trac = trac.p;
+    a.status = status.p;
+    a.lam_e = lam_e.n ? lam_e.p : nullptr;
+    a.mu_e = mu_e.n ? mu_e.p : nullptr;
+    return a;
+  }
+
+  void refresh_tractions() {
+    if (!trac_dirty) return;
+    std::vector<int32_t> idx(ne, -1), slot_elem, face_ptr{0}, face_local;
+    std::vector<double> t;
+    for (int e = 0; e < ne; ++e) {
+      if (faces[e].empty()) continue;
+      idx[e] = (int32_t)slot_elem.size();
+      slot_elem.push_back(e);
+      for (auto& f : faces[e]) {
+        face_local.push_back(f.first);
+        t.insert(t.end(), f.second.begin(), f.second.end());
+      }
+      face_ptr.push_back((int32_t)face_local.size());
+    }
+    trac_idx.upload(idx.data(), idx.size(), stream);
+    DBuf<int32_t> d_se, d_fp, d_fl;
+    DBuf<double> d_t;
+    d_se.upload(slot_elem.data(), slot_elem.size(), stream);
+    d_fp.upload(face_ptr.data(), face_ptr.size(), stream);
+    d_fl.upload(face_local.data(), face_local.size(), stream);
+    d_t.upload(t.data(), t.size(), stream);
+    trac.alloc(std::max<size_t>(1, 24 * slot_elem.size()));
+    ikr::launch_traction_loads(X.p, conn.p, ne, (int)slot_elem.size(), d_se.p, d_fp.p, d_fl.p, d_t.p, trac.p, stream);
+    count(1);
+    CK(cudaStreamSynchronize(stream));
+    trac_dirty = false;
+  }
+
+  void check_status() {
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    if (h) {
+      CK(cudaMemsetAsync(status.p, 0, sizeof(int), stream));
+      if (h & ikr::kStatusNonPositiveDetC)
+        fail(IKR_ERR_NONPOSITIVE_DETC, "Determinant of right Cauchy Green tensor C must be greater than zero");
+      if (h & ikr::kStatusSingularD) fail(IKR_ERR_SINGULAR, "EAS matrix D is singular");
+      if (h & ikr::kStatusPatternOverflow) fail(IKR_ERR_ARG, "a node couples with more than 128 nodes");
+      fail(IKR_ERR_ARG, "device status %d", h);
+    }
+  }
+
+  void launch_elements(const ikr::ElemArgs& a, int mode, bool fp32, const int32_t* list, int n, int base) {
+    if (na > 0) ikr::launch_eas_element(a, mode, fp32, list, n, base, stream);
+    else ikr::launch_disp_element(a, mode, fp32, list, n, base, stream);
+    count(1);
+  }
+  // one launch per colour class: deterministic scatter without atomics
+  void launch_coloured(const ikr::ElemArgs& a, int mode, bool fp32) {
+    for (size_t c = 0; c + 1 < colour_ptr.size(); ++c) {
+      const int n = colour_ptr[c + 1] - colour_ptr[c];
+      launch_elements(a, mode, fp32, colour_elems.p + colour_ptr[c], n, 0);
+    }
+  }
+};
+
+struct ikr_req_s {
+  ikr_fes fes = nullptr;
+  DBuf<double> u;
+  double lambda = 0.0;
+  uint64_t id = 0;
+  uint64_t version = 1;
+};
+
+struct ikr_asm_s {
+  ikr_fes fes = nullptr;
+  int n = 0, nred = 0;
+  bool fp32 = false;
+  std::vector<uint8_t> fixed_h;
+  std::vector<int32_t> cb_h;
+  DBuf<uint8_t> node_fixed;
+  // pattern
+  int64_t nb = 0, npad = 0;
+  int nslices = 0;
+  DBuf<int32_t> row_ptr, col, diag, slot, slice_off, col_sell;
+  std::vector<int32_t> row_ptr_h, col_h, slice_off_h;
+  DBuf<double> val64;
+  DBuf<float> val32;
+  int matrix_dbc = -1;  // option of the last assembled matrix
+  // vector
+  DBuf<double> R;
+  int vector_dbc = -1;
+  DBuf<int32_t> pl_dof;
+  DBuf<double> pl_val;
+  std::map<int32_t, double> pl_h;
+  DBuf<double> norm_part, norm_out;
+  ikr_req bound_req = nullptr;
+  int bound_dbc = IKR_DBC_FULL;
+
+  ikr::Bsr bsr() const {
+    ikr::Bsr b;
+    b.n_rows = fes->nn;
+    b.n_blocks = nb;
+    b.row_ptr = row_ptr.p;
+    b.col = col.p;
+    b.n_slices = nslices;
+    b.n_padded = npad;
+    b.slice_off = slice_off.p;
+    b.col_sell = col_sell.p;
+    b.diag = diag.p;
+    b.val = fp32 ? (const void*)val32.p : (const void*)val64.p;
+    return b;
+  }
+  void* values() { return fp32 ? (void*)val32.p : (void*)val64.p; }
+
+  void build_pattern() {
+    ikr_fes f = fes;
+    cudaStream_t s = f->stream;
+    DBuf<int32_t> cnt, ne_ptr, cursor, ne_elems, rcnt;
+    cnt.alloc(f->nn);
+    ne_ptr.alloc(f->nn + 1);
+    cursor.alloc(f->nn);
+    ne_elems.alloc(8LL * f->ne);
+    ikr::launch_node_elem_count(f->conn.p, f->ne, f->nn, cnt.p, s);
+    ikr::launch_exclusive_scan(cnt.p, ne_ptr.p, f->nn, s);
+    ikr::launch_node_elem_fill(f->conn.p, f->ne, ne_ptr.p, cursor.p, ne_elems.p, f->nn, s);
+    rcnt.alloc(f->nn);
+    ikr::launch_row_build(f->conn.p, f->ne, f->nn, ne_ptr.p, ne_elems.p, nullptr, rcnt.p, false, f->status.p, s);
+    row_ptr.alloc(f->nn + 1);
+    ikr::launch_exclusive_scan(rcnt.p, row_ptr.p, f->nn, s);
+    count(7);
+    int32_t total = 0;
+    CK(cudaMemcpyAsync(&total, row_ptr.p + f->nn, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    f->check_status();
+    nb = total;
+    col.alloc(nb);
+    ikr::launch_row_build(f->conn.p, f->ne, f->nn, ne_ptr.p, ne_elems.p, row_ptr.p, col.p, true, f->status.p, s);
+    // sliced-ELL storage: widest row of every slice of 32 rows, scanned into block-column offsets
+    nslices = (f->nn + 31) / 32;
+    DBuf<int32_t> slen;
+    slen.alloc(nslices);
+    slice_off.alloc(nslices + 1);
+    ikr::launch_slice_lengths(row_ptr.p, f->nn, slen.p, s);
+    ikr::launch_exclusive_scan(slen.p, slice_off.p, nslices, s);
+    int32_t width = 0;
+    CK(cudaMemcpyAsync(&width, slice_off.p + nslices, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    npad = 32LL * width;
+    col_sell.alloc(npad);
+    ikr::launch_sell_fill(row_ptr.p, col.p, slice_off.p, f->nn, col_sell.p, s);
+    slot.alloc(64LL * f->ne);
+    diag.alloc(f->nn);
+    ikr::launch_slot_map(f->conn.p, f->ne, row_ptr.p, col.p, slice_off.p, slot.p, diag.p, f->nn, s);
+    count(6);
+    row_ptr_h.resize(f->nn + 1);
+    col_h.resize(nb);
+    slice_off_h.resize(nslices + 1);
+    row_ptr.download(row_ptr_h.data(), row_ptr_h.size(), s);
+    col.download(col_h.data(), col_h.size(), s);
+    slice_off.download(slice_off_h.data(), slice_off_h.size(), s);
+    CK(cudaStreamSynchronize(s));
+    f->check_status();
+    if (fp32) val32.alloc(9 * npad);
+    else val64.alloc(9 * npad);
+  }
+  // block id of CSR entry k (the (k - row_ptr[r])-th block of row r)
+  int64_t block_id(int r, int64_t k) const { return (slice_off_h[r >> 5] + (k - row_ptr_h[r])) * 32LL + (r & 31); }
+};
+
+struct ikr_ls_s {
+  int tag = IKR_SOLVER_GPU_PCG_BLOCK_JACOBI;
+  double rtol = 1e-10;
+  int max_iter = 100000;
+  ikr_asm asm_ = nullptr;
+  bool fp32 = false;
+  ikr::PcgWork w;
+  DBuf<double> dx, dp, dq, dmv, pa, pb, scal;
+  DBuf<float> fx, fp, fq, fmv;
+  DBuf<double> dz, dr, dp1;
+  DBuf<float> fz, fr, fp1;
+  double* scal_h = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaEvent_t tev[2] = {nullptr, nullptr};  // timing events of the SpMV tuner
+  // SpMV kernel choice (kernels.h PcgWork::spmv_kind / keep_g): requested kind and L2 keep fraction, -1 =
+  // chosen by the tuner at the first factorize on an assembler
+  int spmv_req = -1;
+  double keep_req = -1.0;
+  ikr_asm tuned_for = nullptr;
+  double keep_frac = 0.0;
+  double tuned_us = 0.0;
+  // CG iterations are launched as CUDA graphs of chunk_len iterations.  In profiling mode two graphs
+  // alternate, each with its own event-record nodes around every SpMV, so the SpMV device time of the
+  // chunk that just finished can be read while the next one runs.
+  // Without graphs (use_graphs = false) the same kernels are launched one by one, which profilers that
+  // cannot follow kernels inside graphs need.
+  cudaGraphExec_t chunk[2] = {nullptr, nullptr};
+  int chunk_len = 16;
+  bool use_graphs = true;
+  bool profile = false;
+  std::vector<cudaEvent_t> pev[2];
+  double prof_ms = 0.0;
+  int64_t prof_n = 0;
+  int last_iters = 0;
+  double last_rel = 0.0;
+  bool factorized = false;
+  DBuf<double> b64, x64, r64, c64;  // refinement work
+
+  ~ikr_ls_s() {
+    drop_graphs();
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    for (auto& e : tev)
+      if (e) cudaEventDestroy(e);
+    for (auto& v : pev)
+      for (auto e : v) cudaEventDestroy(e);
+    if (scal_h) cudaFreeHost(scal_h);
+  }
+
+  void drop_graphs() {
+    for (auto& g : chunk)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+  }
+
+  void set_profile(bool on) {
+    if (on != profile) drop_graphs();
+    profile = on;
+    prof_ms = 0.0;
+    prof_n = 0;
+  }
+
+  void setup(ikr_asm a) {
+    if (asm_ == a && w.n_rows == a->fes->nn && fp32 == a->fp32 && w.grid) return;
+    drop_graphs();
+    asm_ = a;
+    fp32 = a->fp32;
+    const int nr = a->fes->nn;
+    const size_t n = 4 * (size_t)nr;  // CG vectors are node-padded (x, y, z, 0)
+    w = ikr::PcgWork{};
+    w.n_rows = nr;
+    w.fp32 = fp32;
+    w.sms = num_sms();
+    w.grid = 4 * w.sms;
+    tuned_for = nullptr;
+    if (fp32) {
+      fx.alloc(n), fr.alloc(n), fz.alloc(n), fp.alloc(n), fp1.alloc(n), fq.alloc(n), fmv.alloc(9 * (size_t)nr);
+      w.x = fx.p, w.r = fr.p, w.z = fz.p, w.p0 = fp.p, w.p1 = fp1.p, w.q = fq.p, w.minv = fmv.p;
+    } else {
+      dx.alloc(n), dr.alloc(n), dz.alloc(n), dp.alloc(n), dp1.alloc(n), dq.alloc(n), dmv.alloc(9 * (size_t)nr);
+      w.x = dx.p, w.r = dr.p, w.z = dz.p, w.p0 = dp.p, w.p1 = dp1.p, w.q = dq.p, w.minv = dmv.p;
+    }
+    pa.alloc(w.grid);
+    pb.alloc(2 * (size_t)w.grid);
+    scal.alloc(ikr::kNScal);
+    w.part_a = pa.p;
+    w.part_b = pb.p;
+    w.scal = scal.p;
+    if (!scal_h) CK(cudaMallocHost(&scal_h, sizeof(double) * 2 * ikr::kNScal));
+    for (auto& e : ev)
+      if (!e) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& e : tev)
+      if (!e) CK(cudaEventCreate(&e));
+    b64.alloc(3 * (size_t)nr), x64.alloc(3 * (size_t)nr), r64.alloc(3 * (size_t)nr), c64.alloc(3 * (size_t)nr);
+  }
+
+  void set_launch(bool graphs, int len) {
+    if (graphs != use_graphs || len != chunk_len) drop_graphs();
+    if (len != chunk_len)
+      for (auto& v : pev) {
+        for (auto e : v) cudaEventDestroy(e);
+        v.clear();
+      }
+    use_graphs = graphs;
+    chunk_len = len;
+  }
+
+  // the kernels of one chunk; with profiling, cudaEventRecordExternal makes the records event-record nodes
+  // when captured (a plain record during capture would only become an internal dependency)
+  void issue_chunk(int gi, cudaStream_t s) {
+    const ikr::Bsr A = asm_->bsr();
+    const unsigned flags = use_graphs ? cudaEventRecordExternal : cudaEventRecordDefault;
+    for (int k = 0; k < chunk_len; ++k) {
+      if (profile) CK(cudaEventRecordWithFlags(pev[gi][2 * k], s, flags));
+      ikr::launch_pcg_spmv(A, w, k & 1, s);
+      if (profile) CK(cudaEventRecordWithFlags(pev[gi][2 * k + 1], s, flags));
+      ikr::launch_pcg_update(A, w, k & 1, s);
+    }
+  }
+
+  void build_chunk(cudaStream_t s) {
+    const int ng = profile ? 2 : 1;
+    for (int gi = 0; gi < ng; ++gi) {
+      if (profile && pev[gi].empty()) {
+        pev[gi].resize(2 * chunk_len);
+        for (auto& e : pev[gi]) CK(cudaEventCreate(&e));
+      }
+      if (!use_graphs || chunk[gi]) continue;
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      issue_chunk(gi, s);
+      CK(cudaStreamEndCapture(s, &g));
+      CK(cudaGraphInstantiate(&chunk[gi], g, 0));
+      cudaGraphDestroy(g);
+    }
+  }
+  void launch_chunk(int gi, cudaStream_t s) {
+    if (use_graphs) CK(cudaGraphLaunch(chunk[gi], s));
+    else issue_chunk(gi, s);
+    count(2 * chunk_len);
+  }
+  // SpMV device time of the first `working` iterations of a finished profiled chunk
+  void read_profile(int gi, int working) {
+    for (int k = 0; k < working && k < chunk_len; ++k) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, pev[gi][2 * k], pev[gi][2 * k + 1]));
+      prof_ms += ms;
+      ++prof_n;
+    }
+  }
+
+  void factorize(ikr_asm a) {
+    setup(a);
+    ikr::launch_block_jacobi(a->bsr(), fp32, w.minv, tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT, a->fes->stream);
+    count(1);
+    factorized = true;
+    if (tuned_for != a) tune(a);
+  }
+
+  void set_kernel(int kind, double keep) {
+    spmv_req = kind;
+    keep_req = keep;
+    tuned_for = nullptr;
+    drop_graphs();
+  }
+
+  // SpMV kernel and L2 keep fraction: the requested ones, or the fastest of timed CG iterations (right-hand
+  // side of ones, tolerance 0) on the assembled tangent.  The kinds are timed with nothing kept in L2, then
+  // the keep fractions in increasing order with the fastest kind.
+  void tune(ikr_asm a) {
+    drop_graphs();
+    const ikr::Bsr A = a->bsr();
+    const int64_t total_g = A.n_padded / 32;
+    auto apply = [&](int kind, double keep) {
+      w.spmv_kind = kind;
+      keep_frac = kind > 0 ? keep : 0.0;
+      w.keep_g = (int64_t)(keep_frac * (double)total_g);
+    };
+    tuned_for = a;
+    tuned_us = 0.0;
+    if (spmv_req >= 0 && keep_req >= 0.0) {
+      apply(spmv_req, keep_req);
+      return;
+    }
+    cudaStream_t s = a->fes->stream;
+    ikr::launch_fill64(b64.p, 1.0, 3LL * A.n_rows, s);
+    ikr::launch_pcg_init(A, w, b64.p, 0.0, 1 << 30, s);
+    count(3);
+    int parity = 0;
+    auto time_it = [&](int kind, double keep) {
+      apply(kind, keep);
+      constexpr int kWarm = 2, kTimed = 8;
+      for (int i = 0; i < kWarm; ++i, parity ^= 1) ikr::launch_pcg_spmv(A, w, parity, s), ikr::launch_pcg_update(A, w, parity, s);
+      CK(cudaEventRecord(tev[0], s));
+      for (int i = 0; i < kTimed; ++i, parity ^= 1) ikr::launch_pcg_spmv(A, w, parity, s), ikr::launch_pcg_update(A, w, parity, s);
+      CK(cudaEventRecord(tev[1], s));
+      CK(cudaEventSynchronize(tev[1]));
+      count(2 * (kWarm + kTimed));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+      return 1e3 * ms / kTimed;
+    };
+    int best_kind = spmv_req >= 0 ? spmv_req : 0;
+    double best = 1e300;
+    if (spmv_req < 0) {
+      for (int k = 0; k <= ikr::spmv_staged_variants(); ++k) {
+        const double us = time_it(k, 0.0);
+        if (us < best) best = us, best_kind = k;
+      }
+    }
+    double best_keep = keep_req >= 0.0 ? keep_req : 0.0;
+    if (keep_req < 0.0 && best_kind > 0) {
+      best = time_it(best_kind, 0.0);
+      for (double f : {0.3, 0.45, 0.6, 0.75}) {
+        const double us = time_it(best_kind, f);
+        if (us < best) best = us, best_keep = f;
+      }
+    } else if (best >= 1e300) {
+      best = time_it(best_kind, best_keep);
+    }
+    apply(best_kind, best_keep);
+    tuned_us = best;
+    double* sc = scal_h;
+    CK(cudaMemcpyAsync(sc, scal.p, sizeof(double) * ikr::kNScal, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (sc[ikr::kDone] == 6.0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the staged SpMV gave up while tuning");
+  }
+
+  // x = K^{-1} b on the device (FP64 in / out); returns CG iterations
+  int solve_device(ikr_asm a, const double* b, double* x, double rt, int maxit) {
+    if (!factorized || asm_ != a) fail(IKR_ERR_INVALID_STATE, "linear solver not factorized for this assembler");
+    cudaStream_t s = a->fes->stream;
+    const ikr::Bsr A = a->bsr();
+    build_chunk(s);
+    ikr::launch_pcg_init(A, w, b, rt, maxit, s);
+    count(2);
+    // Chunks of CG iterations are launched one ahead of the host check: once the device flags
+    // convergence the chunk in flight returns at entry, so polling never stalls the GPU.
+    constexpr int NS = ikr::kNScal;
+    auto gi = [&](int k) { return profile ? (k & 1) : 0; };
+    auto iters_in = [&](int slot) { return (int)scal_h[NS * slot + ikr::kIters]; };
+    int k = 0, prev_iters = 0;
+    launch_chunk(gi(0), s);
+    CK(cudaMemcpyAsync(scal_h, scal.p, sizeof(double) * NS, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(ev[0], s));
+    for (;;) {
+      ++k;
+      launch_chunk(gi(k), s);
+      CK(cudaMemcpyAsync(scal_h + NS * (k & 1), scal.p, sizeof(double) * NS, cudaMemcpyDeviceToHost, s));
+      CK(cudaEventRecord(ev[k & 1], s));
+      CK(cudaEventSynchronize(ev[(k - 1) & 1]));
+      if (profile) {
+        const int it = iters_in((k - 1) & 1);
+        read_profile((k - 1) & 1, it - prev_iters);
+        prev_iters = it;
+      }
+      if (scal_h[NS * ((k - 1) & 1) + ikr::kDone] != 0.0) break;
+    }
+    CK(cudaStreamSynchronize(s));
+    const double* sc = scal_h + NS * (k & 1);  // state after the last (no-op) chunk
+    const double done = sc[ikr::kDone];
+    last_iters = (int)sc[ikr::kIters];
+    last_rel = sc[ikr::kBB] > 0 ? std::sqrt(sc[ikr::kRR] / sc[ikr::kBB]) : 0.0;
+    ikr::launch_pcg_result(w, x, 1.0, s);
+    count(1);
+    if (done == 6.0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the staged SpMV gave up");
+    if (done == 3.0) fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp zero or not finite) after %d iterations", last_iters);
+    return last_iters;
+  }
+
+  // x = K^{-1} b with optional FP64 iterative refinement around the (possibly FP32) CG
+  int64_t solve(ikr_asm a, const double* b, double* x, double rt, int maxit, int refinements) {
+    int64_t its = solve_device(a, b, x, rt, maxit);
+    if (refinements <= 0) return its;
+    cudaStream_t s = a->fes->stream;
+    const int64_t n = 3LL * a->fes->nn;
+    for (int k = 0; k < refinements; ++k) {
+      ikr::launch_residual64(a->bsr(), fp32, x, b, r64.p, s);  // r = b - K x in FP64 accumulation
+      its += solve_device(a, r64.p, c64.p, rt, maxit);
+      ikr::launch_axpy64(x, c64.p, 1.0, n, s);
+      count(2);
+    }
+    return its;
+  }
+};
+
+struct Observer {
+  ikr_nr_observer cb;
+  void* user;
+};
+struct ControlObserver {
+  ikr_control_observer cb;
+  void* user;
+};
+
+struct ikr_nr_s {
+  ikr_asm asm_ = nullptr;
+  ikr_ls ls = nullptr;
+  ikr_nr_settings st{};
+  std::vector<Observer> obs;
+  bool fe_state = false;
+  DBuf<double> corr, rhs;
+  DBuf<double> nrm_part, nrm_out;
+  // per-instance state of the last solve (element sets with instances)
+  std::vector<int32_t> inst_iters;
+  std::vector<double> inst_res;
+  std::vector<uint8_t> inst_conv;
+  DBuf<double> inst_norm, inst_rtol;
+  DBuf<uint8_t> inst_active;
+  DBuf<int32_t> inst_cg_iters;
+  DBuf<double> inst_cg_res;
+};
+
+struct ikr_lc_s {
+  ikr_nr nr = nullptr;
+  int steps = 1;
+  double t0 = 0, t1 = 1;
+  std::vector<ControlObserver> obs;
+  // Newton predictor of each load step (the reference only increments the load factor,
+  // loadcontrol.inl:54-57): 0 = none, 1 = previous increment, 2 = learned; every prediction is kept only when
+  // its FP64 residual is below that of the unpredicted state.  `record` appends each converged increment to
+  // the predictor's training snapshots.
+  int pred_kind = 0;
+  ikr_pred pred = nullptr;
+  std::vector<double> theta;  // load parameters of the current path (learned predictor features)
+  bool record = false;
+  int path_id = 0;
+  int accepted = 0, rejected = 0;
+  // gate of a prediction: 0 = FP64 residual norm at the candidate states; 1 = FP64 residual norm after one
+  // truncated Newton step (relax_iters CG iterations) from each candidate; 2 = none (always kept)
+  int gate = 0;
+  int relax_iters = 30;
+  int64_t gate_cg = 0;  // CG iterations the gate spent in the last run
+  DBuf<double> u_step0, u_try, pred_part, pred_out, r0vec, g_rhs, g_corr;
+  DBuf<float> du1, du2;  // last two converged increments (FP32)
+  int hist = 0;          // how many increments are in du1 / du2
+  // per load step of the last run: FP64 residual norms of the unpredicted state, of the full prediction and
+  // of the prediction scaled by the residual-minimising step s*, and the step length kept (0 = unpredicted)
+  struct PredRecord {
+    double step, r_plain, r_full, s_star, r_scaled, s_used;
+  };
+  std::vector<PredRecord> phist;
+};
+
+// ------------------------------------------------------------------------------------------------------------
+namespace ikr_host {
+// load-control predictor hooks (predictor.cpp)
+void predictor_begin(ikr_lc lc, ikr_req r);
+// after lambda += dlambda: tries the configured prediction, keeps it only if its residual is smaller, and returns
+// the residual norm of the unpredicted state (the reference norm of the relative Newton test), 0 without predictor
+double predictor_apply(ikr_lc lc, ikr_req r, int step);
+void predictor_end_step(ikr_lc lc, ikr_req r, int step);
+void need(bool c, int code, const char* msg);
+double device_norm(ikr_fes f, const double* x, int64_t n, DBuf<double>& part, DBuf<double>& out);
+double device_dot(ikr_fes f, const double* x, const double* y, int64_t n, DBuf<double>& part, DBuf<double>& out);
+void assemble_vector(ikr_asm a, ikr_req r, int dbc);
+void assemble_matrix(ikr_asm a, ikr_req r, int dbc);
+void update_state(ikr_fes f, ikr_req r, const double* corr_dev);
+// Newton-Raphson solve (newtonraphson.hh:193-257); ref_norm > 0 replaces the initial residual norm as the
+// reference of the relative convergence test
+void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double ref_norm = 0.0);
+}  // namespace ikr_host

@@ -25,6 +25,8 @@ struct ElemArgs {
   const double* X = nullptr;     // coordinates, n_nodes x 3
   const int32_t* conn = nullptr; // corner-major: conn[v * n_elems + e]
   double lam = 0, mu = 0;        // Lame parameters of NeoHooke
+  const double* lam_e = nullptr;  // per-element Lame parameters (nullptr: lam / mu for every element)
+  const double* mu_e = nullptr;
   const double* u = nullptr;     // displacement, 3 * n_nodes (FP64)
   const uint8_t* node_fixed = nullptr;  // per node 3-bit Dirichlet mask; nullptr = no masking (Raw)
   // dead tractions: trac_idx[e] >= 0 indexes 24 values of sum_faces N_I t dA at load factor 1
@@ -47,13 +49,25 @@ struct ElemArgs {
   int* status = nullptr;           // StatusBits, OR-ed
 };
 
+// The tangent's 3x3 blocks are stored sliced-ELL: block rows (nodes) are grouped in slices of 32; slice s
+// spans the block columns [slice_off[s], slice_off[s+1]) (its longest row), rows shorter than that are
+// padded with zero blocks whose column is the row itself.  Block k of row r = 32 s + l has the id
+// b = (slice_off[s] + k) * 32 + l; its column is col_sell[b] and entry e = 3i + j (row-major in the block)
+// sits at val[block_entry(b, e)] = (b >> 5) * 288 + e * 32 + (b & 31), so for a fixed (k, e) the 32 rows of a
+// slice are 32 consecutive values.  The sorted CSR view (row_ptr / col) describes the pattern itself.
+__host__ __device__ __forceinline__ int64_t block_entry(int64_t b, int e) { return (b >> 5) * 288 + e * 32 + (b & 31); }
+
 struct Bsr {
-  int n_rows = 0;             // block rows = nodes
-  int64_t n_blocks = 0;
-  const int32_t* row_ptr = nullptr;
+  int n_rows = 0;                   // block rows = nodes
+  int64_t n_blocks = 0;             // blocks of the pattern (without padding)
+  int n_slices = 0;
+  int64_t n_padded = 0;             // 32 * slice_off[n_slices]
+  const int32_t* row_ptr = nullptr; // CSR view of the pattern
   const int32_t* col = nullptr;
-  const int32_t* diag = nullptr;  // position of the diagonal block of each row
-  const void* val = nullptr;      // float or double, 9 per block
+  const int32_t* slice_off = nullptr;
+  const int32_t* col_sell = nullptr;
+  const int32_t* diag = nullptr;    // block id of the diagonal block of each row
+  const void* val = nullptr;        // float or double, 9 * n_padded
 };
 
 // element.cu
@@ -76,24 +90,34 @@ void launch_node_elem_fill(const int32_t* conn, int n_elems, const int32_t* ptr,
                            int n_nodes, cudaStream_t s);
 void launch_row_build(const int32_t* conn, int n_elems, int n_nodes, const int32_t* ne_ptr, const int32_t* ne_elems,
                       const int32_t* row_ptr, int32_t* cnt_or_col, bool fill, int* status, cudaStream_t s);
-void launch_slot_map(const int32_t* conn, int n_elems, const int32_t* row_ptr, const int32_t* col, int32_t* slot,
-                     int32_t* diag, int n_nodes, cudaStream_t s);
-void launch_bsr_reset(void* val, bool fp32, int64_t n_blocks, const int32_t* diag, const uint8_t* node_fixed,
+// per slice of 32 rows: the longest row (slice_len has (n_nodes + 31) / 32 entries)
+void launch_slice_lengths(const int32_t* row_ptr, int n_nodes, int32_t* slice_len, cudaStream_t s);
+// column index of every (padded) block: the CSR columns, then the row itself for padding
+void launch_sell_fill(const int32_t* row_ptr, const int32_t* col, const int32_t* slice_off, int n_nodes,
+                      int32_t* col_sell, cudaStream_t s);
+// element-to-block map (block ids) and the diagonal block of each row
+void launch_slot_map(const int32_t* conn, int n_elems, const int32_t* row_ptr, const int32_t* col,
+                     const int32_t* slice_off, int32_t* slot, int32_t* diag, int n_nodes, cudaStream_t s);
+void launch_bsr_reset(void* val, bool fp32, int64_t n_padded, const int32_t* diag, const uint8_t* node_fixed,
                       int n_nodes, cudaStream_t s);
 void launch_vector_finish(double* R, const uint8_t* node_fixed, int n_nodes, const int32_t* pl_dof,
                           const double* pl_val, int n_pl, double load_factor, cudaStream_t s);
 void launch_norm2(const double* x, int64_t n, double* partials, double* out, cudaStream_t s);
+void launch_dot(const double* x, const double* y, int64_t n, double* partials, double* out, cudaStream_t s);
 
 // solver.cu -- block-Jacobi preconditioned CG
 // device scalar slots of the CG (doubles)
 enum PcgScal : int {
-  kBB = 0,     // |b|^2
-  kTol2 = 1,   // rtol^2 |b|^2
-  kRz = 2,     // r.z by iteration parity: 2, 3
-  kDone = 4,   // 0 running, 1 converged, 2 iteration limit, 3 breakdown
-  kIters = 5,  // iteration count by parity: 5, 6
-  kRR = 7,     // last |r|^2
+  kBB = 0,      // |b|^2
+  kTol2 = 1,    // rtol^2 |b|^2
+  kRz = 2,      // r.z of the current iterate
+  kDone = 4,    // 0 running, 1 converged, 2 iteration limit, 3 breakdown
+  kIters = 5,   // completed iterations
+  kRR = 7,      // last |r|^2
   kMaxIt = 8,
+  kAlpha = 9,
+  kBeta = 10,
+  kTicket = 12, // slots 12-13 hold four 32-bit tickets of the last-block reductions
   kNScal = 16
 };
 struct PcgWork {
@@ -110,6 +134,9 @@ struct PcgWork {
   double* part_b = nullptr;    // partials written by the update kernel (2 per block: rz, rr)
   double* scal = nullptr;      // device scalars, see solver.cu
   int grid = 0;                // fixed grid (multiple of the SM count) for the partial-producing kernels
+  int sms = 0;                 // SM count of the device
+  int spmv_kind = 0;           // 0: direct loads (solver.cu); 1 + v: staged variant v (spmv_staged.cu)
+  int64_t keep_g = 0;          // staged: matrix blocks [0, keep_g) are copied with an L2 evict_last policy
 };
 void launch_block_jacobi(const Bsr& A, bool fp32, void* minv, bool point_jacobi, cudaStream_t s);
 void launch_pcg_init(const Bsr& A, PcgWork& w, const double* b, double rtol, int max_iter, cudaStream_t s);
@@ -118,6 +145,39 @@ void launch_pcg_spmv(const Bsr& A, PcgWork& w, int parity, cudaStream_t s);
 void launch_pcg_update(const Bsr& A, PcgWork& w, int parity, cudaStream_t s);
 void launch_pcg_result(const PcgWork& w, double* x_out, double scale, cudaStream_t s);
 void launch_residual64(const Bsr& A, bool fp32, const double* x, const double* b, double* r, cudaStream_t s);
+// spmv_staged.cu -- the CG SpMV with bulk-copy staging of the matrix (variants differ in chunk size, pipeline
+// depth and warps per CTA); same inputs, outputs and scalars as launch_pcg_spmv
+int spmv_staged_variants();
+const char* spmv_staged_name(bool fp32, int variant);
+void launch_pcg_spmv_staged(const Bsr& A, PcgWork& w, int variant, const void* pold, void* pnew, cudaStream_t s);
+void launch_fill64(double* y, double v, int64_t n, cudaStream_t s);
+
+// batched.cu -- independent instances (disjoint contiguous node ranges) of one element set
+// one CTA per instance runs the instance's whole block-Jacobi PCG; inactive instances get a zero correction;
+// xw..qw are node-padded work vectors of the whole set; rtol per instance
+void launch_batched_pcg(const Bsr& A, bool fp32, const void* minv, const double* b, double* x_out, int n_inst,
+                        const int32_t* node_off, const int32_t* order, const uint8_t* active, void* xw, void* rw,
+                        void* zw, void* pw, void* qw, const double* rtol, int max_iter, int32_t* iters,
+                        double* relres, cudaStream_t s);
+void launch_instance_norms(const double* x, int n_inst, const int32_t* node_off, double* out, cudaStream_t s);
+
+// mlp.cu -- dense network (BF16 weights, FP32 accumulation) and POD helpers of the learned predictor
+// C[M x N] = alpha op(A) op(B) + beta C (row-major; op = transpose when trans_*; A / B FP32 or BF16)
+void launch_gemm(int M, int N, int K, const void* A, bool a_bf16, bool trans_a, int lda, const void* B, bool b_bf16,
+                 bool trans_b, int ldb, float* C, int ldc, float alpha, float beta, cudaStream_t s);
+void launch_bias_act(float* Z, float* Y, const float* bias, int B, int out, bool gelu, cudaStream_t s);
+void launch_gelu_backward(float* dZ, const float* Z, int64_t n, cudaStream_t s);
+void launch_colsum(const float* dZ, float* g, int B, int out, cudaStream_t s);
+int launch_mse(const float* Y, const float* T, float* dY, int64_t n, float scale, float* part, cudaStream_t s);
+void launch_adam(float* p, const float* g, float* m, float* v, void* wb, const int64_t* bf_index, int64_t n, float lr,
+                 float b1, float b2, float eps, int step, cudaStream_t s);
+void launch_to_bf16(const float* p, void* wb, const int64_t* bf_index, int64_t n, cudaStream_t s);
+void launch_gather_rows(const float* X, const int32_t* idx, float* out, int rows, int cols, cudaStream_t s);
+void launch_gram64(const float* Y, int64_t n, int l, double* G, cudaStream_t s);
+void launch_randn(float* out, int64_t n, uint64_t seed, cudaStream_t s);
+void launch_diff_to_f32(const double* a, const double* b, float* out, int64_t n, cudaStream_t s);
+void launch_add_f32(double* u, const float* d, int64_t n, cudaStream_t s);
+void launch_base_plus_scaled(double* u, const double* u0, const float* d, double sc, int64_t n, cudaStream_t s);
 
 // noalloc.cu -- fixed device scratch of the allocation-free CG solve
 constexpr int kNoAllocMaxRows = 32768;  // block rows (nodes) = 98304 dofs

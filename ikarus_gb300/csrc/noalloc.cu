@@ -21,8 +21,9 @@ namespace {
 
 constexpr size_t kAlign = 256;
 constexpr size_t align_up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
-// FP64 worst case: six dof vectors, the 3x3 inverse per block row, partials of the fixed grid, scalars
-constexpr size_t kScratchBytes = 6 * align_up(sizeof(double) * 3 * kNoAllocMaxRows) +
+// FP64 worst case: six node-padded CG vectors (4 values per node), the 3x3 inverse per block row, partials of
+// the fixed grid, scalars
+constexpr size_t kScratchBytes = 6 * align_up(sizeof(double) * 4 * kNoAllocMaxRows) +
                                  align_up(sizeof(double) * 9 * kNoAllocMaxRows) +
                                  align_up(sizeof(double) * kNoAllocMaxGrid) +
                                  align_up(sizeof(double) * 2 * kNoAllocMaxGrid) + align_up(sizeof(double) * kNScal);
@@ -57,7 +58,7 @@ cudaError_t noalloc_scratch_address(void** out) {
 // Carves the CG work set of n_rows block rows out of the scratch (FP32 or FP64 vectors).
 void noalloc_workset(void* base, int n_rows, bool fp32, int grid, PcgWork& w) {
   unsigned char* p = static_cast<unsigned char*>(base);
-  const size_t vb = align_up((fp32 ? 4 : 8) * 3 * (size_t)n_rows);
+  const size_t vb = align_up((fp32 ? 4 : 8) * 4 * (size_t)n_rows);
   w = PcgWork{};
   w.n_rows = n_rows;
   w.fp32 = fp32;

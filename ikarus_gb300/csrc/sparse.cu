@@ -123,22 +123,47 @@ __device__ __forceinline__ int find_col(const int32_t* __restrict__ col, int b, 
   return lo;
 }
 
+// block id of the k-th block of row r (see Bsr in kernels.h)
+__device__ __forceinline__ int32_t block_id(const int32_t* __restrict__ slice_off, int r, int k) {
+  return (slice_off[r >> 5] + k) * 32 + (r & 31);
+}
+
+__global__ void slice_len_kernel(const int32_t* __restrict__ row_ptr, int nn, int32_t* slice_len) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= (nn + 31) / 32) return;
+  int m = 0;
+  for (int r = 32 * s; r < min(nn, 32 * s + 32); ++r) m = max(m, row_ptr[r + 1] - row_ptr[r]);
+  slice_len[s] = m;
+}
+
+__global__ void sell_fill_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                                 const int32_t* __restrict__ slice_off, int nn, int32_t* col_sell) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= (nn + 31) / 32 * 32) return;
+  const int s = r >> 5;
+  const int width = slice_off[s + 1] - slice_off[s];
+  const int len = r < nn ? row_ptr[r + 1] - row_ptr[r] : 0;
+  for (int k = 0; k < width; ++k)
+    col_sell[block_id(slice_off, r, k)] = k < len ? col[row_ptr[r] + k] : (r < nn ? r : 0);
+}
+
 __global__ void slot_map_kernel(const int32_t* __restrict__ conn, int ne, const int32_t* __restrict__ row_ptr,
-                                const int32_t* __restrict__ col, int32_t* slot) {
+                                const int32_t* __restrict__ col, const int32_t* __restrict__ slice_off,
+                                int32_t* slot) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 64LL * ne) return;
   const int e = (int)(t % ne);
   const int pair = (int)(t / ne);
   const int I = pair >> 3, J = pair & 7;
   const int r = conn[I * ne + e], c = conn[J * ne + e];
-  slot[t] = find_col(col, row_ptr[r], row_ptr[r + 1], c);
+  slot[t] = block_id(slice_off, r, find_col(col, row_ptr[r], row_ptr[r + 1], c) - row_ptr[r]);
 }
 
-__global__ void diag_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col, int32_t* diag,
-                            int nn) {
+__global__ void diag_kernel(const int32_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                            const int32_t* __restrict__ slice_off, int32_t* diag, int nn) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= nn) return;
-  diag[n] = find_col(col, row_ptr[n], row_ptr[n + 1], n);
+  diag[n] = block_id(slice_off, n, find_col(col, row_ptr[n], row_ptr[n + 1], n) - row_ptr[n]);
 }
 
 // Full Dirichlet treatment of the matrix (simpleassemblers.inl:159-167): constrained rows and columns are zero
@@ -150,9 +175,8 @@ __global__ void unit_diag_kernel(T* val, const int32_t* __restrict__ diag, const
   if (n >= nn) return;
   const uint8_t m = fixed[n];
   if (!m) return;
-  T* b = val + 9 * (int64_t)diag[n];
   for (int c = 0; c < 3; ++c)
-    if ((m >> c) & 1) b[4 * c] = T(1);
+    if ((m >> c) & 1) val[block_entry(diag[n], 4 * c)] = T(1);
 }
 
 // Manipulator point loads after the Dirichlet treatment (assemblermanipulatorbuildingblocks.hh:110-115):
@@ -169,6 +193,21 @@ __global__ void sumsq_partial_kernel(const double* __restrict__ x, int64_t n, do
   double s = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     s += x[i] * x[i];
+  s = warp_sum(s);
+  __shared__ double ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
+  }
+}
+__global__ void dot_partial_kernel(const double* __restrict__ x, const double* __restrict__ y, int64_t n,
+                                   double* part) {
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += x[i] * y[i];
   s = warp_sum(s);
   __shared__ double ws[32];
   if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
@@ -217,14 +256,22 @@ void launch_row_build(const int32_t* conn, int n_elems, int n_nodes, const int32
   row_build_kernel<<<blocks_for(n_nodes, 64), 64, 0, s>>>(conn, n_elems, n_nodes, ne_ptr, ne_elems, row_ptr,
                                                            cnt_or_col, fill, status);
 }
-void launch_slot_map(const int32_t* conn, int n_elems, const int32_t* row_ptr, const int32_t* col, int32_t* slot,
-                     int32_t* diag, int n_nodes, cudaStream_t s) {
-  slot_map_kernel<<<blocks_for(64LL * n_elems, 256), 256, 0, s>>>(conn, n_elems, row_ptr, col, slot);
-  diag_kernel<<<blocks_for(n_nodes, 256), 256, 0, s>>>(row_ptr, col, diag, n_nodes);
+void launch_slice_lengths(const int32_t* row_ptr, int n_nodes, int32_t* slice_len, cudaStream_t s) {
+  slice_len_kernel<<<blocks_for((n_nodes + 31) / 32, 128), 128, 0, s>>>(row_ptr, n_nodes, slice_len);
 }
-void launch_bsr_reset(void* val, bool fp32, int64_t n_blocks, const int32_t* diag, const uint8_t* node_fixed,
+void launch_sell_fill(const int32_t* row_ptr, const int32_t* col, const int32_t* slice_off, int n_nodes,
+                      int32_t* col_sell, cudaStream_t s) {
+  sell_fill_kernel<<<blocks_for((n_nodes + 31) / 32 * 32LL, 128), 128, 0, s>>>(row_ptr, col, slice_off, n_nodes,
+                                                                               col_sell);
+}
+void launch_slot_map(const int32_t* conn, int n_elems, const int32_t* row_ptr, const int32_t* col,
+                     const int32_t* slice_off, int32_t* slot, int32_t* diag, int n_nodes, cudaStream_t s) {
+  slot_map_kernel<<<blocks_for(64LL * n_elems, 256), 256, 0, s>>>(conn, n_elems, row_ptr, col, slice_off, slot);
+  diag_kernel<<<blocks_for(n_nodes, 256), 256, 0, s>>>(row_ptr, col, slice_off, diag, n_nodes);
+}
+void launch_bsr_reset(void* val, bool fp32, int64_t n_padded, const int32_t* diag, const uint8_t* node_fixed,
                       int n_nodes, cudaStream_t s) {
-  cudaMemsetAsync(val, 0, (size_t)n_blocks * 9 * (fp32 ? 4 : 8), s);
+  cudaMemsetAsync(val, 0, (size_t)n_padded * 9 * (fp32 ? 4 : 8), s);
   if (!node_fixed) return;
   if (fp32) unit_diag_kernel<float><<<blocks_for(n_nodes, 256), 256, 0, s>>>((float*)val, diag, node_fixed, n_nodes);
   else unit_diag_kernel<double><<<blocks_for(n_nodes, 256), 256, 0, s>>>((double*)val, diag, node_fixed, n_nodes);
@@ -238,6 +285,10 @@ void launch_vector_finish(double* R, const uint8_t* node_fixed, int n_nodes, con
 void launch_norm2(const double* x, int64_t n, double* partials, double* out, cudaStream_t s) {
   sumsq_partial_kernel<<<kNormGrid, 256, 0, s>>>(x, n, partials);
   sum_partials_kernel<<<1, 256, 0, s>>>(partials, kNormGrid, out, true);
+}
+void launch_dot(const double* x, const double* y, int64_t n, double* partials, double* out, cudaStream_t s) {
+  dot_partial_kernel<<<kNormGrid, 256, 0, s>>>(x, y, n, partials);
+  sum_partials_kernel<<<1, 256, 0, s>>>(partials, kNormGrid, out, false);
 }
 
 }  // namespace ikr

@@ -31,7 +31,8 @@ enum {
   IKR_ERR_CG_BREAKDOWN = -6,
   IKR_ERR_CUDA = -7,
   IKR_ERR_SINGULAR = -8,
-  IKR_ERR_NO_DEVICE = -9
+  IKR_ERR_NO_DEVICE = -9,
+  IKR_ERR_TIMEOUT = -10           /* a bounded wait inside a kernel gave up (the context stays usable) */
 };
 
 /* ---- enums with the reference's values ------------------------------------------------------------------ */
@@ -52,6 +53,7 @@ enum {
   IKR_SOLVER_NONE = 0,
   IKR_SOLVER_SI_CONJUGATE_GRADIENT = 1,
   IKR_SOLVER_GPU_PCG_BLOCK_JACOBI = 100,  /* FP64 or FP32 CG, 3x3 block-Jacobi, precision of the assembled K */
+  IKR_SOLVER_GPU_PCG_BATCHED = 101,       /* one block-Jacobi CG per instance, all in one launch (see below) */
 };
 /* precision of the assembled tangent */
 enum { IKR_PRECISION_FP64 = 0, IKR_PRECISION_FP32 = 1 };
@@ -87,6 +89,15 @@ int ikr_fes_create(ikr_fes* out, int32_t n_nodes, const double* coords, int32_t 
  * value of f at the face's single quadrature point (the face centre; rule order = order() = 1). */
 int ikr_fes_add_neumann(ikr_fes fes, int32_t n_faces, const int32_t* face_elem, const int32_t* face_local,
                         const double* traction);
+/* removes every Neumann load added so far (the element set keeps its mesh, material and state) */
+int ikr_fes_clear_neumann(ikr_fes fes);
+/* per-element Lame parameters (n_elems each) replacing the set's single NeoHooke material */
+int ikr_fes_set_element_materials(ikr_fes fes, const double* lambda, const double* mu);
+/* Declares the mesh a union of n_instances independent problems on the contiguous node ranges
+ * [node_offsets[i], node_offsets[i+1]) (no element may connect two ranges).  With the solver tag
+ * IKR_SOLVER_GPU_PCG_BATCHED every instance then runs its own Newton test (relative to its own initial
+ * residual) and its own CG, all instances in one launch per Newton iteration (no reference counterpart). */
+int ikr_fes_set_instances(ikr_fes fes, int32_t n_instances, const int32_t* node_offsets);
 int ikr_fes_destroy(ikr_fes fes);
 int ikr_fes_num_colours(ikr_fes fes, int32_t* n_colours);
 /* EAS internal variables alpha_ (enhancedassumedstrains.hh:207, 364): n_elems x n_alpha, row-major */
@@ -160,6 +171,17 @@ int ikr_linear_solver_last_info(ikr_ls ls, int32_t* iterations, double* rel_resi
  * since profiling was switched on. */
 int ikr_linear_solver_profile(ikr_ls ls, int32_t on);
 int ikr_linear_solver_profile_read(ikr_ls ls, double* spmv_ms_total, int64_t* spmv_launches);
+/* Launch shape of the CG (no reference counterpart): iterations are issued in chunks of chunk_len
+ * (1..256, default 16) between host convergence polls, captured as CUDA graphs when use_graphs != 0
+ * (default) or launched kernel by kernel otherwise (for profilers that do not follow graph kernels). */
+int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_len);
+/* SpMV kernel of the CG (no reference counterpart).  spmv_kind 0 = direct loads, 1..4 = bulk-copy staged
+ * variants (chunk size / pipeline depth / warps per block), -1 = autotune; l2_keep_fraction in [0, 1) = share
+ * of the matrix the staged kernels keep in L2 across iterations, -1 = autotune.  The choice is made at the
+ * next factorize from timed CG iterations on the assembled tangent and kept for that assembler.  info
+ * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */
+int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fraction);
+int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* spmv_kind, double* l2_keep_fraction, double* spmv_us);
 /* the CUDA stream (cudaStream_t) all work on this element set is issued on */
 int ikr_fes_stream(ikr_fes fes, void** stream);
 
@@ -167,7 +189,7 @@ int ikr_fes_stream(ikr_fes fes, void** stream);
  * reference).  For callers that may not allocate device memory after start-up (a fixed device-memory
  * budget, or all allocations routed through their own allocator): it calls no cudaMalloc / cudaFree /
  * cudaMallocHost and no allocating library routine.  The CG vectors, the 3x3 block-Jacobi inverse and the
- * reduction slots live in one file-scope device array of the library (about 7.1 MB, held by every GPU that
+ * reduction slots live in one file-scope device array of the library (about 8.7 MB, held by every GPU that
  * loads the library until exit), so the system may have at most IKR_NOALLOC_MAX_NODES nodes (3x as many
  * dofs); larger systems return IKR_ERR_ARG.  b and x are device pointers of size() doubles; the CG runs in
  * the precision of the stored tangent with the same block-Jacobi preconditioner, tolerance rtol on
@@ -218,6 +240,8 @@ int ikr_newton_subscribe(ikr_nr nr, ikr_nr_observer cb, void* user);
 int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on);
 /* solve(x, stepSize) (newtonraphson.hh:193-257) */
 int ikr_newton_solve(ikr_nr nr, ikr_req req, double step_size, ikr_nr_info* info);
+/* per instance (batched solves): Newton iterations, final residual norm and convergence of the last solve */
+int ikr_newton_instance_info(ikr_nr nr, int32_t* iterations, double* residual_norms, int32_t* converged);
 
 /* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
 typedef struct ikr_control_state {   /* ControlRoutineState (controlroutinestate.hh:21-31) */
@@ -242,6 +266,56 @@ int ikr_load_control_subscribe(ikr_lc lc, ikr_control_observer cb, void* user);
  * equilibrium solve at the starting load factor). */
 int ikr_load_control_run(ikr_lc lc, ikr_req req, ikr_control_info* info, ikr_nr_info* solver_infos,
                          int32_t capacity);
+
+/* ---- Newton predictor of LoadControl (no counterpart in the reference, whose predictor only increments
+ * the load factor, loadcontrol.inl:54-57) -------------------------------------------------------------------
+ * kind 0: none (the reference's behaviour); 1: previous converged increment; 2: learned (predictor object).
+ * A prediction is kept only if its FP64 residual is below that of the unpredicted state, and the relative
+ * Newton test of the step stays referenced to the unpredicted residual.  record = 1 appends every converged
+ * increment (and params, the path's load parameters) to the predictor's training snapshots. */
+typedef struct ikr_pred_s* ikr_pred;
+typedef struct ikr_mlp_s* ikr_mlp;
+int ikr_load_control_set_predictor(ikr_lc lc, int32_t kind, ikr_pred pred, const double* params, int32_t record);
+/* predictions kept / rejected by the residual test since the predictor was set */
+int ikr_load_control_predictor_stats(ikr_lc lc, int32_t* accepted, int32_t* rejected);
+/* per load step of the last run, 6 doubles: step, FP64 residual norm of the unpredicted state, of the full
+ * prediction (-1 if none), the residual-minimising step length s* along the prediction, the residual norm at
+ * s* (-1 if not tried) and the step length kept (0 = unpredicted state).  n returns the number of steps;
+ * at most capacity rows are written. */
+int ikr_load_control_predictor_history(ikr_lc lc, int32_t capacity, double* out, int32_t* n);
+/* How a prediction is judged (no reference counterpart): gate 0 (default) keeps the state with the smaller
+ * FP64 residual norm among the unpredicted state, the prediction and the prediction scaled by its
+ * residual-minimising step; gate 1 takes one truncated Newton step (tangent + relax_iters block-Jacobi CG
+ * iterations) from the unpredicted state and from the prediction and keeps the one with the smaller FP64
+ * residual norm (displacement-based elements only); gate 2 keeps every prediction.  In the history of gate
+ * 1, column 2 is the residual after the step from the prediction and column 4 after the step from the
+ * unpredicted state.  gate_cg returns the CG iterations the gate spent in the last run. */
+int ikr_load_control_set_predictor_gate(ikr_lc lc, int32_t gate, int32_t relax_iters);
+int ikr_load_control_predictor_gate_cg(ikr_lc lc, int64_t* cg_iterations);
+/* POD (n_modes) + MLP (depth hidden layers of width, GELU, BF16 weights, FP32 accumulation) over the
+ * features [params, load factor, POD coordinates of the previous two increments]; snapshots: up to capacity
+ * increments of the element set's dofs, held on the device in FP32. */
+int ikr_predictor_create(ikr_pred* out, ikr_fes fes, int32_t n_params, int32_t n_modes, int32_t width,
+                         int32_t depth, int64_t capacity, uint64_t seed);
+int ikr_predictor_destroy(ikr_pred pred);
+int ikr_predictor_num_snapshots(ikr_pred pred, int64_t* n);
+/* builds the POD basis of the recorded increments (randomized range finder on the device) and trains the
+ * network on the device with Adam; returns the last epoch's mean loss and the captured POD energy fraction */
+int ikr_predictor_fit(ikr_pred pred, int32_t epochs, int32_t batch, float lr, float* final_loss,
+                      double* pod_energy);
+
+/* ---- the dense network on its own (gradient checks, stand-alone training); parameters are the FP32 master
+ * copies, per layer W (out x in, row-major) then b (out); the forward pass uses their BF16 rounding -------- */
+int ikr_mlp_create(ikr_mlp* out, int32_t n_in, int32_t width, int32_t depth, int32_t n_out, uint64_t seed);
+int ikr_mlp_destroy(ikr_mlp mlp);
+int ikr_mlp_num_params(ikr_mlp mlp, int64_t* n);
+int ikr_mlp_get_params(ikr_mlp mlp, float* params);
+int ikr_mlp_set_params(ikr_mlp mlp, const float* params);
+int ikr_mlp_forward(ikr_mlp mlp, int32_t batch, const float* x, float* y);
+/* mean-squared-error loss over batch x n_out outputs and its gradient w.r.t. all parameters */
+int ikr_mlp_loss_grad(ikr_mlp mlp, int32_t batch, const float* x, const float* target, float* loss, float* grad);
+int ikr_mlp_train(ikr_mlp mlp, int32_t n, const float* x, const float* target, int32_t epochs, int32_t batch,
+                  float lr, uint64_t seed, float* final_loss);
 
 #ifdef __cplusplus
 }

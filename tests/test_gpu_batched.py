@@ -1,0 +1,29 @@
+"""Independent instances solved together (one CG launch per Newton iteration, CTA per instance) against the
+oracle solving each instance on its own."""
+import numpy as np
+import pytest
+
+import oracle
+from ikarus_gb300 import problems
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batched_instances_match_individual_oracle_solves(ikr, precision):
+    bp = problems.batched_cantilevers(n=12, seed=3, nx=(3, 8), nyz=(1, 3), E=(1e3, 1e4), t=(0.1, 0.5),
+                                      load_steps=4)
+    fes, asm = problems.build_gpu_batched(bp, precision=precision)
+    req = ikr.FERequirements(fes)
+    st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=precision == 1, linear_rtol=1e-10 if
+                        precision == 0 else 1e-2, linear_rtol_min=1e-6)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    info = ikr.LoadControl(nr, bp.load_steps).run(req)
+    assert info.success
+    its, rn, conv = nr.instance_info()
+    assert conv.all()
+    u = req.globalSolution()
+    for i, part in enumerate(bp.parts):
+        ref = oracle.from_problem(part).load_control(bp.load_steps, tol=1e-8, tol_mode=1)
+        ui = u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]]
+        assert np.abs(ui - ref["u"]).max() <= 1e-6 * np.abs(ref["u"]).max(), i

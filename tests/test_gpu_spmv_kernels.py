@@ -1,0 +1,58 @@
+"""Every CG SpMV kernel (direct loads, the bulk-copy staged variants, with and without the L2 keep policy) and
+both launch modes (CUDA graphs, kernel by kernel) solve the same system to the same tolerance, each run to run
+bit-identical; the tuner picks one of them and reports it."""
+import numpy as np
+import pytest
+
+from ikarus_gb300 import problems
+
+pytestmark = pytest.mark.gpu
+
+def true_residual_bound(fp32):
+    """Relative true residual |K x - b| / |b| (FP64 arithmetic on the stored tangent) a converged solve reaches.
+    FP64: the CG tolerance.  FP32: the recursively updated CG residual drifts from the true one by about
+    eps_32 * cond(K) (6e-8 * 2.4e5 here), so the bound is 2e-3; the FP64 Newton residual corrects this."""
+    return 2e-3 if fp32 else 1e-10
+
+
+KINDS = [(0, 0.0), (1, 0.0), (2, 0.0), (3, 0.0), (4, 0.0), (1, 0.5), (2, 0.75)]
+
+
+@pytest.fixture(scope="module", params=[0, 1], ids=["fp64", "fp32"])
+def system(request, ikr):
+    # 12x5x3 elements: 13 * 6 * 4 = 312 nodes, so ten slices of 32 rows with a ragged last slice
+    p = problems.cantilever(12, 5, 3, L=6.0, jitter=0.1, seed=3)
+    fes, asm = problems.build_gpu(p, precision=request.param)
+    # a random state small enough that the tangent stays positive definite (min eigenvalue 0.018 at 0.003)
+    req = ikr.FERequirements(fes, 0.003 * np.random.default_rng(1).standard_normal(p.n_dofs) * (1 - p.fixed), 0.3)
+    K = asm.matrix(req, dbc=ikr.DBCOption.Full)
+    b = np.random.default_rng(0).standard_normal(p.n_dofs) * (1 - p.fixed)
+    return request.param, p, asm, K, b
+
+
+@pytest.mark.parametrize("kind,keep", KINDS)
+@pytest.mark.parametrize("graphs", [True, False], ids=["graphs", "direct"])
+def test_spmv_kernel_solves(ikr, system, kind, keep, graphs):
+    fp32, p, asm, K, b = system
+    rtol = 1e-5 if fp32 else 1e-11
+    ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=rtol)
+    ls.set_kernel(kind, keep)
+    ls.set_launch(use_graphs=graphs, chunk_len=8)
+    ls.compute(asm)
+    assert ls.kernel_info()[0] == kind
+    x1 = ls.solve(asm, b)
+    it1, rel1 = ls.last_info()
+    x2 = ls.solve(asm, b)
+    assert np.array_equal(x1, x2), "repeated solve is not bit-identical"
+    assert 0 < it1 and rel1 <= rtol
+    assert np.linalg.norm(K @ x1 - b) <= true_residual_bound(fp32) * np.linalg.norm(b)
+
+
+def test_tuner_choice_is_reported(ikr, system):
+    fp32, p, asm, K, b = system
+    ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-5 if fp32 else 1e-11)
+    ls.compute(asm)
+    kind, keep, us = ls.kernel_info()
+    assert 0 <= kind <= 4 and 0.0 <= keep < 1.0 and us > 0.0
+    x = ls.solve(asm, b)
+    assert np.linalg.norm(K @ x - b) <= true_residual_bound(fp32) * np.linalg.norm(b)
