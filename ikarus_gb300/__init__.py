@@ -191,8 +191,7 @@ SIGNATURES = {
     "ikr_load_control_set_predictor": ([_vp, _I, _vp, _dp, _I], C.c_int),
     "ikr_load_control_predictor_stats": ([_vp, _ip, _ip], C.c_int),
     "ikr_load_control_predictor_history": ([_vp, _I, _dp, _ip], C.c_int),
-    "ikr_load_control_set_predictor_gate": ([_vp, _I, _I], C.c_int),
-    "ikr_load_control_predictor_gate_cg": ([_vp, _i64p], C.c_int),
+    "ikr_load_control_set_predictor_gate": ([_vp, _I], C.c_int),
     "ikr_predictor_create": ([C.POINTER(_vp), _vp, _I, _I, _I, _I, _L, C.c_uint64], C.c_int),
     "ikr_predictor_destroy": ([_vp], C.c_int),
     "ikr_predictor_num_snapshots": ([_vp, _i64p], C.c_int),
@@ -649,13 +648,14 @@ class NewtonRaphson:
         _err(lib().ikr_newton_subscribe_fe_state(self.h, int(on)))
 
     def instance_info(self):
-        """(iterations, residual norms, converged) per instance of the last batched solve."""
+        """(iterations, residual norms, status) per instance of the last batched solve; status 1 converged,
+        0 not converged, -1 taken out after its elements inverted (det C <= 0)."""
         n = self.assembler.fes.n_instances
         it = np.zeros(n, dtype=np.int32)
         rn = np.zeros(n)
         cv = np.zeros(n, dtype=np.int32)
         _err(lib().ikr_newton_instance_info(self.h, _ptr(it, C.c_int32), _ptr(rn), _ptr(cv, C.c_int32)))
-        return it, rn, cv.astype(bool)
+        return it, rn, cv
 
     def solve(self, req: FERequirements, stepSize: float = 0.0) -> NonLinearSolverInformation:
         info = _NRInfo()
@@ -700,8 +700,8 @@ class LoadControl:
         _err(lib().ikr_load_control_subscribe(self.h, cb, None), "subscribe")
 
     def set_predictor(self, kind: int = 0, predictor: "LearnedPredictor" = None, params=None, record=False):
-        """Newton predictor of every load step: 0 none (reference), 1 previous increment, 2 learned.
-        Predictions are kept only when their FP64 residual is below the unpredicted one."""
+        """Newton predictor of every load step: 0 none (reference), 1 previous increment, 2 learned (falls back
+        to the previous increment when its FP64 residual is not smaller)."""
         par = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
         _err(lib().ikr_load_control_set_predictor(self.h, int(kind), predictor.h if predictor else None,
                                                   _ptr(par) if par is not None else None, int(record)), "predictor")
@@ -711,17 +711,13 @@ class LoadControl:
         _err(lib().ikr_load_control_predictor_stats(self.h, C.byref(a), C.byref(r)))
         return a.value, r.value
 
-    def set_predictor_gate(self, gate=0, relax_iters=30):
-        """0: FP64 residual at the candidates; 1: after one truncated Newton step from each; 2: ungated."""
-        _err(lib().ikr_load_control_set_predictor_gate(self.h, int(gate), int(relax_iters)))
-
-    def predictor_gate_cg(self):
-        n = C.c_int64()
-        _err(lib().ikr_load_control_predictor_gate_cg(self.h, C.byref(n)))
-        return n.value
+    def set_predictor_gate(self, gated=True):
+        """Keep the learned candidate only when its FP64 residual beats its fallback (default), or always."""
+        _err(lib().ikr_load_control_set_predictor_gate(self.h, int(bool(gated))))
 
     def predictor_history(self):
-        """Per load step of the last run: (step, |R| unpredicted, |R| full prediction, s*, |R| at s*, s kept)."""
+        """Per load step of the last run: (step, |R| unpredicted, |R| previous increment, |R| learned, kept, 0);
+        kept: 0 unpredicted, 1 previous increment, 2 learned."""
         n = C.c_int32()
         _err(lib().ikr_load_control_predictor_history(self.h, 0, None, C.byref(n)))
         out = np.zeros((max(n.value, 1), 6))

@@ -1,0 +1,379 @@
+// Persistent block-Jacobi PCG: a whole CG solve in one cooperative launch (sm_103a).
+//
+// Same iteration as the two-kernel CG of solver.cu / spmv_staged.cu (p_new = z + beta p_old formed on the fly
+// for every gathered neighbour, q = K p_new, alpha = rz / p.q, x += alpha p, r -= alpha q, z = M^{-1} r,
+// beta = rz_new / rz), but every CTA stays resident for all iterations and the two global reductions of an
+// iteration are grid barriers:
+//   * each warp owns up to MAXS slices (32 block rows each) and keeps x, r, z, p and q of its rows in registers,
+//     so the update phase touches global memory only to publish z (and p_new in the product phase), which the
+//     neighbours' gathers need;
+//   * the matrix is streamed with the same per-warp bulk-copy pipeline as the staged SpMV; the stream of a
+//     warp's chunks is cyclic over iterations, so the copies of the next iteration's first chunks are in flight
+//     while the CTA waits at the barriers;
+//   * a grid barrier publishes one partial per CTA (double-buffered by iteration parity), arrives on a counter
+//     and waits until every CTA has arrived; every CTA then sums all partials in CTA order, so alpha, beta and
+//     the convergence decision are bit-identical in all CTAs and from run to run.
+// The launch is cooperative (all CTAs co-resident).  Every wait is bounded: a grid barrier or stage wait that
+// gives up sets scal[kDone] = 6, the kernel drains its copies in flight (bounded) and returns.
+#include <mutex>
+
+#include "staging.cuh"
+
+namespace ikr {
+
+namespace {
+
+using namespace cg;
+
+constexpr int kBarrierSpinLimit = 1 << 24;  // polls (with a short sleep) before a grid barrier gives up
+
+// arrive on the grid barrier counter and wait until `target` arrivals; thread 0 of the CTA spins
+__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int target, bool* ok_sh) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(count, 1u);
+    bool ok = false;
+    for (int k = 0; k < kBarrierSpinLimit; ++k) {
+      unsigned int v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
+      if (v >= target) {
+        ok = true;
+        break;
+      }
+      __nanosleep(32);
+    }
+    *ok_sh = ok;
+  }
+  __syncthreads();
+  __threadfence();  // every thread: its later plain loads observe what the other CTAs wrote before arriving
+  return *ok_sh;
+}
+
+// fixed-order sum of the G partials at p[i * st] (i < G), result in every thread
+__device__ __forceinline__ double grid_partial_sum(const double* p, int G, int st, double* sh) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < G; i += blockDim.x) s += __ldcg(p + (size_t)i * st);
+  return block_sum_all(s, sh);
+}
+
+template <typename T, int CB, int NST, int WARPS>
+struct PersistentCfg {
+  static constexpr int kValBytes = CB * 288 * (int)sizeof(T);
+  static constexpr int kColBytes = CB * 32 * 4;
+  static constexpr int kStageBytes = kValBytes + kColBytes;
+  static constexpr int kSmemBytes = WARPS * NST * kStageBytes;
+  static constexpr int kThreads = WARPS * 32;
+};
+
+// cyclic position in a warp's chunk stream: owned slice j (slice gw + j * nw), first block g, slice end gend
+struct CyclicPos {
+  int j, g, gend;
+};
+
+template <typename T, int CB, int NST, int WARPS, int MAXS>
+__global__ void __launch_bounds__(WARPS * 32, 1)
+    pcg_persistent_kernel(Bsr A, const T* __restrict__ val, const T* __restrict__ minv, T* __restrict__ xg,
+                          const T* __restrict__ rg, T* __restrict__ zg, T* __restrict__ p0, T* __restrict__ p1,
+                          double* part_a, double* part_b, double* scal, int64_t keep_g) {
+  using C = PersistentCfg<T, CB, NST, WARPS>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bars[WARPS][NST];
+  __shared__ double sh[32];
+  __shared__ bool ok_sh;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int G = gridDim.x;
+  const int nw = G * WARPS;
+  const int gw = blockIdx.x * WARPS + warp;
+  const int n_slices = A.n_slices;
+  unsigned int* bar_count = &tickets(scal)[3];
+  unsigned char* wbase = smem + (size_t)warp * NST * C::kStageBytes;
+
+  // owned slices and their block ranges
+  int ns = 0;
+  int s_first[MAXS], s_end[MAXS];
+#pragma unroll
+  for (int j = 0; j < MAXS; ++j) {
+    const int sj = gw + j * nw;
+    s_first[j] = 0, s_end[j] = 0;
+    if (sj < n_slices) {
+      s_first[j] = A.slice_off[sj];
+      s_end[j] = A.slice_off[sj + 1];
+      ns = j + 1;
+    }
+  }
+  // CG state of the owned rows
+  T xr[MAXS][3], rr_[MAXS][3], zr[MAXS][3], pr[MAXS][3], qr[MAXS][3];
+#pragma unroll
+  for (int j = 0; j < MAXS; ++j) {
+    const int row = 32 * (gw + j * nw) + lane;
+    const bool own = j < ns && row < A.n_rows;
+    V3<T> r0 = {T(0), T(0), T(0)}, z0 = {T(0), T(0), T(0)};
+    if (own) r0 = load3rw(rg, row), z0 = load3rw(zg, row);
+    xr[j][0] = xr[j][1] = xr[j][2] = T(0);
+    pr[j][0] = pr[j][1] = pr[j][2] = T(0);
+    qr[j][0] = qr[j][1] = qr[j][2] = T(0);
+    rr_[j][0] = r0.x, rr_[j][1] = r0.y, rr_[j][2] = r0.z;
+    zr[j][0] = z0.x, zr[j][1] = z0.y, zr[j][2] = z0.z;
+  }
+  double rz = scal[kRz];
+  const double tol2 = scal[kTol2];
+  const int maxit = (int)scal[kMaxIt];
+  double rrs = scal[kRR];
+  double done = scal[kDone];
+  double beta = 0.0;
+
+  if (lane == 0) {
+    for (int st = 0; st < NST; ++st) mbar_init(smem_addr(&bars[warp][st]), 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+
+  auto issue = [&](int st, const CyclicPos& P) {
+    if (lane == 0) {
+      const int nb = min(CB, P.gend - P.g);
+      const uint32_t vb = nb * 288 * (uint32_t)sizeof(T), cb = nb * 128;
+      const uint32_t b = smem_addr(&bars[warp][st]);
+      unsigned char* stage = wbase + (size_t)st * C::kStageBytes;
+      const uint64_t pol = l2_policy(P.g < keep_g);
+      mbar_expect_tx(b, vb + cb);
+      bulk_g2s(smem_addr(stage), val + (int64_t)P.g * 288, vb, b, pol);
+      bulk_g2s(smem_addr(stage + C::kValBytes), A.col_sell + (int64_t)P.g * 32, cb, b, pol);
+    }
+  };
+  auto advance = [&](CyclicPos& P) {
+    P.g += CB;
+    if (P.g >= P.gend) {
+      P.j = (P.j + 1 == ns) ? 0 : P.j + 1;
+      // s_first / s_end are indexed with a runtime j here: pick through an unrolled select
+#pragma unroll
+      for (int j = 0; j < MAXS; ++j)
+        if (j == P.j) P.g = s_first[j], P.gend = s_end[j];
+    }
+  };
+
+  CyclicPos P{0, s_first[0], s_end[0]};
+  int inflight = 0;
+  if (ns > 0 && done == 0.0) {
+    for (int st = 0; st < NST; ++st) {
+      issue(st, P);
+      ++inflight;
+      advance(P);
+    }
+  }
+  uint32_t phase = 0;
+  int st = 0;
+  bool failed = false;
+  int it = (int)scal[kIters];
+  unsigned int barrier_no = 0;
+
+  while (done == 0.0) {
+    const T tb = T(beta);
+    const T* pold = (it & 1) ? p0 : p1;
+    T* pnew = (it & 1) ? p1 : p0;
+    double pq = 0.0;
+    // ---- product phase: q = K p_new over the owned slices
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) {
+      if (j < ns && !failed) {
+        T a0 = T(0), a1 = T(0), a2 = T(0);
+        for (int g = s_first[j]; g < s_end[j]; g += CB) {
+          const bool okw = __all_sync(0xffffffffu, mbar_wait_bounded(smem_addr(&bars[warp][st]), (phase >> st) & 1u));
+          if (!okw) {
+            failed = true;
+            break;
+          }
+          phase ^= 1u << st;
+          --inflight;
+          const T* sv = reinterpret_cast<const T*>(wbase + (size_t)st * C::kStageBytes);
+          const int32_t* sc = reinterpret_cast<const int32_t*>(wbase + (size_t)st * C::kStageBytes + C::kValBytes);
+          const int nb = min(CB, s_end[j] - g);
+          V3<T> zc[CB], pc[CB];
+#pragma unroll
+          for (int k = 0; k < CB; ++k) {
+            const int c = k < nb ? sc[32 * k + lane] : 0;
+            zc[k] = load3rw(zg, c);
+            pc[k] = load3rw(pold, c);
+          }
+#pragma unroll
+          for (int k = 0; k < CB; ++k) {
+            if (k < nb) {
+              const T x0 = zc[k].x + tb * pc[k].x, x1 = zc[k].y + tb * pc[k].y, x2 = zc[k].z + tb * pc[k].z;
+              const T* v = sv + 288 * k + lane;
+              a0 += v[0] * x0 + v[32] * x1 + v[64] * x2;
+              a1 += v[96] * x0 + v[128] * x1 + v[160] * x2;
+              a2 += v[192] * x0 + v[224] * x1 + v[256] * x2;
+            }
+          }
+          __syncwarp();  // the stage is consumed before it is refilled
+          issue(st, P);
+          ++inflight;
+          advance(P);
+          st = (st + 1 == NST) ? 0 : st + 1;
+        }
+        const int row = 32 * (gw + j * nw) + lane;
+        const T n0 = zr[j][0] + tb * pr[j][0], n1 = zr[j][1] + tb * pr[j][1], n2 = zr[j][2] + tb * pr[j][2];
+        pr[j][0] = n0, pr[j][1] = n1, pr[j][2] = n2;
+        qr[j][0] = a0, qr[j][1] = a1, qr[j][2] = a2;
+        if (row < A.n_rows) {
+          store3(pnew, row, n0, n1, n2);
+          pq += double(n0 * a0 + n1 * a1 + n2 * a2);
+        }
+      }
+    }
+    // ---- grid reduction of p.q
+    const int par = it & 1;
+    const double pq_cta = block_sum_all(pq, sh);
+    if (threadIdx.x == 0) part_a[par * G + blockIdx.x] = pq_cta;
+    ++barrier_no;
+    if (!grid_barrier(bar_count, barrier_no * (unsigned)G, &ok_sh)) failed = true;
+    failed = __syncthreads_or(failed);
+    if (failed) break;
+    const double pqs = grid_partial_sum(part_a + par * G, G, 1, sh);
+    if (!(fabs(pqs) > 0.0) || !isfinite(pqs)) {  // breakdown (negative curvature alone does not stop CG)
+      done = 3.0;
+      break;
+    }
+    const T alpha = T(rz / pqs);
+    // ---- update phase on the owned rows
+    double rzn = 0.0, rrn = 0.0;
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) {
+      const int row = 32 * (gw + j * nw) + lane;
+      if (j < ns && row < A.n_rows) {
+        T r1[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          xr[j][c] += alpha * pr[j][c];
+          r1[c] = rr_[j][c] - alpha * qr[j][c];
+          rr_[j][c] = r1[c];
+        }
+        const T* m = minv + 9 * (int64_t)row;
+        T zv[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          zv[a] = __ldg(m + 3 * a) * r1[0] + __ldg(m + 3 * a + 1) * r1[1] + __ldg(m + 3 * a + 2) * r1[2];
+          zr[j][a] = zv[a];
+        }
+        store3(zg, row, zv[0], zv[1], zv[2]);
+        T trz = T(0), trr = T(0);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          trz += r1[a] * zv[a];
+          trr += r1[a] * r1[a];
+        }
+        rzn += double(trz);
+        rrn += double(trr);
+      }
+    }
+    const double rz_cta = block_sum_all(rzn, sh);
+    const double rr_cta = block_sum_all(rrn, sh);
+    if (threadIdx.x == 0) {
+      part_b[par * 2 * G + 2 * blockIdx.x] = rz_cta;
+      part_b[par * 2 * G + 2 * blockIdx.x + 1] = rr_cta;
+    }
+    ++barrier_no;
+    if (!grid_barrier(bar_count, barrier_no * (unsigned)G, &ok_sh)) failed = true;
+    failed = __syncthreads_or(failed);
+    if (failed) break;
+    const double rzs = grid_partial_sum(part_b + par * 2 * G, G, 2, sh);
+    rrs = grid_partial_sum(part_b + par * 2 * G + 1, G, 2, sh);
+    beta = rzs / rz;
+    rz = rzs;
+    ++it;
+    if (rrs <= tol2) done = 1.0;
+    else if (it >= maxit) done = 2.0;
+  }
+  if (failed) done = kDoneDeviceTimeout;
+  // drain the copies still in flight (the cyclic stream runs ahead of the last iteration)
+  for (int k = 0; k < inflight; ++k) {
+    mbar_wait_bounded(smem_addr(&bars[warp][st]), (phase >> st) & 1u);
+    phase ^= 1u << st;
+    st = (st + 1 == NST) ? 0 : st + 1;
+  }
+  // solution of the owned rows; the final scalars from CTA 0 (identical in every CTA)
+#pragma unroll
+  for (int j = 0; j < MAXS; ++j) {
+    const int row = 32 * (gw + j * nw) + lane;
+    if (j < ns && row < A.n_rows) store3(xg, row, xr[j][0], xr[j][1], xr[j][2]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[kIters] = (double)it;
+    scal[kRR] = rrs;
+    scal[kRz] = rz;
+    scal[kBeta] = beta;
+    scal[kDone] = done;
+  }
+  if (failed && threadIdx.x == 0) scal[kDone] = kDoneDeviceTimeout;
+}
+
+template <typename T, int CB, int NST, int WARPS, int MAXS>
+cudaError_t launch_persistent(const Bsr& A, PcgWork& w, cudaStream_t s, bool query_only, bool* eligible) {
+  using C = PersistentCfg<T, CB, NST, WARPS>;
+  auto kern = pcg_persistent_kernel<T, CB, NST, WARPS, MAXS>;
+  static std::mutex mu;
+  static int blocks_per_sm[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 64) dev = 63;
+  int bps;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!blocks_per_sm[dev]) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmemBytes);
+      int b = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, C::kThreads, C::kSmemBytes);
+      blocks_per_sm[dev] = b > 0 ? b : -1;
+    }
+    bps = blocks_per_sm[dev];
+  }
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  // one wave of co-resident CTAs; the partial buffers hold 2 (part_a) and 4 (part_b) values per CTA
+  int grid = bps > 0 ? w.sms * bps : 0;
+  if (grid > w.grid / 2) grid = w.grid / 2;
+  const int nw = grid * WARPS;
+  *eligible = coop && grid > 0 && (int64_t)nw * MAXS >= A.n_slices;
+  if (query_only || !*eligible) return cudaSuccess;
+  const T* val = (const T*)A.val;
+  const T* minv = (const T*)w.minv;
+  T* xg = (T*)w.x;
+  const T* rg = (const T*)w.r;
+  T* zg = (T*)w.z;
+  T* p0 = (T*)w.p0;
+  T* p1 = (T*)w.p1;
+  Bsr Acopy = A;
+  void* args[] = {&Acopy, &val, &minv, &xg, &rg, &zg, &p0, &p1, &w.part_a, &w.part_b, &w.scal, &w.keep_g};
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(C::kThreads), args, C::kSmemBytes, s);
+}
+
+template <typename T>
+cudaError_t dispatch(int variant, const Bsr& A, PcgWork& w, cudaStream_t s, bool query, bool* eligible) {
+  if constexpr (sizeof(T) == 4) {
+    if (variant == 0) return launch_persistent<float, 8, 2, 8, 4>(A, w, s, query, eligible);
+    return launch_persistent<float, 4, 3, 8, 8>(A, w, s, query, eligible);
+  } else {
+    if (variant == 0) return launch_persistent<double, 4, 2, 8, 4>(A, w, s, query, eligible);
+    return launch_persistent<double, 2, 3, 8, 4>(A, w, s, query, eligible);
+  }
+}
+
+}  // namespace
+
+int pcg_persistent_variants() { return 2; }
+
+bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant) {
+  bool ok = false;
+  if (w.fp32) dispatch<float>(variant, A, w, nullptr, true, &ok);
+  else dispatch<double>(variant, A, w, nullptr, true, &ok);
+  return ok;
+}
+
+cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s) {
+  bool ok = false;
+  cudaError_t e = w.fp32 ? dispatch<float>(variant, A, w, s, false, &ok) : dispatch<double>(variant, A, w, s, false, &ok);
+  if (e == cudaSuccess && !ok) return cudaErrorInvalidConfiguration;
+  return e;
+}
+
+}  // namespace ikr

@@ -173,7 +173,10 @@ __global__ void __launch_bounds__(256) disp_element_kernel(ElemArgs a, const int
   if (WANT_E) psi_tot = sum8(psi);  // last warp-wide operation: inactive lanes may leave after it
 
   if (!active) return;
-  if (bad && a.status) atomicOr(a.status, bad);
+  if (bad) {
+    if (a.inst_status) atomicOr(a.inst_status + a.elem_inst[e], bad);
+    else if (a.status) atomicOr(a.status, bad);
+  }
   if (WANT_E && ELEM_OUT && sub == 0) a.elem_energy[li] = psi_tot;
   if (WANT_R) {
     if (ELEM_OUT) {

@@ -251,10 +251,15 @@ int ikr_fes_set_instances(ikr_fes fes, int32_t n_inst, const int32_t* node_off) 
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
       return node_off[a + 1] - node_off[a] > node_off[b + 1] - node_off[b];  // largest first
     });
+    std::vector<int32_t> elem_inst(fes->ne);
+    for (int e = 0; e < fes->ne; ++e) elem_inst[e] = inst_of[fes->conn_h[8 * e]];
     fes->n_inst = n_inst;
     fes->inst_off_h.assign(node_off, node_off + n_inst + 1);
     fes->inst_off.upload(node_off, n_inst + 1, fes->stream);
     fes->inst_order.upload(order.data(), order.size(), fes->stream);
+    fes->elem_inst.upload(elem_inst.data(), elem_inst.size(), fes->stream);
+    fes->inst_status.alloc(n_inst);
+    CK(cudaMemsetAsync(fes->inst_status.p, 0, sizeof(int) * n_inst, fes->stream));
     CK(cudaStreamSynchronize(fes->stream));
   });
 }
@@ -676,7 +681,8 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
 }
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t kind, double keep) {
   return guarded([&] {
-    need(ls && kind >= -1 && kind <= ikr::spmv_staged_variants() && (keep == -1.0 || (keep >= 0.0 && keep < 1.0)),
+    need(ls && kind >= -1 && kind <= ikr::spmv_staged_variants() + ikr::pcg_persistent_variants() &&
+             (keep == -1.0 || (keep >= 0.0 && keep < 1.0)),
          IKR_ERR_ARG, "invalid SpMV kernel choice");
     ls->set_kernel(kind, keep);
   });
@@ -782,6 +788,9 @@ int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on) {
 namespace ikr_host {
 // Newton-Raphson over independent instances: every instance runs its own Newton iteration and relative
 // convergence test; one assembly and one batched CG launch (CTA per instance) serve all still-active instances.
+// Instances whose elements invert (det C <= 0, or a non-finite state) are taken out of the solve: their element status goes to a
+// per-instance flag, they get no further corrections, count as failed (converged = -1 in the instance info)
+// and do not stop the other instances.  The failures persist until reset_instance_failures.
 static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   ikr_asm a = nr->asm_;
   ikr_fes f = a->fes;
@@ -789,6 +798,26 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   const ikr_nr_settings& st = nr->st;
   const int ni = f->n_inst;
   const int64_t n = a->n;
+  if ((int)nr->inst_failed.size() != ni) nr->inst_failed.assign(ni, 0);
+  struct StatusScope {  // per-instance element status for the duration of the solve
+    ikr_fes f;
+    explicit StatusScope(ikr_fes ff) : f(ff) { f->inst_status_on = true; }
+    ~StatusScope() { f->inst_status_on = false; }
+  } scope(f);
+  std::vector<int> ist(ni);
+  auto collect_failures = [&]() {
+    f->inst_status.download(ist.data(), ni, s);
+    CK(cudaStreamSynchronize(s));
+    bool any_bad = false;
+    for (int i = 0; i < ni; ++i)
+      if (ist[i]) {
+        any_bad = true;
+        if (ist[i] & ~(ikr::kStatusNonPositiveDetC | ikr::kStatusNonFinite))
+          fail(IKR_ERR_ARG, "device status %d in instance %d", ist[i], i);
+        nr->inst_failed[i] = 1;
+      }
+    if (any_bad) CK(cudaMemsetAsync(f->inst_status.p, 0, sizeof(int) * ni, s));
+  };
   nr->corr.alloc(n);
   nr->rhs.alloc(n);
   nr->inst_norm.alloc(ni);
@@ -808,11 +837,12 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
     CK(cudaStreamSynchronize(s));
   };
   assemble_vector(a, r, IKR_DBC_FULL);
+  collect_failures();
   norms();
   r0 = rn;
   for (int i = 0; i < ni; ++i) {
     thr[i] = st.tol_mode == 1 ? st.tol * r0[i] : st.tol;
-    act[i] = rn[i] > thr[i];
+    act[i] = rn[i] > thr[i] && !nr->inst_failed[i];
   }
   if (!a->nb) a->build_pattern();
   nr->ls->setup(a);
@@ -821,6 +851,9 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   auto any = [&] { return std::any_of(act.begin(), act.end(), [](uint8_t v) { return v != 0; }); };
   while ((any() && iter < st.max_iter) || iter < st.min_iter) {
     assemble_matrix(a, r, IKR_DBC_FULL);
+    collect_failures();
+    for (int i = 0; i < ni; ++i)
+      if (nr->inst_failed[i]) act[i] = 0;
     nr->ls->factorize(a);
     for (int i = 0; i < ni; ++i) {
       double e = st.linear_rtol;
@@ -845,18 +878,19 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
     r->version++;
     for (int i = 0; i < ni; ++i) rprev[i] = rn[i];
     assemble_vector(a, r, IKR_DBC_FULL);
+    collect_failures();
     norms();
     for (int i = 0; i < ni; ++i) {
       lin += cgit[i];
       if (act[i]) nr->inst_iters[i]++;
-      act[i] = rn[i] > thr[i] && std::isfinite(rn[i]);
+      act[i] = rn[i] > thr[i] && std::isfinite(rn[i]) && !nr->inst_failed[i];
     }
     ++iter;
   }
   bool ok = true;
   for (int i = 0; i < ni; ++i) {
-    nr->inst_conv[i] = rn[i] <= thr[i];
-    ok = ok && nr->inst_conv[i];
+    nr->inst_conv[i] = nr->inst_failed[i] ? -1 : (rn[i] <= thr[i] ? 1 : 0);
+    ok = ok && nr->inst_conv[i] != 0;
   }
   nr->inst_res = rn;
   ikr_nr_info inf{};
@@ -957,6 +991,7 @@ extern "C" {
 int ikr_newton_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info) {
   return guarded([&] {
     need(nr && r, IKR_ERR_ARG, "null argument");
+    nr->inst_failed.clear();
     nr_solve(nr, r, step_size, info);
   });
 }
@@ -1005,6 +1040,7 @@ int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_in
     notify(IKR_CONTROL_STARTED);
     notify(IKR_STEP_STARTED);
     ikr_nr_info ni{};
+    lc->nr->inst_failed.clear();
     nr_solve(lc->nr, r, 0.0, &ni);  // equilibrium check at the initial load factor (loadcontrol.inl:29-34)
     record(ni);
     if (ni.success) {

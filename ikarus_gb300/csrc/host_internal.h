@@ -135,6 +135,11 @@ struct ikr_fes_s {
   int n_inst = 0;
   std::vector<int32_t> inst_off_h;
   DBuf<int32_t> inst_off, inst_order;
+  // per-instance element status, used instead of `status` while a batched Newton solve runs (an instance
+  // whose elements invert is taken out of that solve instead of failing all instances)
+  DBuf<int32_t> elem_inst;
+  DBuf<int> inst_status;
+  bool inst_status_on = false;
 
   ~ikr_fes_s() {
     if (stream) cudaStreamDestroy(stream);
@@ -159,6 +164,10 @@ struct ikr_fes_s {
     a.status = status.p;
     a.lam_e = lam_e.n ? lam_e.p : nullptr;
     a.mu_e = mu_e.n ? mu_e.p : nullptr;
+    if (inst_status_on) {
+      a.elem_inst = elem_inst.p;
+      a.inst_status = inst_status.p;
+    }
     return a;
   }
 
@@ -526,6 +535,27 @@ struct ikr_ls_s {
       CK(cudaEventElapsedTime(&ms, tev[0], tev[1]));
       return 1e3 * ms / kTimed;
     };
+    // persistent kinds: a solve of kTimed iterations after one untimed solve, per iteration
+    auto time_persistent = [&](int kind, double keep) {
+      apply(kind, keep);
+      constexpr int kTimed = 16;
+      double us = 0.0;
+      for (int rep = 0; rep < 2; ++rep) {
+        ikr::launch_pcg_init(A, w, b64.p, 0.0, kTimed, s);
+        CK(cudaEventRecord(tev[0], s));
+        CK(ikr::launch_pcg_persistent(A, w, kind - first_persistent_kind(), s));
+        CK(cudaEventRecord(tev[1], s));
+        CK(cudaEventSynchronize(tev[1]));
+        count(3);
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+        us = 1e3 * ms / kTimed;
+      }
+      return us;
+    };
+    auto time_kind = [&](int kind, double keep) {
+      return kind >= first_persistent_kind() ? time_persistent(kind, keep) : time_it(kind, keep);
+    };
     int best_kind = spmv_req >= 0 ? spmv_req : 0;
     double best = 1e300;
     if (spmv_req < 0) {
@@ -533,16 +563,26 @@ struct ikr_ls_s {
         const double us = time_it(k, 0.0);
         if (us < best) best = us, best_kind = k;
       }
+      for (int v = 0; v < ikr::pcg_persistent_variants(); ++v) {
+        if (!ikr::pcg_persistent_eligible(A, w, v)) continue;
+        const double us = time_persistent(first_persistent_kind() + v, 0.0);
+        if (us < best) best = us, best_kind = first_persistent_kind() + v;
+      }
+      // the two-kernel CG state was advanced by the persistent trials' inits: restart it for the keep trials
+      ikr::launch_pcg_init(A, w, b64.p, 0.0, 1 << 30, s);
+      count(2);
+    } else if (best_kind >= first_persistent_kind() && !ikr::pcg_persistent_eligible(A, w, best_kind - first_persistent_kind())) {
+      fail(IKR_ERR_ARG, "the persistent CG variant does not fit this system (too many slices per warp)");
     }
     double best_keep = keep_req >= 0.0 ? keep_req : 0.0;
     if (keep_req < 0.0 && best_kind > 0) {
-      best = time_it(best_kind, 0.0);
+      best = time_kind(best_kind, 0.0);
       for (double f : {0.3, 0.45, 0.6, 0.75}) {
-        const double us = time_it(best_kind, f);
+        const double us = time_kind(best_kind, f);
         if (us < best) best = us, best_keep = f;
       }
     } else if (best >= 1e300) {
-      best = time_it(best_kind, best_keep);
+      best = time_kind(best_kind, best_keep);
     }
     apply(best_kind, best_keep);
     tuned_us = best;
@@ -552,9 +592,41 @@ struct ikr_ls_s {
     if (sc[ikr::kDone] == 6.0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the staged SpMV gave up while tuning");
   }
 
+  static int first_persistent_kind() { return 1 + ikr::spmv_staged_variants(); }
+  bool persistent() const { return w.spmv_kind >= first_persistent_kind(); }
+
+  // the whole CG in one cooperative launch: init, persistent kernel, one read of the scalars
+  int solve_persistent(ikr_asm a, const double* b, double* x, double rt, int maxit) {
+    cudaStream_t s = a->fes->stream;
+    const ikr::Bsr A = a->bsr();
+    ikr::launch_pcg_init(A, w, b, rt, maxit, s);
+    count(2);
+    if (profile) CK(cudaEventRecord(tev[0], s));
+    CK(ikr::launch_pcg_persistent(A, w, w.spmv_kind - first_persistent_kind(), s));
+    count(1);
+    if (profile) CK(cudaEventRecord(tev[1], s));
+    CK(cudaMemcpyAsync(scal_h, scal.p, sizeof(double) * ikr::kNScal, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const double done = scal_h[ikr::kDone];
+    last_iters = (int)scal_h[ikr::kIters];
+    last_rel = scal_h[ikr::kBB] > 0 ? std::sqrt(scal_h[ikr::kRR] / scal_h[ikr::kBB]) : 0.0;
+    if (profile) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+      prof_ms += ms;
+      prof_n += last_iters;
+    }
+    ikr::launch_pcg_result(w, x, 1.0, s);
+    count(1);
+    if (done == 6.0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the persistent CG gave up");
+    if (done == 3.0) fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp zero or not finite) after %d iterations", last_iters);
+    return last_iters;
+  }
+
   // x = K^{-1} b on the device (FP64 in / out); returns CG iterations
   int solve_device(ikr_asm a, const double* b, double* x, double rt, int maxit) {
     if (!factorized || asm_ != a) fail(IKR_ERR_INVALID_STATE, "linear solver not factorized for this assembler");
+    if (persistent()) return solve_persistent(a, b, x, rt, maxit);
     cudaStream_t s = a->fes->stream;
     const ikr::Bsr A = a->bsr();
     build_chunk(s);
@@ -630,7 +702,8 @@ struct ikr_nr_s {
   // per-instance state of the last solve (element sets with instances)
   std::vector<int32_t> inst_iters;
   std::vector<double> inst_res;
-  std::vector<uint8_t> inst_conv;
+  std::vector<int8_t> inst_conv;     // 1 converged, 0 not, -1 taken out after an element inversion
+  std::vector<uint8_t> inst_failed;  // inversions seen since the last reset (LoadControl::run, newton_solve)
   DBuf<double> inst_norm, inst_rtol;
   DBuf<uint8_t> inst_active;
   DBuf<int32_t> inst_cg_iters;
@@ -643,27 +716,24 @@ struct ikr_lc_s {
   double t0 = 0, t1 = 1;
   std::vector<ControlObserver> obs;
   // Newton predictor of each load step (the reference only increments the load factor,
-  // loadcontrol.inl:54-57): 0 = none, 1 = previous increment, 2 = learned; every prediction is kept only when
-  // its FP64 residual is below that of the unpredicted state.  `record` appends each converged increment to
-  // the predictor's training snapshots.
+  // loadcontrol.inl:54-57): 0 = none, 1 = previous increment, 2 = learned, which falls back to the previous
+  // increment when its FP64 residual is not smaller (predictor.cpp).  `record` appends each converged
+  // increment to the predictor's training snapshots.
   int pred_kind = 0;
   ikr_pred pred = nullptr;
   std::vector<double> theta;  // load parameters of the current path (learned predictor features)
   bool record = false;
   int path_id = 0;
   int accepted = 0, rejected = 0;
-  // gate of a prediction: 0 = FP64 residual norm at the candidate states; 1 = FP64 residual norm after one
-  // truncated Newton step (relax_iters CG iterations) from each candidate; 2 = none (always kept)
-  int gate = 0;
-  int relax_iters = 30;
-  int64_t gate_cg = 0;  // CG iterations the gate spent in the last run
-  DBuf<double> u_step0, u_try, pred_part, pred_out, r0vec, g_rhs, g_corr;
+  bool gated = true;  // the learned candidate must beat its fallback's FP64 residual norm
+  DBuf<double> u_step0, u_try, pred_part, pred_out;
   DBuf<float> du1, du2;  // last two converged increments (FP32)
   int hist = 0;          // how many increments are in du1 / du2
-  // per load step of the last run: FP64 residual norms of the unpredicted state, of the full prediction and
-  // of the prediction scaled by the residual-minimising step s*, and the step length kept (0 = unpredicted)
+  // per load step of the last run: FP64 residual norms of the unpredicted state, of the previous-increment
+  // candidate and of the learned candidate (-1 when not evaluated, inf when an element inverted), and the
+  // state kept (0 unpredicted, 1 previous increment, 2 learned)
   struct PredRecord {
-    double step, r_plain, r_full, s_star, r_scaled, s_used;
+    double step, r_plain, r_fallback, r_learned, kept, spare;
   };
   std::vector<PredRecord> phist;
 };

@@ -47,6 +47,9 @@ struct ElemArgs {
   double* elem_mat = nullptr;      // element-level: 576 per listed element, column-major
   double* elem_energy = nullptr;   // element-level: 1 per listed element
   int* status = nullptr;           // StatusBits, OR-ed
+  // batched solves: the status of an element goes to its instance, inst_status[elem_inst[e]], instead
+  const int32_t* elem_inst = nullptr;
+  int* inst_status = nullptr;
 };
 
 // The tangent's 3x3 blocks are stored sliced-ELL: block rows (nodes) are grouped in slices of 32; slice s
@@ -135,7 +138,8 @@ struct PcgWork {
   double* scal = nullptr;      // device scalars, see solver.cu
   int grid = 0;                // fixed grid (multiple of the SM count) for the partial-producing kernels
   int sms = 0;                 // SM count of the device
-  int spmv_kind = 0;           // 0: direct loads (solver.cu); 1 + v: staged variant v (spmv_staged.cu)
+  int spmv_kind = 0;           // 0: direct loads (solver.cu); 1 + v: staged variant v (spmv_staged.cu);
+                               // 1 + staged variants + v: persistent CG variant v (cg_persistent.cu)
   int64_t keep_g = 0;          // staged: matrix blocks [0, keep_g) are copied with an L2 evict_last policy
 };
 void launch_block_jacobi(const Bsr& A, bool fp32, void* minv, bool point_jacobi, cudaStream_t s);
@@ -151,6 +155,11 @@ int spmv_staged_variants();
 const char* spmv_staged_name(bool fp32, int variant);
 void launch_pcg_spmv_staged(const Bsr& A, PcgWork& w, int variant, const void* pold, void* pnew, cudaStream_t s);
 void launch_fill64(double* y, double v, int64_t n, cudaStream_t s);
+// cg_persistent.cu -- the whole CG solve (after launch_pcg_init) in one cooperative launch; the result in w.x
+// and the scalars as after the two-kernel iterations
+int pcg_persistent_variants();
+bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant);
+cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s);
 
 // batched.cu -- independent instances (disjoint contiguous node ranges) of one element set
 // one CTA per instance runs the instance's whole block-Jacobi PCG; inactive instances get a zero correction;

@@ -3,9 +3,10 @@
 // reference, whose LoadControl predictor only increments the load factor (loadcontrol.inl:54-57).
 //
 // Features of load step k: the path's load parameters, the new load factor and the POD coordinates of the two
-// previous converged increments; target: the POD coordinates of increment k.  Prediction = u + Phi * MLP(...);
-// the predicted state is kept only if its FP64 residual is smaller than that of the unpredicted state, and the
-// Newton test of the step stays relative to the unpredicted residual, so the predictor can only save iterations.
+// previous converged increments; target: the change of the increment's POD coordinates from step k-1 to k (the
+// increment itself on a path's first step).  Prediction = u + du_{k-1} + Phi * MLP(...); it is kept only if its
+// FP64 residual is smaller than that of the previous-increment prediction u + du_{k-1} (its fallback), and the
+// Newton test of the step stays relative to the residual of the unpredicted state.
 #include <cstring>
 #include <random>
 
@@ -382,20 +383,21 @@ void pod_build(ikr_pred p, cudaStream_t s) {
 void predictor_begin(ikr_lc lc, ikr_req r) {
   lc->hist = 0;
   lc->phist.clear();
-  lc->gate_cg = 0;
   if (lc->pred_kind == 0 && !lc->record) return;
   const int64_t n = 3LL * r->fes->nn;
   lc->u_step0.alloc(n);
   lc->u_try.alloc(n);
   lc->du1.alloc(n);
   lc->du2.alloc(n);
-  lc->r0vec.alloc(n);
 }
 
-// The prediction d is tried along its own direction: with R0 = R(u0) and R1 = R(u0 + d), the linearised
-// residual R(u0 + s d) ~ R0 + s (R1 - R0) has the least norm at s* = (R0.R0 - R0.R1) / |R1 - R0|^2.  The kept
-// state is the one of {u0, u0 + d, u0 + s* d} with the smallest FP64 residual norm, so a prediction never
-// starts Newton from a state whose residual is worse than the unpredicted one.
+// Candidates of a load step (u0 = converged state of the previous step at the new load factor):
+//   previous increment  u0 + du1 (the "previous-step" predictor; needs one recorded increment)
+//   learned             u0 + du1 + Phi c (kind 2: the network predicts the POD coordinates c of the change of
+//                       the increment; on the first step, without du1, it predicts the increment itself)
+// A candidate whose residual assembly meets det C <= 0 is discarded.  Kind 1 keeps the previous increment;
+// kind 2 keeps the learned candidate only when its FP64 residual norm is below that of its fallback (the
+// previous increment, or the unpredicted state on the first step), unless the gate is off.
 double predictor_apply(ikr_lc lc, ikr_req r, int step) {
   ikr_fes f = r->fes;
   cudaStream_t s = f->stream;
@@ -406,11 +408,25 @@ double predictor_apply(ikr_lc lc, ikr_req r, int step) {
   ikr_asm a = lc->nr->asm_;
   assemble_vector(a, r, IKR_DBC_FULL);
   const double r_plain = device_norm(f, a->R.p, n, lc->pred_part, lc->pred_out);
-  ikr_lc_s::PredRecord rec{(double)step, r_plain, -1.0, 0.0, -1.0, 0.0};
-  const float* d = nullptr;
-  if (lc->pred_kind == 1 && lc->hist >= 1) {
-    d = lc->du1.p;
-  } else if (lc->pred_kind == 2 && lc->pred && lc->pred->trained) {
+  ikr_lc_s::PredRecord rec{(double)step, r_plain, -1.0, -1.0, 0.0, 0.0};
+  // FP64 residual norm at u0 + d (+ du1); +inf when an element inverts
+  auto residual_at = [&](const float* d, bool plus_du1) -> double {
+    ikr::launch_base_plus_scaled(r->u.p, lc->u_step0.p, d, 1.0, n, s);
+    if (plus_du1) ikr::launch_add_f32(r->u.p, lc->du1.p, n, s);
+    count(plus_du1 ? 2 : 1);
+    r->version++;
+    try {
+      assemble_vector(a, r, IKR_DBC_FULL);
+    } catch (const IkrError& e) {
+      if (e.code != IKR_ERR_NONPOSITIVE_DETC) throw;
+      return INFINITY;
+    }
+    return device_norm(f, a->R.p, n, lc->pred_part, lc->pred_out);
+  };
+  const bool has_prev = lc->hist >= 1;
+  if (has_prev) rec.r_fallback = residual_at(lc->du1.p, false);
+  const float* dl = nullptr;
+  if (lc->pred_kind == 2 && lc->pred && lc->pred->trained) {
     ikr_pred p = lc->pred;
     p->c1.alloc(p->k), p->c2.alloc(p->k), p->cpred.alloc(p->k), p->dvec.alloc(n);
     std::vector<float> c1h(p->k, 0.f), c2h(p->k, 0.f);
@@ -437,91 +453,31 @@ double predictor_apply(ikr_lc lc, ikr_req r, int step) {
     ikr::launch_gemm(1, (int)n, p->k, p->cpred.p, false, false, p->k, p->phi.p, false, false, (int)n, p->dvec.p,
                      (int)n, 1.f, 0.f, s);
     count(1);
-    d = p->dvec.p;
+    dl = p->dvec.p;
+    rec.r_learned = residual_at(dl, has_prev);
   }
-  if (!d) {
-    lc->phist.push_back(rec);
-    return r_plain;
-  }
-  if (lc->gate == 2) {  // ungated
-    ikr::launch_base_plus_scaled(r->u.p, lc->u_step0.p, d, 1.0, n, s);
-    count(1);
-    r->version++;
-    rec.s_used = 1.0;
-    lc->accepted++;
-    lc->phist.push_back(rec);
-    return r_plain;
-  }
-  if (lc->gate == 1) {
-    // one truncated Newton step from a state: tangent, block-Jacobi CG limited to relax_iters iterations,
-    // update; returns the FP64 residual norm at the updated state
-    ikr_ls ls = lc->nr->ls;
-    lc->g_rhs.alloc(n), lc->g_corr.alloc(n), lc->u_try.alloc(n);
-    auto relax = [&]() {
-      assemble_matrix(a, r, IKR_DBC_FULL);
-      ls->factorize(a);
-      assemble_vector(a, r, IKR_DBC_FULL);
-      ikr::launch_scale64(lc->g_rhs.p, a->R.p, -1.0, n, s);
-      lc->gate_cg += ls->solve(a, lc->g_rhs.p, lc->g_corr.p, 1e-12, lc->relax_iters, 0);
-      ikr::launch_axpy64(r->u.p, lc->g_corr.p, 1.0, n, s);
-      count(2);
-      r->version++;
-      assemble_vector(a, r, IKR_DBC_FULL);
-      return device_norm(f, a->R.p, n, lc->pred_part, lc->pred_out);
-    };
-    rec.r_scaled = relax();  // from the unpredicted state
-    CK(cudaMemcpyAsync(lc->u_try.p, r->u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    ikr::launch_base_plus_scaled(r->u.p, lc->u_step0.p, d, 1.0, n, s);
-    count(1);
-    r->version++;
-    rec.r_full = relax();  // from the prediction
-    if (rec.r_full < rec.r_scaled) {
-      rec.s_used = 1.0;
-      lc->accepted++;
-    } else {
-      CK(cudaMemcpyAsync(r->u.p, lc->u_try.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-      r->version++;
-      rec.s_used = 0.0;
-      lc->rejected++;
+  const double r_fb = has_prev ? rec.r_fallback : r_plain;
+  int keep = 0;  // 0 unpredicted, 1 previous increment, 2 learned
+  if (has_prev && std::isfinite(rec.r_fallback)) keep = 1;
+  if (dl && std::isfinite(rec.r_learned) && (!lc->gated || rec.r_learned < r_fb)) keep = 2;
+  // leave u at the kept state (the last one evaluated may be another)
+  const int last = dl ? 2 : (has_prev ? 1 : 0);
+  if (keep != last) {
+    if (keep == 0) {
+      CK(cudaMemcpyAsync(r->u.p, lc->u_step0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    } else if (keep == 1) {
+      ikr::launch_base_plus_scaled(r->u.p, lc->u_step0.p, lc->du1.p, 1.0, n, s);
+      count(1);
     }
-    rec.s_star = -1.0;
-    lc->phist.push_back(rec);
-    return r_plain;
-  }
-  CK(cudaMemcpyAsync(lc->r0vec.p, a->R.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  auto try_state = [&](double sc) {
-    ikr::launch_base_plus_scaled(r->u.p, lc->u_step0.p, d, sc, n, s);
-    count(1);
     r->version++;
-    assemble_vector(a, r, IKR_DBC_FULL);
-    return device_norm(f, a->R.p, n, lc->pred_part, lc->pred_out);
-  };
-  double best_s = 0.0, best_r = r_plain;
-  rec.r_full = try_state(1.0);
-  if (rec.r_full < best_r) best_s = 1.0, best_r = rec.r_full;
-  const double r01 = device_dot(f, lc->r0vec.p, a->R.p, n, lc->pred_part, lc->pred_out);
-  const double dd = rec.r_full * rec.r_full - 2.0 * r01 + r_plain * r_plain;  // |R1 - R0|^2
-  if (dd > 0.0) {
-    rec.s_star = (r_plain * r_plain - r01) / dd;
-    if (rec.s_star > 0.02 && rec.s_star < 2.0 && std::fabs(rec.s_star - 1.0) > 0.02) {
-      rec.r_scaled = try_state(rec.s_star);
-      if (rec.r_scaled < best_r) best_s = rec.s_star, best_r = rec.r_scaled;
-    }
   }
-  rec.s_used = best_s;
-  if (best_s != 0.0) {
-    lc->accepted++;
-  } else {  // fall back to the unpredicted state
-    lc->rejected++;
-  }
-  // leave u at the kept state (the last state tried may be another one)
-  if (best_s == 0.0) {
-    CK(cudaMemcpyAsync(r->u.p, lc->u_step0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    r->version++;
-  } else if (best_s != (rec.r_scaled >= 0.0 ? rec.s_star : 1.0)) {
-    ikr::launch_base_plus_scaled(r->u.p, lc->u_step0.p, d, best_s, n, s);
-    count(1);
-    r->version++;
+  rec.kept = keep;
+  if (lc->pred_kind == 2) {
+    if (keep == 2) lc->accepted++;
+    else lc->rejected++;
+  } else {
+    if (keep == 1) lc->accepted++;
+    else lc->rejected++;
   }
   lc->phist.push_back(rec);
   return r_plain;
@@ -663,7 +619,7 @@ int ikr_predictor_fit(ikr_pred p, int32_t epochs, int32_t batch, float lr, float
     std::vector<float> Ch((size_t)k * m);
     C.download(Ch.data(), Ch.size(), s);
     CK(cudaStreamSynchronize(s));
-    // samples: features from the same path's previous two increments
+    // samples: features from the same path's previous two increments; targets the change of the increment
     std::vector<float> X((size_t)m * nin), T((size_t)m * k);
     std::vector<float> col1(k), col2(k);
     for (int j = 0; j < m; ++j) {
@@ -673,7 +629,8 @@ int ikr_predictor_fit(ikr_pred p, int32_t epochs, int32_t batch, float lr, float
       for (int i = 0; i < k; ++i) {
         col1[i] = h1 ? Ch[(size_t)i * m + j - 1] : 0.f;
         col2[i] = h2 ? Ch[(size_t)i * m + j - 2] : 0.f;
-        T[(size_t)j * k + i] = Ch[(size_t)i * m + j];
+        // target: the change of the increment's POD coordinates (the increment itself on a path's first step)
+        T[(size_t)j * k + i] = Ch[(size_t)i * m + j] - col1[i];
       }
       const std::vector<float> x = features(p, p->theta[mt.path], mt.lambda, col1.data(), col2.data());
       std::copy(x.begin(), x.end(), X.begin() + (size_t)j * nin);
@@ -735,19 +692,10 @@ int ikr_load_control_set_predictor(ikr_lc lc, int32_t kind, ikr_pred p, const do
     }
   });
 }
-int ikr_load_control_set_predictor_gate(ikr_lc lc, int32_t gate, int32_t relax_iters) {
+int ikr_load_control_set_predictor_gate(ikr_lc lc, int32_t gated) {
   return guarded([&] {
-    need(lc && gate >= 0 && gate <= 2 && relax_iters > 0, IKR_ERR_ARG, "invalid predictor gate");
-    need(gate != 1 || lc->nr->asm_->fes->na == 0, IKR_ERR_NOT_IMPLEMENTED,
-         "the relaxed gate supports displacement-based elements");
-    lc->gate = gate;
-    lc->relax_iters = relax_iters;
-  });
-}
-int ikr_load_control_predictor_gate_cg(ikr_lc lc, int64_t* cg_iterations) {
-  return guarded([&] {
-    need(lc && cg_iterations, IKR_ERR_ARG, "null argument");
-    *cg_iterations = lc->gate_cg;
+    need(lc, IKR_ERR_ARG, "null argument");
+    lc->gated = gated != 0;
   });
 }
 int ikr_load_control_predictor_history(ikr_lc lc, int32_t capacity, double* out, int32_t* n) {
@@ -757,7 +705,7 @@ int ikr_load_control_predictor_history(ikr_lc lc, int32_t capacity, double* out,
     const int m = std::min<int>(capacity, (int)lc->phist.size());
     for (int i = 0; i < m; ++i) {
       const auto& h = lc->phist[i];
-      const double v[6] = {h.step, h.r_plain, h.r_full, h.s_star, h.r_scaled, h.s_used};
+      const double v[6] = {h.step, h.r_plain, h.r_fallback, h.r_learned, h.kept, 0.0};
       std::copy(v, v + 6, out + 6 * i);
     }
   });

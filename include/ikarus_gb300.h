@@ -175,9 +175,11 @@ int ikr_linear_solver_profile_read(ikr_ls ls, double* spmv_ms_total, int64_t* sp
  * (1..256, default 16) between host convergence polls, captured as CUDA graphs when use_graphs != 0
  * (default) or launched kernel by kernel otherwise (for profilers that do not follow graph kernels). */
 int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_len);
-/* SpMV kernel of the CG (no reference counterpart).  spmv_kind 0 = direct loads, 1..4 = bulk-copy staged
- * variants (chunk size / pipeline depth / warps per block), -1 = autotune; l2_keep_fraction in [0, 1) = share
- * of the matrix the staged kernels keep in L2 across iterations, -1 = autotune.  The choice is made at the
+/* CG kernels (no reference counterpart).  spmv_kind 0 = two kernels per iteration with a direct-load SpMV,
+ * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..6 = the
+ * whole solve in one persistent cooperative kernel (grid barriers for the two reductions of an iteration;
+ * only where every warp's rows fit its registers), -1 = autotune; l2_keep_fraction in [0, 1) = share of the
+ * matrix the staged kernels keep in L2 across iterations, -1 = autotune.  The choice is made at the
  * next factorize from timed CG iterations on the assembled tangent and kept for that assembler.  info
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fraction);
@@ -240,7 +242,10 @@ int ikr_newton_subscribe(ikr_nr nr, ikr_nr_observer cb, void* user);
 int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on);
 /* solve(x, stepSize) (newtonraphson.hh:193-257) */
 int ikr_newton_solve(ikr_nr nr, ikr_req req, double step_size, ikr_nr_info* info);
-/* per instance (batched solves): Newton iterations, final residual norm and convergence of the last solve */
+/* per instance (batched solves): Newton iterations, final residual norm and convergence of the last solve
+ * (1 converged, 0 not converged, -1 taken out after its elements inverted, det C <= 0 -- the reference aborts
+ * there; here the other instances go on and the solve succeeds when all instances not taken out converge).
+ * Instances taken out stay out for the rest of a LoadControl run. */
 int ikr_newton_instance_info(ikr_nr nr, int32_t* iterations, double* residual_norms, int32_t* converged);
 
 /* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
@@ -278,20 +283,15 @@ typedef struct ikr_mlp_s* ikr_mlp;
 int ikr_load_control_set_predictor(ikr_lc lc, int32_t kind, ikr_pred pred, const double* params, int32_t record);
 /* predictions kept / rejected by the residual test since the predictor was set */
 int ikr_load_control_predictor_stats(ikr_lc lc, int32_t* accepted, int32_t* rejected);
-/* per load step of the last run, 6 doubles: step, FP64 residual norm of the unpredicted state, of the full
- * prediction (-1 if none), the residual-minimising step length s* along the prediction, the residual norm at
- * s* (-1 if not tried) and the step length kept (0 = unpredicted state).  n returns the number of steps;
- * at most capacity rows are written. */
+/* per load step of the last run, 6 doubles: step, FP64 residual norm of the unpredicted state, of the
+ * previous-increment candidate, of the learned candidate (-1 when not evaluated, inf when an element
+ * inverted), the state kept (0 unpredicted, 1 previous increment, 2 learned) and 0.  n returns the number of
+ * steps; at most capacity rows are written. */
 int ikr_load_control_predictor_history(ikr_lc lc, int32_t capacity, double* out, int32_t* n);
-/* How a prediction is judged (no reference counterpart): gate 0 (default) keeps the state with the smaller
- * FP64 residual norm among the unpredicted state, the prediction and the prediction scaled by its
- * residual-minimising step; gate 1 takes one truncated Newton step (tangent + relax_iters block-Jacobi CG
- * iterations) from the unpredicted state and from the prediction and keeps the one with the smaller FP64
- * residual norm (displacement-based elements only); gate 2 keeps every prediction.  In the history of gate
- * 1, column 2 is the residual after the step from the prediction and column 4 after the step from the
- * unpredicted state.  gate_cg returns the CG iterations the gate spent in the last run. */
-int ikr_load_control_set_predictor_gate(ikr_lc lc, int32_t gate, int32_t relax_iters);
-int ikr_load_control_predictor_gate_cg(ikr_lc lc, int64_t* cg_iterations);
+/* gated != 0 (default): the learned candidate is kept only when its FP64 residual norm is below that of its
+ * fallback (the previous increment, the unpredicted state on the first step); 0: kept whenever no element
+ * inverts (no reference counterpart) */
+int ikr_load_control_set_predictor_gate(ikr_lc lc, int32_t gated);
 /* POD (n_modes) + MLP (depth hidden layers of width, GELU, BF16 weights, FP32 accumulation) over the
  * features [params, load factor, POD coordinates of the previous two increments]; snapshots: up to capacity
  * increments of the element set's dofs, held on the device in FP32. */

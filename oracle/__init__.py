@@ -58,6 +58,7 @@ def lib():
         L.orc_pattern_nnz.argtypes = [vp, C.c_int]
         L.orc_reduced_size.argtypes = [vp]
         L.orc_assemble_matrix_csc.argtypes = [vp, dp, C.c_double, C.c_int, lp, ip, dp]
+        L.orc_cg_jacobi_csc.argtypes = [C.c_int, lp, ip, dp, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
                                        C.c_double, dp, dp, ip, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib = L
@@ -71,6 +72,22 @@ def _p(a, t):
 def _check(code, what):
     if code != 0:
         raise OracleError(code, what)
+
+
+def cg_jacobi(col_ptr, row_idx, values, b, rtol, max_iter):
+    """The oracle's Jacobi-preconditioned CG on a CSC matrix: (x, iterations, converged)."""
+    n = len(col_ptr) - 1
+    cp = np.ascontiguousarray(col_ptr, dtype=np.int64)
+    ri = np.ascontiguousarray(row_idx, dtype=np.int32)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros(n)
+    its = C.c_int(0)
+    code = lib().orc_cg_jacobi_csc(n, _p(cp, C.c_int64), _p(ri, C.c_int32), _p(v, C.c_double), _p(bb, C.c_double),
+                                   _p(x, C.c_double), rtol, max_iter, C.byref(its))
+    if code not in (0, -5):
+        raise OracleError(code, "cg_jacobi")
+    return x, its.value, code == 0
 
 
 def from_problem(p, faithful=False):

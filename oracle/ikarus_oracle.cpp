@@ -784,7 +784,8 @@ bool banded_ldlt_solve(const CSC& A, const std::vector<double>& b, std::vector<d
 
 // Jacobi-preconditioned CG (the reference's si_ConjugateGradient: Eigen ConjugateGradient with its
 // default diagonal preconditioner, linearsolver.cpp:23-25), relative tolerance on ||r||/||b||.
-bool cg_jacobi_solve(const CSC& A, const std::vector<double>& b, std::vector<double>& x, double rtol, int maxit) {
+bool cg_jacobi_solve(const CSC& A, const std::vector<double>& b, std::vector<double>& x, double rtol, int maxit,
+                     int* iterations = nullptr) {
   const int n = A.n;
   std::vector<double> diag(n, 1.0), r(b), z(n), pv(n), q(n);
   for (int c = 0; c < n; ++c)
@@ -814,6 +815,7 @@ bool cg_jacobi_solve(const CSC& A, const std::vector<double>& b, std::vector<dou
       r[i] -= al * q[i];
       rn += r[i] * r[i];
     }
+    if (iterations) *iterations = it + 1;
     if (std::sqrt(rn) <= rtol * bn) return true;
     double rzn = 0;
     for (int i = 0; i < n; ++i) {
@@ -965,6 +967,21 @@ int64_t orc_pattern_nnz(orc_problem* p, int dbc) {
   CSC A;
   build_pattern(*p, dbc, A);
   return (int64_t)A.ri.size();
+}
+int orc_cg_jacobi_csc(int n, const int64_t* col_ptr, const int32_t* row_idx, const double* values, const double* b,
+                      double* x, double rtol, int max_iter, int* iterations) {
+  if (n <= 0 || !col_ptr || !row_idx || !values || !b || !x) return ORC_ERR_ARG;
+  CSC A;
+  A.n = n;
+  A.cp.assign(col_ptr, col_ptr + n + 1);
+  A.ri.assign(row_idx, row_idx + col_ptr[n]);
+  A.v.assign(values, values + col_ptr[n]);
+  std::vector<double> bv(b, b + n), xv;
+  int its = 0;
+  const bool ok = cg_jacobi_solve(A, bv, xv, rtol, max_iter, &its);
+  std::copy(xv.begin(), xv.end(), x);
+  if (iterations) *iterations = its;
+  return ok ? ORC_OK : ORC_ERR_NOT_CONVERGED;
 }
 int orc_reduced_size(orc_problem* p) {
   if (!p) return ORC_ERR_ARG;

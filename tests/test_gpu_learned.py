@@ -48,8 +48,8 @@ def _run(ikr, p, fes, asm, theta, kind=0, pred=None, record=False):
     lc.set_predictor(kind, pred, theta, record)
     info = lc.run(req)
     if kind:
-        # per step: |R| unpredicted, |R| full prediction, s*, |R| at s*, kept step length
-        print(np.array2string(lc.predictor_history()[:, 1:], precision=3))
+        # per step: |R| unpredicted, |R| previous increment, |R| learned, kept (0 none, 1 previous, 2 learned)
+        print(np.array2string(lc.predictor_history()[:, 1:5], precision=3))
     return info, req.globalSolution(), lc.predictor_stats()
 
 
@@ -64,15 +64,19 @@ def test_learned_predictor_saves_newton_iterations(ikr):
     assert pred.num_snapshots() == 300
     loss, energy = pred.fit(epochs=400, batch=32, lr=1e-3)
     assert energy > 0.99
-    plain_its, learned_its = 0, 0
+    plain_its, prev_its, learned_its = 0, 0, 0
     for _ in range(5):
         theta = problems.sample_load_parameters(rng)
         info0, u0, _ = _run(ikr, p, fes, asm, theta, kind=0)
+        info1, u1, _ = _run(ikr, p, fes, asm, theta, kind=1)
         info2, u2, (acc, rej) = _run(ikr, p, fes, asm, theta, kind=2, pred=pred)
-        assert info0.success and info2.success
-        # both reach the FP64 tolerance; the converged paths agree
+        assert info0.success and info1.success and info2.success
+        # all reach the FP64 tolerance; the converged paths agree
         assert np.abs(u2 - u0).max() <= 1e-5 * np.abs(u0).max()
         plain_its += info0.totalIterations
+        prev_its += info1.totalIterations
         learned_its += info2.totalIterations
         assert acc + rej == p.load_steps
+    print(f"Newton iterations over 5 held-out paths: none {plain_its}, previous increment {prev_its}, "
+          f"learned {learned_its}")
     assert learned_its < plain_its

@@ -139,3 +139,19 @@ def test_reduced_is_full_restricted():
     Rf = o.assemble_vector(u, 0.3, oracle.DBC_FULL)
     Rr = o.assemble_vector(u, 0.3, oracle.DBC_REDUCED)
     assert np.array_equal(Rf[free], Rr) and not Rf[fx].any()
+
+
+def test_oracle_cg_matches_a_direct_solve():
+    """The oracle's Jacobi-preconditioned CG (the reference's si_ConjugateGradient, the CPU baseline's CG) solves
+    the assembled Full-DBC tangent to its tolerance."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+
+    p = problems.cantilever(8, 2, 2, jitter=0.1, seed=4)
+    o = oracle.from_problem(p)
+    cp, ri, v, n = o.assemble_matrix_csc(None, 0.0)
+    b = np.random.default_rng(0).standard_normal(n) * (1 - p.fixed)
+    x, its, ok = oracle.cg_jacobi(cp, ri, v, b, 1e-12, 5000)
+    A = sp.csc_matrix((v, ri, cp), shape=(n, n))
+    assert ok and 0 < its < 5000
+    assert np.abs(x - sla.spsolve(A, b)).max() <= 1e-8 * np.abs(x).max()
