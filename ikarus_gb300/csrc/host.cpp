@@ -788,6 +788,57 @@ int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on) {
 namespace ikr_host {
 // Newton-Raphson over independent instances: every instance runs its own Newton iteration and relative
 // convergence test; one assembly and one batched CG launch (CTA per instance) serve all still-active instances.
+// CTA groups of the batched CG: instance i gets C_i CTAs, C_i ~ its node count, with every group's CTAs
+// co-resident (sum C_i <= the device's resident CTAs of the kernel) and at least 64 rows per CTA; largest
+// instances first.  When every C_i is 1 (or there are more instances than resident CTAs) the launch is an
+// ordinary one.
+static void build_batch_plan(ikr_nr nr, ikr_fes f, bool fp32) {
+  auto& P = nr->plan;
+  if (P.fes == f && P.fp32 == fp32 && P.n_cta > 0) return;
+  const int ni = f->n_inst;
+  const int cap = ikr::batched_pcg_capacity(fp32, num_sms());
+  std::vector<int> nodes(ni), c(ni, 1), order(ni);
+  for (int i = 0; i < ni; ++i) nodes[i] = f->inst_off_h[i + 1] - f->inst_off_h[i], order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nodes[a] > nodes[b]; });
+  auto sizes_for = [&](int64_t q, std::vector<int>& out) {
+    int64_t tot = 0;
+    for (int i = 0; i < ni; ++i) {
+      int64_t ci = (nodes[i] + q - 1) / q;
+      ci = std::min<int64_t>(ci, std::max(1, nodes[i] / 64));
+      ci = std::max<int64_t>(1, std::min<int64_t>(ci, 32));
+      out[i] = (int)ci;
+      tot += ci;
+    }
+    return tot;
+  };
+  if (ni < cap) {
+    int64_t lo = 1, hi = *std::max_element(nodes.begin(), nodes.end()) + 1;
+    std::vector<int> tmp(ni);
+    while (lo < hi) {  // smallest rows-per-CTA q whose groups fit the resident CTAs
+      const int64_t mid = (lo + hi) / 2;
+      if (sizes_for(mid, tmp) <= cap) hi = mid;
+      else lo = mid + 1;
+    }
+    sizes_for(lo, c);
+  }
+  std::vector<int32_t> ci, cf, cs;
+  for (int i : order) {
+    const int first = (int)ci.size();
+    for (int k = 0; k < c[i]; ++k) ci.push_back(i), cf.push_back(first), cs.push_back(c[i]);
+  }
+  P.fes = f;
+  P.fp32 = fp32;
+  P.n_cta = (int)ci.size();
+  P.cooperative = std::any_of(c.begin(), c.end(), [](int v) { return v > 1; });
+  cudaStream_t s = f->stream;
+  P.cta_inst.upload(ci.data(), ci.size(), s);
+  P.cta_first.upload(cf.data(), cf.size(), s);
+  P.cta_size.upload(cs.data(), cs.size(), s);
+  P.part.alloc(4 * (size_t)P.n_cta);
+  P.counters.alloc(ni);
+  CK(cudaStreamSynchronize(s));
+}
+
 // Instances whose elements invert (det C <= 0, or a non-finite state) are taken out of the solve: their element status goes to a
 // per-instance flag, they get no further corrections, count as failed (converged = -1 in the instance info)
 // and do not stop the other instances.  The failures persist until reset_instance_failures.
@@ -868,11 +919,17 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
     nr->inst_active.upload(act.data(), ni, s);
     ikr::launch_scale64(nr->rhs.p, a->R.p, -1.0, n, s);
     ikr::PcgWork& w = nr->ls->w;
-    ikr::launch_batched_pcg(a->bsr(), a->fp32, w.minv, nr->rhs.p, nr->corr.p, ni, f->inst_off.p, f->inst_order.p,
-                            nr->inst_active.p, w.x, w.r, w.z, w.p0, w.q, nr->inst_rtol.p, st.linear_max_iter,
-                            nr->inst_cg_iters.p, nr->inst_cg_res.p, s);
-    count(2);
+    build_batch_plan(nr, f, a->fp32);
+    const auto& P = nr->plan;
+    CK(ikr::launch_batched_pcg(a->bsr(), a->fp32, w.minv, nr->rhs.p, nr->corr.p, P.n_cta, f->inst_off.p,
+                               P.cta_inst.p, P.cta_first.p, P.cta_size.p, nr->inst_active.p, w.x, w.r, w.z, w.p0, w.p1,
+                               w.q, nr->inst_rtol.p, st.linear_max_iter, nr->inst_cg_iters.p, nr->inst_cg_res.p,
+                               P.part.p, P.counters.p, ni, P.cooperative, s));
+    count(3);
     nr->inst_cg_iters.download(cgit.data(), ni, s);
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < ni; ++i)
+      if (cgit[i] < 0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the batched CG gave up (instance %d)", i);
     ikr::launch_axpy64(r->u.p, nr->corr.p, 1.0, n, s);
     count(1);
     r->version++;

@@ -489,7 +489,7 @@ struct ikr_ls_s {
     ikr::launch_block_jacobi(a->bsr(), fp32, w.minv, tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT, a->fes->stream);
     count(1);
     factorized = true;
-    if (tuned_for != a) tune(a);
+    if (tag != IKR_SOLVER_GPU_PCG_BATCHED && tuned_for != a) tune(a);
   }
 
   void set_kernel(int kind, double keep) {
@@ -708,6 +708,16 @@ struct ikr_nr_s {
   DBuf<uint8_t> inst_active;
   DBuf<int32_t> inst_cg_iters;
   DBuf<double> inst_cg_res;
+  // CTA groups of the batched CG (kernels.h launch_batched_pcg), built for one element set and precision
+  struct BatchPlan {
+    ikr_fes fes = nullptr;
+    bool fp32 = false;
+    int n_cta = 0;
+    bool cooperative = false;
+    DBuf<int32_t> cta_inst, cta_first, cta_size;
+    DBuf<double> part;
+    DBuf<unsigned int> counters;
+  } plan;
 };
 
 struct ikr_lc_s {

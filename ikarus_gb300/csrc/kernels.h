@@ -162,12 +162,16 @@ bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant);
 cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s);
 
 // batched.cu -- independent instances (disjoint contiguous node ranges) of one element set
-// one CTA per instance runs the instance's whole block-Jacobi PCG; inactive instances get a zero correction;
-// xw..qw are node-padded work vectors of the whole set; rtol per instance
-void launch_batched_pcg(const Bsr& A, bool fp32, const void* minv, const double* b, double* x_out, int n_inst,
-                        const int32_t* node_off, const int32_t* order, const uint8_t* active, void* xw, void* rw,
-                        void* zw, void* pw, void* qw, const double* rtol, int max_iter, int32_t* iters,
-                        double* relres, cudaStream_t s);
+// one cooperative launch runs every active instance's block-Jacobi PCG; instance i is served by the CTAs
+// cta_first[i'] .. + cta_size - 1 listed per CTA (cta_inst, cta_first, cta_size; groups contiguous); inactive
+// instances get a zero correction; xw..qw are node-padded work vectors of the whole set; rtol per instance;
+// part holds 4 doubles per CTA, counters one per instance.  capacity = co-resident CTAs on the device.
+int batched_pcg_capacity(bool fp32, int sms);
+cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, const void* minv, const double* b, double* x_out, int n_cta,
+                               const int32_t* node_off, const int32_t* cta_inst, const int32_t* cta_first,
+                               const int32_t* cta_size, const uint8_t* active, void* xw, void* rw, void* zw, void* p0,
+                               void* p1, void* qw, const double* rtol, int max_iter, int32_t* iters, double* relres,
+                               double* part, unsigned int* counters, int n_inst, bool cooperative, cudaStream_t s);
 void launch_instance_norms(const double* x, int n_inst, const int32_t* node_off, double* out, cudaStream_t s);
 
 // mlp.cu -- dense network (BF16 weights, FP32 accumulation) and POD helpers of the learned predictor
