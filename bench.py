@@ -35,6 +35,9 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--load-steps", type=int, default=20)
     ap.add_argument("--plain-runs", type=int, default=1)
+    ap.add_argument("--predictor", type=int, default=1, choices=[0, 1],
+                    help="mixed form's Newton predictor: 0 none (the reference's), 1 previous increment (the learned "
+                         "predictor's fallback; this single load case has no trained model)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="32x8x8 mesh (profiling runs)")
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
@@ -43,6 +46,9 @@ def parse():
     ap.add_argument("--train-paths", type=int, default=200, help="config 4: training load paths")
     ap.add_argument("--eval-paths", type=int, default=20, help="config 4: held-out load paths")
     ap.add_argument("--no-graphs", action="store_true", help="launch CG kernels one by one (for profilers)")
+    ap.add_argument("--backtracks", type=int, default=10,
+                    help="configs 3 and 5: halve a Newton correction that inverts an element up to this many times "
+                         "(both forms; the reference aborts instead)")
     ap.add_argument("--eas-size", default="64,64,16", help="config 5: elements per direction")
     ap.add_argument("--eas-steps", type=int, default=25, help="config 5: load steps")
     ap.add_argument("--eas-predictor", type=int, default=1, help="config 5: 0 none, 1 previous increment")
@@ -125,12 +131,15 @@ def solver_settings(ikr, mixed: bool):
 class Form:
     """One solution form (mixed or plain) on the GPU: element set, assembler, solver objects, requirements."""
 
-    def __init__(self, ikr, problems, p, mixed):
+    def __init__(self, ikr, problems, p, mixed, predictor=0):
         self.ikr = ikr
+        self.mixed = mixed
         self.fes, self.asm = problems.build_gpu(p, precision=1 if mixed else 0)
         self.ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
         self.nr = ikr.NewtonRaphson(self.asm, ikr.NewtonRaphsonConfig(solver_settings(ikr, mixed), self.ls))
         self.lc = ikr.LoadControl(self.nr, p.load_steps, (0.0, p.t_end))
+        if predictor:
+            self.lc.set_predictor(predictor)
         self.req = ikr.FERequirements(self.fes)
         self.req0 = ikr.FERequirements(self.fes)  # undeformed state, load factor 0 (device resident)
         self.asm.bind(self.req, ikr.DBCOption.Full)
@@ -165,7 +174,7 @@ def run_ours(args, rank, world):
     p = problems.cantilever(32, 8, 8, jitter=0.1, seed=2024, load_steps=args.load_steps, tol=1e-8, relative=True) \
         if args.small else problems.config2(load_steps=args.load_steps)
     n_nodes = p.mesh.n_nodes
-    mixed = Form(ikr, problems, p, mixed=True)
+    mixed = Form(ikr, problems, p, mixed=True, predictor=args.predictor)
     stream, ev0, ev1 = make_events(torch, mixed.fes.stream())
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
@@ -207,7 +216,9 @@ def run_ours(args, rank, world):
     pinfo = mixed.run_device()
     assert pinfo.success
     spmv_ms, spmv_n = mixed.ls.profile_read()
+    prof_solves = pinfo.totalIterations  # one CG solve per Newton iteration (no refinement sweeps in this form)
     mixed.ls.profile(False)
+    assembly = {"mixed": assembly_rates(ikr, torch, mixed, p)}
     assert all(i.success for i in infos)
     t_mixed = sum(times) / len(times)
     if world > 1:
@@ -234,7 +245,7 @@ def run_ours(args, rank, world):
     del flush
     if args.plain_runs <= 0:
         return finish(args, p, world, t_mixed, t_e2e, None, None, infos, launches, mixed, n_nodes, spmv_ms, spmv_n,
-                      clocks, None), p
+                      clocks, None, prof_solves, assembly), p
     plain = Form(ikr, problems, p, mixed=False)
     pstream, pev0, pev1 = make_events(torch, plain.fes.stream())
     plain_times, plain_infos = [], []
@@ -252,12 +263,46 @@ def run_ours(args, rank, world):
     u_plain = plain.req.globalSolution()
     u_mixed = mixed.req.globalSolution()
     rel_diff = float(np.abs(u_mixed - u_plain).max() / np.abs(u_plain).max())
+    assembly["plain_fp64"] = assembly_rates(ikr, torch, plain, p)
     return finish(args, p, world, t_mixed, t_e2e, t_plain, plain_infos[-1], infos, launches, mixed, n_nodes, spmv_ms,
-                  spmv_n, clocks, rel_diff), p
+                  spmv_n, clocks, rel_diff, prof_solves, assembly), p
+
+
+def assembly_rates(ikr, torch, form, p):
+    """Device time of one residual assembly (FP64) and one tangent assembly (the form's precision) at the form's
+    current state, averaged over 5 after a warm-up: elements/s, dofs/s and achieved bytes/s of the algorithmic
+    traffic (values written once, coordinates, displacements, connectivity and the element-to-block map read
+    once; residual written once)."""
+    stream, e0, e1 = make_events(torch, form.fes.stream())
+    out = {}
+    nn, ne, n = p.mesh.n_nodes, p.mesh.n_elems, p.n_dofs
+    rp, col = form.asm.block_pattern()
+    nb = len(col)
+    sK = 4 if form.mixed else 8
+    common = nn * 3 * 8 + n * 8 + ne * 8 * 4
+    for name, call, nbytes in (
+            ("residual_fp64", lambda: form.asm.vector(form.req, dbc=ikr.DBCOption.Full, export=False),
+             common + n * 8),
+            ("tangent_fp32" if form.mixed else "tangent_fp64",
+             lambda: form.asm.matrix(form.req, dbc=ikr.DBCOption.Full, export=False),
+             common + nb * 9 * sK + ne * 64 * 4)):
+        call()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(5):
+            call()
+        e1.record(stream)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 5 / 1e3
+        out[name] = {"ms": round(t * 1e3, 3), "elements_per_s": round(ne / t), "dofs_per_s": round(n / t),
+                     "algorithmic_bytes": nbytes, "achieved_gbs": round(nbytes / t / 1e9, 1)}
+    epb = form.fes.kernel_info()
+    out["elements_per_block"] = {"residual": epb[0], "tangent_fp64": epb[1], "tangent_fp32": epb[2]}
+    return out
 
 
 def finish(args, p, world, t_mixed, t_e2e, t_plain, plain_info, infos, launches, mixed, n_nodes, spmv_ms, spmv_n,
-           clocks, rel_diff):
+           clocks, rel_diff, prof_solves, assembly=None):
 
     # roofline of the dominant kernel: the fused CG SpMV (two-kernel CG) or, when the tuner picked the persistent
     # CG, one CG iteration of it (SpMV streams plus the block-Jacobi inverse of the update phase)
@@ -268,16 +313,22 @@ def finish(args, p, world, t_mixed, t_e2e, t_plain, plain_info, infos, launches,
         bpl += 9 * n_nodes * 4
     kname = ("pcg_persistent_kernel<float> (per CG iteration)" if persistent else
              "pcg_spmv_staged_kernel<float>" if kind > 0 else "pcg_spmv_kernel<float>")
-    avg_s = spmv_ms / max(spmv_n, 1) / 1e3
+    # per launch: a persistent launch is one CG solve (spmv_n counts its iterations), a staged launch one SpMV
+    n_launch = max(prof_solves, 1) if persistent else max(spmv_n, 1)
+    iters_per_launch = spmv_n / n_launch
+    avg_s = spmv_ms / n_launch / 1e3
+    bytes_per_launch = bpl * iters_per_launch
     pk = peaks()
     peak = pk["hbm_gbs"] if pk else 6800.0
-    achieved = bpl / avg_s / 1e9 if avg_s > 0 else None
+    achieved = bytes_per_launch / avg_s / 1e9 if avg_s > 0 else None
     traffic = None
-    tf = os.path.join(ROOT, "profiles", "spmv_fp32_dram_traffic.json")
+    tf = os.path.join(ROOT, "profiles", "cg_dram_traffic.json")
     if os.path.exists(tf) and not args.small:
         try:
-            traffic = json.load(open(tf)).get("bytes_per_launch_config2")
-        except (OSError, ValueError):
+            t = json.load(open(tf))
+            if t.get("cg_kernel_kind") == kind:  # DRAM bytes per CG iteration of that kernel, ncu
+                traffic = round(t["dram_bytes_per_iteration"] * iters_per_launch)
+        except (OSError, ValueError, KeyError):
             traffic = None
 
     info0 = infos[-1]
@@ -298,6 +349,11 @@ def finish(args, p, world, t_mixed, t_e2e, t_plain, plain_info, infos, launches,
         "config": {"workload": p.name, "elements": p.mesh.n_elems, "nodes": n_nodes, "dofs": p.n_dofs,
                    "load_steps": p.load_steps, "tolerance": "||R||/||R0|| < 1e-8 every load step",
                    "material": "NeoHooke E=1000 nu=0.3", "parallelism": f"replicas x{world}",
+                   "mixed_form": "FP32 tangent + FP32 block-Jacobi PCG (Eisenstat-Walker forcing), FP64 residual and "
+                                 "Newton test" + (", Newton predictor = previous increment (the learned predictor's "
+                                 "fallback; no trained model exists for this single load case)" if args.predictor
+                                 else ", no Newton predictor"),
+                   "plain_form": "FP64 tangent + FP64 block-Jacobi PCG to 1e-10, FP64 residual, no predictor",
                    "l2": "256 MB buffer written between timed load paths; working set > L2"},
         "plain_fp64": None if t_plain is None else
         {"s_per_load_path": round(t_plain, 4), "newton_iterations": plain_info.totalIterations,
@@ -310,12 +366,16 @@ def finish(args, p, world, t_mixed, t_e2e, t_plain, plain_info, infos, launches,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1) if achieved
                      else None, "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                     "traffic": traffic, "algorithmic_bytes_per_launch": bpl, "avg_launch_us": round(avg_s * 1e6, 3),
-                     "launches": spmv_n, "unit_of_work": "CG iteration" if persistent else "SpMV launch",
+                     "traffic": traffic, "algorithmic_bytes_per_launch": round(bytes_per_launch),
+                     "avg_launch_us": round(avg_s * 1e6, 3), "launches": n_launch,
+                     "cg_iterations_per_launch": round(iters_per_launch, 2), "algorithmic_bytes_per_cg_iteration": bpl,
+                     "us_per_cg_iteration": round(spmv_ms * 1e3 / max(spmv_n, 1), 3),
                      "cg_kernel_kind": kind, "l2_keep_fraction": keep,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback"},
         "clocks": clocks.summary(),
     }
+    if assembly:
+        out["assembly"] = assembly
     return out
 
 
@@ -417,11 +477,13 @@ def run_batched(args):
     bp = problems.batched_cantilevers(512, seed=7, load_steps=10)
     out = {"metric": "time to ||R||/||R0||<1e-8 on every load step for all 512 instances", "unit": "s",
            "higher_is_better": False, "config": {"workload": bp.name, "elements": bp.mesh.n_elems,
-                                                  "dofs": bp.n_dofs, "instances": 512, "load_steps": 10}}
+                                                  "dofs": bp.n_dofs, "instances": 512, "load_steps": 10,
+                                                  "newton_backtracks": args.backtracks}}
     for mixed in (True, False):
         fes, asm = problems.build_gpu_batched(bp, precision=1 if mixed else 0)
         st = ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, eisenstat_walker=mixed,
-                            linear_rtol=1e-2 if mixed else 1e-10, linear_rtol_min=1e-6, linear_max_iter=20000)
+                            linear_rtol=1e-2 if mixed else 1e-10, linear_rtol_min=1e-6, linear_max_iter=20000,
+                            backtracks=args.backtracks)
         nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
         lc = ikr.LoadControl(nr, bp.load_steps)
         req, req0 = ikr.FERequirements(fes), ikr.FERequirements(fes)
@@ -540,15 +602,18 @@ def run_eas(args):
     out = {"metric": "time to ||R||/||R0||<1e-8 on every load step (nearly incompressible EAS block)", "unit": "s",
            "higher_is_better": False,
            "config": {"workload": p.name, "elements": p.mesh.n_elems, "dofs": p.n_dofs, "load_steps": p.load_steps,
-                      "eas": "GreenLagrange E9", "nu": 0.4999, "predictor": args.eas_predictor}}
+                      "eas": "GreenLagrange E9", "nu": 0.4999, "predictor": args.eas_predictor,
+                      "newton_backtracks": args.backtracks}}
     per_step = {}
     for mixed in (False, True):
         fes, asm = problems.build_gpu(p, precision=1 if mixed else 0)
         if mixed:
             st = ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
-                                linear_rtol_min=1e-5, linear_max_iter=400000, refinements=1)
+                                linear_rtol_min=1e-5, linear_max_iter=400000, refinements=1,
+                                backtracks=args.backtracks)
         else:
-            st = ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, linear_rtol=1e-10, linear_max_iter=1000000)
+            st = ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, linear_rtol=1e-10, linear_max_iter=1000000,
+                                backtracks=args.backtracks)
         ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
         nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ls))
         lc = ikr.LoadControl(nr, p.load_steps)

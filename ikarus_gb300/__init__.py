@@ -94,7 +94,7 @@ class ControlMessages(enum.IntEnum):  # broadcastermessages.hh:18
 class _NRSettings(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int32), ("min_iter", C.c_int32), ("tol_mode", C.c_int32),
                 ("forcing", C.c_int32), ("linear_rtol", C.c_double), ("linear_rtol_min", C.c_double),
-                ("linear_max_iter", C.c_int32), ("refinements", C.c_int32)]
+                ("linear_max_iter", C.c_int32), ("refinements", C.c_int32), ("max_backtracks", C.c_int32)]
 
 
 class _NRInfo(C.Structure):
@@ -137,6 +137,7 @@ SIGNATURES = {
     "ikr_fes_set_instances": ([_vp, _I, _ip], C.c_int),
     "ikr_newton_instance_info": ([_vp, _ip, _dp, _ip], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
+    "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
     "ikr_fes_get_alpha": ([_vp, _dp], C.c_int),
     "ikr_fes_set_alpha": ([_vp, _dp], C.c_int),
     "ikr_fe_calculate_vector": ([_vp, _vp, _I, _I, _I, _dp], C.c_int),
@@ -301,6 +302,12 @@ class FiniteElements:
         self.n_instances = len(off) - 1
         _err(lib().ikr_fes_set_instances(self.h, self.n_instances, _ptr(off, C.c_int32)), "set_instances")
 
+    def kernel_info(self):
+        """Elements per block of the element kernel for residual / FP64 tangent / FP32 tangent (0: not yet)."""
+        a, b, c = C.c_int32(), C.c_int32(), C.c_int32()
+        _err(lib().ikr_fes_kernel_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
     def num_colours(self):
         n = C.c_int32()
         _err(lib().ikr_fes_num_colours(self.h, C.byref(n)))
@@ -460,8 +467,12 @@ class SparseFlatAssembler:
             raise IkarusError(-3, "assembler not bound")
         return req, DBCOption(self._dbc if dbc is None else dbc)
 
-    def vector(self, req=None, affordance=VectorAffordance.forces, dbc=None):
+    def vector(self, req=None, affordance=VectorAffordance.forces, dbc=None, export=True):
+        """Assembles on the device; returns the host copy unless export=False."""
         req, dbc = self._args(req, dbc)
+        if not export:
+            _err(lib().ikr_assembler_vector(self.h, req.h, int(affordance), int(dbc), None), "vector")
+            return None
         n = self.reducedSize() if dbc == DBCOption.Reduced else self.size()
         out = np.zeros(n)
         _err(lib().ikr_assembler_vector(self.h, req.h, int(affordance), int(dbc), _ptr(out)), "vector")
@@ -588,10 +599,12 @@ class NRSettings:
     linear_rtol_min: float = 1e-12
     linear_max_iter: int = 100000
     refinements: int = 0
+    backtracks: int = 0           # halve a correction that inverts an element (the reference aborts)
 
     def _c(self):
         return _NRSettings(self.tol, self.maxIter, self.minIter, int(self.relative), int(self.eisenstat_walker),
-                           self.linear_rtol, self.linear_rtol_min, self.linear_max_iter, self.refinements)
+                           self.linear_rtol, self.linear_rtol_min, self.linear_max_iter, self.refinements,
+                           self.backtracks)
 
 
 @dataclass

@@ -215,7 +215,23 @@ __global__ void instance_norms_kernel(const double* __restrict__ x, const int32_
   if (threadIdx.x == 0) out[inst] = sqrt(s);
 }
 
+// u = u_old + step[i] corr on the dofs of every instance i with step[i] != 1 (one block per instance)
+__global__ void instance_step_kernel(double* __restrict__ u, const double* __restrict__ u_old,
+                                     const double* __restrict__ corr, const int32_t* __restrict__ node_off,
+                                     const double* __restrict__ step) {
+  const int inst = blockIdx.x;
+  const double sc = step[inst];
+  if (sc == 1.0) return;
+  for (int i = 3 * node_off[inst] + threadIdx.x; i < 3 * node_off[inst + 1]; i += blockDim.x)
+    u[i] = u_old[i] + sc * corr[i];
+}
+
 }  // namespace
+
+void launch_instance_step(double* u, const double* u_old, const double* corr, int n_inst, const int32_t* node_off,
+                          const double* step, cudaStream_t s) {
+  instance_step_kernel<<<n_inst, 256, 0, s>>>(u, u_old, corr, node_off, step);
+}
 
 int batched_pcg_capacity(bool fp32, int sms) {
   int b = 0;

@@ -27,34 +27,65 @@ using namespace cg;
 
 constexpr int kBarrierSpinLimit = 1 << 24;  // polls (with a short sleep) before a grid barrier gives up
 
-// arrive on the grid barrier counter and wait until `target` arrivals; thread 0 of the CTA spins
-__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int target, bool* ok_sh) {
+// CTA sums of N values: valid in thread 0 only (one __syncthreads; sw holds WARPS x N doubles)
+template <int N>
+__device__ __forceinline__ void cta_reduce(double (&v)[N], double* sw) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    const double s = warp_sum(v[k]);
+    if (lane == 0) sw[warp * N + k] = s;
+  }
   __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double s = lane < (int)(blockDim.x >> 5) ? sw[lane * N + k] : 0.0;
+      v[k] = warp_sum(s);
+    }
+  }
+}
+
+// Grid-wide sums of N values whose CTA sums are in thread 0: thread 0 publishes them at part[cta * N + k],
+// arrives on the barrier counter and waits (bounded) until `target` arrivals; then warp 0 sums all CTAs'
+// partials with a fixed lane assignment and butterfly order (identical in every CTA) and every thread gets
+// the sums.  Returns false when the wait gave up.
+template <int N>
+__device__ __forceinline__ bool grid_allreduce(double (&v)[N], double* part, unsigned int* count, unsigned int target,
+                                               double* sv, bool* ok_sh) {
   if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) part[blockIdx.x * N + k] = v[k];
     __threadfence();
     atomicAdd(count, 1u);
     bool ok = false;
-    for (int k = 0; k < kBarrierSpinLimit; ++k) {
-      unsigned int v;
-      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
-      if (v >= target) {
+    for (int i = 0; i < kBarrierSpinLimit; ++i) {
+      unsigned int c;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(count) : "memory");
+      if (c >= target) {
         ok = true;
         break;
       }
-      __nanosleep(32);
+      if (i > 64) __nanosleep(16);
     }
     *ok_sh = ok;
   }
   __syncthreads();
   __threadfence();  // every thread: its later plain loads observe what the other CTAs wrote before arriving
-  return *ok_sh;
-}
-
-// fixed-order sum of the G partials at p[i * st] (i < G), result in every thread
-__device__ __forceinline__ double grid_partial_sum(const double* p, int G, int st, double* sh) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < G; i += blockDim.x) s += __ldcg(p + (size_t)i * st);
-  return block_sum_all(s, sh);
+  if (!*ok_sh) return false;
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double s = 0.0;
+      for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) s += __ldcg(part + (size_t)i * N + k);
+      s = warp_sum(s);
+      if (threadIdx.x == 0) sv[k] = s;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; ++k) v[k] = sv[k];
+  return true;
 }
 
 template <typename T, int CB, int NST, int WARPS>
@@ -71,15 +102,16 @@ struct CyclicPos {
   int j, g, gend;
 };
 
-template <typename T, int CB, int NST, int WARPS, int MAXS>
-__global__ void __launch_bounds__(WARPS * 32, 1)
+template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB)
     pcg_persistent_kernel(Bsr A, const T* __restrict__ val, const T* __restrict__ minv, T* __restrict__ xg,
                           const T* __restrict__ rg, T* __restrict__ zg, T* __restrict__ p0, T* __restrict__ p1,
                           double* part_a, double* part_b, double* scal, int64_t keep_g) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[WARPS][NST];
-  __shared__ double sh[32];
+  __shared__ double sw[WARPS * 2];
+  __shared__ double sv[2];
   __shared__ bool ok_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G = gridDim.x;
@@ -223,13 +255,16 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     }
     // ---- grid reduction of p.q
     const int par = it & 1;
-    const double pq_cta = block_sum_all(pq, sh);
-    if (threadIdx.x == 0) part_a[par * G + blockIdx.x] = pq_cta;
-    ++barrier_no;
-    if (!grid_barrier(bar_count, barrier_no * (unsigned)G, &ok_sh)) failed = true;
     failed = __syncthreads_or(failed);
     if (failed) break;
-    const double pqs = grid_partial_sum(part_a + par * G, G, 1, sh);
+    double red1[1] = {pq};
+    cta_reduce<1>(red1, sw);
+    ++barrier_no;
+    if (!grid_allreduce<1>(red1, part_a + par * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
+      failed = true;
+      break;
+    }
+    const double pqs = red1[0];
     if (!(fabs(pqs) > 0.0) || !isfinite(pqs)) {  // breakdown (negative curvature alone does not stop CG)
       done = 3.0;
       break;
@@ -266,18 +301,15 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         rrn += double(trr);
       }
     }
-    const double rz_cta = block_sum_all(rzn, sh);
-    const double rr_cta = block_sum_all(rrn, sh);
-    if (threadIdx.x == 0) {
-      part_b[par * 2 * G + 2 * blockIdx.x] = rz_cta;
-      part_b[par * 2 * G + 2 * blockIdx.x + 1] = rr_cta;
-    }
+    double red2[2] = {rzn, rrn};
+    cta_reduce<2>(red2, sw);
     ++barrier_no;
-    if (!grid_barrier(bar_count, barrier_no * (unsigned)G, &ok_sh)) failed = true;
-    failed = __syncthreads_or(failed);
-    if (failed) break;
-    const double rzs = grid_partial_sum(part_b + par * 2 * G, G, 2, sh);
-    rrs = grid_partial_sum(part_b + par * 2 * G + 1, G, 2, sh);
+    if (!grid_allreduce<2>(red2, part_b + par * 2 * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
+      failed = true;
+      break;
+    }
+    const double rzs = red2[0];
+    rrs = red2[1];
     beta = rzs / rz;
     rz = rzs;
     ++it;
@@ -307,10 +339,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   if (failed && threadIdx.x == 0) scal[kDone] = kDoneDeviceTimeout;
 }
 
-template <typename T, int CB, int NST, int WARPS, int MAXS>
+template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB>
 cudaError_t launch_persistent(const Bsr& A, PcgWork& w, cudaStream_t s, bool query_only, bool* eligible) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
-  auto kern = pcg_persistent_kernel<T, CB, NST, WARPS, MAXS>;
+  auto kern = pcg_persistent_kernel<T, CB, NST, WARPS, MAXS, MINB>;
   static std::mutex mu;
   static int blocks_per_sm[64] = {0};
   int dev = 0;
@@ -350,17 +382,19 @@ cudaError_t launch_persistent(const Bsr& A, PcgWork& w, cudaStream_t s, bool que
 template <typename T>
 cudaError_t dispatch(int variant, const Bsr& A, PcgWork& w, cudaStream_t s, bool query, bool* eligible) {
   if constexpr (sizeof(T) == 4) {
-    if (variant == 0) return launch_persistent<float, 8, 2, 8, 4>(A, w, s, query, eligible);
-    return launch_persistent<float, 4, 3, 8, 8>(A, w, s, query, eligible);
+    if (variant == 0) return launch_persistent<float, 8, 2, 8, 4, 1>(A, w, s, query, eligible);
+    if (variant == 1) return launch_persistent<float, 4, 3, 8, 8, 1>(A, w, s, query, eligible);
+    return launch_persistent<float, 4, 2, 8, 2, 2>(A, w, s, query, eligible);
   } else {
-    if (variant == 0) return launch_persistent<double, 4, 2, 8, 4>(A, w, s, query, eligible);
-    return launch_persistent<double, 2, 3, 8, 4>(A, w, s, query, eligible);
+    if (variant == 0) return launch_persistent<double, 4, 2, 8, 4, 1>(A, w, s, query, eligible);
+    if (variant == 1) return launch_persistent<double, 2, 3, 8, 4, 1>(A, w, s, query, eligible);
+    return launch_persistent<double, 2, 2, 8, 2, 2>(A, w, s, query, eligible);
   }
 }
 
 }  // namespace
 
-int pcg_persistent_variants() { return 2; }
+int pcg_persistent_variants() { return 3; }
 
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant) {
   bool ok = false;

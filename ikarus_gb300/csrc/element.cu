@@ -26,22 +26,21 @@ namespace ikr {
 
 namespace {
 
-constexpr int kElemsPerBlock = 32;
-
-template <typename KT, int MODE>
-__global__ void __launch_bounds__(256) disp_element_kernel(ElemArgs a, const int32_t* __restrict__ list, int n_list,
-                                                           int e_base) {
+// EPB elements per block (8 lanes each): 16, 32 or 64, chosen per element set by timing (host.cpp)
+template <typename KT, int MODE, int EPB>
+__global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const int32_t* __restrict__ list, int n_list,
+                                                               int e_base) {
   constexpr bool WANT_R = MODE & kWantR;
   constexpr bool WANT_K = MODE & kWantK;
   constexpr bool WANT_E = MODE & kWantEnergy;
   constexpr bool ELEM_OUT = MODE & kElemOut;
   static_assert(!(WANT_R || WANT_E) || std::is_same<KT, double>::value, "residual and energy are FP64");
-  __shared__ KT sh[kElemsPerBlock][8][6];
+  __shared__ KT sh[EPB][8][6];
 
   const int lane = threadIdx.x & 31;
   const int sub = threadIdx.x & 7;
   const int es = threadIdx.x >> 3;
-  const int li = blockIdx.x * kElemsPerBlock + es;
+  const int li = blockIdx.x * EPB + es;
   const bool active = li < n_list;
   const int lic = active ? li : n_list - 1;
   const int e = list ? list[lic] : e_base + lic;
@@ -272,10 +271,19 @@ __global__ void traction_kernel(const double* __restrict__ X, const int32_t* __r
   for (int k = 0; k < 24; ++k) trac[24 * (size_t)s + k] = acc[k];
 }
 
+template <typename KT, int MODE, int EPB>
+void launch_disp_epb(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
+  const int blocks = (n_list + EPB - 1) / EPB;
+  disp_element_kernel<KT, MODE, EPB><<<blocks, EPB * 8, 0, s>>>(a, list, n_list, e_base);
+}
+// assembling modes honour a.epb; element-level outputs (tests, single elements) use 32
 template <typename KT, int MODE>
 void launch_disp_t(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
-  const int blocks = (n_list + kElemsPerBlock - 1) / kElemsPerBlock;
-  disp_element_kernel<KT, MODE><<<blocks, 256, 0, s>>>(a, list, n_list, e_base);
+  if constexpr ((MODE & kElemOut) == 0) {
+    if (a.epb == 16) return launch_disp_epb<KT, MODE, 16>(a, list, n_list, e_base, s);
+    if (a.epb == 64) return launch_disp_epb<KT, MODE, 64>(a, list, n_list, e_base, s);
+  }
+  launch_disp_epb<KT, MODE, 32>(a, list, n_list, e_base, s);
 }
 
 }  // namespace

@@ -79,6 +79,32 @@ void need(bool c, int code, const char* msg) {
 // EAS condensation cache key: valid while the same requirement, solution and alpha are in place
 uint64_t cache_key(ikr_req r, ikr_fes f) { return (r->id * 0x9E3779B97F4A7C15ull) ^ (r->version << 20) ^ f->alpha_version; }
 
+// Elements per block of the displacement element kernel: each of 16, 32 and 64 is timed once on a complete
+// coloured pass of the given kind and the fastest is kept for the element set (the choice does not change any
+// result: the summation order into each block is fixed by the colouring).  `pass` runs one pass with args.epb.
+template <typename Pass>
+static int choose_epb(ikr_fes f, Pass pass) {
+  if (f->na > 0) return 32;  // the EAS kernel has its own launch shape
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int best = 32;
+  float best_ms = 1e30f;
+  for (int epb : {16, 32, 64}) {
+    pass(epb);  // warm
+    CK(cudaEventRecord(e0, f->stream));
+    pass(epb);
+    CK(cudaEventRecord(e1, f->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best_ms) best_ms = ms, best = epb;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return best;
+}
+
 void assemble_vector(ikr_asm a, ikr_req r, int dbc) {
   ikr_fes f = a->fes;
   f->refresh_tractions();
@@ -89,6 +115,17 @@ void assemble_vector(ikr_asm a, ikr_req r, int dbc) {
   args.load_factor = r->lambda;
   args.node_fixed = (dbc == IKR_DBC_RAW) ? nullptr : a->node_fixed.p;
   args.R = a->R.p;
+  if (!f->epb_r) {
+    f->epb_r = choose_epb(f, [&](int epb) {
+      CK(cudaMemsetAsync(a->R.p, 0, sizeof(double) * a->n, f->stream));
+      ikr::ElemArgs t = args;
+      t.epb = epb;
+      f->launch_coloured(t, ikr::kWantR, false);
+      f->check_status();
+    });
+    CK(cudaMemsetAsync(a->R.p, 0, sizeof(double) * a->n, f->stream));
+  }
+  args.epb = f->epb_r;
   f->launch_coloured(args, ikr::kWantR, false);
   ikr::launch_vector_finish(a->R.p, nullptr, f->nn, a->pl_dof.p, a->pl_val.p, (int)a->pl_dof.n, r->lambda, f->stream);
   if (a->pl_dof.n) count(1);
@@ -109,6 +146,18 @@ void assemble_matrix(ikr_asm a, ikr_req r, int dbc) {
   args.node_fixed = nf;
   args.Kval = a->values();
   args.slot = a->slot.p;
+  int& epb_k = a->fp32 ? f->epb_k32 : f->epb_k64;
+  if (!epb_k) {
+    epb_k = choose_epb(f, [&](int epb) {
+      ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
+      ikr::ElemArgs t = args;
+      t.epb = epb;
+      f->launch_coloured(t, ikr::kWantK, a->fp32);
+      f->check_status();
+    });
+    ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
+  }
+  args.epb = epb_k;
   f->launch_coloured(args, ikr::kWantK, a->fp32);
   a->matrix_dbc = dbc;
   f->check_status();
@@ -679,6 +728,14 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
     ls->set_launch(use_graphs != 0, chunk_len);
   });
 }
+int ikr_fes_kernel_info(ikr_fes fes, int32_t* epb_residual, int32_t* epb_tangent64, int32_t* epb_tangent32) {
+  return guarded([&] {
+    need(fes, IKR_ERR_ARG, "null argument");
+    if (epb_residual) *epb_residual = fes->epb_r;
+    if (epb_tangent64) *epb_tangent64 = fes->epb_k64;
+    if (epb_tangent32) *epb_tangent32 = fes->epb_k32;
+  });
+}
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t kind, double keep) {
   return guarded([&] {
     need(ls && kind >= -1 && kind <= ikr::spmv_staged_variants() + ikr::pcg_persistent_variants() &&
@@ -754,6 +811,7 @@ int ikr_nr_settings_default(ikr_nr_settings* s) {
     s->linear_rtol_min = 1e-12;
     s->linear_max_iter = 100000;
     s->refinements = 0;
+    s->max_backtracks = 0;
   });
 }
 int ikr_newton_create(ikr_nr* out, ikr_asm a, ikr_ls ls, const ikr_nr_settings* st) {
@@ -930,12 +988,37 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
     CK(cudaStreamSynchronize(s));
     for (int i = 0; i < ni; ++i)
       if (cgit[i] < 0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the batched CG gave up (instance %d)", i);
+    std::vector<uint8_t> failed_before(nr->inst_failed);
+    if (st.max_backtracks > 0) {
+      nr->u_old.alloc(n);
+      CK(cudaMemcpyAsync(nr->u_old.p, r->u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    }
     ikr::launch_axpy64(r->u.p, nr->corr.p, 1.0, n, s);
     count(1);
     r->version++;
     for (int i = 0; i < ni; ++i) rprev[i] = rn[i];
     assemble_vector(a, r, IKR_DBC_FULL);
     collect_failures();
+    // instances whose corrected state inverts an element go back and take half their step, up to
+    // max_backtracks times; the others keep their full step
+    std::vector<double> step(ni, 1.0);
+    for (int bt = 0; bt < st.max_backtracks; ++bt) {
+      bool any_new = false;
+      for (int i = 0; i < ni; ++i)
+        if (nr->inst_failed[i] && !failed_before[i] && act[i]) {
+          nr->inst_failed[i] = 0;
+          step[i] *= 0.5;
+          any_new = true;
+          ++nr->backtracks;
+        }
+      if (!any_new) break;
+      nr->inst_step.upload(step.data(), ni, s);
+      ikr::launch_instance_step(r->u.p, nr->u_old.p, nr->corr.p, ni, f->inst_off.p, nr->inst_step.p, s);
+      count(1);
+      r->version++;
+      assemble_vector(a, r, IKR_DBC_FULL);
+      collect_failures();
+    }
     norms();
     for (int i = 0; i < ni; ++i) {
       lin += cgit[i];
@@ -1018,13 +1101,42 @@ void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double 
     lin += nr->ls->solve(a, nr->rhs.p, nr->corr.p, eta, st.linear_max_iter, st.refinements);
     inf.correction_norm = device_norm(f, nr->corr.p, n, nr->nrm_part, nr->nrm_out);
     notify(IKR_NLS_CORRECTION_UPDATED);
-    if (nr->fe_state) update_state(f, r, nr->corr.p);
-    ikr::launch_axpy64(r->u.p, nr->corr.p, 1.0, n, f->stream);
-    count(1);
-    r->version++;
+    const bool eas_state = nr->fe_state && f->na > 0;
+    if (st.max_backtracks > 0) {  // keep the state the correction starts from
+      nr->u_old.alloc(n);
+      CK(cudaMemcpyAsync(nr->u_old.p, r->u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, f->stream));
+      if (eas_state) {
+        nr->alpha_old.alloc(f->alpha.n);
+        CK(cudaMemcpyAsync(nr->alpha_old.p, f->alpha.p, sizeof(double) * f->alpha.n, cudaMemcpyDeviceToDevice,
+                           f->stream));
+      }
+    }
+    for (int bt = 0;; ++bt) {
+      if (nr->fe_state) update_state(f, r, nr->corr.p);
+      ikr::launch_axpy64(r->u.p, nr->corr.p, 1.0, n, f->stream);
+      count(1);
+      r->version++;
+      try {
+        assemble_vector(a, r, IKR_DBC_FULL);
+        break;
+      } catch (const IkrError& e) {
+        if (e.code != IKR_ERR_NONPOSITIVE_DETC || bt >= st.max_backtracks) throw;
+        // the corrected state inverts an element: go back and take half the step
+        CK(cudaMemcpyAsync(r->u.p, nr->u_old.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, f->stream));
+        if (eas_state) {
+          CK(cudaMemcpyAsync(f->alpha.p, nr->alpha_old.p, sizeof(double) * f->alpha.n, cudaMemcpyDeviceToDevice,
+                             f->stream));
+          f->alpha_version++;
+        }
+        ikr::launch_scale64(nr->corr.p, nr->corr.p, 0.5, n, f->stream);
+        count(1);
+        r->version++;
+        inf.correction_norm *= 0.5;
+        ++nr->backtracks;
+      }
+    }
     notify(IKR_NLS_CORRECTIONNORM_UPDATED);
     notify(IKR_NLS_SOLUTION_CHANGED);
-    assemble_vector(a, r, IKR_DBC_FULL);
     k_valid = false;  // the reference reassembles K here (newtonraphson.hh:243); it is built when next needed
     rprev = rnorm;
     rnorm = device_norm(f, a->R.p, n, nr->nrm_part, nr->nrm_out);

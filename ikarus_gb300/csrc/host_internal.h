@@ -110,6 +110,9 @@ using namespace ikr_host;
 // ------------------------------------------------------------------------------------------------------------
 struct ikr_fes_s {
   int nn = 0, ne = 0, na = 0, eas = 0;
+  // elements per block of the displacement element kernel, chosen by timing at the first assembly of each kind
+  // (0 = not chosen yet): residual, FP64 tangent, FP32 tangent
+  int epb_r = 0, epb_k64 = 0, epb_k32 = 0;
   double lam = 0, mu = 0;
   cudaStream_t stream = nullptr;
   std::vector<int32_t> conn_h;  // row-major n_elems x 8
@@ -704,6 +707,8 @@ struct ikr_nr_s {
   std::vector<double> inst_res;
   std::vector<int8_t> inst_conv;     // 1 converged, 0 not, -1 taken out after an element inversion
   std::vector<uint8_t> inst_failed;  // inversions seen since the last reset (LoadControl::run, newton_solve)
+  DBuf<double> u_old, alpha_old, inst_step;  // backtracking: state before the correction, per-instance steps
+  int64_t backtracks = 0;                    // corrections halved since creation
   DBuf<double> inst_norm, inst_rtol;
   DBuf<uint8_t> inst_active;
   DBuf<int32_t> inst_cg_iters;

@@ -47,6 +47,7 @@ struct ElemArgs {
   double* elem_mat = nullptr;      // element-level: 576 per listed element, column-major
   double* elem_energy = nullptr;   // element-level: 1 per listed element
   int* status = nullptr;           // StatusBits, OR-ed
+  int epb = 32;                    // displacement element kernel: elements per block (16, 32 or 64)
   // batched solves: the status of an element goes to its instance, inst_status[elem_inst[e]], instead
   const int32_t* elem_inst = nullptr;
   int* inst_status = nullptr;
@@ -173,6 +174,9 @@ cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, const void* minv, const 
                                void* p1, void* qw, const double* rtol, int max_iter, int32_t* iters, double* relres,
                                double* part, unsigned int* counters, int n_inst, bool cooperative, cudaStream_t s);
 void launch_instance_norms(const double* x, int n_inst, const int32_t* node_off, double* out, cudaStream_t s);
+// u = u_old + step[i] corr on the dofs of instance i (instances with step 1 untouched)
+void launch_instance_step(double* u, const double* u_old, const double* corr, int n_inst, const int32_t* node_off,
+                          const double* step, cudaStream_t s);
 
 // mlp.cu -- dense network (BF16 weights, FP32 accumulation) and POD helpers of the learned predictor
 // C[M x N] = alpha op(A) op(B) + beta C (row-major; op = transpose when trans_*; A / B FP32 or BF16)

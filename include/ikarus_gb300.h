@@ -176,7 +176,7 @@ int ikr_linear_solver_profile_read(ikr_ls ls, double* spmv_ms_total, int64_t* sp
  * (default) or launched kernel by kernel otherwise (for profilers that do not follow graph kernels). */
 int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_len);
 /* CG kernels (no reference counterpart).  spmv_kind 0 = two kernels per iteration with a direct-load SpMV,
- * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..6 = the
+ * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..7 = the
  * whole solve in one persistent cooperative kernel (grid barriers for the two reductions of an iteration;
  * only where every warp's rows fit its registers), -1 = autotune; l2_keep_fraction in [0, 1) = share of the
  * matrix the staged kernels keep in L2 across iterations, -1 = autotune.  The choice is made at the
@@ -184,6 +184,10 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fraction);
 int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* spmv_kind, double* l2_keep_fraction, double* spmv_us);
+/* elements per block the displacement element kernel uses for residual / FP64 tangent / FP32 tangent
+ * assembly (16, 32 or 64, chosen by timing at the first assembly of each kind; 0 = not assembled yet; no
+ * reference counterpart) */
+int ikr_fes_kernel_info(ikr_fes fes, int32_t* epb_residual, int32_t* epb_tangent64, int32_t* epb_tangent32);
 /* the CUDA stream (cudaStream_t) all work on this element set is issued on */
 int ikr_fes_stream(ikr_fes fes, void** stream);
 
@@ -216,6 +220,9 @@ typedef struct ikr_nr_settings {
   double linear_rtol_min;
   int32_t linear_max_iter;
   int32_t refinements; /* FP64 iterative-refinement sweeps around an FP32 solve (0 = none) */
+  int32_t max_backtracks; /* a correction that inverts an element (det C <= 0; the reference aborts) is halved up
+                             to this many times before the error is returned (0 = reference behaviour); batched
+                             solves halve the correction of the affected instances only */
 } ikr_nr_settings;
 typedef struct ikr_nr_info {   /* NonLinearSolverInformation (solverinfos.hh:20-32) */
   int32_t success;

@@ -279,3 +279,27 @@ def test_cpp_facade_cantilever_goldens(ikr, es, tmp_path):
     r = subprocess.run([exe, str(kind), str(g["eas_parameters"][es]), str(want["iterations"]), repr(want["max_disp"])],
                        capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_backtracking_recovers_a_step_the_reference_aborts(ikr):
+    """8x2x2 cantilever, tip traction 5 in ONE load step: the reference's Newton (and the oracle's) meets
+    det C <= 0 on the way and aborts.  With max_backtracks the device Newton halves the corrections that invert
+    an element and converges to the equilibrium the oracle reaches in 10 load steps."""
+    p1 = problems.cantilever(8, 2, 2, traction=(0.0, 0.0, -5.0), load_steps=1, tol=1e-8, relative=True)
+    with pytest.raises(oracle.OracleError):
+        oracle.from_problem(p1).load_control(1, tol=1e-8, tol_mode=1, max_iter=60)
+    ref = oracle.from_problem(p1).load_control(10, tol=1e-10, tol_mode=1, max_iter=60)
+
+    def run(backtracks):
+        fes, asm = problems.build_gpu(p1, precision=0)
+        req = ikr.FERequirements(fes)
+        st = ikr.NRSettings(tol=1e-10, maxIter=100, relative=True, linear_rtol=1e-12, backtracks=backtracks)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(rtol=1e-12)))
+        info = ikr.LoadControl(nr, 1).run(req)
+        return info, req.globalSolution()
+
+    with pytest.raises(ikr.IkarusError, match="NONPOSITIVE_DETC"):
+        run(0)
+    info, u = run(30)
+    assert info.success
+    assert np.abs(u - ref["u"]).max() <= 1e-7 * np.abs(ref["u"]).max()
