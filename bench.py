@@ -35,6 +35,8 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--load-steps", type=int, default=20)
     ap.add_argument("--plain-runs", type=int, default=1)
+    ap.add_argument("--eta-max", type=float, default=1e-2, help="mixed form: Eisenstat-Walker forcing upper bound")
+    ap.add_argument("--eta-min", type=float, default=1e-5, help="mixed form: Eisenstat-Walker forcing lower bound")
     ap.add_argument("--predictor", type=int, default=1, choices=[0, 1],
                     help="mixed form's Newton predictor: 0 none (the reference's), 1 previous increment (the learned "
                          "predictor's fallback; this single load case has no trained model)")
@@ -121,22 +123,22 @@ def peaks():
 
 
 # ---------------------------------------------------------------------------------------------------------
-def solver_settings(ikr, mixed: bool):
+def solver_settings(ikr, mixed: bool, eta=(1e-2, 1e-5)):
     if mixed:
-        return ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
-                              linear_rtol_min=1e-5, linear_max_iter=200000)
+        return ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=eta[0],
+                              linear_rtol_min=eta[1], linear_max_iter=200000)
     return ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, linear_rtol=1e-10, linear_max_iter=400000)
 
 
 class Form:
     """One solution form (mixed or plain) on the GPU: element set, assembler, solver objects, requirements."""
 
-    def __init__(self, ikr, problems, p, mixed, predictor=0):
+    def __init__(self, ikr, problems, p, mixed, predictor=0, eta=(1e-2, 1e-5)):
         self.ikr = ikr
         self.mixed = mixed
         self.fes, self.asm = problems.build_gpu(p, precision=1 if mixed else 0)
         self.ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
-        self.nr = ikr.NewtonRaphson(self.asm, ikr.NewtonRaphsonConfig(solver_settings(ikr, mixed), self.ls))
+        self.nr = ikr.NewtonRaphson(self.asm, ikr.NewtonRaphsonConfig(solver_settings(ikr, mixed, eta), self.ls))
         self.lc = ikr.LoadControl(self.nr, p.load_steps, (0.0, p.t_end))
         if predictor:
             self.lc.set_predictor(predictor)
@@ -174,7 +176,7 @@ def run_ours(args, rank, world):
     p = problems.cantilever(32, 8, 8, jitter=0.1, seed=2024, load_steps=args.load_steps, tol=1e-8, relative=True) \
         if args.small else problems.config2(load_steps=args.load_steps)
     n_nodes = p.mesh.n_nodes
-    mixed = Form(ikr, problems, p, mixed=True, predictor=args.predictor)
+    mixed = Form(ikr, problems, p, mixed=True, predictor=args.predictor, eta=(args.eta_max, args.eta_min))
     stream, ev0, ev1 = make_events(torch, mixed.fes.stream())
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 

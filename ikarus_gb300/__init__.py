@@ -138,6 +138,7 @@ SIGNATURES = {
     "ikr_newton_instance_info": ([_vp, _ip, _dp, _ip], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
+    "ikr_assembler_set_dirichlet_values": ([_vp, _dp], C.c_int),
     "ikr_fes_get_alpha": ([_vp, _dp], C.c_int),
     "ikr_fes_set_alpha": ([_vp, _dp], C.c_int),
     "ikr_fe_calculate_vector": ([_vp, _vp, _I, _I, _I, _dp], C.c_int),
@@ -466,6 +467,17 @@ class SparseFlatAssembler:
         if req is None:
             raise IkarusError(-3, "assembler not bound")
         return req, DBCOption(self._dbc if dbc is None else dbc)
+
+    def set_dirichlet_values(self, rate):
+        """Inhomogeneous Dirichlet values lambda * rate on constrained dofs (storeInhomogeneousBoundaryCondition for
+        values linear in the load factor); None removes them."""
+        if rate is None:
+            _err(lib().ikr_assembler_set_dirichlet_values(self.h, None), "set_dirichlet_values")
+            return
+        r = np.ascontiguousarray(rate, dtype=np.float64)
+        if r.size != self.size():
+            raise ValueError("Dirichlet value size mismatch")
+        _err(lib().ikr_assembler_set_dirichlet_values(self.h, _ptr(r)), "set_dirichlet_values")
 
     def vector(self, req=None, affordance=VectorAffordance.forces, dbc=None, export=True):
         """Assembles on the device; returns the host copy unless export=False."""

@@ -361,9 +361,10 @@ cudaError_t launch_persistent(const Bsr& A, PcgWork& w, cudaStream_t s, bool que
   }
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-  // one wave of co-resident CTAs; the partial buffers hold 2 (part_a) and 4 (part_b) values per CTA
+  // one wave of co-resident CTAs; the partial buffers hold 2 w.grid (part_a) and 4 w.grid (part_b) values,
+  // 2 and 4 per CTA here
   int grid = bps > 0 ? w.sms * bps : 0;
-  if (grid > w.grid / 2) grid = w.grid / 2;
+  if (grid > w.grid) grid = w.grid;
   const int nw = grid * WARPS;
   *eligible = coop && grid > 0 && (int64_t)nw * MAXS >= A.n_slices;
   if (query_only || !*eligible) return cudaSuccess;
@@ -384,17 +385,19 @@ cudaError_t dispatch(int variant, const Bsr& A, PcgWork& w, cudaStream_t s, bool
   if constexpr (sizeof(T) == 4) {
     if (variant == 0) return launch_persistent<float, 8, 2, 8, 4, 1>(A, w, s, query, eligible);
     if (variant == 1) return launch_persistent<float, 4, 3, 8, 8, 1>(A, w, s, query, eligible);
-    return launch_persistent<float, 4, 2, 8, 2, 2>(A, w, s, query, eligible);
+    if (variant == 2) return launch_persistent<float, 4, 2, 8, 2, 2>(A, w, s, query, eligible);
+    return launch_persistent<float, 2, 3, 8, 2, 3>(A, w, s, query, eligible);
   } else {
     if (variant == 0) return launch_persistent<double, 4, 2, 8, 4, 1>(A, w, s, query, eligible);
     if (variant == 1) return launch_persistent<double, 2, 3, 8, 4, 1>(A, w, s, query, eligible);
-    return launch_persistent<double, 2, 2, 8, 2, 2>(A, w, s, query, eligible);
+    if (variant == 2) return launch_persistent<double, 2, 2, 8, 2, 2>(A, w, s, query, eligible);
+    return launch_persistent<double, 1, 3, 8, 2, 2>(A, w, s, query, eligible);
   }
 }
 
 }  // namespace
 
-int pcg_persistent_variants() { return 3; }
+int pcg_persistent_variants() { return 4; }
 
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant) {
   bool ok = false;

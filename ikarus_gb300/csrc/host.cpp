@@ -728,6 +728,23 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
     ls->set_launch(use_graphs != 0, chunk_len);
   });
 }
+int ikr_assembler_set_dirichlet_values(ikr_asm a, const double* rate) {
+  return guarded([&] {
+    need(a, IKR_ERR_ARG, "null argument");
+    if (!rate) {
+      a->has_idbc = false;
+      a->idbc_rate.release();
+      return;
+    }
+    for (int i = 0; i < a->n; ++i) {
+      need(std::isfinite(rate[i]), IKR_ERR_ARG, "non-finite Dirichlet value");
+      need(rate[i] == 0.0 || a->fixed_h[i], IKR_ERR_ARG, "a Dirichlet value on a free dof");
+    }
+    a->idbc_rate.upload(rate, a->n, a->fes->stream);
+    CK(cudaStreamSynchronize(a->fes->stream));
+    a->has_idbc = true;
+  });
+}
 int ikr_fes_kernel_info(ikr_fes fes, int32_t* epb_residual, int32_t* epb_tangent64, int32_t* epb_tangent32) {
   return guarded([&] {
     need(fes, IKR_ERR_ARG, "null argument");
@@ -1042,10 +1059,17 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   if (info) *info = inf;
 }
 
+// the inhomogeneous Dirichlet values at the requirement's load factor (nonlinearsolverfactory.hh:45-52)
+void idbc_sync(ikr_asm a, ikr_req r) {
+  ikr::launch_idbc_sync(r->u.p, a->idbc_rate.p, r->lambda, 3LL * a->fes->nn, a->fes->stream);
+  count(1);
+  r->version++;
+}
+
 void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double ref_norm) {
-  (void)step_size;
   if (nr->asm_->fes->n_inst > 0 && nr->ls->tag == IKR_SOLVER_GPU_PCG_BATCHED) {
     need(nr->asm_->fes->na == 0, IKR_ERR_NOT_IMPLEMENTED, "the batched solve supports displacement-based elements");
+    need(!nr->asm_->has_idbc, IKR_ERR_NOT_IMPLEMENTED, "the batched solve has no inhomogeneous Dirichlet values");
     nr_solve_batched(nr, r, info);
     return;
   }
@@ -1071,10 +1095,19 @@ void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double 
   nr->corr.alloc(n);
   nr->rhs.alloc(n);
   assemble_vector(a, r, IKR_DBC_FULL);
+  bool k_valid = false;
+  if (a->has_idbc && step_size != 0.0) {
+    // rx += idbcForce(x) * stepSize (newtonraphson.hh:212-215): obtainForcesDueToIDBC (functionhelper.hh:170-184)
+    // = K_raw du_D/dlambda, zero at the constrained dofs
+    assemble_matrix(a, r, IKR_DBC_RAW);
+    a->idbc_force.alloc(n);
+    ikr::launch_spmv64(a->bsr(), a->fp32, a->idbc_rate.p, a->idbc_force.p, f->stream);
+    ikr::launch_idbc_force(a->R.p, a->idbc_force.p, a->node_fixed.p, step_size, n, f->stream);
+    count(2);
+  }
   double rnorm = device_norm(f, a->R.p, n, nr->nrm_part, nr->nrm_out);
   inf.residual_norm = rnorm;
   const double thr = st.tol_mode == 1 ? st.tol * (ref_norm > 0.0 ? ref_norm : rnorm) : st.tol;
-  bool k_valid = false;
   if (!a->nb) a->build_pattern();
   nr->ls->setup(a);
   int iter = 0;
@@ -1115,6 +1148,7 @@ void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double 
       if (nr->fe_state) update_state(f, r, nr->corr.p);
       ikr::launch_axpy64(r->u.p, nr->corr.p, 1.0, n, f->stream);
       count(1);
+      if (a->has_idbc) idbc_sync(a, r);  // syncParameterAndGlobalSolution (newtonraphson.hh:235-236)
       r->version++;
       try {
         assemble_vector(a, r, IKR_DBC_FULL);
@@ -1222,6 +1256,7 @@ int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_in
         r->lambda += step;  // LoadControl::predictor (loadcontrol.inl:54-57)
         const double ref = predictor_apply(lc, r, ls);  // optional displacement prediction, FP64-gated
         nr_solve(lc->nr, r, step, &ni, ref);
+        if (ni.iterations == 0 && lc->nr->asm_->has_idbc) idbc_sync(lc->nr->asm_, r);  // loadcontrol.inl:43-44
         predictor_end_step(lc, r, ls);
         record(ni);
         if (!ni.success) {

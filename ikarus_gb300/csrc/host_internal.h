@@ -245,6 +245,9 @@ struct ikr_asm_s {
   std::vector<uint8_t> fixed_h;
   std::vector<int32_t> cb_h;
   DBuf<uint8_t> node_fixed;
+  // inhomogeneous Dirichlet values u_D(lambda) = lambda * idbc_rate on constrained dofs (empty: none)
+  DBuf<double> idbc_rate, idbc_force;
+  bool has_idbc = false;
   // pattern
   int64_t nb = 0, npad = 0;
   int nslices = 0;
@@ -418,8 +421,8 @@ struct ikr_ls_s {
       dx.alloc(n), dr.alloc(n), dz.alloc(n), dp.alloc(n), dp1.alloc(n), dq.alloc(n), dmv.alloc(9 * (size_t)nr);
       w.x = dx.p, w.r = dr.p, w.z = dz.p, w.p0 = dp.p, w.p1 = dp1.p, w.q = dq.p, w.minv = dmv.p;
     }
-    pa.alloc(w.grid);
-    pb.alloc(2 * (size_t)w.grid);
+    pa.alloc(2 * (size_t)w.grid);  // two-kernel CG: 1 per block; persistent CG: 2 per CTA (parity)
+    pb.alloc(4 * (size_t)w.grid);  // two-kernel CG: 2 per block; persistent CG: 4 per CTA
     scal.alloc(ikr::kNScal);
     w.part_a = pa.p;
     w.part_b = pb.p;

@@ -107,6 +107,9 @@ void launch_bsr_reset(void* val, bool fp32, int64_t n_padded, const int32_t* dia
 void launch_vector_finish(double* R, const uint8_t* node_fixed, int n_nodes, const int32_t* pl_dof,
                           const double* pl_val, int n_pl, double load_factor, cudaStream_t s);
 void launch_norm2(const double* x, int64_t n, double* partials, double* out, cudaStream_t s);
+// inhomogeneous Dirichlet values: u[i] = lambda rate[i] where nonzero; R += step F on the free dofs
+void launch_idbc_sync(double* u, const double* rate, double lambda, int64_t n, cudaStream_t s);
+void launch_idbc_force(double* R, const double* F, const uint8_t* node_fixed, double step, int64_t n, cudaStream_t s);
 void launch_dot(const double* x, const double* y, int64_t n, double* partials, double* out, cudaStream_t s);
 
 // solver.cu -- block-Jacobi preconditioned CG

@@ -188,6 +188,20 @@ __global__ void point_load_kernel(double* R, const int32_t* __restrict__ dof, co
   R[dof[k]] += lf * val[k];
 }
 
+// inhomogeneous Dirichlet values: u[i] = lambda rate[i] where that value is nonzero
+__global__ void idbc_sync_kernel(double* __restrict__ u, const double* __restrict__ rate, double lambda, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = lambda * rate[i];
+    if (v != 0.0) u[i] = v;
+  }
+}
+// R += step F on the free dofs (F = K_raw du_D/dlambda)
+__global__ void idbc_force_kernel(double* __restrict__ R, const double* __restrict__ F,
+                                  const uint8_t* __restrict__ node_fixed, double step, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (!((node_fixed[i / 3] >> (i % 3)) & 1)) R[i] += step * F[i];
+}
+
 // deterministic sum of squares: fixed grid, per-block partials, then one block sums them in order
 __global__ void sumsq_partial_kernel(const double* __restrict__ x, int64_t n, double* part) {
   double s = 0.0;
@@ -281,6 +295,12 @@ void launch_vector_finish(double* R, const uint8_t* node_fixed, int n_nodes, con
   (void)node_fixed;
   (void)n_nodes;
   if (n_pl > 0) point_load_kernel<<<blocks_for(n_pl, 128), 128, 0, s>>>(R, pl_dof, pl_val, n_pl, load_factor);
+}
+void launch_idbc_sync(double* u, const double* rate, double lambda, int64_t n, cudaStream_t s) {
+  idbc_sync_kernel<<<kNormGrid, 256, 0, s>>>(u, rate, lambda, n);
+}
+void launch_idbc_force(double* R, const double* F, const uint8_t* node_fixed, double step, int64_t n, cudaStream_t s) {
+  idbc_force_kernel<<<kNormGrid, 256, 0, s>>>(R, F, node_fixed, step, n);
 }
 void launch_norm2(const double* x, int64_t n, double* partials, double* out, cudaStream_t s) {
   sumsq_partial_kernel<<<kNormGrid, 256, 0, s>>>(x, n, partials);

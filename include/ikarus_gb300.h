@@ -151,6 +151,13 @@ int ikr_assembler_matrix(ikr_asm a, ikr_req req, int32_t affordance, int32_t dbc
  * SparseMatrix): col_ptr (cols+1), row_idx (nnz), values (nnz); pass NULLs to query nnz. */
 int ikr_assembler_matrix_nnz(ikr_asm a, int32_t dbc_option, int64_t* nnz);
 int ikr_assembler_export_csc(ikr_asm a, int32_t dbc_option, int64_t* col_ptr, int32_t* row_idx, double* values);
+/* inhomogeneous Dirichlet values (DirichletValues::storeInhomogeneousBoundaryCondition, dirichletvalues.hh:213-222,
+ * for values linear in the load factor): u_D(lambda) = lambda * rate on constrained dofs (rate must vanish on free
+ * dofs; NULL removes them).  NewtonRaphson then adds the IDBC forces K_raw rate * stepSize to its first residual
+ * (newtonraphson.hh:212-215, functionhelper.hh:170-184) and sets the constrained entries to u_D(lambda) after
+ * every update (nonlinearsolverfactory.hh:45-52); LoadControl also after a step that needed no iteration
+ * (loadcontrol.inl:43-44).  Not available in batched solves. */
+int ikr_assembler_set_dirichlet_values(ikr_asm a, const double* rate);
 /* the block pattern itself: row_ptr (n_nodes+1), col (n_blocks) */
 int ikr_assembler_block_pattern(ikr_asm a, int32_t* n_rows, int64_t* n_blocks, int32_t* row_ptr, int32_t* col);
 /* ||R|| of the last assembled vector (FP64, deterministic device reduction) */
@@ -176,7 +183,7 @@ int ikr_linear_solver_profile_read(ikr_ls ls, double* spmv_ms_total, int64_t* sp
  * (default) or launched kernel by kernel otherwise (for profilers that do not follow graph kernels). */
 int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_len);
 /* CG kernels (no reference counterpart).  spmv_kind 0 = two kernels per iteration with a direct-load SpMV,
- * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..7 = the
+ * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..8 = the
  * whole solve in one persistent cooperative kernel (grid barriers for the two reductions of an iteration;
  * only where every warp's rows fit its registers), -1 = autotune; l2_keep_fraction in [0, 1) = share of the
  * matrix the staged kernels keep in L2 across iterations, -1 = autotune.  The choice is made at the

@@ -58,6 +58,7 @@ def lib():
         L.orc_pattern_nnz.argtypes = [vp, C.c_int]
         L.orc_reduced_size.argtypes = [vp]
         L.orc_assemble_matrix_csc.argtypes = [vp, dp, C.c_double, C.c_int, lp, ip, dp]
+        L.orc_set_dirichlet_values.argtypes = [vp, dp]
         L.orc_cg_jacobi_csc.argtypes = [C.c_int, lp, ip, dp, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
                                        C.c_double, dp, dp, ip, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -126,6 +127,14 @@ class OracleProblem:
     def set_dirichlet(self, fixed):
         f = np.ascontiguousarray(fixed, dtype=np.uint8)
         _check(lib().orc_set_dirichlet(self.h, _p(f, C.c_uint8)), "set_dirichlet")
+
+    def set_dirichlet_values(self, rate):
+        """Inhomogeneous Dirichlet values lambda * rate on constrained dofs (None removes them)."""
+        if rate is None:
+            _check(lib().orc_set_dirichlet_values(self.h, None), "set_dirichlet_values")
+            return
+        r = np.ascontiguousarray(rate, dtype=np.float64)
+        _check(lib().orc_set_dirichlet_values(self.h, _p(r, C.c_double)), "set_dirichlet_values")
 
     def add_neumann(self, face_elem, face_local, traction):
         fe = np.ascontiguousarray(face_elem, dtype=np.int32)

@@ -249,6 +249,8 @@ struct orc_problem {
   std::vector<std::vector<std::pair<int, std::array<double, 3>>>> faces;
   std::vector<int32_t> pl_dof;
   std::vector<double> pl_val;
+  // inhomogeneous Dirichlet values u_D(lambda) = lambda * idbc_rate on constrained dofs (empty: none)
+  std::vector<double> idbc_rate;
   // pattern caches
   std::vector<std::vector<int32_t>> nodeAdj;
   int ndof() const { return 3 * nn; }
@@ -891,6 +893,19 @@ int orc_set_dirichlet(orc_problem* p, const uint8_t* f) {
   for (int i = 0; i < p->ndof(); ++i) p->fixed[i] = f[i] ? 1 : 0;
   return ORC_OK;
 }
+// DirichletValues::storeInhomogeneousBoundaryCondition (dirichletvalues.hh:213-222) for prescribed values linear
+// in the load factor: u_D(lambda) = lambda * rate, derivative rate; rate must vanish on free dofs.
+int orc_set_dirichlet_values(orc_problem* p, const double* rate) {
+  if (!p) return ORC_ERR_ARG;
+  if (!rate) {
+    p->idbc_rate.clear();
+    return ORC_OK;
+  }
+  for (int i = 0; i < p->ndof(); ++i)
+    if ((rate[i] != 0.0 && !p->fixed[i]) || !std::isfinite(rate[i])) return ORC_ERR_ARG;
+  p->idbc_rate.assign(rate, rate + p->ndof());
+  return ORC_OK;
+}
 int orc_add_neumann(orc_problem* p, int nf, const int32_t* fe, const int32_t* fl, const double* t) {
   if (!p || nf < 0) return ORC_ERR_ARG;
   if (p->faces.empty()) p->faces.assign(p->ne, {});
@@ -1011,10 +1026,32 @@ int orc_load_control(orc_problem* p, int steps, double t0, double t1, double tol
   const double step = (t1 - t0) / steps;  // loadcontrol.hh:77
   int total = 0, solves = 0;
   CSC K;
+  const bool idbc = !p->idbc_rate.empty();
+  // syncParameterAndGlobalSolution with the inhomogeneous values (nonlinearsolverfactory.hh:45-52): entries whose
+  // prescribed value is nonzero take it
+  auto sync = [&]() {
+    if (!idbc) return;
+    for (int i = 0; i < n; ++i) {
+      const double v = *lambda * p->idbc_rate[i];
+      if (v != 0.0) x[i] = v;
+    }
+  };
   for (int s = 0; s <= steps; ++s) {
     if (s > 0) *lambda += step;  // LoadControl::predictor (loadcontrol.inl:54-57)
+    const double step_size = s > 0 ? step : 0.0;  // solve(x) for the initial check, solve(x, stepSize) after
     int st = assemble_vector(*p, x.data(), *lambda, ORC_DBC_FULL, R);
     if (st) return st;
+    if (idbc && step_size != 0.0) {
+      // rx += idbcForce(x) * stepSize (newtonraphson.hh:212-215) with obtainForcesDueToIDBC
+      // (functionhelper.hh:170-184): K_raw * du_D/dlambda, zero at constrained dofs
+      st = assemble_matrix(*p, x.data(), ORC_DBC_RAW, K);
+      if (st) return st;
+      std::vector<double> F(n, 0.0);
+      for (int c = 0; c < n; ++c)
+        for (int64_t k = K.cp[c]; k < K.cp[c + 1]; ++k) F[K.ri[k]] += K.v[k] * p->idbc_rate[c];
+      for (int i = 0; i < n; ++i)
+        if (!p->fixed[i]) R[i] += F[i] * step_size;
+    }
     double rn = norm2(R);
     const double thr = tol_mode == 1 ? tol * rn : tol;
     int it = 0;
@@ -1029,11 +1066,13 @@ int orc_load_control(orc_problem* p, int steps, double t0, double t1, double tol
       st = update_state(*p, x.data(), dx.data());  // CORRECTION_UPDATED before x += dx (newtonraphson.hh:230-233)
       if (st) return st;
       for (int i = 0; i < n; ++i) x[i] += dx[i];
+      sync();  // newtonraphson.hh:235-236
       st = assemble_vector(*p, x.data(), *lambda, ORC_DBC_FULL, R);
       if (st) return st;
       rn = norm2(R);
       ++it;
     }
+    if (it == 0) sync();  // loadcontrol.inl:43-44
     if (iterations) iterations[s] = it;
     if (res_norms) res_norms[s] = rn;
     total += it;

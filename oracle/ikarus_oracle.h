@@ -48,6 +48,9 @@ void orc_problem_destroy(orc_problem* p);
 int orc_set_dirichlet(orc_problem* p, const uint8_t* fixed_dofs);
 /* Dead Neumann load on element faces (Dune face numbering: 2d -> xi_d = 0, 2d+1 -> xi_d = 1).
  * traction: 3 values per face = t(X_face_center, lambda = 1); the applied load is lambda * t. */
+/* inhomogeneous Dirichlet values u_D(lambda) = lambda * rate on constrained dofs (rate zero on free dofs;
+ * NULL removes them); load_control then applies them like the reference's NR with its IDBC force function */
+int orc_set_dirichlet_values(orc_problem* p, const double* rate);
 int orc_add_neumann(orc_problem* p, int n_faces, const int32_t* face_elem, const int32_t* face_local,
                     const double* traction);
 /* Manipulator-style point loads: after the Dirichlet treatment, R[dof] += lambda * value. */

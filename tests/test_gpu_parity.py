@@ -303,3 +303,37 @@ def test_backtracking_recovers_a_step_the_reference_aborts(ikr):
     info, u = run(30)
     assert info.success
     assert np.abs(u - ref["u"]).max() <= 1e-7 * np.abs(ref["u"]).max()
+
+
+@pytest.mark.parametrize("eas,n", [(0, 0), (1, 9)])
+def test_inhomogeneous_dirichlet_values_match_oracle(ikr, eas, n):
+    """Prescribed tip displacement lambda * (-2) (storeInhomogeneousBoundaryCondition) under LoadControl: the
+    device Newton adds the IDBC forces K_raw rate * stepSize to its first residual and re-imposes the values
+    after every update like the reference; iteration counts per step and the converged displacement match the
+    oracle, the constrained entries end exactly at lambda * rate, and the mixed form reaches the same state."""
+    p = problems.cantilever(8, 2, 2, traction=(0.0, 0.0, 0.0), load_steps=4, tol=1e-10, eas=eas, n_eas=n)
+    tip = np.nonzero(np.abs(p.mesh.coords[:, 0] - p.mesh.lengths[0]) < 1e-8)[0]
+    fixed = p.fixed.copy()
+    fixed[3 * tip + 2] = 1
+    rate = np.zeros(p.n_dofs)
+    rate[3 * tip + 2] = -2.0
+    p.fixed = fixed
+    o = oracle.from_problem(p)
+    o.set_dirichlet_values(rate)
+    ref = o.load_control(4, tol=1e-10, max_iter=30)
+    for precision in (0, 1):
+        fes, asm = problems.build_gpu(p, precision=precision)
+        asm.set_dirichlet_values(rate)
+        req = ikr.FERequirements(fes)
+        if precision == 0:
+            st = ikr.NRSettings(tol=1e-10, maxIter=30, linear_rtol=1e-13)
+        else:
+            st = ikr.NRSettings(tol=1e-10, maxIter=40, eisenstat_walker=True, linear_rtol=1e-2, linear_rtol_min=1e-6)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(rtol=1e-13)))
+        info = ikr.LoadControl(nr, 4).run(req)
+        assert info.success
+        u = req.globalSolution()
+        assert np.array_equal(u[rate != 0], rate[rate != 0])
+        assert np.abs(u - ref["u"]).max() <= 1e-8 * np.abs(ref["u"]).max()
+        if precision == 0:
+            assert [s.iterations for s in info.solverInfos] == list(ref["iterations"])

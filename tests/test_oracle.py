@@ -155,3 +155,33 @@ def test_oracle_cg_matches_a_direct_solve():
     A = sp.csc_matrix((v, ri, cp), shape=(n, n))
     assert ok and 0 < its < 5000
     assert np.abs(x - sla.spsolve(A, b)).max() <= 1e-8 * np.abs(x).max()
+
+
+def _prescribed_tip(p, uz):
+    """The cantilever's tip face z-displacements prescribed as lambda * uz (inhomogeneous Dirichlet values)."""
+    tip = np.nonzero(np.abs(p.mesh.coords[:, 0] - p.mesh.lengths[0]) < 1e-8)[0]
+    fixed = p.fixed.copy()
+    fixed[3 * tip + 2] = 1
+    rate = np.zeros(p.n_dofs)
+    rate[3 * tip + 2] = uz
+    p.fixed = fixed
+    return rate
+
+
+def test_oracle_inhomogeneous_dirichlet_values():
+    """storeInhomogeneousBoundaryCondition semantics (dirichletvalues.hh:213-282, nonlinearsolverfactory.hh:45-52):
+    the constrained entries end at lambda * rate, the free residual vanishes, and the equilibrium does not depend
+    on the number of load steps."""
+    res = []
+    for steps in (4, 8):
+        p = problems.cantilever(8, 2, 2, traction=(0.0, 0.0, 0.0), load_steps=steps, tol=1e-10)
+        rate = _prescribed_tip(p, -2.0)
+        o = oracle.from_problem(p)
+        o.set_dirichlet_values(rate)
+        r = o.load_control(steps, tol=1e-10, max_iter=30)
+        u = r["u"]
+        assert np.array_equal(u[rate != 0], rate[rate != 0])
+        R = o.assemble_vector(u, 1.0)
+        assert np.abs(R[p.fixed == 0]).max() <= 1e-9
+        res.append(u)
+    assert np.abs(res[0] - res[1]).max() <= 1e-8 * np.abs(res[1]).max()
