@@ -271,6 +271,122 @@ __global__ void traction_kernel(const double* __restrict__ X, const int32_t* __r
   for (int k = 0; k < 24; ++k) trac[24 * (size_t)s + k] = acc[k];
 }
 
+// FP64 residual assembly with the material work spread over the Gauss points: lane q of an element's 8 lanes
+// evaluates Gauss point q (geometry J, dN/dX of all 8 nodes, F, F^-1, ln J, P) once, instead of every lane
+// evaluating every Gauss point; the nodal forces w P dN_v of each point are exchanged through shared memory and
+// lane v sums its node's over the points in ascending order.  About a quarter of the FP64 operations of the
+// node-per-lane form, which matters because GB300's FP64 rate bounds this kernel.
+template <int EPB>
+__global__ void __launch_bounds__(EPB * 8) disp_residual_gp_kernel(ElemArgs a, const int32_t* __restrict__ list,
+                                                                    int n_list, int e_base) {
+  __shared__ double fs[EPB][8][8][3];  // [element][Gauss point][node][component]
+  const int lane = threadIdx.x & 31;
+  const int sub = threadIdx.x & 7;  // node for loads and the scatter, Gauss point for the material work
+  const int es = threadIdx.x >> 3;
+  const int li = blockIdx.x * EPB + es;
+  const bool active = li < n_list;
+  const int lic = active ? li : n_list - 1;
+  const int e = list ? list[lic] : e_base + lic;
+  const int ne = a.n_elems;
+  const int node = a.conn[sub * ne + e];
+  const int src = lane & ~7;
+  double Xd[3], Ud[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    Xd[c] = a.X[3 * node + c];
+    Ud[c] = a.u ? a.u[3 * node + c] : 0.0;
+  }
+  // coordinates and displacements relative to the element's first corner (as the node-per-lane kernel does)
+  double dX[3], dU[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    dX[c] = Xd[c] - __shfl_sync(0xffffffffu, Xd[c], src);
+    dU[c] = Ud[c] - __shfl_sync(0xffffffffu, Ud[c], src);
+  }
+  const double lam = a.lam_e ? a.lam_e[e] : a.lam, mu = a.mu_e ? a.mu_e[e] : a.mu;
+  const int q = sub;
+  // J = sum_v dX_v (x) dxi_v(q)
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    double xv[3], dxi[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) xv[c] = __shfl_sync(0xffffffffu, dX[c], src + v);
+    ref_gradient_at_gp<double>(v, q, dxi);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) J[i][j] += xv[i] * dxi[j];
+  }
+  double Ji[3][3];
+  const double detJ = inv3(J, Ji);
+  // F = I + sum_v dU_v (x) dN_v(q)
+  double F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    double uv[3], dxi[3], dN[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) uv[c] = __shfl_sync(0xffffffffu, dU[c], src + v);
+    ref_gradient_at_gp<double>(v, q, dxi);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dN[k] = dxi[0] * Ji[0][k] + dxi[1] * Ji[1][k] + dxi[2] * Ji[2][k];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) F[i][j] += uv[i] * dN[j];
+  }
+  double Fi[3][3];
+  const double detF = inv3(F, Fi);
+  int bad = 0;
+  // det C = det(F)^2 must exceed 1e-10 (checkPositiveOrAbort); NaN fails the test as well
+  if (!(detF * detF > 1e-10) || !(detF > 0.0)) bad |= kStatusNonPositiveDetC;
+  const double lnJ = log(detF);
+  const double w = kGaussW * detJ;
+  // P = mu (F - F^-T) + lambda ln J F^-T (F - F^-T keeps the undeformed internal force exactly zero)
+  double P[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) P[i][j] = w * (mu * (F[i][j] - Fi[j][i]) + lam * lnJ * Fi[j][i]);
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    double dxi[3], dN[3];
+    ref_gradient_at_gp<double>(v, q, dxi);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) dN[k] = dxi[0] * Ji[0][k] + dxi[1] * Ji[1][k] + dxi[2] * Ji[2][k];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) fs[es][q][v][i] = P[i][0] * dN[0] + P[i][1] * dN[1] + P[i][2] * dN[2];
+  }
+  __syncwarp();
+  double f[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+  for (int g = 0; g < 8; ++g)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) f[i] += fs[es][g][sub][i];
+  if (a.trac_idx) {
+    const int t = a.trac_idx[e];
+    if (t >= 0) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] -= a.load_factor * a.trac[24 * t + 3 * sub + c];
+    }
+  }
+  if (!active) return;
+  if (bad) {
+    if (a.inst_status) atomicOr(a.inst_status + a.elem_inst[e], bad);
+    else if (a.status) atomicOr(a.status, bad);
+  }
+  const uint8_t fmask = a.node_fixed ? a.node_fixed[node] : uint8_t(0);
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    if (!((fmask >> c) & 1)) a.R[3 * node + c] += f[c];
+}
+
+template <int EPB>
+void launch_residual_gp(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
+  const int blocks = (n_list + EPB - 1) / EPB;
+  disp_residual_gp_kernel<EPB><<<blocks, EPB * 8, 0, s>>>(a, list, n_list, e_base);
+}
+
 template <typename KT, int MODE, int EPB>
 void launch_disp_epb(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
   const int blocks = (n_list + EPB - 1) / EPB;
@@ -292,7 +408,10 @@ void launch_disp_element(const ElemArgs& a, int mode, bool fp32_tangent, const i
                          cudaStream_t s) {
   if (n_list <= 0) return;
   switch (mode) {
-    case kWantR: launch_disp_t<double, kWantR>(a, list, n_list, e_base, s); break;
+    case kWantR:  // assembled residual: Gauss-point-per-lane kernel (its shared exchange fits up to 32 per block)
+      if (a.epb == 16) launch_residual_gp<16>(a, list, n_list, e_base, s);
+      else launch_residual_gp<32>(a, list, n_list, e_base, s);
+      break;
     case kWantR | kWantK: launch_disp_t<double, kWantR | kWantK>(a, list, n_list, e_base, s); break;
     case kWantK:
       if (fp32_tangent) launch_disp_t<float, kWantK>(a, list, n_list, e_base, s);
