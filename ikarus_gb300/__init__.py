@@ -145,6 +145,7 @@ SIGNATURES = {
     "ikr_fe_calculate_matrix": ([_vp, _vp, _I, _I, _I, _dp], C.c_int),
     "ikr_fe_calculate_scalar": ([_vp, _vp, _I, _I, _I, _dp], C.c_int),
     "ikr_fe_update_state": ([_vp, _vp, _dp, _I], C.c_int),
+    "ikr_fe_calculate_at": ([_vp, _vp, _I, _I, _I, _dp, _I, _dp], C.c_int),
     "ikr_req_create": ([C.POINTER(_vp), _vp], C.c_int),
     "ikr_req_destroy": ([_vp], C.c_int),
     "ikr_req_insert_global_solution": ([_vp, _dp], C.c_int),
@@ -395,6 +396,27 @@ def calculateScalar(fes: FiniteElements, req: FERequirements,
     e0, e1 = elements if elements is not None else (0, fes.n_elems)
     out = np.zeros(e1 - e0)
     _err(lib().ikr_fe_calculate_scalar(fes.h, req.h, int(affordance), e0, e1, _ptr(out)), "calculateScalar")
+    return out
+
+
+class ResultTypes(enum.IntEnum):  # feresulttypes.hh:125-128 (the stresses of the nonlinear-elastic element)
+    PK2Stress = 0
+    kirchhoffStress = 1
+    cauchyStress = 2
+
+
+def calculateAt(fes: FiniteElements, req: FERequirements, result_type: ResultTypes, local=(0.5, 0.5, 0.5),
+                elements=None):
+    """Stress at local points of the reference cube (nonlinearelastic.hh:237-271): one point for all elements or
+    one per element (n x 3); returns n x 6 Voigt values [11, 22, 33, 23, 13, 12]."""
+    e0, e1 = elements if elements is not None else (0, fes.n_elems)
+    loc = np.ascontiguousarray(local, dtype=np.float64)
+    per = loc.ndim == 2
+    if per and loc.shape != (e1 - e0, 3):
+        raise ValueError("one local point per element expected")
+    out = np.zeros((e1 - e0, 6))
+    _err(lib().ikr_fe_calculate_at(fes.h, req.h, int(result_type), e0, e1, _ptr(loc), int(per), _ptr(out)),
+         "calculateAt")
     return out
 
 

@@ -387,6 +387,96 @@ void launch_residual_gp(const ElemArgs& a, const int32_t* list, int n_list, int 
   disp_residual_gp_kernel<EPB><<<blocks, EPB * 8, 0, s>>>(a, list, n_list, e_base);
 }
 
+// calculateAt<PK2Stress / kirchhoffStress / cauchyStress> (nonlinearelastic.hh:237-271) of elements
+// [e0, e0 + count) at local points xi (one per element or one for all): thread per element, FP64.
+// H at xi, E = GL(H), C = 2E + I, S = mu (I - C^-1) + lambda ln J C^-1, tau = F S F^T, sigma = tau / det F
+// (stressconversions.hh:88-125); Voigt [11, 22, 33, 23, 13, 12] without shear factors.
+__global__ void stress_at_kernel(ElemArgs a, int e0, int count, const double* __restrict__ xi, int xi_per_elem,
+                                 int type, double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const int e = e0 + k;
+  const int ne = a.n_elems;
+  const double* x = xi + (xi_per_elem ? 3 * k : 0);
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  double dxi[8][3], U[8][3];
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    const int node = a.conn[v * ne + e];
+    double f[3], df[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const bool b = (v >> d) & 1;
+      f[d] = b ? x[d] : 1.0 - x[d];
+      df[d] = b ? 1.0 : -1.0;
+    }
+    dxi[v][0] = df[0] * f[1] * f[2];
+    dxi[v][1] = f[0] * df[1] * f[2];
+    dxi[v][2] = f[0] * f[1] * df[2];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) U[v][c] = a.u ? a.u[3 * node + c] : 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) J[i][j] += a.X[3 * node + i] * dxi[v][j];
+  }
+  double Ji[3][3];
+  inv3(J, Ji);
+  double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    double dN[3];
+#pragma unroll
+    for (int kk = 0; kk < 3; ++kk) dN[kk] = dxi[v][0] * Ji[0][kk] + dxi[v][1] * Ji[1][kk] + dxi[v][2] * Ji[2][kk];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) H[i][j] += U[v][i] * dN[j];
+  }
+  double C[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double hh = H[0][i] * H[0][j] + H[1][i] * H[1][j] + H[2][i] * H[2][j];
+      C[i][j] = H[i][j] + H[j][i] + hh + (i == j ? 1.0 : 0.0);
+    }
+  double Ci[3][3];
+  const double detC = inv3(C, Ci);
+  if (!(detC > 1e-10) && a.status) atomicOr(a.status, kStatusNonPositiveDetC);
+  const double lam = a.lam_e ? a.lam_e[e] : a.lam, mu = a.mu_e ? a.mu_e[e] : a.mu;
+  const double lnJ = log(sqrt(detC));
+  double S[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+  double R[3][3];
+  if (type == 0) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) R[i][j] = S[i][j];
+  } else {
+    double F[3][3], FS[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) F[i][j] = H[i][j] + (i == j ? 1.0 : 0.0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) FS[i][j] = F[i][0] * S[0][j] + F[i][1] * S[1][j] + F[i][2] * S[2][j];
+    const double sc = type == 2 ? 1.0 / det3(F) : 1.0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) R[i][j] = sc * (FS[i][0] * F[j][0] + FS[i][1] * F[j][1] + FS[i][2] * F[j][2]);
+  }
+  double* o = out + 6 * (size_t)k;
+  o[0] = R[0][0], o[1] = R[1][1], o[2] = R[2][2], o[3] = R[1][2], o[4] = R[0][2], o[5] = R[0][1];
+}
+
 template <typename KT, int MODE, int EPB>
 void launch_disp_epb(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
   const int blocks = (n_list + EPB - 1) / EPB;
@@ -425,6 +515,12 @@ void launch_disp_element(const ElemArgs& a, int mode, bool fp32_tangent, const i
     case kWantEnergy | kElemOut: launch_disp_t<double, kWantEnergy | kElemOut>(a, list, n_list, e_base, s); break;
     default: break;
   }
+}
+
+void launch_stress_at(const ElemArgs& a, int e0, int count, const double* xi, bool xi_per_elem, int type, double* out,
+                      cudaStream_t s) {
+  if (count <= 0) return;
+  stress_at_kernel<<<(count + 127) / 128, 128, 0, s>>>(a, e0, count, xi, xi_per_elem ? 1 : 0, type, out);
 }
 
 void launch_traction_loads(const double* X, const int32_t* conn, int n_elems, int n_slots, const int32_t* slot_elem,

@@ -400,6 +400,29 @@ int ikr_fe_calculate_scalar(ikr_fes fes, ikr_req req, int32_t aff, int32_t e0, i
     element_level(fes, req, ikr::kWantEnergy | ikr::kElemOut, e0, e1, out, 1);
   });
 }
+int ikr_fe_calculate_at(ikr_fes fes, ikr_req req, int32_t result_type, int32_t e_begin, int32_t e_end,
+                        const double* local, int32_t local_per_element, double* out) {
+  return guarded([&] {
+    need(fes && req && req->fes == fes && local && out, IKR_ERR_ARG, "invalid arguments");
+    need(result_type >= IKR_RESULT_PK2_STRESS && result_type <= IKR_RESULT_CAUCHY_STRESS, IKR_ERR_NOT_IMPLEMENTED,
+         "result type not implemented");
+    need(fes->na == 0, IKR_ERR_NOT_IMPLEMENTED, "calculateAt is implemented for displacement-based elements");
+    need(e_begin >= 0 && e_end <= fes->ne && e_begin <= e_end, IKR_ERR_ARG, "element range out of bounds");
+    const int count = e_end - e_begin;
+    if (count == 0) return;
+    cudaStream_t s = fes->stream;
+    DBuf<double> xi, o;
+    xi.upload(local, local_per_element ? 3 * (size_t)count : 3, s);
+    o.alloc(6 * (size_t)count);
+    ikr::ElemArgs args = fes->args();
+    args.u = req->u.p;
+    ikr::launch_stress_at(args, e_begin, count, xi.p, local_per_element != 0, result_type, o.p, s);
+    ikr_host::count(1);
+    o.download(out, 6 * (size_t)count, s);
+    CK(cudaStreamSynchronize(s));
+    fes->check_status();
+  });
+}
 int ikr_fe_update_state(ikr_fes fes, ikr_req req, const double* correction, int32_t n) {
   return guarded([&] {
     need(fes && req && correction && req->fes == fes, IKR_ERR_ARG, "invalid arguments");

@@ -570,7 +570,9 @@ struct ikr_ls_s {
         if (us < best) best = us, best_kind = k;
       }
       for (int v = 0; v < ikr::pcg_persistent_variants(); ++v) {
-        if (!ikr::pcg_persistent_eligible(A, w, v)) continue;
+        // the pipelined variants' recurrences drift (attainable relative residual about 1e-9 in FP64): they are
+        // available on request, the tuner does not pick them
+        if (v >= ikr::pcg_persistent_first_pipelined() || !ikr::pcg_persistent_eligible(A, w, v)) continue;
         const double us = time_persistent(first_persistent_kind() + v, 0.0);
         if (us < best) best = us, best_kind = first_persistent_kind() + v;
       }

@@ -82,6 +82,10 @@ void launch_eas_element(const ElemArgs& a, int mode, bool fp32_tangent, const in
 void launch_eas_geometry(const ElemArgs& a, double* geo_out, cudaStream_t s);
 void launch_eas_update(const ElemArgs& a, double* alpha, const double* correction, cudaStream_t s);
 int eas_geo_stride(int eas_kind);
+// stresses of elements [e0, e0 + count) at local points (3 per element, or 3 for all): type 0 PK2, 1 Kirchhoff,
+// 2 Cauchy; 6 Voigt values per element
+void launch_stress_at(const ElemArgs& a, int e0, int count, const double* xi, bool xi_per_elem, int type, double* out,
+                      cudaStream_t s);
 // one thread per loaded element: slot_elem[s] is the element, faces face_ptr[s]..face_ptr[s+1]-1
 void launch_traction_loads(const double* X, const int32_t* conn, int n_elems, int n_slots, const int32_t* slot_elem,
                            const int32_t* face_ptr, const int32_t* face_local, const double* traction, double* trac,
@@ -162,6 +166,7 @@ void launch_fill64(double* y, double v, int64_t n, cudaStream_t s);
 // cg_persistent.cu -- the whole CG solve (after launch_pcg_init) in one cooperative launch; the result in w.x
 // and the scalars as after the two-kernel iterations
 int pcg_persistent_variants();
+int pcg_persistent_first_pipelined();  // variants from here on use the pipelined recurrences
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant);
 cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s);
 

@@ -111,6 +111,13 @@ int ikr_fe_calculate_vector(ikr_fes fes, ikr_req req, int32_t affordance, int32_
                             double* out);
 int ikr_fe_calculate_matrix(ikr_fes fes, ikr_req req, int32_t affordance, int32_t e_begin, int32_t e_end,
                             double* out);
+/* calculateAt<ResultType> (nonlinearelastic.hh:237-271, feresulttypes.hh:125-133): stress of every element in
+ * [e_begin, e_end) at a local point of the reference cube [0,1]^3 (local: 3 values per element when
+ * local_per_element != 0, else 3 for all); out: 6 Voigt values per element [11, 22, 33, 23, 13, 12] without shear
+ * factors (toVoigt(S, false)).  Displacement-based elements only (EAS sets: IKR_ERR_NOT_IMPLEMENTED). */
+enum { IKR_RESULT_PK2_STRESS = 0, IKR_RESULT_KIRCHHOFF_STRESS = 1, IKR_RESULT_CAUCHY_STRESS = 2 };
+int ikr_fe_calculate_at(ikr_fes fes, ikr_req req, int32_t result_type, int32_t e_begin, int32_t e_end,
+                        const double* local, int32_t local_per_element, double* out);
 int ikr_fe_calculate_scalar(ikr_fes fes, ikr_req req, int32_t affordance, int32_t e_begin, int32_t e_end,
                             double* out);
 /* EAS::updateStateImpl (enhancedassumedstrains.hh:225-248) on every element; correction has n dofs (a
@@ -185,7 +192,9 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
 /* CG kernels (no reference counterpart).  spmv_kind 0 = two kernels per iteration with a direct-load SpMV,
  * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..8 = the
  * whole solve in one persistent cooperative kernel (grid barriers for the two reductions of an iteration;
- * only where every warp's rows fit its registers), -1 = autotune; l2_keep_fraction in [0, 1) = share of the
+ * only where every warp's rows fit its registers), 9..10 = the same with the pipelined CG recurrences (one
+ * grid barrier per iteration; their recurrences drift, attainable relative residual about 1e-9 in FP64, so the
+ * tuner does not pick them), -1 = autotune; l2_keep_fraction in [0, 1) = share of the
  * matrix the staged kernels keep in L2 across iterations, -1 = autotune.  The choice is made at the
  * next factorize from timed CG iterations on the assembled tangent and kept for that assembler.  info
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */

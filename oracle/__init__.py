@@ -59,6 +59,7 @@ def lib():
         L.orc_reduced_size.argtypes = [vp]
         L.orc_assemble_matrix_csc.argtypes = [vp, dp, C.c_double, C.c_int, lp, ip, dp]
         L.orc_set_dirichlet_values.argtypes = [vp, dp]
+        L.orc_calculate_at.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp]
         L.orc_cg_jacobi_csc.argtypes = [C.c_int, lp, ip, dp, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
                                        C.c_double, dp, dp, ip, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
@@ -127,6 +128,15 @@ class OracleProblem:
     def set_dirichlet(self, fixed):
         f = np.ascontiguousarray(fixed, dtype=np.uint8)
         _check(lib().orc_set_dirichlet(self.h, _p(f, C.c_uint8)), "set_dirichlet")
+
+    def calculate_at(self, e, u, result_type, xi=(0.5, 0.5, 0.5)):
+        """Stress of element e at local xi: result_type 0 PK2, 1 Kirchhoff, 2 Cauchy (Voigt, 6 values)."""
+        uu = self._u(u)
+        x = np.ascontiguousarray(xi, dtype=np.float64)
+        out = np.zeros(6)
+        _check(lib().orc_calculate_at(self.h, e, _p(uu, C.c_double), result_type, _p(x, C.c_double),
+                                      _p(out, C.c_double)), "calculate_at")
+        return out
 
     def set_dirichlet_values(self, rate):
         """Inhomogeneous Dirichlet values lambda * rate on constrained dofs (None removes them)."""

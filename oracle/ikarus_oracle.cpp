@@ -964,6 +964,52 @@ int orc_element_energy(orc_problem* p, int e, const double* u, double lambda, do
   *energy = en;
   return ORC_OK;
 }
+// calculateAt<PK2Stress / kirchhoffStress / cauchyStress> of the displacement-based element at a local point
+// (nonlinearelastic.hh:237-271): H at xi, E = GL(H), S = NeoHooke PK2, tau = F S F^T, sigma = tau / det F
+// (stressconversions.hh:88-125); result in Voigt without shear factors [11, 22, 33, 23, 13, 12].
+int orc_calculate_at(orc_problem* p, int e, const double* u, int type, const double* xi, double* out6) {
+  if (!p || e < 0 || e >= p->ne || !xi || !out6 || type < 0 || type > 2) return ORC_ERR_ARG;
+  if (p->na > 0) return ORC_ERR_NOT_IMPLEMENTED;
+  double X[NN][3], ue[NN][3];
+  gather(*p, e, u, X, ue);
+  Geo g;
+  geometry(X, xi, g);
+  double H[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int v = 0; v < NN; ++v) s += ue[v][i] * g.dNdX[v][j];
+      H[i][j] = s;
+    }
+  double Ev[6];
+  gl_strain(H, Ev);
+  MatState m;
+  neohooke(p->lam, p->mu, Ev, m, false);
+  if (!m.ok) return ORC_ERR_NONPOSITIVE_DETC;
+  if (type == 0) {
+    std::copy(m.S, m.S + 6, out6);
+    return ORC_OK;
+  }
+  double S[3][3], F[3][3], FS[3][3], tau[3][3];
+  for (int v = 0; v < 6; ++v) S[VA[v]][VB[v]] = S[VB[v]][VA[v]] = m.S[v];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) F[i][j] = H[i][j] + (i == j ? 1.0 : 0.0);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += F[i][k] * S[k][j];
+      FS[i][j] = s;
+    }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += FS[i][k] * F[j][k];
+      tau[i][j] = s;
+    }
+  const double sc = type == 2 ? 1.0 / det3(F) : 1.0;
+  for (int v = 0; v < 6; ++v) out6[v] = sc * tau[VA[v]][VB[v]];
+  return ORC_OK;
+}
 int orc_update_state(orc_problem* p, const double* u, double lambda, const double* corr) {
   (void)lambda;
   if (!p || !corr) return ORC_ERR_ARG;

@@ -337,3 +337,28 @@ def test_inhomogeneous_dirichlet_values_match_oracle(ikr, eas, n):
         assert np.abs(u - ref["u"]).max() <= 1e-8 * np.abs(ref["u"]).max()
         if precision == 0:
             assert [s.iterations for s in info.solverInfos] == list(ref["iterations"])
+
+
+def test_calculate_at_stresses_match_oracle(ikr):
+    """calculateAt<PK2Stress / kirchhoffStress / cauchyStress> (nonlinearelastic.hh:237-271) at random local
+    points of every element, FP64 within 1e-12 of the oracle; zero at the undeformed state; EAS sets report
+    NotImplemented."""
+    p = problems.cantilever(4, 3, 2, L=4.0, jitter=0.15, seed=9)
+    fes, asm = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(4)
+    u = 0.01 * rng.standard_normal(p.n_dofs)
+    req = ikr.FERequirements(fes, u, 0.0)
+    local = rng.uniform(0.0, 1.0, (p.mesh.n_elems, 3))
+    for rt in ikr.ResultTypes:
+        got = ikr.calculateAt(fes, req, rt, local)
+        ref = np.array([o.calculate_at(e, u, int(rt), local[e]) for e in range(p.mesh.n_elems)])
+        assert rel_err(got, ref) <= FP64_RTOL, rt
+        centre = ikr.calculateAt(fes, req, rt, elements=(2, 5))
+        ref_c = np.array([o.calculate_at(e, u, int(rt)) for e in range(2, 5)])
+        assert rel_err(centre, ref_c) <= FP64_RTOL
+    assert np.abs(ikr.calculateAt(fes, ikr.FERequirements(fes), ikr.ResultTypes.cauchyStress)).max() == 0.0
+    pe = problems.cantilever(2, 1, 1, eas=1, n_eas=9)
+    fe_eas, _ = problems.build_gpu(pe)
+    with pytest.raises(ikr.IkarusError, match="NOT_IMPLEMENTED"):
+        ikr.calculateAt(fe_eas, ikr.FERequirements(fe_eas), ikr.ResultTypes.PK2Stress)
