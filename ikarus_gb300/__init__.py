@@ -138,6 +138,7 @@ SIGNATURES = {
     "ikr_newton_instance_info": ([_vp, _ip, _dp, _ip], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
+    "ikr_fes_set_material": ([_vp, _I], C.c_int),
     "ikr_assembler_set_dirichlet_values": ([_vp, _dp], C.c_int),
     "ikr_fes_get_alpha": ([_vp, _dp], C.c_int),
     "ikr_fes_set_alpha": ([_vp, _dp], C.c_int),
@@ -252,6 +253,19 @@ class NeoHooke:
     """Compressible Neo-Hooke law on C (materials/hyperelastic/neohooke.hh:37-208)."""
     lambda_: float
     mu: float
+    kind = 0
+
+    @classmethod
+    def from_E_nu(cls, E, nu):
+        return cls(*toLamesFirstParameterAndShearModulus(E, nu))
+
+
+@dataclass
+class StVenantKirchhoff:
+    """Saint Venant-Kirchhoff law S = lambda tr(E) I + 2 mu E (materials/svk.hh:63-163)."""
+    lambda_: float
+    mu: float
+    kind = 1
 
     @classmethod
     def from_E_nu(cls, E, nu):
@@ -263,7 +277,7 @@ class FiniteElements:
     """All elements of one Q1 hexahedral mesh with skills nonLinearElastic(NeoHooke) [+ eas<ES>(n)]
     [+ neumannBoundaryLoad], bound to their grid elements (the reference's ``std::vector<FE>``)."""
 
-    def __init__(self, coords, conn, material: NeoHooke, eas: EAS = EAS.none, n_eas: int = 0):
+    def __init__(self, coords, conn, material, eas: EAS = EAS.none, n_eas: int = 0):
         self.coords = np.ascontiguousarray(coords, dtype=np.float64)
         self.conn = np.ascontiguousarray(conn, dtype=np.int32)
         self.n_nodes, self.n_elems = self.coords.shape[0], self.conn.shape[0]
@@ -275,6 +289,8 @@ class FiniteElements:
                                   _ptr(self.conn, C.c_int32), material.lambda_, material.mu, int(eas), self.n_eas),
              "fes_create")
         self.h = h
+        if getattr(material, "kind", 0):
+            _err(lib().ikr_fes_set_material(self.h, int(material.kind)), "set_material")
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:

@@ -27,7 +27,8 @@ namespace ikr {
 namespace {
 
 // EPB elements per block (8 lanes each): 16, 32 or 64, chosen per element set by timing (host.cpp)
-template <typename KT, int MODE, int EPB>
+// MAT 0: NeoHooke (neohooke.hh:78-142); MAT 1: StVenantKirchhoff (svk.hh:63-163)
+template <typename KT, int MODE, int EPB, int MAT = 0>
 __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const int32_t* __restrict__ list, int n_list,
                                                                int e_base) {
   constexpr bool WANT_R = MODE & kWantR;
@@ -97,6 +98,75 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) F[i][j] = sum8(dU[i] * dN[j]) + (i == j ? KT(1) : KT(0));
+    if constexpr (MAT == 1) {
+      // StVenantKirchhoff: E = (F^T F - I) / 2, S = lambda tr(E) I + 2 mu E, P = F S; first elasticity tensor
+      // contracted with two gradients, g = F grad N:
+      // K_IJ = w [lambda g_I (x) g_J + mu (dN_I . dN_J) F F^T + mu g_J (x) g_I + (dN_I . S dN_J) I]
+      KT E[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          E[i][j] = KT(0.5) * (F[0][i] * F[0][j] + F[1][i] * F[1][j] + F[2][i] * F[2][j] - (i == j ? KT(1) : KT(0)));
+      const KT trE = E[0][0] + E[1][1] + E[2][2];
+      KT S[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) S[i][j] = KT(2) * mu * E[i][j] + (i == j ? lam * trE : KT(0));
+      const KT w = KT(kGaussW) * detJ;
+      KT SdN[3], g[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        SdN[k] = S[k][0] * dN[0] + S[k][1] * dN[1] + S[k][2] * dN[2];
+        g[k] = F[k][0] * dN[0] + F[k][1] * dN[1] + F[k][2] * dN[2];
+      }
+      if (WANT_R) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) f[i] += double(w * (F[i][0] * SdN[0] + F[i][1] * SdN[1] + F[i][2] * SdN[2]));
+      }
+      if (WANT_E && sub == 0) {
+        KT EE = 0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) EE += E[i][j] * E[i][j];
+        psi += double(w * (lam / KT(2) * trE * trE + mu * EE));
+      }
+      if (WANT_K) {
+        KT FFt[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) FFt[i][j] = F[i][0] * F[j][0] + F[i][1] * F[j][1] + F[i][2] * F[j][2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          sh[es][sub][k] = dN[k];
+          sh[es][sub][3 + k] = g[k];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int d = 0; d < 5; ++d) {
+          const int Jn = (sub + d) & 7;
+          KT dNJ[3], gJ[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            dNJ[k] = sh[es][Jn][k];
+            gJ[k] = sh[es][Jn][3 + k];
+          }
+          const KT wm = w * mu * (dN[0] * dNJ[0] + dN[1] * dNJ[1] + dN[2] * dNJ[2]);
+          const KT ws = w * (SdN[0] * dNJ[0] + SdN[1] * dNJ[1] + SdN[2] * dNJ[2]);
+          const KT wl = w * lam, wu = w * mu;
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              Kacc[d][i][j] += wl * g[i] * gJ[j] + wm * FFt[i][j] + wu * gJ[i] * g[j] + (i == j ? ws : KT(0));
+        }
+        __syncwarp();
+      }
+      continue;
+    }
     KT Fi[3][3];
     const KT detF = inv3(F, Fi);
     // det C = det(F)^2 must exceed 1e-10 (checkPositiveOrAbort); NaN fails the test as well
@@ -335,19 +405,38 @@ __global__ void __launch_bounds__(EPB * 8) disp_residual_gp_kernel(ElemArgs a, c
 #pragma unroll
       for (int j = 0; j < 3; ++j) F[i][j] += uv[i] * dN[j];
   }
-  double Fi[3][3];
-  const double detF = inv3(F, Fi);
   int bad = 0;
-  // det C = det(F)^2 must exceed 1e-10 (checkPositiveOrAbort); NaN fails the test as well
-  if (!(detF * detF > 1e-10) || !(detF > 0.0)) bad |= kStatusNonPositiveDetC;
-  const double lnJ = log(detF);
   const double w = kGaussW * detJ;
-  // P = mu (F - F^-T) + lambda ln J F^-T (F - F^-T keeps the undeformed internal force exactly zero)
   double P[3][3];
+  if (a.material == 1) {
+    // StVenantKirchhoff: P = F S, S = lambda tr(E) I + 2 mu E, E = (F^T F - I) / 2
+    double E[3][3], S[3][3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) P[i][j] = w * (mu * (F[i][j] - Fi[j][i]) + lam * lnJ * Fi[j][i]);
+      for (int j = 0; j < 3; ++j)
+        E[i][j] = 0.5 * (F[0][i] * F[0][j] + F[1][i] * F[1][j] + F[2][i] * F[2][j] - (i == j ? 1.0 : 0.0));
+    const double trE = E[0][0] + E[1][1] + E[2][2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[i][j] = 2.0 * mu * E[i][j] + (i == j ? lam * trE : 0.0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) P[i][j] = w * (F[i][0] * S[0][j] + F[i][1] * S[1][j] + F[i][2] * S[2][j]);
+  } else {
+    double Fi[3][3];
+    const double detF = inv3(F, Fi);
+    // det C = det(F)^2 must exceed 1e-10 (checkPositiveOrAbort); NaN fails the test as well
+    if (!(detF * detF > 1e-10) || !(detF > 0.0)) bad |= kStatusNonPositiveDetC;
+    const double lnJ = log(detF);
+    // P = mu (F - F^-T) + lambda ln J F^-T (F - F^-T keeps the undeformed internal force exactly zero)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) P[i][j] = w * (mu * (F[i][j] - Fi[j][i]) + lam * lnJ * Fi[j][i]);
+  }
 #pragma unroll
   for (int v = 0; v < 8; ++v) {
     double dxi[3], dN[3];
@@ -441,16 +530,24 @@ __global__ void stress_at_kernel(ElemArgs a, int e0, int count, const double* __
       double hh = H[0][i] * H[0][j] + H[1][i] * H[1][j] + H[2][i] * H[2][j];
       C[i][j] = H[i][j] + H[j][i] + hh + (i == j ? 1.0 : 0.0);
     }
-  double Ci[3][3];
-  const double detC = inv3(C, Ci);
-  if (!(detC > 1e-10) && a.status) atomicOr(a.status, kStatusNonPositiveDetC);
   const double lam = a.lam_e ? a.lam_e[e] : a.lam, mu = a.mu_e ? a.mu_e[e] : a.mu;
-  const double lnJ = log(sqrt(detC));
   double S[3][3];
+  if (a.material == 1) {  // StVenantKirchhoff: S = lambda tr(E) I + 2 mu E with E = (C - I) / 2
+    const double trE = 0.5 * (C[0][0] + C[1][1] + C[2][2] - 3.0);
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+      for (int j = 0; j < 3; ++j) S[i][j] = mu * (C[i][j] - (i == j ? 1.0 : 0.0)) + (i == j ? lam * trE : 0.0);
+  } else {
+    double Ci[3][3];
+    const double detC = inv3(C, Ci);
+    if (!(detC > 1e-10) && a.status) atomicOr(a.status, kStatusNonPositiveDetC);
+    const double lnJ = log(sqrt(detC));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+  }
   double R[3][3];
   if (type == 0) {
 #pragma unroll
@@ -477,14 +574,15 @@ __global__ void stress_at_kernel(ElemArgs a, int e0, int count, const double* __
   o[0] = R[0][0], o[1] = R[1][1], o[2] = R[2][2], o[3] = R[1][2], o[4] = R[0][2], o[5] = R[0][1];
 }
 
-template <typename KT, int MODE, int EPB>
+template <typename KT, int MODE, int EPB, int MAT = 0>
 void launch_disp_epb(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
   const int blocks = (n_list + EPB - 1) / EPB;
-  disp_element_kernel<KT, MODE, EPB><<<blocks, EPB * 8, 0, s>>>(a, list, n_list, e_base);
+  disp_element_kernel<KT, MODE, EPB, MAT><<<blocks, EPB * 8, 0, s>>>(a, list, n_list, e_base);
 }
 // assembling modes honour a.epb; element-level outputs (tests, single elements) use 32
 template <typename KT, int MODE>
 void launch_disp_t(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
+  if (a.material == 1) return launch_disp_epb<KT, MODE, 32, 1>(a, list, n_list, e_base, s);  // SVK: one shape
   if constexpr ((MODE & kElemOut) == 0) {
     if (a.epb == 16) return launch_disp_epb<KT, MODE, 16>(a, list, n_list, e_base, s);
     if (a.epb == 64) return launch_disp_epb<KT, MODE, 64>(a, list, n_list, e_base, s);

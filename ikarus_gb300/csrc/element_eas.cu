@@ -251,27 +251,42 @@ __global__ void __launch_bounds__(EasCfg<NA>::EPB * 8) eas_element_kernel(ElemAr
         for (int r = 0; r < 6; ++r) Ev[r] += w * sm[Cfg::O_GEO + 6 * r + rr];
       }
     }
-    // NeoHooke on C = 2E + I (neohooke.hh:100-142)
-    double C[3][3], Ci[3][3];
-    C[0][0] = 2.0 * Ev[0] + 1.0, C[1][1] = 2.0 * Ev[1] + 1.0, C[2][2] = 2.0 * Ev[2] + 1.0;
-    C[1][2] = C[2][1] = Ev[3];
-    C[0][2] = C[2][0] = Ev[4];
-    C[0][1] = C[1][0] = Ev[5];
-    const double detC = inv3(C, Ci);
-    if (!(detC > 1e-10)) bad |= kStatusNonPositiveDetC;
-    const double lnJ = log(sqrt(detC));
     double S[6], Sm[3][3];
+    if (a.material == 1) {
+      // StVenantKirchhoff (svk.hh:96-163): S = lambda tr(E) + 2 mu E (Voigt shears mu * 2E_ij), constant moduli
+      const double trE = Ev[0] + Ev[1] + Ev[2];
 #pragma unroll
-    for (int v = 0; v < 6; ++v) {
-      const int i = voigt_a(v), j = voigt_b(v);
-      S[v] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
-      Sm[i][j] = Sm[j][i] = S[v];
-    }
-    const double cc = mu - lam * lnJ;
-    for (int t = sub; t < 36; t += 8) {
-      const int r = t / 6, c = t % 6;
-      const int i = voigt_a(r), j = voigt_b(r), k = voigt_a(c), l = voigt_b(c);
-      sm[Cfg::O_C6 + t] = lam * Ci[i][j] * Ci[k][l] + cc * (Ci[i][k] * Ci[j][l] + Ci[i][l] * Ci[j][k]);
+      for (int v = 0; v < 6; ++v) {
+        const int i = voigt_a(v), j = voigt_b(v);
+        S[v] = v < 3 ? lam * trE + 2.0 * mu * Ev[v] : mu * Ev[v];
+        Sm[i][j] = Sm[j][i] = S[v];
+      }
+      for (int t = sub; t < 36; t += 8) {
+        const int r = t / 6, c = t % 6;
+        sm[Cfg::O_C6 + t] = (r < 3 && c < 3 ? lam : 0.0) + (r == c ? (r < 3 ? 2.0 * mu : mu) : 0.0);
+      }
+    } else {
+      // NeoHooke on C = 2E + I (neohooke.hh:100-142)
+      double C[3][3], Ci[3][3];
+      C[0][0] = 2.0 * Ev[0] + 1.0, C[1][1] = 2.0 * Ev[1] + 1.0, C[2][2] = 2.0 * Ev[2] + 1.0;
+      C[1][2] = C[2][1] = Ev[3];
+      C[0][2] = C[2][0] = Ev[4];
+      C[0][1] = C[1][0] = Ev[5];
+      const double detC = inv3(C, Ci);
+      if (!(detC > 1e-10)) bad |= kStatusNonPositiveDetC;
+      const double lnJ = log(sqrt(detC));
+#pragma unroll
+      for (int v = 0; v < 6; ++v) {
+        const int i = voigt_a(v), j = voigt_b(v);
+        S[v] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+        Sm[i][j] = Sm[j][i] = S[v];
+      }
+      const double cc = mu - lam * lnJ;
+      for (int t = sub; t < 36; t += 8) {
+        const int r = t / 6, c = t % 6;
+        const int i = voigt_a(r), j = voigt_b(r), k = voigt_a(c), l = voigt_b(c);
+        sm[Cfg::O_C6 + t] = lam * Ci[i][j] * Ci[k][l] + cc * (Ci[i][k] * Ci[j][l] + Ci[i][l] * Ci[j][k]);
+      }
     }
     // nodal gradients entering B and kg (HT adds Ht dN0, displacementgradienttransposed.hh:126-140)
     double dNm[3];

@@ -110,6 +110,7 @@ using namespace ikr_host;
 // ------------------------------------------------------------------------------------------------------------
 struct ikr_fes_s {
   int nn = 0, ne = 0, na = 0, eas = 0;
+  int material = IKR_MATERIAL_NEOHOOKE;
   // elements per block of the displacement element kernel, chosen by timing at the first assembly of each kind
   // (0 = not chosen yet): residual, FP64 tangent, FP32 tangent
   int epb_r = 0, epb_k64 = 0, epb_k32 = 0;
@@ -156,6 +157,7 @@ struct ikr_fes_s {
     a.conn = conn.p;
     a.lam = lam;
     a.mu = mu;
+    a.material = material;
     a.eas_kind = na > 0 ? eas : 0;
     a.n_alpha = na;
     a.alpha = alpha.p;

@@ -24,7 +24,8 @@ struct ElemArgs {
   int n_nodes = 0, n_elems = 0;
   const double* X = nullptr;     // coordinates, n_nodes x 3
   const int32_t* conn = nullptr; // corner-major: conn[v * n_elems + e]
-  double lam = 0, mu = 0;        // Lame parameters of NeoHooke
+  double lam = 0, mu = 0;        // Lame parameters
+  int material = 0;              // 0 NeoHooke, 1 StVenantKirchhoff
   const double* lam_e = nullptr;  // per-element Lame parameters (nullptr: lam / mu for every element)
   const double* mu_e = nullptr;
   const double* u = nullptr;     // displacement, 3 * n_nodes (FP64)

@@ -36,13 +36,14 @@ class Problem:
     t_end: float = 1.0
     tol: float = 1e-10
     relative: bool = False
+    material: int = 0  # 0 NeoHooke, 1 StVenantKirchhoff
 
     @property
     def n_dofs(self):
         return self.mesh.n_dofs
 
 
-def cantilever_golden(eas: int, n_eas: int, nx=10, ny=1, nz=1) -> Problem:
+def cantilever_golden(eas: int, n_eas: int, nx=10, ny=1, nz=1, material=0) -> Problem:
     """tests/src/testcantileverbeam.hh:42-198 in 3D: YaspGrid 10x1x1 on (10, 2, 2), E = 100, nu = 0.3, clamped at
     x = 0, manipulator point loads R[y-dof] += lambda at the vertices (10,2,2) and (10,2,0), 20 load steps,
     ||R|| < 1e-10 (testcantileverbeamEAS.cpp:60-124)."""
@@ -52,7 +53,7 @@ def cantilever_golden(eas: int, n_eas: int, nx=10, ny=1, nz=1) -> Problem:
     fixed = fixed_dofs_where(m, lambda X: np.abs(X[:, 0]) < 1e-8)
     dofs = np.array([3 * vertex_at(m, (L, h, h)) + 1, 3 * vertex_at(m, (L, h, 0.0)) + 1], dtype=np.int32)
     return Problem(f"cantilever_golden_eas{eas}_{n_eas}", m, lam, mu, eas, n_eas, fixed, pl_dofs=dofs,
-                   pl_values=np.ones(2), load_steps=20, tol=1e-10)
+                   pl_values=np.ones(2), load_steps=20, tol=1e-10, material=material)
 
 
 def cantilever(nx, ny, nz, L=10.0, E=1000.0, nu=0.3, jitter=0.0, seed=0, load_steps=10, traction=(0.0, 0.0, -1.0),
@@ -207,8 +208,9 @@ def single_element(offsets=None, E=1000.0, nu=0.3, eas=0, n_eas=0) -> Problem:
 
 def build_gpu(p: Problem, precision=0):
     """GPU objects for a problem: (FiniteElements, SparseFlatAssembler)."""
-    from . import FiniteElements, NeoHooke, Precision, SparseFlatAssembler
-    fes = FiniteElements(p.mesh.coords, p.mesh.conn, NeoHooke(p.lam, p.mu), p.eas, p.n_eas)
+    from . import FiniteElements, NeoHooke, Precision, SparseFlatAssembler, StVenantKirchhoff
+    law = StVenantKirchhoff if getattr(p, "material", 0) == 1 else NeoHooke
+    fes = FiniteElements(p.mesh.coords, p.mesh.conn, law(p.lam, p.mu), p.eas, p.n_eas)
     if p.face_elem is not None and len(p.face_elem):
         fes.add_neumann(p.face_elem, p.face_local, p.face_traction)
     asm = SparseFlatAssembler(fes, p.fixed, Precision(precision))

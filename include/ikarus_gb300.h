@@ -200,6 +200,10 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fraction);
 int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* spmv_kind, double* l2_keep_fraction, double* spmv_us);
+/* material law of all elements (the reference's Material template argument of makeFE): NeoHooke (default,
+ * neohooke.hh) or StVenantKirchhoff (svk.hh); both with the Lame parameters given at creation */
+enum { IKR_MATERIAL_NEOHOOKE = 0, IKR_MATERIAL_SVK = 1 };
+int ikr_fes_set_material(ikr_fes fes, int32_t material);
 /* elements per block the displacement element kernel uses for residual / FP64 tangent / FP32 tangent
  * assembly (16, 32 or 64, chosen by timing at the first assembly of each kind; 0 = not assembled yet; no
  * reference counterpart) */

@@ -19,6 +19,7 @@ _lib = None
 EAS_NONE, EAS_GL, EAS_H, EAS_HT = 0, 1, 2, 3
 DBC_RAW, DBC_REDUCED, DBC_FULL = 0, 1, 2
 SOLVER_BANDED_LDLT, SOLVER_CG_JACOBI = 0, 1
+MATERIAL_NEOHOOKE, MATERIAL_SVK = 0, 1
 ERRORS = {-1: "ARG", -2: "NOT_IMPLEMENTED", -3: "NONPOSITIVE_DETC", -4: "SINGULAR", -5: "NOT_CONVERGED"}
 
 
@@ -59,6 +60,7 @@ def lib():
         L.orc_reduced_size.argtypes = [vp]
         L.orc_assemble_matrix_csc.argtypes = [vp, dp, C.c_double, C.c_int, lp, ip, dp]
         L.orc_set_dirichlet_values.argtypes = [vp, dp]
+        L.orc_set_material.argtypes = [vp, C.c_int]
         L.orc_calculate_at.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp]
         L.orc_cg_jacobi_csc.argtypes = [C.c_int, lp, ip, dp, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
@@ -96,6 +98,8 @@ def from_problem(p, faithful=False):
     """Oracle twin of an ``ikarus_gb300.problems.Problem`` definition (plain data, no GPU objects)."""
     o = OracleProblem(p.mesh.coords, p.mesh.conn, p.lam, p.mu, p.eas if p.n_eas else EAS_NONE, p.n_eas)
     o.set_dirichlet(p.fixed)
+    if getattr(p, "material", 0):
+        o.set_material(p.material)
     if p.face_elem is not None and len(p.face_elem):
         o.add_neumann(p.face_elem, p.face_local, p.face_traction)
     if p.pl_dofs is not None:
@@ -137,6 +141,10 @@ class OracleProblem:
         _check(lib().orc_calculate_at(self.h, e, _p(uu, C.c_double), result_type, _p(x, C.c_double),
                                       _p(out, C.c_double)), "calculate_at")
         return out
+
+    def set_material(self, material):
+        """MATERIAL_NEOHOOKE (default) or MATERIAL_SVK for all elements."""
+        _check(lib().orc_set_material(self.h, int(material)), "set_material")
 
     def set_dirichlet_values(self, rate):
         """Inhomogeneous Dirichlet values lambda * rate on constrained dofs (None removes them)."""

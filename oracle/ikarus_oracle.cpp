@@ -185,6 +185,24 @@ void neohooke(double lam, double mu, const double Ev[6], MatState& m, bool wantT
     }
 }
 
+// StVenantKirchhoff (svk.hh:63-163): psi = lambda/2 tr(E)^2 + mu E:E, S = lambda tr(E) I + 2 mu E (Voigt shear
+// entries mu * 2E_ij, the strain's doubled shears), constant moduli; no determinant check in the reference.
+void svk(double lam, double mu, const double Ev[6], MatState& m, bool wantTangent = true) {
+  const double trE = Ev[0] + Ev[1] + Ev[2];
+  m.ok = true;
+  m.psi = lam / 2.0 * trE * trE + mu * (Ev[0] * Ev[0] + Ev[1] * Ev[1] + Ev[2] * Ev[2] +
+                                        (Ev[3] * Ev[3] + Ev[4] * Ev[4] + Ev[5] * Ev[5]) / 2.0);
+  for (int v = 0; v < 3; ++v) m.S[v] = lam * trE + 2.0 * mu * Ev[v];
+  for (int v = 3; v < 6; ++v) m.S[v] = mu * Ev[v];
+  if (!wantTangent) return;
+  for (int r = 0; r < 6; ++r)
+    for (int c = 0; c < 6; ++c) m.C6[r][c] = (r < 3 && c < 3 ? lam : 0.0) + (r == c ? (r < 3 ? 2.0 * mu : mu) : 0.0);
+}
+void material_law(int material, double lam, double mu, const double Ev[6], MatState& m, bool wantTangent = true) {
+  if (material == ORC_MATERIAL_SVK) svk(lam, mu, Ev, m, wantTangent);
+  else neohooke(lam, mu, Ev, m, wantTangent);
+}
+
 // Green-Lagrange strain of a displacement gradient, Voigt with doubled shears
 // (dune-localfefunctions greenLagrangeStrains; easfunctions/displacementgradient.hh:86-87).
 void gl_strain(const double H[3][3], double Ev[6]) {
@@ -241,6 +259,7 @@ struct orc_problem {
   std::vector<double> X;      // nn*3
   std::vector<int32_t> conn;  // ne*8
   double lam = 0, mu = 0;
+  int material = 0;  // ORC_MATERIAL_NEOHOOKE / ORC_MATERIAL_SVK
   int eas = 0, na = 0;
   bool faithful = false;
   std::vector<uint8_t> fixed;   // n dofs
@@ -390,7 +409,7 @@ void element_internal(const orc_problem& p, int e, const double* u, bool wantK, 
         for (int k = 0; k < na; ++k) Ev[r] += M[r][k] * al[k];
 
     MatState m;
-    neohooke(p.lam, p.mu, Ev, m, true);
+    material_law(p.material, p.lam, p.mu, Ev, m, true);
     if (!m.ok) out.ok = false;
     out.energy += m.psi * wdJ;
     double Smat[3][3];
@@ -422,7 +441,7 @@ void element_internal(const orc_problem& p, int e, const double* u, bool wantK, 
           MatState mm;
           const MatState* mp = &m;
           if (p.faithful) {  // the reference evaluates the moduli inside the (i,j) loop
-            neohooke(p.lam, p.mu, Ev, mm, true);
+            material_law(p.material, p.lam, p.mu, Ev, mm, true);
             mp = &mm;
           }
           double CB[6][3];
@@ -888,6 +907,11 @@ orc_problem* orc_problem_create(int n_nodes, const double* coords, int n_elems, 
   return p;
 }
 void orc_problem_destroy(orc_problem* p) { delete p; }
+int orc_set_material(orc_problem* p, int material) {
+  if (!p || (material != ORC_MATERIAL_NEOHOOKE && material != ORC_MATERIAL_SVK)) return ORC_ERR_ARG;
+  p->material = material;
+  return ORC_OK;
+}
 int orc_set_dirichlet(orc_problem* p, const uint8_t* f) {
   if (!p || !f) return ORC_ERR_ARG;
   for (int i = 0; i < p->ndof(); ++i) p->fixed[i] = f[i] ? 1 : 0;
@@ -984,7 +1008,7 @@ int orc_calculate_at(orc_problem* p, int e, const double* u, int type, const dou
   double Ev[6];
   gl_strain(H, Ev);
   MatState m;
-  neohooke(p->lam, p->mu, Ev, m, false);
+  material_law(p->material, p->lam, p->mu, Ev, m, false);
   if (!m.ok) return ORC_ERR_NONPOSITIVE_DETC;
   if (type == 0) {
     std::copy(m.S, m.S + 6, out6);

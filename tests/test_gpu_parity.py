@@ -206,13 +206,15 @@ def test_linear_solver(ikr):
     assert 0 < it and rel <= 1e-12
 
 
+@pytest.mark.parametrize("material", ["NeoHooke", "StVenantKirchhoff"])
 @pytest.mark.parametrize("es", ["GreenLagrangeStrain", "DisplacementGradient", "DisplacementGradientTransposed"])
-def test_cantilever_goldens_on_gpu(ikr, es):
-    """tests/src/testcantileverbeamEAS.cpp:60-124 through the device path: 80 Newton iterations, max |d|."""
+def test_cantilever_goldens_on_gpu(ikr, es, material):
+    """tests/src/testcantileverbeamEAS.cpp:60-124 through the device path: 80 Newton iterations, max |d|, for
+    the NeoHooke and StVenantKirchhoff materials of the reference test."""
     g = GOLD["cantilever_3d"]
-    want = g["results"][es]["NeoHooke"]
+    want = g["results"][es][material]
     kind = {"GreenLagrangeStrain": 1, "DisplacementGradient": 2, "DisplacementGradientTransposed": 3}[es]
-    p = problems.cantilever_golden(kind, g["eas_parameters"][es])
+    p = problems.cantilever_golden(kind, g["eas_parameters"][es], material=1 if material == "StVenantKirchhoff" else 0)
     fes, asm = problems.build_gpu(p)
     req = ikr.FERequirements(fes)
     asm.bind(req, ikr.DBCOption.Full)
@@ -362,3 +364,34 @@ def test_calculate_at_stresses_match_oracle(ikr):
     fe_eas, _ = problems.build_gpu(pe)
     with pytest.raises(ikr.IkarusError, match="NOT_IMPLEMENTED"):
         ikr.calculateAt(fe_eas, ikr.FERequirements(fe_eas), ikr.ResultTypes.PK2Stress)
+
+
+@pytest.mark.parametrize("eas,n", [(0, 0), (1, 9), (2, 9)])
+def test_svk_element_and_assembly_match_oracle(ikr, eas, n):
+    """StVenantKirchhoff (svk.hh:63-163) in the element kernels: element vectors and matrices, the assembled
+    residual and tangent (FP64) within 1e-12 of the oracle, the FP32 tangent within 2e-6, energy for the
+    displacement-based element."""
+    p = problems.cantilever(4, 2, 2, L=4.0, jitter=0.15, seed=11, eas=eas, n_eas=n)
+    p.material = 1
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(5)
+    u = 0.02 * rng.standard_normal(p.n_dofs)
+    for precision in (0, 1):
+        fes, asm = problems.build_gpu(p, precision=precision)
+        req = ikr.FERequirements(fes, u, 0.4)
+        if precision == 0:
+            ev = ikr.calculateVector(fes, req)
+            ref_v = np.array([o.element_vector(e, u, 0.4) for e in range(p.mesh.n_elems)])
+            assert rel_err(ev, ref_v) <= FP64_RTOL
+            em = ikr.calculateMatrix(fes, req)
+            for e in range(p.mesh.n_elems):
+                assert rel_err(em[e], o.element_matrix(e, u, 0.4)) <= FP64_RTOL
+            if eas == 0:
+                en = ikr.calculateScalar(fes, req)
+                ref_e = np.array([o.element_energy(e, u, 0.4) for e in range(p.mesh.n_elems)])
+                assert rel_err(en, ref_e) <= FP64_RTOL
+            R = asm.vector(req, dbc=ikr.DBCOption.Full)
+            assert rel_err(R, o.assemble_vector(u, 0.4)) <= FP64_RTOL
+        K = asm.matrix(req, dbc=ikr.DBCOption.Full).toarray()
+        Kref = o.assemble_matrix_dense(u, 0.4)
+        assert rel_err(K, Kref) <= (2e-6 if precision else FP64_RTOL)

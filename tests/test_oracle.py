@@ -19,11 +19,13 @@ EAS_KINDS = {"GreenLagrangeStrain": oracle.EAS_GL, "DisplacementGradient": oracl
              "DisplacementGradientTransposed": oracle.EAS_HT}
 
 
+@pytest.mark.parametrize("material", ["NeoHooke", "StVenantKirchhoff"])
 @pytest.mark.parametrize("es", sorted(EAS_KINDS))
-def test_cantilever_goldens(es):
+def test_cantilever_goldens(es, material):
     g = GOLD["cantilever_3d"]
-    want = g["results"][es]["NeoHooke"]
-    p = problems.cantilever_golden(EAS_KINDS[es], g["eas_parameters"][es])
+    want = g["results"][es][material]
+    p = problems.cantilever_golden(EAS_KINDS[es], g["eas_parameters"][es],
+                                   material=oracle.MATERIAL_SVK if material == "StVenantKirchhoff" else 0)
     o = oracle.from_problem(p)
     r = o.load_control(g["load_steps"], 0.0, 1.0, tol=g["tol"])
     assert r["success"]
@@ -185,3 +187,29 @@ def test_oracle_inhomogeneous_dirichlet_values():
         assert np.abs(R[p.fixed == 0]).max() <= 1e-9
         res.append(u)
     assert np.abs(res[0] - res[1]).max() <= 1e-8 * np.abs(res[1]).max()
+
+
+@pytest.mark.parametrize("eas,n", [(0, 0), (oracle.EAS_GL, 9), (oracle.EAS_H, 9)])
+def test_svk_tangent_and_residual_are_consistent(eas, n):
+    """StVenantKirchhoff (svk.hh:63-163) in the oracle: K = dR/dd and (displacement-based) R = dPsi/dd by
+    central differences, as checkfebyautodiff.hh does for the reference's elements."""
+    p = _distorted(eas, n)
+    p.material = oracle.MATERIAL_SVK
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(8)
+    u = 0.05 * rng.standard_normal(24)
+    if n:
+        _relax_alpha(o, u)
+    K = o.element_matrix(0, u)
+    h = 1e-6
+    Kfd = np.zeros((24, 24))
+    for j in range(24):
+        e = np.zeros(24)
+        e[j] = h
+        Kfd[:, j] = (o.element_vector(0, u + e) - o.element_vector(0, u - e)) / (2 * h)
+    assert np.abs(K.reshape(24, 24, order="F") - Kfd).max() <= 1e-6 * np.abs(K).max()
+    if n == 0:
+        R = o.element_vector(0, u)
+        Rfd = np.array([(o.element_energy(0, u + h * np.eye(24)[j]) - o.element_energy(0, u - h * np.eye(24)[j]))
+                        / (2 * h) for j in range(24)])
+        assert np.abs(R - Rfd).max() <= 1e-6 * np.abs(R).max()
