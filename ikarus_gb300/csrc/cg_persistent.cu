@@ -339,252 +339,10 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   if (failed && threadIdx.x == 0) scal[kDone] = kDoneDeviceTimeout;
 }
 
-// Pipelined variant (Ghysels & Vanroose's preconditioned pipelined CG): one grid barrier per iteration.  The
-// recurrences keep u = M^-1 r, w = A u, s = A p, q = M^-1 s and z = A q, so the three dot products an iteration
-// needs, (r,u), (w,u) and (r,r), are all formed from values known before its matrix product, and one barrier
-// both sums them and publishes m = M^-1 w, the only vector the product n = A m gathers:
-//   gamma = (r,u), delta = (w,u), m = M^-1 w        [barrier: sums, m visible]
-//   n = A m;  beta = gamma / gamma_old, alpha = gamma / (delta - beta gamma / alpha_old)  (first: beta 0, alpha gamma/delta)
-//   z = n + beta z, q = m + beta q, s = w + beta s, p = u + beta p,
-//   x += alpha p, r -= alpha s, u -= alpha q, w -= alpha z.
-// The first w = A u0 is one product before the loop.  m is double-buffered by iteration parity (p0 / p1).
 template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB>
-__global__ void __launch_bounds__(WARPS * 32, MINB)
-    pcg_pipelined_kernel(Bsr A, const T* __restrict__ val, const T* __restrict__ minv, T* __restrict__ xg,
-                         const T* __restrict__ rg, T* __restrict__ zg, T* __restrict__ p0, T* __restrict__ p1,
-                         double* part_a, double* part_b, double* scal, int64_t keep_g) {
-  using C = PersistentCfg<T, CB, NST, WARPS>;
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) uint64_t bars[WARPS][NST];
-  __shared__ double sw[WARPS * 3];
-  __shared__ double sv[3];
-  __shared__ bool ok_sh;
-  (void)part_a;  // the three partials per CTA, double-buffered, use part_b (4 per CTA and parity available)
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int G = gridDim.x;
-  const int nw = G * WARPS;
-  const int gw = blockIdx.x * WARPS + warp;
-  const int n_slices = A.n_slices;
-  unsigned int* bar_count = &tickets(scal)[3];
-  unsigned char* wbase = smem + (size_t)warp * NST * C::kStageBytes;
-
-  int ns = 0;
-  int s_first[MAXS], s_end[MAXS];
-#pragma unroll
-  for (int j = 0; j < MAXS; ++j) {
-    const int sj = gw + j * nw;
-    s_first[j] = 0, s_end[j] = 0;
-    if (sj < n_slices) {
-      s_first[j] = A.slice_off[sj];
-      s_end[j] = A.slice_off[sj + 1];
-      ns = j + 1;
-    }
-  }
-  // recurrence vectors of the owned rows
-  T xv[MAXS][3], rv[MAXS][3], uv[MAXS][3], wv[MAXS][3], zv[MAXS][3], qv[MAXS][3], sv3[MAXS][3], pv[MAXS][3];
-#pragma unroll
-  for (int j = 0; j < MAXS; ++j) {
-    const int row = 32 * (gw + j * nw) + lane;
-    const bool own = j < ns && row < A.n_rows;
-    V3<T> r0 = {T(0), T(0), T(0)}, u0 = {T(0), T(0), T(0)};
-    if (own) r0 = load3rw(rg, row), u0 = load3rw(zg, row);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) xv[j][c] = wv[j][c] = zv[j][c] = qv[j][c] = sv3[j][c] = pv[j][c] = T(0);
-    rv[j][0] = r0.x, rv[j][1] = r0.y, rv[j][2] = r0.z;
-    uv[j][0] = u0.x, uv[j][1] = u0.y, uv[j][2] = u0.z;
-  }
-  const double tol2 = scal[kTol2];
-  const int maxit = (int)scal[kMaxIt];
-  double rrs = scal[kRR];
-  double done = scal[kDone];
-  double gamma_old = 1.0, alpha_old = 1.0;
-
-  if (lane == 0) {
-    for (int st = 0; st < NST; ++st) mbar_init(smem_addr(&bars[warp][st]), 1);
-    mbar_init_fence();
-  }
-  __syncwarp();
-  auto issue = [&](int st, const CyclicPos& P) {
-    if (lane == 0) {
-      const int nb = min(CB, P.gend - P.g);
-      const uint32_t vb = nb * 288 * (uint32_t)sizeof(T), cb = nb * 128;
-      const uint32_t b = smem_addr(&bars[warp][st]);
-      unsigned char* stage = wbase + (size_t)st * C::kStageBytes;
-      const uint64_t pol = l2_policy(P.g < keep_g);
-      mbar_expect_tx(b, vb + cb);
-      bulk_g2s(smem_addr(stage), val + (int64_t)P.g * 288, vb, b, pol);
-      bulk_g2s(smem_addr(stage + C::kValBytes), A.col_sell + (int64_t)P.g * 32, cb, b, pol);
-    }
-  };
-  auto advance = [&](CyclicPos& P) {
-    P.g += CB;
-    if (P.g >= P.gend) {
-      P.j = (P.j + 1 == ns) ? 0 : P.j + 1;
-#pragma unroll
-      for (int j = 0; j < MAXS; ++j)
-        if (j == P.j) P.g = s_first[j], P.gend = s_end[j];
-    }
-  };
-  CyclicPos P{0, s_first[0], s_end[0]};
-  int inflight = 0;
-  if (ns > 0 && done == 0.0) {
-    for (int st = 0; st < NST; ++st) {
-      issue(st, P);
-      ++inflight;
-      advance(P);
-    }
-  }
-  uint32_t phase = 0;
-  int st = 0;
-  bool failed = false;
-  int it = (int)scal[kIters];
-  unsigned int barrier_no = 0;
-  // out[j] = (K src)[rows of owned slice j], consuming the warp's chunk stream
-  auto product = [&](const T* src, T (*out)[3]) {
-#pragma unroll
-    for (int j = 0; j < MAXS; ++j) {
-      if (j < ns && !failed) {
-        T a0 = T(0), a1 = T(0), a2 = T(0);
-        for (int g = s_first[j]; g < s_end[j]; g += CB) {
-          const bool okw =
-              __all_sync(0xffffffffu, mbar_wait_bounded(smem_addr(&bars[warp][st]), (phase >> st) & 1u));
-          if (!okw) {
-            failed = true;
-            break;
-          }
-          phase ^= 1u << st;
-          --inflight;
-          const T* sv_ = reinterpret_cast<const T*>(wbase + (size_t)st * C::kStageBytes);
-          const int32_t* sc = reinterpret_cast<const int32_t*>(wbase + (size_t)st * C::kStageBytes + C::kValBytes);
-          const int nb = min(CB, s_end[j] - g);
-          V3<T> xc[CB];
-#pragma unroll
-          for (int k = 0; k < CB; ++k) xc[k] = load3rw(src, k < nb ? sc[32 * k + lane] : 0);
-#pragma unroll
-          for (int k = 0; k < CB; ++k) {
-            if (k < nb) {
-              const T* v = sv_ + 288 * k + lane;
-              a0 += v[0] * xc[k].x + v[32] * xc[k].y + v[64] * xc[k].z;
-              a1 += v[96] * xc[k].x + v[128] * xc[k].y + v[160] * xc[k].z;
-              a2 += v[192] * xc[k].x + v[224] * xc[k].y + v[256] * xc[k].z;
-            }
-          }
-          __syncwarp();
-          issue(st, P);
-          ++inflight;
-          advance(P);
-          st = (st + 1 == NST) ? 0 : st + 1;
-        }
-        out[j][0] = a0, out[j][1] = a1, out[j][2] = a2;
-      }
-    }
-  };
-  // w0 = A u0 (u0 = z of the init kernel, visible since the previous launch)
-  if (done == 0.0) product(zg, wv);
-  while (done == 0.0) {
-    failed = __syncthreads_or(failed);
-    if (failed) break;
-    const int par = it & 1;
-    T* mbuf = par ? p1 : p0;
-    // m = M^-1 w on the owned rows (published), gamma = (r,u), delta = (w,u), (r,r)
-    double red[3] = {0.0, 0.0, 0.0};
-#pragma unroll
-    for (int j = 0; j < MAXS; ++j) {
-      const int row = 32 * (gw + j * nw) + lane;
-      if (j < ns && row < A.n_rows) {
-        const T* m = minv + 9 * (int64_t)row;
-        T mv[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a)
-          mv[a] = __ldg(m + 3 * a) * wv[j][0] + __ldg(m + 3 * a + 1) * wv[j][1] + __ldg(m + 3 * a + 2) * wv[j][2];
-        store3(mbuf, row, mv[0], mv[1], mv[2]);
-        T g_ = T(0), d_ = T(0), r_ = T(0);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          g_ += rv[j][c] * uv[j][c];
-          d_ += wv[j][c] * uv[j][c];
-          r_ += rv[j][c] * rv[j][c];
-        }
-        red[0] += double(g_), red[1] += double(d_), red[2] += double(r_);
-      }
-    }
-    cta_reduce<3>(red, sw);
-    ++barrier_no;
-    if (!grid_allreduce<3>(red, part_b + par * 3 * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
-      failed = true;
-      break;
-    }
-    const double gamma = red[0], delta = red[1];
-    rrs = red[2];
-    if (rrs <= tol2) {
-      done = 1.0;
-      break;
-    }
-    if (it >= maxit) {
-      done = 2.0;
-      break;
-    }
-    double beta = 0.0, alpha;
-    if (it == 0) {
-      alpha = gamma / delta;
-    } else {
-      beta = gamma / gamma_old;
-      alpha = gamma / (delta - beta * gamma / alpha_old);
-    }
-    if (!isfinite(alpha) || alpha == 0.0) {  // breakdown
-      done = 3.0;
-      break;
-    }
-    // n = A m
-    T nv[MAXS][3];
-    product(mbuf, nv);
-    const T tb = T(beta), ta = T(alpha);
-#pragma unroll
-    for (int j = 0; j < MAXS; ++j) {
-      const int row = 32 * (gw + j * nw) + lane;
-      V3<T> m3 = {T(0), T(0), T(0)};
-      if (j < ns && row < A.n_rows) m3 = load3rw(mbuf, row);  // this thread's own m, written above
-      const T mv[3] = {m3.x, m3.y, m3.z};
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        zv[j][c] = nv[j][c] + tb * zv[j][c];
-        qv[j][c] = mv[c] + tb * qv[j][c];
-        sv3[j][c] = wv[j][c] + tb * sv3[j][c];
-        pv[j][c] = uv[j][c] + tb * pv[j][c];
-        xv[j][c] += ta * pv[j][c];
-        rv[j][c] -= ta * sv3[j][c];
-        uv[j][c] -= ta * qv[j][c];
-        wv[j][c] -= ta * zv[j][c];
-      }
-    }
-    gamma_old = gamma;
-    alpha_old = alpha;
-    ++it;
-  }
-  if (failed) done = kDoneDeviceTimeout;
-  for (int k = 0; k < inflight; ++k) {
-    mbar_wait_bounded(smem_addr(&bars[warp][st]), (phase >> st) & 1u);
-    phase ^= 1u << st;
-    st = (st + 1 == NST) ? 0 : st + 1;
-  }
-#pragma unroll
-  for (int j = 0; j < MAXS; ++j) {
-    const int row = 32 * (gw + j * nw) + lane;
-    if (j < ns && row < A.n_rows) store3(xg, row, xv[j][0], xv[j][1], xv[j][2]);
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    scal[kIters] = (double)it;
-    scal[kRR] = rrs;
-    scal[kDone] = done;
-  }
-  if (failed && threadIdx.x == 0) scal[kDone] = kDoneDeviceTimeout;
-}
-
-template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB, bool PIPE = false>
 cudaError_t launch_persistent(const Bsr& A, PcgWork& w, cudaStream_t s, bool query_only, bool* eligible) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
-  auto kern = PIPE ? pcg_pipelined_kernel<T, CB, NST, WARPS, MAXS, MINB>
-                   : pcg_persistent_kernel<T, CB, NST, WARPS, MAXS, MINB>;
+  auto kern = pcg_persistent_kernel<T, CB, NST, WARPS, MAXS, MINB>;
   static std::mutex mu;
   static int blocks_per_sm[64] = {0};
   int dev = 0;
@@ -628,23 +386,18 @@ cudaError_t dispatch(int variant, const Bsr& A, PcgWork& w, cudaStream_t s, bool
     if (variant == 0) return launch_persistent<float, 8, 2, 8, 4, 1>(A, w, s, query, eligible);
     if (variant == 1) return launch_persistent<float, 4, 3, 8, 8, 1>(A, w, s, query, eligible);
     if (variant == 2) return launch_persistent<float, 4, 2, 8, 2, 2>(A, w, s, query, eligible);
-    if (variant == 3) return launch_persistent<float, 2, 3, 8, 2, 3>(A, w, s, query, eligible);
-    if (variant == 4) return launch_persistent<float, 4, 2, 8, 2, 2, true>(A, w, s, query, eligible);
-    return launch_persistent<float, 8, 2, 8, 4, 1, true>(A, w, s, query, eligible);
+    return launch_persistent<float, 2, 3, 8, 2, 3>(A, w, s, query, eligible);
   } else {
     if (variant == 0) return launch_persistent<double, 4, 2, 8, 4, 1>(A, w, s, query, eligible);
     if (variant == 1) return launch_persistent<double, 2, 3, 8, 4, 1>(A, w, s, query, eligible);
     if (variant == 2) return launch_persistent<double, 2, 2, 8, 2, 2>(A, w, s, query, eligible);
-    if (variant == 3) return launch_persistent<double, 1, 3, 8, 2, 2>(A, w, s, query, eligible);
-    if (variant == 4) return launch_persistent<double, 2, 2, 8, 2, 2, true>(A, w, s, query, eligible);
-    return launch_persistent<double, 4, 2, 8, 4, 1, true>(A, w, s, query, eligible);
+    return launch_persistent<double, 1, 3, 8, 2, 2>(A, w, s, query, eligible);
   }
 }
 
 }  // namespace
 
-int pcg_persistent_variants() { return 6; }
-int pcg_persistent_first_pipelined() { return 4; }
+int pcg_persistent_variants() { return 4; }
 
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant) {
   bool ok = false;

@@ -167,7 +167,6 @@ void launch_fill64(double* y, double v, int64_t n, cudaStream_t s);
 // cg_persistent.cu -- the whole CG solve (after launch_pcg_init) in one cooperative launch; the result in w.x
 // and the scalars as after the two-kernel iterations
 int pcg_persistent_variants();
-int pcg_persistent_first_pipelined();  // variants from here on use the pipelined recurrences
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant);
 cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s);
 

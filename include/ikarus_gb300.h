@@ -192,9 +192,7 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
 /* CG kernels (no reference counterpart).  spmv_kind 0 = two kernels per iteration with a direct-load SpMV,
  * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..8 = the
  * whole solve in one persistent cooperative kernel (grid barriers for the two reductions of an iteration;
- * only where every warp's rows fit its registers), 9..10 = the same with the pipelined CG recurrences (one
- * grid barrier per iteration; their recurrences drift, attainable relative residual about 1e-9 in FP64, so the
- * tuner does not pick them), -1 = autotune; l2_keep_fraction in [0, 1) = share of the
+ * only where every warp's rows fit its registers), -1 = autotune; l2_keep_fraction in [0, 1) = share of the
  * matrix the staged kernels keep in L2 across iterations, -1 = autotune.  The choice is made at the
  * next factorize from timed CG iterations on the assembled tangent and kept for that assembler.  info
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */

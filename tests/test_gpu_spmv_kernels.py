@@ -8,9 +8,6 @@ from ikarus_gb300 import problems
 
 pytestmark = pytest.mark.gpu
 
-PIPELINED = (9, 10)
-
-
 def true_residual_bound(fp32):
     """Relative true residual |K x - b| / |b| (FP64 arithmetic on the stored tangent) a converged solve reaches.
     FP64: the CG tolerance.  FP32: the recursively updated CG residual drifts from the true one by about
@@ -18,10 +15,9 @@ def true_residual_bound(fp32):
     return 2e-3 if fp32 else 1e-10
 
 
-# 0 direct-load SpMV, 1-4 staged SpMV variants, 5-8 persistent CG variants, 9-10 pipelined persistent CG;
-# keep = L2 evict_last share
+# 0 direct-load SpMV, 1-4 staged SpMV variants, 5-8 persistent CG variants; keep = L2 evict_last share
 KINDS = [(0, 0.0), (1, 0.0), (2, 0.0), (3, 0.0), (4, 0.0), (1, 0.5), (2, 0.75), (5, 0.0), (6, 0.0), (7, 0.0),
-         (8, 0.0), (5, 0.4), (9, 0.0), (10, 0.0), (9, 0.45)]
+         (8, 0.0), (5, 0.4)]
 
 
 @pytest.fixture(scope="module", params=[0, 1], ids=["fp64", "fp32"])
@@ -41,8 +37,6 @@ def system(request, ikr):
 def test_spmv_kernel_solves(ikr, system, kind, keep, graphs):
     fp32, p, asm, K, b = system
     rtol = 1e-5 if fp32 else 1e-11
-    if kind in PIPELINED and not fp32:
-        rtol = 1e-8  # the pipelined recurrences drift: attainable relative residual about 1e-9 in FP64
     ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=rtol, max_iter=20000)
     ls.set_kernel(kind, keep)
     ls.set_launch(use_graphs=graphs, chunk_len=8)
@@ -53,8 +47,7 @@ def test_spmv_kernel_solves(ikr, system, kind, keep, graphs):
     x2 = ls.solve(asm, b)
     assert np.array_equal(x1, x2), "repeated solve is not bit-identical"
     assert 0 < it1 and rel1 <= rtol
-    bound = true_residual_bound(fp32) if kind not in PIPELINED or fp32 else 1e-7
-    assert np.linalg.norm(K @ x1 - b) <= bound * np.linalg.norm(b)
+    assert np.linalg.norm(K @ x1 - b) <= true_residual_bound(fp32) * np.linalg.norm(b)
 
 
 def test_tuner_choice_is_reported(ikr, system):
@@ -62,6 +55,6 @@ def test_tuner_choice_is_reported(ikr, system):
     ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-5 if fp32 else 1e-11)
     ls.compute(asm)
     kind, keep, us = ls.kernel_info()
-    assert 0 <= kind <= 10 and 0.0 <= keep < 1.0 and us > 0.0
+    assert 0 <= kind <= 8 and 0.0 <= keep < 1.0 and us > 0.0
     x = ls.solve(asm, b)
     assert np.linalg.norm(K @ x - b) <= true_residual_bound(fp32) * np.linalg.norm(b)
