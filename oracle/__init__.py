@@ -20,6 +20,7 @@ EAS_NONE, EAS_GL, EAS_H, EAS_HT = 0, 1, 2, 3
 DBC_RAW, DBC_REDUCED, DBC_FULL = 0, 1, 2
 SOLVER_BANDED_LDLT, SOLVER_CG_JACOBI = 0, 1
 MATERIAL_NEOHOOKE, MATERIAL_SVK = 0, 1
+PF_ARC_LENGTH, PF_LOAD_CONTROL, PF_DISPLACEMENT_CONTROL = 0, 1, 2
 ERRORS = {-1: "ARG", -2: "NOT_IMPLEMENTED", -3: "NONPOSITIVE_DETC", -4: "SINGULAR", -5: "NOT_CONVERGED"}
 
 
@@ -65,6 +66,11 @@ def lib():
         L.orc_cg_jacobi_csc.argtypes = [C.c_int, lp, ip, dp, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_int)]
         L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
                                        C.c_double, dp, dp, ip, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.orc_path_following.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int, ip, C.c_int, C.c_double, C.c_int,
+                                         C.c_int, C.c_double, dp, dp, ip, dp, dp, dp, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_int)]
+        L.orc_path_following_toy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, dp,
+                                             dp, ip, dp, C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -92,6 +98,22 @@ def cg_jacobi(col_ptr, row_idx, values, b, rtol, max_iter):
     if code not in (0, -5):
         raise OracleError(code, "cg_jacobi")
     return x, its.value, code == 0
+
+
+def path_following_toy(kind=PF_ARC_LENGTH, idbc=False, steps=5, step_size=0.1, target_iterations=0, tol=1e-8,
+                       max_iter=20):
+    """The oracle's path-following routine on the reference's two-dof test operator
+    (tests/src/testpathfollowing.cpp:26-40), starting from D = 0, lambda = 0."""
+    d = np.zeros(2)
+    lam = np.zeros(1)
+    its = np.zeros(steps + 1, dtype=np.int32)
+    lams = np.zeros(steps + 1)
+    ns = C.c_int(0)
+    code = lib().orc_path_following_toy(kind, int(idbc), steps, step_size, target_iterations, tol, max_iter,
+                                        _p(d, C.c_double), _p(lam, C.c_double), _p(its, C.c_int32),
+                                        _p(lams, C.c_double), C.byref(ns))
+    _check(code, "path_following_toy")
+    return dict(d=d, lam=float(lam[0]), iterations=its[: ns.value].tolist(), lambdas=lams[: ns.value])
 
 
 def from_problem(p, faithful=False):
@@ -250,3 +272,25 @@ class OracleProblem:
             raise OracleError(code, "load_control")
         return dict(u=u, lam=float(lam[0]), iterations=its[: ns.value], res_norms=rn[: ns.value],
                     total_iterations=tot.value, success=(code == 0))
+
+    def path_following(self, steps, step_size, kind=PF_ARC_LENGTH, controlled=None, target_iterations=0, tol=1e-8,
+                       max_iter=20, solver=SOLVER_BANDED_LDLT, cg_rtol=1e-12, u0=None, lam0=0.0,
+                       allow_failure=False):
+        """PathFollowing::run with NewtonRaphsonWithSubsidiaryFunction (pathfollowing.inl:25-73); entry k of the
+        per-solve arrays belongs to load step k - 1."""
+        u = self._u(u0).copy()
+        lam = np.array([lam0])
+        its = np.zeros(steps + 1, dtype=np.int32)
+        rn = np.zeros(steps + 1)
+        lams = np.zeros(steps + 1)
+        psi = np.zeros(1)
+        ci = np.ascontiguousarray(controlled if controlled is not None else [], dtype=np.int32)
+        ns, tot = C.c_int(0), C.c_int(0)
+        code = lib().orc_path_following(self.h, kind, steps, step_size, len(ci), _p(ci, C.c_int32) if len(ci) else None,
+                                        target_iterations, tol, max_iter, solver, cg_rtol, _p(u, C.c_double),
+                                        _p(lam, C.c_double), _p(its, C.c_int32), _p(rn, C.c_double),
+                                        _p(lams, C.c_double), _p(psi, C.c_double), C.byref(ns), C.byref(tot))
+        if code != 0 and not (allow_failure and code == -5):
+            raise OracleError(code, "path_following")
+        return dict(u=u, lam=float(lam[0]), iterations=its[: ns.value], res_norms=rn[: ns.value],
+                    lambdas=lams[: ns.value], psi=float(psi[0]), total_iterations=tot.value, success=(code == 0))

@@ -14,6 +14,7 @@
 #include <array>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <numeric>
 #include <vector>
 
@@ -1153,6 +1154,388 @@ int orc_load_control(orc_problem* p, int steps, double t0, double t1, double tol
     if (it == max_iter) return ORC_ERR_NOT_CONVERGED;  // success = (iter != maxIter)
   }
   return ORC_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------------------
+// Path following: Newton-Raphson with a scalar subsidiary function (newtonraphsonwithscalarsubsidiaryfunction.hh
+// :207-316) under PathFollowing::run (pathfollowing.inl:25-73), with the subsidiary functions ArcLength,
+// LoadControlSubsidiaryFunction and DisplacementControl (pathfollowingfunctions.hh:88-368), idbcIncrement
+// (common.hh:38-51) and the IterationBased step-size adaptation (adaptivestepsizing.hh:36-57).  The core is
+// written over callbacks so that the same code runs the reference's two-dof test operator (golden values of
+// tests/src/testpathfollowing.cpp) and the finite-element problem.
+namespace {
+
+using Vec = std::vector<double>;
+
+double dotv(const Vec& a, const Vec& b) {
+  double s = 0;
+  for (size_t i = 0; i < a.size(); ++i) s += a[i] * b[i];
+  return s;
+}
+
+struct PFOps {
+  int nx = 0;  // size of the global solution
+  int nr = 0;  // size of the residual / correction
+  std::function<int(const Vec& x, double lam, Vec& R)> residual;
+  std::function<int(const Vec& x, double lam)> tangent;   // assemble (and factor) K at (x, lam)
+  std::function<int(const Vec& b, Vec& sol)> solve;         // K^{-1} b with the last tangent
+  bool has_idbc = false;
+  std::function<int(const Vec& x, double lam, Vec& F)> idbc_force;
+  std::function<void(Vec& x, const Vec& dx)> update;       // updateFunction(x, dx)
+  std::function<void(Vec& x, double lam)> sync;            // syncParameterAndGlobalSolution
+  std::function<int(const Vec& x, const Vec& corr)> on_correction;  // CORRECTION_UPDATED (EAS state)
+};
+
+struct PFArgs {  // SubsidiaryArgs (pathfollowingfunctions.hh:30-69)
+  double step_size = 0;
+  Vec DD;
+  double Dlambda = 0, f = 0;
+  Vec dfdDD;
+  double dfdDlambda = 0;
+  int current_step = 0;
+};
+
+struct PFType {
+  int kind = ORC_PF_ARC_LENGTH;
+  double psi = 0;
+  bool computed = false;
+  std::vector<int> ci;  // DisplacementControl's controlled indices
+};
+
+// idbcIncrement (common.hh:38-51): the change of the synchronised solution when the load factor grows by Dlambda
+Vec idbc_increment(const PFOps& o, const Vec& x, double lam, double Dlambda) {
+  Vec d(o.nx, 0.0);
+  if (!o.has_idbc) return d;
+  Vec y = x;
+  o.sync(y, lam + Dlambda);
+  for (int i = 0; i < o.nx; ++i) d[i] = y[i] - x[i];
+  return d;
+}
+
+void subsidiary(const PFOps& o, PFType& t, const Vec& x, double lam, PFArgs& a) {
+  if (t.kind == ORC_PF_ARC_LENGTH) {  // ArcLength::operator() (pathfollowingfunctions.hh:102-115)
+    const Vec d = idbc_increment(o, x, lam, a.Dlambda);
+    const double dd2 = dotv(d, d);
+    const double root = std::sqrt(dotv(a.DD, a.DD) + dd2 + t.psi * t.psi * a.Dlambda * a.Dlambda);
+    a.f = root - a.step_size;
+    if (!t.computed) {
+      std::fill(a.dfdDD.begin(), a.dfdDD.end(), 0.0);
+      a.dfdDlambda = 0.0;
+    } else {
+      for (int i = 0; i < o.nr; ++i) a.dfdDD[i] = a.DD[i] / root;
+      const double dhat02 = dd2 / (a.Dlambda * a.Dlambda);  // Dhat0 = idbcDelta / Dlambda
+      a.dfdDlambda = ((dhat02 + t.psi * t.psi) * a.Dlambda) / root;
+    }
+  } else if (t.kind == ORC_PF_LOAD_CONTROL) {  // LoadControlSubsidiaryFunction::operator() (:230-236)
+    a.f = a.Dlambda - a.step_size;
+    std::fill(a.dfdDD.begin(), a.dfdDD.end(), 0.0);
+    a.dfdDlambda = 1.0;
+  } else {  // DisplacementControl::operator() (:316-324)
+    double s = 0;
+    for (int i : t.ci) s += a.DD[i] * a.DD[i];
+    const double nrm = std::sqrt(s);
+    a.f = nrm - a.step_size;
+    a.dfdDlambda = 0.0;
+    std::fill(a.dfdDD.begin(), a.dfdDD.end(), 0.0);
+    for (int i : t.ci) a.dfdDD[i] = a.DD[i] / nrm;
+  }
+}
+
+struct PFSolveInfo {
+  int iterations = 0;
+  double residual_norm = 0, correction_norm = 0;
+  bool success = true;
+};
+
+// NewtonRaphsonWithSubsidiaryFunction::solve (newtonraphsonwithscalarsubsidiaryfunction.hh:207-316)
+int pf_nr_solve(const PFOps& o, PFType& t, Vec& x, double& lam, PFArgs& a, double tol, int max_iter,
+                PFSolveInfo& info) {
+  info = PFSolveInfo{};
+  // Fext0 = -R(x = 0, lambda = 1): the load is taken as lambda * Fext0 (:225-232)
+  Vec zero(o.nx, 0.0), R, fext0(o.nr);
+  int st = o.residual(zero, 1.0, R);
+  if (st) return st;
+  for (int i = 0; i < o.nr; ++i) fext0[i] = -R[i];
+  Vec rx;
+  st = o.residual(x, lam, rx);
+  if (st) return st;
+  a.dfdDD.assign(o.nr, 0.0);
+  if ((int)a.DD.size() != o.nr) a.DD.assign(o.nr, 0.0);
+  subsidiary(o, t, x, lam, a);
+  double rnorm = std::sqrt(dotv(rx, rx));
+  info.residual_norm = rnorm;
+  int iter = 0;
+  Vec b1(o.nr), b2(o.nr), dR, dL, dD(o.nr), F;
+  while (rnorm > tol && iter < max_iter) {
+    st = o.tangent(x, lam);
+    if (st) return st;
+    for (int i = 0; i < o.nr; ++i) b1[i] = -rx[i];
+    b2 = fext0;
+    if (o.has_idbc) {  // second column Fext0 - idbcForce(req) (:260-263)
+      st = o.idbc_force(x, lam, F);
+      if (st) return st;
+      for (int i = 0; i < o.nr; ++i) b2[i] -= F[i];
+    }
+    if ((st = o.solve(b1, dR)) || (st = o.solve(b2, dL))) return st;
+    const double dlam = (-a.f - dotv(a.dfdDD, dR)) / (dotv(a.dfdDD, dL) + a.dfdDlambda);  // :275-276
+    for (int i = 0; i < o.nr; ++i) dD[i] = dR[i] + dlam * dL[i];
+    if (o.on_correction && (st = o.on_correction(x, dD))) return st;
+    o.update(x, dD);
+    for (int i = 0; i < o.nr; ++i) a.DD[i] += dD[i];
+    lam += dlam;
+    a.Dlambda += dlam;
+    if (o.has_idbc) o.sync(x, lam);
+    info.correction_norm = std::sqrt(dotv(dD, dD) + dlam * dlam);
+    st = o.residual(x, lam, rx);
+    if (st) return st;
+    subsidiary(o, t, x, lam, a);
+    rnorm = std::sqrt(dotv(rx, rx) + a.f * a.f);  // :298
+    info.residual_norm = rnorm;
+    ++iter;
+    if (!std::isfinite(rnorm)) break;
+  }
+  info.iterations = iter;
+  info.success = iter != max_iter && std::isfinite(rnorm);
+  return ORC_OK;
+}
+
+// ArcLength::initialPrediction (pathfollowingfunctions.hh:132-174) and the other kinds' initial predictions
+int pf_initial_prediction(const PFOps& o, PFType& t, Vec& x, double& lam, PFArgs& a) {
+  if (t.kind == ORC_PF_LOAD_CONTROL) {  // :249-255
+    a.Dlambda = a.step_size;
+    lam = a.Dlambda;
+  } else if (t.kind == ORC_PF_DISPLACEMENT_CONTROL) {  // :330-336
+    for (int i : t.ci) a.DD[i] = a.step_size;
+    for (int i = 0; i < o.nx; ++i) x[i] = a.DD[i];
+  } else {
+    const double dlambda = 1.0;
+    Vec idbc_delta = idbc_increment(o, x, lam, dlambda);
+    const double dhat02 = dotv(idbc_delta, idbc_delta) / (dlambda * dlambda);
+    lam = dlambda;
+    Vec R, F;
+    int st = o.residual(x, lam, R);
+    if (st) return st;
+    if ((st = o.tangent(x, lam))) return st;
+    if (o.has_idbc) {
+      if ((st = o.idbc_force(x, lam, F))) return st;
+      for (int i = 0; i < o.nr; ++i) R[i] += F[i];
+    }
+    for (double& v : R) v = -v;
+    if ((st = o.solve(R, a.DD))) return st;
+    const double dd2 = dotv(a.DD, a.DD);
+    t.psi = std::sqrt(dd2 + dhat02);
+    const double s = std::sqrt(dd2 + dhat02 + t.psi * t.psi * dlambda * dlambda);
+    for (double& v : a.DD) v *= a.step_size / s;
+    a.Dlambda = a.step_size / s;
+    for (double& v : idbc_delta) v *= a.Dlambda / dlambda;
+    o.update(x, a.DD);
+    lam = a.Dlambda;
+    if (o.has_idbc) o.sync(x, lam);
+    t.psi = std::sqrt((dotv(idbc_delta, idbc_delta) + dotv(a.DD, a.DD)) / (a.Dlambda * a.Dlambda));
+  }
+  t.computed = true;
+  return ORC_OK;
+}
+
+// intermediatePrediction of the three kinds (:188-195, :269-274, :339-344)
+void pf_intermediate_prediction(const PFOps& o, PFType& t, Vec& x, double& lam, PFArgs& a) {
+  if (t.kind == ORC_PF_LOAD_CONTROL) {
+    lam += a.Dlambda;
+    return;
+  }
+  if (t.kind == ORC_PF_DISPLACEMENT_CONTROL) {
+    for (int i = 0; i < o.nx; ++i) x[i] += a.DD[i];
+    return;
+  }
+  o.update(x, a.DD);
+  lam += a.Dlambda;
+  if (o.has_idbc) o.sync(x, lam);
+}
+
+// PathFollowing::run (pathfollowing.inl:25-73); infos receive steps + 1 entries (load step -1 first)
+int pf_run(const PFOps& o, PFType& t, int steps, double step_size, int target_iterations, double tol, int max_iter,
+           Vec& x, double& lam, int32_t* iterations, double* res_norms, double* lambdas, double* psi_out,
+           int* n_solves, int* total) {
+  PFArgs a;
+  a.DD.assign(o.nr, 0.0);
+  a.dfdDD.assign(o.nr, 0.0);
+  a.step_size = step_size;
+  PFSolveInfo info;
+  int solves = 0, tot = 0;
+  auto record = [&]() {
+    if (iterations) iterations[solves] = info.iterations;
+    if (res_norms) res_norms[solves] = info.residual_norm;
+    if (lambdas) lambdas[solves] = lam;
+    tot += info.iterations;
+    ++solves;
+    if (n_solves) *n_solves = solves;
+    if (total) *total = tot;
+    if (psi_out) *psi_out = t.psi;
+  };
+  int st = pf_nr_solve(o, t, x, lam, a, tol, max_iter, info);  // load step -1
+  if (st) return st;
+  record();
+  if (!info.success) return ORC_ERR_NOT_CONVERGED;
+  if ((st = pf_initial_prediction(o, t, x, lam, a))) return st;
+  if ((st = pf_nr_solve(o, t, x, lam, a, tol, max_iter, info))) return st;
+  record();
+  if (!info.success) return ORC_ERR_NOT_CONVERGED;
+  for (int ls = 1; ls < steps; ++ls) {
+    a.current_step = ls;
+    // AdaptiveStepSizing::IterationBased (adaptivestepsizing.hh:36-47); 0 = NoOp
+    if (target_iterations > 0 && info.iterations > target_iterations)
+      a.step_size = std::sqrt((double)target_iterations / info.iterations) * a.step_size;
+    pf_intermediate_prediction(o, t, x, lam, a);
+    if ((st = pf_nr_solve(o, t, x, lam, a, tol, max_iter, info))) return st;
+    record();
+    if (!info.success) return ORC_ERR_NOT_CONVERGED;
+  }
+  return ORC_OK;
+}
+
+// The two-dof operator of the reference's path-following tests (tests/src/testpathfollowing.cpp:26-40), D = (u, w)
+void toy_residual(double u, double w, double lam, double R[2]) {
+  R[0] = 16.0 * u - 3 * w - w * w * w - (2.0 / 3.0) * lam;
+  R[1] = -3 * u + 4 * w - 3 * u * w * w - (9.0 / 4.0) * lam;
+}
+void toy_stiffness(double u, double w, double K[2][2]) {
+  K[0][0] = 16.0;
+  K[0][1] = -3.0 * w * w - 3;
+  K[1][0] = -3 * w * w - 3;
+  K[1][1] = -6 * u * w + 4;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_path_following(orc_problem* p, int kind, int steps, double step_size, int n_controlled,
+                       const int32_t* controlled, int target_iterations, double tol, int max_iter, int solver,
+                       double cg_rtol, double* u, double* lambda, int32_t* iterations, double* res_norms,
+                       double* lambdas, double* psi, int* n_solves, int* total_iterations) {
+  if (!p || !u || !lambda || steps <= 0 || kind < 0 || kind > 2) return ORC_ERR_ARG;
+  const int n = p->ndof();
+  const bool idbc = !p->idbc_rate.empty();
+  if (idbc && kind != ORC_PF_ARC_LENGTH) return ORC_ERR_NOT_IMPLEMENTED;  // checkHasNoValidIDBCForceFunction
+  PFType t;
+  t.kind = kind;
+  if (kind == ORC_PF_DISPLACEMENT_CONTROL) {
+    if (n_controlled <= 0 || !controlled) return ORC_ERR_ARG;
+    for (int k = 0; k < n_controlled; ++k) {
+      if (controlled[k] < 0 || controlled[k] >= n) return ORC_ERR_ARG;
+      t.ci.push_back(controlled[k]);
+    }
+  }
+  CSC K;
+  PFOps o;
+  o.nx = o.nr = n;
+  o.residual = [&](const Vec& x, double lam, Vec& R) -> int { return assemble_vector(*p, x.data(), lam, ORC_DBC_FULL, R); };
+  o.tangent = [&](const Vec& x, double) -> int { return assemble_matrix(*p, x.data(), ORC_DBC_FULL, K); };
+  o.solve = [&](const Vec& b, Vec& sol) -> int {
+    const bool ok = solver == ORC_SOLVER_CG_JACOBI ? cg_jacobi_solve(K, b, sol, cg_rtol, 20 * n)
+                                                   : banded_ldlt_solve(K, b, sol);
+    return ok ? ORC_OK : ORC_ERR_SINGULAR;
+  };
+  o.has_idbc = idbc;
+  o.idbc_force = [&](const Vec& x, double, Vec& F) -> int {  // obtainForcesDueToIDBC (functionhelper.hh:170-184)
+    CSC Kr;
+    int st = assemble_matrix(*p, x.data(), ORC_DBC_RAW, Kr);
+    if (st) return st;
+    F.assign(n, 0.0);
+    for (int c = 0; c < n; ++c)
+      for (int64_t k = Kr.cp[c]; k < Kr.cp[c + 1]; ++k) F[Kr.ri[k]] += Kr.v[k] * p->idbc_rate[c];
+    for (int i = 0; i < n; ++i)
+      if (p->fixed[i]) F[i] = 0.0;
+    return ORC_OK;
+  };
+  o.update = [](Vec& x, const Vec& dx) {
+    for (size_t i = 0; i < x.size(); ++i) x[i] += dx[i];
+  };
+  o.sync = [&](Vec& x, double lam) {  // entries whose prescribed value is nonzero take it
+    for (int i = 0; i < n; ++i) {
+      const double v = lam * p->idbc_rate[i];
+      if (v != 0.0) x[i] = v;
+    }
+  };
+  o.on_correction = [&](const Vec& x, const Vec& corr) -> int { return update_state(*p, x.data(), corr.data()); };
+  Vec x(u, u + n);
+  double lam = *lambda;
+  const int st = pf_run(o, t, steps, step_size, target_iterations, tol, max_iter, x, lam, iterations, res_norms,
+                        lambdas, psi, n_solves, total_iterations);
+  std::copy(x.begin(), x.end(), u);
+  *lambda = lam;
+  return st;
+}
+
+int orc_path_following_toy(int kind, int idbc, int steps, double step_size, int target_iterations, double tol,
+                           int max_iter, double* d2, double* lambda, int32_t* iterations, double* lambdas,
+                           int* n_solves) {
+  if (!d2 || !lambda || steps <= 0 || kind < 0 || kind > 2) return ORC_ERR_ARG;
+  if (idbc && kind != ORC_PF_ARC_LENGTH) return ORC_ERR_NOT_IMPLEMENTED;
+  PFType t;
+  t.kind = kind;
+  if (kind == ORC_PF_DISPLACEMENT_CONTROL) t.ci = {0};  // testpathfollowing.cpp:356
+  double Kd[2][2] = {{0, 0}, {0, 0}};
+  PFOps o;
+  o.nx = 2;
+  if (!idbc) {
+    o.nr = 2;
+    o.residual = [](const Vec& x, double lam, Vec& R) -> int {
+      R.assign(2, 0.0);
+      toy_residual(x[0], x[1], lam, R.data());
+      return ORC_OK;
+    };
+    o.tangent = [&](const Vec& x, double) -> int {
+      toy_stiffness(x[0], x[1], Kd);
+      return ORC_OK;
+    };
+    o.solve = [&](const Vec& b, Vec& s) -> int {  // dense 2x2 solve
+      const double det = Kd[0][0] * Kd[1][1] - Kd[0][1] * Kd[1][0];
+      if (det == 0.0) return ORC_ERR_SINGULAR;
+      s = {(Kd[1][1] * b[0] - Kd[0][1] * b[1]) / det, (Kd[0][0] * b[1] - Kd[1][0] * b[0]) / det};
+      return ORC_OK;
+    };
+    o.update = [](Vec& x, const Vec& dx) {
+      x[0] += dx[0];
+      x[1] += dx[1];
+    };
+  } else {  // w free, u = 0.1 lambda prescribed (testpathfollowing.cpp:80-94, 358-365)
+    o.nr = 1;
+    o.has_idbc = true;
+    o.residual = [](const Vec& x, double lam, Vec& R) -> int {
+      double r[2];
+      toy_residual(x[0], x[1], lam, r);
+      R.assign(1, r[1]);
+      return ORC_OK;
+    };
+    o.tangent = [&](const Vec& x, double) -> int {
+      toy_stiffness(x[0], x[1], Kd);
+      return ORC_OK;
+    };
+    o.solve = [&](const Vec& b, Vec& s) -> int {
+      if (Kd[1][1] == 0.0) return ORC_ERR_SINGULAR;
+      s.assign(1, b[0] / Kd[1][1]);
+      return ORC_OK;
+    };
+    o.idbc_force = [&](const Vec& x, double, Vec& F) -> int {
+      double K[2][2];
+      toy_stiffness(x[0], x[1], K);
+      F.assign(1, K[1][0] * 0.1);
+      return ORC_OK;
+    };
+    o.update = [](Vec& x, const Vec& dx) { x[1] += dx[0]; };
+    o.sync = [](Vec& x, double lam) { x[0] = 0.1 * lam; };
+  }
+  Vec x(d2, d2 + 2);
+  double lam = *lambda;
+  const int st = pf_run(o, t, steps, step_size, target_iterations, tol, max_iter, x, lam, iterations, nullptr,
+                        lambdas, nullptr, n_solves, nullptr);
+  d2[0] = x[0];
+  d2[1] = x[1];
+  *lambda = lam;
+  return st;
 }
 
 }  // extern "C"

@@ -95,6 +95,23 @@ int orc_load_control(orc_problem* p, int load_steps, double t_begin, double t_en
                      int max_iter, int solver, double cg_rtol, double* u, double* lambda, int32_t* iterations,
                      double* res_norms, int* n_solves, int* total_iterations);
 
+/* Path following (pathfollowing.inl:25-73) with Newton-Raphson and a scalar subsidiary function
+ * (newtonraphsonwithscalarsubsidiaryfunction.hh:207-316).  kind: ORC_PF_* (pathfollowingfunctions.hh);
+ * controlled: DisplacementControl's dof indices; target_iterations > 0 selects AdaptiveStepSizing::IterationBased
+ * (0 = NoOp).  Full Dirichlet handling; inhomogeneous Dirichlet values (orc_set_dirichlet_values) only with the
+ * arc length.  iterations / res_norms / lambdas: steps + 1 entries (the solve at load step -1 first); psi: the arc
+ * length's scaling factor after the run. */
+enum { ORC_PF_ARC_LENGTH = 0, ORC_PF_LOAD_CONTROL = 1, ORC_PF_DISPLACEMENT_CONTROL = 2 };
+int orc_path_following(orc_problem* p, int kind, int steps, double step_size, int n_controlled,
+                       const int32_t* controlled, int target_iterations, double tol, int max_iter, int solver,
+                       double cg_rtol, double* u, double* lambda, int32_t* iterations, double* res_norms,
+                       double* lambdas, double* psi, int* n_solves, int* total_iterations);
+/* The same routine on the two-dof operator of tests/src/testpathfollowing.cpp:26-40 (idbc = 1: only w is free and
+ * u = 0.1 lambda is prescribed, :80-94); pins the routine against that test's golden values. */
+int orc_path_following_toy(int kind, int idbc, int steps, double step_size, int target_iterations, double tol,
+                           int max_iter, double* d2, double* lambda, int32_t* iterations, double* lambdas,
+                           int* n_solves);
+
 #ifdef __cplusplus
 }
 #endif
