@@ -193,6 +193,13 @@ SIGNATURES = {
     "ikr_load_control_subscribe": ([_vp, _CTRL_OBS, _vp], C.c_int),
     "ikr_load_control_run": ([_vp, _vp, C.POINTER(_ControlInfo), C.POINTER(_NRInfo), _I], C.c_int),
     "ikr_load_control_set_predictor": ([_vp, _I, _vp, _dp, _I], C.c_int),
+    "ikr_path_following_create": ([C.POINTER(_vp), _vp, _I, _D, _I, _I, _ip], C.c_int),
+    "ikr_path_following_destroy": ([_vp], C.c_int),
+    "ikr_path_following_set_adaptive_step_sizing": ([_vp, _I, _I], C.c_int),
+    "ikr_path_following_subscribe": ([_vp, _CTRL_OBS, _vp], C.c_int),
+    "ikr_path_following_run": ([_vp, _vp, C.POINTER(_ControlInfo), C.POINTER(_NRInfo), _I], C.c_int),
+    "ikr_path_following_subsidiary_args": ([_vp, _dp], C.c_int),
+    "ikr_path_following_increment": ([_vp, _dp], C.c_int),
     "ikr_load_control_predictor_stats": ([_vp, _ip, _ip], C.c_int),
     "ikr_load_control_predictor_history": ([_vp, _I, _dp, _ip], C.c_int),
     "ikr_load_control_set_predictor_gate": ([_vp, _I], C.c_int),
@@ -792,6 +799,119 @@ class LoadControl:
         infos = (_NRInfo * cap)()
         ci = _ControlInfo()
         _err(lib().ikr_load_control_run(self.h, req.h, C.byref(ci), infos, cap), "LoadControl::run")
+        return ControlInformation(bool(ci.success), [NonLinearSolverInformation._from(infos[i])
+                                                     for i in range(min(ci.n_solver_infos, cap))],
+                                  ci.total_iterations, ci.total_linear_iterations)
+
+
+class ArcLength:
+    """Subsidiary function of the standard arc-length method (pathfollowingfunctions.hh:88-203)."""
+    kind = 0
+
+    def name(self):
+        return "Arc length"
+
+
+class LoadControlSubsidiaryFunction:
+    """Subsidiary function f = Dlambda - s (pathfollowingfunctions.hh:217-281)."""
+    kind = 1
+
+    def name(self):
+        return "Load Control"
+
+
+class DisplacementControl:
+    """Subsidiary function f = ||DD(controlledIndices)|| - s (pathfollowingfunctions.hh:295-368)."""
+    kind = 2
+
+    def __init__(self, controlledIndices):
+        self.controlledIndices = [int(i) for i in controlledIndices]
+
+    def name(self):
+        return "Displacement Control"
+
+
+class AdaptiveStepSizing:
+    """AdaptiveStepSizing::NoOp and ::IterationBased (adaptivestepsizing.hh:14-57)."""
+
+    class NoOp:
+        kind = 0
+
+        def targetIterations(self):
+            return 0
+
+    class IterationBased:
+        kind = 1
+
+        def __init__(self, targetIterations=0):
+            self._t = int(targetIterations)
+
+        def targetIterations(self):
+            return self._t
+
+        def setTargetIterations(self, t):
+            if int(t) == 0:
+                raise IkarusError(-3, "TargetIterations should not be equal to 0.")
+            self._t = int(t)
+
+
+class PathFollowing:
+    """PathFollowing (pathfollowing.hh:148-236) with NewtonRaphsonWithSubsidiaryFunction: the Newton object
+    supplies the assembler, the linear solver and the tolerances; the default subsidiary function is the arc
+    length and the default step-size adaptation NoOp."""
+
+    def __init__(self, nonLinearSolver: NewtonRaphson, steps: int, stepSize: float, pathFollowingType=None,
+                 adaptiveStepSizing=None):
+        self.nonLinearSolver = nonLinearSolver
+        self.steps = steps
+        self.pathFollowingType = pathFollowingType if pathFollowingType is not None else ArcLength()
+        ci = getattr(self.pathFollowingType, "controlledIndices", None)
+        arr = np.ascontiguousarray(ci if ci else [], dtype=np.int32)
+        h = C.c_void_p()
+        _err(lib().ikr_path_following_create(C.byref(h), nonLinearSolver.h, int(steps), float(stepSize),
+                                             int(self.pathFollowingType.kind), len(arr),
+                                             _ptr(arr, C.c_int32) if len(arr) else None), "path following")
+        self.h = h
+        self._cbs = []
+        if adaptiveStepSizing is not None and adaptiveStepSizing.kind == 1:
+            _err(lib().ikr_path_following_set_adaptive_step_sizing(self.h, 1, adaptiveStepSizing.targetIterations()),
+                 "adaptive step sizing")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_path_following_destroy(self.h)
+            self.h = None
+
+    def name(self):
+        return "Path following with " + self.pathFollowingType.name()
+
+    def subscribe(self, fn):
+        """fn(message: ControlMessages, state: dict)"""
+        def tramp(msg, st, _user):
+            s = st.contents
+            fn(ControlMessages(msg), dict(loadStep=s.load_step, stepSize=s.step_size, loadFactor=s.load_factor))
+        cb = _CTRL_OBS(tramp)
+        self._cbs.append(cb)
+        _err(lib().ikr_path_following_subscribe(self.h, cb, None), "subscribe")
+
+    def subsidiary_args(self):
+        """dict(stepSize, Dlambda, f, dfdDlambda, psi, currentStep) of the current state."""
+        out = np.zeros(6)
+        _err(lib().ikr_path_following_subsidiary_args(self.h, _ptr(out)))
+        return dict(stepSize=out[0], Dlambda=out[1], f=out[2], dfdDlambda=out[3], psi=out[4],
+                    currentStep=int(out[5]))
+
+    def increment(self, n):
+        """SubsidiaryArgs::DD of the current step (n dofs)."""
+        out = np.zeros(n)
+        _err(lib().ikr_path_following_increment(self.h, _ptr(out)))
+        return out
+
+    def run(self, req: FERequirements) -> ControlInformation:
+        cap = self.steps + 1
+        infos = (_NRInfo * cap)()
+        ci = _ControlInfo()
+        _err(lib().ikr_path_following_run(self.h, req.h, C.byref(ci), infos, cap), "PathFollowing::run")
         return ControlInformation(bool(ci.success), [NonLinearSolverInformation._from(infos[i])
                                                      for i in range(min(ci.n_solver_infos, cap))],
                                   ci.total_iterations, ci.total_linear_iterations)

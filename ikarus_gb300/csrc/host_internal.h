@@ -779,6 +779,8 @@ double device_dot(ikr_fes f, const double* x, const double* y, int64_t n, DBuf<d
 void assemble_vector(ikr_asm a, ikr_req r, int dbc);
 void assemble_matrix(ikr_asm a, ikr_req r, int dbc);
 void update_state(ikr_fes f, ikr_req r, const double* corr_dev);
+// syncParameterAndGlobalSolution: u = lambda * rate where that value is nonzero
+void idbc_sync(ikr_asm a, ikr_req r);
 // Newton-Raphson solve (newtonraphson.hh:193-257); ref_norm > 0 replaces the initial residual norm as the
 // reference of the relative convergence test
 void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double ref_norm = 0.0);

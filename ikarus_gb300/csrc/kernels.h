@@ -115,6 +115,10 @@ void launch_norm2(const double* x, int64_t n, double* partials, double* out, cud
 // inhomogeneous Dirichlet values: u[i] = lambda rate[i] where nonzero; R += step F on the free dofs
 void launch_idbc_sync(double* u, const double* rate, double lambda, int64_t n, cudaStream_t s);
 void launch_idbc_force(double* R, const double* F, const uint8_t* node_fixed, double step, int64_t n, cudaStream_t s);
+// *out = sum over entries with lambda_new * rate != 0 of (lambda_new * rate - u)^2 (two launches)
+void launch_idbc_delta_sq(const double* u, const double* rate, double lambda_new, int64_t n, double* partials,
+                          double* out, cudaStream_t s);
+void launch_mul64(double* y, const double* x, const double* m, int64_t n, cudaStream_t s);  // y = x * m
 void launch_dot(const double* x, const double* y, int64_t n, double* partials, double* out, cudaStream_t s);
 
 // solver.cu -- block-Jacobi preconditioned CG

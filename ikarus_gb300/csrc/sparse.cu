@@ -202,6 +202,31 @@ __global__ void idbc_force_kernel(double* __restrict__ R, const double* __restri
     if (!((node_fixed[i / 3] >> (i % 3)) & 1)) R[i] += step * F[i];
 }
 
+// ||sync(u, lambda_new) - u||^2: the squared change of the solution when the inhomogeneous Dirichlet values are
+// re-imposed at the load factor lambda_new (entries whose prescribed value is nonzero take it)
+__global__ void idbc_delta_sq_partial_kernel(const double* __restrict__ u, const double* __restrict__ rate,
+                                             double lambda_new, int64_t n, double* part) {
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = lambda_new * rate[i];
+    if (v != 0.0) s += (v - u[i]) * (v - u[i]);
+  }
+  s = warp_sum(s);
+  __shared__ double ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) part[blockIdx.x] = v;
+  }
+}
+__global__ void mul_kernel(double* __restrict__ y, const double* __restrict__ x, const double* __restrict__ m,
+                           int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = x[i] * m[i];
+}
+
 // deterministic sum of squares: fixed grid, per-block partials, then one block sums them in order
 __global__ void sumsq_partial_kernel(const double* __restrict__ x, int64_t n, double* part) {
   double s = 0.0;
@@ -301,6 +326,14 @@ void launch_idbc_sync(double* u, const double* rate, double lambda, int64_t n, c
 }
 void launch_idbc_force(double* R, const double* F, const uint8_t* node_fixed, double step, int64_t n, cudaStream_t s) {
   idbc_force_kernel<<<kNormGrid, 256, 0, s>>>(R, F, node_fixed, step, n);
+}
+void launch_idbc_delta_sq(const double* u, const double* rate, double lambda_new, int64_t n, double* partials,
+                          double* out, cudaStream_t s) {
+  idbc_delta_sq_partial_kernel<<<kNormGrid, 256, 0, s>>>(u, rate, lambda_new, n, partials);
+  sum_partials_kernel<<<1, 256, 0, s>>>(partials, kNormGrid, out, false);
+}
+void launch_mul64(double* y, const double* x, const double* m, int64_t n, cudaStream_t s) {
+  mul_kernel<<<kNormGrid, 256, 0, s>>>(y, x, m, n);
 }
 void launch_norm2(const double* x, int64_t n, double* partials, double* out, cudaStream_t s) {
   sumsq_partial_kernel<<<kNormGrid, 256, 0, s>>>(x, n, partials);

@@ -297,6 +297,36 @@ int ikr_load_control_subscribe(ikr_lc lc, ikr_control_observer cb, void* user);
 int ikr_load_control_run(ikr_lc lc, ikr_req req, ikr_control_info* info, ikr_nr_info* solver_infos,
                          int32_t capacity);
 
+/* ---- PathFollowing (pathfollowing.hh:148-236, pathfollowing.inl:25-73) with NewtonRaphsonWithSubsidiaryFunction
+ * (newtonraphsonwithscalarsubsidiaryfunction.hh:128-316) ---------------------------------------------------------
+ * Each Newton iteration solves K dR = -R and K dL = Fext0 - F_idbc with the Newton object's linear solver and takes
+ * dlambda = (-f - dfdDD.dR) / (dfdDD.dL + dfdDlambda), dD = dR + dlambda dL (Fext0 = -R(u = 0, lambda = 1)). */
+typedef struct ikr_pf_s* ikr_pf;
+enum { IKR_PF_ARC_LENGTH = 0,              /* ArcLength (pathfollowingfunctions.hh:88-203) */
+       IKR_PF_LOAD_CONTROL = 1,            /* LoadControlSubsidiaryFunction (:217-281) */
+       IKR_PF_DISPLACEMENT_CONTROL = 2 };  /* DisplacementControl (:295-368) */
+/* PathFollowing(nr, steps, stepSize, pathFollowingType): the Newton object supplies the assembler (Full Dirichlet
+ * handling), the linear solver and NewtonRaphsonWithSubsidiaryFunctionSettings{tol, maxIter} plus this library's
+ * linear-tolerance additions.  controlled: DisplacementControl's dof indices (free, not repeated).  steps <= 0:
+ * IKR_ERR_INVALID_STATE.  Also subscribes the elements' state update (EAS) to the solver. */
+int ikr_path_following_create(ikr_pf* out, ikr_nr nr, int32_t steps, double step_size, int32_t kind,
+                              int32_t n_controlled, const int32_t* controlled);
+int ikr_path_following_destroy(ikr_pf pf);
+/* kind 0: AdaptiveStepSizing::NoOp (default); 1: IterationBased with target_iterations (adaptivestepsizing.hh:36-57;
+ * target 0 is IKR_ERR_INVALID_STATE as in setTargetIterations) */
+int ikr_path_following_set_adaptive_step_sizing(ikr_pf pf, int32_t kind, int32_t target_iterations);
+int ikr_path_following_subscribe(ikr_pf pf, ikr_control_observer cb, void* user);
+/* run(req): per-solve NonLinearSolverInformation, steps + 1 entries (the solve at load step -1 first).  Load-control
+ * and displacement-control subsidiary functions with inhomogeneous Dirichlet values: IKR_ERR_NOT_IMPLEMENTED (the
+ * reference rejects them at compile time, pathfollowingfunctions.hh:22-26). */
+int ikr_path_following_run(ikr_pf pf, ikr_req req, ikr_control_info* info, ikr_nr_info* solver_infos,
+                           int32_t capacity);
+/* SubsidiaryArgs of the current state (pathfollowingfunctions.hh:30-41): out[0] stepSize, [1] Dlambda, [2] f,
+ * [3] dfdDlambda, [4] the arc length's psi, [5] currentStep */
+int ikr_path_following_subsidiary_args(ikr_pf pf, double* out6);
+/* SubsidiaryArgs::DD, the solution increment of the current step (n doubles, host memory) */
+int ikr_path_following_increment(ikr_pf pf, double* dd);
+
 /* ---- Newton predictor of LoadControl (no counterpart in the reference, whose predictor only increments
  * the load factor, loadcontrol.inl:54-57) -------------------------------------------------------------------
  * kind 0: none (the reference's behaviour); 1: previous converged increment; 2: learned (predictor object).

@@ -70,7 +70,7 @@ def lib():
                                          C.c_int, C.c_double, dp, dp, ip, dp, dp, dp, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]
         L.orc_path_following_toy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, dp,
-                                             dp, ip, dp, C.POINTER(C.c_int)]
+                                             dp, ip, dp, dp, C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -108,12 +108,14 @@ def path_following_toy(kind=PF_ARC_LENGTH, idbc=False, steps=5, step_size=0.1, t
     lam = np.zeros(1)
     its = np.zeros(steps + 1, dtype=np.int32)
     lams = np.zeros(steps + 1)
+    ds = np.zeros((steps + 1, 2))
     ns = C.c_int(0)
     code = lib().orc_path_following_toy(kind, int(idbc), steps, step_size, target_iterations, tol, max_iter,
                                         _p(d, C.c_double), _p(lam, C.c_double), _p(its, C.c_int32),
-                                        _p(lams, C.c_double), C.byref(ns))
+                                        _p(lams, C.c_double), _p(ds, C.c_double), C.byref(ns))
     _check(code, "path_following_toy")
-    return dict(d=d, lam=float(lam[0]), iterations=its[: ns.value].tolist(), lambdas=lams[: ns.value])
+    return dict(d=d, lam=float(lam[0]), iterations=its[: ns.value].tolist(), lambdas=lams[: ns.value],
+                d_steps=ds[: ns.value])
 
 
 def from_problem(p, faithful=False):

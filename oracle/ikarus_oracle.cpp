@@ -1357,7 +1357,7 @@ void pf_intermediate_prediction(const PFOps& o, PFType& t, Vec& x, double& lam, 
 // PathFollowing::run (pathfollowing.inl:25-73); infos receive steps + 1 entries (load step -1 first)
 int pf_run(const PFOps& o, PFType& t, int steps, double step_size, int target_iterations, double tol, int max_iter,
            Vec& x, double& lam, int32_t* iterations, double* res_norms, double* lambdas, double* psi_out,
-           int* n_solves, int* total) {
+           int* n_solves, int* total, double* x_steps = nullptr) {
   PFArgs a;
   a.DD.assign(o.nr, 0.0);
   a.dfdDD.assign(o.nr, 0.0);
@@ -1368,6 +1368,7 @@ int pf_run(const PFOps& o, PFType& t, int steps, double step_size, int target_it
     if (iterations) iterations[solves] = info.iterations;
     if (res_norms) res_norms[solves] = info.residual_norm;
     if (lambdas) lambdas[solves] = lam;
+    if (x_steps) std::copy(x.begin(), x.end(), x_steps + (size_t)solves * o.nx);
     tot += info.iterations;
     ++solves;
     if (n_solves) *n_solves = solves;
@@ -1471,7 +1472,7 @@ int orc_path_following(orc_problem* p, int kind, int steps, double step_size, in
 
 int orc_path_following_toy(int kind, int idbc, int steps, double step_size, int target_iterations, double tol,
                            int max_iter, double* d2, double* lambda, int32_t* iterations, double* lambdas,
-                           int* n_solves) {
+                           double* d_steps, int* n_solves) {
   if (!d2 || !lambda || steps <= 0 || kind < 0 || kind > 2) return ORC_ERR_ARG;
   if (idbc && kind != ORC_PF_ARC_LENGTH) return ORC_ERR_NOT_IMPLEMENTED;
   PFType t;
@@ -1531,7 +1532,7 @@ int orc_path_following_toy(int kind, int idbc, int steps, double step_size, int 
   Vec x(d2, d2 + 2);
   double lam = *lambda;
   const int st = pf_run(o, t, steps, step_size, target_iterations, tol, max_iter, x, lam, iterations, nullptr,
-                        lambdas, nullptr, n_solves, nullptr);
+                        lambdas, nullptr, n_solves, nullptr, d_steps);
   d2[0] = x[0];
   d2[1] = x[1];
   *lambda = lam;

@@ -107,10 +107,11 @@ int orc_path_following(orc_problem* p, int kind, int steps, double step_size, in
                        double cg_rtol, double* u, double* lambda, int32_t* iterations, double* res_norms,
                        double* lambdas, double* psi, int* n_solves, int* total_iterations);
 /* The same routine on the two-dof operator of tests/src/testpathfollowing.cpp:26-40 (idbc = 1: only w is free and
- * u = 0.1 lambda is prescribed, :80-94); pins the routine against that test's golden values. */
+ * u = 0.1 lambda is prescribed, :80-94); pins the routine against that test's golden values.  d_steps: (u, w)
+ * after each of the steps + 1 solves. */
 int orc_path_following_toy(int kind, int idbc, int steps, double step_size, int target_iterations, double tol,
                            int max_iter, double* d2, double* lambda, int32_t* iterations, double* lambdas,
-                           int* n_solves);
+                           double* d_steps, int* n_solves);
 
 #ifdef __cplusplus
 }

@@ -9,6 +9,10 @@ Sources:
   tests/src/testcantileverbeamEAS.cpp:101     material parameters (E = 100, nu = 0.3)
   tests/src/testcantileverbeam.hh:42-53, 96-151  mesh 10x1x1 on (L, h, h) = (10, 2, 2), tol 1e-10, 20 steps
   tests/src/testcommon.hh:199-207             fixed corner distortion of the single-element tests
+  tests/src/testpathfollowing.cpp:41-370      two-dof operator under PathFollowing (ArcLength, LoadControl
+                                               subsidiary function, DisplacementControl, ArcLength with
+                                               inhomogeneous Dirichlet values): iterations per solve, final
+                                               (u, w) (per step for the load control), final lambda
 """
 import json
 import os
@@ -32,6 +36,19 @@ def main():
     blk = common[common.index("if constexpr (gridDim == 3)", common.index("fixedDistorted")):]
     blk = blk[: blk.index("} else")]
     offsets = [[float(x) for x in m] for m in re.findall(r"push_back\(\{([-0-9.]+), ([-0-9.]+), ([-0-9.]+)\}\)", blk)]
+    pf_src = open(os.path.join(REF, "tests/src/testpathfollowing.cpp")).read()
+    pf = {}
+    for name in ("simple2DOperatorArcLengthTest", "simple2DOperatorArcLengthTestWithIDBC",
+                 "simple2DOperatorLoadControlTestPF", "simple2DOperatorDisplacementControlTest"):
+        body = pf_src[pf_src.index("static auto " + name + "("):]
+        body = body[: body.index("return t;")]
+        its = [int(x) for x in re.search(r"expectedIterations = \{([^}]*)\}", body).group(1).split(",")]
+        disp = [float(x) for x in re.search(r"expectedDisplacement <<([^;]*);", body).group(1).split(",")]
+        lam = float(re.search(r"expectedLambda = ([0-9.e+-]+);", body).group(1))
+        pf[name] = {"iterations": its, "displacement": disp, "lambda": lam}
+    main_src = pf_src[pf_src.index("int main"):]
+    step = float(re.search(r"stepSize = ([0-9.e+-]+);", main_src).group(1))
+    steps = int(re.search(r"loadSteps\s*= (\d+);", main_src).group(1))
     data = {
         "source": "ikarus-project/ikarus tests/src/testcantileverbeamEAS.cpp:60-96, testcantileverbeam.hh:42-198, "
                   "testcommon.hh:199-207",
@@ -41,6 +58,8 @@ def main():
                                              "DisplacementGradientTransposed": 9},
                           "results": goldens},
         "fixed_distortion_3d": offsets,
+        "path_following_2dof": {"source": "tests/src/testpathfollowing.cpp", "step_size": step, "load_steps": steps,
+                                "tol": 1e-8, "max_iter": 20, "cases": pf},
     }
     with open(OUT, "w") as f:
         json.dump(data, f, indent=1)

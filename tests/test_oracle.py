@@ -213,3 +213,73 @@ def test_svk_tangent_and_residual_are_consistent(eas, n):
         Rfd = np.array([(o.element_energy(0, u + h * np.eye(24)[j]) - o.element_energy(0, u - h * np.eye(24)[j]))
                         / (2 * h) for j in range(24)])
         assert np.abs(R - Rfd).max() <= 1e-6 * np.abs(R).max()
+
+
+# ---- path following (pathfollowing.inl, newtonraphsonwithscalarsubsidiaryfunction.hh) -------------------------
+PF_CASES = {"simple2DOperatorArcLengthTest": (oracle.PF_ARC_LENGTH, False),
+            "simple2DOperatorArcLengthTestWithIDBC": (oracle.PF_ARC_LENGTH, True),
+            "simple2DOperatorLoadControlTestPF": (oracle.PF_LOAD_CONTROL, False),
+            "simple2DOperatorDisplacementControlTest": (oracle.PF_DISPLACEMENT_CONTROL, False)}
+
+
+@pytest.mark.parametrize("case", sorted(PF_CASES))
+def test_path_following_two_dof_goldens(case):
+    """The oracle's path-following routine on the reference's two-dof operator reproduces testpathfollowing.cpp:
+    Newton iterations of every solve, final (u, w) (every step's for the load control) and final lambda, within the
+    test's FloatCmp tolerance scaled to 1e-12."""
+    g = GOLD["path_following_2dof"]
+    want = g["cases"][case]
+    kind, idbc = PF_CASES[case]
+    r = oracle.path_following_toy(kind, idbc, steps=g["load_steps"], step_size=g["step_size"], tol=g["tol"],
+                                  max_iter=g["max_iter"])
+    assert r["iterations"] == want["iterations"]
+    if len(want["displacement"]) == 2:
+        np.testing.assert_allclose(r["d"], want["displacement"], rtol=1e-12, atol=0)
+    else:
+        per_step = np.asarray(want["displacement"]).reshape(2, -1)
+        np.testing.assert_allclose(r["d_steps"].T, per_step, rtol=1e-12, atol=1e-15)
+    assert abs(r["lam"] - want["lambda"]) <= 1e-12 * abs(want["lambda"])
+
+
+def test_path_following_iteration_based_step_sizing():
+    """AdaptiveStepSizing::IterationBased (adaptivestepsizing.hh:36-47): with a target of one iteration the step
+    size shrinks by sqrt(1 / iterations) after every step that took more, so the path advances less."""
+    g = GOLD["path_following_2dof"]
+    noop = oracle.path_following_toy(oracle.PF_ARC_LENGTH, steps=5, step_size=0.1)
+    ad = oracle.path_following_toy(oracle.PF_ARC_LENGTH, steps=5, step_size=0.1, target_iterations=1)
+    assert noop["iterations"] == g["cases"]["simple2DOperatorArcLengthTest"]["iterations"]
+    assert ad["lam"] < noop["lam"]
+    assert np.all(np.diff(ad["lambdas"][1:]) < np.diff(noop["lambdas"][1:]) + 1e-15)
+
+
+def test_oracle_path_following_load_control_matches_load_control():
+    """The load-control subsidiary function walks lambda = s, 2s, ... like LoadControl over [0, N s]: both reach the
+    same equilibria (tolerance-level differences only)."""
+    p = problems.cantilever(4, 2, 2, load_steps=4, traction=(0.0, 0.0, -5.0))
+    o = oracle.from_problem(p)
+    lc = o.load_control(4, 0.0, 1.0, tol=1e-11)
+    pf = oracle.from_problem(p).path_following(4, 0.25, kind=oracle.PF_LOAD_CONTROL, tol=1e-11)
+    assert pf["success"] and lc["success"]
+    np.testing.assert_allclose(pf["lambdas"], [0.0, 0.25, 0.5, 0.75, 1.0], atol=1e-14)
+    np.testing.assert_allclose(pf["u"], lc["u"], rtol=0, atol=1e-9 * np.abs(lc["u"]).max())
+
+
+def test_oracle_arc_length_constraint_and_equilibrium():
+    """Every converged arc-length step is an equilibrium and lies on the sphere ||DD||^2 + psi^2 Dlambda^2 = s^2
+    around the previous one (pathfollowingfunctions.hh:102-115)."""
+    p = problems.cantilever(4, 2, 2, load_steps=4, traction=(0.0, 0.0, -5.0))
+    s = 0.5
+    us, lams = [], []
+    for steps in (1, 2, 3):
+        r = oracle.from_problem(p).path_following(steps, s, tol=1e-11)
+        assert r["success"]
+        us.append(r["u"])
+        lams.append(r["lam"])
+        o = oracle.from_problem(p)
+        R = o.assemble_vector(r["u"], r["lam"])
+        assert np.linalg.norm(R) <= 1e-11
+    psi = oracle.from_problem(p).path_following(3, s, tol=1e-11)["psi"]
+    for k in (1, 2):
+        dd = us[k] - us[k - 1]
+        dl = lams[k] - lams[k - 1]
+        assert abs(np.sqrt(dd @ dd + psi * psi * dl * dl) - s) <= 1e-10
