@@ -7,6 +7,9 @@
 //   LinearSolver              ~ LinearSolver(SolverTypeTag)                    (linearsolver.hh:49-233)
 //   NewtonRaphson             ~ NewtonRaphson with NRSettings / observers      (newtonraphson.hh:27-303)
 //   LoadControl               ~ LoadControl via ControlRoutineFactory::create  (loadcontrol.hh:29-113)
+//   PathFollowing             ~ PathFollowing with NewtonRaphsonWithSubsidiaryFunction, ArcLength /
+//                               LoadControlSubsidiaryFunction / DisplacementControl, AdaptiveStepSizing
+//                               (pathfollowing.hh:148-236, pathfollowingfunctions.hh, adaptivestepsizing.hh)
 // Errors are thrown where the reference throws (NotImplemented, InvalidStateException) and as
 // Ikarus::GB300::Error otherwise; det C <= 0 throws NonPositiveDetC instead of aborting.
 #pragma once
@@ -309,6 +312,82 @@ class LoadControl {
     (*static_cast<Observer*>(u))(static_cast<ControlMessages>(m), *s);
   }
   ikr_lc h_ = nullptr;
+  int steps_;
+  std::vector<std::unique_ptr<Observer>> observers_;
+};
+
+// Subsidiary functions of PathFollowing (pathfollowingfunctions.hh:88-368)
+struct ArcLength {
+  static constexpr int32_t kind = IKR_PF_ARC_LENGTH;
+  std::vector<int32_t> controlledIndices{};
+};
+struct LoadControlSubsidiaryFunction {
+  static constexpr int32_t kind = IKR_PF_LOAD_CONTROL;
+  std::vector<int32_t> controlledIndices{};
+};
+struct DisplacementControl {
+  static constexpr int32_t kind = IKR_PF_DISPLACEMENT_CONTROL;
+  explicit DisplacementControl(std::vector<int32_t> idx) : controlledIndices(std::move(idx)) {}
+  std::vector<int32_t> controlledIndices;
+};
+// AdaptiveStepSizing (adaptivestepsizing.hh:14-57)
+namespace AdaptiveStepSizing {
+struct NoOp {
+  static constexpr int32_t kind = 0;
+  int targetIterations() const { return 0; }
+};
+struct IterationBased {
+  static constexpr int32_t kind = 1;
+  int targetIterations() const { return target_; }
+  void setTargetIterations(int t) {
+    if (t == 0) throw InvalidStateException(IKR_ERR_INVALID_STATE, "TargetIterations should not be equal to 0.");
+    target_ = t;
+  }
+
+ private:
+  int target_ = 0;
+};
+}  // namespace AdaptiveStepSizing
+
+// PathFollowing(nr, steps, stepSize, pathFollowingType, adaptiveStepSizing) (pathfollowing.hh:185-194) with
+// NewtonRaphsonWithSubsidiaryFunction; the NewtonRaphson object supplies assembler, linear solver and tolerances
+class PathFollowing {
+ public:
+  using Observer = std::function<void(ControlMessages, const ikr_control_state&)>;
+  template <typename PF = ArcLength, typename ASS = AdaptiveStepSizing::NoOp>
+  PathFollowing(NewtonRaphson& nr, int steps, double stepSize, const PF& pft = {}, const ASS& ass = {})
+      : steps_(steps) {
+    check(ikr_path_following_create(&h_, nr.handle(), steps, stepSize, PF::kind,
+                                    (int32_t)pft.controlledIndices.size(),
+                                    pft.controlledIndices.empty() ? nullptr : pft.controlledIndices.data()),
+          "PathFollowing");
+    if (ASS::kind == 1) check(ikr_path_following_set_adaptive_step_sizing(h_, 1, ass.targetIterations()), "steps");
+  }
+  ~PathFollowing() { ikr_path_following_destroy(h_); }
+  PathFollowing(const PathFollowing&) = delete;
+  PathFollowing& operator=(const PathFollowing&) = delete;
+  void subscribe(Observer f) {
+    observers_.push_back(std::make_unique<Observer>(std::move(f)));
+    check(ikr_path_following_subscribe(h_, &PathFollowing::tramp, observers_.back().get()), "subscribe");
+  }
+  [[nodiscard]] ControlInformation run(FERequirements& req) {
+    std::vector<ikr_nr_info> infos(steps_ + 1);
+    ikr_control_info ci{};
+    check(ikr_path_following_run(h_, req.handle(), &ci, infos.data(), (int32_t)infos.size()), "PathFollowing::run");
+    ControlInformation out;
+    out.success = ci.success != 0;
+    out.totalIterations = ci.total_iterations;
+    for (int i = 0; i < ci.n_solver_infos && i < (int)infos.size(); ++i)
+      out.solverInfos.push_back({infos[i].success != 0, infos[i].residual_norm, infos[i].correction_norm,
+                                 infos[i].iterations, infos[i].linear_iterations});
+    return out;
+  }
+
+ private:
+  static void tramp(int32_t m, const ikr_control_state* s, void* u) {
+    (*static_cast<Observer*>(u))(static_cast<ControlMessages>(m), *s);
+  }
+  ikr_pf h_ = nullptr;
   int steps_;
   std::vector<std::unique_ptr<Observer>> observers_;
 };
