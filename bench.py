@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--eas-size", default="64,64,16", help="config 5: elements per direction")
     ap.add_argument("--eas-steps", type=int, default=25, help="config 5: load steps")
     ap.add_argument("--eas-predictor", type=int, default=1, help="config 5: 0 none, 1 previous increment")
+    ap.add_argument("--path-following", type=int, default=0,
+                    help="arc-length path of this many steps on the 128x32x32 cantilever instead of the load control")
+    ap.add_argument("--no-multi-rhs", action="store_true",
+                    help="--path-following: solve the two bordered columns one after the other")
     ap.add_argument("--spmv-kinds", default="-1", help="--spmv-only: comma-separated kind[:keep] SpMV choices")
     ap.add_argument("--spmv-precision", type=int, default=1, help="--spmv-only: 1 FP32 tangent, 0 FP64")
     ap.add_argument("--spmv-only", type=int, default=0,
@@ -657,6 +661,81 @@ def run_eas(args):
     print(json.dumps(out))
 
 
+def run_path_following(args):
+    """Arc-length path following (PathFollowing + NewtonRaphsonWithSubsidiaryFunction) on the 128x32x32 cantilever:
+    `steps` arc-length steps sized so that the first step takes Dlambda = 1 / steps (s = sqrt(2) psi / steps with
+    psi = ||K^-1 Fext|| from a one-step calibration run of the plain form), every solve to
+    sqrt(||R||^2 + f^2) <= 1e-8 x its initial value.  Each Newton iteration is two CG solves with the same tangent
+    (K dR = -R, K dL = Fext0).  Plain FP64 form against the mixed form; the CPU figure is the oracle port's
+    per-element / per-nonzero costs scaled to the plain run's Newton and CG counts."""
+    import numpy as np
+    import torch
+
+    import ikarus_gb300 as ikr
+    from ikarus_gb300 import problems
+
+    steps = args.path_following
+    p = problems.config2(load_steps=steps)
+    out = {"metric": f"time per arc-length path ({steps} steps, sqrt(||R||^2+f^2) <= 1e-8 x initial, every step)",
+           "unit": "s", "higher_is_better": False,
+           "config": {"workload": "cantilever_128x32x32_jittered", "elements": p.mesh.n_elems, "dofs": p.n_dofs,
+                      "path_following": "ArcLength, AdaptiveStepSizing::NoOp", "steps": steps,
+                      "bordered_solve": "two CG columns one after the other" if args.no_multi_rhs else
+                                        "two CG columns in one persistent launch (one matrix stream per iteration)",
+                      "material": "NeoHooke E=1000 nu=0.3", "l2": "256 MB buffer written before each timed path"}}
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    s_hat = None
+    finals = {}
+    for mixed in (False, True):
+        fes, asm = problems.build_gpu(p, precision=1 if mixed else 0)
+        ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
+        ls.set_multi_rhs(not args.no_multi_rhs)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(solver_settings(ikr, mixed, (args.eta_max, args.eta_min)),
+                                                            ls))
+        req = ikr.FERequirements(fes)
+        stream, ev0, ev1 = make_events(torch, fes.stream())
+        if s_hat is None:  # calibration: psi = ||DD0|| of the initial prediction (plain form)
+            cal = ikr.PathFollowing(nr, 1, 1.0, ikr.ArcLength())
+            assert cal.run(req).success
+            s_hat = np.sqrt(2.0) * cal.subsidiary_args()["psi"] / steps
+            out["config"]["arc_length"] = s_hat
+            del cal
+        pf = ikr.PathFollowing(nr, steps, s_hat, ikr.ArcLength())
+        times = []
+        for k in range(args.warmup + args.steps):
+            req.insertGlobalSolution(np.zeros(p.n_dofs))
+            req.insertParameter(0.0)
+            flush.zero_()
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            info = pf.run(req)
+            ev1.record(stream)
+            ev1.synchronize()
+            assert info.success, "arc-length path failed"
+            if k >= args.warmup:
+                times.append(ev0.elapsed_time(ev1) / 1e3)
+            log(f"path following {'mixed' if mixed else 'plain'}: {ev0.elapsed_time(ev1) / 1e3:.3f} s, newton "
+                f"{info.totalIterations}, cg {info.totalLinearIterations}, lambda {req.parameter():.6f}")
+        key = "mixed" if mixed else "plain_fp64"
+        out[key] = {"s": round(sum(times) / len(times), 4), "newton_iterations": info.totalIterations,
+                    "cg_iterations": info.totalLinearIterations,
+                    "newton_per_step": [si.iterations for si in info.solverInfos],
+                    "final_lambda": req.parameter(), "psi": pf.subsidiary_args()["psi"],
+                    "spmv_kernel": ls.kernel_info()[:2]}
+        finals[key] = req.globalSolution()
+        del pf, nr, ls, req, asm, fes
+    out["value"] = out["mixed"]["s"]
+    out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 2)
+    out["mixed"]["rel_psi_diff_vs_plain"] = abs(out["mixed"]["psi"] / out["plain_fp64"]["psi"] - 1.0)
+    if not args.no_cpu_baseline:
+        v, parts = cpu_sample(out["plain_fp64"]["newton_iterations"], out["plain_fp64"]["cg_iterations"])
+        out["cpu_baseline"] = {"value": round(v, 2), "unit": "s", "cores": 1, "kind": "port",
+                               "sample": "oracle port, 1 thread: R+K assembly and 500 Jacobi-CG iterations on the "
+                                         "64x16x16 cantilever, scaled to 128x32x32 and to the plain FP64 path's "
+                                         "Newton / CG counts", **{k: round(x, 6) for k, x in parts.items()}}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -702,6 +781,8 @@ def main():
         return
     if args.spmv_only:
         return run_spmv_only(args)
+    if args.path_following:
+        return run_path_following(args)
     if args.config == 3:
         return run_batched(args)
     if args.config == 4:

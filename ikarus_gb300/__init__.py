@@ -193,6 +193,8 @@ SIGNATURES = {
     "ikr_load_control_subscribe": ([_vp, _CTRL_OBS, _vp], C.c_int),
     "ikr_load_control_run": ([_vp, _vp, C.POINTER(_ControlInfo), C.POINTER(_NRInfo), _I], C.c_int),
     "ikr_load_control_set_predictor": ([_vp, _I, _vp, _dp, _I], C.c_int),
+    "ikr_linear_solver_set_multi_rhs": ([_vp, _I], C.c_int),
+    "ikr_linear_solver_solve2": ([_vp, _vp, _dp, _dp, _dp, _dp], C.c_int),
     "ikr_path_following_create": ([C.POINTER(_vp), _vp, _I, _D, _I, _I, _ip], C.c_int),
     "ikr_path_following_destroy": ([_vp], C.c_int),
     "ikr_path_following_set_adaptive_step_sizing": ([_vp, _I, _I], C.c_int),
@@ -609,7 +611,17 @@ class LinearSolver:
         self.factorize(assembler)
 
     def solve(self, assembler: SparseFlatAssembler, b):
-        b = np.ascontiguousarray(b, dtype=np.float64)
+        """x = K^-1 b; b of shape (n,) or (n, 2) (two columns, as the path-following Newton solves them)."""
+        b = np.asarray(b, dtype=np.float64)
+        if b.ndim == 2:
+            if b.shape[1] != 2:
+                raise ValueError("two right-hand-side columns are supported")
+            b0, b1 = np.ascontiguousarray(b[:, 0]), np.ascontiguousarray(b[:, 1])
+            x0, x1 = np.zeros_like(b0), np.zeros_like(b1)
+            _err(lib().ikr_linear_solver_solve2(self.h, assembler.h, _ptr(x0), _ptr(x1), _ptr(b0), _ptr(b1)),
+                 "solve")
+            return np.stack([x0, x1], axis=1)
+        b = np.ascontiguousarray(b)
         x = np.zeros_like(b)
         _err(lib().ikr_linear_solver_solve(self.h, assembler.h, _ptr(x), _ptr(b)), "solve")
         return x
@@ -630,6 +642,11 @@ class LinearSolver:
     def set_kernel(self, spmv_kind=-1, l2_keep_fraction=-1.0):
         """SpMV kernel (0 direct, 1..4 staged, -1 autotune) and L2 keep fraction (-1 autotune)."""
         _err(lib().ikr_linear_solver_set_kernel(self.h, int(spmv_kind), float(l2_keep_fraction)))
+
+    def set_multi_rhs(self, on=True):
+        """Two right-hand sides with one tangent (path following): one persistent launch streaming the matrix once
+        per iteration for both (default), or one solve after the other."""
+        _err(lib().ikr_linear_solver_set_multi_rhs(self.h, int(bool(on))))
 
     def kernel_info(self):
         """(spmv kind, L2 keep fraction, tuned SpMV microseconds per launch)."""

@@ -102,23 +102,37 @@ struct CyclicPos {
   int j, g, gend;
 };
 
-template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB>
+// the right-hand sides one launch solves together: per RHS its solution, residual, preconditioned residual, the
+// two search-direction buffers (alternating by iteration parity) and its scalar block
+template <typename T, int NR>
+struct RhsSet {
+  T* x[NR];
+  const T* r[NR];
+  T* z[NR];
+  T* p0[NR];
+  T* p1[NR];
+  double* scal[NR];
+};
+
+// NR right-hand sides with the same matrix: every chunk of the matrix stream is staged once and multiplied
+// against each unfinished RHS, so two solves cost one matrix stream per iteration instead of two.  Each RHS
+// keeps its own CG scalars, iteration count and stop decision; the grid reductions carry the NR values together.
+template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB, int NR>
 __global__ void __launch_bounds__(WARPS * 32, MINB)
-    pcg_persistent_kernel(Bsr A, const T* __restrict__ val, const T* __restrict__ minv, T* __restrict__ xg,
-                          const T* __restrict__ rg, T* __restrict__ zg, T* __restrict__ p0, T* __restrict__ p1,
-                          double* part_a, double* part_b, double* scal, int64_t keep_g) {
+    pcg_persistent_kernel(Bsr A, const T* __restrict__ val, const T* __restrict__ minv, RhsSet<T, NR> V,
+                          double* part_a, double* part_b, int64_t keep_g) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[WARPS][NST];
-  __shared__ double sw[WARPS * 2];
-  __shared__ double sv[2];
+  __shared__ double sw[WARPS * 2 * NR];
+  __shared__ double sv[2 * NR];
   __shared__ bool ok_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G = gridDim.x;
   const int nw = G * WARPS;
   const int gw = blockIdx.x * WARPS + warp;
   const int n_slices = A.n_slices;
-  unsigned int* bar_count = &tickets(scal)[3];
+  unsigned int* bar_count = &tickets(V.scal[0])[3];
   unsigned char* wbase = smem + (size_t)warp * NST * C::kStageBytes;
 
   // owned slices and their block ranges
@@ -134,26 +148,34 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       ns = j + 1;
     }
   }
-  // CG state of the owned rows
-  T xr[MAXS][3], rr_[MAXS][3], zr[MAXS][3], pr[MAXS][3], qr[MAXS][3];
+  // CG state of the owned rows, per RHS
+  T xr[NR][MAXS][3], rr_[NR][MAXS][3], zr[NR][MAXS][3], pr[NR][MAXS][3], qr[NR][MAXS][3];
+  double rz[NR], tol2[NR], rrs[NR], done[NR], beta[NR];
+  int maxit[NR], it[NR];
+  bool all_done = true;
 #pragma unroll
-  for (int j = 0; j < MAXS; ++j) {
-    const int row = 32 * (gw + j * nw) + lane;
-    const bool own = j < ns && row < A.n_rows;
-    V3<T> r0 = {T(0), T(0), T(0)}, z0 = {T(0), T(0), T(0)};
-    if (own) r0 = load3rw(rg, row), z0 = load3rw(zg, row);
-    xr[j][0] = xr[j][1] = xr[j][2] = T(0);
-    pr[j][0] = pr[j][1] = pr[j][2] = T(0);
-    qr[j][0] = qr[j][1] = qr[j][2] = T(0);
-    rr_[j][0] = r0.x, rr_[j][1] = r0.y, rr_[j][2] = r0.z;
-    zr[j][0] = z0.x, zr[j][1] = z0.y, zr[j][2] = z0.z;
+  for (int q = 0; q < NR; ++q) {
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) {
+      const int row = 32 * (gw + j * nw) + lane;
+      const bool own = j < ns && row < A.n_rows;
+      V3<T> r0 = {T(0), T(0), T(0)}, z0 = {T(0), T(0), T(0)};
+      if (own) r0 = load3rw(V.r[q], row), z0 = load3rw(V.z[q], row);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) xr[q][j][c] = pr[q][j][c] = qr[q][j][c] = T(0);
+      rr_[q][j][0] = r0.x, rr_[q][j][1] = r0.y, rr_[q][j][2] = r0.z;
+      zr[q][j][0] = z0.x, zr[q][j][1] = z0.y, zr[q][j][2] = z0.z;
+    }
+    const double* sc = V.scal[q];
+    rz[q] = sc[kRz];
+    tol2[q] = sc[kTol2];
+    maxit[q] = (int)sc[kMaxIt];
+    rrs[q] = sc[kRR];
+    done[q] = sc[kDone];
+    it[q] = (int)sc[kIters];
+    beta[q] = 0.0;
+    all_done = all_done && done[q] != 0.0;
   }
-  double rz = scal[kRz];
-  const double tol2 = scal[kTol2];
-  const int maxit = (int)scal[kMaxIt];
-  double rrs = scal[kRR];
-  double done = scal[kDone];
-  double beta = 0.0;
 
   if (lane == 0) {
     for (int st = 0; st < NST; ++st) mbar_init(smem_addr(&bars[warp][st]), 1);
@@ -186,7 +208,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
 
   CyclicPos P{0, s_first[0], s_end[0]};
   int inflight = 0;
-  if (ns > 0 && done == 0.0) {
+  if (ns > 0 && !all_done) {
     for (int st = 0; st < NST; ++st) {
       issue(st, P);
       ++inflight;
@@ -196,19 +218,30 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   uint32_t phase = 0;
   int st = 0;
   bool failed = false;
-  int it = (int)scal[kIters];
   unsigned int barrier_no = 0;
+  int loop = 0;  // parity of the partial buffers
 
-  while (done == 0.0) {
-    const T tb = T(beta);
-    const T* pold = (it & 1) ? p0 : p1;
-    T* pnew = (it & 1) ? p1 : p0;
-    double pq = 0.0;
-    // ---- product phase: q = K p_new over the owned slices
+  while (!all_done) {
+    T tb[NR];
+    const T* pold[NR];
+    T* pnew[NR];
+    bool act[NR];
+    double pq[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      act[q] = done[q] == 0.0;
+      tb[q] = T(beta[q]);
+      pold[q] = (it[q] & 1) ? V.p0[q] : V.p1[q];
+      pnew[q] = (it[q] & 1) ? V.p1[q] : V.p0[q];
+      pq[q] = 0.0;
+    }
+    // ---- product phase: q = K p_new over the owned slices, every active RHS from the same staged chunk
 #pragma unroll
     for (int j = 0; j < MAXS; ++j) {
       if (j < ns && !failed) {
-        T a0 = T(0), a1 = T(0), a2 = T(0);
+        T acc[NR][3];
+#pragma unroll
+        for (int q = 0; q < NR; ++q) acc[q][0] = acc[q][1] = acc[q][2] = T(0);
         for (int g = s_first[j]; g < s_end[j]; g += CB) {
           const bool okw = __all_sync(0xffffffffu, mbar_wait_bounded(smem_addr(&bars[warp][st]), (phase >> st) & 1u));
           if (!okw) {
@@ -217,24 +250,31 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
           }
           phase ^= 1u << st;
           --inflight;
-          const T* sv = reinterpret_cast<const T*>(wbase + (size_t)st * C::kStageBytes);
-          const int32_t* sc = reinterpret_cast<const int32_t*>(wbase + (size_t)st * C::kStageBytes + C::kValBytes);
+          const T* sval = reinterpret_cast<const T*>(wbase + (size_t)st * C::kStageBytes);
+          const int32_t* scol = reinterpret_cast<const int32_t*>(wbase + (size_t)st * C::kStageBytes + C::kValBytes);
           const int nb = min(CB, s_end[j] - g);
-          V3<T> zc[CB], pc[CB];
+          int cols[CB];
 #pragma unroll
-          for (int k = 0; k < CB; ++k) {
-            const int c = k < nb ? sc[32 * k + lane] : 0;
-            zc[k] = load3rw(zg, c);
-            pc[k] = load3rw(pold, c);
-          }
+          for (int k = 0; k < CB; ++k) cols[k] = k < nb ? scol[32 * k + lane] : 0;
 #pragma unroll
-          for (int k = 0; k < CB; ++k) {
-            if (k < nb) {
-              const T x0 = zc[k].x + tb * pc[k].x, x1 = zc[k].y + tb * pc[k].y, x2 = zc[k].z + tb * pc[k].z;
-              const T* v = sv + 288 * k + lane;
-              a0 += v[0] * x0 + v[32] * x1 + v[64] * x2;
-              a1 += v[96] * x0 + v[128] * x1 + v[160] * x2;
-              a2 += v[192] * x0 + v[224] * x1 + v[256] * x2;
+          for (int q = 0; q < NR; ++q) {
+            if (!act[q]) continue;
+            V3<T> zc[CB], pc[CB];
+#pragma unroll
+            for (int k = 0; k < CB; ++k) {
+              zc[k] = load3rw(V.z[q], cols[k]);
+              pc[k] = load3rw(pold[q], cols[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < CB; ++k) {
+              if (k < nb) {
+                const T x0 = zc[k].x + tb[q] * pc[k].x, x1 = zc[k].y + tb[q] * pc[k].y,
+                        x2 = zc[k].z + tb[q] * pc[k].z;
+                const T* v = sval + 288 * k + lane;
+                acc[q][0] += v[0] * x0 + v[32] * x1 + v[64] * x2;
+                acc[q][1] += v[96] * x0 + v[128] * x1 + v[160] * x2;
+                acc[q][2] += v[192] * x0 + v[224] * x1 + v[256] * x2;
+              }
             }
           }
           __syncwarp();  // the stage is consumed before it is refilled
@@ -244,107 +284,138 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
           st = (st + 1 == NST) ? 0 : st + 1;
         }
         const int row = 32 * (gw + j * nw) + lane;
-        const T n0 = zr[j][0] + tb * pr[j][0], n1 = zr[j][1] + tb * pr[j][1], n2 = zr[j][2] + tb * pr[j][2];
-        pr[j][0] = n0, pr[j][1] = n1, pr[j][2] = n2;
-        qr[j][0] = a0, qr[j][1] = a1, qr[j][2] = a2;
-        if (row < A.n_rows) {
-          store3(pnew, row, n0, n1, n2);
-          pq += double(n0 * a0 + n1 * a1 + n2 * a2);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+          if (!act[q]) continue;
+          const T n0 = zr[q][j][0] + tb[q] * pr[q][j][0], n1 = zr[q][j][1] + tb[q] * pr[q][j][1],
+                  n2 = zr[q][j][2] + tb[q] * pr[q][j][2];
+          pr[q][j][0] = n0, pr[q][j][1] = n1, pr[q][j][2] = n2;
+          qr[q][j][0] = acc[q][0], qr[q][j][1] = acc[q][1], qr[q][j][2] = acc[q][2];
+          if (row < A.n_rows) {
+            store3(pnew[q], row, n0, n1, n2);
+            pq[q] += double(n0 * acc[q][0] + n1 * acc[q][1] + n2 * acc[q][2]);
+          }
         }
       }
     }
-    // ---- grid reduction of p.q
-    const int par = it & 1;
+    // ---- grid reduction of p.q (all RHS together)
+    const int par = loop & 1;
     failed = __syncthreads_or(failed);
     if (failed) break;
-    double red1[1] = {pq};
-    cta_reduce<1>(red1, sw);
+    cta_reduce<NR>(pq, sw);
     ++barrier_no;
-    if (!grid_allreduce<1>(red1, part_a + par * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
+    if (!grid_allreduce<NR>(pq, part_a + par * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
       failed = true;
       break;
     }
-    const double pqs = red1[0];
-    if (!(fabs(pqs) > 0.0) || !isfinite(pqs)) {  // breakdown (negative curvature alone does not stop CG)
-      done = 3.0;
-      break;
-    }
-    const T alpha = T(rz / pqs);
-    // ---- update phase on the owned rows
-    double rzn = 0.0, rrn = 0.0;
+    T alpha[NR];
 #pragma unroll
-    for (int j = 0; j < MAXS; ++j) {
-      const int row = 32 * (gw + j * nw) + lane;
-      if (j < ns && row < A.n_rows) {
-        T r1[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          xr[j][c] += alpha * pr[j][c];
-          r1[c] = rr_[j][c] - alpha * qr[j][c];
-          rr_[j][c] = r1[c];
-        }
-        const T* m = minv + 9 * (int64_t)row;
-        T zv[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          zv[a] = __ldg(m + 3 * a) * r1[0] + __ldg(m + 3 * a + 1) * r1[1] + __ldg(m + 3 * a + 2) * r1[2];
-          zr[j][a] = zv[a];
-        }
-        store3(zg, row, zv[0], zv[1], zv[2]);
-        T trz = T(0), trr = T(0);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          trz += r1[a] * zv[a];
-          trr += r1[a] * r1[a];
-        }
-        rzn += double(trz);
-        rrn += double(trr);
+    for (int q = 0; q < NR; ++q) {
+      alpha[q] = T(0);
+      if (!act[q]) continue;
+      if (!(fabs(pq[q]) > 0.0) || !isfinite(pq[q])) {  // breakdown (negative curvature alone does not stop CG)
+        done[q] = 3.0;
+        act[q] = false;
+        continue;
       }
+      alpha[q] = T(rz[q] / pq[q]);
     }
-    double red2[2] = {rzn, rrn};
-    cta_reduce<2>(red2, sw);
+    // ---- update phase on the owned rows
+    double red2[2 * NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      double rzn = 0.0, rrn = 0.0;
+      if (act[q]) {
+        const T a = alpha[q];
+#pragma unroll
+        for (int j = 0; j < MAXS; ++j) {
+          const int row = 32 * (gw + j * nw) + lane;
+          if (j < ns && row < A.n_rows) {
+            T r1[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              xr[q][j][c] += a * pr[q][j][c];
+              r1[c] = rr_[q][j][c] - a * qr[q][j][c];
+              rr_[q][j][c] = r1[c];
+            }
+            const T* m = minv + 9 * (int64_t)row;
+            T zv[3];
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              zv[b] = __ldg(m + 3 * b) * r1[0] + __ldg(m + 3 * b + 1) * r1[1] + __ldg(m + 3 * b + 2) * r1[2];
+              zr[q][j][b] = zv[b];
+            }
+            store3(V.z[q], row, zv[0], zv[1], zv[2]);
+            T trz = T(0), trr = T(0);
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+              trz += r1[b] * zv[b];
+              trr += r1[b] * r1[b];
+            }
+            rzn += double(trz);
+            rrn += double(trr);
+          }
+        }
+      }
+      red2[2 * q] = rzn;
+      red2[2 * q + 1] = rrn;
+    }
+    cta_reduce<2 * NR>(red2, sw);
     ++barrier_no;
-    if (!grid_allreduce<2>(red2, part_b + par * 2 * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
+    if (!grid_allreduce<2 * NR>(red2, part_b + par * 2 * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
       failed = true;
       break;
     }
-    const double rzs = red2[0];
-    rrs = red2[1];
-    beta = rzs / rz;
-    rz = rzs;
-    ++it;
-    if (rrs <= tol2) done = 1.0;
-    else if (it >= maxit) done = 2.0;
+    all_done = true;
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      if (act[q]) {
+        const double rzs = red2[2 * q];
+        rrs[q] = red2[2 * q + 1];
+        beta[q] = rzs / rz[q];
+        rz[q] = rzs;
+        ++it[q];
+        if (rrs[q] <= tol2[q]) done[q] = 1.0;
+        else if (it[q] >= maxit[q]) done[q] = 2.0;
+      }
+      all_done = all_done && done[q] != 0.0;
+    }
+    ++loop;
   }
-  if (failed) done = kDoneDeviceTimeout;
   // drain the copies still in flight (the cyclic stream runs ahead of the last iteration)
   for (int k = 0; k < inflight; ++k) {
     mbar_wait_bounded(smem_addr(&bars[warp][st]), (phase >> st) & 1u);
     phase ^= 1u << st;
     st = (st + 1 == NST) ? 0 : st + 1;
   }
-  // solution of the owned rows; the final scalars from CTA 0 (identical in every CTA)
+  // solutions of the owned rows; the final scalars from CTA 0 (identical in every CTA)
 #pragma unroll
-  for (int j = 0; j < MAXS; ++j) {
-    const int row = 32 * (gw + j * nw) + lane;
-    if (j < ns && row < A.n_rows) store3(xg, row, xr[j][0], xr[j][1], xr[j][2]);
+  for (int q = 0; q < NR; ++q) {
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) {
+      const int row = 32 * (gw + j * nw) + lane;
+      if (j < ns && row < A.n_rows) store3(V.x[q], row, xr[q][j][0], xr[q][j][1], xr[q][j][2]);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      double* sc = V.scal[q];
+      sc[kIters] = (double)it[q];
+      sc[kRR] = rrs[q];
+      sc[kRz] = rz[q];
+      sc[kBeta] = beta[q];
+      sc[kDone] = failed ? kDoneDeviceTimeout : done[q];
+    }
+    if (failed && threadIdx.x == 0) V.scal[q][kDone] = kDoneDeviceTimeout;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    scal[kIters] = (double)it;
-    scal[kRR] = rrs;
-    scal[kRz] = rz;
-    scal[kBeta] = beta;
-    scal[kDone] = done;
-  }
-  if (failed && threadIdx.x == 0) scal[kDone] = kDoneDeviceTimeout;
 }
 
-template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB>
-cudaError_t launch_persistent(const Bsr& A, PcgWork& w, cudaStream_t s, bool query_only, bool* eligible) {
+template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB, int NR>
+cudaError_t launch_persistent(const Bsr& A, PcgWork* const* ws, double* part_a, double* part_b, cudaStream_t s,
+                              bool query_only, bool* eligible) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
-  auto kern = pcg_persistent_kernel<T, CB, NST, WARPS, MAXS, MINB>;
+  auto kern = pcg_persistent_kernel<T, CB, NST, WARPS, MAXS, MINB, NR>;
   static std::mutex mu;
   static int blocks_per_sm[64] = {0};
+  PcgWork& w = *ws[0];
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 64) dev = 63;
@@ -361,8 +432,8 @@ cudaError_t launch_persistent(const Bsr& A, PcgWork& w, cudaStream_t s, bool que
   }
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
-  // one wave of co-resident CTAs; the partial buffers hold 2 w.grid (part_a) and 4 w.grid (part_b) values,
-  // 2 and 4 per CTA here
+  // one wave of co-resident CTAs; the partial buffers hold 2 NR w.grid (part_a) and 4 NR w.grid (part_b) values,
+  // 2 NR and 4 NR per CTA here
   int grid = bps > 0 ? w.sms * bps : 0;
   if (grid > w.grid) grid = w.grid;
   const int nw = grid * WARPS;
@@ -370,28 +441,34 @@ cudaError_t launch_persistent(const Bsr& A, PcgWork& w, cudaStream_t s, bool que
   if (query_only || !*eligible) return cudaSuccess;
   const T* val = (const T*)A.val;
   const T* minv = (const T*)w.minv;
-  T* xg = (T*)w.x;
-  const T* rg = (const T*)w.r;
-  T* zg = (T*)w.z;
-  T* p0 = (T*)w.p0;
-  T* p1 = (T*)w.p1;
+  RhsSet<T, NR> V;
+  for (int q = 0; q < NR; ++q) {
+    V.x[q] = (T*)ws[q]->x;
+    V.r[q] = (const T*)ws[q]->r;
+    V.z[q] = (T*)ws[q]->z;
+    V.p0[q] = (T*)ws[q]->p0;
+    V.p1[q] = (T*)ws[q]->p1;
+    V.scal[q] = ws[q]->scal;
+  }
   Bsr Acopy = A;
-  void* args[] = {&Acopy, &val, &minv, &xg, &rg, &zg, &p0, &p1, &w.part_a, &w.part_b, &w.scal, &w.keep_g};
+  int64_t keep = w.keep_g;
+  void* args[] = {&Acopy, &val, &minv, &V, &part_a, &part_b, &keep};
   return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(C::kThreads), args, C::kSmemBytes, s);
 }
 
-template <typename T>
-cudaError_t dispatch(int variant, const Bsr& A, PcgWork& w, cudaStream_t s, bool query, bool* eligible) {
+template <typename T, int NR>
+cudaError_t dispatch(int variant, const Bsr& A, PcgWork* const* ws, double* pa, double* pb, cudaStream_t s,
+                     bool query, bool* eligible) {
   if constexpr (sizeof(T) == 4) {
-    if (variant == 0) return launch_persistent<float, 8, 2, 8, 4, 1>(A, w, s, query, eligible);
-    if (variant == 1) return launch_persistent<float, 4, 3, 8, 8, 1>(A, w, s, query, eligible);
-    if (variant == 2) return launch_persistent<float, 4, 2, 8, 2, 2>(A, w, s, query, eligible);
-    return launch_persistent<float, 2, 3, 8, 2, 3>(A, w, s, query, eligible);
+    if (variant == 0) return launch_persistent<float, 8, 2, 8, 4, 1, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 1) return launch_persistent<float, 4, 3, 8, 8, 1, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 2) return launch_persistent<float, 4, 2, 8, 2, 2, NR>(A, ws, pa, pb, s, query, eligible);
+    return launch_persistent<float, 2, 3, 8, 2, 3, NR>(A, ws, pa, pb, s, query, eligible);
   } else {
-    if (variant == 0) return launch_persistent<double, 4, 2, 8, 4, 1>(A, w, s, query, eligible);
-    if (variant == 1) return launch_persistent<double, 2, 3, 8, 4, 1>(A, w, s, query, eligible);
-    if (variant == 2) return launch_persistent<double, 2, 2, 8, 2, 2>(A, w, s, query, eligible);
-    return launch_persistent<double, 1, 3, 8, 2, 2>(A, w, s, query, eligible);
+    if (variant == 0) return launch_persistent<double, 4, 2, 8, 4, 1, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 1) return launch_persistent<double, 2, 3, 8, 4, 1, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 2) return launch_persistent<double, 2, 2, 8, 2, 2, NR>(A, ws, pa, pb, s, query, eligible);
+    return launch_persistent<double, 1, 3, 8, 2, 2, NR>(A, ws, pa, pb, s, query, eligible);
   }
 }
 
@@ -401,14 +478,35 @@ int pcg_persistent_variants() { return 4; }
 
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant) {
   bool ok = false;
-  if (w.fp32) dispatch<float>(variant, A, w, nullptr, true, &ok);
-  else dispatch<double>(variant, A, w, nullptr, true, &ok);
+  PcgWork* ws[1] = {&w};
+  if (w.fp32) dispatch<float, 1>(variant, A, ws, w.part_a, w.part_b, nullptr, true, &ok);
+  else dispatch<double, 1>(variant, A, ws, w.part_a, w.part_b, nullptr, true, &ok);
   return ok;
 }
 
 cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s) {
   bool ok = false;
-  cudaError_t e = w.fp32 ? dispatch<float>(variant, A, w, s, false, &ok) : dispatch<double>(variant, A, w, s, false, &ok);
+  PcgWork* ws[1] = {&w};
+  cudaError_t e = w.fp32 ? dispatch<float, 1>(variant, A, ws, w.part_a, w.part_b, s, false, &ok)
+                         : dispatch<double, 1>(variant, A, ws, w.part_a, w.part_b, s, false, &ok);
+  if (e == cudaSuccess && !ok) return cudaErrorInvalidConfiguration;
+  return e;
+}
+
+bool pcg_persistent2_eligible(const Bsr& A, PcgWork& w0, PcgWork& w1, int variant) {
+  bool ok = false;
+  PcgWork* ws[2] = {&w0, &w1};
+  if (w0.fp32) dispatch<float, 2>(variant, A, ws, nullptr, nullptr, nullptr, true, &ok);
+  else dispatch<double, 2>(variant, A, ws, nullptr, nullptr, nullptr, true, &ok);
+  return ok;
+}
+
+cudaError_t launch_pcg_persistent2(const Bsr& A, PcgWork& w0, PcgWork& w1, int variant, double* part_a,
+                                   double* part_b, cudaStream_t s) {
+  bool ok = false;
+  PcgWork* ws[2] = {&w0, &w1};
+  cudaError_t e = w0.fp32 ? dispatch<float, 2>(variant, A, ws, part_a, part_b, s, false, &ok)
+                          : dispatch<double, 2>(variant, A, ws, part_a, part_b, s, false, &ok);
   if (e == cudaSuccess && !ok) return cudaErrorInvalidConfiguration;
   return e;
 }

@@ -724,6 +724,21 @@ int ikr_linear_solver_solve(ikr_ls ls, ikr_asm a, double* x, const double* b) {
     CK(cudaStreamSynchronize(a->fes->stream));
   });
 }
+int ikr_linear_solver_solve2(ikr_ls ls, ikr_asm a, double* x0, double* x1, const double* b0, const double* b1) {
+  return guarded([&] {
+    need(ls && a && x0 && x1 && b0 && b1, IKR_ERR_ARG, "null argument");
+    cudaStream_t s = a->fes->stream;
+    DBuf<double> db0, db1, dx0, dx1;
+    db0.upload(b0, a->n, s);
+    db1.upload(b1, a->n, s);
+    dx0.alloc(a->n);
+    dx1.alloc(a->n);
+    ls->solve2(a, db0.p, db1.p, dx0.p, dx1.p, ls->rtol, ls->max_iter, 0);
+    dx0.download(x0, a->n, s);
+    dx1.download(x1, a->n, s);
+    CK(cudaStreamSynchronize(s));
+  });
+}
 int ikr_linear_solver_last_info(ikr_ls ls, int32_t* it, double* rel) {
   return guarded([&] {
     need(ls, IKR_ERR_ARG, "null argument");
@@ -791,6 +806,12 @@ int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t kind, double keep) {
              (keep == -1.0 || (keep >= 0.0 && keep < 1.0)),
          IKR_ERR_ARG, "invalid SpMV kernel choice");
     ls->set_kernel(kind, keep);
+  });
+}
+int ikr_linear_solver_set_multi_rhs(ikr_ls ls, int32_t on) {
+  return guarded([&] {
+    need(ls, IKR_ERR_ARG, "null argument");
+    ls->multi_rhs = on != 0;
   });
 }
 int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* kind, double* keep, double* us) {

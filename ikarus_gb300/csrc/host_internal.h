@@ -376,6 +376,12 @@ struct ikr_ls_s {
   double last_rel = 0.0;
   bool factorized = false;
   DBuf<double> b64, x64, r64, c64;  // refinement work
+  // second right-hand side of solve2 (its own CG vectors and scalars; matrix, preconditioner, grid and L2
+  // policy are w's) and the partials of the two-RHS persistent kernel (4 and 8 per CTA)
+  bool multi_rhs = true;
+  ikr::PcgWork w2;
+  DBuf<double> dx2, dr2, dz2, dp2, dp12, pa2, pb2, pbi2, scal2;
+  DBuf<float> fx2, fr2, fz2, fp2, fp12;
 
   ~ikr_ls_s() {
     drop_graphs();
@@ -678,6 +684,75 @@ struct ikr_ls_s {
     count(1);
     if (done == 6.0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the staged SpMV gave up");
     if (done == 3.0) fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp zero or not finite) after %d iterations", last_iters);
+    return last_iters;
+  }
+
+  // the second right-hand side's work (same sizes as w)
+  void setup2() {
+    if (w2.scal && w2.n_rows == w.n_rows && w2.fp32 == w.fp32 && w2.grid == w.grid) return;
+    w2 = w;
+    const size_t n = 4 * (size_t)w.n_rows;
+    if (fp32) {
+      fx2.alloc(n), fr2.alloc(n), fz2.alloc(n), fp2.alloc(n), fp12.alloc(n);
+      w2.x = fx2.p, w2.r = fr2.p, w2.z = fz2.p, w2.p0 = fp2.p, w2.p1 = fp12.p;
+    } else {
+      dx2.alloc(n), dr2.alloc(n), dz2.alloc(n), dp2.alloc(n), dp12.alloc(n);
+      w2.x = dx2.p, w2.r = dr2.p, w2.z = dz2.p, w2.p0 = dp2.p, w2.p1 = dp12.p;
+    }
+    w2.q = nullptr;
+    pbi2.alloc(4 * (size_t)w.grid);
+    scal2.alloc(ikr::kNScal);
+    w2.part_a = nullptr;
+    w2.part_b = pbi2.p;  // written by the init kernel only
+    w2.scal = scal2.p;
+    pa2.alloc(4 * (size_t)w.grid);
+    pb2.alloc(8 * (size_t)w.grid);
+  }
+
+  // x0 = K^{-1} b0 and x1 = K^{-1} b1 with the same tangent.  With a persistent CG kind both run in one
+  // cooperative launch that streams the matrix once per iteration for the two; otherwise (or with refinement
+  // sweeps, or when disabled) one solve after the other.  Returns the CG iterations of both right-hand sides.
+  int64_t solve2(ikr_asm a, const double* b0, const double* b1, double* x0, double* x1, double rt, int maxit,
+                 int refinements) {
+    if (!factorized || asm_ != a) fail(IKR_ERR_INVALID_STATE, "linear solver not factorized for this assembler");
+    const ikr::Bsr A = a->bsr();
+    bool two = multi_rhs && persistent() && refinements <= 0;
+    if (two) {
+      setup2();
+      w2.minv = w.minv, w2.keep_g = w.keep_g, w2.spmv_kind = w.spmv_kind;
+      two = ikr::pcg_persistent2_eligible(A, w, w2, w.spmv_kind - first_persistent_kind());
+    }
+    if (!two) return solve(a, b0, x0, rt, maxit, refinements) + solve(a, b1, x1, rt, maxit, refinements);
+    cudaStream_t s = a->fes->stream;
+    ikr::launch_pcg_init(A, w, b0, rt, maxit, s);
+    ikr::launch_pcg_init(A, w2, b1, rt, maxit, s);
+    count(4);
+    if (profile) CK(cudaEventRecord(tev[0], s));
+    CK(ikr::launch_pcg_persistent2(A, w, w2, w.spmv_kind - first_persistent_kind(), pa2.p, pb2.p, s));
+    count(1);
+    if (profile) CK(cudaEventRecord(tev[1], s));
+    CK(cudaMemcpyAsync(scal_h, scal.p, sizeof(double) * ikr::kNScal, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(scal_h + ikr::kNScal, scal2.p, sizeof(double) * ikr::kNScal, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    ikr::launch_pcg_result(w, x0, 1.0, s);
+    ikr::launch_pcg_result(w2, x1, 1.0, s);
+    count(2);
+    const double* s0 = scal_h;
+    const double* s1 = scal_h + ikr::kNScal;
+    const int it0 = (int)s0[ikr::kIters], it1 = (int)s1[ikr::kIters];
+    if (profile) {  // one matrix stream per iteration of the longer solve
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+      prof_ms += ms;
+      prof_n += std::max(it0, it1);
+    }
+    last_iters = it0 + it1;
+    last_rel = s0[ikr::kBB] > 0 ? std::sqrt(s0[ikr::kRR] / s0[ikr::kBB]) : 0.0;
+    for (const double* sc : {s0, s1}) {
+      if (sc[ikr::kDone] == 6.0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the persistent CG gave up");
+      if (sc[ikr::kDone] == 3.0)
+        fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp zero or not finite) after %d iterations", (int)sc[ikr::kIters]);
+    }
     return last_iters;
   }
 

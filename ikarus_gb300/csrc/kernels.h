@@ -173,6 +173,11 @@ void launch_fill64(double* y, double v, int64_t n, cudaStream_t s);
 int pcg_persistent_variants();
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant);
 cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s);
+// the same solve for two right-hand sides with one matrix stream per iteration (w1 shares w0's matrix,
+// preconditioner, grid and L2 policy); part_a / part_b hold 4 and 8 doubles per grid CTA
+bool pcg_persistent2_eligible(const Bsr& A, PcgWork& w0, PcgWork& w1, int variant);
+cudaError_t launch_pcg_persistent2(const Bsr& A, PcgWork& w0, PcgWork& w1, int variant, double* part_a,
+                                   double* part_b, cudaStream_t s);
 
 // batched.cu -- independent instances (disjoint contiguous node ranges) of one element set
 // one cooperative launch runs every active instance's block-Jacobi PCG; instance i is served by the CTAs

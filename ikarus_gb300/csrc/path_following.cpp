@@ -163,9 +163,10 @@ void pf_solve(ikr_pf pf, ikr_req r, ikr_nr_info* info) {
     }
     ikr::launch_scale64(nr->rhs.p, a->R.p, -1.0, n, s);
     count(1);
-    lin += nr->ls->solve(a, nr->rhs.p, pf->dR.p, eta, st.linear_max_iter, st.refinements);
-    lin += nr->ls->solve(a, a->has_idbc ? pf->b2.p : pf->fext0.p, pf->dL.p, eta, st.linear_max_iter,
-                         st.refinements);
+    // both columns with the same tangent (one matrix stream per CG iteration for the two when the solver
+    // runs a persistent kind)
+    lin += nr->ls->solve2(a, nr->rhs.p, a->has_idbc ? pf->b2.p : pf->fext0.p, pf->dR.p, pf->dL.p, eta,
+                          st.linear_max_iter, st.refinements);
     const double dlam = (-pf->f - dfdDD_dot(pf, f, pf->dR.p, n)) /
                         (dfdDD_dot(pf, f, pf->dL.p, n) + pf->dfdDlambda);  // :275-276
     CK(cudaMemcpyAsync(nr->corr.p, pf->dR.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));

@@ -178,6 +178,9 @@ int ikr_linear_solver_analyze_pattern(ikr_ls ls, ikr_asm a);
 int ikr_linear_solver_factorize(ikr_ls ls, ikr_asm a);       /* builds the preconditioner from the device K */
 /* solve(x, b) with host arrays of size() (Full option system) */
 int ikr_linear_solver_solve(ikr_ls ls, ikr_asm a, double* x, const double* b);
+/* solve(x, B) with two right-hand-side columns (LinearSolver::solve on an n x 2 Eigen matrix, as the bordered
+ * path-following solve calls it, newtonraphsonwithscalarsubsidiaryfunction.hh:265-267); host arrays */
+int ikr_linear_solver_solve2(ikr_ls ls, ikr_asm a, double* x0, double* x1, const double* b0, const double* b1);
 /* iterations and achieved relative residual of the last solve */
 int ikr_linear_solver_last_info(ikr_ls ls, int32_t* iterations, double* rel_residual);
 /* Measurement hooks (no reference counterpart): with profiling on, every CG SpMV launch is bracketed by
@@ -197,6 +200,10 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
  * next factorize from timed CG iterations on the assembled tangent and kept for that assembler.  info
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fraction);
+/* no reference counterpart: solves with two right-hand sides and one tangent (path following's bordered
+ * system) run both CGs in one persistent launch that streams the matrix once per iteration (on = 1, default)
+ * or one after the other (0) */
+int ikr_linear_solver_set_multi_rhs(ikr_ls ls, int32_t on);
 int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* spmv_kind, double* l2_keep_fraction, double* spmv_us);
 /* material law of all elements (the reference's Material template argument of makeFE): NeoHooke (default,
  * neohooke.hh) or StVenantKirchhoff (svk.hh); both with the Lame parameters given at creation */
