@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--eas-predictor", type=int, default=1, help="config 5: 0 none, 1 previous increment")
     ap.add_argument("--path-following", type=int, default=0,
                     help="arc-length path of this many steps on the 128x32x32 cantilever instead of the load control")
+    ap.add_argument("--no-warm-start", action="store_true",
+                    help="--path-following: start the load column's CG from zero in every Newton iteration")
     ap.add_argument("--no-multi-rhs", action="store_true",
                     help="--path-following: solve the two bordered columns one after the other")
     ap.add_argument("--spmv-kinds", default="-1", help="--spmv-only: comma-separated kind[:keep] SpMV choices")
@@ -466,6 +468,15 @@ def run_spmv_only(args):
                 rec["spmv_us"] = round(ms / max(n, 1) * 1e3, 3)
                 rec["spmv_gbs"] = round(bpl / (ms / max(n, 1) / 1e3) / 1e9, 1) if ms > 0 else None
                 rec["iterations"] = it
+        if k_used >= 5:  # persistent kinds: the same iterations for two right-hand sides in one launch
+            ls.profile(True)
+            try:
+                ls.solve(asm, np.stack([b, 0.5 * b + 1e-3], axis=1))
+            except ikr.IkarusError as e:
+                if e.code != -5 and "NOT_CONVERGED" not in str(e):
+                    log(f"solve2: {e}")
+            ms, n = ls.profile_read()
+            rec["two_rhs_us_per_iteration"] = round(ms / max(n, 1) * 1e3, 3)
         ls.profile(False)
         out["runs"].append(rec)
         log(f"spmv-only: {rec}")
@@ -682,6 +693,8 @@ def run_path_following(args):
                       "path_following": "ArcLength, AdaptiveStepSizing::NoOp", "steps": steps,
                       "bordered_solve": "two CG columns one after the other" if args.no_multi_rhs else
                                         "two CG columns in one persistent launch (one matrix stream per iteration)",
+                      "load_column": "from zero" if args.no_warm_start else
+                                     "warm start from the previous Newton iteration's solution",
                       "material": "NeoHooke E=1000 nu=0.3", "l2": "256 MB buffer written before each timed path"}}
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     s_hat = None
@@ -701,6 +714,7 @@ def run_path_following(args):
             out["config"]["arc_length"] = s_hat
             del cal
         pf = ikr.PathFollowing(nr, steps, s_hat, ikr.ArcLength())
+        pf.set_warm_start(not args.no_warm_start)
         times = []
         for k in range(args.warmup + args.steps):
             req.insertGlobalSolution(np.zeros(p.n_dofs))

@@ -202,6 +202,7 @@ SIGNATURES = {
     "ikr_path_following_run": ([_vp, _vp, C.POINTER(_ControlInfo), C.POINTER(_NRInfo), _I], C.c_int),
     "ikr_path_following_subsidiary_args": ([_vp, _dp], C.c_int),
     "ikr_path_following_increment": ([_vp, _dp], C.c_int),
+    "ikr_path_following_set_warm_start": ([_vp, _I], C.c_int),
     "ikr_load_control_predictor_stats": ([_vp, _ip, _ip], C.c_int),
     "ikr_load_control_predictor_history": ([_vp, _I, _dp, _ip], C.c_int),
     "ikr_load_control_set_predictor_gate": ([_vp, _I], C.c_int),
@@ -917,6 +918,10 @@ class PathFollowing:
         _err(lib().ikr_path_following_subsidiary_args(self.h, _ptr(out)))
         return dict(stepSize=out[0], Dlambda=out[1], f=out[2], dfdDlambda=out[3], psi=out[4],
                     currentStep=int(out[5]))
+
+    def set_warm_start(self, on=True):
+        """Start the load column's CG from the previous Newton iteration's solution (default) or from zero."""
+        _err(lib().ikr_path_following_set_warm_start(self.h, int(bool(on))))
 
     def increment(self, n):
         """SubsidiaryArgs::DD of the current step (n dofs)."""

@@ -148,8 +148,12 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       ns = j + 1;
     }
   }
-  // CG state of the owned rows, per RHS
-  T xr[NR][MAXS][3], rr_[NR][MAXS][3], zr[NR][MAXS][3], pr[NR][MAXS][3], qr[NR][MAXS][3];
+  // CG state of the owned rows, per RHS.  With one RHS x, r, z, p and q of the owned rows live in registers;
+  // with several (kLean) only r and q do, and x, z, p of the owned rows are re-read from the global vectors
+  // (which the gathers need anyway; own-row reads hit L2) to keep the register count without spills.
+  constexpr bool kLean = NR > 1;
+  constexpr int XS = kLean ? 1 : MAXS;
+  T xr[NR][XS][3], rr_[NR][MAXS][3], zr[NR][XS][3], pr[NR][XS][3], qr[NR][MAXS][3];
   double rz[NR], tol2[NR], rrs[NR], done[NR], beta[NR];
   int maxit[NR], it[NR];
   bool all_done = true;
@@ -162,9 +166,13 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       V3<T> r0 = {T(0), T(0), T(0)}, z0 = {T(0), T(0), T(0)};
       if (own) r0 = load3rw(V.r[q], row), z0 = load3rw(V.z[q], row);
 #pragma unroll
-      for (int c = 0; c < 3; ++c) xr[q][j][c] = pr[q][j][c] = qr[q][j][c] = T(0);
+      for (int c = 0; c < 3; ++c) qr[q][j][c] = T(0);
       rr_[q][j][0] = r0.x, rr_[q][j][1] = r0.y, rr_[q][j][2] = r0.z;
-      zr[q][j][0] = z0.x, zr[q][j][1] = z0.y, zr[q][j][2] = z0.z;
+      if constexpr (!kLean) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) xr[q][j][c] = pr[q][j][c] = T(0);
+        zr[q][j][0] = z0.x, zr[q][j][1] = z0.y, zr[q][j][2] = z0.z;
+      }
     }
     const double* sc = V.scal[q];
     rz[q] = sc[kRz];
@@ -287,9 +295,16 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
 #pragma unroll
         for (int q = 0; q < NR; ++q) {
           if (!act[q]) continue;
-          const T n0 = zr[q][j][0] + tb[q] * pr[q][j][0], n1 = zr[q][j][1] + tb[q] * pr[q][j][1],
-                  n2 = zr[q][j][2] + tb[q] * pr[q][j][2];
-          pr[q][j][0] = n0, pr[q][j][1] = n1, pr[q][j][2] = n2;
+          V3<T> zo, po;
+          if constexpr (kLean) {
+            zo = {T(0), T(0), T(0)}, po = {T(0), T(0), T(0)};
+            if (row < A.n_rows) zo = load3rw(V.z[q], row), po = load3rw(pold[q], row);
+          } else {
+            zo = {zr[q][j][0], zr[q][j][1], zr[q][j][2]};
+            po = {pr[q][j][0], pr[q][j][1], pr[q][j][2]};
+          }
+          const T n0 = zo.x + tb[q] * po.x, n1 = zo.y + tb[q] * po.y, n2 = zo.z + tb[q] * po.z;
+          if constexpr (!kLean) pr[q][j][0] = n0, pr[q][j][1] = n1, pr[q][j][2] = n2;
           qr[q][j][0] = acc[q][0], qr[q][j][1] = acc[q][1], qr[q][j][2] = acc[q][2];
           if (row < A.n_rows) {
             store3(pnew[q], row, n0, n1, n2);
@@ -332,9 +347,16 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
           const int row = 32 * (gw + j * nw) + lane;
           if (j < ns && row < A.n_rows) {
             T r1[3];
+            if constexpr (kLean) {
+              const V3<T> pv = load3rw(pnew[q], row);
+              const V3<T> xv = load3rw(V.x[q], row);
+              store3(V.x[q], row, xv.x + a * pv.x, xv.y + a * pv.y, xv.z + a * pv.z);
+            } else {
+#pragma unroll
+              for (int c = 0; c < 3; ++c) xr[q][j][c] += a * pr[q][j][c];
+            }
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              xr[q][j][c] += a * pr[q][j][c];
               r1[c] = rr_[q][j][c] - a * qr[q][j][c];
               rr_[q][j][c] = r1[c];
             }
@@ -343,7 +365,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
               zv[b] = __ldg(m + 3 * b) * r1[0] + __ldg(m + 3 * b + 1) * r1[1] + __ldg(m + 3 * b + 2) * r1[2];
-              zr[q][j][b] = zv[b];
+              if constexpr (!kLean) zr[q][j][b] = zv[b];
             }
             store3(V.z[q], row, zv[0], zv[1], zv[2]);
             T trz = T(0), trr = T(0);
@@ -391,10 +413,12 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   // solutions of the owned rows; the final scalars from CTA 0 (identical in every CTA)
 #pragma unroll
   for (int q = 0; q < NR; ++q) {
+    if constexpr (!kLean) {
 #pragma unroll
-    for (int j = 0; j < MAXS; ++j) {
-      const int row = 32 * (gw + j * nw) + lane;
-      if (j < ns && row < A.n_rows) store3(V.x[q], row, xr[q][j][0], xr[q][j][1], xr[q][j][2]);
+      for (int j = 0; j < MAXS; ++j) {
+        const int row = 32 * (gw + j * nw) + lane;
+        if (j < ns && row < A.n_rows) store3(V.x[q], row, xr[q][j][0], xr[q][j][1], xr[q][j][2]);
+      }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       double* sc = V.scal[q];

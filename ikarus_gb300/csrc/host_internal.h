@@ -713,19 +713,22 @@ struct ikr_ls_s {
   // cooperative launch that streams the matrix once per iteration for the two; otherwise (or with refinement
   // sweeps, or when disabled) one solve after the other.  Returns the CG iterations of both right-hand sides.
   int64_t solve2(ikr_asm a, const double* b0, const double* b1, double* x0, double* x1, double rt, int maxit,
-                 int refinements) {
+                 int refinements, double rt1 = -1.0) {
+    if (rt1 < 0.0) rt1 = rt;
     if (!factorized || asm_ != a) fail(IKR_ERR_INVALID_STATE, "linear solver not factorized for this assembler");
     const ikr::Bsr A = a->bsr();
-    bool two = multi_rhs && persistent() && refinements <= 0;
+    // FP64 CG iterations are bound by GB300's FP64 pipe, not by the matrix stream: two right-hand sides cost
+    // twice the time in one launch as well, so only the FP32 tangent runs them together
+    bool two = multi_rhs && fp32 && persistent() && refinements <= 0;
     if (two) {
       setup2();
       w2.minv = w.minv, w2.keep_g = w.keep_g, w2.spmv_kind = w.spmv_kind;
       two = ikr::pcg_persistent2_eligible(A, w, w2, w.spmv_kind - first_persistent_kind());
     }
-    if (!two) return solve(a, b0, x0, rt, maxit, refinements) + solve(a, b1, x1, rt, maxit, refinements);
+    if (!two) return solve(a, b0, x0, rt, maxit, refinements) + solve(a, b1, x1, rt1, maxit, refinements);
     cudaStream_t s = a->fes->stream;
     ikr::launch_pcg_init(A, w, b0, rt, maxit, s);
-    ikr::launch_pcg_init(A, w2, b1, rt, maxit, s);
+    ikr::launch_pcg_init(A, w2, b1, rt1, maxit, s);
     count(4);
     if (profile) CK(cudaEventRecord(tev[0], s));
     CK(ikr::launch_pcg_persistent2(A, w, w2, w.spmv_kind - first_persistent_kind(), pa2.p, pb2.p, s));

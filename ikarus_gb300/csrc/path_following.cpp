@@ -27,6 +27,11 @@ struct ikr_pf_s {
   double dfdDD_scale = 0;  // dfdDD = dfdDD_scale * DD (arc length) or * (mask . DD) (displacement control)
   int current_step = 0;
   DBuf<double> DD, DDc, mask, fext0, dR, dL, b2, u_save, part, out;
+  // warm start of the load column: its right-hand side Fext0 (- F_idbc) changes little along the path, so the
+  // previous dL is the initial guess of the next solve
+  bool warm = true, dl_valid = false;
+  DBuf<double> dl_res, dl_corr;
+  int64_t dl_skipped = 0;
 };
 
 namespace {
@@ -164,9 +169,29 @@ void pf_solve(ikr_pf pf, ikr_req r, ikr_nr_info* info) {
     ikr::launch_scale64(nr->rhs.p, a->R.p, -1.0, n, s);
     count(1);
     // both columns with the same tangent (one matrix stream per CG iteration for the two when the solver
-    // runs a persistent kind)
-    lin += nr->ls->solve2(a, nr->rhs.p, a->has_idbc ? pf->b2.p : pf->fext0.p, pf->dR.p, pf->dL.p, eta,
-                          st.linear_max_iter, st.refinements);
+    // runs a persistent kind).  The load column starts from the previous dL: the CG solves for the change c with
+    // K c = b2 - K dL_prev to the same accuracy relative to b2 (no solve when dL_prev already meets it).
+    const double* b2 = a->has_idbc ? pf->b2.p : pf->fext0.p;
+    if (pf->warm && pf->dl_valid) {
+      pf->dl_res.alloc(n);
+      pf->dl_corr.alloc(n);
+      ikr::launch_residual64(a->bsr(), a->fp32, pf->dL.p, b2, pf->dl_res.p, s);
+      count(1);
+      const double nb2 = device_norm(f, b2, n, nr->nrm_part, nr->nrm_out);
+      const double nres = device_norm(f, pf->dl_res.p, n, nr->nrm_part, nr->nrm_out);
+      if (nres <= eta * nb2) {
+        lin += nr->ls->solve(a, nr->rhs.p, pf->dR.p, eta, st.linear_max_iter, st.refinements);
+        ++pf->dl_skipped;
+      } else {
+        lin += nr->ls->solve2(a, nr->rhs.p, pf->dl_res.p, pf->dR.p, pf->dl_corr.p, eta, st.linear_max_iter,
+                              st.refinements, eta * nb2 / nres);
+        ikr::launch_axpy64(pf->dL.p, pf->dl_corr.p, 1.0, n, s);
+        count(1);
+      }
+    } else {
+      lin += nr->ls->solve2(a, nr->rhs.p, b2, pf->dR.p, pf->dL.p, eta, st.linear_max_iter, st.refinements);
+    }
+    pf->dl_valid = true;
     const double dlam = (-pf->f - dfdDD_dot(pf, f, pf->dR.p, n)) /
                         (dfdDD_dot(pf, f, pf->dL.p, n) + pf->dfdDlambda);  // :275-276
     CK(cudaMemcpyAsync(nr->corr.p, pf->dR.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
@@ -338,6 +363,12 @@ int ikr_path_following_subsidiary_args(ikr_pf pf, double* out6) {
     out6[5] = pf->current_step;
   });
 }
+int ikr_path_following_set_warm_start(ikr_pf pf, int32_t on) {
+  return guarded([&] {
+    need(pf, IKR_ERR_ARG, "null argument");
+    pf->warm = on != 0;
+  });
+}
 int ikr_path_following_increment(ikr_pf pf, double* dd) {
   return guarded([&] {
     need(pf && dd, IKR_ERR_ARG, "null argument");
@@ -374,6 +405,8 @@ int ikr_path_following_run(ikr_pf pf, ikr_req r, ikr_control_info* info, ikr_nr_
     pf->current_step = 0;
     pf->psi = 0.0;
     pf->computed = false;
+    pf->dl_valid = false;
+    pf->dl_skipped = 0;
     if (pf->kind == IKR_PF_DISPLACEMENT_CONTROL) {
       std::vector<double> m(n, 0.0);
       for (int32_t d : pf->controlled) m[d] = 1.0;

@@ -331,6 +331,10 @@ int ikr_path_following_run(ikr_pf pf, ikr_req req, ikr_control_info* info, ikr_n
 /* SubsidiaryArgs of the current state (pathfollowingfunctions.hh:30-41): out[0] stepSize, [1] Dlambda, [2] f,
  * [3] dfdDlambda, [4] the arc length's psi, [5] currentStep */
 int ikr_path_following_subsidiary_args(ikr_pf pf, double* out6);
+/* no reference counterpart: the load column K dL = Fext0 - F_idbc of every Newton iteration starts from the
+ * previous dL and is solved for the change to the same relative accuracy (on = 1, default), or from zero (0, as
+ * the reference's direct solve has no initial guess) */
+int ikr_path_following_set_warm_start(ikr_pf pf, int32_t on);
 /* SubsidiaryArgs::DD, the solution increment of the current step (n doubles, host memory) */
 int ikr_path_following_increment(ikr_pf pf, double* dd);
 

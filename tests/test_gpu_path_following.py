@@ -29,7 +29,7 @@ def _step_size(p, lam_per_step=0.25):
     return np.sqrt(2.0) * np.linalg.norm(dd0) * lam_per_step
 
 
-def _device(ikr, p, steps, s, pft, precision=0, rate=None, adaptive=None):
+def _device(ikr, p, steps, s, pft, precision=0, rate=None, adaptive=None, warm=True, multi=True):
     fes, asm = problems.build_gpu(p, precision=precision)
     if rate is not None:
         asm.set_dirichlet_values(rate)
@@ -38,8 +38,11 @@ def _device(ikr, p, steps, s, pft, precision=0, rate=None, adaptive=None):
         st = ikr.NRSettings(tol=1e-10, maxIter=30, linear_rtol=1e-13, linear_rtol_min=1e-13)
     else:
         st = ikr.NRSettings(tol=1e-10, maxIter=60, eisenstat_walker=True, linear_rtol=1e-2, linear_rtol_min=1e-7)
-    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(rtol=1e-13)))
+    ls = ikr.LinearSolver(rtol=1e-13)
+    ls.set_multi_rhs(multi)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ls))
     pf = ikr.PathFollowing(nr, steps, s, pft, adaptive)
+    pf.set_warm_start(warm)
     states = []
 
     def obs(msg, state):
@@ -60,12 +63,13 @@ def _check_fp64(info, states, ref):
     assert np.abs(u - ref["u"]).max() <= 1e-8 * np.abs(ref["u"]).max()
 
 
-@pytest.mark.parametrize("eas,n", [(0, 0), (2, 9)])
-def test_arc_length_matches_oracle(ikr, eas, n):
+@pytest.mark.parametrize("eas,n,warm", [(0, 0, True), (0, 0, False), (2, 9, True)])
+def test_arc_length_matches_oracle(ikr, eas, n, warm):
+    """warm: the load column's CG starts from the previous Newton iteration's solution (default) or from zero."""
     p = _problem(eas=eas, n=n)
     s = _step_size(p)
     ref = oracle.from_problem(p).path_following(4, s, tol=1e-10, max_iter=30)
-    info, req, pf, states = _device(ikr, p, 4, s, ikr.ArcLength())
+    info, req, pf, states = _device(ikr, p, 4, s, ikr.ArcLength(), warm=warm)
     _check_fp64(info, states, ref)
     assert [st[0] for st in states] == [-1, 0, 1, 2, 3]
     assert abs(pf.subsidiary_args()["psi"] - ref["psi"]) <= 1e-10 * ref["psi"]
@@ -121,11 +125,12 @@ def test_iteration_based_step_sizing_matches_oracle(ikr):
         ikr.AdaptiveStepSizing.IterationBased().setTargetIterations(0)
 
 
-def test_mixed_arc_length_is_on_the_path(ikr):
+@pytest.mark.parametrize("multi", [True, False], ids=["two-rhs-launch", "sequential"])
+def test_mixed_arc_length_is_on_the_path(ikr, multi):
     p = _problem()
     s = _step_size(p)
     ref = oracle.from_problem(p).path_following(4, s, tol=1e-10, max_iter=30)
-    info, req, pf, states = _device(ikr, p, 4, s, ikr.ArcLength(), precision=1)
+    info, req, pf, states = _device(ikr, p, 4, s, ikr.ArcLength(), precision=1, multi=multi)
     assert info.success
     psi = pf.subsidiary_args()["psi"]
     o = oracle.from_problem(p)
