@@ -254,7 +254,29 @@ void initial_prediction(ikr_pf pf, ikr_req r) {
     r->lambda = dlambda;
     r->version++;
     assemble_vector(a, r, IKR_DBC_FULL);
-    if (a->has_idbc) {  // R += idbcForceFunction(req)
+    // With an FP32 tangent the solve below is refined against the FP64 tangent: psi, and with it where every
+    // arc-length step lands on the path, then agrees with the FP64 form (an FP32 solve alone is off by up to
+    // cond(K) eps_32).  The FP64 tangent (and the FP64 K_raw of the prescribed values) are assembled into the
+    // assembler's FP64 value array with the same kernels.
+    const bool mixed = a->fp32;
+    ikr::Bsr k64{};
+    if (mixed) {
+      a->val64.alloc(9 * (size_t)a->npad);
+      a->fp32 = false;
+      try {
+        if (a->has_idbc) {
+          idbc_force(a, r);
+          ikr::launch_idbc_force(a->R.p, a->idbc_force.p, a->node_fixed.p, 1.0, n, s);
+          count(1);
+        }
+        assemble_matrix(a, r, IKR_DBC_FULL);
+      } catch (...) {
+        a->fp32 = true;
+        throw;
+      }
+      k64 = a->bsr();
+      a->fp32 = true;
+    } else if (a->has_idbc) {  // R += idbcForceFunction(req)
       idbc_force(a, r);
       ikr::launch_idbc_force(a->R.p, a->idbc_force.p, a->node_fixed.p, 1.0, n, s);
       count(1);
@@ -267,6 +289,22 @@ void initial_prediction(ikr_pf pf, ikr_req r) {
     // the reference factorises a direct solver here; the CG runs to the tightest tolerance configured
     const double eta = st.forcing == 1 ? st.linear_rtol_min : st.linear_rtol;
     nr->ls->solve(a, nr->rhs.p, pf->DD.p, eta, st.linear_max_iter, st.refinements);
+    if (mixed) {  // iterative refinement: r = b - K64 DD in FP64, correction by the FP32 CG
+      constexpr double kTarget = 1e-10, kInner = 1e-3;
+      constexpr int kSweeps = 12;
+      pf->dl_res.alloc(n);
+      pf->dl_corr.alloc(n);
+      const double nb = device_norm(f, nr->rhs.p, n, nr->nrm_part, nr->nrm_out);
+      for (int k = 0; k < kSweeps; ++k) {
+        ikr::launch_residual64(k64, false, pf->DD.p, nr->rhs.p, pf->dl_res.p, s);
+        count(1);
+        const double nres = device_norm(f, pf->dl_res.p, n, nr->nrm_part, nr->nrm_out);
+        if (!(nres > kTarget * nb)) break;
+        nr->ls->solve(a, pf->dl_res.p, pf->dl_corr.p, kInner, st.linear_max_iter, 0);
+        ikr::launch_axpy64(pf->DD.p, pf->dl_corr.p, 1.0, n, s);
+        count(1);
+      }
+    }
     const double dd2 = device_dot(f, pf->DD.p, pf->DD.p, n, pf->part, pf->out);
     pf->psi = std::sqrt(dd2 + dhat02);
     const double sc = std::sqrt(dd2 + dhat02 + pf->psi * pf->psi * dlambda * dlambda);

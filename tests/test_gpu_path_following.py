@@ -4,8 +4,8 @@ reference's testpathfollowing.cpp goldens (tests/test_oracle.py).
 
 FP64 form: Newton iterations of every solve equal the oracle's, the load factor after every step within 1e-10
 and the displacement within 1e-8 of the largest entry.  Mixed form (FP32 tangent and CG): every step converges to
-an equilibrium on the arc-length sphere of its own psi; the path point agrees with the oracle's within the FP32
-solve's accuracy (1e-3).
+an equilibrium on the arc-length sphere of its own psi, and psi (the initial prediction refined against the
+FP64 tangent) and the path points agree with the FP64 oracle (psi 1e-7, lambda 1e-6, u 1e-5).
 """
 import numpy as np
 import pytest
@@ -140,5 +140,9 @@ def test_mixed_arc_length_is_on_the_path(ikr, multi):
         du = u - states[k - 1][2]
         dl = lam - states[k - 1][1]
         assert abs(np.sqrt(du @ du + psi * psi * dl * dl) - s) <= 1e-8 * s
+    # the initial prediction is refined against the FP64 tangent, so psi and the path points agree with the
+    # FP64 oracle far below the FP32 solve's own accuracy
+    assert abs(psi - ref["psi"]) <= 1e-7 * ref["psi"]
     lams = np.array([st[1] for st in states])
-    np.testing.assert_allclose(lams, ref["lambdas"], rtol=1e-3, atol=1e-12)
+    np.testing.assert_allclose(lams, ref["lambdas"], rtol=1e-6, atol=1e-12)
+    assert np.abs(states[-1][2] - ref["u"]).max() <= 1e-5 * np.abs(ref["u"]).max()
