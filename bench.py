@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--eas-predictor", type=int, default=1, help="config 5: 0 none, 1 previous increment")
     ap.add_argument("--path-following", type=int, default=0,
                     help="arc-length path of this many steps on the 128x32x32 cantilever instead of the load control")
+    ap.add_argument("--pf-mixed-only", action="store_true", help="--path-following: skip the plain FP64 form")
     ap.add_argument("--no-warm-start", action="store_true",
                     help="--path-following: start the load column's CG from zero in every Newton iteration")
     ap.add_argument("--no-multi-rhs", action="store_true",
@@ -699,7 +700,7 @@ def run_path_following(args):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     s_hat = None
     finals = {}
-    for mixed in (False, True):
+    for mixed in ((True,) if args.pf_mixed_only else (False, True)):
         fes, asm = problems.build_gpu(p, precision=1 if mixed else 0)
         ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
         ls.set_multi_rhs(not args.no_multi_rhs)
@@ -729,18 +730,24 @@ def run_path_following(args):
             if k >= args.warmup:
                 times.append(ev0.elapsed_time(ev1) / 1e3)
             log(f"path following {'mixed' if mixed else 'plain'}: {ev0.elapsed_time(ev1) / 1e3:.3f} s, newton "
-                f"{info.totalIterations}, cg {info.totalLinearIterations}, lambda {req.parameter():.6f}")
+                f"{info.totalIterations}, cg {info.totalLinearIterations}, lambda {req.parameter():.6f}, "
+                f"{pf.stats()}")
         key = "mixed" if mixed else "plain_fp64"
         out[key] = {"s": round(sum(times) / len(times), 4), "newton_iterations": info.totalIterations,
                     "cg_iterations": info.totalLinearIterations,
                     "newton_per_step": [si.iterations for si in info.solverInfos],
-                    "final_lambda": req.parameter(), "psi": pf.subsidiary_args()["psi"],
+                    "final_lambda": req.parameter(), "psi": pf.subsidiary_args()["psi"], **pf.stats(),
                     "spmv_kernel": ls.kernel_info()[:2]}
         finals[key] = req.globalSolution()
         del pf, nr, ls, req, asm, fes
     out["value"] = out["mixed"]["s"]
+    if args.pf_mixed_only:
+        print(json.dumps(out))
+        return
     out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 2)
     out["mixed"]["rel_psi_diff_vs_plain"] = abs(out["mixed"]["psi"] / out["plain_fp64"]["psi"] - 1.0)
+    out["mixed"]["max_rel_diff_vs_plain"] = float(np.abs(finals["mixed"] - finals["plain_fp64"]).max()
+                                                  / np.abs(finals["plain_fp64"]).max())
     if not args.no_cpu_baseline:
         v, parts = cpu_sample(out["plain_fp64"]["newton_iterations"], out["plain_fp64"]["cg_iterations"])
         out["cpu_baseline"] = {"value": round(v, 2), "unit": "s", "cores": 1, "kind": "port",

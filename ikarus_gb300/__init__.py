@@ -203,6 +203,7 @@ SIGNATURES = {
     "ikr_path_following_subsidiary_args": ([_vp, _dp], C.c_int),
     "ikr_path_following_increment": ([_vp, _dp], C.c_int),
     "ikr_path_following_set_warm_start": ([_vp, _I], C.c_int),
+    "ikr_path_following_stats": ([_vp, _dp], C.c_int),
     "ikr_load_control_predictor_stats": ([_vp, _ip, _ip], C.c_int),
     "ikr_load_control_predictor_history": ([_vp, _I, _dp, _ip], C.c_int),
     "ikr_load_control_set_predictor_gate": ([_vp, _I], C.c_int),
@@ -918,6 +919,14 @@ class PathFollowing:
         _err(lib().ikr_path_following_subsidiary_args(self.h, _ptr(out)))
         return dict(stepSize=out[0], Dlambda=out[1], f=out[2], dfdDlambda=out[3], psi=out[4],
                     currentStep=int(out[5]))
+
+    def stats(self):
+        """Last run: FP64 refinement sweeps of the initial prediction, its final relative residual, its CG
+        iterations, load-column solves skipped by the warm start."""
+        out = np.zeros(4)
+        _err(lib().ikr_path_following_stats(self.h, _ptr(out)))
+        return dict(prediction_sweeps=int(out[0]), prediction_rel_residual=out[1], prediction_cg=int(out[2]),
+                    load_solves_skipped=int(out[3]))
 
     def set_warm_start(self, on=True):
         """Start the load column's CG from the previous Newton iteration's solution (default) or from zero."""

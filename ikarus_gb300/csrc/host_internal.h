@@ -725,7 +725,12 @@ struct ikr_ls_s {
       w2.minv = w.minv, w2.keep_g = w.keep_g, w2.spmv_kind = w.spmv_kind;
       two = ikr::pcg_persistent2_eligible(A, w, w2, w.spmv_kind - first_persistent_kind());
     }
-    if (!two) return solve(a, b0, x0, rt, maxit, refinements) + solve(a, b1, x1, rt1, maxit, refinements);
+    if (!two) {
+      const int64_t i0 = solve(a, b0, x0, rt, maxit, refinements);
+      const int64_t i1 = solve(a, b1, x1, rt1, maxit, refinements);
+      last_iters = (int)(i0 + i1);
+      return i0 + i1;
+    }
     cudaStream_t s = a->fes->stream;
     ikr::launch_pcg_init(A, w, b0, rt, maxit, s);
     ikr::launch_pcg_init(A, w2, b1, rt1, maxit, s);

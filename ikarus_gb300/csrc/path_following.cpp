@@ -32,6 +32,10 @@ struct ikr_pf_s {
   bool warm = true, dl_valid = false;
   DBuf<double> dl_res, dl_corr;
   int64_t dl_skipped = 0;
+  // initial prediction of the last run: refinement sweeps, final relative FP64 residual, CG iterations
+  int pred_sweeps = 0;
+  double pred_rel = 0.0;
+  int64_t pred_cg = 0;
 };
 
 namespace {
@@ -288,21 +292,30 @@ void initial_prediction(ikr_pf pf, ikr_req r) {
     count(1);
     // the reference factorises a direct solver here; the CG runs to the tightest tolerance configured
     const double eta = st.forcing == 1 ? st.linear_rtol_min : st.linear_rtol;
-    nr->ls->solve(a, nr->rhs.p, pf->DD.p, eta, st.linear_max_iter, st.refinements);
+    pf->pred_cg = nr->ls->solve(a, nr->rhs.p, pf->DD.p, eta, st.linear_max_iter, st.refinements);
+    pf->pred_sweeps = 0;
+    pf->pred_rel = 0.0;
     if (mixed) {  // iterative refinement: r = b - K64 DD in FP64, correction by the FP32 CG
-      constexpr double kTarget = 1e-10, kInner = 1e-3;
-      constexpr int kSweeps = 12;
+      // A sweep cannot reduce the residual by more than about cond(K) eps_32 (the FP32 tangent's own error),
+      // so the correction's CG tolerance follows the reduction the previous sweep achieved.
+      constexpr double kTarget = 1e-10;
+      constexpr int kSweeps = 20;
       pf->dl_res.alloc(n);
       pf->dl_corr.alloc(n);
       const double nb = device_norm(f, nr->rhs.p, n, nr->nrm_part, nr->nrm_out);
-      for (int k = 0; k < kSweeps; ++k) {
+      double inner = 1e-2, prev = -1.0;
+      for (int k = 0;; ++k) {
         ikr::launch_residual64(k64, false, pf->DD.p, nr->rhs.p, pf->dl_res.p, s);
         count(1);
         const double nres = device_norm(f, pf->dl_res.p, n, nr->nrm_part, nr->nrm_out);
-        if (!(nres > kTarget * nb)) break;
-        nr->ls->solve(a, pf->dl_res.p, pf->dl_corr.p, kInner, st.linear_max_iter, 0);
+        pf->pred_rel = nb > 0.0 ? nres / nb : 0.0;
+        if (!(nres > kTarget * nb) || k == kSweeps) break;
+        if (prev > 0.0) inner = std::min(0.25, std::max(1e-3, 0.25 * nres / prev));
+        prev = nres;
+        pf->pred_cg += nr->ls->solve(a, pf->dl_res.p, pf->dl_corr.p, inner, st.linear_max_iter, 0);
         ikr::launch_axpy64(pf->DD.p, pf->dl_corr.p, 1.0, n, s);
         count(1);
+        pf->pred_sweeps = k + 1;
       }
     }
     const double dd2 = device_dot(f, pf->DD.p, pf->DD.p, n, pf->part, pf->out);
@@ -399,6 +412,15 @@ int ikr_path_following_subsidiary_args(ikr_pf pf, double* out6) {
     out6[3] = pf->dfdDlambda;
     out6[4] = pf->psi;
     out6[5] = pf->current_step;
+  });
+}
+int ikr_path_following_stats(ikr_pf pf, double* out4) {
+  return guarded([&] {
+    need(pf && out4, IKR_ERR_ARG, "null argument");
+    out4[0] = pf->pred_sweeps;
+    out4[1] = pf->pred_rel;
+    out4[2] = (double)pf->pred_cg;
+    out4[3] = (double)pf->dl_skipped;
   });
 }
 int ikr_path_following_set_warm_start(ikr_pf pf, int32_t on) {

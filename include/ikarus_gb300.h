@@ -335,6 +335,10 @@ int ikr_path_following_subsidiary_args(ikr_pf pf, double* out6);
  * previous dL and is solved for the change to the same relative accuracy (on = 1, default), or from zero (0, as
  * the reference's direct solve has no initial guess) */
 int ikr_path_following_set_warm_start(ikr_pf pf, int32_t on);
+/* no reference counterpart, last run: out[0] FP64 refinement sweeps of the arc length's initial prediction (FP32
+ * tangent only), [1] its final relative FP64 residual, [2] its CG iterations, [3] load-column solves the warm start
+ * made unnecessary */
+int ikr_path_following_stats(ikr_pf pf, double* out4);
 /* SubsidiaryArgs::DD, the solution increment of the current step (n doubles, host memory) */
 int ikr_path_following_increment(ikr_pf pf, double* dd);
 
