@@ -738,7 +738,134 @@ void launch_kind(const ElemArgs& a, int mode, bool fp32, const int32_t* list, in
   }
 }
 
+// calculateAt of EAS elements (enhancedassumedstrains.hh:127-188), one thread per element, FP64: the stored alpha
+// enhances the strain at the local point xi.  GL (E9/E21): E = E(H_c) + M(xi) alpha, F = I + H_c; H9 / H9T: the
+// displacement gradient H = H_c + H~ (or H_c + F_c0 H~^T), F = I + H, E = E(H).  type 0 PK2, 1 Kirchhoff, 2 Cauchy.
+__global__ void eas_stress_at_kernel(ElemArgs a, int e0, int count, const double* __restrict__ xi, int xi_per_elem,
+                                     int type, double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const int e = e0 + k;
+  const int ne = a.n_elems;
+  const int kind = a.eas_kind, na = a.n_alpha;
+  const double* x = xi + (xi_per_elem ? 3 * k : 0);
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  double dxi[8][3], U[8][3];
+  for (int v = 0; v < 8; ++v) {
+    const int node = a.conn[v * ne + e];
+    double f[3], df[3];
+    for (int d = 0; d < 3; ++d) {
+      const bool b = (v >> d) & 1;
+      f[d] = b ? x[d] : 1.0 - x[d];
+      df[d] = b ? 1.0 : -1.0;
+    }
+    dxi[v][0] = df[0] * f[1] * f[2];
+    dxi[v][1] = f[0] * df[1] * f[2];
+    dxi[v][2] = f[0] * f[1] * df[2];
+    for (int c = 0; c < 3; ++c) U[v][c] = a.u ? a.u[3 * node + c] : 0.0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) J[i][j] += a.X[3 * node + i] * dxi[v][j];
+  }
+  double Ji[3][3];
+  const double detJ = inv3(J, Ji);
+  double H[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int v = 0; v < 8; ++v) {
+    double dN[3];
+    for (int kk = 0; kk < 3; ++kk) dN[kk] = dxi[v][0] * Ji[0][kk] + dxi[v][1] * Ji[1][kk] + dxi[v][2] * Ji[2][kk];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) H[i][j] += U[v][i] * dN[j];
+  }
+  if (kind != 1) {  // H9 / H9T enhancement of the gradient
+    double A0[3][3], Ht[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) A0[i][j] = a.eas_geo[(size_t)(3 * i + j) * ne + e];
+    const double sc = a.eas_geo[(size_t)9 * ne + e] / detJ;
+    for (int p = 0; p < na; ++p) {
+      const int r = p / 3, c = p % 3;
+      const double w = a.alpha[(size_t)p * ne + e] * sc * (2.0 * x[c] - 1.0);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Ht[i][j] += w * A0[i][r] * A0[j][c];
+    }
+    if (kind == 2) {
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) H[i][j] += Ht[i][j];
+    } else {
+      double Fc0[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double t = (i == j) ? 1.0 : 0.0;
+          for (int v = 0; v < 8; ++v) t += U[v][i] * a.eas_geo[(size_t)(10 + 3 * v + j) * ne + e];
+          Fc0[i][j] = t;
+        }
+      double add[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) add[i][j] = Fc0[i][0] * Ht[j][0] + Fc0[i][1] * Ht[j][1] + Fc0[i][2] * Ht[j][2];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) H[i][j] += add[i][j];
+    }
+  }
+  double Ev[6];
+  {
+    double E[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        E[i][j] = 0.5 * (H[i][j] + H[j][i] + H[0][i] * H[0][j] + H[1][i] * H[1][j] + H[2][i] * H[2][j]);
+    Ev[0] = E[0][0], Ev[1] = E[1][1], Ev[2] = E[2][2];
+    Ev[3] = 2.0 * E[1][2], Ev[4] = 2.0 * E[0][2], Ev[5] = 2.0 * E[0][1];
+  }
+  if (kind == 1) {  // GL: E += (T0^{-1} / detJ) M0(xi) alpha
+    for (int q = 0; q < na; ++q) {
+      double v = 2.0 * x[kF1[q]] - 1.0;
+      if (kF2[q] >= 0) v *= 2.0 * x[kF2[q]] - 1.0;
+      const double w = v / detJ * a.alpha[(size_t)q * ne + e];
+      for (int r = 0; r < 6; ++r) Ev[r] += w * a.eas_geo[(size_t)(6 * r + kRow[q]) * ne + e];
+    }
+  }
+  const double lam = a.lam_e ? a.lam_e[e] : a.lam, mu = a.mu_e ? a.mu_e[e] : a.mu;
+  double S[3][3];
+  if (a.material == 1) {
+    const double trE = Ev[0] + Ev[1] + Ev[2];
+    for (int v = 0; v < 6; ++v) {
+      const int i = voigt_a(v), j = voigt_b(v);
+      S[i][j] = S[j][i] = v < 3 ? lam * trE + 2.0 * mu * Ev[v] : mu * Ev[v];
+    }
+  } else {
+    double C[3][3], Ci[3][3];
+    C[0][0] = 2.0 * Ev[0] + 1.0, C[1][1] = 2.0 * Ev[1] + 1.0, C[2][2] = 2.0 * Ev[2] + 1.0;
+    C[1][2] = C[2][1] = Ev[3];
+    C[0][2] = C[2][0] = Ev[4];
+    C[0][1] = C[1][0] = Ev[5];
+    const double detC = inv3(C, Ci);
+    if (!(detC > 1e-10) && a.status) atomicOr(a.status, kStatusNonPositiveDetC);
+    const double lnJ = log(sqrt(detC));
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+  }
+  double R[3][3];
+  if (type == 0) {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) R[i][j] = S[i][j];
+  } else {
+    double F[3][3], FS[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) F[i][j] = H[i][j] + (i == j ? 1.0 : 0.0);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) FS[i][j] = F[i][0] * S[0][j] + F[i][1] * S[1][j] + F[i][2] * S[2][j];
+    const double scl = type == 2 ? 1.0 / det3(F) : 1.0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) R[i][j] = scl * (FS[i][0] * F[j][0] + FS[i][1] * F[j][1] + FS[i][2] * F[j][2]);
+  }
+  double* o = out + 6 * (size_t)k;
+  o[0] = R[0][0], o[1] = R[1][1], o[2] = R[2][2], o[3] = R[1][2], o[4] = R[0][2], o[5] = R[0][1];
+}
+
 }  // namespace
+
+void launch_eas_stress_at(const ElemArgs& a, int e0, int count, const double* xi, bool xi_per_elem, int type,
+                          double* out, cudaStream_t s) {
+  if (count <= 0) return;
+  eas_stress_at_kernel<<<(count + 127) / 128, 128, 0, s>>>(a, e0, count, xi, xi_per_elem ? 1 : 0, type, out);
+}
 
 int eas_geo_stride(int kind) { return kind == 1 ? 36 : (kind == 3 ? 34 : 10); }
 

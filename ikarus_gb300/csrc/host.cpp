@@ -406,7 +406,6 @@ int ikr_fe_calculate_at(ikr_fes fes, ikr_req req, int32_t result_type, int32_t e
     need(fes && req && req->fes == fes && local && out, IKR_ERR_ARG, "invalid arguments");
     need(result_type >= IKR_RESULT_PK2_STRESS && result_type <= IKR_RESULT_CAUCHY_STRESS, IKR_ERR_NOT_IMPLEMENTED,
          "result type not implemented");
-    need(fes->na == 0, IKR_ERR_NOT_IMPLEMENTED, "calculateAt is implemented for displacement-based elements");
     need(e_begin >= 0 && e_end <= fes->ne && e_begin <= e_end, IKR_ERR_ARG, "element range out of bounds");
     const int count = e_end - e_begin;
     if (count == 0) return;
@@ -416,7 +415,8 @@ int ikr_fe_calculate_at(ikr_fes fes, ikr_req req, int32_t result_type, int32_t e
     o.alloc(6 * (size_t)count);
     ikr::ElemArgs args = fes->args();
     args.u = req->u.p;
-    ikr::launch_stress_at(args, e_begin, count, xi.p, local_per_element != 0, result_type, o.p, s);
+    if (fes->na > 0) ikr::launch_eas_stress_at(args, e_begin, count, xi.p, local_per_element != 0, result_type, o.p, s);
+    else ikr::launch_stress_at(args, e_begin, count, xi.p, local_per_element != 0, result_type, o.p, s);
     ikr_host::count(1);
     o.download(out, 6 * (size_t)count, s);
     CK(cudaStreamSynchronize(s));

@@ -87,6 +87,9 @@ int eas_geo_stride(int eas_kind);
 // 2 Cauchy; 6 Voigt values per element
 void launch_stress_at(const ElemArgs& a, int e0, int count, const double* xi, bool xi_per_elem, int type, double* out,
                       cudaStream_t s);
+// the same for EAS elements with their stored alpha (element_eas.cu)
+void launch_eas_stress_at(const ElemArgs& a, int e0, int count, const double* xi, bool xi_per_elem, int type,
+                          double* out, cudaStream_t s);
 // one thread per loaded element: slot_elem[s] is the element, faces face_ptr[s]..face_ptr[s+1]-1
 void launch_traction_loads(const double* X, const int32_t* conn, int n_elems, int n_slots, const int32_t* slot_elem,
                            const int32_t* face_ptr, const int32_t* face_local, const double* traction, double* trac,

@@ -114,7 +114,8 @@ int ikr_fe_calculate_matrix(ikr_fes fes, ikr_req req, int32_t affordance, int32_
 /* calculateAt<ResultType> (nonlinearelastic.hh:237-271, feresulttypes.hh:125-133): stress of every element in
  * [e_begin, e_end) at a local point of the reference cube [0,1]^3 (local: 3 values per element when
  * local_per_element != 0, else 3 for all); out: 6 Voigt values per element [11, 22, 33, 23, 13, 12] without shear
- * factors (toVoigt(S, false)).  Displacement-based elements only (EAS sets: IKR_ERR_NOT_IMPLEMENTED). */
+ * factors (toVoigt(S, false)).  EAS element sets use their stored alpha (enhancedassumedstrains.hh:127-188): GL
+ * enhances the strain (F compatible), H9 / H9T the displacement gradient. */
 enum { IKR_RESULT_PK2_STRESS = 0, IKR_RESULT_KIRCHHOFF_STRESS = 1, IKR_RESULT_CAUCHY_STRESS = 2 };
 int ikr_fe_calculate_at(ikr_fes fes, ikr_req req, int32_t result_type, int32_t e_begin, int32_t e_end,
                         const double* local, int32_t local_per_element, double* out);

@@ -298,6 +298,40 @@ void gather(const orc_problem& p, int e, const double* u, double X[NN][3], doubl
   }
 }
 
+// Element-centre data of the enhanced-strain ansatz (helperfunctions.hh:19-36, linearandglstrains.hh:238-250,
+// displacementgradienttransposed.hh:336-369): centre geometry, T0^{-1} / detJ0 (GL), J0^{-T} (H, HT) and the
+// compatible deformation gradient at the centre (HT).
+struct EasCentre {
+  Geo g0;
+  double T0inv[6][6] = {};
+  double JIT0[3][3];
+  double Fc0[3][3];
+};
+void eas_centre(int kind, const double X[NN][3], const double ue[NN][3], EasCentre& ec) {
+  const double xc[3] = {0.5, 0.5, 0.5};
+  geometry(X, xc, ec.g0);
+  const Geo& g0 = ec.g0;
+  if (kind == ORC_EAS_GL) {
+    double T[6][6];
+    transformation_matrix(g0.J, T);
+    std::vector<double> A(36), B(36, 0.0);
+    for (int r = 0; r < 6; ++r)
+      for (int s = 0; s < 6; ++s) A[r * 6 + s] = T[r][s] * g0.detJ;
+    for (int r = 0; r < 6; ++r) B[r * 6 + r] = 1.0;
+    lu_solve(6, A, B.data(), 6);
+    for (int r = 0; r < 6; ++r)
+      for (int s = 0; s < 6; ++s) ec.T0inv[r][s] = B[r * 6 + s];
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) ec.JIT0[i][j] = g0.Jinv[j][i];  // jacobianInverseTransposed at the centre
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = (i == j) ? 1.0 : 0.0;
+      for (int v = 0; v < NN; ++v) s += ue[v][i] * g0.dNdX[v][j];
+      ec.Fc0[i][j] = s;
+    }
+}
+
 // Enhanced-strain element at the current (u, alpha): internal force, tangent, D, L, R~ and energy.
 // Restates NonLinearElastic::calculate{Vector,Matrix}Impl (nonlinearelastic.hh:375-430) and
 // EnhancedAssumedStrains::calculate{Vector,Matrix}Impl / calculateDAndLMatrix / calculateRtilde
@@ -312,31 +346,12 @@ void element_internal(const orc_problem& p, int e, const double* u, bool wantK, 
   out.ok = true;
 
   // centre data (helperfunctions.hh:19-36, displacementgradienttransposed.hh:336-369)
-  Geo g0;
-  const double xc[3] = {0.5, 0.5, 0.5};
-  geometry(X, xc, g0);
-  double T0inv[6][6] = {};
-  if (kind == ORC_EAS_GL) {
-    double T[6][6];
-    transformation_matrix(g0.J, T);
-    std::vector<double> A(36), B(36, 0.0);
-    for (int r = 0; r < 6; ++r)
-      for (int s = 0; s < 6; ++s) A[r * 6 + s] = T[r][s] * g0.detJ;
-    for (int r = 0; r < 6; ++r) B[r * 6 + r] = 1.0;
-    lu_solve(6, A, B.data(), 6);
-    for (int r = 0; r < 6; ++r)
-      for (int s = 0; s < 6; ++s) T0inv[r][s] = B[r * 6 + s];
-  }
-  double JIT0[3][3];  // jacobianInverseTransposed at the centre = J0^{-T}
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) JIT0[i][j] = g0.Jinv[j][i];
-  double Fc0[3][3];  // compatible deformation gradient at the centre (H9T)
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      double s = (i == j) ? 1.0 : 0.0;
-      for (int v = 0; v < NN; ++v) s += ue[v][i] * g0.dNdX[v][j];
-      Fc0[i][j] = s;
-    }
+  EasCentre ec;
+  eas_centre(kind, X, ue, ec);
+  const Geo& g0 = ec.g0;
+  const auto& T0inv = ec.T0inv;
+  const auto& JIT0 = ec.JIT0;
+  const auto& Fc0 = ec.Fc0;
 
   const Rule& R = gauss2();
   for (int q = 0; q < 8; ++q) {
@@ -994,7 +1009,6 @@ int orc_element_energy(orc_problem* p, int e, const double* u, double lambda, do
 // (stressconversions.hh:88-125); result in Voigt without shear factors [11, 22, 33, 23, 13, 12].
 int orc_calculate_at(orc_problem* p, int e, const double* u, int type, const double* xi, double* out6) {
   if (!p || e < 0 || e >= p->ne || !xi || !out6 || type < 0 || type > 2) return ORC_ERR_ARG;
-  if (p->na > 0) return ORC_ERR_NOT_IMPLEMENTED;
   double X[NN][3], ue[NN][3];
   gather(*p, e, u, X, ue);
   Geo g;
@@ -1007,7 +1021,45 @@ int orc_calculate_at(orc_problem* p, int e, const double* u, int type, const dou
       H[i][j] = s;
     }
   double Ev[6];
-  gl_strain(H, Ev);
+  const int na = p->na;
+  const int kind = na > 0 ? p->eas : ORC_EAS_NONE;
+  if (kind == ORC_EAS_NONE) {
+    gl_strain(H, Ev);
+  } else {
+    // EnhancedAssumedStrains::calculateAtImpl (enhancedassumedstrains.hh:127-188) with the stored alpha: GL adds
+    // M(xi) alpha to the strain of the compatible gradient (F stays compatible); H / HT enhance the gradient
+    const double* al = &p->alpha[(size_t)e * na];
+    EasCentre ec;
+    eas_centre(kind, X, ue, ec);
+    if (kind == ORC_EAS_GL) {
+      gl_strain(H, Ev);
+      for (int k = 0; k < na; ++k) {
+        const AnsatzEntry& a = kE21[k];
+        double v = 2.0 * xi[a.f1] - 1.0;
+        if (a.f2 >= 0) v *= 2.0 * xi[a.f2] - 1.0;
+        for (int r = 0; r < 6; ++r) Ev[r] += ec.T0inv[r][a.row] * v / g.detJ * al[k];
+      }
+    } else {
+      const double sc = ec.g0.detJ / g.detJ;
+      double Ht[3][3] = {};
+      for (int pm = 0; pm < na; ++pm) {
+        const int r = pm / 3, c = pm % 3;
+        const double val = 2.0 * xi[c] - 1.0;
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) Ht[i][j] += sc * ec.JIT0[i][r] * val * ec.JIT0[j][c] * al[pm];
+      }
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double add = Ht[i][j];
+          if (kind == ORC_EAS_HT) {
+            add = 0.0;
+            for (int k = 0; k < 3; ++k) add += ec.Fc0[i][k] * Ht[j][k];
+          }
+          H[i][j] += add;
+        }
+      gl_strain(H, Ev);
+    }
+  }
   MatState m;
   material_law(p->material, p->lam, p->mu, Ev, m, false);
   if (!m.ok) return ORC_ERR_NONPOSITIVE_DETC;

@@ -70,7 +70,8 @@ int orc_element_vector(orc_problem* p, int e, const double* u, double lambda, do
 int orc_element_matrix(orc_problem* p, int e, const double* u, double lambda, double* out576_colmajor);
 int orc_element_energy(orc_problem* p, int e, const double* u, double lambda, double* energy);
 /* calculateAt (nonlinearelastic.hh:237-271): type 0 PK2, 1 Kirchhoff, 2 Cauchy stress of element e at local xi,
- * Voigt [11,22,33,23,13,12] without shear factors; displacement-based elements only (else NOT_IMPLEMENTED) */
+ * Voigt [11,22,33,23,13,12] without shear factors; EAS elements (enhancedassumedstrains.hh:127-188) use the stored
+ * alpha: GL adds M(xi) alpha to the strain (F compatible), H / HT enhance the displacement gradient */
 int orc_calculate_at(orc_problem* p, int e, const double* u, int type, const double* xi, double* out6);
 int orc_update_state(orc_problem* p, const double* u, double lambda, const double* correction);
 

@@ -13,6 +13,10 @@ Sources:
                                                subsidiary function, DisplacementControl, ArcLength with
                                                inhomogeneous Dirichlet values): iterations per solve, final
                                                (u, w) (per step for the load control), final lambda
+  tests/src/teststresscomputation.cpp:29-47, 150-200, 245-250
+                                               displacement-based "Q1" stresses (PK2, Kirchhoff, Cauchy) of
+                                               the unit-square element under planeStrain(StVenantKirchhoff(E =
+                                               1000, nu = 0.49)) at the displacement d and the local position
 """
 import json
 import os
@@ -49,6 +53,17 @@ def main():
     main_src = pf_src[pf_src.index("int main"):]
     step = float(re.search(r"stepSize = ([0-9.e+-]+);", main_src).group(1))
     steps = int(re.search(r"loadSteps\s*= (\d+);", main_src).group(1))
+    st_src = open(os.path.join(REF, "tests/src/teststresscomputation.cpp")).read()
+    blk = st_src[st_src.index('elementType == "Q1")'):]
+    blk = blk[: blk.index("return std::make_tuple")]
+    mats = re.findall(r"MatrixType\{\s*\{([^}]*)\},\s*\{([^}]*)\}\s*\}", blk)
+    to_m = lambda m: [[float(x) for x in row.split(",")] for row in m]
+    d_line = re.search(r"else\s*d << ([^;]*);", st_src).group(1)
+    pos = [float(x) for x in re.search(r"FieldVector<double, 2> pos\{([^}]*)\}", st_src).group(1).split(",")]
+    mp = re.search(r"emodul = ([0-9.]+), \.nu = ([0-9.]+)", st_src)
+    stress = {"source": "tests/src/teststresscomputation.cpp", "element": "Q1 (2D, unit square, planeStrain SVK)",
+              "E": float(mp.group(1)), "nu": float(mp.group(2)), "d": [float(x) for x in d_line.split(",")],
+              "position": pos, "PK2": to_m(mats[0]), "kirchhoff": to_m(mats[1]), "cauchy": to_m(mats[2])}
     data = {
         "source": "ikarus-project/ikarus tests/src/testcantileverbeamEAS.cpp:60-96, testcantileverbeam.hh:42-198, "
                   "testcommon.hh:199-207",
@@ -58,6 +73,7 @@ def main():
                                              "DisplacementGradientTransposed": 9},
                           "results": goldens},
         "fixed_distortion_3d": offsets,
+        "stress_q1_plane_strain_svk": stress,
         "path_following_2dof": {"source": "tests/src/testpathfollowing.cpp", "step_size": step, "load_steps": steps,
                                 "tol": 1e-8, "max_iter": 20, "cases": pf},
     }

@@ -343,8 +343,7 @@ def test_inhomogeneous_dirichlet_values_match_oracle(ikr, eas, n):
 
 def test_calculate_at_stresses_match_oracle(ikr):
     """calculateAt<PK2Stress / kirchhoffStress / cauchyStress> (nonlinearelastic.hh:237-271) at random local
-    points of every element, FP64 within 1e-12 of the oracle; zero at the undeformed state; EAS sets report
-    NotImplemented."""
+    points of every element, FP64 within 1e-12 of the oracle; zero at the undeformed state."""
     p = problems.cantilever(4, 3, 2, L=4.0, jitter=0.15, seed=9)
     fes, asm = problems.build_gpu(p)
     o = oracle.from_problem(p)
@@ -360,10 +359,50 @@ def test_calculate_at_stresses_match_oracle(ikr):
         ref_c = np.array([o.calculate_at(e, u, int(rt)) for e in range(2, 5)])
         assert rel_err(centre, ref_c) <= FP64_RTOL
     assert np.abs(ikr.calculateAt(fes, ikr.FERequirements(fes), ikr.ResultTypes.cauchyStress)).max() == 0.0
-    pe = problems.cantilever(2, 1, 1, eas=1, n_eas=9)
-    fe_eas, _ = problems.build_gpu(pe)
-    with pytest.raises(ikr.IkarusError, match="NOT_IMPLEMENTED"):
-        ikr.calculateAt(fe_eas, ikr.FERequirements(fe_eas), ikr.ResultTypes.PK2Stress)
+
+
+@pytest.mark.parametrize("material", [0, 1], ids=["NeoHooke", "SVK"])
+@pytest.mark.parametrize("eas,n", [(1, 9), (1, 21), (2, 9), (3, 9)])
+def test_eas_calculate_at_matches_oracle(ikr, eas, n, material):
+    """calculateAt of EAS elements (enhancedassumedstrains.hh:127-188) with a stored alpha: the GL ansatz enhances
+    the strain, H9 / H9T the displacement gradient (and with it F); FP64 within 1e-12 of the oracle."""
+    p = problems.cantilever(4, 3, 2, L=4.0, jitter=0.15, seed=9, eas=eas, n_eas=n)
+    p.material = material
+    fes, asm = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    rng = np.random.default_rng(21)
+    u = 0.01 * rng.standard_normal(p.n_dofs)
+    alpha = alpha_scale(eas) * rng.standard_normal((p.mesh.n_elems, n))
+    fes.alpha = alpha
+    o.alpha = alpha
+    req = ikr.FERequirements(fes, u, 0.0)
+    local = rng.uniform(0.0, 1.0, (p.mesh.n_elems, 3))
+    for rt in ikr.ResultTypes:
+        got = ikr.calculateAt(fes, req, rt, local)
+        ref = np.array([o.calculate_at(e, u, int(rt), local[e]) for e in range(p.mesh.n_elems)])
+        assert rel_err(got, ref) <= FP64_RTOL, rt
+
+
+def test_calculate_at_reproduces_reference_q1_stresses(ikr):
+    """tests/src/teststresscomputation.cpp ("Q1"): planeStrain(StVenantKirchhoff(E = 1000, nu = 0.49)) on the unit
+    square with the test's nodal displacements, PK2 / Kirchhoff / Cauchy stress at the test's local point.  The hex
+    extruded along z with the in-plane displacements on both faces and w = 0 has F33 = 1, so its in-plane stresses
+    are the plane-strain ones (the golden's own tolerance is 1e-8; met to 1e-12)."""
+    g = GOLD["stress_q1_plane_strain_svk"]
+    p = problems.single_element(None, E=g["E"], nu=g["nu"])
+    p.material = 1
+    fes, _ = problems.build_gpu(p)
+    d = np.asarray(g["d"]).reshape(4, 2)
+    u = np.zeros(24)
+    for v in range(8):
+        u[3 * v:3 * v + 2] = d[v & 3]
+    req = ikr.FERequirements(fes, u, 0.0)
+    loc = (g["position"][0], g["position"][1], 0.5)
+    for rt, key in zip(ikr.ResultTypes, ("PK2", "kirchhoff", "cauchy")):
+        r = ikr.calculateAt(fes, req, rt, loc)[0]
+        got = np.array([[r[0], r[5]], [r[5], r[1]]])
+        want = np.asarray(g[key])
+        assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max(), key
 
 
 @pytest.mark.parametrize("eas,n", [(0, 0), (1, 9), (2, 9)])

@@ -283,3 +283,36 @@ def test_oracle_arc_length_constraint_and_equilibrium():
         dd = us[k] - us[k - 1]
         dl = lams[k] - lams[k - 1]
         assert abs(np.sqrt(dd @ dd + psi * psi * dl * dl) - s) <= 1e-10
+
+
+def test_oracle_stresses_reproduce_reference_q1_goldens():
+    """tests/src/teststresscomputation.cpp ("Q1", planeStrain(StVenantKirchhoff(E = 1000, nu = 0.49)), unit square,
+    the test's displacements and local point): the extruded hex (in-plane displacements on both faces, w = 0, so
+    F33 = 1 and the in-plane stresses are the plane-strain ones) reproduces PK2, Kirchhoff and Cauchy stress."""
+    g = GOLD["stress_q1_plane_strain_svk"]
+    p = problems.single_element(None, E=g["E"], nu=g["nu"])
+    o = oracle.from_problem(p)
+    o.set_material(oracle.MATERIAL_SVK)
+    d = np.asarray(g["d"]).reshape(4, 2)
+    u = np.zeros(24)
+    for v in range(8):
+        u[3 * v:3 * v + 2] = d[v & 3]
+    for t, key in enumerate(("PK2", "kirchhoff", "cauchy")):
+        r = o.calculate_at(0, u, t, (g["position"][0], g["position"][1], 0.5))
+        got = np.array([[r[0], r[5]], [r[5], r[1]]])
+        want = np.asarray(g[key])
+        assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max(), key
+
+
+@pytest.mark.parametrize("eas,n", [(1, 9), (2, 9), (3, 9)])
+def test_oracle_eas_stresses_at_zero_alpha_are_the_displacement_ones(eas, n):
+    """With alpha = 0 the enhanced element's calculateAt is the displacement-based one (EAS(0) = NonLinearElastic,
+    testnonlineareas.cpp:145-189 for the element quantities)."""
+    p = problems.cantilever(3, 2, 2, L=3.0, jitter=0.1, seed=5)
+    pe = problems.cantilever(3, 2, 2, L=3.0, jitter=0.1, seed=5, eas=eas, n_eas=n)
+    o, oe = oracle.from_problem(p), oracle.from_problem(pe)
+    u = 0.02 * np.random.default_rng(3).standard_normal(p.n_dofs)
+    for e in range(p.mesh.n_elems):
+        for t in range(3):
+            np.testing.assert_allclose(oe.calculate_at(e, u, t, (0.3, 0.6, 0.2)), o.calculate_at(e, u, t, (0.3, 0.6, 0.2)),
+                                       rtol=1e-13, atol=1e-13)
