@@ -283,6 +283,18 @@ class StVenantKirchhoff:
         return cls(*toLamesFirstParameterAndShearModulus(E, nu))
 
 
+@dataclass
+class BlatzKo:
+    """Blatz-Ko law W = mu/2 (sum 1/lambda_i^2 + 2 lambda_1 lambda_2 lambda_3 - 5) on the total principal stretches,
+    no volumetric part (materials/hyperelastic/deviatoric/blatzko.hh, factory.hh:34-39 makeBlatzKo(mu))."""
+    mu: float
+    kind = 2
+
+    @property
+    def lambda_(self):
+        return 0.0
+
+
 # ---- finite elements -------------------------------------------------------------------------------------
 class FiniteElements:
     """All elements of one Q1 hexahedral mesh with skills nonLinearElastic(NeoHooke) [+ eas<ES>(n)]

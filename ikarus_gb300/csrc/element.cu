@@ -27,7 +27,8 @@ namespace ikr {
 namespace {
 
 // EPB elements per block (8 lanes each): 16, 32 or 64, chosen per element set by timing (host.cpp)
-// MAT 0: NeoHooke (neohooke.hh:78-142); MAT 1: StVenantKirchhoff (svk.hh:63-163)
+// MAT 0: NeoHooke (neohooke.hh:78-142); MAT 1: StVenantKirchhoff (svk.hh:63-163); MAT 2: BlatzKo
+// (hyperelastic/deviatoric/blatzko.hh with total stretches and no volumetric part, factory.hh:34-39)
 template <typename KT, int MODE, int EPB, int MAT = 0>
 __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const int32_t* __restrict__ list, int n_list,
                                                                int e_base) {
@@ -171,11 +172,60 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
     const KT detF = inv3(F, Fi);
     // det C = det(F)^2 must exceed 1e-10 (checkPositiveOrAbort); NaN fails the test as well
     if (!(detF * detF > KT(1e-10)) || !(detF > KT(0))) bad |= kStatusNonPositiveDetC;
-    const KT lnJ = log(detF);
     const KT w = KT(kGaussW) * detJ;
     KT g[3];  // F^{-T} grad N_I
 #pragma unroll
     for (int k = 0; k < 3; ++k) g[k] = Fi[0][k] * dN[0] + Fi[1][k] * dN[1] + Fi[2][k] * dN[2];
+    if constexpr (MAT == 2) {
+      // BlatzKo, W = mu/2 (tr C^-1 + 2 J - 5) (the principal-stretch form sum 1/lambda_i^2 + 2 lambda_1 lambda_2
+      // lambda_3 written with invariants): P = mu (J I - b^-1) F^-T, b^-1 = F^-T F^-1; with g = F^-T grad N:
+      // K_IJ = w mu [J (g_I (x) g_J - g_J (x) g_I) + g_J (x) b^-1 g_I + (g_I . g_J) b^-1 + b^-1 g_J (x) g_I]
+      KT binv[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) binv[i][k] = Fi[0][i] * Fi[0][k] + Fi[1][i] * Fi[1][k] + Fi[2][i] * Fi[2][k];
+      KT bg[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) bg[i] = binv[i][0] * g[0] + binv[i][1] * g[1] + binv[i][2] * g[2];
+      if (WANT_R) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) f[i] += double(w * mu * (detF * g[i] - bg[i]));
+      }
+      if (WANT_E && sub == 0) {
+        const KT trCi = binv[0][0] + binv[1][1] + binv[2][2];
+        psi += double(w * (mu / KT(2) * (trCi + KT(2) * detF - KT(5))));
+      }
+      if (WANT_K) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          sh[es][sub][k] = g[k];
+          sh[es][sub][3 + k] = bg[k];
+        }
+        __syncwarp();
+        const KT wm = w * mu, wj = w * mu * detF;
+#pragma unroll
+        for (int d = 0; d < 5; ++d) {
+          const int Jn = (sub + d) & 7;
+          KT gJ[3], bgJ[3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            gJ[k] = sh[es][Jn][k];
+            bgJ[k] = sh[es][Jn][3 + k];
+          }
+          const KT gg = wm * (g[0] * gJ[0] + g[1] * gJ[1] + g[2] * gJ[2]);
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              Kacc[d][i][j] += wj * (g[i] * gJ[j] - gJ[i] * g[j]) + wm * (gJ[i] * bg[j] + bgJ[i] * g[j]) +
+                               gg * binv[i][j];
+        }
+        __syncwarp();
+      }
+      continue;
+    }
+    const KT lnJ = log(detF);
 
     if (WANT_R) {
       // P = mu (F - F^{-T}) + lambda ln J F^{-T}: written with F - F^{-T} so the undeformed state gives an
@@ -425,6 +475,21 @@ __global__ void __launch_bounds__(EPB * 8) disp_residual_gp_kernel(ElemArgs a, c
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) P[i][j] = w * (F[i][0] * S[0][j] + F[i][1] * S[1][j] + F[i][2] * S[2][j]);
+  } else if (a.material == 2) {
+    // BlatzKo: P = mu (J I - b^-1) F^-T = mu (J F^-T - F^-T F^-1 F^-T)
+    double Fi[3][3];
+    const double detF = inv3(F, Fi);
+    if (!(detF * detF > 1e-10) || !(detF > 0.0)) bad |= kStatusNonPositiveDetC;
+    double binv[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) binv[i][k] = Fi[0][i] * Fi[0][k] + Fi[1][i] * Fi[1][k] + Fi[2][i] * Fi[2][k];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        P[i][j] = w * mu * (detF * Fi[j][i] - (binv[i][0] * Fi[j][0] + binv[i][1] * Fi[j][1] + binv[i][2] * Fi[j][2]));
   } else {
     double Fi[3][3];
     const double detF = inv3(F, Fi);
@@ -542,11 +607,20 @@ __global__ void stress_at_kernel(ElemArgs a, int e0, int count, const double* __
     double Ci[3][3];
     const double detC = inv3(C, Ci);
     if (!(detC > 1e-10) && a.status) atomicOr(a.status, kStatusNonPositiveDetC);
-    const double lnJ = log(sqrt(detC));
+    if (a.material == 2) {  // BlatzKo: S = mu (J C^-1 - C^-2)
+      const double Jd = sqrt(detC);
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+      for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+        for (int j = 0; j < 3; ++j)
+          S[i][j] = mu * (Jd * Ci[i][j] - (Ci[i][0] * Ci[0][j] + Ci[i][1] * Ci[1][j] + Ci[i][2] * Ci[2][j]));
+    } else {
+      const double lnJ = log(sqrt(detC));
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+    }
   }
   double R[3][3];
   if (type == 0) {
@@ -583,6 +657,7 @@ void launch_disp_epb(const ElemArgs& a, const int32_t* list, int n_list, int e_b
 template <typename KT, int MODE>
 void launch_disp_t(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
   if (a.material == 1) return launch_disp_epb<KT, MODE, 32, 1>(a, list, n_list, e_base, s);  // SVK: one shape
+  if (a.material == 2) return launch_disp_epb<KT, MODE, 32, 2>(a, list, n_list, e_base, s);  // BlatzKo: one shape
   if constexpr ((MODE & kElemOut) == 0) {
     if (a.epb == 16) return launch_disp_epb<KT, MODE, 16>(a, list, n_list, e_base, s);
     if (a.epb == 64) return launch_disp_epb<KT, MODE, 64>(a, list, n_list, e_base, s);

@@ -265,6 +265,34 @@ __global__ void __launch_bounds__(EasCfg<NA>::EPB * 8) eas_element_kernel(ElemAr
         const int r = t / 6, c = t % 6;
         sm[Cfg::O_C6 + t] = (r < 3 && c < 3 ? lam : 0.0) + (r == c ? (r < 3 ? 2.0 * mu : mu) : 0.0);
       }
+    } else if (a.material == 2) {
+      // BlatzKo on C = 2E + I: S = mu (J C^-1 - C^-2), moduli mu [J Ci_ij Ci_kl - J (Ci_ik Ci_jl + Ci_il Ci_jk)
+      // + Ci_ik Ci2_jl + Ci_il Ci2_jk + Ci2_ik Ci_jl + Ci2_il Ci_jk] with Ci2 = C^-2
+      double C[3][3], Ci[3][3], Ci2[3][3];
+      C[0][0] = 2.0 * Ev[0] + 1.0, C[1][1] = 2.0 * Ev[1] + 1.0, C[2][2] = 2.0 * Ev[2] + 1.0;
+      C[1][2] = C[2][1] = Ev[3];
+      C[0][2] = C[2][0] = Ev[4];
+      C[0][1] = C[1][0] = Ev[5];
+      const double detC = inv3(C, Ci);
+      if (!(detC > 1e-10)) bad |= kStatusNonPositiveDetC;
+      const double Jd = sqrt(detC);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Ci2[i][j] = Ci[i][0] * Ci[0][j] + Ci[i][1] * Ci[1][j] + Ci[i][2] * Ci[2][j];
+#pragma unroll
+      for (int v = 0; v < 6; ++v) {
+        const int i = voigt_a(v), j = voigt_b(v);
+        S[v] = mu * (Jd * Ci[i][j] - Ci2[i][j]);
+        Sm[i][j] = Sm[j][i] = S[v];
+      }
+      for (int t = sub; t < 36; t += 8) {
+        const int r = t / 6, c = t % 6;
+        const int i = voigt_a(r), j = voigt_b(r), k = voigt_a(c), l = voigt_b(c);
+        sm[Cfg::O_C6 + t] = mu * (Jd * Ci[i][j] * Ci[k][l] - Jd * (Ci[i][k] * Ci[j][l] + Ci[i][l] * Ci[j][k]) +
+                                  Ci[i][k] * Ci2[j][l] + Ci[i][l] * Ci2[j][k] + Ci2[i][k] * Ci[j][l] +
+                                  Ci2[i][l] * Ci[j][k]);
+      }
     } else {
       // NeoHooke on C = 2E + I (neohooke.hh:100-142)
       double C[3][3], Ci[3][3];
@@ -837,9 +865,16 @@ __global__ void eas_stress_at_kernel(ElemArgs a, int e0, int count, const double
     C[0][1] = C[1][0] = Ev[5];
     const double detC = inv3(C, Ci);
     if (!(detC > 1e-10) && a.status) atomicOr(a.status, kStatusNonPositiveDetC);
-    const double lnJ = log(sqrt(detC));
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+    if (a.material == 2) {  // BlatzKo
+      const double Jd = sqrt(detC);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          S[i][j] = mu * (Jd * Ci[i][j] - (Ci[i][0] * Ci[0][j] + Ci[i][1] * Ci[1][j] + Ci[i][2] * Ci[2][j]));
+    } else {
+      const double lnJ = log(sqrt(detC));
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+    }
   }
   double R[3][3];
   if (type == 0) {

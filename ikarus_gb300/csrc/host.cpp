@@ -786,8 +786,8 @@ int ikr_assembler_set_dirichlet_values(ikr_asm a, const double* rate) {
 int ikr_fes_set_material(ikr_fes fes, int32_t material) {
   return guarded([&] {
     need(fes, IKR_ERR_ARG, "null argument");
-    need(material == IKR_MATERIAL_NEOHOOKE || material == IKR_MATERIAL_SVK, IKR_ERR_NOT_IMPLEMENTED,
-         "material not implemented");
+    need(material == IKR_MATERIAL_NEOHOOKE || material == IKR_MATERIAL_SVK || material == IKR_MATERIAL_BLATZKO,
+         IKR_ERR_NOT_IMPLEMENTED, "material not implemented");
     fes->material = material;
     fes->alpha_version++;  // cached EAS condensation data depend on the material
   });

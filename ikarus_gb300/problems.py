@@ -44,12 +44,12 @@ class Problem:
 
 
 def cantilever_golden(eas: int, n_eas: int, nx=10, ny=1, nz=1, material=0) -> Problem:
-    """tests/src/testcantileverbeam.hh:42-198 in 3D: YaspGrid 10x1x1 on (10, 2, 2), E = 100, nu = 0.3, clamped at
-    x = 0, manipulator point loads R[y-dof] += lambda at the vertices (10,2,2) and (10,2,0), 20 load steps,
-    ||R|| < 1e-10 (testcantileverbeamEAS.cpp:60-124)."""
+    """tests/src/testcantileverbeam.hh:42-198 in 3D: YaspGrid 10x1x1 on (10, 2, 2), E = 100, nu = 0.3 (BlatzKo:
+    mu = 40, testcantileverbeamEAS.cpp:101-104), clamped at x = 0, manipulator point loads R[y-dof] += lambda at
+    the vertices (10,2,2) and (10,2,0), 20 load steps, ||R|| < 1e-10 (testcantileverbeamEAS.cpp:60-124)."""
     L, h = 10.0, 2.0
     m = structured_hex_grid(nx, ny, nz, (L, h, h))
-    lam, mu = lame(100.0, 0.3)
+    lam, mu = lame(100.0, 0.3) if material != 2 else (0.0, 40.0)
     fixed = fixed_dofs_where(m, lambda X: np.abs(X[:, 0]) < 1e-8)
     dofs = np.array([3 * vertex_at(m, (L, h, h)) + 1, 3 * vertex_at(m, (L, h, 0.0)) + 1], dtype=np.int32)
     return Problem(f"cantilever_golden_eas{eas}_{n_eas}", m, lam, mu, eas, n_eas, fixed, pl_dofs=dofs,
@@ -208,9 +208,11 @@ def single_element(offsets=None, E=1000.0, nu=0.3, eas=0, n_eas=0) -> Problem:
 
 def build_gpu(p: Problem, precision=0):
     """GPU objects for a problem: (FiniteElements, SparseFlatAssembler)."""
-    from . import FiniteElements, NeoHooke, Precision, SparseFlatAssembler, StVenantKirchhoff
-    law = StVenantKirchhoff if getattr(p, "material", 0) == 1 else NeoHooke
-    fes = FiniteElements(p.mesh.coords, p.mesh.conn, law(p.lam, p.mu), p.eas, p.n_eas)
+    from . import BlatzKo, FiniteElements, NeoHooke, Precision, SparseFlatAssembler, StVenantKirchhoff
+    material = getattr(p, "material", 0)
+    law = {0: lambda: NeoHooke(p.lam, p.mu), 1: lambda: StVenantKirchhoff(p.lam, p.mu),
+           2: lambda: BlatzKo(p.mu)}[material]()
+    fes = FiniteElements(p.mesh.coords, p.mesh.conn, law, p.eas, p.n_eas)
     if p.face_elem is not None and len(p.face_elem):
         fes.add_neumann(p.face_elem, p.face_local, p.face_traction)
     asm = SparseFlatAssembler(fes, p.fixed, Precision(precision))

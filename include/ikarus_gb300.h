@@ -207,8 +207,10 @@ int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fr
 int ikr_linear_solver_set_multi_rhs(ikr_ls ls, int32_t on);
 int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* spmv_kind, double* l2_keep_fraction, double* spmv_us);
 /* material law of all elements (the reference's Material template argument of makeFE): NeoHooke (default,
- * neohooke.hh) or StVenantKirchhoff (svk.hh); both with the Lame parameters given at creation */
-enum { IKR_MATERIAL_NEOHOOKE = 0, IKR_MATERIAL_SVK = 1 };
+ * neohooke.hh) or StVenantKirchhoff (svk.hh), both with the Lame parameters given at creation, or BlatzKo
+ * (makeBlatzKo(mu), hyperelastic/factory.hh:34-39: deviatoric function on the total principal stretches, no
+ * volumetric part) with the shear modulus given at creation (the first Lame parameter is not used) */
+enum { IKR_MATERIAL_NEOHOOKE = 0, IKR_MATERIAL_SVK = 1, IKR_MATERIAL_BLATZKO = 2 };
 int ikr_fes_set_material(ikr_fes fes, int32_t material);
 /* elements per block the displacement element kernel uses for residual / FP64 tangent / FP32 tangent
  * assembly (16, 32 or 64, chosen by timing at the first assembly of each kind; 0 = not assembled yet; no

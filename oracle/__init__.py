@@ -19,7 +19,7 @@ _lib = None
 EAS_NONE, EAS_GL, EAS_H, EAS_HT = 0, 1, 2, 3
 DBC_RAW, DBC_REDUCED, DBC_FULL = 0, 1, 2
 SOLVER_BANDED_LDLT, SOLVER_CG_JACOBI = 0, 1
-MATERIAL_NEOHOOKE, MATERIAL_SVK = 0, 1
+MATERIAL_NEOHOOKE, MATERIAL_SVK, MATERIAL_BLATZKO = 0, 1, 2
 PF_ARC_LENGTH, PF_LOAD_CONTROL, PF_DISPLACEMENT_CONTROL = 0, 1, 2
 ERRORS = {-1: "ARG", -2: "NOT_IMPLEMENTED", -3: "NONPOSITIVE_DETC", -4: "SINGULAR", -5: "NOT_CONVERGED"}
 

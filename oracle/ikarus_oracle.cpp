@@ -199,8 +199,42 @@ void svk(double lam, double mu, const double Ev[6], MatState& m, bool wantTangen
   for (int r = 0; r < 6; ++r)
     for (int c = 0; c < 6; ++c) m.C6[r][c] = (r < 3 && c < 3 ? lam : 0.0) + (r == c ? (r < 3 ? 2.0 * mu : mu) : 0.0);
 }
+// BlatzKo (hyperelastic/deviatoric/blatzko.hh, makeBlatzKo(mu) in factory.hh:34-39: a deviatoric function of the
+// total principal stretches with no volumetric part): W = mu/2 (sum 1/lambda_i^2 + 2 lambda_1 lambda_2 lambda_3 - 5)
+// = mu/2 (tr C^-1 + 2 J - 5).  S = 2 dW/dC = mu (J C^-1 - C^-2); C = 2 dS/dC =
+// mu [J Ci_ij Ci_kl - J (Ci_ik Ci_jl + Ci_il Ci_jk) + Ci_ik Ci2_jl + Ci_il Ci2_jk + Ci2_ik Ci_jl + Ci2_il Ci_jk].
+// The same functions of C as the reference's principal-stretch evaluation (spectral form), without the eigen
+// decomposition; det C checked as in Hyperelastic::detF (hyperelastic/interface.hh:249-250).
+void blatzko(double mu, const double Ev[6], MatState& m, bool wantTangent = true) {
+  double C[3][3];
+  for (int i = 0; i < 3; ++i) C[i][i] = 2.0 * Ev[i] + 1.0;
+  C[1][2] = C[2][1] = Ev[3];
+  C[0][2] = C[2][0] = Ev[4];
+  C[0][1] = C[1][0] = Ev[5];
+  double Ci[3][3], detC;
+  inv3(C, Ci, &detC);
+  m.ok = detC > 1e-10;
+  const double J = std::sqrt(detC);
+  double Ci2[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Ci2[i][j] = Ci[i][0] * Ci[0][j] + Ci[i][1] * Ci[1][j] + Ci[i][2] * Ci[2][j];
+  m.psi = mu / 2.0 * (Ci[0][0] + Ci[1][1] + Ci[2][2] + 2.0 * J - 5.0);
+  for (int v = 0; v < 6; ++v) {
+    const int i = VA[v], j = VB[v];
+    m.S[v] = mu * (J * Ci[i][j] - Ci2[i][j]);
+  }
+  if (!wantTangent) return;
+  for (int r = 0; r < 6; ++r)
+    for (int s = 0; s < 6; ++s) {
+      const int i = VA[r], j = VB[r], k = VA[s], l = VB[s];
+      m.C6[r][s] = mu * (J * Ci[i][j] * Ci[k][l] - J * (Ci[i][k] * Ci[j][l] + Ci[i][l] * Ci[j][k]) +
+                         Ci[i][k] * Ci2[j][l] + Ci[i][l] * Ci2[j][k] + Ci2[i][k] * Ci[j][l] + Ci2[i][l] * Ci[j][k]);
+    }
+}
+
 void material_law(int material, double lam, double mu, const double Ev[6], MatState& m, bool wantTangent = true) {
   if (material == ORC_MATERIAL_SVK) svk(lam, mu, Ev, m, wantTangent);
+  else if (material == ORC_MATERIAL_BLATZKO) blatzko(mu, Ev, m, wantTangent);
   else neohooke(lam, mu, Ev, m, wantTangent);
 }
 
@@ -924,7 +958,7 @@ orc_problem* orc_problem_create(int n_nodes, const double* coords, int n_elems, 
 }
 void orc_problem_destroy(orc_problem* p) { delete p; }
 int orc_set_material(orc_problem* p, int material) {
-  if (!p || (material != ORC_MATERIAL_NEOHOOKE && material != ORC_MATERIAL_SVK)) return ORC_ERR_ARG;
+  if (!p || material < ORC_MATERIAL_NEOHOOKE || material > ORC_MATERIAL_BLATZKO) return ORC_ERR_ARG;
   p->material = material;
   return ORC_OK;
 }

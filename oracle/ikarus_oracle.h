@@ -37,7 +37,7 @@ enum {
 enum { ORC_EAS_NONE = 0, ORC_EAS_GL = 1, ORC_EAS_H = 2, ORC_EAS_HT = 3 };
 /* DBCOption (ikarus/assembler/dirichletbcenforcement.hh:8) */
 enum { ORC_DBC_RAW = 0, ORC_DBC_REDUCED = 1, ORC_DBC_FULL = 2 };
-enum { ORC_MATERIAL_NEOHOOKE = 0, ORC_MATERIAL_SVK = 1 };
+enum { ORC_MATERIAL_NEOHOOKE = 0, ORC_MATERIAL_SVK = 1, ORC_MATERIAL_BLATZKO = 2 };
 /* linear solvers of the oracle */
 enum { ORC_SOLVER_BANDED_LDLT = 0, ORC_SOLVER_CG_JACOBI = 1 };
 
@@ -46,7 +46,8 @@ typedef struct orc_problem orc_problem;
 orc_problem* orc_problem_create(int n_nodes, const double* coords, int n_elems, const int32_t* conn,
                                 double lambda, double mu, int eas_kind, int n_alpha);
 void orc_problem_destroy(orc_problem* p);
-/* material law of all elements: NeoHooke (default, neohooke.hh) or StVenantKirchhoff (svk.hh) */
+/* material law of all elements: NeoHooke (default, neohooke.hh), StVenantKirchhoff (svk.hh) or BlatzKo
+ * (makeBlatzKo(mu), hyperelastic/factory.hh:34-39; uses mu only) */
 int orc_set_material(orc_problem* p, int material);
 int orc_set_dirichlet(orc_problem* p, const uint8_t* fixed_dofs);
 /* Dead Neumann load on element faces (Dune face numbering: 2d -> xi_d = 0, 2d+1 -> xi_d = 1).

@@ -6,7 +6,7 @@ the tests never read the reference at run time.
 Sources:
   tests/src/testcantileverbeamEAS.cpp:60-96   3D cantilever (NR + LoadControl + SparseFlatAssembler + EAS):
                                                (total Newton iterations, max |d|) per enhanced strain & material
-  tests/src/testcantileverbeamEAS.cpp:101     material parameters (E = 100, nu = 0.3)
+  tests/src/testcantileverbeamEAS.cpp:101-104 material parameters (E = 100, nu = 0.3; BlatzKo mu = 40)
   tests/src/testcantileverbeam.hh:42-53, 96-151  mesh 10x1x1 on (L, h, h) = (10, 2, 2), tol 1e-10, 20 steps
   tests/src/testcommon.hh:199-207             fixed corner distortion of the single-element tests
   tests/src/testpathfollowing.cpp:41-370      two-dof operator under PathFollowing (ArcLength, LoadControl
@@ -34,8 +34,10 @@ def main():
     goldens = {}
     for es_block in re.split(r"std::same_as<ES, EAS::", body)[1:]:
         es = es_block.split(">")[0]
-        for mat, it, md in re.findall(r"is_same_v<MAT, ([^>]+(?:>[^>]*>)*?)>\)\s*\{\s*return std::make_pair\((\d+), ([0-9.e+-]+)\)", es_block):
-            goldens.setdefault(es, {})[mat.strip()] = {"iterations": int(it), "max_disp": float(md)}
+        for mat, it, md in re.findall(r"is_same_v<MAT, (.+?)>\)\s*\{\s*return std::make_pair\((\d+), ([0-9.e+-]+)\)", es_block):
+            name = "BlatzKo" if "BlatzKo" in mat else mat.strip()
+            goldens.setdefault(es, {})[name] = {"iterations": int(it), "max_disp": float(md)}
+    blatzko_mu = float(re.search(r"makeBlatzKo\(([0-9.]+)\)", src).group(1))
     common = open(os.path.join(REF, "tests/src/testcommon.hh")).read()
     blk = common[common.index("if constexpr (gridDim == 3)", common.index("fixedDistorted")):]
     blk = blk[: blk.index("} else")]
@@ -71,7 +73,7 @@ def main():
                           "tol": 1e-10, "point_load_nodes": [[10.0, 2.0, 2.0], [10.0, 2.0, 0.0]],
                           "eas_parameters": {"GreenLagrangeStrain": 21, "DisplacementGradient": 9,
                                              "DisplacementGradientTransposed": 9},
-                          "results": goldens},
+                          "blatzko_mu": blatzko_mu, "results": goldens},
         "fixed_distortion_3d": offsets,
         "stress_q1_plane_strain_svk": stress,
         "path_following_2dof": {"source": "tests/src/testpathfollowing.cpp", "step_size": step, "load_steps": steps,

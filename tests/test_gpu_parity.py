@@ -206,15 +206,16 @@ def test_linear_solver(ikr):
     assert 0 < it and rel <= 1e-12
 
 
-@pytest.mark.parametrize("material", ["NeoHooke", "StVenantKirchhoff"])
+@pytest.mark.parametrize("material", ["NeoHooke", "StVenantKirchhoff", "BlatzKo"])
 @pytest.mark.parametrize("es", ["GreenLagrangeStrain", "DisplacementGradient", "DisplacementGradientTransposed"])
 def test_cantilever_goldens_on_gpu(ikr, es, material):
     """tests/src/testcantileverbeamEAS.cpp:60-124 through the device path: 80 Newton iterations, max |d|, for
-    the NeoHooke and StVenantKirchhoff materials of the reference test."""
+    the NeoHooke, StVenantKirchhoff and BlatzKo materials of the reference test."""
     g = GOLD["cantilever_3d"]
     want = g["results"][es][material]
     kind = {"GreenLagrangeStrain": 1, "DisplacementGradient": 2, "DisplacementGradientTransposed": 3}[es]
-    p = problems.cantilever_golden(kind, g["eas_parameters"][es], material=1 if material == "StVenantKirchhoff" else 0)
+    p = problems.cantilever_golden(kind, g["eas_parameters"][es],
+                                   material={"NeoHooke": 0, "StVenantKirchhoff": 1, "BlatzKo": 2}[material])
     fes, asm = problems.build_gpu(p)
     req = ikr.FERequirements(fes)
     asm.bind(req, ikr.DBCOption.Full)
@@ -341,10 +342,12 @@ def test_inhomogeneous_dirichlet_values_match_oracle(ikr, eas, n):
             assert [s.iterations for s in info.solverInfos] == list(ref["iterations"])
 
 
-def test_calculate_at_stresses_match_oracle(ikr):
+@pytest.mark.parametrize("material", [0, 2], ids=["NeoHooke", "BlatzKo"])
+def test_calculate_at_stresses_match_oracle(ikr, material):
     """calculateAt<PK2Stress / kirchhoffStress / cauchyStress> (nonlinearelastic.hh:237-271) at random local
     points of every element, FP64 within 1e-12 of the oracle; zero at the undeformed state."""
     p = problems.cantilever(4, 3, 2, L=4.0, jitter=0.15, seed=9)
+    p.material = material
     fes, asm = problems.build_gpu(p)
     o = oracle.from_problem(p)
     rng = np.random.default_rng(4)
@@ -361,7 +364,7 @@ def test_calculate_at_stresses_match_oracle(ikr):
     assert np.abs(ikr.calculateAt(fes, ikr.FERequirements(fes), ikr.ResultTypes.cauchyStress)).max() == 0.0
 
 
-@pytest.mark.parametrize("material", [0, 1], ids=["NeoHooke", "SVK"])
+@pytest.mark.parametrize("material", [0, 1, 2], ids=["NeoHooke", "SVK", "BlatzKo"])
 @pytest.mark.parametrize("eas,n", [(1, 9), (1, 21), (2, 9), (3, 9)])
 def test_eas_calculate_at_matches_oracle(ikr, eas, n, material):
     """calculateAt of EAS elements (enhancedassumedstrains.hh:127-188) with a stored alpha: the GL ansatz enhances
@@ -405,13 +408,14 @@ def test_calculate_at_reproduces_reference_q1_stresses(ikr):
         assert np.abs(got - want).max() <= 1e-12 * np.abs(want).max(), key
 
 
-@pytest.mark.parametrize("eas,n", [(0, 0), (1, 9), (2, 9)])
-def test_svk_element_and_assembly_match_oracle(ikr, eas, n):
-    """StVenantKirchhoff (svk.hh:63-163) in the element kernels: element vectors and matrices, the assembled
-    residual and tangent (FP64) within 1e-12 of the oracle, the FP32 tangent within 2e-6, energy for the
-    displacement-based element."""
+@pytest.mark.parametrize("material", [1, 2], ids=["SVK", "BlatzKo"])
+@pytest.mark.parametrize("eas,n", [(0, 0), (1, 9), (2, 9), (3, 9)])
+def test_svk_element_and_assembly_match_oracle(ikr, eas, n, material):
+    """StVenantKirchhoff (svk.hh:63-163) and BlatzKo (blatzko.hh) in the element kernels: element vectors and
+    matrices, the assembled residual and tangent (FP64) within 1e-12 of the oracle, the FP32 tangent within 2e-6,
+    energy for the displacement-based element."""
     p = problems.cantilever(4, 2, 2, L=4.0, jitter=0.15, seed=11, eas=eas, n_eas=n)
-    p.material = 1
+    p.material = material
     o = oracle.from_problem(p)
     rng = np.random.default_rng(5)
     u = 0.02 * rng.standard_normal(p.n_dofs)

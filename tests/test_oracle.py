@@ -19,13 +19,16 @@ EAS_KINDS = {"GreenLagrangeStrain": oracle.EAS_GL, "DisplacementGradient": oracl
              "DisplacementGradientTransposed": oracle.EAS_HT}
 
 
-@pytest.mark.parametrize("material", ["NeoHooke", "StVenantKirchhoff"])
+MATERIALS = {"NeoHooke": oracle.MATERIAL_NEOHOOKE, "StVenantKirchhoff": oracle.MATERIAL_SVK,
+             "BlatzKo": oracle.MATERIAL_BLATZKO}
+
+
+@pytest.mark.parametrize("material", sorted(MATERIALS))
 @pytest.mark.parametrize("es", sorted(EAS_KINDS))
 def test_cantilever_goldens(es, material):
     g = GOLD["cantilever_3d"]
     want = g["results"][es][material]
-    p = problems.cantilever_golden(EAS_KINDS[es], g["eas_parameters"][es],
-                                   material=oracle.MATERIAL_SVK if material == "StVenantKirchhoff" else 0)
+    p = problems.cantilever_golden(EAS_KINDS[es], g["eas_parameters"][es], material=MATERIALS[material])
     o = oracle.from_problem(p)
     r = o.load_control(g["load_steps"], 0.0, 1.0, tol=g["tol"])
     assert r["success"]
@@ -189,12 +192,14 @@ def test_oracle_inhomogeneous_dirichlet_values():
     assert np.abs(res[0] - res[1]).max() <= 1e-8 * np.abs(res[1]).max()
 
 
+@pytest.mark.parametrize("material", [oracle.MATERIAL_SVK, oracle.MATERIAL_BLATZKO], ids=["SVK", "BlatzKo"])
 @pytest.mark.parametrize("eas,n", [(0, 0), (oracle.EAS_GL, 9), (oracle.EAS_H, 9)])
-def test_svk_tangent_and_residual_are_consistent(eas, n):
-    """StVenantKirchhoff (svk.hh:63-163) in the oracle: K = dR/dd and (displacement-based) R = dPsi/dd by
-    central differences, as checkfebyautodiff.hh does for the reference's elements."""
+def test_svk_tangent_and_residual_are_consistent(eas, n, material):
+    """StVenantKirchhoff (svk.hh:63-163) and BlatzKo (blatzko.hh) in the oracle: K = dR/dd and
+    (displacement-based) R = dPsi/dd by central differences, as checkfebyautodiff.hh does for the reference's
+    elements."""
     p = _distorted(eas, n)
-    p.material = oracle.MATERIAL_SVK
+    p.material = material
     o = oracle.from_problem(p)
     rng = np.random.default_rng(8)
     u = 0.05 * rng.standard_normal(24)
