@@ -56,6 +56,12 @@ enum class ScalarAffordance : int32_t { noAffordance = 0, mechanicalPotentialEne
 enum class EAS : int32_t { none = 0, GreenLagrangeStrain = 1, DisplacementGradient = 2, DisplacementGradientTransposed = 3 };
 enum class SolverTypeTag : int32_t { none = 0, si_ConjugateGradient = 1, gpu_PCG_BlockJacobi = 100 };
 enum class Precision : int32_t { fp64 = IKR_PRECISION_FP64, fp32 = IKR_PRECISION_FP32 };
+// material law of the elements (NeoHooke / StVenantKirchhoff with lambda, mu; BlatzKo with mu only)
+enum class Material : int32_t {
+  NeoHooke = IKR_MATERIAL_NEOHOOKE,
+  StVenantKirchhoff = IKR_MATERIAL_SVK,
+  BlatzKo = IKR_MATERIAL_BLATZKO
+};
 enum class NonLinearSolverMessages : int32_t { INIT = 0, ITERATION_STARTED, ITERATION_ENDED, RESIDUALNORM_UPDATED,
                                                CORRECTIONNORM_UPDATED, CORRECTION_UPDATED, SOLUTION_CHANGED,
                                                FINISHED_SUCESSFULLY };
@@ -85,6 +91,7 @@ class FiniteElements {
     check(ikr_fes_add_neumann(h_, (int32_t)face_elem.size(), face_elem.data(), face_local.data(), traction.data()),
           "neumannBoundaryLoad");
   }
+  void setMaterial(Material m) { check(ikr_fes_set_material(h_, (int32_t)m), "material"); }
   int32_t size() const { return n_elems_; }
   int32_t dofs() const { return 3 * n_nodes_; }
   int32_t numberOfInternalVariables() const { return n_eas_; }
