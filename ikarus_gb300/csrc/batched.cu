@@ -93,13 +93,13 @@ __device__ __forceinline__ double spmv_rows(const Bsr& A, const T* __restrict__ 
     T a0 = T(0), a1 = T(0), a2 = T(0);
     for (int g = A.slice_off[s]; g < A.slice_off[s + 1]; ++g) {
       const int c = A.col_sell[32 * g + l];
-      const T* v = val + ((int64_t)g * 32 + l) * 9;
+      const T* v = val + (int64_t)g * 288 + l;
       const T x0 = ld(zw + 4 * c) + tb * ld(pold + 4 * c);
       const T x1 = ld(zw + 4 * c + 1) + tb * ld(pold + 4 * c + 1);
       const T x2 = ld(zw + 4 * c + 2) + tb * ld(pold + 4 * c + 2);
-      a0 += v[0] * x0 + v[1] * x1 + v[2] * x2;
-      a1 += v[3] * x0 + v[4] * x1 + v[5] * x2;
-      a2 += v[6] * x0 + v[7] * x1 + v[8] * x2;
+      a0 += v[0] * x0 + v[32] * x1 + v[64] * x2;
+      a1 += v[96] * x0 + v[128] * x1 + v[160] * x2;
+      a2 += v[192] * x0 + v[224] * x1 + v[256] * x2;
     }
     const V3<T> zr = load3rw(zw, row), pr = load3rw(pold, row);
     const T n0 = zr.x + tb * pr.x, n1 = zr.y + tb * pr.y, n2 = zr.z + tb * pr.z;

@@ -278,10 +278,10 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
               if (k < nb) {
                 const T x0 = zc[k].x + tb[q] * pc[k].x, x1 = zc[k].y + tb[q] * pc[k].y,
                         x2 = zc[k].z + tb[q] * pc[k].z;
-                const T* v = sval + 9 * (32 * k + lane);
-                acc[q][0] += v[0] * x0 + v[1] * x1 + v[2] * x2;
-                acc[q][1] += v[3] * x0 + v[4] * x1 + v[5] * x2;
-                acc[q][2] += v[6] * x0 + v[7] * x1 + v[8] * x2;
+                const T* v = sval + 288 * k + lane;
+                acc[q][0] += v[0] * x0 + v[32] * x1 + v[64] * x2;
+                acc[q][1] += v[96] * x0 + v[128] * x1 + v[160] * x2;
+                acc[q][2] += v[192] * x0 + v[224] * x1 + v[256] * x2;
               }
             }
           }

@@ -328,12 +328,12 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
         const int Jn = (sub + d) & 7;
         const uint8_t fmaskJ = a.node_fixed ? a.node_fixed[a.conn[Jn * ne + e]] : uint8_t(0);
         const int64_t s1 = a.slot[(size_t)(sub * 8 + Jn) * ne + e];
-        KT* b1 = val + block_entry(s1, 0);  // the 9 entries of a block are contiguous
+        KT* b1 = val + block_entry(s1, 0);  // entries of a block are 32 apart
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int j = 0; j < 3; ++j)
-            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[3 * i + j] += Kacc[d][i][j];
+            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[32 * (3 * i + j)] += Kacc[d][i][j];
         if (d >= 1 && d <= 3) {
           const int64_t s2 = a.slot[(size_t)(Jn * 8 + sub) * ne + e];
           KT* b2 = val + block_entry(s2, 0);
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
           for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j)
-              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[3 * j + i] += Kacc[d][i][j];
+              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[32 * (3 * j + i)] += Kacc[d][i][j];
         }
       }
     }

@@ -636,14 +636,14 @@ __global__ void __launch_bounds__(EasCfg<NA>::EPB * 8) eas_element_kernel(ElemAr
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int j = 0; j < 3; ++j)
-            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[3 * i + j] += KT(Kacc[d][i][j]);
+            if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b1[32 * (3 * i + j)] += KT(Kacc[d][i][j]);
         if (d >= 1 && d <= 3) {
           KT* b2 = val + block_entry(a.slot[(size_t)(Jn * 8 + sub) * ne + e], 0);
 #pragma unroll
           for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j)
-              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[3 * j + i] += KT(Kacc[d][i][j]);
+              if (!(((fmaskI >> i) | (fmaskJ >> j)) & 1)) b2[32 * (3 * j + i)] += KT(Kacc[d][i][j]);
         }
       }
     }

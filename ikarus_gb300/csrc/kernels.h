@@ -58,11 +58,9 @@ struct ElemArgs {
 // spans the block columns [slice_off[s], slice_off[s+1]) (its longest row), rows shorter than that are
 // padded with zero blocks whose column is the row itself.  Block k of row r = 32 s + l has the id
 // b = (slice_off[s] + k) * 32 + l; its column is col_sell[b] and entry e = 3i + j (row-major in the block)
-// sits at val[block_entry(b, e)] = 9 b + e: the 32 blocks of one k of a slice are 288 consecutive values (one
-// bulk copy), and the 9 entries of a block are contiguous, so the element kernels' read-modify-write of a block
-// touches one or two 32-byte sectors.  In shared memory lane l reads its block's entries at stride 9 words,
-// which no two lanes share a bank for.  The sorted CSR view (row_ptr / col) describes the pattern itself.
-__host__ __device__ __forceinline__ int64_t block_entry(int64_t b, int e) { return 9 * b + e; }
+// sits at val[block_entry(b, e)] = (b >> 5) * 288 + e * 32 + (b & 31), so for a fixed (k, e) the 32 rows of a
+// slice are 32 consecutive values.  The sorted CSR view (row_ptr / col) describes the pattern itself.
+__host__ __device__ __forceinline__ int64_t block_entry(int64_t b, int e) { return (b >> 5) * 288 + e * 32 + (b & 31); }
 
 struct Bsr {
   int n_rows = 0;                   // block rows = nodes

@@ -42,12 +42,12 @@ __global__ void __launch_bounds__(kThreads) pcg_spmv_kernel(Bsr A, const T* __re
 #pragma unroll 4
     for (int g = g0; g < g1; ++g) {
       const int c = __ldg(A.col_sell + 32 * g + l);
-      const T* v = val + ((int64_t)g * 32 + l) * 9;
+      const T* v = val + (int64_t)g * 288 + l;
       const V3<T> zc = load3(z, c), pc = load3(pold, c);
       const T x0 = zc.x + beta * pc.x, x1 = zc.y + beta * pc.y, x2 = zc.z + beta * pc.z;
-      a0 += __ldg(v) * x0 + __ldg(v + 1) * x1 + __ldg(v + 2) * x2;
-      a1 += __ldg(v + 3) * x0 + __ldg(v + 4) * x1 + __ldg(v + 5) * x2;
-      a2 += __ldg(v + 6) * x0 + __ldg(v + 7) * x1 + __ldg(v + 8) * x2;
+      a0 += __ldg(v) * x0 + __ldg(v + 32) * x1 + __ldg(v + 64) * x2;
+      a1 += __ldg(v + 96) * x0 + __ldg(v + 128) * x1 + __ldg(v + 160) * x2;
+      a2 += __ldg(v + 192) * x0 + __ldg(v + 224) * x1 + __ldg(v + 256) * x2;
     }
     const V3<T> zr = load3(z, row), pr = load3(pold, row);
     const T p0 = zr.x + beta * pr.x, p1 = zr.y + beta * pr.y, p2 = zr.z + beta * pr.z;
@@ -170,7 +170,7 @@ __global__ void block_jacobi_kernel(Bsr A, const T* __restrict__ val, T* __restr
   const T* b = val + block_entry(A.diag[row], 0);
   double m[3][3], r[3][3];
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) m[i][j] = double(b[3 * i + j]);
+    for (int j = 0; j < 3; ++j) m[i][j] = double(b[32 * (3 * i + j)]);
   if (point) {
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) r[i][j] = (i == j && m[i][i] != 0.0) ? 1.0 / m[i][i] : 0.0;
@@ -191,11 +191,11 @@ __global__ void residual64_kernel(Bsr A, const T* __restrict__ val, const double
 #pragma unroll 4
     for (int g = A.slice_off[s]; g < A.slice_off[s + 1]; ++g) {
       const int c3 = 3 * A.col_sell[32 * g + l];
-      const T* v = val + ((int64_t)g * 32 + l) * 9;
+      const T* v = val + (int64_t)g * 288 + l;
       const double x0 = x[c3], x1 = x[c3 + 1], x2 = x[c3 + 2];
-      a0 += double(v[0]) * x0 + double(v[1]) * x1 + double(v[2]) * x2;
-      a1 += double(v[3]) * x0 + double(v[4]) * x1 + double(v[5]) * x2;
-      a2 += double(v[6]) * x0 + double(v[7]) * x1 + double(v[8]) * x2;
+      a0 += double(v[0]) * x0 + double(v[32]) * x1 + double(v[64]) * x2;
+      a1 += double(v[96]) * x0 + double(v[128]) * x1 + double(v[160]) * x2;
+      a2 += double(v[192]) * x0 + double(v[224]) * x1 + double(v[256]) * x2;
     }
     const int i = 3 * row;
     out[i] = subtract ? b[i] - a0 : a0;

@@ -121,10 +121,10 @@ __global__ void __launch_bounds__(WARPS * 32) pcg_spmv_staged_kernel(Bsr A, cons
     for (int k = 0; k < CB; ++k) {
       if (k < nb) {
         const T x0 = zc[k].x + beta * pc[k].x, x1 = zc[k].y + beta * pc[k].y, x2 = zc[k].z + beta * pc[k].z;
-        const T* v = sv + 9 * (32 * k + lane);
-        a0 += v[0] * x0 + v[1] * x1 + v[2] * x2;
-        a1 += v[3] * x0 + v[4] * x1 + v[5] * x2;
-        a2 += v[6] * x0 + v[7] * x1 + v[8] * x2;
+        const T* v = sv + 288 * k + lane;
+        a0 += v[0] * x0 + v[32] * x1 + v[64] * x2;
+        a1 += v[96] * x0 + v[128] * x1 + v[160] * x2;
+        a2 += v[192] * x0 + v[224] * x1 + v[256] * x2;
       }
     }
     __syncwarp();  // every lane is done with the stage before it is refilled
