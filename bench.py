@@ -35,7 +35,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--load-steps", type=int, default=20)
     ap.add_argument("--plain-runs", type=int, default=1)
-    ap.add_argument("--eta-max", type=float, default=1e-2, help="mixed form: Eisenstat-Walker forcing upper bound")
+    ap.add_argument("--eta-max", type=float, default=2e-2, help="mixed form: Eisenstat-Walker forcing upper bound")
     ap.add_argument("--eta-min", type=float, default=1e-5, help="mixed form: Eisenstat-Walker forcing lower bound")
     ap.add_argument("--predictor", type=int, default=1, choices=[0, 1],
                     help="mixed form's Newton predictor: 0 none (the reference's), 1 previous increment (the learned "
