@@ -37,9 +37,10 @@ def parse():
     ap.add_argument("--plain-runs", type=int, default=1)
     ap.add_argument("--eta-max", type=float, default=2e-2, help="mixed form: Eisenstat-Walker forcing upper bound")
     ap.add_argument("--eta-min", type=float, default=1e-5, help="mixed form: Eisenstat-Walker forcing lower bound")
-    ap.add_argument("--predictor", type=int, default=1, choices=[0, 1],
+    ap.add_argument("--predictor", type=int, default=1, choices=[0, 1, 3],
                     help="mixed form's Newton predictor: 0 none (the reference's), 1 previous increment (the learned "
-                         "predictor's fallback; this single load case has no trained model)")
+                         "predictor's fallback; this single load case has no trained model), 3 second-order "
+                         "extrapolation with the previous increment as fallback")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="32x8x8 mesh (profiling runs)")
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
@@ -133,7 +134,7 @@ def peaks():
 
 
 # ---------------------------------------------------------------------------------------------------------
-def solver_settings(ikr, mixed: bool, eta=(1e-2, 1e-5)):
+def solver_settings(ikr, mixed: bool, eta=(2e-2, 1e-5)):
     if mixed:
         return ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=eta[0],
                               linear_rtol_min=eta[1], linear_max_iter=200000)

@@ -801,8 +801,9 @@ class LoadControl:
         _err(lib().ikr_load_control_subscribe(self.h, cb, None), "subscribe")
 
     def set_predictor(self, kind: int = 0, predictor: "LearnedPredictor" = None, params=None, record=False):
-        """Newton predictor of every load step: 0 none (reference), 1 previous increment, 2 learned (falls back
-        to the previous increment when its FP64 residual is not smaller)."""
+        """Newton predictor of every load step: 0 none (reference), 1 previous increment, 2 learned, 3 second-order
+        extrapolation u + 2 du1 - du2 (2 and 3 fall back to the previous increment when their FP64 residual is not
+        smaller)."""
         par = None if params is None else np.ascontiguousarray(params, dtype=np.float64)
         _err(lib().ikr_load_control_set_predictor(self.h, int(kind), predictor.h if predictor else None,
                                                   _ptr(par) if par is not None else None, int(record)), "predictor")
@@ -817,8 +818,9 @@ class LoadControl:
         _err(lib().ikr_load_control_set_predictor_gate(self.h, int(bool(gated))))
 
     def predictor_history(self):
-        """Per load step of the last run: (step, |R| unpredicted, |R| previous increment, |R| learned, kept, 0);
-        kept: 0 unpredicted, 1 previous increment, 2 learned."""
+        """Per load step of the last run: (step, |R| unpredicted, |R| previous increment, |R| learned, kept,
+        |R| second-order extrapolation); kept: 0 unpredicted, 1 previous increment, 2 learned, 3 second-order
+        (-1 where a candidate was not evaluated)."""
         n = C.c_int32()
         _err(lib().ikr_load_control_predictor_history(self.h, 0, None, C.byref(n)))
         out = np.zeros((max(n.value, 1), 6))

@@ -214,6 +214,7 @@ void launch_gram64(const float* Y, int64_t n, int l, double* G, cudaStream_t s);
 void launch_randn(float* out, int64_t n, uint64_t seed, cudaStream_t s);
 void launch_diff_to_f32(const double* a, const double* b, float* out, int64_t n, cudaStream_t s);
 void launch_add_f32(double* u, const float* d, int64_t n, cudaStream_t s);
+void launch_add_scaled_f32(double* u, const float* d, double a, int64_t n, cudaStream_t s);  // u += a d
 void launch_base_plus_scaled(double* u, const double* u0, const float* d, double sc, int64_t n, cudaStream_t s);
 
 // noalloc.cu -- fixed device scratch of the allocation-free CG solve

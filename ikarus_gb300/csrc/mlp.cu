@@ -202,6 +202,10 @@ __global__ void add_f32_kernel(double* __restrict__ u, const float* __restrict__
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) u[t] += double(d[t]);
 }
+__global__ void add_scaled_f32_kernel(double* __restrict__ u, const float* __restrict__ d, double a, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    u[i] += a * double(d[i]);
+}
 __global__ void base_plus_scaled_kernel(double* __restrict__ u, const double* __restrict__ u0,
                                         const float* __restrict__ d, double sc, int64_t n) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -269,6 +273,9 @@ void launch_diff_to_f32(const double* a, const double* b, float* out, int64_t n,
 }
 void launch_add_f32(double* u, const float* d, int64_t n, cudaStream_t s) {
   add_f32_kernel<<<blocks(n, 256), 256, 0, s>>>(u, d, n);
+}
+void launch_add_scaled_f32(double* u, const float* d, double a, int64_t n, cudaStream_t s) {
+  add_scaled_f32_kernel<<<blocks(n, 256), 256, 0, s>>>(u, d, a, n);
 }
 void launch_base_plus_scaled(double* u, const double* u0, const float* d, double sc, int64_t n, cudaStream_t s) {
   base_plus_scaled_kernel<<<blocks(n, 256), 256, 0, s>>>(u, u0, d, sc, n);

@@ -408,7 +408,7 @@ double predictor_apply(ikr_lc lc, ikr_req r, int step) {
   ikr_asm a = lc->nr->asm_;
   assemble_vector(a, r, IKR_DBC_FULL);
   const double r_plain = device_norm(f, a->R.p, n, lc->pred_part, lc->pred_out);
-  ikr_lc_s::PredRecord rec{(double)step, r_plain, -1.0, -1.0, 0.0, 0.0};
+  ikr_lc_s::PredRecord rec{(double)step, r_plain, -1.0, -1.0, 0.0, -1.0};
   // FP64 residual norm at u0 + d (+ du1); +inf when an element inverts
   auto residual_at = [&](const float* d, bool plus_du1) -> double {
     ikr::launch_base_plus_scaled(r->u.p, lc->u_step0.p, d, 1.0, n, s);
@@ -456,12 +456,28 @@ double predictor_apply(ikr_lc lc, ikr_req r, int step) {
     dl = p->dvec.p;
     rec.r_learned = residual_at(dl, has_prev);
   }
+  // second-order extrapolation of the path, u0 + du1 + (du1 - du2) (kind 3, from the third step on)
+  const bool quad = lc->pred_kind == 3 && lc->hist >= 2;
+  if (quad) {
+    ikr::launch_base_plus_scaled(r->u.p, lc->u_step0.p, lc->du1.p, 2.0, n, s);
+    ikr::launch_add_scaled_f32(r->u.p, lc->du2.p, -1.0, n, s);
+    count(2);
+    r->version++;
+    try {
+      assemble_vector(a, r, IKR_DBC_FULL);
+      rec.spare = device_norm(f, a->R.p, n, lc->pred_part, lc->pred_out);
+    } catch (const IkrError& e) {
+      if (e.code != IKR_ERR_NONPOSITIVE_DETC) throw;
+      rec.spare = INFINITY;
+    }
+  }
   const double r_fb = has_prev ? rec.r_fallback : r_plain;
-  int keep = 0;  // 0 unpredicted, 1 previous increment, 2 learned
+  int keep = 0;  // 0 unpredicted, 1 previous increment, 2 learned, 3 second-order extrapolation
   if (has_prev && std::isfinite(rec.r_fallback)) keep = 1;
   if (dl && std::isfinite(rec.r_learned) && (!lc->gated || rec.r_learned < r_fb)) keep = 2;
+  if (quad && std::isfinite(rec.spare) && (!lc->gated || rec.spare < r_fb)) keep = 3;
   // leave u at the kept state (the last one evaluated may be another)
-  const int last = dl ? 2 : (has_prev ? 1 : 0);
+  const int last = quad ? 3 : (dl ? 2 : (has_prev ? 1 : 0));
   if (keep != last) {
     if (keep == 0) {
       CK(cudaMemcpyAsync(r->u.p, lc->u_step0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
@@ -472,8 +488,8 @@ double predictor_apply(ikr_lc lc, ikr_req r, int step) {
     r->version++;
   }
   rec.kept = keep;
-  if (lc->pred_kind == 2) {
-    if (keep == 2) lc->accepted++;
+  if (lc->pred_kind == 2 || lc->pred_kind == 3) {
+    if (keep == lc->pred_kind) lc->accepted++;
     else lc->rejected++;
   } else {
     if (keep == 1) lc->accepted++;
@@ -675,7 +691,7 @@ int ikr_predictor_fit(ikr_pred p, int32_t epochs, int32_t batch, float lr, float
 
 int ikr_load_control_set_predictor(ikr_lc lc, int32_t kind, ikr_pred p, const double* params, int32_t record) {
   return guarded([&] {
-    need(lc && kind >= 0 && kind <= 2, IKR_ERR_ARG, "invalid predictor kind");
+    need(lc && kind >= 0 && kind <= 3, IKR_ERR_ARG, "invalid predictor kind");
     need(kind != 2 || p, IKR_ERR_ARG, "the learned predictor needs a predictor object");
     need(!record || p, IKR_ERR_ARG, "recording needs a predictor object");
     lc->pred_kind = kind;

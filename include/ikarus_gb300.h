@@ -347,10 +347,12 @@ int ikr_path_following_increment(ikr_pf pf, double* dd);
 
 /* ---- Newton predictor of LoadControl (no counterpart in the reference, whose predictor only increments
  * the load factor, loadcontrol.inl:54-57) -------------------------------------------------------------------
- * kind 0: none (the reference's behaviour); 1: previous converged increment; 2: learned (predictor object).
- * A prediction is kept only if its FP64 residual is below that of the unpredicted state, and the relative
- * Newton test of the step stays referenced to the unpredicted residual.  record = 1 appends every converged
- * increment (and params, the path's load parameters) to the predictor's training snapshots. */
+ * kind 0: none (the reference's behaviour); 1: previous converged increment; 2: learned (predictor object);
+ * 3: second-order extrapolation u + 2 du_{k-1} - du_{k-2}.  The learned and the second-order candidates are kept
+ * only when their FP64 residual is below the previous-increment candidate's (their fallback); candidates that
+ * invert an element are discarded; the relative Newton test of the step stays referenced to the unpredicted
+ * residual.  record = 1 appends every converged increment (and params, the path's load parameters) to the
+ * predictor's training snapshots. */
 typedef struct ikr_pred_s* ikr_pred;
 typedef struct ikr_mlp_s* ikr_mlp;
 int ikr_load_control_set_predictor(ikr_lc lc, int32_t kind, ikr_pred pred, const double* params, int32_t record);
@@ -358,8 +360,9 @@ int ikr_load_control_set_predictor(ikr_lc lc, int32_t kind, ikr_pred pred, const
 int ikr_load_control_predictor_stats(ikr_lc lc, int32_t* accepted, int32_t* rejected);
 /* per load step of the last run, 6 doubles: step, FP64 residual norm of the unpredicted state, of the
  * previous-increment candidate, of the learned candidate (-1 when not evaluated, inf when an element
- * inverted), the state kept (0 unpredicted, 1 previous increment, 2 learned) and 0.  n returns the number of
- * steps; at most capacity rows are written. */
+ * inverted), the state kept (0 unpredicted, 1 previous increment, 2 learned, 3 second-order extrapolation) and
+ * the residual norm of the second-order candidate (-1 when not evaluated).  n returns the number of steps; at
+ * most capacity rows are written. */
 int ikr_load_control_predictor_history(ikr_lc lc, int32_t capacity, double* out, int32_t* n);
 /* gated != 0 (default): the learned candidate is kept only when its FP64 residual norm is below that of its
  * fallback (the previous increment, the unpredicted state on the first step); 0: kept whenever no element

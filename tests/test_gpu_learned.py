@@ -80,3 +80,17 @@ def test_learned_predictor_saves_newton_iterations(ikr):
     print(f"Newton iterations over 5 held-out paths: none {plain_its}, previous increment {prev_its}, "
           f"learned {learned_its}")
     assert learned_its < plain_its
+
+
+def test_second_order_extrapolation_predictor_reaches_the_same_path(ikr):
+    """Predictor kind 3 (u + 2 du_{k-1} - du_{k-2}, previous increment as its fallback): every step reaches the
+    FP64 tolerance and the converged path agrees with the unpredicted one; from the third step on the candidate is
+    evaluated (its residual norm is recorded) and kept or rejected by the residual test."""
+    p = problems.learned_cantilever(16, 4, 4, load_steps=10)
+    fes, asm = problems.build_gpu(p, precision=1)
+    theta = problems.sample_load_parameters(np.random.default_rng(5))
+    info0, u0, _ = _run(ikr, p, fes, asm, theta, kind=0)
+    info3, u3, (acc, rej) = _run(ikr, p, fes, asm, theta, kind=3)
+    assert info0.success and info3.success
+    assert np.abs(u3 - u0).max() <= 1e-5 * np.abs(u0).max()
+    assert acc + rej == p.load_steps
