@@ -27,6 +27,17 @@ sys.path.insert(0, ROOT)
 METRIC = "time to ||R||/||R0||<1e-8 per load path (mixed vs plain FP64 GPU)"
 
 
+def max_over_ranks(value: float, world: int, device="cuda") -> float:
+    """The slowest rank's value (replicas: every rank times its own copy of the workload); plain value at N = 1.
+    The all-reduce runs on `device` ("cuda" under NCCL, "cpu" under gloo)."""
+    if world <= 1:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -208,7 +219,8 @@ def run_ours(args, rank, world):
     # timed: device-resident inputs
     times, infos = [], []
     launches0 = ikr.kernel_launches()
-    with ClockSampler(0) as clocks:
+    local_gpu = 0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank))
+    with ClockSampler(local_gpu) as clocks:
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
@@ -220,6 +232,7 @@ def run_ours(args, rank, world):
             ev1.synchronize()
             times.append(ev0.elapsed_time(ev1) / 1e3)
             infos.append(info)
+        barrier()
     launches = (ikr.kernel_launches() - launches0) // max(1, args.steps)
     # one more (untimed) load path with device events around every CG SpMV inside the graphs: the dominant
     # kernel's average duration for the roofline (the event nodes would perturb the timed region)
@@ -233,11 +246,7 @@ def run_ours(args, rank, world):
     mixed.ls.profile(False)
     assembly = {"mixed": assembly_rates(ikr, torch, mixed, p)}
     assert all(i.success for i in infos)
-    t_mixed = sum(times) / len(times)
-    if world > 1:
-        t = torch.tensor([t_mixed], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_mixed = float(t.item())
+    t_mixed = max_over_ranks(sum(times) / len(times), world)
 
     # e2e: public API with host buffers (h2d initial displacement, d2h converged displacement)
     u0 = np.zeros(p.n_dofs)
