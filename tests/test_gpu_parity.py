@@ -438,3 +438,28 @@ def test_svk_element_and_assembly_match_oracle(ikr, eas, n, material):
         K = asm.matrix(req, dbc=ikr.DBCOption.Full).toarray()
         Kref = o.assemble_matrix_dense(u, 0.4)
         assert rel_err(K, Kref) <= (2e-6 if precision else FP64_RTOL)
+
+
+def test_newton_on_a_reduced_binding_gives_the_full_iterates(ikr):
+    """DBCOption::Reduced bound to the assembler (the reference then solves the reduced system and expands the
+    correction, nonlinearsolverfactory.hh:32-56): the reduced system is the Full one without its identity rows and
+    columns, so the device Newton, which solves the Full system for every binding, gives the same iterations,
+    norms and displacement; the constrained dofs stay at zero."""
+    p = problems.cantilever(8, 2, 2, traction=(0.0, 0.0, -0.5), load_steps=3, tol=1e-10)
+    results = []
+    for dbc in (ikr.DBCOption.Full, ikr.DBCOption.Reduced):
+        fes, asm = problems.build_gpu(p)
+        req = ikr.FERequirements(fes)
+        asm.bind(req, dbc)
+        st = ikr.NRSettings(tol=1e-10, maxIter=30, linear_rtol=1e-13)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(rtol=1e-13)))
+        info = ikr.LoadControl(nr, 3).run(req)
+        assert info.success
+        results.append((info, req.globalSolution()))
+    (i0, u0), (i1, u1) = results
+    assert [s.iterations for s in i0.solverInfos] == [s.iterations for s in i1.solverInfos]
+    assert [s.residualNorm for s in i0.solverInfos] == [s.residualNorm for s in i1.solverInfos]
+    assert np.array_equal(u0, u1)
+    assert np.all(u1[p.fixed.astype(bool)] == 0.0)
+    ref = oracle.from_problem(p).load_control(3, tol=1e-10, max_iter=30)
+    assert np.abs(u1 - ref["u"]).max() <= 1e-8 * np.abs(ref["u"]).max()
