@@ -496,12 +496,333 @@ cudaError_t dispatch(int variant, const Bsr& A, PcgWork* const* ws, double* pa, 
   }
 }
 
+
+// ---- one grid reduction per iteration -------------------------------------------------------------------
+// The same preconditioned CG rearranged so that an iteration needs one grid-wide reduction instead of two (the
+// second reduction is what dominates the fixed cost of an iteration: two grid barriers).  Iteration k of a row
+// owner, with alpha_{k-1}, beta_{k-1} from the previous reduction:
+//   r_k = r_{k-1} - alpha q_{k-1},  z_k = z_{k-1} - alpha w_{k-1},  x_k = x_{k-1} + alpha p_{k-1},
+//   p_k = z_k + beta p_{k-1},  q_k = K p_k,  w_k = M^{-1} q_k,
+// where a gathered neighbour's p_k is formed from its stored z_{k-1}, w_{k-1} and p_{k-1} with the same two
+// operations, so no barrier is needed between the vector update and the product.  z follows the recurrence
+// z_k = z_{k-1} - alpha w_{k-1} (= M^{-1} r_k in exact arithmetic).  The reduction carries p.q, r.w, q.z, q.w,
+// r.q, q.q, r.z and r.r of the iterate; then
+//   alpha_k = rho_k / p.q,  rho_{k+1} = rho_k - alpha_k (r.w + q.z) + alpha_k^2 q.w,  beta_k = rho_{k+1} / rho_k,
+//   |r_{k+1}|^2 = |r_k|^2 - 2 alpha_k r.q + alpha_k^2 q.q,
+// with rho_k = r_k.z_k and |r_k|^2 computed from the vectors every iteration (no drift accumulates through the
+// recurrences).  Buffers: z, p and w double-buffered by iteration parity (gathers read parity k-1 while the
+// owners write parity k).  Dot products accumulate in FP64.
+__device__ __forceinline__ float cg1_z(float z, float w, float a) { return z - a * w; }
+__device__ __forceinline__ double cg1_z(double z, double w, double a) { return z - a * w; }
+__device__ __forceinline__ float cg1_p(float z, float p, float b) { return z + b * p; }
+__device__ __forceinline__ double cg1_p(double z, double p, double b) { return z + b * p; }
+
+template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB>
+__global__ void __launch_bounds__(WARPS * 32, MINB)
+    pcg_onered_kernel(Bsr A, const T* __restrict__ val, const T* __restrict__ minv, T* __restrict__ xg,
+                      const T* __restrict__ rg, T* Z0, T* Z1, T* P0, T* P1, T* W0, T* W1, double* part,
+                      double* scal, int64_t keep_g) {
+  using C = PersistentCfg<T, CB, NST, WARPS>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bars[WARPS][NST];
+  __shared__ double sw[WARPS * 8];
+  __shared__ double sv[8];
+  __shared__ bool ok_sh;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int G = gridDim.x;
+  const int nw = G * WARPS;
+  const int gw = blockIdx.x * WARPS + warp;
+  const int n_slices = A.n_slices;
+  unsigned int* bar_count = &tickets(scal)[3];
+  unsigned char* wbase = smem + (size_t)warp * NST * C::kStageBytes;
+
+  int ns = 0;
+  int s_first[MAXS], s_end[MAXS];
+#pragma unroll
+  for (int j = 0; j < MAXS; ++j) {
+    const int sj = gw + j * nw;
+    s_first[j] = 0, s_end[j] = 0;
+    if (sj < n_slices) {
+      s_first[j] = A.slice_off[sj];
+      s_end[j] = A.slice_off[sj + 1];
+      ns = j + 1;
+    }
+  }
+  // own rows: r, z (from the init kernel: Z1 holds z_0), p = q = w = 0 in registers; x (zero from the init
+  // kernel) is updated in place in global memory, which keeps the kernel within its register budget
+  T rr_[MAXS][3], zr[MAXS][3], pr[MAXS][3], qr[MAXS][3], wr[MAXS][3];
+#pragma unroll
+  for (int j = 0; j < MAXS; ++j) {
+    const int row = 32 * (gw + j * nw) + lane;
+    V3<T> r0 = {T(0), T(0), T(0)}, z0 = {T(0), T(0), T(0)};
+    if (j < ns && row < A.n_rows) r0 = load3rw(rg, row), z0 = load3rw(Z1, row);
+    rr_[j][0] = r0.x, rr_[j][1] = r0.y, rr_[j][2] = r0.z;
+    zr[j][0] = z0.x, zr[j][1] = z0.y, zr[j][2] = z0.z;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) pr[j][c] = qr[j][c] = wr[j][c] = T(0);
+  }
+  const double tol2 = scal[kTol2];
+  const int maxit = (int)scal[kMaxIt];
+  double rrs = scal[kRR], rho = scal[kRz];
+  double done = scal[kDone];
+  double alpha_p = 0.0, beta_p = 0.0;
+
+  if (lane == 0) {
+    for (int st = 0; st < NST; ++st) mbar_init(smem_addr(&bars[warp][st]), 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+
+  auto issue = [&](int st, const CyclicPos& P) {
+    if (lane == 0) {
+      const int nb = min(CB, P.gend - P.g);
+      const uint32_t vb = nb * 288 * (uint32_t)sizeof(T), cb = nb * 128;
+      const uint32_t b = smem_addr(&bars[warp][st]);
+      unsigned char* stage = wbase + (size_t)st * C::kStageBytes;
+      const uint64_t pol = l2_policy(P.g < keep_g);
+      mbar_expect_tx(b, vb + cb);
+      bulk_g2s(smem_addr(stage), val + (int64_t)P.g * 288, vb, b, pol);
+      bulk_g2s(smem_addr(stage + C::kValBytes), A.col_sell + (int64_t)P.g * 32, cb, b, pol);
+    }
+  };
+  auto advance = [&](CyclicPos& P) {
+    P.g += CB;
+    if (P.g >= P.gend) {
+      P.j = (P.j + 1 == ns) ? 0 : P.j + 1;
+#pragma unroll
+      for (int j = 0; j < MAXS; ++j)
+        if (j == P.j) P.g = s_first[j], P.gend = s_end[j];
+    }
+  };
+
+  CyclicPos P{0, s_first[0], s_end[0]};
+  int inflight = 0;
+  if (ns > 0 && done == 0.0) {
+    for (int st = 0; st < NST; ++st) {
+      issue(st, P);
+      ++inflight;
+      advance(P);
+    }
+  }
+  uint32_t phase = 0;
+  int st = 0;
+  bool failed = false;
+  int it = (int)scal[kIters];
+  unsigned int barrier_no = 0;
+
+  while (done == 0.0) {
+    const int par = it & 1;
+    const T ta = T(alpha_p), tb = T(beta_p);
+    T* Zw = par ? Z1 : Z0;
+    const T* Zr = par ? Z0 : Z1;
+    T* Pw = par ? P1 : P0;
+    const T* Pr = par ? P0 : P1;
+    T* Ww = par ? W1 : W0;
+    const T* Wr = par ? W0 : W1;
+    double red[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // p.q, r.w, q.z, q.w, r.q, q.q, r.z, r.r
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) {
+      if (j < ns && !failed) {
+        const int row = 32 * (gw + j * nw) + lane;
+        const bool own = row < A.n_rows;
+        // lagged update with alpha_{k-1}, beta_{k-1}, then p_k; published for the neighbours' next gathers
+        if (own && it > 0) {
+          const V3<T> xo = load3rw(xg, row);
+          store3(xg, row, xo.x + ta * pr[j][0], xo.y + ta * pr[j][1], xo.z + ta * pr[j][2]);
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          rr_[j][c] = rr_[j][c] - ta * qr[j][c];
+          zr[j][c] = cg1_z(zr[j][c], wr[j][c], ta);
+          pr[j][c] = cg1_p(zr[j][c], pr[j][c], tb);
+        }
+        if (own) {
+          store3(Zw, row, zr[j][0], zr[j][1], zr[j][2]);
+          store3(Pw, row, pr[j][0], pr[j][1], pr[j][2]);
+        }
+        T a0 = T(0), a1 = T(0), a2 = T(0);
+        for (int g = s_first[j]; g < s_end[j]; g += CB) {
+          const bool okw = __all_sync(0xffffffffu, mbar_wait_bounded(smem_addr(&bars[warp][st]), (phase >> st) & 1u));
+          if (!okw) {
+            failed = true;
+            break;
+          }
+          phase ^= 1u << st;
+          --inflight;
+          const T* sval = reinterpret_cast<const T*>(wbase + (size_t)st * C::kStageBytes);
+          const int32_t* scol = reinterpret_cast<const int32_t*>(wbase + (size_t)st * C::kStageBytes + C::kValBytes);
+          const int nb = min(CB, s_end[j] - g);
+          V3<T> zc[CB], wc[CB], pc[CB];
+#pragma unroll
+          for (int k = 0; k < CB; ++k) {
+            const int c = k < nb ? scol[32 * k + lane] : 0;
+            zc[k] = load3rw(Zr, c);
+            wc[k] = load3rw(Wr, c);
+            pc[k] = load3rw(Pr, c);
+          }
+#pragma unroll
+          for (int k = 0; k < CB; ++k) {
+            if (k < nb) {
+              const T x0 = cg1_p(cg1_z(zc[k].x, wc[k].x, ta), pc[k].x, tb);
+              const T x1 = cg1_p(cg1_z(zc[k].y, wc[k].y, ta), pc[k].y, tb);
+              const T x2 = cg1_p(cg1_z(zc[k].z, wc[k].z, ta), pc[k].z, tb);
+              const T* v = sval + 288 * k + lane;
+              a0 += v[0] * x0 + v[32] * x1 + v[64] * x2;
+              a1 += v[96] * x0 + v[128] * x1 + v[160] * x2;
+              a2 += v[192] * x0 + v[224] * x1 + v[256] * x2;
+            }
+          }
+          __syncwarp();  // the stage is consumed before it is refilled
+          issue(st, P);
+          ++inflight;
+          advance(P);
+          st = (st + 1 == NST) ? 0 : st + 1;
+        }
+        qr[j][0] = a0, qr[j][1] = a1, qr[j][2] = a2;
+        if (own) {
+          const T* m = minv + 9 * (int64_t)row;
+#pragma unroll
+          for (int b = 0; b < 3; ++b)
+            wr[j][b] = __ldg(m + 3 * b) * a0 + __ldg(m + 3 * b + 1) * a1 + __ldg(m + 3 * b + 2) * a2;
+          store3(Ww, row, wr[j][0], wr[j][1], wr[j][2]);
+          const T* pj = pr[j];
+          const T* qj = qr[j];
+          const T* rj = rr_[j];
+          const T* zj = zr[j];
+          const T* wj = wr[j];
+          red[0] += double(pj[0] * qj[0] + pj[1] * qj[1] + pj[2] * qj[2]);
+          red[1] += double(rj[0] * wj[0] + rj[1] * wj[1] + rj[2] * wj[2]);
+          red[2] += double(qj[0] * zj[0] + qj[1] * zj[1] + qj[2] * zj[2]);
+          red[3] += double(qj[0] * wj[0] + qj[1] * wj[1] + qj[2] * wj[2]);
+          red[4] += double(rj[0] * qj[0] + rj[1] * qj[1] + rj[2] * qj[2]);
+          red[5] += double(qj[0] * qj[0] + qj[1] * qj[1] + qj[2] * qj[2]);
+          red[6] += double(rj[0] * zj[0] + rj[1] * zj[1] + rj[2] * zj[2]);
+          red[7] += double(rj[0] * rj[0] + rj[1] * rj[1] + rj[2] * rj[2]);
+        } else {
+          wr[j][0] = wr[j][1] = wr[j][2] = T(0);
+        }
+      }
+    }
+    failed = __syncthreads_or(failed);
+    if (failed) break;
+    cta_reduce<8>(red, sw);
+    ++barrier_no;
+    if (!grid_allreduce<8>(red, part + par * 8 * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
+      failed = true;
+      break;
+    }
+    rho = red[6];
+    const double pq = red[0];
+    if (!(fabs(pq) > 0.0) || !isfinite(pq) || !isfinite(rho)) {  // breakdown; x_k is the result
+      done = 3.0;
+      break;
+    }
+    const double alpha = rho / pq;
+    const double rho_next = rho - alpha * (red[1] + red[2]) + alpha * alpha * red[3];
+    rrs = red[7] - 2.0 * alpha * red[4] + alpha * alpha * red[5];
+    beta_p = rho_next / rho;
+    alpha_p = alpha;
+    rho = rho_next;
+    ++it;
+    if (rrs <= tol2) done = 1.0;
+    else if (it >= maxit) done = 2.0;
+  }
+  if (failed) done = kDoneDeviceTimeout;
+  for (int k = 0; k < inflight; ++k) {
+    mbar_wait_bounded(smem_addr(&bars[warp][st]), (phase >> st) & 1u);
+    phase ^= 1u << st;
+    st = (st + 1 == NST) ? 0 : st + 1;
+  }
+  // the last step's x update (x_{k+1} = x_k + alpha_k p_k) when the iteration stopped by its test
+  if (done == 1.0 || done == 2.0) {
+    const T tfin = T(alpha_p);
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) {
+      const int row = 32 * (gw + j * nw) + lane;
+      if (j < ns && row < A.n_rows) {
+        const V3<T> xo = load3rw(xg, row);
+        store3(xg, row, xo.x + tfin * pr[j][0], xo.y + tfin * pr[j][1], xo.z + tfin * pr[j][2]);
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    scal[kIters] = (double)it;
+    scal[kRR] = rrs;
+    scal[kRz] = rho;
+    scal[kBeta] = beta_p;
+    scal[kDone] = done;
+  }
+  if (failed && threadIdx.x == 0) scal[kDone] = kDoneDeviceTimeout;
+}
+
+template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB>
+cudaError_t launch_onered(const Bsr& A, PcgWork& w, cudaStream_t s, bool query_only, bool* eligible) {
+  using C = PersistentCfg<T, CB, NST, WARPS>;
+  auto kern = pcg_onered_kernel<T, CB, NST, WARPS, MAXS, MINB>;
+  static std::mutex mu;
+  static int blocks_per_sm[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 64) dev = 63;
+  int bps;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!blocks_per_sm[dev]) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmemBytes);
+      int b = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, C::kThreads, C::kSmemBytes);
+      blocks_per_sm[dev] = b > 0 ? b : -1;
+    }
+    bps = blocks_per_sm[dev];
+  }
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  // part_c holds 16 doubles per w.grid CTA: 8 partials per CTA, double-buffered by iteration parity
+  int grid = bps > 0 ? w.sms * bps : 0;
+  if (grid > w.grid) grid = w.grid;
+  const int nw = grid * WARPS;
+  *eligible = coop && grid > 0 && w.z2 && w.w0 && w.w1 && w.part_c && (int64_t)nw * MAXS >= A.n_slices;
+  if (query_only || !*eligible) return cudaSuccess;
+  // W1 = w_{-1} = 0; Z1 = z_0 and P1 = p_{-1} = 0 come from the init kernel (w.z, w.p1)
+  cudaError_t e = cudaMemsetAsync(w.w1, 0, sizeof(T) * 4 * (size_t)w.n_rows, s);
+  if (e != cudaSuccess) return e;
+  const T* val = (const T*)A.val;
+  const T* minv = (const T*)w.minv;
+  T* xg = (T*)w.x;
+  const T* rg = (const T*)w.r;
+  T *Z0 = (T*)w.z2, *Z1 = (T*)w.z, *P0 = (T*)w.p0, *P1 = (T*)w.p1, *W0 = (T*)w.w0, *W1 = (T*)w.w1;
+  double* part = w.part_c;
+  double* scal = w.scal;
+  int64_t keep = w.keep_g;
+  Bsr Acopy = A;
+  void* args[] = {&Acopy, &val, &minv, &xg, &rg, &Z0, &Z1, &P0, &P1, &W0, &W1, &part, &scal, &keep};
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(C::kThreads), args, C::kSmemBytes, s);
+}
+
+template <typename T>
+cudaError_t dispatch_onered(int variant, const Bsr& A, PcgWork& w, cudaStream_t s, bool query, bool* eligible) {
+  if constexpr (sizeof(T) == 4) {
+    if (variant == 0) return launch_onered<float, 4, 2, 8, 2, 2>(A, w, s, query, eligible);
+    return launch_onered<float, 8, 2, 8, 4, 1>(A, w, s, query, eligible);
+  } else {
+    if (variant == 0) return launch_onered<double, 2, 2, 8, 2, 2>(A, w, s, query, eligible);
+    return launch_onered<double, 4, 2, 8, 4, 1>(A, w, s, query, eligible);
+  }
+}
+constexpr int kClassicVariants = 4;
+constexpr int kOneRedVariants = 2;
+
 }  // namespace
 
-int pcg_persistent_variants() { return 4; }
+int pcg_persistent_variants() { return kClassicVariants + kOneRedVariants; }
 
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant) {
   bool ok = false;
+  if (variant >= kClassicVariants) {
+    if (w.fp32) dispatch_onered<float>(variant - kClassicVariants, A, w, nullptr, true, &ok);
+    else dispatch_onered<double>(variant - kClassicVariants, A, w, nullptr, true, &ok);
+    return ok;
+  }
   PcgWork* ws[1] = {&w};
   if (w.fp32) dispatch<float, 1>(variant, A, ws, w.part_a, w.part_b, nullptr, true, &ok);
   else dispatch<double, 1>(variant, A, ws, w.part_a, w.part_b, nullptr, true, &ok);
@@ -510,14 +831,21 @@ bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant) {
 
 cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s) {
   bool ok = false;
-  PcgWork* ws[1] = {&w};
-  cudaError_t e = w.fp32 ? dispatch<float, 1>(variant, A, ws, w.part_a, w.part_b, s, false, &ok)
-                         : dispatch<double, 1>(variant, A, ws, w.part_a, w.part_b, s, false, &ok);
+  cudaError_t e;
+  if (variant >= kClassicVariants) {
+    e = w.fp32 ? dispatch_onered<float>(variant - kClassicVariants, A, w, s, false, &ok)
+               : dispatch_onered<double>(variant - kClassicVariants, A, w, s, false, &ok);
+  } else {
+    PcgWork* ws[1] = {&w};
+    e = w.fp32 ? dispatch<float, 1>(variant, A, ws, w.part_a, w.part_b, s, false, &ok)
+               : dispatch<double, 1>(variant, A, ws, w.part_a, w.part_b, s, false, &ok);
+  }
   if (e == cudaSuccess && !ok) return cudaErrorInvalidConfiguration;
   return e;
 }
 
 bool pcg_persistent2_eligible(const Bsr& A, PcgWork& w0, PcgWork& w1, int variant) {
+  if (variant >= kClassicVariants) return false;  // the one-reduction form runs one right-hand side
   bool ok = false;
   PcgWork* ws[2] = {&w0, &w1};
   if (w0.fp32) dispatch<float, 2>(variant, A, ws, nullptr, nullptr, nullptr, true, &ok);
@@ -527,6 +855,7 @@ bool pcg_persistent2_eligible(const Bsr& A, PcgWork& w0, PcgWork& w1, int varian
 
 cudaError_t launch_pcg_persistent2(const Bsr& A, PcgWork& w0, PcgWork& w1, int variant, double* part_a,
                                    double* part_b, cudaStream_t s) {
+  if (variant >= kClassicVariants) return cudaErrorInvalidConfiguration;
   bool ok = false;
   PcgWork* ws[2] = {&w0, &w1};
   cudaError_t e = w0.fp32 ? dispatch<float, 2>(variant, A, ws, part_a, part_b, s, false, &ok)

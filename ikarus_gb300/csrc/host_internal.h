@@ -348,8 +348,8 @@ struct ikr_ls_s {
   ikr::PcgWork w;
   DBuf<double> dx, dp, dq, dmv, pa, pb, scal;
   DBuf<float> fx, fp, fq, fmv;
-  DBuf<double> dz, dr, dp1;
-  DBuf<float> fz, fr, fp1;
+  DBuf<double> dz, dr, dp1, dzb, dw0, dw1, pc;  // dzb / fzb, dw / fw: one-reduction CG (second z, w = M^-1 q)
+  DBuf<float> fz, fr, fp1, fzb, fw0, fw1;
   double* scal_h = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaEvent_t tev[2] = {nullptr, nullptr};  // timing events of the SpMV tuner
@@ -424,11 +424,17 @@ struct ikr_ls_s {
     tuned_for = nullptr;
     if (fp32) {
       fx.alloc(n), fr.alloc(n), fz.alloc(n), fp.alloc(n), fp1.alloc(n), fq.alloc(n), fmv.alloc(9 * (size_t)nr);
+      fzb.alloc(n), fw0.alloc(n), fw1.alloc(n);
       w.x = fx.p, w.r = fr.p, w.z = fz.p, w.p0 = fp.p, w.p1 = fp1.p, w.q = fq.p, w.minv = fmv.p;
+      w.z2 = fzb.p, w.w0 = fw0.p, w.w1 = fw1.p;
     } else {
       dx.alloc(n), dr.alloc(n), dz.alloc(n), dp.alloc(n), dp1.alloc(n), dq.alloc(n), dmv.alloc(9 * (size_t)nr);
+      dzb.alloc(n), dw0.alloc(n), dw1.alloc(n);
       w.x = dx.p, w.r = dr.p, w.z = dz.p, w.p0 = dp.p, w.p1 = dp1.p, w.q = dq.p, w.minv = dmv.p;
+      w.z2 = dzb.p, w.w0 = dw0.p, w.w1 = dw1.p;
     }
+    pc.alloc(16 * (size_t)w.grid);
+    w.part_c = pc.p;
     pa.alloc(2 * (size_t)w.grid);  // two-kernel CG: 1 per block; persistent CG: 2 per CTA (parity)
     pb.alloc(4 * (size_t)w.grid);  // two-kernel CG: 2 per block; persistent CG: 4 per CTA
     scal.alloc(ikr::kNScal);

@@ -157,6 +157,12 @@ struct PcgWork {
   int spmv_kind = 0;           // 0: direct loads (solver.cu); 1 + v: staged variant v (spmv_staged.cu);
                                // 1 + staged variants + v: persistent CG variant v (cg_persistent.cu)
   int64_t keep_g = 0;          // staged: matrix blocks [0, keep_g) are copied with an L2 evict_last policy
+  // one-reduction persistent CG (variants 4 and 5 of cg_persistent.cu): a second z buffer, the two buffers of
+  // w = M^-1 q and 16 partials per grid CTA
+  void* z2 = nullptr;
+  void* w0 = nullptr;
+  void* w1 = nullptr;
+  double* part_c = nullptr;
 };
 void launch_block_jacobi(const Bsr& A, bool fp32, void* minv, bool point_jacobi, cudaStream_t s);
 void launch_pcg_init(const Bsr& A, PcgWork& w, const double* b, double rtol, int max_iter, cudaStream_t s);

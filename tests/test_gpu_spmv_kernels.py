@@ -15,9 +15,10 @@ def true_residual_bound(fp32):
     return 2e-3 if fp32 else 1e-10
 
 
-# 0 direct-load SpMV, 1-4 staged SpMV variants, 5-8 persistent CG variants; keep = L2 evict_last share
+# 0 direct-load SpMV, 1-4 staged SpMV variants, 5-8 persistent CG variants, 9-10 one-reduction persistent CG;
+# keep = L2 evict_last share
 KINDS = [(0, 0.0), (1, 0.0), (2, 0.0), (3, 0.0), (4, 0.0), (1, 0.5), (2, 0.75), (5, 0.0), (6, 0.0), (7, 0.0),
-         (8, 0.0), (5, 0.4)]
+         (8, 0.0), (5, 0.4), (9, 0.0), (10, 0.0), (9, 0.45)]
 
 
 @pytest.fixture(scope="module", params=[0, 1], ids=["fp64", "fp32"])
@@ -55,7 +56,7 @@ def test_tuner_choice_is_reported(ikr, system):
     ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-5 if fp32 else 1e-11)
     ls.compute(asm)
     kind, keep, us = ls.kernel_info()
-    assert 0 <= kind <= 8 and 0.0 <= keep < 1.0 and us > 0.0
+    assert 0 <= kind <= 10 and 0.0 <= keep < 1.0 and us > 0.0
     x = ls.solve(asm, b)
     assert np.linalg.norm(K @ x - b) <= true_residual_bound(fp32) * np.linalg.norm(b)
 
