@@ -487,12 +487,18 @@ cudaError_t dispatch(int variant, const Bsr& A, PcgWork* const* ws, double* pa, 
     if (variant == 0) return launch_persistent<float, 8, 2, 8, 4, 1, NR>(A, ws, pa, pb, s, query, eligible);
     if (variant == 1) return launch_persistent<float, 4, 3, 8, 8, 1, NR>(A, ws, pa, pb, s, query, eligible);
     if (variant == 2) return launch_persistent<float, 4, 2, 8, 2, 2, NR>(A, ws, pa, pb, s, query, eligible);
-    return launch_persistent<float, 2, 3, 8, 2, 3, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 3) return launch_persistent<float, 2, 3, 8, 2, 3, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 4) return launch_persistent<float, 4, 2, 16, 2, 1, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 5) return launch_persistent<float, 4, 2, 12, 3, 1, NR>(A, ws, pa, pb, s, query, eligible);
+    return launch_persistent<float, 5, 2, 16, 2, 1, NR>(A, ws, pa, pb, s, query, eligible);
   } else {
     if (variant == 0) return launch_persistent<double, 4, 2, 8, 4, 1, NR>(A, ws, pa, pb, s, query, eligible);
     if (variant == 1) return launch_persistent<double, 2, 3, 8, 4, 1, NR>(A, ws, pa, pb, s, query, eligible);
     if (variant == 2) return launch_persistent<double, 2, 2, 8, 2, 2, NR>(A, ws, pa, pb, s, query, eligible);
-    return launch_persistent<double, 1, 3, 8, 2, 2, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 3) return launch_persistent<double, 1, 3, 8, 2, 2, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 4) return launch_persistent<double, 2, 2, 16, 2, 1, NR>(A, ws, pa, pb, s, query, eligible);
+    if (variant == 5) return launch_persistent<double, 2, 2, 12, 3, 1, NR>(A, ws, pa, pb, s, query, eligible);
+    return launch_persistent<double, 1, 3, 16, 2, 1, NR>(A, ws, pa, pb, s, query, eligible);
   }
 }
 
@@ -809,7 +815,7 @@ cudaError_t dispatch_onered(int variant, const Bsr& A, PcgWork& w, cudaStream_t 
     return launch_onered<double, 4, 2, 8, 4, 1>(A, w, s, query, eligible);
   }
 }
-constexpr int kClassicVariants = 4;
+constexpr int kClassicVariants = 7;
 constexpr int kOneRedVariants = 2;
 
 }  // namespace

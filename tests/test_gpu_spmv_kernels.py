@@ -15,10 +15,10 @@ def true_residual_bound(fp32):
     return 2e-3 if fp32 else 1e-10
 
 
-# 0 direct-load SpMV, 1-4 staged SpMV variants, 5-8 persistent CG variants, 9-10 one-reduction persistent CG;
+# 0 direct-load SpMV, 1-4 staged SpMV variants, 5-11 persistent CG variants, 12-13 one-reduction persistent CG;
 # keep = L2 evict_last share
 KINDS = [(0, 0.0), (1, 0.0), (2, 0.0), (3, 0.0), (4, 0.0), (1, 0.5), (2, 0.75), (5, 0.0), (6, 0.0), (7, 0.0),
-         (8, 0.0), (5, 0.4), (9, 0.0), (10, 0.0), (9, 0.45)]
+         (8, 0.0), (9, 0.0), (10, 0.0), (11, 0.0), (5, 0.4), (12, 0.0), (13, 0.0), (12, 0.45)]
 
 
 @pytest.fixture(scope="module", params=[0, 1], ids=["fp64", "fp32"])
@@ -56,12 +56,12 @@ def test_tuner_choice_is_reported(ikr, system):
     ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-5 if fp32 else 1e-11)
     ls.compute(asm)
     kind, keep, us = ls.kernel_info()
-    assert 0 <= kind <= 10 and 0.0 <= keep < 1.0 and us > 0.0
+    assert 0 <= kind <= 13 and 0.0 <= keep < 1.0 and us > 0.0
     x = ls.solve(asm, b)
     assert np.linalg.norm(K @ x - b) <= true_residual_bound(fp32) * np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("kind", [5, 6, 7, 8])
+@pytest.mark.parametrize("kind", [5, 6, 7, 8, 9, 10, 11])
 def test_two_rhs_persistent_solve_matches_two_solves(ikr, system, kind):
     """Two right-hand sides in one persistent launch (the matrix streamed once per iteration for both) give
     bit-identical solutions and the same iteration counts as two single solves: each RHS keeps its own scalars and
