@@ -662,11 +662,21 @@ def run_eas(args):
         stream, ev0, ev1 = make_events(torch, fes.stream())
         torch.cuda.synchronize()
         ev0.record(stream)
-        info = lc.run(req)
+        key = "mixed" if mixed else "plain_fp64"
+        try:
+            info = lc.run(req)
+        except ikr.IkarusError as e:  # e.g. an iterate that inverts an element (the reference aborts there)
+            ev1.record(stream)
+            ev1.synchronize()
+            out[key] = {"s": round(ev0.elapsed_time(ev1) / 1e3, 3), "success": False, "error": str(e),
+                        "steps_completed": max(len(us) - 1, 0), "spmv_kernel": ls.kernel_info()[:2]}
+            per_step[key] = us
+            log(f"eas {key}: failed after {out[key]['s']} s: {e}")
+            del lc, nr, ls, asm, fes
+            continue
         ev1.record(stream)
         ev1.synchronize()
         t = ev0.elapsed_time(ev1) / 1e3  # includes the observer's per-step downloads
-        key = "mixed" if mixed else "plain_fp64"
         out[key] = {"s": round(t, 3), "success": bool(info.success), "newton_iterations": info.totalIterations,
                     "cg_iterations": info.totalLinearIterations,
                     "newton_per_step": [si.iterations for si in info.solverInfos], "spmv_kernel": ls.kernel_info()[:2]}
@@ -678,8 +688,9 @@ def run_eas(args):
         out["mixed"]["max_rel_diff_vs_plain_per_step"] = [
             float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
             for a, b in zip(per_step["mixed"], per_step["plain_fp64"])]
-    out["value"] = out["mixed"]["s"]
-    out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 3)
+    out["value"] = out["mixed"]["s"] if out["mixed"]["success"] else None
+    if out["mixed"]["success"] and out["plain_fp64"]["success"]:
+        out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 3)
     print(json.dumps(out))
 
 
