@@ -146,3 +146,22 @@ def test_mixed_arc_length_is_on_the_path(ikr, multi):
     lams = np.array([st[1] for st in states])
     np.testing.assert_allclose(lams, ref["lambdas"], rtol=1e-6, atol=1e-12)
     assert np.abs(states[-1][2] - ref["u"]).max() <= 1e-5 * np.abs(ref["u"]).max()
+
+
+def test_path_following_argument_errors(ikr):
+    """PathFollowing with steps <= 0 is an InvalidStateException (pathfollowing.hh:192-193); displacement control
+    on a constrained or repeated dof is rejected before any solve."""
+    p = _problem()
+    fes, asm = problems.build_gpu(p)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(ikr.NRSettings(), ikr.LinearSolver()))
+    with pytest.raises(ikr.IkarusError) as e:
+        ikr.PathFollowing(nr, 0, 0.1)
+    assert e.value.code == -3
+    fixed = int(np.nonzero(p.fixed)[0][0])
+    free = int(np.nonzero(p.fixed == 0)[0][0])
+    with pytest.raises(ikr.IkarusError):
+        ikr.PathFollowing(nr, 2, 0.1, ikr.DisplacementControl([fixed]))
+    with pytest.raises(ikr.IkarusError):
+        ikr.PathFollowing(nr, 2, 0.1, ikr.DisplacementControl([free, free]))
+    pf = ikr.PathFollowing(nr, 2, 0.1, ikr.DisplacementControl([free]))
+    assert pf.name() == "Path following with Displacement Control"
