@@ -20,7 +20,7 @@
 extern "C" {
 #endif
 
-/* ---- status codes (replace DUNE_THROW / abort(); SURVEY error conventions) ---------------------------- */
+/* ---- status codes (replace DUNE_THROW / abort(): no exception crosses the C ABI) ----------------------- */
 enum {
   IKR_OK = 0,
   IKR_ERR_ARG = -1,

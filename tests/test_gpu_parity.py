@@ -1,6 +1,6 @@
 """GPU parity: the CUDA path (through the C ABI) against the CPU oracle on the same seeded inputs.
 
-Tolerances (the spec bar): FP64 element and assembled residual / stiffness within 1e-12 relative
+Tolerances: FP64 element and assembled residual / stiffness within 1e-12 relative
 (max-norm, relative to the largest entry of the oracle's result); sparsity patterns and Dirichlet maps
 bit-exact; FP32 tangents within 1e-6 relative; converged displacements within 1e-8 relative.
 """
