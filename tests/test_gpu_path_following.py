@@ -165,3 +165,25 @@ def test_path_following_argument_errors(ikr):
         ikr.PathFollowing(nr, 2, 0.1, ikr.DisplacementControl([free, free]))
     pf = ikr.PathFollowing(nr, 2, 0.1, ikr.DisplacementControl([free]))
     assert pf.name() == "Path following with Displacement Control"
+
+
+def test_cpp_facade_arc_length_matches_oracle(ikr, tmp_path):
+    """PathFollowing through the C++ facade (tests/cpp/arclength.cpp) on the reference's 3D cantilever test mesh
+    with H9 EAS and point loads: final load factor and max |d| of five arc-length steps as the oracle's."""
+    import json
+    import os
+    import subprocess
+
+    from ikarus_gb300 import build
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    gold = json.load(open(os.path.join(root, "tests", "golden", "reference_goldens.json")))["cantilever_3d"]
+    p = problems.cantilever_golden(2, gold["eas_parameters"]["DisplacementGradient"])
+    s = _step_size(p, 0.1)
+    ref = oracle.from_problem(p).path_following(5, s, tol=1e-10, max_iter=30)
+    exe = str(tmp_path / "arclength")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(root, "include"),
+                    os.path.join(root, "tests", "cpp", "arclength.cpp"), "-L" + build.OUT, "-likarus_gb300",
+                    "-Wl,-rpath," + build.OUT, "-o", exe], check=True)
+    r = subprocess.run([exe, "2", "9", "5", repr(s), repr(ref["lam"]), repr(float(np.abs(ref["u"]).max()))],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
