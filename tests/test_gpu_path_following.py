@@ -184,6 +184,6 @@ def test_cpp_facade_arc_length_matches_oracle(ikr, tmp_path):
     subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(root, "include"),
                     os.path.join(root, "tests", "cpp", "arclength.cpp"), "-L" + build.OUT, "-likarus_gb300",
                     "-Wl,-rpath," + build.OUT, "-o", exe], check=True)
-    r = subprocess.run([exe, "2", "9", "5", repr(s), repr(ref["lam"]), repr(float(np.abs(ref["u"]).max()))],
-                       capture_output=True, text=True, timeout=300)
+    args = [repr(float(v)) for v in (s, ref["lam"], np.abs(ref["u"]).max())]
+    r = subprocess.run([exe, "2", "9", "5", *args], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
