@@ -320,6 +320,8 @@ def assembly_rates(ikr, torch, form, p):
                      "algorithmic_bytes": nbytes, "achieved_gbs": round(nbytes / t / 1e9, 1)}
     epb = form.fes.kernel_info()
     out["elements_per_block"] = {"residual": epb[0], "tangent_fp64": epb[1], "tangent_fp32": epb[2]}
+    if form.mixed:  # the FP32 tangent kernel the timed choice kept (1 coloured element kernel, 2 row kernel)
+        out["tangent_fp32_kernel"] = form.asm.tangent_kernel()
     return out
 
 

@@ -194,6 +194,8 @@ SIGNATURES = {
     "ikr_load_control_run": ([_vp, _vp, C.POINTER(_ControlInfo), C.POINTER(_NRInfo), _I], C.c_int),
     "ikr_load_control_set_predictor": ([_vp, _I, _vp, _dp, _I], C.c_int),
     "ikr_linear_solver_set_multi_rhs": ([_vp, _I], C.c_int),
+    "ikr_assembler_set_tangent_kernel": ([_vp, _I], C.c_int),
+    "ikr_assembler_tangent_kernel": ([_vp, _ip], C.c_int),
     "ikr_linear_solver_solve2": ([_vp, _vp, _dp, _dp, _dp, _dp], C.c_int),
     "ikr_path_following_create": ([C.POINTER(_vp), _vp, _I, _D, _I, _I, _ip], C.c_int),
     "ikr_path_following_destroy": ([_vp], C.c_int),
@@ -528,6 +530,16 @@ class SparseFlatAssembler:
         if req is None:
             raise IkarusError(-3, "assembler not bound")
         return req, DBCOption(self._dbc if dbc is None else dbc)
+
+    def set_tangent_kernel(self, path=0):
+        """FP32 displacement-based NeoHooke tangent: 1 coloured element kernel, 2 row kernel, 0 timed choice."""
+        _err(lib().ikr_assembler_set_tangent_kernel(self.h, int(path)))
+
+    def tangent_kernel(self):
+        """The FP32 tangent kernel in use (0 = not chosen yet, 1 coloured, 2 rows)."""
+        v = C.c_int32()
+        _err(lib().ikr_assembler_tangent_kernel(self.h, C.byref(v)))
+        return v.value
 
     def set_dirichlet_values(self, rate):
         """Inhomogeneous Dirichlet values lambda * rate on constrained dofs (storeInhomogeneousBoundaryCondition for

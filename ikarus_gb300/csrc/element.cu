@@ -348,6 +348,131 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
   }
 }
 
+
+// Tangent assembly by block rows (displacement-based NeoHooke): one thread per node row I.  For every element
+// adjacent to I (ascending element index) the thread evaluates the element's 8 Gauss points and adds row a of the
+// element tangent (a = I's corner), K_aJ for the 8 corners J, into its own row's blocks:
+//   K_aJ += w [lambda g_a (x) g_J + (mu - lambda ln J) g_J (x) g_a + mu (dN_a . dN_J) I],  g = F^-T grad N.
+// No two threads write a block, so there is no colouring and one launch; the 32 rows of a warp are one slice,
+// whose blocks of equal k lie side by side in the entry-interleaved layout, so a warp's read-modify-writes
+// coalesce.  The Gauss-point kinematics of an element are evaluated once per adjacent node (8 times): arithmetic
+// traded for colouring-free, coalesced writes.
+template <typename KT>
+__global__ void __launch_bounds__(128) row_tangent_kernel(ElemArgs a, const int32_t* __restrict__ ne_ptr,
+                                                        const int32_t* __restrict__ ne_elems) {
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= a.n_nodes) return;
+  const int ne = a.n_elems;
+  const uint8_t fmaskI = a.node_fixed ? a.node_fixed[I] : uint8_t(0);
+  KT* val = static_cast<KT*>(a.Kval);
+  for (int t = ne_ptr[I]; t < ne_ptr[I + 1]; ++t) {
+    const int e = ne_elems[t];
+    int nodes[8];
+    int ai = 0;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      nodes[v] = a.conn[v * ne + e];
+      if (nodes[v] == I) ai = v;
+    }
+    // coordinates and displacements relative to the element's first corner (as the element kernel does)
+    KT dX[8][3], dU[8][3];
+    {
+      double x0[3], u0[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        x0[c] = a.X[3 * nodes[0] + c];
+        u0[c] = a.u ? a.u[3 * nodes[0] + c] : 0.0;
+      }
+#pragma unroll
+      for (int v = 0; v < 8; ++v)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          dX[v][c] = KT(a.X[3 * nodes[v] + c] - x0[c]);
+          dU[v][c] = KT((a.u ? a.u[3 * nodes[v] + c] : 0.0) - u0[c]);
+        }
+    }
+    const KT lam = KT(a.lam_e ? a.lam_e[e] : a.lam), mu = KT(a.mu_e ? a.mu_e[e] : a.mu);
+    KT K[8][3][3];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) K[j][r][c] = KT(0);
+    int bad = 0;
+#pragma unroll 1
+    for (int q = 0; q < 8; ++q) {
+      KT J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        KT d[3];
+        ref_gradient_at_gp<KT>(v, q, d);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) J[r][c] += dX[v][r] * d[c];
+      }
+      KT Ji[3][3];
+      const KT detJ = inv3(J, Ji);
+      KT F[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        KT d[3], dn[3];
+        ref_gradient_at_gp<KT>(v, q, d);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] = d[0] * Ji[0][k] + d[1] * Ji[1][k] + d[2] * Ji[2][k];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) F[r][c] += dU[v][r] * dn[c];
+      }
+      KT Fi[3][3];
+      const KT detF = inv3(F, Fi);
+      if (!(detF * detF > KT(1e-10)) || !(detF > KT(0))) bad |= kStatusNonPositiveDetC;
+      const KT lnJ = log(detF);
+      const KT w = KT(kGaussW) * detJ;
+      const KT wl = w * lam, wc = w * (mu - lam * lnJ), wm = w * mu;
+      KT dna[3], ga[3];
+      {
+        KT d[3];
+        ref_gradient_at_gp<KT>(ai, q, d);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dna[k] = d[0] * Ji[0][k] + d[1] * Ji[1][k] + d[2] * Ji[2][k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) ga[k] = Fi[0][k] * dna[0] + Fi[1][k] * dna[1] + Fi[2][k] * dna[2];
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        KT d[3], dn[3], gj[3];
+        ref_gradient_at_gp<KT>(j, q, d);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) dn[k] = d[0] * Ji[0][k] + d[1] * Ji[1][k] + d[2] * Ji[2][k];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) gj[k] = Fi[0][k] * dn[0] + Fi[1][k] * dn[1] + Fi[2][k] * dn[2];
+        const KT dd = wm * (dna[0] * dn[0] + dna[1] * dn[1] + dna[2] * dn[2]);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) K[j][r][c] += wl * ga[r] * gj[c] + wc * gj[r] * ga[c] + (r == c ? dd : KT(0));
+      }
+    }
+    if (bad) {
+      if (a.inst_status) atomicOr(a.inst_status + a.elem_inst[e], bad);
+      else if (a.status) atomicOr(a.status, bad);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const uint8_t fmaskJ = a.node_fixed ? a.node_fixed[nodes[j]] : uint8_t(0);
+      KT* b = val + block_entry(a.slot[(size_t)(ai * 8 + j) * ne + e], 0);
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if (!(((fmaskI >> r) | (fmaskJ >> c)) & 1)) b[32 * (3 * r + c)] += K[j][r][c];
+    }
+  }
+}
+
 // Dead traction at load factor 1 on the element's Neumann faces, 1-point rule per face
 // (loads/traction.hh:122-135: quadrature order = order() = 1 -> the face centre, weight 1):
 // trac[slot][3v+c] = sum_faces N_v(centre) t_c dA.  One thread per loaded element, faces in input order.
@@ -666,6 +791,11 @@ void launch_disp_t(const ElemArgs& a, const int32_t* list, int n_list, int e_bas
 }
 
 }  // namespace
+
+void launch_row_tangent(const ElemArgs& a, const int32_t* ne_ptr, const int32_t* ne_elems, cudaStream_t s) {
+  // FP32 only: the FP64 form of this kernel exceeds the register file (the coloured element kernel assembles it)
+  row_tangent_kernel<float><<<(a.n_nodes + 127) / 128, 128, 0, s>>>(a, ne_ptr, ne_elems);
+}
 
 void launch_disp_element(const ElemArgs& a, int mode, bool fp32_tangent, const int32_t* list, int n_list, int e_base,
                          cudaStream_t s) {

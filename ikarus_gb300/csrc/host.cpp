@@ -158,7 +158,40 @@ void assemble_matrix(ikr_asm a, ikr_req r, int dbc) {
     ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
   }
   args.epb = epb_k;
-  f->launch_coloured(args, ikr::kWantK, a->fp32);
+  // FP32 displacement-based NeoHooke: the coloured element kernel or the row kernel, whichever is faster
+  const bool row_ok = a->fp32 && f->na == 0 && f->material == 0 && f->n_inst == 0;
+  if (row_ok && a->tan_req) a->tan_path = a->tan_req;
+  if (row_ok && !a->tan_path) {
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int path : {1, 2}) {
+      float t = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
+        CK(cudaEventRecord(e0, f->stream));
+        if (path == 1) f->launch_coloured(args, ikr::kWantK, true);
+        else ikr::launch_row_tangent(args, a->ne_ptr.p, a->ne_elems.p, f->stream);
+        CK(cudaEventRecord(e1, f->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        t = std::min(t, ms);
+      }
+      f->check_status();
+      if (t < best) best = t, a->tan_path = path;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
+  }
+  if (row_ok && a->tan_path == 2) {
+    ikr::launch_row_tangent(args, a->ne_ptr.p, a->ne_elems.p, f->stream);
+    count(1);
+  } else {
+    f->launch_coloured(args, ikr::kWantK, a->fp32);
+  }
   a->matrix_dbc = dbc;
   f->check_status();
 }
@@ -806,6 +839,19 @@ int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t kind, double keep) {
              (keep == -1.0 || (keep >= 0.0 && keep < 1.0)),
          IKR_ERR_ARG, "invalid SpMV kernel choice");
     ls->set_kernel(kind, keep);
+  });
+}
+int ikr_assembler_set_tangent_kernel(ikr_asm a, int32_t path) {
+  return guarded([&] {
+    need(a && path >= 0 && path <= 2, IKR_ERR_ARG, "tangent kernel: 0 timed choice, 1 coloured, 2 rows");
+    a->tan_req = path;
+    a->tan_path = path;
+  });
+}
+int ikr_assembler_tangent_kernel(ikr_asm a, int32_t* path) {
+  return guarded([&] {
+    need(a && path, IKR_ERR_ARG, "null argument");
+    *path = a->tan_path;
   });
 }
 int ikr_linear_solver_set_multi_rhs(ikr_ls ls, int32_t on) {

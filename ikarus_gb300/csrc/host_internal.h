@@ -253,6 +253,9 @@ struct ikr_asm_s {
   // pattern
   int64_t nb = 0, npad = 0;
   int nslices = 0;
+  DBuf<int32_t> ne_ptr, ne_elems;  // elements of every node, ascending (row-tangent kernel)
+  // FP32 tangent kernel: 0 = not chosen yet, 1 = coloured element kernel, 2 = row kernel; req = forced choice
+  int tan_path = 0, tan_req = 0;
   DBuf<int32_t> row_ptr, col, diag, slot, slice_off, col_sell;
   std::vector<int32_t> row_ptr_h, col_h, slice_off_h;
   DBuf<double> val64;
@@ -287,7 +290,7 @@ struct ikr_asm_s {
   void build_pattern() {
     ikr_fes f = fes;
     cudaStream_t s = f->stream;
-    DBuf<int32_t> cnt, ne_ptr, cursor, ne_elems, rcnt;
+    DBuf<int32_t> cnt, cursor, rcnt;
     cnt.alloc(f->nn);
     ne_ptr.alloc(f->nn + 1);
     cursor.alloc(f->nn);

@@ -80,6 +80,9 @@ void launch_disp_element(const ElemArgs& a, int mode, bool fp32_tangent, const i
                          cudaStream_t s);
 void launch_eas_element(const ElemArgs& a, int mode, bool fp32_tangent, const int32_t* list, int n_list, int e_base,
                         cudaStream_t s);
+// displacement-based NeoHooke FP32 tangent by block rows (thread per node row, no colouring; element.cu);
+// ne_ptr / ne_elems: the elements of every node in ascending order
+void launch_row_tangent(const ElemArgs& a, const int32_t* ne_ptr, const int32_t* ne_elems, cudaStream_t s);
 void launch_eas_geometry(const ElemArgs& a, double* geo_out, cudaStream_t s);
 void launch_eas_update(const ElemArgs& a, double* alpha, const double* correction, cudaStream_t s);
 int eas_geo_stride(int eas_kind);

@@ -201,6 +201,12 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
  * next factorize from timed CG iterations on the assembled tangent and kept for that assembler.  info
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fraction);
+/* no reference counterpart: the kernel of the FP32 displacement-based NeoHooke tangent -- 1: coloured element
+ * kernel (8 lanes per element, one launch per colour class), 2: row kernel (a thread per node row adds its row of
+ * every adjacent element's tangent, one launch, no colouring), 0 (default): the faster of the two, timed at the
+ * first assembly.  Both give the same FP32 tangent up to the order of the FP32 additions. */
+int ikr_assembler_set_tangent_kernel(ikr_asm a, int32_t path);
+int ikr_assembler_tangent_kernel(ikr_asm a, int32_t* path);
 /* no reference counterpart: solves with two right-hand sides and one tangent (path following's bordered
  * system) run both CGs in one persistent launch that streams the matrix once per iteration (on = 1, default)
  * or one after the other (0) */
