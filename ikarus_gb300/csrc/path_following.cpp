@@ -133,15 +133,23 @@ void pf_solve(ikr_pf pf, ikr_req r, ikr_nr_info* info) {
   // Fext0 = -R(u = 0, lambda = 1): the load is lambda Fext0 (:225-232)
   CK(cudaMemcpyAsync(pf->u_save.p, r->u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
   const double lam_save = r->lambda;
+  auto restore = [&]() {
+    CK(cudaMemcpyAsync(r->u.p, pf->u_save.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    r->lambda = lam_save;
+    r->version++;
+  };
   CK(cudaMemsetAsync(r->u.p, 0, sizeof(double) * n, s));
   r->lambda = 1.0;
   r->version++;
-  assemble_vector(a, r, IKR_DBC_FULL);
+  try {
+    assemble_vector(a, r, IKR_DBC_FULL);
+  } catch (...) {
+    restore();  // the caller's state is left as it was
+    throw;
+  }
   ikr::launch_scale64(pf->fext0.p, a->R.p, -1.0, n, s);
   count(1);
-  CK(cudaMemcpyAsync(r->u.p, pf->u_save.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-  r->lambda = lam_save;
-  r->version++;
+  restore();
   assemble_vector(a, r, IKR_DBC_FULL);
   subsidiary(pf, a, r);
   double rnorm = device_norm(f, a->R.p, n, nr->nrm_part, nr->nrm_out);  // :244, without f
