@@ -565,10 +565,11 @@ struct ikr_ls_s {
       }
       return best_us;
     };
-    // persistent kinds: a solve of kTimed iterations after one untimed solve, per iteration
+    // persistent kinds: a solve of kTimed iterations after one untimed solve, per iteration (long enough that the
+    // launch overhead and run-to-run noise stay below the few per cent that separate the variants)
     auto time_persistent = [&](int kind, double keep) {
       apply(kind, keep);
-      constexpr int kTimed = 40;
+      constexpr int kTimed = 160;
       double us = 1e300;
       for (int rep = 0; rep < 4; ++rep) {  // the first run warms up; the least of the other three counts
         ikr::launch_pcg_init(A, w, b64.p, 0.0, kTimed, s);
