@@ -523,7 +523,7 @@ struct ikr_ls_s {
   }
 
   // SpMV kernel and L2 keep fraction: the requested ones, or the fastest of timed CG iterations (right-hand
-  // side of ones, tolerance 0) on the assembled tangent.  The kinds are timed with nothing kept in L2, then
+  // side of ones, tolerance 0) on the assembled tangent.  The kinds are timed with an L2 keep share of 0.45, then
   // the keep fractions in increasing order with the fastest kind.
   void tune(ikr_asm a) {
     drop_graphs();
@@ -590,13 +590,15 @@ struct ikr_ls_s {
     int best_kind = spmv_req >= 0 ? spmv_req : 0;
     double best = 1e300;
     if (spmv_req < 0) {
+      // the kinds are compared with a mid L2 keep share (the share changes their ranking), kind 0 has none
+      constexpr double kProbeKeep = 0.45;
       for (int k = 0; k <= ikr::spmv_staged_variants(); ++k) {
-        const double us = time_it(k, 0.0);
+        const double us = time_it(k, k > 0 ? kProbeKeep : 0.0);
         if (us < best) best = us, best_kind = k;
       }
       for (int v = 0; v < ikr::pcg_persistent_variants(); ++v) {
         if (!ikr::pcg_persistent_eligible(A, w, v)) continue;
-        const double us = time_persistent(first_persistent_kind() + v, 0.0);
+        const double us = time_persistent(first_persistent_kind() + v, kProbeKeep);
         if (us < best) best = us, best_kind = first_persistent_kind() + v;
       }
       // the two-kernel CG state was advanced by the persistent trials' inits: restart it for the keep trials
