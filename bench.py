@@ -52,6 +52,11 @@ def parse():
                     help="mixed form's Newton predictor: 0 none (the reference's), 1 previous increment (the learned "
                          "predictor's fallback; this single load case has no trained model), 3 second-order "
                          "extrapolation with the previous increment as fallback")
+    ap.add_argument("--coarse", type=int, default=32,
+                    help="slabs of the CG's coarse correction for the extra two-level measurement beside the "
+                         "headline (0: skip it)")
+    ap.add_argument("--two-level-only", action="store_true",
+                    help="only the two-level measurement (mixed and plain FP64 with the coarse correction)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--small", action="store_true", help="32x8x8 mesh (profiling runs)")
     ap.add_argument("--config", type=int, default=2, choices=[2, 3, 4, 5],
@@ -155,11 +160,13 @@ def solver_settings(ikr, mixed: bool, eta=(2e-2, 1e-5)):
 class Form:
     """One solution form (mixed or plain) on the GPU: element set, assembler, solver objects, requirements."""
 
-    def __init__(self, ikr, problems, p, mixed, predictor=0, eta=(1e-2, 1e-5)):
+    def __init__(self, ikr, problems, p, mixed, predictor=0, eta=(1e-2, 1e-5), coarse=0):
         self.ikr = ikr
         self.mixed = mixed
         self.fes, self.asm = problems.build_gpu(p, precision=1 if mixed else 0)
         self.ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
+        if coarse:
+            self.ls.set_coarse_space(coarse)
         self.nr = ikr.NewtonRaphson(self.asm, ikr.NewtonRaphsonConfig(solver_settings(ikr, mixed, eta), self.ls))
         self.lc = ikr.LoadControl(self.nr, p.load_steps, (0.0, p.t_end))
         if predictor:
@@ -286,8 +293,78 @@ def run_ours(args, rank, world):
     u_mixed = mixed.req.globalSolution()
     rel_diff = float(np.abs(u_mixed - u_plain).max() / np.abs(u_plain).max())
     assembly["plain_fp64"] = assembly_rates(ikr, torch, plain, p)
-    return finish(args, p, world, t_mixed, t_e2e, t_plain, plain_infos[-1], infos, launches, mixed, n_nodes, spmv_ms,
-                  spmv_n, clocks, rel_diff, prof_solves, assembly), p
+    out = finish(args, p, world, t_mixed, t_e2e, t_plain, plain_infos[-1], infos, launches, mixed, n_nodes, spmv_ms,
+                 spmv_n, clocks, rel_diff, prof_solves, assembly)
+    del plain, mixed
+    if args.coarse > 0:
+        out["two_level"] = run_two_level(args, ikr, torch, problems, p, u_plain, t_plain)
+    return out, p
+
+
+def run_two_level(args, ikr, torch, problems, p, u_plain, t_plain_bj):
+    """Not the headline (whose method is block-Jacobi PCG): the same load path with the CG's coarse correction
+    (LinearSolver.set_coarse_space, an additive two-level preconditioner with the rigid-body modes of
+    `args.coarse` slabs), mixed form (one untimed and two timed paths) and plain FP64 form (one path), device
+    time with the same 256 MB L2 flush before each path."""
+    import numpy as np
+
+    res = {"slabs": args.coarse, "preconditioner": "block Jacobi + P A_c^-1 P^T (six rigid-body modes per slab, "
+                                                    "A_c = P^T K P rebuilt at every factorize)"}
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    try:
+        for key, mixed, runs in (("mixed", True, 3), ("plain_fp64", False, 1)):
+            f = Form(ikr, problems, p, mixed=mixed, predictor=args.predictor if mixed else 0,
+                     eta=(args.eta_max, args.eta_min), coarse=args.coarse)
+            st, e0, e1 = make_events(torch, f.fes.stream())
+            times = []
+            for k in range(runs):
+                f.req.assign(f.req0)
+                flush.zero_()
+                torch.cuda.synchronize()
+                e0.record(st)
+                info = f.lc.run(f.req)
+                e1.record(st)
+                e1.synchronize()
+                assert info.success, f"two-level {key} load path failed"
+                if not mixed or k > 0:
+                    times.append(e0.elapsed_time(e1) / 1e3)
+                log(f"two-level {key}: {e0.elapsed_time(e1) / 1e3:.3f} s, newton {info.totalIterations}, "
+                    f"cg {info.totalLinearIterations}, {f.ls.coarse_info()}")
+            u = f.req.globalSolution()
+            if mixed:  # cost split on the last tangent: factorize (with A_c) and CG iterations, with and without
+                b = np.where(p.fixed == 1, 0.0, 1.0)
+                split = {}
+                for slabs in (args.coarse, 0):
+                    ls2 = ikr.LinearSolver(rtol=1e-5, max_iter=20000)
+                    ls2.set_coarse_space(slabs)
+                    ls2.compute(f.asm)  # the kind is tuned here
+                    ls2.solve(f.asm, b)
+                    torch.cuda.synchronize()
+                    t0 = time.perf_counter()
+                    ls2.compute(f.asm)
+                    torch.cuda.synchronize()
+                    t1 = time.perf_counter()
+                    ls2.solve(f.asm, b)
+                    t2 = time.perf_counter()
+                    it, _ = ls2.last_info()
+                    split["with_coarse" if slabs else "block_jacobi_two_kernel"] = {
+                        "factorize_ms": round(1e3 * (t1 - t0), 3), "cg_iterations_to_1e-5": it,
+                        "us_per_cg_iteration": round(1e6 * (t2 - t1) / max(it, 1), 2), "kind": ls2.kernel_info()[:2]}
+                    del ls2
+                res["cost_split_fp32_last_tangent"] = split
+            res[key] = {"s_per_load_path": round(sum(times) / len(times), 4), "newton_iterations": info.totalIterations,
+                        "cg_iterations": info.totalLinearIterations, "spmv_kernel": f.ls.kernel_info()[:2],
+                        "max_rel_diff_vs_plain_block_jacobi": None if u_plain is None else
+                        float(np.abs(u - u_plain).max() / np.abs(u_plain).max()),
+                        **f.ls.coarse_info()}
+            del f
+        res["speedup_mixed_vs_plain_fp64_both_two_level"] = round(res["plain_fp64"]["s_per_load_path"]
+                                                                   / res["mixed"]["s_per_load_path"], 2)
+        if t_plain_bj:
+            res["speedup_vs_plain_fp64_block_jacobi"] = round(t_plain_bj / res["mixed"]["s_per_load_path"], 2)
+    except Exception as e:  # reported, the headline stands on its own
+        res["failed"] = f"{type(e).__name__}: {e}"
+    return res
 
 
 def assembly_rates(ikr, torch, form, p):
@@ -833,6 +910,14 @@ def main():
         return run_learned(args)
     if args.config == 5:
         return run_eas(args)
+    if args.two_level_only:
+        import torch
+
+        import ikarus_gb300 as ikr
+        from ikarus_gb300 import problems
+        print(json.dumps({"two_level": run_two_level(args, ikr, torch, problems,
+                                                          problems.config2(load_steps=args.load_steps), None, None)}))
+        return
     out, p = run_ours(args, rank, world)
     if rank == 0:
         if not args.no_cpu_baseline and not args.small and out["plain_fp64"]:

@@ -194,6 +194,8 @@ SIGNATURES = {
     "ikr_load_control_run": ([_vp, _vp, C.POINTER(_ControlInfo), C.POINTER(_NRInfo), _I], C.c_int),
     "ikr_load_control_set_predictor": ([_vp, _I, _vp, _dp, _I], C.c_int),
     "ikr_linear_solver_set_multi_rhs": ([_vp, _I], C.c_int),
+    "ikr_linear_solver_set_coarse_space": ([_vp, _I], C.c_int),
+    "ikr_linear_solver_coarse_info": ([_vp, _ip], C.c_int),
     "ikr_assembler_set_tangent_kernel": ([_vp, _I], C.c_int),
     "ikr_assembler_tangent_kernel": ([_vp, _ip], C.c_int),
     "ikr_linear_solver_solve2": ([_vp, _vp, _dp, _dp, _dp, _dp], C.c_int),
@@ -673,6 +675,18 @@ class LinearSolver:
         """Two right-hand sides with one tangent (path following): one persistent launch streaming the matrix once
         per iteration for both (default), or one solve after the other."""
         _err(lib().ikr_linear_solver_set_multi_rhs(self.h, int(bool(on))))
+
+    def set_coarse_space(self, n_slabs):
+        """Coarse correction of the block-Jacobi CG (0 = off, the default): n_slabs in [1, 128] slabs of equal node
+        count along the mesh's longest extent, six rigid-body modes each, A_c = P^T K P rebuilt at every
+        factorize (an additive two-level preconditioner; two-kernel CG forms only)."""
+        _err(lib().ikr_linear_solver_set_coarse_space(self.h, int(n_slabs)))
+
+    def coarse_info(self):
+        """{"slabs", "coarse_dofs", "dropped_modes", "colours"} of the coarse correction in use (zeros when off)."""
+        out = (C.c_int32 * 4)()
+        _err(lib().ikr_linear_solver_coarse_info(self.h, out))
+        return dict(zip(("slabs", "coarse_dofs", "dropped_modes", "colours"), list(out)))
 
     def kernel_info(self):
         """(spmv kind, L2 keep fraction, tuned SpMV microseconds per launch)."""

@@ -860,6 +860,32 @@ int ikr_linear_solver_set_multi_rhs(ikr_ls ls, int32_t on) {
     ls->multi_rhs = on != 0;
   });
 }
+int ikr_linear_solver_set_coarse_space(ikr_ls ls, int32_t n_slabs) {
+  return guarded([&] {
+    need(ls, IKR_ERR_ARG, "null argument");
+    need(n_slabs >= 0 && 6 * n_slabs <= ikr::kCoarseMaxDofs, IKR_ERR_ARG, "coarse slabs must be in [0, 128]");
+    need(n_slabs == 0 || ls->tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI, IKR_ERR_NOT_IMPLEMENTED,
+         "the coarse correction is a preconditioner of the block-Jacobi GPU CG");
+    if (n_slabs != ls->coarse_req) {
+      ls->coarse_req = n_slabs;
+      ls->tuned_for = nullptr;  // the kind is chosen again (two-kernel forms only with a coarse correction)
+      ls->factorized = false;
+      ls->drop_graphs();
+      ls->co.built_for = nullptr;
+      ls->w.coarse = 0;
+    }
+  });
+}
+int ikr_linear_solver_coarse_info(ikr_ls ls, int32_t* out4) {
+  return guarded([&] {
+    need(ls && out4, IKR_ERR_ARG, "null argument");
+    const bool on = ls->w.coarse != 0;
+    out4[0] = on ? ls->co.n_slabs : 0;
+    out4[1] = on ? 6 * ls->co.n_slabs : 0;
+    out4[2] = on ? ls->co.dropped : 0;
+    out4[3] = on ? ls->co.n_colours : 0;
+  });
+}
 int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* kind, double* keep, double* us) {
   return guarded([&] {
     need(ls, IKR_ERR_ARG, "null argument");

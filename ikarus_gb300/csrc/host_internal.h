@@ -383,6 +383,22 @@ struct ikr_ls_s {
   // policy are w's) and the partials of the two-RHS persistent kernel (4 and 8 per CTA)
   bool multi_rhs = true;
   ikr::PcgWork w2;
+  // Coarse correction of the CG (coarse.cu), off by default: coarse_req > 0 slab aggregates of equal node
+  // count along the mesh's longest extent, six rigid-body modes each; rebuilt (A_c and its inverse) at every
+  // factorize.  Two-kernel CG forms only (the tuner then skips the persistent ones).
+  int coarse_req = 0;
+  struct CoarseSet {
+    ikr_asm built_for = nullptr;
+    int n_slabs = 0, reach = 0, n_colours = 0, dropped = 0;
+    ikr::Coarse C;
+    DBuf<float> y4;
+    DBuf<int32_t> nodes, chunk_off, agg_chunk, agg_colour;
+    std::vector<int32_t> agg_chunk_h;
+    DBuf<double> rpart, gpart, V, W, ainv64, e64;
+    DBuf<float> ainv32, e32;
+    std::vector<double> gpart_h, ac, inv, fac;
+    std::vector<float> inv32;
+  } co;
   DBuf<double> dx2, dr2, dz2, dp2, dp12, pa2, pb2, pbi2, scal2;
   DBuf<float> fx2, fr2, fz2, fp2, fp12;
 
@@ -473,6 +489,7 @@ struct ikr_ls_s {
       ikr::launch_pcg_spmv(A, w, k & 1, s);
       if (profile) CK(cudaEventRecordWithFlags(pev[gi][2 * k + 1], s, flags));
       ikr::launch_pcg_update(A, w, k & 1, s);
+      if (w.coarse) ikr::launch_coarse_correction(co.C, w, false, s);
     }
   }
 
@@ -495,7 +512,7 @@ struct ikr_ls_s {
   void launch_chunk(int gi, cudaStream_t s) {
     if (use_graphs) CK(cudaGraphLaunch(chunk[gi], s));
     else issue_chunk(gi, s);
-    count(2 * chunk_len);
+    count((w.coarse ? 4 : 2) * chunk_len);
   }
   // SpMV device time of the first `working` iterations of a finished profiled chunk
   void read_profile(int gi, int working) {
@@ -513,6 +530,202 @@ struct ikr_ls_s {
     count(1);
     factorized = true;
     if (tag != IKR_SOLVER_GPU_PCG_BATCHED && tuned_for != a) tune(a);
+    w.coarse = 0;
+    if (coarse_req > 0) {
+      if (persistent()) fail(IKR_ERR_ARG, "the coarse correction runs with the two-kernel CG kinds only");
+      coarse_operator(a);
+      w.coarse = 1;
+    }
+  }
+
+  // ---- coarse correction: aggregates, A_c = P^T K P and its inverse (coarse.cu has the device side) ----
+
+  // slab aggregates and the per-node mode data, once per assembler and slab count
+  void coarse_layout(ikr_asm a) {
+    ikr_fes f = a->fes;
+    if (f->n_inst != 0) fail(IKR_ERR_NOT_IMPLEMENTED, "coarse correction of element sets with independent instances");
+    if (a->matrix_dbc != IKR_DBC_FULL) fail(IKR_ERR_NOT_IMPLEMENTED, "coarse correction needs a Full-DBC tangent");
+    drop_graphs();
+    cudaStream_t s = f->stream;
+    const int nn = f->nn;
+    const int S = std::min(coarse_req, nn);
+    std::vector<double> X(3 * (size_t)nn);
+    f->X.download(X.data(), X.size(), s);
+    CK(cudaStreamSynchronize(s));
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = 0; i < nn; ++i)
+      for (int c = 0; c < 3; ++c) lo[c] = std::min(lo[c], X[3 * i + c]), hi[c] = std::max(hi[c], X[3 * i + c]);
+    int ax = 0;
+    for (int c = 1; c < 3; ++c)
+      if (hi[c] - lo[c] > hi[ax] - lo[ax]) ax = c;
+    // nodes in order of their coordinate along the longest axis, cut into S runs of equal count; each run
+    // sorted by node id (monotone gathers)
+    std::vector<int32_t> order(nn);
+    for (int i = 0; i < nn; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t i, int32_t j) { return X[3 * i + ax] < X[3 * j + ax]; });
+    std::vector<int32_t> agg(nn), agg_off(S + 1);
+    for (int k = 0; k <= S; ++k) agg_off[k] = (int32_t)((int64_t)k * nn / S);
+    for (int a_ = 0; a_ < S; ++a_) {
+      std::sort(order.begin() + agg_off[a_], order.begin() + agg_off[a_ + 1]);
+      for (int k = agg_off[a_]; k < agg_off[a_ + 1]; ++k) agg[order[k]] = a_;
+    }
+    // centroids, offsets, free-dof masks
+    std::vector<double> cen(3 * (size_t)S, 0.0);
+    for (int i = 0; i < nn; ++i)
+      for (int c = 0; c < 3; ++c) cen[3 * agg[i] + c] += X[3 * i + c];
+    for (int a_ = 0; a_ < S; ++a_)
+      for (int c = 0; c < 3; ++c) cen[3 * a_ + c] /= (double)(agg_off[a_ + 1] - agg_off[a_]);
+    std::vector<float> y4(4 * (size_t)nn);
+    for (int i = 0; i < nn; ++i) {
+      int mask = 0;
+      for (int c = 0; c < 3; ++c) {
+        y4[4 * i + c] = (float)(X[3 * i + c] - cen[3 * agg[i] + c]);
+        if (!a->fixed_h[3 * (size_t)i + c]) mask |= 1 << c;
+      }
+      const int32_t bits = agg[i] | (mask << 24);
+      std::memcpy(&y4[4 * i + 3], &bits, sizeof(bits));
+    }
+    // reach: the largest aggregate distance of two coupled nodes; colours of a distance-2 colouring of the
+    // aggregate chain (any 2 reach + 1 consecutive aggregates differ)
+    int reach = 0;
+    for (int i = 0; i < nn; ++i)
+      for (int k = a->row_ptr_h[i]; k < a->row_ptr_h[i + 1]; ++k) reach = std::max(reach, std::abs(agg[i] - agg[a->col_h[k]]));
+    if (reach > 3)
+      fail(IKR_ERR_ARG, "coarse correction: slabs thinner than the elements couple %d slabs apart; use fewer slabs",
+           reach);
+    const int ncol = std::min(2 * reach + 1, S);
+    std::vector<int32_t> colour(S);
+    for (int a_ = 0; a_ < S; ++a_) colour[a_] = a_ % ncol;
+    // chunks of at most 2048 nodes per aggregate: one 1024-thread CTA of the restrict kernel each, one CTA per SM
+    // (its registers), so about as many chunks as SMs keep the launch in one wave
+    constexpr int kChunk = 2048;
+    std::vector<int32_t> chunk_off{0};
+    co.agg_chunk_h.assign(1, 0);
+    for (int a_ = 0; a_ < S; ++a_) {
+      for (int k = agg_off[a_]; k < agg_off[a_ + 1]; k += kChunk) chunk_off.push_back(std::min(k + kChunk, agg_off[a_ + 1]));
+      co.agg_chunk_h.push_back((int32_t)chunk_off.size() - 1);
+    }
+    const int nchunks = (int)chunk_off.size() - 1;
+    co.y4.upload(y4.data(), y4.size(), s);
+    co.nodes.upload(order.data(), order.size(), s);
+    co.chunk_off.upload(chunk_off.data(), chunk_off.size(), s);
+    co.agg_chunk.upload(co.agg_chunk_h.data(), co.agg_chunk_h.size(), s);
+    co.agg_colour.upload(colour.data(), colour.size(), s);
+    co.rpart.alloc(6 * (size_t)nchunks);
+    const size_t nc = 6 * (size_t)S;
+    if (fp32) co.ainv32.alloc(nc * nc), co.e32.alloc(nc);
+    else co.ainv64.alloc(nc * nc), co.e64.alloc(nc);
+    ikr::Coarse& C = co.C;
+    C.n_rows = nn, C.n_agg = S, C.n_c = (int)nc, C.n_chunks = nchunks;
+    C.y4 = reinterpret_cast<const float4*>(co.y4.p);
+    C.nodes = co.nodes.p, C.chunk_off = co.chunk_off.p, C.agg_chunk = co.agg_chunk.p, C.agg_colour = co.agg_colour.p;
+    C.rpart = co.rpart.p;
+    C.ainv = fp32 ? (const void*)co.ainv32.p : (const void*)co.ainv64.p;
+    C.e = fp32 ? (void*)co.e32.p : (void*)co.e64.p;
+    CK(cudaStreamSynchronize(s));  // host vectors above go out of scope
+    co.built_for = a, co.n_slabs = S, co.reach = reach, co.n_colours = ncol;
+  }
+
+  // A_c = P^T K P from probe products (one SpMV per colour and mode), then its inverse
+  void coarse_operator(ikr_asm a) {
+    if (co.built_for != a || co.n_slabs != std::min(coarse_req, a->fes->nn) ||
+        (fp32 ? (const void*)co.ainv32.p : (const void*)co.ainv64.p) != co.C.ainv)
+      coarse_layout(a);
+    cudaStream_t s = a->fes->stream;
+    const ikr::Bsr A = a->bsr();
+    const int S = co.n_slabs, nc = 6 * S, nch = co.C.n_chunks, ncol = co.n_colours;
+    const int64_t n3 = 3LL * a->fes->nn;
+    co.V.alloc(6 * (size_t)n3), co.W.alloc(6 * (size_t)n3);
+    co.gpart.alloc(36 * (size_t)nch * ncol);
+    for (int c = 0; c < ncol; ++c) {
+      ikr::launch_coarse_probe(co.C, c, co.V.p, s);
+      for (int m = 0; m < 6; ++m) ikr::launch_spmv64(A, fp32, co.V.p + m * n3, co.W.p + m * n3, s);
+      ikr::launch_coarse_galerkin(co.C, co.W.p, co.gpart.p + 36LL * nch * c, s);
+      count(8);
+    }
+    co.gpart_h.resize(co.gpart.n);
+    co.gpart.download(co.gpart_h.data(), co.gpart.n, s);
+    CK(cudaStreamSynchronize(s));
+    // the blocks: row aggregate b, column aggregate = the one aggregate of colour c within reach of b
+    co.ac.assign((size_t)nc * nc, 0.0);
+    for (int c = 0; c < ncol; ++c)
+      for (int b = 0; b < S; ++b) {
+        int col_agg = -1;
+        for (int d = -co.reach; d <= co.reach; ++d)
+          if (b + d >= 0 && b + d < S && (b + d) % ncol == c) col_agg = b + d;
+        if (col_agg < 0) continue;
+        double blk[36] = {};
+        for (int k = co.agg_chunk_h[b]; k < co.agg_chunk_h[b + 1]; ++k)
+          for (int q = 0; q < 36; ++q) blk[q] += co.gpart_h[36 * ((size_t)nch * c + k) + q];
+        for (int r = 0; r < 6; ++r)
+          for (int m = 0; m < 6; ++m) co.ac[(size_t)(6 * b + r) * nc + 6 * col_agg + m] = blk[6 * r + m];
+      }
+    for (int i = 0; i < nc; ++i)
+      for (int j = 0; j < i; ++j) {
+        const double v = 0.5 * (co.ac[(size_t)i * nc + j] + co.ac[(size_t)j * nc + i]);
+        co.ac[(size_t)i * nc + j] = co.ac[(size_t)j * nc + i] = v;
+      }
+    co.dropped = band_spd_inverse(co.ac, nc, 6 * (co.reach + 1) - 1, co.fac, co.inv);
+    if (fp32) {
+      co.inv32.assign(co.inv.begin(), co.inv.end());
+      co.ainv32.upload(co.inv32.data(), co.inv32.size(), s);
+    } else {
+      co.ainv64.upload(co.inv.data(), co.inv.size(), s);
+    }
+    CK(cudaStreamSynchronize(s));
+  }
+
+  // Inverse of the symmetric matrix A (n x n, zero outside half bandwidth bw) by a band Cholesky factorisation
+  // A = L L^T.  A pivot at or below 1e-9 of its diagonal entry marks a mode that depends on the earlier ones (or
+  // has no free dof): its column of L is the unit vector and its row and column of the inverse are zero, so the
+  // returned matrix is symmetric positive semi-definite.  Returns the number of such modes.
+  static int band_spd_inverse(const std::vector<double>& A, int n, int bw, std::vector<double>& L,
+                              std::vector<double>& inv) {
+    L.assign((size_t)n * n, 0.0);
+    std::vector<char> drop(n, 0);
+    int dropped = 0;
+    for (int j = 0; j < n; ++j) {
+      const int k0 = std::max(0, j - bw);
+      double d = A[(size_t)j * n + j];
+      for (int k = k0; k < j; ++k) d -= L[(size_t)j * n + k] * L[(size_t)j * n + k];
+      if (!(A[(size_t)j * n + j] > 0.0) || !(d > 1e-9 * A[(size_t)j * n + j])) {
+        drop[j] = 1, ++dropped;
+        for (int k = k0; k < j; ++k) L[(size_t)j * n + k] = 0.0;  // the mode leaves the factorisation
+        L[(size_t)j * n + j] = 1.0;
+        continue;
+      }
+      const double ljj = std::sqrt(d);
+      L[(size_t)j * n + j] = ljj;
+      for (int i = j + 1; i <= std::min(n - 1, j + bw); ++i) {
+        double v = A[(size_t)i * n + j];
+        for (int k = std::max(0, i - bw); k < j; ++k) v -= L[(size_t)i * n + k] * L[(size_t)j * n + k];
+        L[(size_t)i * n + j] = v / ljj;
+      }
+    }
+    inv.assign((size_t)n * n, 0.0);
+    std::vector<double> y(n);
+    for (int i = 0; i < n; ++i) {
+      if (drop[i]) continue;
+      // L y = e_i (y_k = 0 for k < i), then L^T x = y
+      for (int k = 0; k < n; ++k) y[k] = 0.0;
+      for (int k = i; k < n; ++k) {
+        double v = (k == i) ? 1.0 : 0.0;
+        for (int l = std::max(i, k - bw); l < k; ++l) v -= L[(size_t)k * n + l] * y[l];
+        y[k] = v / L[(size_t)k * n + k];
+      }
+      for (int k = n - 1; k >= 0; --k) {
+        double v = y[k];
+        for (int l = k + 1; l <= std::min(n - 1, k + bw); ++l) v -= L[(size_t)l * n + k] * y[l];
+        y[k] = v / L[(size_t)k * n + k];
+      }
+      for (int k = 0; k < n; ++k) inv[(size_t)k * n + i] = drop[k] ? 0.0 : y[k];
+    }
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < i; ++j) {
+        const double v = 0.5 * (inv[(size_t)i * n + j] + inv[(size_t)j * n + i]);
+        inv[(size_t)i * n + j] = inv[(size_t)j * n + i] = v;
+      }
+    return dropped;
   }
 
   void set_kernel(int kind, double keep) {
@@ -527,6 +740,7 @@ struct ikr_ls_s {
   // the keep fractions in increasing order with the fastest kind.
   void tune(ikr_asm a) {
     drop_graphs();
+    w.coarse = 0;  // kinds are timed as plain block-Jacobi iterations
     const ikr::Bsr A = a->bsr();
     const int64_t total_g = A.n_padded / 32;
     auto apply = [&](int kind, double keep) {
@@ -596,7 +810,7 @@ struct ikr_ls_s {
         const double us = time_it(k, k > 0 ? kProbeKeep : 0.0);
         if (us < best) best = us, best_kind = k;
       }
-      for (int v = 0; v < ikr::pcg_persistent_variants(); ++v) {
+      for (int v = 0; v < ikr::pcg_persistent_variants() && coarse_req == 0; ++v) {
         if (!ikr::pcg_persistent_eligible(A, w, v)) continue;
         const double us = time_persistent(first_persistent_kind() + v, kProbeKeep);
         if (us < best) best = us, best_kind = first_persistent_kind() + v;
@@ -604,6 +818,9 @@ struct ikr_ls_s {
       // the two-kernel CG state was advanced by the persistent trials' inits: restart it for the keep trials
       ikr::launch_pcg_init(A, w, b64.p, 0.0, 1 << 30, s);
       count(2);
+    } else if (best_kind >= first_persistent_kind() && coarse_req > 0) {
+      fail(IKR_ERR_ARG, "the coarse correction runs with the two-kernel CG kinds only (0 .. %d)",
+           first_persistent_kind() - 1);
     } else if (best_kind >= first_persistent_kind() && !ikr::pcg_persistent_eligible(A, w, best_kind - first_persistent_kind())) {
       fail(IKR_ERR_ARG, "the persistent CG variant does not fit this system (too many slices per warp)");
     }
@@ -665,6 +882,10 @@ struct ikr_ls_s {
     build_chunk(s);
     ikr::launch_pcg_init(A, w, b, rt, maxit, s);
     count(2);
+    if (w.coarse) {
+      ikr::launch_coarse_correction(co.C, w, true, s);
+      count(2);
+    }
     // Chunks of CG iterations are launched one ahead of the host check: once the device flags
     // convergence the chunk in flight returns at entry, so polling never stalls the GPU.
     constexpr int NS = ikr::kNScal;

@@ -139,7 +139,8 @@ enum PcgScal : int {
   kMaxIt = 8,
   kAlpha = 9,
   kBeta = 10,
-  kTicket = 12, // slots 12-13 hold four 32-bit tickets of the last-block reductions
+  kRzF = 11,    // with a coarse correction: r.D^-1 r of the current iterate (coarse.cu completes r.z)
+  kTicket = 12, // slots 12-14 hold six 32-bit tickets of the last-block reductions (the fifth: coarse.cu)
   kNScal = 16
 };
 struct PcgWork {
@@ -166,6 +167,9 @@ struct PcgWork {
   void* w0 = nullptr;
   void* w1 = nullptr;
   double* part_c = nullptr;
+  // 1: a coarse correction (coarse.cu) follows the init and update kernels, which then leave r.D^-1 r in kRzF
+  // and let it set r.z and beta
+  int coarse = 0;
 };
 void launch_block_jacobi(const Bsr& A, bool fp32, void* minv, bool point_jacobi, cudaStream_t s);
 void launch_pcg_init(const Bsr& A, PcgWork& w, const double* b, double rtol, int max_iter, cudaStream_t s);
@@ -182,6 +186,23 @@ void launch_pcg_spmv_staged(const Bsr& A, PcgWork& w, int variant, const void* p
 void launch_fill64(double* y, double v, int64_t n, cudaStream_t s);
 // cg_persistent.cu -- the whole CG solve (after launch_pcg_init) in one cooperative launch; the result in w.x
 // and the scalars as after the two-kernel iterations
+// coarse.cu -- coarse correction of the block-Jacobi CG (additive two-level preconditioner with the rigid-body
+// modes of node aggregates); device data built by the linear solver (host_internal.h)
+constexpr int kCoarseMaxDofs = 768;  // six modes per aggregate, at most 128 aggregates
+struct Coarse {
+  int n_rows = 0, n_agg = 0, n_c = 0, n_chunks = 0;
+  const float4* y4 = nullptr;          // per node: offset from its aggregate's centroid, agg id | free mask << 24
+  const int32_t* nodes = nullptr;      // node ids grouped by aggregate
+  const int32_t* chunk_off = nullptr;  // nodes of chunk k: nodes[chunk_off[k] .. chunk_off[k+1])
+  const int32_t* agg_chunk = nullptr;  // chunks of aggregate a: [agg_chunk[a], agg_chunk[a+1])
+  const int32_t* agg_colour = nullptr; // colour of every aggregate (distance-2 colouring)
+  double* rpart = nullptr;             // 6 per chunk: P^T r of the chunk
+  const void* ainv = nullptr;          // A_c^-1, n_c x n_c in the CG's type
+  void* e = nullptr;                   // A_c^-1 P^T r, n_c in the CG's type
+};
+void launch_coarse_correction(const Coarse& C, const PcgWork& w, bool init, cudaStream_t s);
+void launch_coarse_probe(const Coarse& C, int colour, double* V, cudaStream_t s);
+void launch_coarse_galerkin(const Coarse& C, const double* W, double* part, cudaStream_t s);
 int pcg_persistent_variants();
 bool pcg_persistent_eligible(const Bsr& A, PcgWork& w, int variant);
 cudaError_t launch_pcg_persistent(const Bsr& A, PcgWork& w, int variant, cudaStream_t s);

@@ -74,7 +74,8 @@ __global__ void __launch_bounds__(kThreads) pcg_spmv_kernel(Bsr A, const T* __re
 template <typename T>
 __global__ void __launch_bounds__(kThreads) pcg_update_kernel(int n_rows, const T* __restrict__ minv,
                                                               const T* __restrict__ pnew, const T* __restrict__ q,
-                                                              T* x, T* r, T* z, double* part, double* scal) {
+                                                              T* x, T* r, T* z, double* part, double* scal,
+                                                              int coarse) {
   __shared__ double sh[32];
   __shared__ bool last;
   if (scal[kDone] != 0.0) return;
@@ -110,8 +111,12 @@ __global__ void __launch_bounds__(kThreads) pcg_update_kernel(int n_rows, const 
       scal[kRR] = rrs;
       if (rrs <= scal[kTol2]) scal[kDone] = 1.0;
       else if (it >= scal[kMaxIt]) scal[kDone] = 2.0;
-      scal[kBeta] = rzs / scal[kRz];
-      scal[kRz] = rzs;
+      if (coarse) {
+        scal[kRzF] = rzs;  // the coarse correction adds r_c . e and sets beta
+      } else {
+        scal[kBeta] = rzs / scal[kRz];
+        scal[kRz] = rzs;
+      }
       tickets(scal)[1] = 0u;
     }
   }
@@ -120,7 +125,8 @@ __global__ void __launch_bounds__(kThreads) pcg_update_kernel(int n_rows, const 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) pcg_init_kernel(int n_rows, const T* __restrict__ minv,
                                                             const double* __restrict__ b, T* x, T* r, T* z, T* pold,
-                                                            double* part, double* scal, double rtol, int max_iter) {
+                                                            double* part, double* scal, double rtol, int max_iter,
+                                                            int coarse) {
   __shared__ double sh[32];
   __shared__ bool last;
   double rz = 0.0, rr = 0.0;
@@ -151,7 +157,7 @@ __global__ void __launch_bounds__(kThreads) pcg_init_kernel(int n_rows, const T*
     if (threadIdx.x == 0) {
       scal[kBB] = rrs;
       scal[kTol2] = rtol * rtol * rrs;
-      scal[kRz] = rzs;
+      scal[coarse ? kRzF : kRz] = rzs;
       scal[kBeta] = 0.0;
       scal[kAlpha] = 0.0;
       scal[kIters] = 0.0;
@@ -245,11 +251,12 @@ void launch_pcg_init(const Bsr& A, PcgWork& w, const double* b, double rtol, int
   cudaMemsetAsync(w.scal, 0, sizeof(double) * kNScal, s);  // scalars and tickets start at zero
   if (w.fp32)
     pcg_init_kernel<float><<<w.grid, kThreads, 0, s>>>(w.n_rows, (const float*)w.minv, b, (float*)w.x, (float*)w.r,
-                                                        (float*)w.z, (float*)w.p1, w.part_b, w.scal, rtol, max_iter);
+                                                        (float*)w.z, (float*)w.p1, w.part_b, w.scal, rtol, max_iter,
+                                                        w.coarse);
   else
     pcg_init_kernel<double><<<w.grid, kThreads, 0, s>>>(w.n_rows, (const double*)w.minv, b, (double*)w.x,
                                                          (double*)w.r, (double*)w.z, (double*)w.p1, w.part_b, w.scal,
-                                                         rtol, max_iter);
+                                                         rtol, max_iter, w.coarse);
 }
 
 void launch_pcg_spmv(const Bsr& A, PcgWork& w, int parity, cudaStream_t s) {
@@ -273,11 +280,11 @@ void launch_pcg_update(const Bsr& A, PcgWork& w, int parity, cudaStream_t s) {
   if (w.fp32)
     pcg_update_kernel<float><<<w.grid, kThreads, 0, s>>>(w.n_rows, (const float*)w.minv, (const float*)pnew,
                                                           (const float*)w.q, (float*)w.x, (float*)w.r, (float*)w.z,
-                                                          w.part_b, w.scal);
+                                                          w.part_b, w.scal, w.coarse);
   else
     pcg_update_kernel<double><<<w.grid, kThreads, 0, s>>>(w.n_rows, (const double*)w.minv, (const double*)pnew,
                                                            (const double*)w.q, (double*)w.x, (double*)w.r,
-                                                           (double*)w.z, w.part_b, w.scal);
+                                                           (double*)w.z, w.part_b, w.scal, w.coarse);
 }
 void launch_pcg_iteration(const Bsr& A, PcgWork& w, int parity, cudaStream_t s) {
   launch_pcg_spmv(A, w, parity, s);

@@ -212,6 +212,15 @@ int ikr_assembler_tangent_kernel(ikr_asm a, int32_t* path);
  * or one after the other (0) */
 int ikr_linear_solver_set_multi_rhs(ikr_ls ls, int32_t on);
 int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* spmv_kind, double* l2_keep_fraction, double* spmv_us);
+/* no reference counterpart: coarse correction of IKR_SOLVER_GPU_PCG_BLOCK_JACOBI (off by default, n_slabs = 0).
+ * n_slabs in [1, 128] adds P A_c^-1 P^T to the block-Jacobi preconditioner, an additive two-level method: the
+ * nodes are cut into n_slabs slabs of equal node count along the mesh's longest extent, P holds the six
+ * rigid-body modes of every slab (zero at constrained dofs) and A_c = P^T K P is rebuilt at every factorize.
+ * The CG then runs the two-kernel forms only.  Needs a Full-DBC tangent of an element set without instances;
+ * slabs thinner than the elements (coupling more than 3 slabs apart) are rejected at factorize.  coarse_info
+ * out4: slabs in use (0 = off), coarse dofs, modes dropped as linearly dependent, probe colours. */
+int ikr_linear_solver_set_coarse_space(ikr_ls ls, int32_t n_slabs);
+int ikr_linear_solver_coarse_info(ikr_ls ls, int32_t* out4);
 /* material law of all elements (the reference's Material template argument of makeFE): NeoHooke (default,
  * neohooke.hh) or StVenantKirchhoff (svk.hh), both with the Lame parameters given at creation, or BlatzKo
  * (makeBlatzKo(mu), hyperelastic/factory.hh:34-39: deviatoric function on the total principal stretches, no
