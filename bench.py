@@ -915,8 +915,8 @@ def main():
 
         import ikarus_gb300 as ikr
         from ikarus_gb300 import problems
-        print(json.dumps({"two_level": run_two_level(args, ikr, torch, problems,
-                                                          problems.config2(load_steps=args.load_steps), None, None)}))
+        p = problems.config2(load_steps=args.load_steps)
+        print(json.dumps({"two_level": run_two_level(args, ikr, torch, problems, p, None, None)}))
         return
     out, p = run_ours(args, rank, world)
     if rank == 0:

@@ -223,6 +223,8 @@ class LinearSolver {
     x.resize(b.size());
     check(ikr_linear_solver_solve(h_, a.handle(), x.data(), b.data()), "solve");
   }
+  // no reference counterpart: coarse correction of the block-Jacobi CG with nSlabs slab aggregates (0 = off)
+  void setCoarseSpace(int32_t nSlabs) { check(ikr_linear_solver_set_coarse_space(h_, nSlabs), "setCoarseSpace"); }
   ikr_ls handle() const { return h_; }
 
  private:
