@@ -6,7 +6,9 @@ GPU form (FP64 tangent, FP64 block-Jacobi CG to 1e-10), plus the roofline of the
 
 A step = one complete load path from the undeformed state.  `value` is device time per load path with the
 inputs resident in HBM; `e2e` adds the host->device copy of the initial displacement and the device->host
-copy of the converged displacement, through the public API.  Prints one JSON line.
+copy of the converged displacement, through the public API.  Prints one JSON line.  Beside the headline the
+line carries `two_level`: the same load path with the CG's coarse correction (an additive two-level
+preconditioner, `--coarse` slabs; not the headline's block-Jacobi method), both forms.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
