@@ -17,8 +17,8 @@
 // Setup per tangent (A_c): for every colour of a distance-2 colouring of the aggregates, the six probe vectors
 // sum_{a of that colour} P_{a,m} are multiplied by K (launch_spmv64) and restricted per chunk (36 sums); the
 // host adds the chunks of each aggregate in a fixed order, places each block at the single aggregate of the
-// colour that touches it, and inverts A_c (ikr_ls_s in host_internal.h).  All sums are fixed-order: results are bit-identical
-// run to run.
+// colour that touches it, and inverts A_c (ikr_ls_s in host_internal.h).  All sums are fixed-order: results are
+// bit-identical run to run.
 #include "cg_common.cuh"
 
 namespace ikr {
