@@ -172,6 +172,8 @@ SIGNATURES = {
     "ikr_linear_solver_destroy": ([_vp], C.c_int),
     "ikr_linear_solver_set_tolerance": ([_vp, _D, _I], C.c_int),
     "ikr_linear_solver_analyze_pattern": ([_vp, _vp], C.c_int),
+    "ikr_linear_solver_set_fp64_outer": ([_vp, _I, _D, _I, _I], C.c_int),
+    "ikr_linear_solver_outer_info": ([_vp, _ip, _ip], C.c_int),
     "ikr_linear_solver_factorize": ([_vp, _vp], C.c_int),
     "ikr_linear_solver_solve": ([_vp, _vp, _dp, _dp], C.c_int),
     "ikr_linear_solver_last_info": ([_vp, _ip, _dp], C.c_int),
@@ -675,6 +677,19 @@ class LinearSolver:
         """Two right-hand sides with one tangent (path following): one persistent launch streaming the matrix once
         per iteration for both (default), or one solve after the other."""
         _err(lib().ikr_linear_solver_set_multi_rhs(self.h, int(bool(on))))
+
+    def set_fp64_outer(self, restart=20, inner_rtol=1e-2, inner_max_iter=2000, outer_max_iter=2000):
+        """FP64 outer solve of an FP32 tangent (restart 0 switches it off): flexible GMRES(restart) on the FP64
+        tangent, right-preconditioned by the FP32 block-Jacobi CG (to inner_rtol, at most inner_max_iter iterations
+        per application) on the FP32 rounding of the same tangent."""
+        _err(lib().ikr_linear_solver_set_fp64_outer(self.h, int(restart), float(inner_rtol), int(inner_max_iter),
+                                                    int(outer_max_iter)))
+
+    def outer_info(self):
+        """(Arnoldi steps, restart cycles) of the last FP64 outer solve."""
+        o, c = C.c_int32(), C.c_int32()
+        _err(lib().ikr_linear_solver_outer_info(self.h, C.byref(o), C.byref(c)))
+        return o.value, c.value
 
     def set_coarse_space(self, n_slabs):
         """Coarse correction of the block-Jacobi CG (0 = off, the default): n_slabs in [1, 128] slabs of equal node

@@ -27,6 +27,7 @@ namespace {
 
 using namespace cg;
 constexpr int kThreads = 1024;       // CTA of the restrict-and-solve kernel (a chunk is up to 2048 nodes)
+static_assert(kCoarseMaxDofs <= kThreads, "the coarse solve splits the coarse dofs over the threads of one CTA");
 constexpr int kCoarseTicket = 4;     // ticket slot of its last-block reduction (scalar slot 14)
 
 // node data: offset from the aggregate centroid (x, y, z) and, in the fourth lane as integer bits, the

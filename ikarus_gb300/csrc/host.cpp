@@ -134,7 +134,32 @@ void assemble_vector(ikr_asm a, ikr_req r, int dbc) {
   f->check_status();
 }
 
+static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc);
+
+// The tangent in the assembler's precision; an FP32 tangent with an FP64 twin (dual64) is assembled in FP64 and
+// rounded to FP32 once, so the FP32 CG and the FP64 outer solve see the same tangent.
 void assemble_matrix(ikr_asm a, ikr_req r, int dbc) {
+  if (a->fp32 && a->dual64) {
+    if (!a->nb) a->build_pattern();
+    a->val64.alloc(9 * (size_t)a->npad);
+    a->fp32 = false;
+    try {
+      assemble_matrix_into(a, r, dbc);
+    } catch (...) {
+      a->fp32 = true;
+      throw;
+    }
+    a->fp32 = true;
+    ikr::launch_round_values(a->val64.p, a->val32.p, 9 * a->npad, a->fes->stream);
+    count(1);
+    a->k64_stamp = ++a->k_stamp;
+    return;
+  }
+  assemble_matrix_into(a, r, dbc);
+  ++a->k_stamp;
+}
+
+static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc) {
   ikr_fes f = a->fes;
   if (!a->nb) a->build_pattern();
   const uint8_t* nf = (dbc == IKR_DBC_RAW) ? nullptr : a->node_fixed.p;
@@ -733,6 +758,28 @@ int ikr_linear_solver_set_tolerance(ikr_ls ls, double rtol, int32_t max_iter) {
     ls->max_iter = max_iter;
   });
 }
+int ikr_linear_solver_set_fp64_outer(ikr_ls ls, int32_t restart, double inner_rtol, int32_t inner_max_iter,
+                                     int32_t outer_max_iter) {
+  return guarded([&] {
+    need(ls, IKR_ERR_ARG, "null argument");
+    need(restart >= 0 && restart < ikr::kKrylovMaxBasis, IKR_ERR_ARG, "restart length must be in [0, 63]");
+    need(inner_rtol > 0 && inner_rtol < 1 && inner_max_iter > 0 && outer_max_iter > 0, IKR_ERR_ARG,
+         "invalid inner tolerance or iteration limits");
+    need(ls->tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI || ls->tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT,
+         IKR_ERR_NOT_IMPLEMENTED, "the FP64 outer solve wraps the single-system CG solvers");
+    ls->outer_m = restart;
+    ls->inner_rtol = inner_rtol;
+    ls->inner_max_iter = inner_max_iter;
+    ls->outer_max_iter = outer_max_iter;
+  });
+}
+int ikr_linear_solver_outer_info(ikr_ls ls, int32_t* outer_iterations, int32_t* cycles) {
+  return guarded([&] {
+    need(ls, IKR_ERR_ARG, "null argument");
+    if (outer_iterations) *outer_iterations = ls->last_outer;
+    if (cycles) *cycles = ls->last_cycles;
+  });
+}
 int ikr_linear_solver_analyze_pattern(ikr_ls ls, ikr_asm a) {
   return guarded([&] {
     need(ls && a, IKR_ERR_ARG, "null argument");
@@ -897,6 +944,8 @@ int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* kind, double* keep, double
 // Allocation-free variant of the solve: the CG work set is carved out of the library's fixed device array
 // (noalloc.cu) instead of cudaMalloc'ed buffers; no graphs, events or pinned buffers either, the host polls
 // the device scalars with a plain copy into a static host array after every 32 iterations.
+static_assert(ikr::kNoAllocMaxRows >= IKR_NOALLOC_MAX_NODES,
+              "the fixed scratch of noalloc.cu must hold the largest system the entry point accepts");
 int ikr_linear_solver_solve_noalloc(ikr_asm a, const double* b, double* x, double rtol, int32_t max_iter,
                                     int32_t* iterations) {
   return guarded([&] {

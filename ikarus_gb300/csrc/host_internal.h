@@ -261,6 +261,11 @@ struct ikr_asm_s {
   DBuf<double> val64;
   DBuf<float> val32;
   int matrix_dbc = -1;  // option of the last assembled matrix
+  // FP32 tangent with an FP64 twin: when dual64 is set (a linear solver with the FP64 outer Krylov solve asks for
+  // it), the tangent is assembled in FP64 into val64 and val32 is its FP32 rounding.  k_stamp counts matrix
+  // assemblies, k64_stamp is the assembly whose FP64 twin val64 holds.
+  bool dual64 = false;
+  uint64_t k_stamp = 0, k64_stamp = 0;
   // vector
   DBuf<double> R;
   int vector_dbc = -1;
@@ -342,6 +347,12 @@ struct ikr_asm_s {
   int64_t block_id(int r, int64_t k) const { return (slice_off_h[r >> 5] + (k - row_ptr_h[r])) * 32LL + (r & 31); }
 };
 
+namespace ikr_host {
+// FP64 outer Krylov solve of an FP32 tangent with an FP64 twin (krylov.cpp): x = K64^{-1} b to ||b - K64 x|| <=
+// eta ||b|| by flexible GMRES, right-preconditioned by the FP32 block-Jacobi CG on K32; returns inner CG iterations
+int64_t fgmres_solve(ikr_ls ls, ikr_asm a, const double* b, double* x, double eta);
+}  // namespace ikr_host
+
 struct ikr_ls_s {
   int tag = IKR_SOLVER_GPU_PCG_BLOCK_JACOBI;
   double rtol = 1e-10;
@@ -401,6 +412,14 @@ struct ikr_ls_s {
   } co;
   DBuf<double> dx2, dr2, dz2, dp2, dp12, pa2, pb2, pbi2, scal2;
   DBuf<float> fx2, fr2, fz2, fp2, fp12;
+  // FP64 outer Krylov solve (krylov.cpp), off while outer_m = 0: restart length, tolerance and iteration cap of
+  // the inner FP32 CG, cap on outer iterations; Arnoldi basis V, directions Z and small device work
+  int outer_m = 0;
+  double inner_rtol = 1e-2;
+  int inner_max_iter = 2000;
+  int outer_max_iter = 2000;
+  int last_outer = 0, last_cycles = 0;
+  DBuf<double> gm_V, gm_Z, gm_w, gm_r, gm_h, gm_part, gm_c, gm_npart, gm_nout;
 
   ~ikr_ls_s() {
     drop_graphs();
@@ -429,6 +448,7 @@ struct ikr_ls_s {
   }
 
   void setup(ikr_asm a) {
+    a->dual64 = outer_m > 0 && a->fp32;  // the FP64 outer solve needs the FP64 twin of every later assembly
     if (asm_ == a && w.n_rows == a->fes->nn && fp32 == a->fp32 && w.grid) return;
     drop_graphs();
     asm_ = a;
@@ -997,8 +1017,10 @@ struct ikr_ls_s {
     return last_iters;
   }
 
-  // x = K^{-1} b with optional FP64 iterative refinement around the (possibly FP32) CG
+  // x = K^{-1} b with optional FP64 iterative refinement around the (possibly FP32) CG; with the FP64 outer
+  // Krylov solve on (outer_m > 0) an FP32 tangent is solved against its FP64 twin instead
   int64_t solve(ikr_asm a, const double* b, double* x, double rt, int maxit, int refinements) {
+    if (outer_m > 0 && a->fp32) return fgmres_solve(this, a, b, x, rt);
     int64_t its = solve_device(a, b, x, rt, maxit);
     if (refinements <= 0) return its;
     cudaStream_t s = a->fes->stream;

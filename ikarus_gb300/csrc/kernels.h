@@ -247,6 +247,19 @@ void launch_add_f32(double* u, const float* d, int64_t n, cudaStream_t s);
 void launch_add_scaled_f32(double* u, const float* d, double a, int64_t n, cudaStream_t s);  // u += a d
 void launch_base_plus_scaled(double* u, const double* u0, const float* d, double sc, int64_t n, cudaStream_t s);
 
+// krylov.cu -- vector kernels of the FP64 outer Krylov solve (krylov.cpp): V holds m vectors of length n one after
+// the other (leading dimension ld)
+constexpr int kKrylovMaxBasis = 64;
+int multi_dot_blocks(int64_t n);
+// out[i] = V[i] . w for i < m; part holds m * multi_dot_blocks(n) doubles
+void launch_multi_dot(const double* V, int64_t ld, int m, const double* w, int64_t n, double* part, double* out,
+                      cudaStream_t s);
+// y += sign * sum_{i < m} c[i] V[i], c on the device, m <= kKrylovMaxBasis
+void launch_multi_axpy(double* y, const double* V, int64_t ld, int m, const double* c, double sign, int64_t n,
+                       cudaStream_t s);
+// out = FP32 rounding of in (n values)
+void launch_round_values(const double* in, float* out, int64_t n, cudaStream_t s);
+
 // noalloc.cu -- fixed device scratch of the allocation-free CG solve
 constexpr int kNoAllocMaxRows = 32768;  // block rows (nodes) = 98304 dofs
 constexpr int kNoAllocMaxGrid = 1216;   // blocks of the partial-producing CG kernels

@@ -175,6 +175,19 @@ int ikr_assembler_vector_norm(ikr_asm a, double* norm);
 int ikr_linear_solver_create(ikr_ls* out, int32_t solver_type_tag);
 int ikr_linear_solver_destroy(ikr_ls ls);
 int ikr_linear_solver_set_tolerance(ikr_ls ls, double rtol, int32_t max_iter);
+/* no reference counterpart: FP64 outer solve of an FP32 tangent (off while restart = 0, the default).  The tangent
+ * is then assembled in FP64 and rounded to FP32 once; each solve runs flexible GMRES(restart) on the FP64 tangent,
+ * right-preconditioned by the FP32 block-Jacobi CG on the FP32 one (relative tolerance inner_rtol, at most
+ * inner_max_iter iterations per application), until ||b - K64 x|| <= rtol ||b|| or outer_max_iter Arnoldi steps.
+ * For tangents whose FP32 rounding is too coarse for an FP32 Newton correction (cond(K) eps_32 > 1, e.g. nearly
+ * incompressible EAS elements).  Newton and path-following solves with this solver assemble the FP64 twin
+ * themselves; a direct caller of ikr_linear_solver_solve calls ikr_linear_solver_analyze_pattern before
+ * assembling the matrix (a solve without the twin of the last assembly returns IKR_ERR_INVALID_STATE).
+ * restart in [1, 63]; FP64 tangents are solved by the CG as before.  last_info then reports the inner CG iterations
+ * and the achieved FP64 relative residual, outer_info the Arnoldi steps and restart cycles of the last solve. */
+int ikr_linear_solver_set_fp64_outer(ikr_ls ls, int32_t restart, double inner_rtol, int32_t inner_max_iter,
+                                     int32_t outer_max_iter);
+int ikr_linear_solver_outer_info(ikr_ls ls, int32_t* outer_iterations, int32_t* cycles);
 int ikr_linear_solver_analyze_pattern(ikr_ls ls, ikr_asm a);
 int ikr_linear_solver_factorize(ikr_ls ls, ikr_asm a);       /* builds the preconditioner from the device K */
 /* solve(x, b) with host arrays of size() (Full option system) */
@@ -238,15 +251,18 @@ int ikr_fes_stream(ikr_fes fes, void** stream);
  * reference).  For callers that may not allocate device memory after start-up (a fixed device-memory
  * budget, or all allocations routed through their own allocator): it calls no cudaMalloc / cudaFree /
  * cudaMallocHost and no allocating library routine.  The CG vectors, the 3x3 block-Jacobi inverse and the
- * reduction slots live in one file-scope device array of the library (about 8.7 MB, held by every GPU that
- * loads the library until exit), so the system may have at most IKR_NOALLOC_MAX_NODES nodes (3x as many
- * dofs); larger systems return IKR_ERR_ARG.  b and x are device pointers of size() doubles; the CG runs in
+ * reduction slots live in one file-scope device array of the library (about 8.7 MB), so the system may have
+ * at most IKR_NOALLOC_MAX_NODES nodes (3x as many dofs); larger systems return IKR_ERR_ARG.  The array's
+ * device memory is committed when the library's device code is loaded on a GPU -- with CUDA's lazy module
+ * loading (the default) at the first call of this entry point on that GPU -- and held until the process
+ * exits; later calls change no device-memory figure.  b and x are device pointers of size() doubles; the CG runs in
  * the precision of the stored tangent with the same block-Jacobi preconditioner, tolerance rtol on
  * ||r|| / ||b|| and at most max_iter iterations (IKR_ERR_NOT_CONVERGED when that limit is hit).
  * The first call on a device looks up the array's device address; make that call before any stream
  * capture.  All calls share the one array, which keeps the last call's contents (every call re-initialises
  * what it reads), so calls whose GPU work overlaps -- e.g. from two element sets on different streams --
- * race on it: serialise them. */
+ * race on it: serialise them.  The looked-up address is kept for the process; after cudaDeviceReset (which
+ * also frees every handle's device memory) no handle of this library, this entry point included, is valid. */
 #define IKR_NOALLOC_MAX_NODES 32768
 int ikr_linear_solver_solve_noalloc(ikr_asm a, const double* b_device, double* x_device, double rtol,
                                     int32_t max_iter, int32_t* iterations);

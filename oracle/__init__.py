@@ -69,6 +69,8 @@ def lib():
         L.orc_path_following.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int, ip, C.c_int, C.c_double, C.c_int,
                                          C.c_int, C.c_double, dp, dp, ip, dp, dp, dp, C.POINTER(C.c_int),
                                          C.POINTER(C.c_int)]
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_load_step.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp, dp]
         L.orc_path_following_toy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, dp,
                                              dp, ip, dp, dp, C.POINTER(C.c_int)]
         _lib = L
@@ -82,6 +84,11 @@ def _p(a, t):
 def _check(code, what):
     if code != 0:
         raise OracleError(code, what)
+
+
+def set_threads(n):
+    """Threads of the oracle's CG (assembly stays serial); results depend only on the count."""
+    _check(lib().orc_set_threads(int(n)), "set_threads")
 
 
 def cg_jacobi(col_ptr, row_idx, values, b, rtol, max_iter):
@@ -274,6 +281,18 @@ class OracleProblem:
             raise OracleError(code, "load_control")
         return dict(u=u, lam=float(lam[0]), iterations=its[: ns.value], res_norms=rn[: ns.value],
                     total_iterations=tot.value, success=(code == 0))
+
+    def load_step(self, u, lam, dlambda, tol=1e-8, tol_mode=1, max_iter=30, solver=SOLVER_CG_JACOBI, cg_rtol=1e-10):
+        """One LoadControl step from (u, lam): lambda += dlambda and Newton to the tolerance.  Returns (u, lambda,
+        stats) with stats = dict(newton, cg, t_residual, t_tangent, t_solve, residual_norm)."""
+        uu = self._u(u).copy()
+        lm = np.array([lam], dtype=np.float64)
+        st = np.zeros(6)
+        code = lib().orc_load_step(self.h, dlambda, tol, tol_mode, max_iter, solver, cg_rtol, _p(uu, C.c_double),
+                                   _p(lm, C.c_double), _p(st, C.c_double))
+        _check(code, "load_step")
+        return uu, float(lm[0]), dict(zip(("newton", "cg", "t_residual", "t_tangent", "t_solve", "residual_norm"),
+                                          st.tolist()))
 
     def path_following(self, steps, step_size, kind=PF_ARC_LENGTH, controlled=None, target_iterations=0, tol=1e-8,
                        max_iter=20, solver=SOLVER_BANDED_LDLT, cg_rtol=1e-12, u0=None, lam0=0.0,

@@ -12,10 +12,14 @@
 
 #include <algorithm>
 #include <array>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <functional>
+#include <mutex>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -855,9 +859,81 @@ bool banded_ldlt_solve(const CSC& A, const std::vector<double>& b, std::vector<d
 
 // Jacobi-preconditioned CG (the reference's si_ConjugateGradient: Eigen ConjugateGradient with its
 // default diagonal preconditioner, linearsolver.cpp:23-25), relative tolerance on ||r||/||b||.
+// Fork-join pool for the CG's vector work: task t of T covers the rows [t n / T, (t + 1) n / T), and partial sums
+// are added in task order, so results depend only on the thread count (one thread: the plain serial loops).
+// Eigen runs ConjugateGradient<SparseMatrix, Lower | Upper> -- the reference's si_ConjugateGradient
+// (solver/linearsolver/linearsolver.cpp:24) -- with a multithreaded matrix-vector product when OpenMP is on; this
+// pool stands in for that.  Element assembly stays serial, as in the reference's assembler.
+int g_threads = 1;
+class Pool {
+ public:
+  explicit Pool(int n) : n_(n) {
+    for (int t = 1; t < n_; ++t) th_.emplace_back([this, t] { loop(t); });
+  }
+  ~Pool() {
+    {
+      std::lock_guard<std::mutex> l(m_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  int size() const { return n_; }
+  // runs f(t) for t = 0..n-1 (t = 0 on the calling thread) and waits for all
+  void run(const std::function<void(int)>& f) {
+    {
+      std::lock_guard<std::mutex> l(m_);
+      job_ = &f;
+      pending_ = n_ - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    f(0);
+    std::unique_lock<std::mutex> l(m_);
+    done_.wait(l, [this] { return pending_ == 0; });
+  }
+
+ private:
+  void loop(int t) {
+    int seen = 0;
+    for (;;) {
+      const std::function<void(int)>* job;
+      {
+        std::unique_lock<std::mutex> l(m_);
+        cv_.wait(l, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+        job = job_;
+      }
+      (*job)(t);
+      {
+        std::lock_guard<std::mutex> l(m_);
+        if (--pending_ == 0) done_.notify_one();
+      }
+    }
+  }
+  int n_;
+  std::vector<std::thread> th_;
+  std::mutex m_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* job_ = nullptr;
+  int pending_ = 0, gen_ = 0;
+  bool stop_ = false;
+};
+
 bool cg_jacobi_solve(const CSC& A, const std::vector<double>& b, std::vector<double>& x, double rtol, int maxit,
                      int* iterations = nullptr) {
   const int n = A.n;
+  const int T = std::max(1, std::min(g_threads, n));
+  Pool pool(T);
+  auto lo = [&](int t) { return (int)((int64_t)n * t / T); };
+  std::vector<double> part(T);
+  auto reduce = [&] {
+    double s = 0;
+    for (double v : part) s += v;
+    return s;
+  };
   std::vector<double> diag(n, 1.0), r(b), z(n), pv(n), q(n);
   for (int c = 0; c < n; ++c)
     for (int64_t k = A.cp[c]; k < A.cp[c + 1]; ++k)
@@ -872,30 +948,44 @@ bool cg_jacobi_solve(const CSC& A, const std::vector<double>& b, std::vector<dou
   double rz = 0;
   for (int i = 0; i < n; ++i) rz += r[i] * z[i];
   for (int it = 0; it < maxit; ++it) {
-    std::fill(q.begin(), q.end(), 0.0);
-    for (int c = 0; c < n; ++c) {  // symmetric: q = A p
-      const double pc = pv[c];
-      for (int64_t k = A.cp[c]; k < A.cp[c + 1]; ++k) q[A.ri[k]] += A.v[k] * pc;
-    }
-    double pq = 0;
-    for (int i = 0; i < n; ++i) pq += pv[i] * q[i];
-    const double al = rz / pq;
-    double rn = 0;
-    for (int i = 0; i < n; ++i) {
-      x[i] += al * pv[i];
-      r[i] -= al * q[i];
-      rn += r[i] * r[i];
-    }
+    // q = A p (A symmetric: column i of the CSC is row i) and p.q
+    pool.run([&](int t) {
+      double pq = 0;
+      for (int i = lo(t); i < lo(t + 1); ++i) {
+        double acc = 0;
+        for (int64_t k = A.cp[i]; k < A.cp[i + 1]; ++k) acc += A.v[k] * pv[A.ri[k]];
+        q[i] = acc;
+        pq += pv[i] * acc;
+      }
+      part[t] = pq;
+    });
+    const double al = rz / reduce();
+    pool.run([&](int t) {
+      double rn = 0;
+      for (int i = lo(t); i < lo(t + 1); ++i) {
+        x[i] += al * pv[i];
+        r[i] -= al * q[i];
+        rn += r[i] * r[i];
+      }
+      part[t] = rn;
+    });
+    const double rn = reduce();
     if (iterations) *iterations = it + 1;
     if (std::sqrt(rn) <= rtol * bn) return true;
-    double rzn = 0;
-    for (int i = 0; i < n; ++i) {
-      z[i] = r[i] / diag[i];
-      rzn += r[i] * z[i];
-    }
+    pool.run([&](int t) {
+      double rzn = 0;
+      for (int i = lo(t); i < lo(t + 1); ++i) {
+        z[i] = r[i] / diag[i];
+        rzn += r[i] * z[i];
+      }
+      part[t] = rzn;
+    });
+    const double rzn = reduce();
     const double be = rzn / rz;
     rz = rzn;
-    for (int i = 0; i < n; ++i) pv[i] = z[i] + be * pv[i];
+    pool.run([&](int t) {
+      for (int i = lo(t); i < lo(t + 1); ++i) pv[i] = z[i] + be * pv[i];
+    });
   }
   return false;
 }
@@ -1172,6 +1262,64 @@ int orc_assemble_matrix_csc(orc_problem* p, const double* u, double lambda, int 
   if (ri) std::copy(A.ri.begin(), A.ri.end(), ri);
   if (v) std::copy(A.v.begin(), A.v.end(), v);
   return ORC_OK;
+}
+
+int orc_set_threads(int n) {
+  if (n < 1) return ORC_ERR_ARG;
+  g_threads = n;
+  return ORC_OK;
+}
+
+int orc_load_step(orc_problem* p, double dlambda, double tol, int tol_mode, int max_iter, int solver, double cg_rtol,
+                  double* u, double* lambda, double* stats) {
+  if (!p || !u || !lambda || !stats || !p->idbc_rate.empty()) return ORC_ERR_ARG;
+  using clk = std::chrono::steady_clock;
+  auto secs = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+  const int n = p->ndof();
+  std::vector<double> x(u, u + n), R, dx;
+  CSC K;
+  double t_res = 0, t_mat = 0, t_sol = 0;
+  int64_t cg_total = 0;
+  *lambda += dlambda;  // LoadControl::predictor (loadcontrol.inl:54-57)
+  auto t0 = clk::now();
+  int st = assemble_vector(*p, x.data(), *lambda, ORC_DBC_FULL, R);
+  t_res += secs(t0, clk::now());
+  if (st) return st;
+  double rn = norm2(R);
+  const double thr = tol_mode == 1 ? tol * rn : tol;
+  int it = 0;
+  while (rn > thr && it < max_iter) {  // newtonraphson.hh:219-247
+    t0 = clk::now();
+    st = assemble_matrix(*p, x.data(), ORC_DBC_FULL, K);
+    t_mat += secs(t0, clk::now());
+    if (st) return st;
+    std::vector<double> b(n);
+    for (int i = 0; i < n; ++i) b[i] = -R[i];
+    t0 = clk::now();
+    int its = 0;
+    const bool ok = solver == ORC_SOLVER_CG_JACOBI ? cg_jacobi_solve(K, b, dx, cg_rtol, 20 * n, &its)
+                                                   : banded_ldlt_solve(K, b, dx);
+    t_sol += secs(t0, clk::now());
+    cg_total += its;
+    if (!ok) return ORC_ERR_SINGULAR;
+    st = update_state(*p, x.data(), dx.data());
+    if (st) return st;
+    for (int i = 0; i < n; ++i) x[i] += dx[i];
+    t0 = clk::now();
+    st = assemble_vector(*p, x.data(), *lambda, ORC_DBC_FULL, R);
+    t_res += secs(t0, clk::now());
+    if (st) return st;
+    rn = norm2(R);
+    ++it;
+  }
+  std::copy(x.begin(), x.end(), u);
+  stats[0] = it;
+  stats[1] = (double)cg_total;
+  stats[2] = t_res;
+  stats[3] = t_mat;
+  stats[4] = t_sol;
+  stats[5] = rn;
+  return it == max_iter ? ORC_ERR_NOT_CONVERGED : ORC_OK;
 }
 
 int orc_load_control(orc_problem* p, int steps, double t0, double t1, double tol, int tol_mode, int max_iter,

@@ -97,6 +97,16 @@ int orc_load_control(orc_problem* p, int load_steps, double t_begin, double t_en
                      int max_iter, int solver, double cg_rtol, double* u, double* lambda, int32_t* iterations,
                      double* res_norms, int* n_solves, int* total_iterations);
 
+/* Threads of the oracle's CG (default 1; matrix-vector products and vector updates split into fixed row ranges,
+ * partial sums added in range order, so results depend only on the count).  Assembly stays serial. */
+int orc_set_threads(int n);
+/* One load step of LoadControl (loadcontrol.inl:54-57) with Newton-Raphson (newtonraphson.hh:193-257): lambda +=
+ * dlambda, Newton from u to ||R|| <= tol ||R at the step start|| (tol_mode 1) or ||R|| <= tol (0), Full Dirichlet
+ * handling, no inhomogeneous Dirichlet values.  stats[6]: Newton iterations, linear-solver (CG) iterations, seconds
+ * in residual assembly, in tangent assembly, in linear solves, final ||R||. */
+int orc_load_step(orc_problem* p, double dlambda, double tol, int tol_mode, int max_iter, int solver, double cg_rtol,
+                  double* u, double* lambda, double* stats);
+
 /* Path following (pathfollowing.inl:25-73) with Newton-Raphson and a scalar subsidiary function
  * (newtonraphsonwithscalarsubsidiaryfunction.hh:207-316).  kind: ORC_PF_* (pathfollowingfunctions.hh);
  * controlled: DisplacementControl's dof indices; target_iterations > 0 selects AdaptiveStepSizing::IterationBased

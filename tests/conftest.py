@@ -1,3 +1,4 @@
+import json
 import os
 import sys
 
@@ -18,3 +19,18 @@ def ikr():
     import ikarus_gb300
     ikarus_gb300.lib()
     return ikarus_gb300
+
+
+@pytest.fixture
+def parity_log(request):
+    """record(output, error, bound): prints the measured error of an output beside its bound and, when the
+    environment variable IKR_PARITY_LOG names a file, appends it there as one JSON line."""
+    def record(output, error, bound, **extra):
+        line = dict(test=request.node.nodeid, output=output, error=float(error), bound=float(bound), **extra)
+        print(f"PARITY {output}: error {error:.3e} (bound {bound:.1e})")
+        path = os.environ.get("IKR_PARITY_LOG")
+        if path:
+            with open(path, "a") as f:
+                f.write(json.dumps(line) + "\n")
+        return error <= bound
+    return record

@@ -1,7 +1,7 @@
 """Generates tests/golden/reference_goldens.json from the reference's own test sources (read as text).
 
-Run in a container where the reference is mounted at /root/reference; the JSON it writes is committed so
-the tests never read the reference at run time.
+Run with the path of a reference checkout as its only argument; the JSON it writes is committed so the tests
+never read the reference at run time.
 
 Sources:
   tests/src/testcantileverbeamEAS.cpp:60-96   3D cantilever (NR + LoadControl + SparseFlatAssembler + EAS):
@@ -23,7 +23,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python make_goldens.py <path of the reference checkout>")
+REF = sys.argv[1]
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
 
 

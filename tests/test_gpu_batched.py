@@ -10,23 +10,35 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-def test_batched_instances_match_individual_oracle_solves(ikr, precision):
+def test_batched_instances_match_individual_oracle_solves(ikr, precision, parity_log):
+    """Plain FP64: every instance's Newton to ||R|| <= 1e-9 ||R0|| per step (1e-10 is at the FP64 residual floor of
+    one of these small beams), displacement within 1e-8 of the oracle's (solved to the same tolerance with its
+    direct solve).  Mixed: FP32 tangent and CG with the FP64
+    residual test at 1e-8 per step (the benchmark's criterion); its displacement error against the oracle is
+    logged and bounded by 1e-6."""
     bp = problems.batched_cantilevers(n=12, seed=3, nx=(3, 8), nyz=(1, 3), E=(1e3, 1e4), t=(0.1, 0.5),
                                       load_steps=4)
     fes, asm = problems.build_gpu_batched(bp, precision=precision)
     req = ikr.FERequirements(fes)
-    st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=precision == 1, linear_rtol=1e-10 if
-                        precision == 0 else 1e-2, linear_rtol_min=1e-6)
+    if precision == 0:
+        st = ikr.NRSettings(tol=1e-9, maxIter=30, relative=True, linear_rtol=1e-12)
+    else:
+        st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                            linear_rtol_min=1e-6)
     nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
     info = ikr.LoadControl(nr, bp.load_steps).run(req)
     assert info.success
     its, rn, conv = nr.instance_info()
     assert (conv == 1).all()
     u = req.globalSolution()
+    worst = 0.0
     for i, part in enumerate(bp.parts):
-        ref = oracle.from_problem(part).load_control(bp.load_steps, tol=1e-8, tol_mode=1)
+        ref = oracle.from_problem(part).load_control(bp.load_steps, tol=1e-9, tol_mode=1, max_iter=30)
         ui = u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]]
-        assert np.abs(ui - ref["u"]).max() <= 1e-6 * np.abs(ref["u"]).max(), i
+        worst = max(worst, np.abs(ui - ref["u"]).max() / np.abs(ref["u"]).max())
+    form = "FP64" if precision == 0 else "mixed"
+    assert parity_log(f"batched {form}: max over instances of max|u - u_oracle| / max|u_oracle|", worst,
+                      1e-8 if precision == 0 else 1e-6)
 
 
 def test_an_inverting_instance_is_taken_out_and_the_others_converge(ikr):

@@ -234,7 +234,7 @@ def test_cantilever_goldens_on_gpu(ikr, es, material):
     assert all(si.residualNorm <= g["tol"] for si in info.solverInfos)
 
 
-def test_config1_plain_fp64_matches_oracle(ikr):
+def test_config1_plain_fp64_matches_oracle(ikr, parity_log):
     p = problems.config1()
     o = oracle.from_problem(p)
     ref = o.load_control(p.load_steps, tol=p.tol)
@@ -245,13 +245,14 @@ def test_config1_plain_fp64_matches_oracle(ikr):
     info = ikr.LoadControl(nr, p.load_steps).run(req)
     assert info.success
     assert [s.iterations for s in info.solverInfos] == list(ref["iterations"])
-    assert rel_err(req.globalSolution(), ref["u"]) <= 1e-8
+    assert parity_log("config1 FP64: max|u - u_oracle| / max|u_oracle|", rel_err(req.globalSolution(), ref["u"]),
+                      1e-8)
 
 
-def test_config1_mixed_precision_reaches_fp64_tolerance(ikr):
+def test_config1_mixed_precision_reaches_fp64_tolerance(ikr, parity_log):
     p = problems.config1()
     o = oracle.from_problem(p)
-    ref = o.load_control(p.load_steps, tol=1e-8, tol_mode=1)
+    ref = o.load_control(p.load_steps, tol=1e-10, tol_mode=1)
     fes, asm = problems.build_gpu(p, precision=1)
     req = ikr.FERequirements(fes)
     st = ikr.NRSettings(tol=1e-8, relative=True, eisenstat_walker=True, linear_rtol=1e-2, linear_rtol_min=1e-6)
@@ -263,7 +264,8 @@ def test_config1_mixed_precision_reaches_fp64_tolerance(ikr):
     # the FP64 residual of every load step reached 1e-8 of its starting value
     for si in info.solverInfos[1:]:
         assert si.success
-    assert rel_err(req.globalSolution(), ref["u"]) <= 1e-6
+    assert parity_log("config1 mixed: max|u - u_oracle| / max|u_oracle|", rel_err(req.globalSolution(), ref["u"]),
+                      1e-6)
 
 
 @pytest.mark.parametrize("es", ["GreenLagrangeStrain", "DisplacementGradient", "DisplacementGradientTransposed"])

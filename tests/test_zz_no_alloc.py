@@ -4,13 +4,17 @@ ikr_linear_solver_solve_noalloc serves callers that may not allocate device memo
 (a device-memory budget fixed at start-up, or allocations that must all go through the caller's own
 allocator): its CG work set lives in a fixed device array inside the library.  The caller still provides
 the right-hand side and the solution buffer.  This test calls it through the C ABI twice in a row and
-compares both results with ikr_linear_solver_solve on the same assembled tangent.
+compares both results with ikr_linear_solver_solve on the same assembled tangent, checks the residual of
+each result against the oracle's FP64 tangent, and checks that the second call leaves the device's free
+memory unchanged (the first call on a device may still commit the library's fixed array when CUDA loads
+device code lazily).
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
+import oracle
 from ikarus_gb300 import problems
 
 pytestmark = pytest.mark.gpu
@@ -40,16 +44,32 @@ def test_noalloc_solve_matches_regular_solve_twice(ikr, precision):
     ls.compute(asm)
     x_ref = ls.solve(asm, b)
 
+    # the oracle's FP64 tangent at the same state: K x - b of every result
+    sp = pytest.importorskip("scipy.sparse")
+    cp, ri, v, n = oracle.from_problem(p).assemble_matrix_csc(u, 0.5)
+    K = sp.csc_matrix((v, ri, cp), shape=(n, n))
+    # FP64: the CG's own tolerance plus round-off; FP32: the FP32 tangent's rounding (entries within 2e-6 of the
+    # FP64 ones) times this small system's condition number adds to the 1e-5 of the FP32 CG
+    res_tol = 1e-11 if precision == 0 else 1e-3
+
     b_dev = torch.tensor(b, dtype=torch.float64, device="cuda")
     for call in range(2):  # the shared scratch keeps the previous call's contents; results must not depend on it
         x_dev = torch.full((p.n_dofs,), float("nan"), dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         code, its = _solve_noalloc(ikr, asm, b_dev.data_ptr(), x_dev.data_ptr(), rtol)
+        torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
         assert code == 0, (call, code)
         assert its > 0
+        if call == 1:
+            assert free_after == free_before, (free_before, free_after)
         x = x_dev.cpu().numpy()
         tol = 1e-10 if precision == 0 else 1e-4
         assert np.abs(x - x_ref).max() <= tol * np.abs(x_ref).max(), call
+        rel = np.linalg.norm(K @ x - b) / np.linalg.norm(b)
+        print(f"noalloc precision {precision} call {call}: ||K64 x - b|| / ||b|| = {rel:.3e} ({its} iterations)")
+        assert rel <= res_tol, (call, rel)
 
 
 def test_noalloc_rejects_systems_above_its_limit(ikr):
