@@ -561,7 +561,8 @@ def run_reference(args, world):
               f"1e-10 on {T} threads; serial assembly with the reference's per-(i,j) moduli); value = "
               f"{p.load_steps} x the mean measured load-step time")
     detail = {"load_steps_measured": len(steps), "threads": T,
-              "per_step": [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in s.items()} for s in steps]}
+              "per_step": [{k: (float(f"{v:.4g}") if isinstance(v, float) else v) for k, v in s.items()}
+                           for s in steps]}
     print(json.dumps({"metric": METRIC, "value": round(val, 2), "unit": "s", "impl": "reference", "n_gpus": world,
                       "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
                       "vs_baseline": None, "dtype": "fp64", "data": "synthetic",

@@ -61,10 +61,32 @@ class EAS(enum.IntEnum):  # strain measure enhanced by the EAS skill (strainenha
 
 
 class SolverTypeTag(enum.IntEnum):  # ikarus/solver/linearsolver/linearsolver.hh:28-31 (+ device solvers)
+    """The reference's 19 tags with their values (what each runs on the device: include/ikarus_gb300.h), then the
+    device solvers of this library."""
     none = 0
     si_ConjugateGradient = 1
+    si_LeastSquaresConjugateGradient = 2
+    si_BiCGSTAB = 3
+    sd_SimplicialLLT = 4
+    sd_SimplicialLDLT = 5
+    sd_SparseLU = 6
+    sd_SparseQR = 7
+    sd_CholmodSupernodalLLT = 8
+    sd_UmfPackLU = 9
+    sd_SuperLU = 10
+    d_PartialPivLU = 11
+    d_FullPivLU = 12
+    d_HouseholderQR = 13
+    d_ColPivHouseholderQR = 14
+    d_FullPivHouseholderQR = 15
+    d_CompleteOrthogonalDecomposition = 16
+    d_LLT = 17
+    d_LDLT = 18
     gpu_PCG_BlockJacobi = 100
     gpu_PCG_Batched = 101
+
+
+DIRECT_SOLVE_RTOL = 1e-13  # IKR_DIRECT_SOLVE_RTOL: accuracy of the sparse direct tags' device solve
 
 
 class Precision(enum.IntEnum):
@@ -109,7 +131,7 @@ class _NRState(C.Structure):
 
 class _ControlState(C.Structure):
     _fields_ = [("domain", C.c_void_p), ("load_step", C.c_int32), ("step_size", C.c_double),
-                ("load_factor", C.c_double)]
+                ("load_factor", C.c_double), ("total_iterations", C.c_int32), ("name", C.c_char_p)]
 
 
 class _ControlInfo(C.Structure):
@@ -118,6 +140,7 @@ class _ControlInfo(C.Structure):
 
 
 _NR_OBS = C.CFUNCTYPE(None, C.c_int32, C.POINTER(_NRState), C.c_void_p)
+_LOG_SINK = C.CFUNCTYPE(None, C.c_char_p, C.c_void_p)
 _CTRL_OBS = C.CFUNCTYPE(None, C.c_int32, C.POINTER(_ControlState), C.c_void_p)
 
 # exported entry points and their ctypes signatures (kept in sync with include/ikarus_gb300.h)
@@ -159,6 +182,7 @@ SIGNATURES = {
     "ikr_assembler_destroy": ([_vp], C.c_int),
     "ikr_assembler_add_point_loads": ([_vp, _I, _ip, _dp], C.c_int),
     "ikr_assembler_bind": ([_vp, _vp, _I], C.c_int),
+    "ikr_assembler_add_matrix_entries": ([_vp, _I, _ip, _ip, _dp], C.c_int),
     "ikr_assembler_size": ([_vp, _ip], C.c_int),
     "ikr_assembler_reduced_size": ([_vp, _ip], C.c_int),
     "ikr_assembler_constraints_below": ([_vp, _ip], C.c_int),
@@ -172,8 +196,19 @@ SIGNATURES = {
     "ikr_linear_solver_destroy": ([_vp], C.c_int),
     "ikr_linear_solver_set_tolerance": ([_vp, _D, _I], C.c_int),
     "ikr_linear_solver_analyze_pattern": ([_vp, _vp], C.c_int),
+    "ikr_assembler_scalar": ([_vp, _vp, _I, _dp], C.c_int),
+    "ikr_nonlinear_operator_create": ([C.POINTER(_vp), _vp, _I, _I, _I, _I], C.c_int),
+    "ikr_nonlinear_operator_destroy": ([_vp], C.c_int),
+    "ikr_nonlinear_operator_evaluate": ([_vp, _I, _vp, _dp, _ip], C.c_int),
+    "ikr_newton_residual": ([_vp, _vp, _dp], C.c_int),
+    "ikr_newton_jacobian": ([_vp, _vp], C.c_int),
+    "ikr_newton_update": ([_vp, _vp, _dp], C.c_int),
+    "ikr_newton_subscribe_logger": ([_vp, _LOG_SINK, _vp], C.c_int),
+    "ikr_load_control_subscribe_logger": ([_vp, _LOG_SINK, _vp], C.c_int),
+    "ikr_path_following_subscribe_logger": ([_vp, _LOG_SINK, _vp], C.c_int),
     "ikr_linear_solver_set_fp64_outer": ([_vp, _I, _D, _I, _I], C.c_int),
     "ikr_linear_solver_outer_info": ([_vp, _ip, _ip], C.c_int),
+    "ikr_linear_solver_set_wait_test": ([_vp, _I, _I], C.c_int),
     "ikr_linear_solver_factorize": ([_vp, _vp], C.c_int),
     "ikr_linear_solver_solve": ([_vp, _vp, _dp, _dp], C.c_int),
     "ikr_linear_solver_last_info": ([_vp, _ip, _dp], C.c_int),
@@ -505,6 +540,14 @@ class SparseFlatAssembler:
         v = np.ascontiguousarray(values, dtype=np.float64)
         _err(lib().ikr_assembler_add_point_loads(self.h, len(d), _ptr(d, C.c_int32), _ptr(v)), "point loads")
 
+    def add_matrix_entries(self, rows, cols, values):
+        """AssemblerManipulator matrix hook: K(row, col) += value after every assembly (springs)."""
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        c = np.ascontiguousarray(cols, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        _err(lib().ikr_assembler_add_matrix_entries(self.h, len(r), _ptr(r, C.c_int32), _ptr(c, C.c_int32), _ptr(v)),
+             "add_matrix_entries")
+
     def size(self):
         return self.fes.n_dofs
 
@@ -609,16 +652,136 @@ class SparseFlatAssembler:
         _err(lib().ikr_assembler_vector_norm(self.h, C.byref(v)))
         return v.value
 
+    def scalar(self, req=None, affordance=ScalarAffordance.mechanicalPotentialEnergy):
+        """scalar(req, affordance): the sum of the element energies in element order (simpleassemblers.inl)."""
+        req, _ = self._args(req, None)
+        v = C.c_double()
+        _err(lib().ikr_assembler_scalar(self.h, req.h, int(affordance), C.byref(v)), "scalar")
+        return v.value
+
+
+# ---- NonLinearOperator ------------------------------------------------------------------------------------
+@dataclass(frozen=True)
+class AffordanceCollection:  # ferequirements.hh:35-89, 205-208
+    scalarAffordance: ScalarAffordance = ScalarAffordance.noAffordance
+    vectorAffordance: VectorAffordance = VectorAffordance.forces
+    matrixAffordance: MatrixAffordance = MatrixAffordance.stiffness
+
+    @property
+    def hasScalarAffordance(self):
+        return self.scalarAffordance != ScalarAffordance.noAffordance
+
+
+class AffordanceCollections:
+    elastoStatics = AffordanceCollection(ScalarAffordance.mechanicalPotentialEnergy, VectorAffordance.forces,
+                                         MatrixAffordance.stiffness)
+
+
+class DifferentiableFunction:
+    """One derivative order of the non-linear operator: f(req) returns the energy (float), the force vector
+    (numpy) or the tangent (scipy CSC exported from the assembler's device storage)."""
+
+    def __init__(self, op, order):
+        self._op, self.order = op, order
+
+    def __call__(self, req):
+        a = self._op.assembler
+        kind = C.c_int32()
+        if self._op.kind_of(self.order) == 1:
+            n = a.reducedSize() if self._op.dbcOption == DBCOption.Reduced else a.size()
+            out = np.zeros(n)
+            _err(lib().ikr_nonlinear_operator_evaluate(self._op.h, self.order, req.h, _ptr(out), C.byref(kind)), "op")
+            return out
+        v = C.c_double()
+        _err(lib().ikr_nonlinear_operator_evaluate(self._op.h, self.order, req.h, C.byref(v), C.byref(kind)), "op")
+        return v.value if kind.value == 0 else a.export_csc(self._op.dbcOption)
+
+    def derivative(self):
+        return DifferentiableFunction(self._op, self.order + 1)
+
+
+def derivative(f: DifferentiableFunction) -> DifferentiableFunction:
+    """derivative(f) of the reference's DifferentiableFunction (differentiablefunction.hh:60-87)."""
+    return f.derivative()
+
+
+class _NonLinearOperator:
+    def __init__(self, assembler, affordances: AffordanceCollection, dbcOption: DBCOption):
+        h = C.c_void_p()
+        _err(lib().ikr_nonlinear_operator_create(C.byref(h), assembler.h, int(affordances.scalarAffordance),
+                                                 int(affordances.vectorAffordance),
+                                                 int(affordances.matrixAffordance), int(dbcOption)), "op")
+        self.h, self.assembler, self.affordances, self.dbcOption = h, assembler, affordances, DBCOption(dbcOption)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.ikr_nonlinear_operator_destroy(self.h)
+            self.h = None
+
+    def kind_of(self, order):
+        return order if self.affordances.hasScalarAffordance else order + 1
+
+
+class DifferentiableFunctionFactory:  # utils/differentiablefunctionfactory.hh:22-65
+    @staticmethod
+    def op(assembler, affordances: AffordanceCollection = None, dbcOption: DBCOption = DBCOption.Full):
+        """The non-linear operator over the assembler: energy -> forces -> stiffness with a scalar affordance in the
+        collection, forces -> stiffness without.  Returns f; derivative(f) is the next order."""
+        if affordances is None:
+            affordances = AffordanceCollection()
+        return DifferentiableFunction(_NonLinearOperator(assembler, affordances, dbcOption), 0)
+
+
+# ---- listeners --------------------------------------------------------------------------------------------
+class _Logger:
+    def __init__(self, sink=None):
+        """sink(line) receives every line; None prints through the library ("[info] <line>" on stdout)."""
+        self.lines = []
+        self._sink = sink
+
+        def tramp(line, _user):
+            text = line.decode()
+            self.lines.append(text)
+            if self._sink is not None:
+                self._sink(text)
+        self._cb = _LOG_SINK(tramp) if sink is not None else _LOG_SINK()
+        self._subscribed = []
+
+    def _cb_for(self):
+        return self._cb
+
+
+class NonLinearSolverLogger(_Logger):
+    """NonLinearSolverLogger (utils/listener/nonlinearsolverlogger.hh:22-95)."""
+
+    def subscribeTo(self, nr: "NewtonRaphson"):
+        _err(lib().ikr_newton_subscribe_logger(nr.h, self._cb, None), "logger")
+        self._subscribed.append(nr)
+        return self
+
+
+class ControlLogger(_Logger):
+    """ControlLogger (utils/listener/controllogger.hh:22-66)."""
+
+    def subscribeTo(self, control):
+        fn = lib().ikr_path_following_subscribe_logger if isinstance(control, PathFollowing) else \
+            lib().ikr_load_control_subscribe_logger
+        _err(fn(control.h, self._cb, None), "logger")
+        self._subscribed.append(control)
+        return self
+
 
 # ---- solvers ---------------------------------------------------------------------------------------------
 class LinearSolver:
     """LinearSolver facade (linearsolver.hh:49-233) over the device CG solvers."""
 
-    def __init__(self, tag: SolverTypeTag = SolverTypeTag.gpu_PCG_BlockJacobi, rtol=1e-10, max_iter=100000):
+    def __init__(self, tag: SolverTypeTag = SolverTypeTag.gpu_PCG_BlockJacobi, rtol=None, max_iter=100000):
         h = C.c_void_p()
         _err(lib().ikr_linear_solver_create(C.byref(h), int(tag)), "linear solver")
         self.h = h
         self.tag = tag
+        if rtol is None:  # the sparse direct tags default to a direct solver's accuracy
+            rtol = DIRECT_SOLVE_RTOL if SolverTypeTag.sd_SimplicialLLT <= tag <= SolverTypeTag.sd_UmfPackLU else 1e-10
         self.setTolerance(rtol, max_iter)
 
     def __del__(self):
@@ -684,6 +847,11 @@ class LinearSolver:
         per application) on the FP32 rounding of the same tangent."""
         _err(lib().ikr_linear_solver_set_fp64_outer(self.h, int(restart), float(inner_rtol), int(inner_max_iter),
                                                     int(outer_max_iter)))
+
+    def set_wait_test(self, barrier_polls=0, withhold_first_arrival=False):
+        """Test hook of the bounded device waits: grid-barrier poll limit of the persistent CG (0 = default) and a
+        one-launch switch that withholds CTA 0's first barrier arrival (the solve then reports the timeout)."""
+        _err(lib().ikr_linear_solver_set_wait_test(self.h, int(barrier_polls), int(bool(withhold_first_arrival))))
 
     def outer_info(self):
         """(Arnoldi steps, restart cycles) of the last FP64 outer solve."""
@@ -789,6 +957,35 @@ class NewtonRaphson:
     def subscribe_fe_state(self, on=True):
         _err(lib().ikr_newton_subscribe_fe_state(self.h, int(on)))
 
+    def residual(self):
+        """residual() (newtonraphson.hh:260-268): f(req) -> force vector with the Full Dirichlet treatment."""
+        nr = self
+
+        def f(req):
+            out = np.zeros(nr.assembler.size())
+            _err(lib().ikr_newton_residual(nr.h, req.h, _ptr(out)), "residual")
+            return out
+        return f
+
+    def jacobian(self):
+        """jacobian() (newtonraphson.hh:270-280): f(req) -> tangent (scipy CSC, Full Dirichlet treatment)."""
+        nr = self
+
+        def f(req):
+            _err(lib().ikr_newton_jacobian(nr.h, req.h), "jacobian")
+            return nr.assembler.export_csc(DBCOption.Full)
+        return f
+
+    def updateFunction(self):
+        """updateFunction() (newtonraphson.hh:282-287): f(req, dx) adds dx to the displacement (and re-imposes
+        inhomogeneous Dirichlet values)."""
+        nr = self
+
+        def f(req, dx):
+            d = np.ascontiguousarray(dx, dtype=np.float64)
+            _err(lib().ikr_newton_update(nr.h, req.h, _ptr(d)), "update")
+        return f
+
     def instance_info(self):
         """(iterations, residual norms, status) per instance of the last batched solve; status 1 converged,
         0 not converged, -1 taken out after its elements inverted (det C <= 0)."""
@@ -836,7 +1033,9 @@ class LoadControl:
         """fn(message: ControlMessages, state: dict)"""
         def tramp(msg, st, _user):
             s = st.contents
-            fn(ControlMessages(msg), dict(loadStep=s.load_step, stepSize=s.step_size, loadFactor=s.load_factor))
+            fn(ControlMessages(msg), dict(loadStep=s.load_step, stepSize=s.step_size, loadFactor=s.load_factor,
+                                          totalIterations=s.total_iterations,
+                                          name=s.name.decode() if s.name else ""))
         cb = _CTRL_OBS(tramp)
         self._cbs.append(cb)
         _err(lib().ikr_load_control_subscribe(self.h, cb, None), "subscribe")
@@ -963,7 +1162,9 @@ class PathFollowing:
         """fn(message: ControlMessages, state: dict)"""
         def tramp(msg, st, _user):
             s = st.contents
-            fn(ControlMessages(msg), dict(loadStep=s.load_step, stepSize=s.step_size, loadFactor=s.load_factor))
+            fn(ControlMessages(msg), dict(loadStep=s.load_step, stepSize=s.step_size, loadFactor=s.load_factor,
+                                          totalIterations=s.total_iterations,
+                                          name=s.name.decode() if s.name else ""))
         cb = _CTRL_OBS(tramp)
         self._cbs.append(cb)
         _err(lib().ikr_path_following_subscribe(self.h, cb, None), "subscribe")

@@ -50,16 +50,23 @@ __device__ __forceinline__ void cta_reduce(double (&v)[N], double* sw) {
 // arrives on the barrier counter and waits (bounded) until `target` arrivals; then warp 0 sums all CTAs'
 // partials with a fixed lane assignment and butterfly order (identical in every CTA) and every thread gets
 // the sums.  Returns false when the wait gave up.
+// WaitCtl: the poll limit, and (tests of the bounded wait only) CTA 0 withholding its arrival at the first barrier,
+// so that every CTA's first wait runs out and the solve ends with the timeout status.
+struct WaitCtl {
+  int polls;
+  int withhold_first;
+};
+
 template <int N>
 __device__ __forceinline__ bool grid_allreduce(double (&v)[N], double* part, unsigned int* count, unsigned int target,
-                                               double* sv, bool* ok_sh) {
+                                               double* sv, bool* ok_sh, WaitCtl wc) {
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < N; ++k) part[blockIdx.x * N + k] = v[k];
     __threadfence();
-    atomicAdd(count, 1u);
+    if (!(wc.withhold_first && blockIdx.x == 0 && target == gridDim.x)) atomicAdd(count, 1u);
     bool ok = false;
-    for (int i = 0; i < kBarrierSpinLimit; ++i) {
+    for (int i = 0; i < wc.polls; ++i) {
       unsigned int c;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(count) : "memory");
       if (c >= target) {
@@ -120,7 +127,7 @@ struct RhsSet {
 template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB, int NR>
 __global__ void __launch_bounds__(WARPS * 32, MINB)
     pcg_persistent_kernel(Bsr A, const T* __restrict__ val, const T* __restrict__ minv, RhsSet<T, NR> V,
-                          double* part_a, double* part_b, int64_t keep_g) {
+                          double* part_a, double* part_b, int64_t keep_g, WaitCtl wc) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[WARPS][NST];
@@ -319,7 +326,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     if (failed) break;
     cta_reduce<NR>(pq, sw);
     ++barrier_no;
-    if (!grid_allreduce<NR>(pq, part_a + par * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
+    if (!grid_allreduce<NR>(pq, part_a + par * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh, wc)) {
       failed = true;
       break;
     }
@@ -384,7 +391,8 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     }
     cta_reduce<2 * NR>(red2, sw);
     ++barrier_no;
-    if (!grid_allreduce<2 * NR>(red2, part_b + par * 2 * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
+    if (!grid_allreduce<2 * NR>(red2, part_b + par * 2 * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh,
+                                wc)) {
       failed = true;
       break;
     }
@@ -476,7 +484,8 @@ cudaError_t launch_persistent(const Bsr& A, PcgWork* const* ws, double* part_a, 
   }
   Bsr Acopy = A;
   int64_t keep = w.keep_g;
-  void* args[] = {&Acopy, &val, &minv, &V, &part_a, &part_b, &keep};
+  WaitCtl wc{w.barrier_polls > 0 ? w.barrier_polls : kBarrierSpinLimit, w.withhold_first_arrival};
+  void* args[] = {&Acopy, &val, &minv, &V, &part_a, &part_b, &keep, &wc};
   return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(C::kThreads), args, C::kSmemBytes, s);
 }
 
@@ -713,7 +722,8 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     if (failed) break;
     cta_reduce<8>(red, sw);
     ++barrier_no;
-    if (!grid_allreduce<8>(red, part + par * 8 * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh)) {
+    if (!grid_allreduce<8>(red, part + par * 8 * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh,
+                           WaitCtl{kBarrierSpinLimit, 0})) {
       failed = true;
       break;
     }

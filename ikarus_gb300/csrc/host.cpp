@@ -217,6 +217,10 @@ static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc) {
   } else {
     f->launch_coloured(args, ikr::kWantK, a->fp32);
   }
+  if (a->me_idx.n) {  // AssemblerManipulator matrix hooks run after the Dirichlet treatment
+    ikr::launch_add_entries(a->values(), a->fp32, a->me_idx.p, a->me_val.p, (int)a->me_idx.n, f->stream);
+    count(1);
+  }
   a->matrix_dbc = dbc;
   f->check_status();
 }
@@ -595,6 +599,34 @@ int ikr_assembler_add_point_loads(ikr_asm a, int32_t n, const int32_t* dofs, con
     CK(cudaStreamSynchronize(a->fes->stream));
   });
 }
+int ikr_assembler_add_matrix_entries(ikr_asm a, int32_t n, const int32_t* rows, const int32_t* cols,
+                                     const double* values) {
+  return guarded([&] {
+    need(a && n >= 0 && (n == 0 || (rows && cols && values)), IKR_ERR_ARG, "invalid matrix entries");
+    if (!a->nb) a->build_pattern();
+    for (int k = 0; k < n; ++k)
+      need(rows[k] >= 0 && rows[k] < a->n && cols[k] >= 0 && cols[k] < a->n, IKR_ERR_ARG,
+           "matrix entry index out of range");
+    auto value_index = [&](int32_t r, int32_t c) -> int64_t {
+      const int rn = r / 3, cn = c / 3;
+      const int32_t* b = a->col_h.data() + a->row_ptr_h[rn];
+      const int32_t* e = a->col_h.data() + a->row_ptr_h[rn + 1];
+      const int32_t* it = std::lower_bound(b, e, cn);
+      if (it == e || *it != cn) return -1;
+      return ikr::block_entry(a->block_id(rn, a->row_ptr_h[rn] + (it - b)), 3 * (r % 3) + c % 3);
+    };
+    for (int k = 0; k < n; ++k)
+      if (value_index(rows[k], cols[k]) < 0)
+        fail(IKR_ERR_ARG, "matrix entry (%d, %d) is not in the sparsity pattern", rows[k], cols[k]);
+    for (int k = 0; k < n; ++k) a->me_h[{rows[k], cols[k]}] += values[k];
+    std::vector<int64_t> idx;
+    std::vector<double> val;
+    for (auto& kv : a->me_h) idx.push_back(value_index(kv.first.first, kv.first.second)), val.push_back(kv.second);
+    a->me_idx.upload(idx.data(), idx.size(), a->fes->stream);
+    a->me_val.upload(val.data(), val.size(), a->fes->stream);
+    CK(cudaStreamSynchronize(a->fes->stream));
+  });
+}
 int ikr_assembler_bind(ikr_asm a, ikr_req r, int32_t dbc) {
   return guarded([&] {
     need(a && r && r->fes == a->fes, IKR_ERR_ARG, "requirement of another element set");
@@ -740,11 +772,16 @@ int ikr_assembler_block_pattern(ikr_asm a, int32_t* n_rows, int64_t* n_blocks, i
 int ikr_linear_solver_create(ikr_ls* out, int32_t tag) {
   return guarded([&] {
     need(out, IKR_ERR_ARG, "null argument");
-    need(tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI || tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT ||
+    need((tag >= IKR_SOLVER_NONE && tag <= IKR_SOLVER_D_LDLT) || tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI ||
              tag == IKR_SOLVER_GPU_PCG_BATCHED,
-         IKR_ERR_NOT_IMPLEMENTED, "this SolverTypeTag has no device implementation");
+         IKR_ERR_NOT_IMPLEMENTED, "unknown SolverTypeTag");
+    need(tag != IKR_SOLVER_SD_SUPER_LU, IKR_ERR_NOT_IMPLEMENTED, "sd_SuperLU: Not implemented yet.");
     auto l = std::make_unique<ikr_ls_s>();
     l->tag = tag;
+    l->point_jacobi = tag >= IKR_SOLVER_SI_CONJUGATE_GRADIENT && tag <= IKR_SOLVER_SI_BICGSTAB;
+    l->direct = tag >= IKR_SOLVER_SD_SIMPLICIAL_LLT && tag <= IKR_SOLVER_SD_UMFPACK_LU;
+    l->dense = tag >= IKR_SOLVER_D_PARTIAL_PIV_LU && tag <= IKR_SOLVER_D_LDLT;
+    if (l->direct) l->rtol = IKR_DIRECT_SOLVE_RTOL;
     *out = l.release();
   });
 }
@@ -765,12 +802,19 @@ int ikr_linear_solver_set_fp64_outer(ikr_ls ls, int32_t restart, double inner_rt
     need(restart >= 0 && restart < ikr::kKrylovMaxBasis, IKR_ERR_ARG, "restart length must be in [0, 63]");
     need(inner_rtol > 0 && inner_rtol < 1 && inner_max_iter > 0 && outer_max_iter > 0, IKR_ERR_ARG,
          "invalid inner tolerance or iteration limits");
-    need(ls->tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI || ls->tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT,
+    need(ls->tag != IKR_SOLVER_GPU_PCG_BATCHED && !ls->dense && ls->tag != IKR_SOLVER_NONE,
          IKR_ERR_NOT_IMPLEMENTED, "the FP64 outer solve wraps the single-system CG solvers");
     ls->outer_m = restart;
     ls->inner_rtol = inner_rtol;
     ls->inner_max_iter = inner_max_iter;
     ls->outer_max_iter = outer_max_iter;
+  });
+}
+int ikr_linear_solver_set_wait_test(ikr_ls ls, int32_t barrier_polls, int32_t withhold_first_arrival) {
+  return guarded([&] {
+    need(ls && barrier_polls >= 0, IKR_ERR_ARG, "invalid arguments");
+    ls->w.barrier_polls = barrier_polls;
+    ls->w.withhold_first_arrival = withhold_first_arrival ? 1 : 0;
   });
 }
 int ikr_linear_solver_outer_info(ikr_ls ls, int32_t* outer_iterations, int32_t* cycles) {
@@ -911,7 +955,7 @@ int ikr_linear_solver_set_coarse_space(ikr_ls ls, int32_t n_slabs) {
   return guarded([&] {
     need(ls, IKR_ERR_ARG, "null argument");
     need(n_slabs >= 0 && 6 * n_slabs <= ikr::kCoarseMaxDofs, IKR_ERR_ARG, "coarse slabs must be in [0, 128]");
-    need(n_slabs == 0 || ls->tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI, IKR_ERR_NOT_IMPLEMENTED,
+    need(n_slabs == 0 || ls->tag == IKR_SOLVER_GPU_PCG_BLOCK_JACOBI || ls->direct, IKR_ERR_NOT_IMPLEMENTED,
          "the coarse correction is a preconditioner of the block-Jacobi GPU CG");
     if (n_slabs != ls->coarse_req) {
       ls->coarse_req = n_slabs;
@@ -1401,7 +1445,7 @@ int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_in
     need(lc && r, IKR_ERR_ARG, "null argument");
     const double step = (lc->t1 - lc->t0) / lc->steps;
     ikr_control_info ci{};
-    ikr_control_state cs{r, 0, 0.0, r->lambda};
+    ikr_control_state cs{r, -1, 0.0, r->lambda, 0, "Load Control Method"};  // loadcontrol.hh:63
     auto notify = [&](int msg) {
       cs.load_factor = r->lambda;
       for (auto& o : lc->obs) o.cb(msg, &cs, o.user);
@@ -1411,6 +1455,7 @@ int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_in
       ci.n_solver_infos++;
       ci.total_iterations += ni.iterations;
       ci.total_linear_iterations += ni.linear_iterations;
+      cs.total_iterations = ci.total_iterations;
       notify(IKR_CONTROL_SOLUTION_CHANGED);
       notify(IKR_STEP_ENDED);
     };

@@ -272,6 +272,11 @@ struct ikr_asm_s {
   DBuf<int32_t> pl_dof;
   DBuf<double> pl_val;
   std::map<int32_t, double> pl_h;
+  // manipulator matrix entries K(row, col) += value after every matrix assembly: (row, col) -> value, and their
+  // value indices in the sliced-ELL storage
+  std::map<std::pair<int32_t, int32_t>, double> me_h;
+  DBuf<int64_t> me_idx;
+  DBuf<double> me_val;
   DBuf<double> norm_part, norm_out;
   ikr_req bound_req = nullptr;
   int bound_dbc = IKR_DBC_FULL;
@@ -355,6 +360,9 @@ int64_t fgmres_solve(ikr_ls ls, ikr_asm a, const double* b, double* x, double et
 
 struct ikr_ls_s {
   int tag = IKR_SOLVER_GPU_PCG_BLOCK_JACOBI;
+  // what the reference tag runs (include/ikarus_gb300.h): point-Jacobi CG (Eigen's iterative solvers), a
+  // direct-accuracy FP64 solve (sparse direct tags), nothing on a sparse tangent (dense tags)
+  bool point_jacobi = false, direct = false, dense = false;
   double rtol = 1e-10;
   int max_iter = 100000;
   ikr_asm asm_ = nullptr;
@@ -545,8 +553,12 @@ struct ikr_ls_s {
   }
 
   void factorize(ikr_asm a) {
+    if (tag == IKR_SOLVER_NONE) fail(IKR_ERR_INVALID_STATE, "SolverTypeTag::none has no linear solver");
+    if (dense) fail(IKR_ERR_NOT_IMPLEMENTED, "This solver does not support solving with sparse matrices.");
+    if (direct && a->fp32 && outer_m == 0)
+      fail(IKR_ERR_NOT_IMPLEMENTED, "a direct-accuracy solve of an FP32 tangent needs the FP64 outer solve");
     setup(a);
-    ikr::launch_block_jacobi(a->bsr(), fp32, w.minv, tag == IKR_SOLVER_SI_CONJUGATE_GRADIENT, a->fes->stream);
+    ikr::launch_block_jacobi(a->bsr(), fp32, w.minv, point_jacobi, a->fes->stream);
     count(1);
     factorized = true;
     if (tag != IKR_SOLVER_GPU_PCG_BATCHED && tuned_for != a) tune(a);
@@ -874,6 +886,7 @@ struct ikr_ls_s {
     if (profile) CK(cudaEventRecord(tev[0], s));
     CK(ikr::launch_pcg_persistent(A, w, w.spmv_kind - first_persistent_kind(), s));
     count(1);
+    w.withhold_first_arrival = 0;  // the test switch acts on one launch
     if (profile) CK(cudaEventRecord(tev[1], s));
     CK(cudaMemcpyAsync(scal_h, scal.p, sizeof(double) * ikr::kNScal, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -968,11 +981,13 @@ struct ikr_ls_s {
   int64_t solve2(ikr_asm a, const double* b0, const double* b1, double* x0, double* x1, double rt, int maxit,
                  int refinements, double rt1 = -1.0) {
     if (rt1 < 0.0) rt1 = rt;
+    if (direct) rt = std::min(rt, rtol), rt1 = std::min(rt1, rtol);
     if (!factorized || asm_ != a) fail(IKR_ERR_INVALID_STATE, "linear solver not factorized for this assembler");
     const ikr::Bsr A = a->bsr();
     // FP64 CG iterations are bound by GB300's FP64 pipe, not by the matrix stream: two right-hand sides cost
-    // twice the time in one launch as well, so only the FP32 tangent runs them together
-    bool two = multi_rhs && fp32 && persistent() && refinements <= 0;
+    // twice the time in one launch as well, so only the FP32 tangent runs them together (and only without the
+    // FP64 outer solve, whose operator is the FP64 tangent)
+    bool two = multi_rhs && fp32 && persistent() && refinements <= 0 && outer_m == 0;
     if (two) {
       setup2();
       w2.minv = w.minv, w2.keep_g = w.keep_g, w2.spmv_kind = w.spmv_kind;
@@ -1020,6 +1035,7 @@ struct ikr_ls_s {
   // x = K^{-1} b with optional FP64 iterative refinement around the (possibly FP32) CG; with the FP64 outer
   // Krylov solve on (outer_m > 0) an FP32 tangent is solved against its FP64 twin instead
   int64_t solve(ikr_asm a, const double* b, double* x, double rt, int maxit, int refinements) {
+    if (direct) rt = std::min(rt, rtol);  // a direct solver's accuracy, whatever the Newton's linear tolerance
     if (outer_m > 0 && a->fp32) return fgmres_solve(this, a, b, x, rt);
     int64_t its = solve_device(a, b, x, rt, maxit);
     if (refinements <= 0) return its;
@@ -1033,6 +1049,11 @@ struct ikr_ls_s {
     }
     return its;
   }
+};
+
+// listeners owned by the broadcaster they are subscribed to (operators.cpp: the reference's loggers)
+struct ListenerBase {
+  virtual ~ListenerBase() = default;
 };
 
 struct Observer {
@@ -1049,6 +1070,7 @@ struct ikr_nr_s {
   ikr_ls ls = nullptr;
   ikr_nr_settings st{};
   std::vector<Observer> obs;
+  std::vector<std::unique_ptr<ListenerBase>> listeners;
   bool fe_state = false;
   DBuf<double> corr, rhs;
   DBuf<double> nrm_part, nrm_out;
@@ -1080,6 +1102,7 @@ struct ikr_lc_s {
   int steps = 1;
   double t0 = 0, t1 = 1;
   std::vector<ControlObserver> obs;
+  std::vector<std::unique_ptr<ListenerBase>> listeners;
   // Newton predictor of each load step (the reference only increments the load factor,
   // loadcontrol.inl:54-57): 0 = none, 1 = previous increment, 2 = learned, which falls back to the previous
   // increment when its FP64 residual is not smaller (predictor.cpp).  `record` appends each converged
@@ -1119,6 +1142,8 @@ void assemble_matrix(ikr_asm a, ikr_req r, int dbc);
 void update_state(ikr_fes f, ikr_req r, const double* corr_dev);
 // syncParameterAndGlobalSolution: u = lambda * rate where that value is nonzero
 void idbc_sync(ikr_asm a, ikr_req r);
+// ControlLogger (operators.cpp): a listener and the control observer that feeds it
+std::unique_ptr<ListenerBase> make_control_logger(ikr_log_sink sink, void* user, ControlObserver* obs);
 // Newton-Raphson solve (newtonraphson.hh:193-257); ref_norm > 0 replaces the initial residual norm as the
 // reference of the relative convergence test
 void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double ref_norm = 0.0);

@@ -115,6 +115,8 @@ void launch_slot_map(const int32_t* conn, int n_elems, const int32_t* row_ptr, c
                      const int32_t* slice_off, int32_t* slot, int32_t* diag, int n_nodes, cudaStream_t s);
 void launch_bsr_reset(void* val, bool fp32, int64_t n_padded, const int32_t* diag, const uint8_t* node_fixed,
                       int n_nodes, cudaStream_t s);
+// val[idx[k]] += v[k] for n unique value indices (the assembler manipulator's matrix entries)
+void launch_add_entries(void* val, bool fp32, const int64_t* idx, const double* v, int n, cudaStream_t s);
 void launch_vector_finish(double* R, const uint8_t* node_fixed, int n_nodes, const int32_t* pl_dof,
                           const double* pl_val, int n_pl, double load_factor, cudaStream_t s);
 void launch_norm2(const double* x, int64_t n, double* partials, double* out, cudaStream_t s);
@@ -170,6 +172,10 @@ struct PcgWork {
   // 1: a coarse correction (coarse.cu) follows the init and update kernels, which then leave r.D^-1 r in kRzF
   // and let it set r.z and beta
   int coarse = 0;
+  // persistent CG: polls of a grid barrier before it gives up (0: the default), and a test switch with which CTA 0
+  // withholds its first barrier arrival (every CTA's first wait then runs out and the solve reports the timeout)
+  int barrier_polls = 0;
+  int withhold_first_arrival = 0;
 };
 void launch_block_jacobi(const Bsr& A, bool fp32, void* minv, bool point_jacobi, cudaStream_t s);
 void launch_pcg_init(const Bsr& A, PcgWork& w, const double* b, double rtol, int max_iter, cudaStream_t s);

@@ -7,6 +7,8 @@
 // DisplacementControl (:295-368); step-size adaptation AdaptiveStepSizing::IterationBased
 // (adaptivestepsizing.hh:36-57).  Vectors stay on the device; only the scalars of the bordering (dot products)
 // come back to the host.
+#include <string>
+
 #include "host_internal.h"
 
 using namespace ikr_host;
@@ -19,6 +21,8 @@ struct ikr_pf_s {
   std::vector<int32_t> controlled;
   int adaptive = 0, target_iterations = 0;
   std::vector<ControlObserver> obs;
+  std::vector<std::unique_ptr<ListenerBase>> listeners;
+  std::string name;  // PathFollowing::name (pathfollowing.hh:175)
   // ArcLength's private state (pathfollowingfunctions.hh:200-202)
   double psi = 0;
   bool computed = false;
@@ -411,6 +415,14 @@ int ikr_path_following_subscribe(ikr_pf pf, ikr_control_observer cb, void* user)
     pf->obs.push_back({cb, user});
   });
 }
+int ikr_path_following_subscribe_logger(ikr_pf pf, ikr_log_sink sink, void* user) {
+  return guarded([&] {
+    need(pf, IKR_ERR_ARG, "null argument");
+    ControlObserver o{};
+    pf->listeners.push_back(make_control_logger(sink, user, &o));
+    pf->obs.push_back(o);
+  });
+}
 int ikr_path_following_subsidiary_args(ikr_pf pf, double* out6) {
   return guarded([&] {
     need(pf && out6, IKR_ERR_ARG, "null argument");
@@ -483,7 +495,9 @@ int ikr_path_following_run(ikr_pf pf, ikr_req r, ikr_control_info* info, ikr_nr_
       CK(cudaStreamSynchronize(s));
     }
     ikr_control_info ci{};
-    ikr_control_state cs{r, -1, 0.0, r->lambda};
+    static const char* kNames[] = {"Arc length", "Load Control", "Displacement Control"};  // pathfollowingfunctions.hh
+    pf->name = std::string("Path following with ") + kNames[pf->kind];
+    ikr_control_state cs{r, -1, 0.0, r->lambda, 0, pf->name.c_str()};
     auto notify = [&](int msg) {
       cs.load_factor = r->lambda;
       for (auto& o : pf->obs) o.cb(msg, &cs, o.user);
@@ -494,6 +508,7 @@ int ikr_path_following_run(ikr_pf pf, ikr_req r, ikr_control_info* info, ikr_nr_
       ci.n_solver_infos++;
       ci.total_iterations += ni.iterations;
       ci.total_linear_iterations += ni.linear_iterations;
+      cs.total_iterations = ci.total_iterations;
       notify(IKR_CONTROL_SOLUTION_CHANGED);
       notify(IKR_STEP_ENDED);
     };

@@ -315,6 +315,19 @@ void launch_bsr_reset(void* val, bool fp32, int64_t n_padded, const int32_t* dia
   if (fp32) unit_diag_kernel<float><<<blocks_for(n_nodes, 256), 256, 0, s>>>((float*)val, diag, node_fixed, n_nodes);
   else unit_diag_kernel<double><<<blocks_for(n_nodes, 256), 256, 0, s>>>((double*)val, diag, node_fixed, n_nodes);
 }
+// AssemblerManipulator matrix entries: val[idx[k]] += v[k] (indices unique, so no two threads touch one value)
+template <typename T>
+__global__ void add_entries_kernel(T* __restrict__ val, const int64_t* __restrict__ idx, const double* __restrict__ v,
+                                   int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) val[idx[k]] = T(double(val[idx[k]]) + v[k]);
+}
+void launch_add_entries(void* val, bool fp32, const int64_t* idx, const double* v, int n, cudaStream_t s) {
+  if (n <= 0) return;
+  if (fp32) add_entries_kernel<float><<<blocks_for(n, 128), 128, 0, s>>>((float*)val, idx, v, n);
+  else add_entries_kernel<double><<<blocks_for(n, 128), 128, 0, s>>>((double*)val, idx, v, n);
+}
+
 void launch_vector_finish(double* R, const uint8_t* node_fixed, int n_nodes, const int32_t* pl_dof,
                           const double* pl_val, int n_pl, double load_factor, cudaStream_t s) {
   (void)node_fixed;

@@ -46,15 +46,45 @@ enum { IKR_SCALAR_NO_AFFORDANCE = 0, IKR_SCALAR_MECHANICAL_POTENTIAL_ENERGY = 1 
  * EAS::DisplacementGradient, EAS::DisplacementGradientTransposed (strainenhancements/easfunctions/) */
 enum { IKR_EAS_NONE = 0, IKR_EAS_GREEN_LAGRANGE = 1, IKR_EAS_DISPLACEMENT_GRADIENT = 2,
        IKR_EAS_DISPLACEMENT_GRADIENT_TRANSPOSED = 3 };
-/* SolverTypeTag (ikarus/solver/linearsolver/linearsolver.hh:28-31) keeps its values; the device solvers
- * of this library are added after it.  si_ConjugateGradient maps to device CG with point-Jacobi
- * preconditioning (Eigen's default diagonal preconditioner); the sparse direct tags are not provided. */
+/* SolverTypeTag (ikarus/solver/linearsolver/linearsolver.hh:28-31): all 19 names with the reference's values, then
+ * the device solvers of this library.  What each reference tag runs on the device (tangents of this path are
+ * symmetric, and nonsingular wherever the reference's solvers succeed, so every sparse tag has the same solution):
+ *   si_ConjugateGradient, si_LeastSquaresConjugateGradient, si_BiCGSTAB (Eigen's iterative solvers with their
+ *     default diagonal preconditioner): device CG with point-Jacobi preconditioning, tolerance as set (1e-10);
+ *   sd_SimplicialLLT, sd_SimplicialLDLT (the reference's default SPD solver, controlroutines/common.hh:39-54),
+ *     sd_SparseLU, sd_SparseQR, sd_CholmodSupernodalLLT, sd_UmfPackLU (the cantilever goldens' solver): a
+ *     direct-accuracy solve -- FP64 block-Jacobi CG to ||r|| <= 1e-13 ||b|| (or the tolerance set, whichever is
+ *     tighter, whatever the Newton's linear tolerance); an FP32 tangent needs the FP64 outer solve
+ *     (ikr_linear_solver_set_fp64_outer), else IKR_ERR_NOT_IMPLEMENTED;
+ *   sd_SuperLU: IKR_ERR_NOT_IMPLEMENTED at creation (the reference throws there, linearsolver.cpp:51-53);
+ *   d_* (dense solvers): created, but factorize / compute on the sparse assembled tangent return
+ *     IKR_ERR_NOT_IMPLEMENTED (the reference throws "does not support solving with sparse matrices",
+ *     linearsolver.hh:139-144);
+ *   none: created; factorize returns IKR_ERR_INVALID_STATE (no solver behind it). */
 enum {
   IKR_SOLVER_NONE = 0,
   IKR_SOLVER_SI_CONJUGATE_GRADIENT = 1,
+  IKR_SOLVER_SI_LEAST_SQUARES_CONJUGATE_GRADIENT = 2,
+  IKR_SOLVER_SI_BICGSTAB = 3,
+  IKR_SOLVER_SD_SIMPLICIAL_LLT = 4,
+  IKR_SOLVER_SD_SIMPLICIAL_LDLT = 5,
+  IKR_SOLVER_SD_SPARSE_LU = 6,
+  IKR_SOLVER_SD_SPARSE_QR = 7,
+  IKR_SOLVER_SD_CHOLMOD_SUPERNODAL_LLT = 8,
+  IKR_SOLVER_SD_UMFPACK_LU = 9,
+  IKR_SOLVER_SD_SUPER_LU = 10,
+  IKR_SOLVER_D_PARTIAL_PIV_LU = 11,
+  IKR_SOLVER_D_FULL_PIV_LU = 12,
+  IKR_SOLVER_D_HOUSEHOLDER_QR = 13,
+  IKR_SOLVER_D_COL_PIV_HOUSEHOLDER_QR = 14,
+  IKR_SOLVER_D_FULL_PIV_HOUSEHOLDER_QR = 15,
+  IKR_SOLVER_D_COMPLETE_ORTHOGONAL_DECOMPOSITION = 16,
+  IKR_SOLVER_D_LLT = 17,
+  IKR_SOLVER_D_LDLT = 18,
   IKR_SOLVER_GPU_PCG_BLOCK_JACOBI = 100,  /* FP64 or FP32 CG, 3x3 block-Jacobi, precision of the assembled K */
   IKR_SOLVER_GPU_PCG_BATCHED = 101,       /* one block-Jacobi CG per instance, all in one launch (see below) */
 };
+#define IKR_DIRECT_SOLVE_RTOL 1e-13
 /* precision of the assembled tangent */
 enum { IKR_PRECISION_FP64 = 0, IKR_PRECISION_FP32 = 1 };
 /* messages, ikarus/utils/broadcaster/broadcastermessages.hh:18,23-24 (spelling of the reference kept) */
@@ -146,6 +176,12 @@ int ikr_assembler_destroy(ikr_asm a);
 /* AssemblerManipulator vector hook (assemblermanipulatorbuildingblocks.hh:94-121) of the form
  * vec[dof] += load_factor * value, applied after the Dirichlet treatment. */
 int ikr_assembler_add_point_loads(ikr_asm a, int32_t n, const int32_t* dofs, const double* values);
+/* AssemblerManipulator matrix hook (assemblermanipulatorbuildingblocks.hh:155-183) in the form of the reference's
+ * springs (testassembler.cpp:212-219): after every matrix assembly and its Dirichlet treatment K(rows[k], cols[k])
+ * += values[k] (full-system dof indices inside the sparsity pattern; repeated calls accumulate).  The Reduced
+ * option keeps the entries of free rows and columns only. */
+int ikr_assembler_add_matrix_entries(ikr_asm a, int32_t n, const int32_t* rows, const int32_t* cols,
+                                     const double* values);
 int ikr_assembler_bind(ikr_asm a, ikr_req req, int32_t dbc_option);                    /* interface.hh:150-175 */
 int ikr_assembler_size(ikr_asm a, int32_t* size);
 int ikr_assembler_reduced_size(ikr_asm a, int32_t* size);
@@ -188,6 +224,12 @@ int ikr_linear_solver_set_tolerance(ikr_ls ls, double rtol, int32_t max_iter);
 int ikr_linear_solver_set_fp64_outer(ikr_ls ls, int32_t restart, double inner_rtol, int32_t inner_max_iter,
                                      int32_t outer_max_iter);
 int ikr_linear_solver_outer_info(ikr_ls ls, int32_t* outer_iterations, int32_t* cycles);
+/* no reference counterpart; for tests of the bounded device waits: barrier_polls = polls of a grid barrier of the
+ * persistent CG before it gives up (0 = the default, 2^24); withhold_first_arrival != 0 makes CTA 0 of the next
+ * persistent CG launch skip its arrival at the first grid barrier, so every CTA's first wait runs out after
+ * barrier_polls polls: that solve returns IKR_ERR_TIMEOUT (after its in-flight copies have been drained), the switch
+ * clears itself, and the handle solves normally afterwards.  No fault and no unbounded wait are involved. */
+int ikr_linear_solver_set_wait_test(ikr_ls ls, int32_t barrier_polls, int32_t withhold_first_arrival);
 int ikr_linear_solver_analyze_pattern(ikr_ls ls, ikr_asm a);
 int ikr_linear_solver_factorize(ikr_ls ls, ikr_asm a);       /* builds the preconditioner from the device K */
 /* solve(x, b) with host arrays of size() (Full option system) */
@@ -267,6 +309,30 @@ int ikr_fes_stream(ikr_fes fes, void** stream);
 int ikr_linear_solver_solve_noalloc(ikr_asm a, const double* b_device, double* x_device, double rtol,
                                     int32_t max_iter, int32_t* iterations);
 
+/* ---- assembled scalar and NonLinearOperator ----------------------------------------------------------------
+ * scalar(req, affordance) (simpleassemblers.inl, scalarImpl): the sum over all elements, in element order, of
+ * calculateScalar (mechanical potential energy: stored energy minus the work of the dead loads); EAS element sets
+ * return IKR_ERR_NOT_IMPLEMENTED as the reference's EAS skill throws (enhancedassumedstrains.hh:305-309). */
+int ikr_assembler_scalar(ikr_asm a, ikr_req req, int32_t affordance, double* out);
+/* DifferentiableFunctionFactory::op(assembler, affordances, dbcOption) (utils/differentiablefunctionfactory.hh:
+ * 24-51): the non-linear operator over the assembler.  With a scalar affordance (not IKR_SCALAR_NO_AFFORDANCE) the
+ * function is the energy, its derivative the force vector and its second derivative the tangent; otherwise the
+ * function is the force vector and its derivative the tangent.  evaluate(order): 0 = f(req), 1 = derivative(f)(req),
+ * 2 = derivative(derivative(f))(req); kind returns 0 scalar, 1 vector, 2 matrix.  A scalar or vector result is
+ * copied to out (1, size() or reducedSize() doubles; out may be NULL); a matrix stays in the assembler (the
+ * reference returns a reference to the assembler's storage): export it with ikr_assembler_export_csc.  An order
+ * above the operator's is IKR_ERR_ARG. */
+typedef struct ikr_nlo_s* ikr_nlo;
+int ikr_nonlinear_operator_create(ikr_nlo* out, ikr_asm a, int32_t scalar_affordance, int32_t vector_affordance,
+                                  int32_t matrix_affordance, int32_t dbc_option);
+int ikr_nonlinear_operator_destroy(ikr_nlo f);
+int ikr_nonlinear_operator_evaluate(ikr_nlo f, int32_t order, ikr_req req, double* out, int32_t* kind);
+
+/* ---- listeners: NonLinearSolverLogger (utils/listener/nonlinearsolverlogger.hh:22-95) and ControlLogger
+ * (controllogger.hh:22-66, controllogger.cpp) write the reference's lines (spdlog's info level) through sink, or to
+ * stdout as "[info] <line>" when sink is NULL.  The logger lives as long as the object it is subscribed to. ---- */
+typedef void (*ikr_log_sink)(const char* line, void* user);
+
 /* ---- NewtonRaphson (newtonraphson.hh:27-303, nonlinearsolverfactory.hh:110-122) -------------------------- */
 typedef struct ikr_nr_settings {
   double tol;          /* NRSettings::tol (default 1e-8) */
@@ -308,6 +374,15 @@ int ikr_newton_subscribe(ikr_nr nr, ikr_nr_observer cb, void* user);
 int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on);
 /* solve(x, stepSize) (newtonraphson.hh:193-257) */
 int ikr_newton_solve(ikr_nr nr, ikr_req req, double step_size, ikr_nr_info* info);
+/* residual() / jacobian() / updateFunction() (newtonraphson.hh:260-287): the solver's residual function (force
+ * vector with the Full Dirichlet treatment, out: size() doubles, may be NULL), its derivative (the tangent, kept in
+ * the assembler) and the update x += dx of the requirement's displacement (dx: size() host doubles; inhomogeneous
+ * Dirichlet values re-imposed afterwards, nonlinearsolverfactory.hh:45-52). */
+int ikr_newton_residual(ikr_nr nr, ikr_req req, double* out);
+int ikr_newton_jacobian(ikr_nr nr, ikr_req req);
+int ikr_newton_update(ikr_nr nr, ikr_req req, const double* correction);
+/* NonLinearSolverLogger::subscribeTo(nr) */
+int ikr_newton_subscribe_logger(ikr_nr nr, ikr_log_sink sink, void* user);
 /* per instance (batched solves): Newton iterations, final residual norm and convergence of the last solve
  * (1 converged, 0 not converged, -1 taken out after its elements inverted, det C <= 0 -- the reference aborts
  * there; here the other instances go on and the solve succeeds when all instances not taken out converge).
@@ -317,9 +392,11 @@ int ikr_newton_instance_info(ikr_nr nr, int32_t* iterations, double* residual_no
 /* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
 typedef struct ikr_control_state {   /* ControlRoutineState (controlroutinestate.hh:21-31) */
   ikr_req domain;
-  int32_t load_step;
+  int32_t load_step;                 /* -1 during the initial equilibrium solve, as the reference's state */
   double step_size;
   double load_factor;
+  int32_t total_iterations;          /* ControlInformation::totalIterations so far */
+  const char* name;                  /* ControlInformation::name ("Load Control Method", "Path following with ...") */
 } ikr_control_state;
 typedef void (*ikr_control_observer)(int32_t message, const ikr_control_state* state, void* user);
 typedef struct ikr_control_info {    /* ControlInformation (controlinfos.hh:22-32) */
@@ -333,6 +410,8 @@ typedef struct ikr_control_info {    /* ControlInformation (controlinfos.hh:22-3
 int ikr_load_control_create(ikr_lc* out, ikr_nr nr, int32_t load_steps, double t_begin, double t_end);
 int ikr_load_control_destroy(ikr_lc lc);
 int ikr_load_control_subscribe(ikr_lc lc, ikr_control_observer cb, void* user);
+/* ControlLogger::subscribeTo(lc) */
+int ikr_load_control_subscribe_logger(ikr_lc lc, ikr_log_sink sink, void* user);
 /* run(req): info plus per-solve NonLinearSolverInformation (capacity entries; index 0 = the initial
  * equilibrium solve at the starting load factor). */
 int ikr_load_control_run(ikr_lc lc, ikr_req req, ikr_control_info* info, ikr_nr_info* solver_infos,
@@ -357,6 +436,8 @@ int ikr_path_following_destroy(ikr_pf pf);
  * target 0 is IKR_ERR_INVALID_STATE as in setTargetIterations) */
 int ikr_path_following_set_adaptive_step_sizing(ikr_pf pf, int32_t kind, int32_t target_iterations);
 int ikr_path_following_subscribe(ikr_pf pf, ikr_control_observer cb, void* user);
+/* ControlLogger::subscribeTo(pf) */
+int ikr_path_following_subscribe_logger(ikr_pf pf, ikr_log_sink sink, void* user);
 /* run(req): per-solve NonLinearSolverInformation, steps + 1 entries (the solve at load step -1 first).  Load-control
  * and displacement-control subsidiary functions with inhomogeneous Dirichlet values: IKR_ERR_NOT_IMPLEMENTED (the
  * reference rejects them at compile time, pathfollowingfunctions.hh:22-26). */

@@ -54,7 +54,31 @@ enum class VectorAffordance : int32_t { noAffordance = 0, forces = IKR_VEC_FORCE
 enum class MatrixAffordance : int32_t { noAffordance = 0, stiffness = IKR_MAT_STIFFNESS };
 enum class ScalarAffordance : int32_t { noAffordance = 0, mechanicalPotentialEnergy = 1 };
 enum class EAS : int32_t { none = 0, GreenLagrangeStrain = 1, DisplacementGradient = 2, DisplacementGradientTransposed = 3 };
-enum class SolverTypeTag : int32_t { none = 0, si_ConjugateGradient = 1, gpu_PCG_BlockJacobi = 100 };
+// the reference's 19 tags with their values (linearsolver.hh:28-31), then the device solvers of this library; what
+// each runs on the device is listed in ikarus_gb300.h
+enum class SolverTypeTag : int32_t {
+  none = IKR_SOLVER_NONE,
+  si_ConjugateGradient = IKR_SOLVER_SI_CONJUGATE_GRADIENT,
+  si_LeastSquaresConjugateGradient = IKR_SOLVER_SI_LEAST_SQUARES_CONJUGATE_GRADIENT,
+  si_BiCGSTAB = IKR_SOLVER_SI_BICGSTAB,
+  sd_SimplicialLLT = IKR_SOLVER_SD_SIMPLICIAL_LLT,
+  sd_SimplicialLDLT = IKR_SOLVER_SD_SIMPLICIAL_LDLT,
+  sd_SparseLU = IKR_SOLVER_SD_SPARSE_LU,
+  sd_SparseQR = IKR_SOLVER_SD_SPARSE_QR,
+  sd_CholmodSupernodalLLT = IKR_SOLVER_SD_CHOLMOD_SUPERNODAL_LLT,
+  sd_UmfPackLU = IKR_SOLVER_SD_UMFPACK_LU,
+  sd_SuperLU = IKR_SOLVER_SD_SUPER_LU,
+  d_PartialPivLU = IKR_SOLVER_D_PARTIAL_PIV_LU,
+  d_FullPivLU = IKR_SOLVER_D_FULL_PIV_LU,
+  d_HouseholderQR = IKR_SOLVER_D_HOUSEHOLDER_QR,
+  d_ColPivHouseholderQR = IKR_SOLVER_D_COL_PIV_HOUSEHOLDER_QR,
+  d_FullPivHouseholderQR = IKR_SOLVER_D_FULL_PIV_HOUSEHOLDER_QR,
+  d_CompleteOrthogonalDecomposition = IKR_SOLVER_D_COMPLETE_ORTHOGONAL_DECOMPOSITION,
+  d_LLT = IKR_SOLVER_D_LLT,
+  d_LDLT = IKR_SOLVER_D_LDLT,
+  gpu_PCG_BlockJacobi = IKR_SOLVER_GPU_PCG_BLOCK_JACOBI,
+  gpu_PCG_Batched = IKR_SOLVER_GPU_PCG_BATCHED
+};
 enum class Precision : int32_t { fp64 = IKR_PRECISION_FP64, fp32 = IKR_PRECISION_FP32 };
 // material law of the elements (NeoHooke / StVenantKirchhoff with lambda, mu; BlatzKo with mu only)
 enum class Material : int32_t {

@@ -14,7 +14,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_FUSED_PATH = os.path.join(_HERE, "_build", "liboracle_fused.so")
 _lib = None
+_lib_fused = None
 
 EAS_NONE, EAS_GL, EAS_H, EAS_HT = 0, 1, 2, 3
 DBC_RAW, DBC_REDUCED, DBC_FULL = 0, 1, 2
@@ -34,47 +36,59 @@ def build():
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
 
 
-def lib():
-    global _lib
+def lib(fused=False):
+    """The oracle library; fused=True: the same restatement compiled with multiply-adds contracted to fused
+    multiply-adds where the target has them (a second valid FP64 evaluation, for FP64 floors)."""
+    global _lib, _lib_fused
+    if fused:
+        if _lib_fused is None:
+            if not os.path.exists(_FUSED_PATH):
+                build()
+            _lib_fused = _declare(C.CDLL(_FUSED_PATH))
+        return _lib_fused
     if _lib is None:
         if not os.path.exists(_LIB_PATH):
             build()
-        L = C.CDLL(_LIB_PATH)
-        dp, ip, up, lp = (C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint8), C.POINTER(C.c_int64))
-        vp = C.c_void_p
-        L.orc_problem_create.restype = vp
-        L.orc_problem_create.argtypes = [C.c_int, dp, C.c_int, ip, C.c_double, C.c_double, C.c_int, C.c_int]
-        L.orc_problem_destroy.argtypes = [vp]
-        L.orc_set_dirichlet.argtypes = [vp, up]
-        L.orc_add_neumann.argtypes = [vp, C.c_int, ip, ip, dp]
-        L.orc_add_point_loads.argtypes = [vp, C.c_int, ip, dp]
-        L.orc_set_faithful_moduli.argtypes = [vp, C.c_int]
-        L.orc_get_alpha.argtypes = [vp, dp]
-        L.orc_set_alpha.argtypes = [vp, dp]
-        L.orc_element_vector.argtypes = [vp, C.c_int, dp, C.c_double, dp]
-        L.orc_element_matrix.argtypes = [vp, C.c_int, dp, C.c_double, dp]
-        L.orc_element_energy.argtypes = [vp, C.c_int, dp, C.c_double, dp]
-        L.orc_update_state.argtypes = [vp, dp, C.c_double, dp]
-        L.orc_assemble_vector.argtypes = [vp, dp, C.c_double, C.c_int, dp]
-        L.orc_pattern_nnz.restype = C.c_int64
-        L.orc_pattern_nnz.argtypes = [vp, C.c_int]
-        L.orc_reduced_size.argtypes = [vp]
-        L.orc_assemble_matrix_csc.argtypes = [vp, dp, C.c_double, C.c_int, lp, ip, dp]
-        L.orc_set_dirichlet_values.argtypes = [vp, dp]
-        L.orc_set_material.argtypes = [vp, C.c_int]
-        L.orc_calculate_at.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp]
-        L.orc_cg_jacobi_csc.argtypes = [C.c_int, lp, ip, dp, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_int)]
-        L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
-                                       C.c_double, dp, dp, ip, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
-        L.orc_path_following.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int, ip, C.c_int, C.c_double, C.c_int,
-                                         C.c_int, C.c_double, dp, dp, ip, dp, dp, dp, C.POINTER(C.c_int),
-                                         C.POINTER(C.c_int)]
-        L.orc_set_threads.argtypes = [C.c_int]
-        L.orc_load_step.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp, dp]
-        L.orc_path_following_toy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, dp,
-                                             dp, ip, dp, dp, C.POINTER(C.c_int)]
-        _lib = L
+        _lib = _declare(C.CDLL(_LIB_PATH))
     return _lib
+
+
+def _declare(L):
+    dp, ip, up, lp = (C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_uint8), C.POINTER(C.c_int64))
+    vp = C.c_void_p
+    L.orc_problem_create.restype = vp
+    L.orc_problem_create.argtypes = [C.c_int, dp, C.c_int, ip, C.c_double, C.c_double, C.c_int, C.c_int]
+    L.orc_problem_destroy.argtypes = [vp]
+    L.orc_set_dirichlet.argtypes = [vp, up]
+    L.orc_add_neumann.argtypes = [vp, C.c_int, ip, ip, dp]
+    L.orc_add_point_loads.argtypes = [vp, C.c_int, ip, dp]
+    L.orc_set_faithful_moduli.argtypes = [vp, C.c_int]
+    L.orc_get_alpha.argtypes = [vp, dp]
+    L.orc_set_alpha.argtypes = [vp, dp]
+    L.orc_element_vector.argtypes = [vp, C.c_int, dp, C.c_double, dp]
+    L.orc_element_matrix.argtypes = [vp, C.c_int, dp, C.c_double, dp]
+    L.orc_element_energy.argtypes = [vp, C.c_int, dp, C.c_double, dp]
+    L.orc_update_state.argtypes = [vp, dp, C.c_double, dp]
+    L.orc_assemble_vector.argtypes = [vp, dp, C.c_double, C.c_int, dp]
+    L.orc_pattern_nnz.restype = C.c_int64
+    L.orc_pattern_nnz.argtypes = [vp, C.c_int]
+    L.orc_reduced_size.argtypes = [vp]
+    L.orc_assemble_matrix_csc.argtypes = [vp, dp, C.c_double, C.c_int, lp, ip, dp]
+    L.orc_set_dirichlet_values.argtypes = [vp, dp]
+    L.orc_set_material.argtypes = [vp, C.c_int]
+    L.orc_calculate_at.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp]
+    L.orc_cg_jacobi_csc.argtypes = [C.c_int, lp, ip, dp, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_int)]
+    L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
+                                   C.c_double, dp, dp, ip, dp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.orc_path_following.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_int, ip, C.c_int, C.c_double, C.c_int,
+                                     C.c_int, C.c_double, dp, dp, ip, dp, dp, dp, C.POINTER(C.c_int),
+                                     C.POINTER(C.c_int)]
+    L.orc_set_threads.argtypes = [C.c_int]
+    L.orc_constraints_below.argtypes = [vp, ip]
+    L.orc_load_step.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp, dp]
+    L.orc_path_following_toy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, dp,
+                                         dp, ip, dp, dp, C.POINTER(C.c_int)]
+    return L
 
 
 def _p(a, t):
@@ -125,9 +139,10 @@ def path_following_toy(kind=PF_ARC_LENGTH, idbc=False, steps=5, step_size=0.1, t
                 d_steps=ds[: ns.value])
 
 
-def from_problem(p, faithful=False):
-    """Oracle twin of an ``ikarus_gb300.problems.Problem`` definition (plain data, no GPU objects)."""
-    o = OracleProblem(p.mesh.coords, p.mesh.conn, p.lam, p.mu, p.eas if p.n_eas else EAS_NONE, p.n_eas)
+def from_problem(p, faithful=False, fused=False):
+    """Oracle twin of an ``ikarus_gb300.problems.Problem`` definition (plain data, no GPU objects); fused: evaluated
+    by the fused-multiply-add build of the oracle."""
+    o = OracleProblem(p.mesh.coords, p.mesh.conn, p.lam, p.mu, p.eas if p.n_eas else EAS_NONE, p.n_eas, fused=fused)
     o.set_dirichlet(p.fixed)
     if getattr(p, "material", 0):
         o.set_material(p.material)
@@ -143,74 +158,74 @@ def from_problem(p, faithful=False):
 class OracleProblem:
     """One mesh + NeoHooke material + EAS choice, with Dirichlet flags and dead loads."""
 
-    def __init__(self, coords, conn, lam, mu, eas_kind=EAS_NONE, n_alpha=0):
+    def __init__(self, coords, conn, lam, mu, eas_kind=EAS_NONE, n_alpha=0, fused=False):
         self.coords = np.ascontiguousarray(coords, dtype=np.float64)
         self.conn = np.ascontiguousarray(conn, dtype=np.int32)
         self.n_nodes, self.n_elems = self.coords.shape[0], self.conn.shape[0]
         self.n_dofs = 3 * self.n_nodes
         self.n_alpha = n_alpha
-        L = lib()
+        self._L = L = lib(fused)
         self.h = L.orc_problem_create(self.n_nodes, _p(self.coords, C.c_double), self.n_elems,
                                       _p(self.conn, C.c_int32), lam, mu, eas_kind, n_alpha)
         if not self.h:
             raise OracleError(-1, "create")
 
     def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
-            _lib.orc_problem_destroy(self.h)
+        if getattr(self, "h", None) and getattr(self, "_L", None) is not None:
+            self._L.orc_problem_destroy(self.h)
             self.h = None
 
     def set_dirichlet(self, fixed):
         f = np.ascontiguousarray(fixed, dtype=np.uint8)
-        _check(lib().orc_set_dirichlet(self.h, _p(f, C.c_uint8)), "set_dirichlet")
+        _check(self._L.orc_set_dirichlet(self.h, _p(f, C.c_uint8)), "set_dirichlet")
 
     def calculate_at(self, e, u, result_type, xi=(0.5, 0.5, 0.5)):
         """Stress of element e at local xi: result_type 0 PK2, 1 Kirchhoff, 2 Cauchy (Voigt, 6 values)."""
         uu = self._u(u)
         x = np.ascontiguousarray(xi, dtype=np.float64)
         out = np.zeros(6)
-        _check(lib().orc_calculate_at(self.h, e, _p(uu, C.c_double), result_type, _p(x, C.c_double),
+        _check(self._L.orc_calculate_at(self.h, e, _p(uu, C.c_double), result_type, _p(x, C.c_double),
                                       _p(out, C.c_double)), "calculate_at")
         return out
 
     def set_material(self, material):
         """MATERIAL_NEOHOOKE (default) or MATERIAL_SVK for all elements."""
-        _check(lib().orc_set_material(self.h, int(material)), "set_material")
+        _check(self._L.orc_set_material(self.h, int(material)), "set_material")
 
     def set_dirichlet_values(self, rate):
         """Inhomogeneous Dirichlet values lambda * rate on constrained dofs (None removes them)."""
         if rate is None:
-            _check(lib().orc_set_dirichlet_values(self.h, None), "set_dirichlet_values")
+            _check(self._L.orc_set_dirichlet_values(self.h, None), "set_dirichlet_values")
             return
         r = np.ascontiguousarray(rate, dtype=np.float64)
-        _check(lib().orc_set_dirichlet_values(self.h, _p(r, C.c_double)), "set_dirichlet_values")
+        _check(self._L.orc_set_dirichlet_values(self.h, _p(r, C.c_double)), "set_dirichlet_values")
 
     def add_neumann(self, face_elem, face_local, traction):
         fe = np.ascontiguousarray(face_elem, dtype=np.int32)
         fl = np.ascontiguousarray(face_local, dtype=np.int32)
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(traction, dtype=np.float64), (len(fe), 3)))
-        _check(lib().orc_add_neumann(self.h, len(fe), _p(fe, C.c_int32), _p(fl, C.c_int32), _p(t, C.c_double)),
+        _check(self._L.orc_add_neumann(self.h, len(fe), _p(fe, C.c_int32), _p(fl, C.c_int32), _p(t, C.c_double)),
                "add_neumann")
 
     def add_point_loads(self, dofs, values):
         d = np.ascontiguousarray(dofs, dtype=np.int32)
         v = np.ascontiguousarray(values, dtype=np.float64)
-        _check(lib().orc_add_point_loads(self.h, len(d), _p(d, C.c_int32), _p(v, C.c_double)), "add_point_loads")
+        _check(self._L.orc_add_point_loads(self.h, len(d), _p(d, C.c_int32), _p(v, C.c_double)), "add_point_loads")
 
     def set_faithful_moduli(self, on=True):
-        _check(lib().orc_set_faithful_moduli(self.h, int(on)), "faithful")
+        _check(self._L.orc_set_faithful_moduli(self.h, int(on)), "faithful")
 
     @property
     def alpha(self):
         a = np.zeros(self.n_elems * self.n_alpha)
         if a.size:
-            _check(lib().orc_get_alpha(self.h, _p(a, C.c_double)), "get_alpha")
+            _check(self._L.orc_get_alpha(self.h, _p(a, C.c_double)), "get_alpha")
         return a.reshape(self.n_elems, self.n_alpha)
 
     @alpha.setter
     def alpha(self, a):
         a = np.ascontiguousarray(a, dtype=np.float64).ravel()
-        _check(lib().orc_set_alpha(self.h, _p(a, C.c_double)), "set_alpha")
+        _check(self._L.orc_set_alpha(self.h, _p(a, C.c_double)), "set_alpha")
 
     def _u(self, u):
         return np.ascontiguousarray(u if u is not None else np.zeros(self.n_dofs), dtype=np.float64)
@@ -218,45 +233,50 @@ class OracleProblem:
     def element_vector(self, e, u=None, lam=0.0):
         u = self._u(u)
         out = np.zeros(24)
-        _check(lib().orc_element_vector(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_vector")
+        _check(self._L.orc_element_vector(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_vector")
         return out
 
     def element_matrix(self, e, u=None, lam=0.0):
         u = self._u(u)
         out = np.zeros(576)
-        _check(lib().orc_element_matrix(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_matrix")
+        _check(self._L.orc_element_matrix(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_matrix")
         return out.reshape(24, 24).T.copy()  # stored column-major
 
     def element_energy(self, e, u=None, lam=0.0):
         u = self._u(u)
         out = np.zeros(1)
-        _check(lib().orc_element_energy(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_energy")
+        _check(self._L.orc_element_energy(self.h, e, _p(u, C.c_double), lam, _p(out, C.c_double)), "element_energy")
         return float(out[0])
 
     def update_state(self, u, correction, lam=0.0):
         u = self._u(u)
         c = np.ascontiguousarray(correction, dtype=np.float64)
-        _check(lib().orc_update_state(self.h, _p(u, C.c_double), lam, _p(c, C.c_double)), "update_state")
+        _check(self._L.orc_update_state(self.h, _p(u, C.c_double), lam, _p(c, C.c_double)), "update_state")
+
+    def constraints_below(self):
+        out = np.zeros(self.n_dofs, dtype=np.int32)
+        _check(self._L.orc_constraints_below(self.h, _p(out, C.c_int32)), "constraints_below")
+        return out
 
     def reduced_size(self):
-        return lib().orc_reduced_size(self.h)
+        return self._L.orc_reduced_size(self.h)
 
     def assemble_vector(self, u=None, lam=0.0, dbc=DBC_FULL):
         u = self._u(u)
         n = self.reduced_size() if dbc == DBC_REDUCED else self.n_dofs
         out = np.zeros(n)
-        _check(lib().orc_assemble_vector(self.h, _p(u, C.c_double), lam, dbc, _p(out, C.c_double)), "assemble_vector")
+        _check(self._L.orc_assemble_vector(self.h, _p(u, C.c_double), lam, dbc, _p(out, C.c_double)), "assemble_vector")
         return out
 
     def assemble_matrix_csc(self, u=None, lam=0.0, dbc=DBC_FULL):
         """Returns (col_ptr int64, row_idx int32, values float64, n)."""
         u = self._u(u)
         n = self.reduced_size() if dbc == DBC_REDUCED else self.n_dofs
-        nnz = lib().orc_pattern_nnz(self.h, dbc)
+        nnz = self._L.orc_pattern_nnz(self.h, dbc)
         cp = np.zeros(n + 1, dtype=np.int64)
         ri = np.zeros(nnz, dtype=np.int32)
         v = np.zeros(nnz)
-        _check(lib().orc_assemble_matrix_csc(self.h, _p(u, C.c_double), lam, dbc, _p(cp, C.c_int64),
+        _check(self._L.orc_assemble_matrix_csc(self.h, _p(u, C.c_double), lam, dbc, _p(cp, C.c_int64),
                                              _p(ri, C.c_int32), _p(v, C.c_double)), "assemble_matrix")
         return cp, ri, v, n
 
@@ -274,7 +294,7 @@ class OracleProblem:
         its = np.zeros(steps + 1, dtype=np.int32)
         rn = np.zeros(steps + 1)
         ns, tot = C.c_int(0), C.c_int(0)
-        code = lib().orc_load_control(self.h, steps, t_begin, t_end, tol, tol_mode, max_iter, solver, cg_rtol,
+        code = self._L.orc_load_control(self.h, steps, t_begin, t_end, tol, tol_mode, max_iter, solver, cg_rtol,
                                       _p(u, C.c_double), _p(lam, C.c_double), _p(its, C.c_int32), _p(rn, C.c_double),
                                       C.byref(ns), C.byref(tot))
         if code != 0 and not (allow_failure and code == -5):
@@ -288,7 +308,7 @@ class OracleProblem:
         uu = self._u(u).copy()
         lm = np.array([lam], dtype=np.float64)
         st = np.zeros(6)
-        code = lib().orc_load_step(self.h, dlambda, tol, tol_mode, max_iter, solver, cg_rtol, _p(uu, C.c_double),
+        code = self._L.orc_load_step(self.h, dlambda, tol, tol_mode, max_iter, solver, cg_rtol, _p(uu, C.c_double),
                                    _p(lm, C.c_double), _p(st, C.c_double))
         _check(code, "load_step")
         return uu, float(lm[0]), dict(zip(("newton", "cg", "t_residual", "t_tangent", "t_solve", "residual_norm"),
@@ -307,7 +327,7 @@ class OracleProblem:
         psi = np.zeros(1)
         ci = np.ascontiguousarray(controlled if controlled is not None else [], dtype=np.int32)
         ns, tot = C.c_int(0), C.c_int(0)
-        code = lib().orc_path_following(self.h, kind, steps, step_size, len(ci), _p(ci, C.c_int32) if len(ci) else None,
+        code = self._L.orc_path_following(self.h, kind, steps, step_size, len(ci), _p(ci, C.c_int32) if len(ci) else None,
                                         target_iterations, tol, max_iter, solver, cg_rtol, _p(u, C.c_double),
                                         _p(lam, C.c_double), _p(its, C.c_int32), _p(rn, C.c_double),
                                         _p(lams, C.c_double), _p(psi, C.c_double), C.byref(ns), C.byref(tot))

@@ -1264,6 +1264,17 @@ int orc_assemble_matrix_csc(orc_problem* p, const double* u, double lambda, int 
   return ORC_OK;
 }
 
+// FlatAssemblerBase constructor (assembler/interface.hh:50-62): constraintsBelow[i] = constrained dofs below i
+int orc_constraints_below(const orc_problem* p, int32_t* out) {
+  if (!p || !out) return ORC_ERR_ARG;
+  int32_t counter = 0;
+  for (int i = 0; i < p->ndof(); ++i) {
+    out[i] = counter;
+    if (p->fixed[i]) ++counter;
+  }
+  return ORC_OK;
+}
+
 int orc_set_threads(int n) {
   if (n < 1) return ORC_ERR_ARG;
   g_threads = n;

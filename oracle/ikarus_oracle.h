@@ -83,6 +83,8 @@ int64_t orc_pattern_nnz(orc_problem* p, int dbc);
 int orc_assemble_matrix_csc(orc_problem* p, const double* u, double lambda, int dbc, int64_t* col_ptr,
                             int32_t* row_idx, double* values);
 int orc_reduced_size(orc_problem* p);
+/* constraintsBelow (assembler/interface.hh:50-62): out[i] = number of constrained dofs with index < i (n values) */
+int orc_constraints_below(const orc_problem* p, int32_t* out);
 /* Jacobi-preconditioned CG (the reference's si_ConjugateGradient) on a symmetric CSC matrix: x = A^{-1} b to
  * ||r|| <= rtol ||b|| or max_iter iterations (ORC_ERR_NOT_CONVERGED); iterations returns the count. */
 int orc_cg_jacobi_csc(int n, const int64_t* col_ptr, const int32_t* row_idx, const double* values, const double* b,

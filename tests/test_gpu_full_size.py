@@ -12,10 +12,11 @@
 nu = 0.4999:
   * alpha updates, element-level and assembled FP64 residual and condensed tangent within 1e-12, the FP32
     condensed tangent within 2e-6, the pattern bit-exact.  At nu = 0.4999 the FP64 problem itself limits the
-    agreement of two FP64 implementations: the oracle's own condensed tangent moves by about 6e-10 relative when its
-    input coordinates are scaled by one ulp (the enhanced-strain modes scale like h^-8, the pressure term carries
-    lambda = 1.7e6), so there the bound of the condensed tangent and of the element matrices is that measured
-    one-ulp sensitivity of the oracle (never below 1e-12).
+    agreement of two FP64 implementations (the pressure term carries lambda = 1.7e6 and the static condensation
+    cancels lambda-sized terms): the oracle compiled with fused multiply-adds and the oracle compiled without them --
+    two equally valid FP64 evaluations of one restatement -- already differ by up to 7.5e-11 on single element
+    matrices (the device, which fuses multiply-adds, differs from the oracle by the same amount on the same
+    element).  There every quantity is bounded by max(1e-12, 2 x that spread), measured here for the same state.
 Each measured error is printed beside its bound (and logged by the parity_log fixture).
 """
 import numpy as np
@@ -168,52 +169,62 @@ def smooth_block_field(p, rng, scale):
 def test_config5_eas_block_state_update_element_and_assembly(ikr, parity_log, nu):
     p = problems.eas_block(nu=nu)
     o = oracle.from_problem(p)
+    of = oracle.from_problem(p, fused=True) if nu > 0.49 else None  # second valid FP64 evaluation
     rng = np.random.default_rng(23)
     du1 = smooth_block_field(p, rng, 2e-4)
     du2 = smooth_block_field(p, rng, 2e-5)
     lam = 0.4
     fes, asm = problems.build_gpu(p, precision=0)
+
+    def bound(spread):  # FP64 floor of an ill-conditioned quantity: twice the spread of the two oracle builds
+        if of is None:
+            return FP64_RTOL
+        parity_log(f"config5 nu={nu}: oracle with vs without fused multiply-adds", spread, 1.0)
+        return max(FP64_RTOL, 2.0 * spread)
+
     # alpha from the state update at the undeformed state with the increment du1 (updateStateImpl,
     # enhancedassumedstrains.hh:225-248), then a second update at u = du1 with du2
     z = np.zeros(p.n_dofs)
     ikr.updateState(fes, ikr.FERequirements(fes, z, lam), du1)
     o.update_state(z, du1, lam)
-    assert parity_log(f"config5 nu={nu}: alpha after update 1", rel_err(fes.alpha, o.alpha), FP64_RTOL)
+    b = FP64_RTOL
+    if of is not None:
+        of.update_state(z, du1, lam)
+        b = bound(rel_err(of.alpha, o.alpha))
+    assert parity_log(f"config5 nu={nu}: alpha after update 1", rel_err(fes.alpha, o.alpha), b)
     u = du1
-    Ko = o.assemble_matrix_csc(u, lam)
-    bound = FP64_RTOL
-    if nu > 0.49:
-        # the oracle's own sensitivity: the same state on coordinates scaled by one ulp
-        o2 = oracle.OracleProblem(p.mesh.coords * (1.0 + 2.0 ** -52), p.mesh.conn, p.lam, p.mu, p.eas, p.n_eas)
-        o2.set_dirichlet(p.fixed)
-        o2.alpha = o.alpha
-        sens = rel_err(o2.assemble_matrix_csc(u, lam)[2], Ko[2])
-        parity_log(f"config5 nu={nu}: oracle tangent moved by a one-ulp coordinate scaling", sens, 1.0)
-        bound = max(FP64_RTOL, sens)
-        del o2
     req = ikr.FERequirements(fes, u, lam)
     asm.bind(req, ikr.DBCOption.Full)
-    # element level: every element's force vector and stiffness matrix
+    # element level: every element's force vector and stiffness matrix (each matrix relative to its largest entry)
     ev = ikr.calculateVector(fes, req)
     ref_v = np.array([o.element_vector(e, u, lam) for e in range(p.mesh.n_elems)])
-    assert parity_log(f"config5 nu={nu}: element vectors", rel_err(ev, ref_v), FP64_RTOL)
+    b = bound(rel_err([of.element_vector(e, u, lam) for e in range(p.mesh.n_elems)], ref_v)) if of else FP64_RTOL
+    assert parity_log(f"config5 nu={nu}: element vectors", rel_err(ev, ref_v), b)
     del ev, ref_v
-    worst, where = 0.0, -1
+    worst, where, spread = 0.0, -1, 0.0
     for e0 in range(0, p.mesh.n_elems, 8192):
         em = ikr.calculateMatrix(fes, req, elements=(e0, e0 + 8192))
         for k in range(em.shape[0]):
             Ke = o.element_matrix(e0 + k, u, lam)
-            err = np.abs(em[k] - Ke).max() / np.abs(Ke).max()
+            scale = np.abs(Ke).max()
+            err = np.abs(em[k] - Ke).max() / scale
             if err > worst:
                 worst, where = err, e0 + k
-    assert parity_log(f"config5 nu={nu}: element matrices (worst element {where})", worst, bound)
+            if of is not None:
+                spread = max(spread, np.abs(of.element_matrix(e0 + k, u, lam) - Ke).max() / scale)
+    b = bound(spread) if of else FP64_RTOL
+    assert parity_log(f"config5 nu={nu}: element matrices (worst element {where})", worst, b)
     # assembled (Full) residual and condensed tangent, pattern bit-exact
     R = asm.vector(req, dbc=ikr.DBCOption.Full)
-    assert parity_log(f"config5 nu={nu}: FP64 residual (Full)", rel_err(R, o.assemble_vector(u, lam)), FP64_RTOL)
+    Ro = o.assemble_vector(u, lam)
+    b = bound(rel_err(of.assemble_vector(u, lam), Ro)) if of else FP64_RTOL
+    assert parity_log(f"config5 nu={nu}: FP64 residual (Full)", rel_err(R, Ro), b)
     K = asm.matrix(req, dbc=ikr.DBCOption.Full)
+    Ko = o.assemble_matrix_csc(u, lam)
     K.sort_indices()
     assert np.array_equal(K.indptr.astype(np.int64), Ko[0]) and np.array_equal(K.indices, Ko[1])
-    assert parity_log(f"config5 nu={nu}: FP64 condensed tangent (Full)", rel_err(K.data, Ko[2]), bound)
+    b = bound(rel_err(of.assemble_matrix_csc(u, lam)[2], Ko[2])) if of else FP64_RTOL
+    assert parity_log(f"config5 nu={nu}: FP64 condensed tangent (Full)", rel_err(K.data, Ko[2]), b)
     del K
     fes32, asm32 = problems.build_gpu(p, precision=1)
     fes32.alpha = fes.alpha
@@ -224,4 +235,8 @@ def test_config5_eas_block_state_update_element_and_assembly(ikr, parity_log, nu
     # second state update at u
     ikr.updateState(fes, req, du2)
     o.update_state(u, du2, lam)
-    assert parity_log(f"config5 nu={nu}: alpha after update 2", rel_err(fes.alpha, o.alpha), FP64_RTOL)
+    b = FP64_RTOL
+    if of is not None:
+        of.update_state(u, du2, lam)
+        b = bound(rel_err(of.alpha, o.alpha))
+    assert parity_log(f"config5 nu={nu}: alpha after update 2", rel_err(fes.alpha, o.alpha), b)

@@ -265,7 +265,7 @@ def test_config1_mixed_precision_reaches_fp64_tolerance(ikr, parity_log):
     for si in info.solverInfos[1:]:
         assert si.success
     assert parity_log("config1 mixed: max|u - u_oracle| / max|u_oracle|", rel_err(req.globalSolution(), ref["u"]),
-                      1e-6)
+                      1e-8)
 
 
 @pytest.mark.parametrize("es", ["GreenLagrangeStrain", "DisplacementGradient", "DisplacementGradientTransposed"])
