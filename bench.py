@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--train-paths", type=int, default=200, help="config 4: training load paths")
     ap.add_argument("--eval-paths", type=int, default=20, help="config 4: held-out load paths")
     ap.add_argument("--no-graphs", action="store_true", help="launch CG kernels one by one (for profilers)")
+    ap.add_argument("--batched-backtracks", type=int, default=8,
+                    help="config 3: halvings of an instance's correction that inverts an element (0: take it out)")
     ap.add_argument("--backtracks", type=int, default=0,
                     help="configs 3 and 5: halve a Newton correction that inverts an element up to this many times "
                          "(both forms; 0 = abort like the reference)")
@@ -650,12 +652,13 @@ def run_batched(args):
     out = {"metric": "time to ||R||/||R0||<1e-8 on every load step for all 512 instances", "unit": "s",
            "higher_is_better": False, "config": {"workload": bp.name, "elements": bp.mesh.n_elems,
                                                   "dofs": bp.n_dofs, "instances": 512, "load_steps": 10,
-                                                  "newton_backtracks": args.backtracks}}
+                                                  "newton_backtracks": args.batched_backtracks}}
+    finals, status = {}, {}
     for mixed in (True, False):
         fes, asm = problems.build_gpu_batched(bp, precision=1 if mixed else 0)
         st = ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, eisenstat_walker=mixed,
                             linear_rtol=1e-2 if mixed else 1e-10, linear_rtol_min=1e-6, linear_max_iter=20000,
-                            backtracks=args.backtracks)
+                            backtracks=args.batched_backtracks)
         nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
         lc = ikr.LoadControl(nr, bp.load_steps)
         req, req0 = ikr.FERequirements(fes), ikr.FERequirements(fes)
@@ -677,8 +680,18 @@ def run_batched(args):
         out[key] = {"s": round(sum(times) / len(times), 4), "success": bool(info.success),
                     "newton_iterations_batch": info.totalIterations, "cg_iterations_sum": info.totalLinearIterations,
                     "instances_converged_last_step": int((conv == 1).sum()),
-                    "instances_taken_out_element_inversion": int((conv == -1).sum())}
+                    "instances_taken_out_element_inversion": int((conv == -1).sum()),
+                    "taken_out": [int(i) for i in np.nonzero(conv == -1)[0]]}
+        finals[key], status[key] = req.globalSolution(), conv.copy()
         del lc, nr, asm, fes
+    both = np.nonzero((status["mixed"] == 1) & (status["plain_fp64"] == 1))[0]
+    worst = 0.0
+    for i in both:
+        sl = slice(3 * bp.node_offsets[i], 3 * bp.node_offsets[i + 1])
+        ref = finals["plain_fp64"][sl]
+        worst = max(worst, float(np.abs(finals["mixed"][sl] - ref).max() / max(np.abs(ref).max(), 1e-300)))
+    out["same_instances_solved"] = bool(np.array_equal(status["mixed"] == 1, status["plain_fp64"] == 1))
+    out["mixed_vs_plain_max_rel_diff"] = worst
     out["value"] = out["mixed"]["s"]
     out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 3)
     out["instances_per_s"] = round(512 / out["mixed"]["s"], 2)

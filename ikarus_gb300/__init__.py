@@ -141,6 +141,15 @@ class _ControlInfo(C.Structure):
 
 _NR_OBS = C.CFUNCTYPE(None, C.c_int32, C.POINTER(_NRState), C.c_void_p)
 _LOG_SINK = C.CFUNCTYPE(None, C.c_char_p, C.c_void_p)
+_POINT_FN = C.CFUNCTYPE(None, C.c_int32, C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double), C.c_void_p)
+
+
+def _point_fn(fn):
+    """ctypes trampoline of a load function fn(X: (n, 3) array, lambda) -> (n, 3) values."""
+    def tramp(n, X, lam, out, _user):
+        x = np.ctypeslib.as_array(X, shape=(n, 3))
+        np.ctypeslib.as_array(out, shape=(n, 3))[:] = np.asarray(fn(x, lam), dtype=np.float64).reshape(n, 3)
+    return _POINT_FN(tramp)
 _CTRL_OBS = C.CFUNCTYPE(None, C.c_int32, C.POINTER(_ControlState), C.c_void_p)
 
 # exported entry points and their ctypes signatures (kept in sync with include/ikarus_gb300.h)
@@ -156,6 +165,9 @@ SIGNATURES = {
     "ikr_fes_add_neumann": ([_vp, _I, _ip, _ip, _dp], C.c_int),
     "ikr_fes_destroy": ([_vp], C.c_int),
     "ikr_fes_clear_neumann": ([_vp], C.c_int),
+    "ikr_fes_add_neumann_function": ([_vp, _I, _ip, _ip, _POINT_FN, _vp], C.c_int),
+    "ikr_fes_add_volume_load": ([_vp, _POINT_FN, _vp], C.c_int),
+    "ikr_fes_clear_volume_loads": ([_vp], C.c_int),
     "ikr_fes_set_element_materials": ([_vp, _dp, _dp], C.c_int),
     "ikr_fes_set_instances": ([_vp, _I, _ip], C.c_int),
     "ikr_newton_instance_info": ([_vp, _ip, _dp, _ip], C.c_int),
@@ -353,6 +365,7 @@ class FiniteElements:
                                   _ptr(self.conn, C.c_int32), material.lambda_, material.mu, int(eas), self.n_eas),
              "fes_create")
         self.h = h
+        self._load_cbs = []  # ctypes trampolines of function-defined loads (kept alive with the element set)
         if getattr(material, "kind", 0):
             _err(lib().ikr_fes_set_material(self.h, int(material.kind)), "set_material")
 
@@ -368,6 +381,25 @@ class FiniteElements:
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(traction, dtype=np.float64), (len(fe), 3)))
         _err(lib().ikr_fes_add_neumann(self.h, len(fe), _ptr(fe, C.c_int32), _ptr(fl, C.c_int32), _ptr(t)),
              "add_neumann")
+
+    def add_neumann_function(self, face_elem, face_local, fn):
+        """neumannBoundaryLoad(patch, f) with f(X, lambda): fn(X (n, 3), lambda) -> tractions (n, 3) at the faces'
+        quadrature points (face centres), evaluated whenever the load factor changes."""
+        fe = np.ascontiguousarray(face_elem, dtype=np.int32)
+        fl = np.ascontiguousarray(face_local, dtype=np.int32)
+        cb = _point_fn(fn)
+        self._load_cbs.append(cb)
+        _err(lib().ikr_fes_add_neumann_function(self.h, len(fe), _ptr(fe, C.c_int32), _ptr(fl, C.c_int32), cb,
+                                                None), "add_neumann_function")
+
+    def add_volume_load(self, fn):
+        """volumeLoad(f) (loads/volume.hh): fn(X (n, 3), lambda) -> body forces (n, 3) at the Gauss points."""
+        cb = _point_fn(fn)
+        self._load_cbs.append(cb)
+        _err(lib().ikr_fes_add_volume_load(self.h, cb, None), "add_volume_load")
+
+    def clear_volume_loads(self):
+        _err(lib().ikr_fes_clear_volume_loads(self.h))
 
     def clear_neumann(self):
         _err(lib().ikr_fes_clear_neumann(self.h), "clear_neumann")

@@ -287,6 +287,14 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
         }
       }
     }
+    if (a.ext) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const double tv = a.ext[24 * (size_t)e + 3 * sub + c];
+        f[c] -= tv;
+        if (WANT_E) psi -= tv * Ud[c];
+      }
+    }
   }
   double psi_tot = 0.0;
   if (WANT_E) psi_tot = sum8(psi);  // last warp-wide operation: inactive lanes may leave after it
@@ -649,6 +657,10 @@ __global__ void __launch_bounds__(EPB * 8) disp_residual_gp_kernel(ElemArgs a, c
       for (int c = 0; c < 3; ++c) f[c] -= a.load_factor * a.trac[24 * t + 3 * sub + c];
     }
   }
+  if (a.ext) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) f[c] -= a.ext[24 * (size_t)e + 3 * sub + c];
+  }
   if (!active) return;
   if (bad) {
     if (a.inst_status) atomicOr(a.inst_status + a.elem_inst[e], bad);
@@ -824,6 +836,92 @@ void launch_stress_at(const ElemArgs& a, int e0, int count, const double* xi, bo
                       cudaStream_t s) {
   if (count <= 0) return;
   stress_at_kernel<<<(count + 127) / 128, 128, 0, s>>>(a, e0, count, xi, xi_per_elem ? 1 : 0, type, out);
+}
+
+// Gauss-point positions, one thread per element
+__global__ void gauss_points_kernel(const double* __restrict__ X, const int32_t* __restrict__ conn, int ne,
+                                    double* __restrict__ xgp) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double Xv[8][3];
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    const int n = conn[(size_t)v * ne + e];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Xv[v][c] = X[3 * (size_t)n + c];
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    double x[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      const double N = (((v ^ q) & 1) ? kGaussLo : kGaussHi) * (((v ^ q) & 2) ? kGaussLo : kGaussHi) *
+                       (((v ^ q) & 4) ? kGaussLo : kGaussHi);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[c] += N * Xv[v][c];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) xgp[(8 * (size_t)e + q) * 3 + c] = x[c];
+  }
+}
+
+// VolumeLoad at the element's Gauss rule, one thread per element (adds to ext)
+__global__ void volume_load_kernel(const double* __restrict__ X, const int32_t* __restrict__ conn, int ne,
+                                   const double* __restrict__ b, double* __restrict__ ext) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne) return;
+  double Xv[8][3], acc[24];
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    const int n = conn[(size_t)v * ne + e];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Xv[v][c] = X[3 * (size_t)n + c];
+  }
+#pragma unroll
+  for (int k = 0; k < 24; ++k) acc[k] = 0.0;
+  for (int q = 0; q < 8; ++q) {
+    double J[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      double dxi[3];
+      ref_gradient_at_gp<double>(v, q, dxi);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) J[i][j] += Xv[v][i] * dxi[j];
+    }
+    const double w = kGaussW * det3(J);
+    const double* bq = b + (8 * (size_t)e + q) * 3;
+    const double b0 = bq[0] * w, b1 = bq[1] * w, b2 = bq[2] * w;
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      const double N = (((v ^ q) & 1) ? kGaussLo : kGaussHi) * (((v ^ q) & 2) ? kGaussLo : kGaussHi) *
+                       (((v ^ q) & 4) ? kGaussLo : kGaussHi);
+      acc[3 * v] += N * b0;
+      acc[3 * v + 1] += N * b1;
+      acc[3 * v + 2] += N * b2;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 24; ++k) ext[24 * (size_t)e + k] += acc[k];
+}
+
+__global__ void add_slot_loads_kernel(const int32_t* __restrict__ slot_elem, int n_slots,
+                                      const double* __restrict__ vals, double* __restrict__ ext) {
+  const int s = blockIdx.x;
+  if (s >= n_slots || threadIdx.x >= 24) return;
+  ext[24 * (size_t)slot_elem[s] + threadIdx.x] += vals[24 * (size_t)s + threadIdx.x];
+}
+
+void launch_gauss_points(const double* X, const int32_t* conn, int n_elems, double* xgp, cudaStream_t s) {
+  if (n_elems > 0) gauss_points_kernel<<<(n_elems + 127) / 128, 128, 0, s>>>(X, conn, n_elems, xgp);
+}
+void launch_volume_loads(const double* X, const int32_t* conn, int n_elems, const double* b, double* ext,
+                         cudaStream_t s) {
+  if (n_elems > 0) volume_load_kernel<<<(n_elems + 127) / 128, 128, 0, s>>>(X, conn, n_elems, b, ext);
+}
+void launch_add_slot_loads(const int32_t* slot_elem, int n_slots, const double* vals, double* ext, cudaStream_t s) {
+  if (n_slots > 0) add_slot_loads_kernel<<<n_slots, 32, 0, s>>>(slot_elem, n_slots, vals, ext);
 }
 
 void launch_traction_loads(const double* X, const int32_t* conn, int n_elems, int n_slots, const int32_t* slot_elem,

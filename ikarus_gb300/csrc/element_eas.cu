@@ -602,6 +602,10 @@ __global__ void __launch_bounds__(EasCfg<NA>::EPB * 8) eas_element_kernel(ElemAr
 #pragma unroll
         for (int c = 0; c < 3; ++c) f[c] -= a.load_factor * a.trac[24 * t + 3 * sub + c];
     }
+    if (a.ext) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] -= a.ext[24 * (size_t)e + 3 * sub + c];
+    }
     if (ELEM_OUT) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) a.elem_vec[24 * (size_t)li + 3 * sub + c] = f[c];

@@ -108,6 +108,7 @@ static int choose_epb(ikr_fes f, Pass pass) {
 void assemble_vector(ikr_asm a, ikr_req r, int dbc) {
   ikr_fes f = a->fes;
   f->refresh_tractions();
+  f->refresh_function_loads(r->lambda);
   a->R.alloc(a->n);
   CK(cudaMemsetAsync(a->R.p, 0, sizeof(double) * a->n, f->stream));
   ikr::ElemArgs args = f->args();
@@ -290,6 +291,7 @@ int ikr_fes_create(ikr_fes* out, int32_t n_nodes, const double* coords, int32_t 
     f->mu = mu;
     CK(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
     f->conn_h.assign(conn, conn + 8LL * n_elems);
+    f->X_h.assign(coords, coords + 3LL * n_nodes);
     f->X.upload(coords, 3LL * n_nodes, f->stream);
     std::vector<int32_t> soa(8LL * n_elems);
     for (int e = 0; e < n_elems; ++e)
@@ -327,6 +329,52 @@ int ikr_fes_add_neumann(ikr_fes fes, int32_t n_faces, const int32_t* face_elem, 
   });
 }
 
+int ikr_fes_add_volume_load(ikr_fes fes, ikr_point_fn f, void* user) {
+  return guarded([&] {
+    need(fes && f, IKR_ERR_ARG, "null argument");
+    fes->vol_fns.push_back({f, user});
+    fes->ext_dirty = true;
+  });
+}
+int ikr_fes_clear_volume_loads(ikr_fes fes) {
+  return guarded([&] {
+    need(fes, IKR_ERR_ARG, "null argument");
+    fes->vol_fns.clear();
+    fes->ext_dirty = true;
+  });
+}
+int ikr_fes_add_neumann_function(ikr_fes fes, int32_t n_faces, const int32_t* face_elem, const int32_t* face_local,
+                                 ikr_point_fn f, void* user) {
+  return guarded([&] {
+    need(fes && f && n_faces >= 0 && (n_faces == 0 || (face_elem && face_local)), IKR_ERR_ARG, "invalid arguments");
+    std::vector<std::pair<int32_t, int32_t>> faces;
+    for (int k = 0; k < n_faces; ++k) {
+      need(face_elem[k] >= 0 && face_elem[k] < fes->ne && face_local[k] >= 0 && face_local[k] < 6, IKR_ERR_ARG,
+           "face out of range");
+      faces.push_back({face_elem[k], face_local[k]});
+    }
+    std::stable_sort(faces.begin(), faces.end(),
+                     [](const auto& x, const auto& y) { return x.first < y.first; });
+    ikr_fes_s::FaceFnSet fs{f, user, {}, {0}, {}, {}};
+    for (size_t k = 0; k < faces.size(); ++k) {
+      const int e = faces[k].first, lf = faces[k].second, d = lf / 2, side = lf % 2;
+      if (fs.slot_elem.empty() || fs.slot_elem.back() != e) {
+        if (!fs.slot_elem.empty()) fs.face_ptr.push_back((int32_t)k);
+        fs.slot_elem.push_back(e);
+      }
+      fs.face_local.push_back(lf);
+      // the face's quadrature point: the centre of the face, the mean of its four corners
+      double c[3] = {0.0, 0.0, 0.0};
+      for (int v = 0; v < 8; ++v)
+        if (((v >> d) & 1) == side)
+          for (int i = 0; i < 3; ++i) c[i] += 0.25 * fes->X_h[3 * (size_t)fes->conn_h[8 * (size_t)e + v] + i];
+      fs.points.insert(fs.points.end(), c, c + 3);
+    }
+    if (!fs.slot_elem.empty()) fs.face_ptr.push_back((int32_t)faces.size());
+    if (!faces.empty()) fes->face_fns.push_back(std::move(fs));
+    fes->ext_dirty = true;
+  });
+}
 int ikr_fes_clear_neumann(ikr_fes fes) {
   return guarded([&] {
     need(fes, IKR_ERR_ARG, "null argument");
@@ -334,6 +382,8 @@ int ikr_fes_clear_neumann(ikr_fes fes) {
     fes->trac_idx.release();
     fes->trac.release();
     fes->trac_dirty = false;
+    fes->face_fns.clear();
+    fes->ext_dirty = true;
   });
 }
 int ikr_fes_set_element_materials(ikr_fes fes, const double* lambda, const double* mu) {
@@ -425,6 +475,7 @@ static void element_level(ikr_fes fes, ikr_req req, int mode, int32_t e0, int32_
   const int n = e1 - e0;
   if (n == 0) return;
   fes->refresh_tractions();
+  fes->refresh_function_loads(req->lambda);
   fes->scratch_out.alloc((size_t)per * n);
   ikr::ElemArgs a = fes->args();
   a.u = req->u.p;

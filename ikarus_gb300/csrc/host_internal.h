@@ -132,6 +132,21 @@ struct ikr_fes_s {
   DBuf<int32_t> trac_idx;
   DBuf<double> trac;
   bool trac_dirty = false;
+  // loads given as functions f(X, lambda), evaluated on the host whenever the load factor changes: volume loads
+  // at the Gauss points, Neumann faces at their quadrature point; their sum per element in ext (24 per element)
+  struct FaceFnSet {
+    ikr_point_fn f;
+    void* user;
+    std::vector<int32_t> slot_elem, face_ptr, face_local;  // faces grouped by element (traction kernel layout)
+    std::vector<double> points;                            // quadrature point of every face, grouped order
+  };
+  std::vector<std::pair<ikr_point_fn, void*>> vol_fns;
+  std::vector<FaceFnSet> face_fns;
+  std::vector<double> X_h;    // coordinates (host copy)
+  std::vector<double> xgp_h;  // Gauss-point positions (host, computed once on the device)
+  DBuf<double> ext;
+  bool ext_dirty = false;
+  double ext_lambda = 0.0;
   DBuf<int> status;
   DBuf<double> scratch_out;  // element-level outputs
   DBuf<double> lam_e, mu_e;  // per-element Lame parameters (empty: lam / mu everywhere)
@@ -166,6 +181,7 @@ struct ikr_fes_s {
     a.eas_Y = eas_Y.p;
     a.trac_idx = trac_idx.n ? trac_idx.p : nullptr;
     a.trac = trac.p;
+    a.ext = (vol_fns.empty() && face_fns.empty()) ? nullptr : ext.p;
     a.status = status.p;
     a.lam_e = lam_e.n ? lam_e.p : nullptr;
     a.mu_e = mu_e.n ? mu_e.p : nullptr;
@@ -202,6 +218,52 @@ struct ikr_fes_s {
     count(1);
     CK(cudaStreamSynchronize(stream));
     trac_dirty = false;
+  }
+
+  // the function-defined loads at load factor lambda (re-evaluated only when lambda or the loads changed)
+  void refresh_function_loads(double lambda) {
+    if (vol_fns.empty() && face_fns.empty()) return;
+    if (!ext_dirty && ext.p && lambda == ext_lambda) return;
+    ext.alloc(24 * (size_t)ne);
+    CK(cudaMemsetAsync(ext.p, 0, sizeof(double) * 24 * (size_t)ne, stream));
+    if (!vol_fns.empty()) {
+      if (xgp_h.empty()) {
+        DBuf<double> d;
+        d.alloc(24 * (size_t)ne);
+        ikr::launch_gauss_points(X.p, conn.p, ne, d.p, stream);
+        count(1);
+        xgp_h.resize(24 * (size_t)ne);
+        d.download(xgp_h.data(), xgp_h.size(), stream);
+        CK(cudaStreamSynchronize(stream));
+      }
+      std::vector<double> b(24 * (size_t)ne);
+      DBuf<double> db;
+      for (auto& vf : vol_fns) {
+        vf.first(8 * ne, xgp_h.data(), lambda, b.data(), vf.second);
+        db.upload(b.data(), b.size(), stream);
+        ikr::launch_volume_loads(X.p, conn.p, ne, db.p, ext.p, stream);
+        count(1);
+        CK(cudaStreamSynchronize(stream));
+      }
+    }
+    for (auto& fs : face_fns) {
+      const int nf = (int)fs.face_local.size(), ns = (int)fs.slot_elem.size();
+      std::vector<double> t(3 * (size_t)nf);
+      fs.f(nf, fs.points.data(), lambda, t.data(), fs.user);
+      DBuf<int32_t> d_se, d_fp, d_fl;
+      DBuf<double> d_t, vals;
+      d_se.upload(fs.slot_elem.data(), ns, stream);
+      d_fp.upload(fs.face_ptr.data(), fs.face_ptr.size(), stream);
+      d_fl.upload(fs.face_local.data(), nf, stream);
+      d_t.upload(t.data(), t.size(), stream);
+      vals.alloc(24 * (size_t)ns);
+      ikr::launch_traction_loads(X.p, conn.p, ne, ns, d_se.p, d_fp.p, d_fl.p, d_t.p, vals.p, stream);
+      ikr::launch_add_slot_loads(d_se.p, ns, vals.p, ext.p, stream);
+      count(2);
+      CK(cudaStreamSynchronize(stream));
+    }
+    ext_lambda = lambda;
+    ext_dirty = false;
   }
 
   void check_status() {

@@ -33,6 +33,9 @@ struct ElemArgs {
   // dead tractions: trac_idx[e] >= 0 indexes 24 values of sum_faces N_I t dA at load factor 1
   const int32_t* trac_idx = nullptr;
   const double* trac = nullptr;
+  // loads given as functions of (X, lambda): 24 values per element, sum_q N_I b w detJ + sum_faces N_I t dA at the
+  // current load factor (not scaled by it); nullptr = none
+  const double* ext = nullptr;
   double load_factor = 0;
   // EAS
   int eas_kind = 0, n_alpha = 0;
@@ -97,6 +100,14 @@ void launch_eas_stress_at(const ElemArgs& a, int e0, int count, const double* xi
 void launch_traction_loads(const double* X, const int32_t* conn, int n_elems, int n_slots, const int32_t* slot_elem,
                            const int32_t* face_ptr, const int32_t* face_local, const double* traction, double* trac,
                            cudaStream_t s);
+// global positions of the 8 Gauss points of every element, q = x + 2y + 4z (xi_d = lo for bit 0, hi for bit 1):
+// xgp[(8 e + q) * 3 + c]
+void launch_gauss_points(const double* X, const int32_t* conn, int n_elems, double* xgp, cudaStream_t s);
+// VolumeLoad (loads/volume.hh:86-106): ext[24 e + 3 v + c] += sum_q N_v(xi_q) b[(8 e + q) * 3 + c] w_q detJ(xi_q)
+void launch_volume_loads(const double* X, const int32_t* conn, int n_elems, const double* b, double* ext,
+                         cudaStream_t s);
+// ext[24 slot_elem[k] + i] += vals[24 k + i] (each element in at most one slot)
+void launch_add_slot_loads(const int32_t* slot_elem, int n_slots, const double* vals, double* ext, cudaStream_t s);
 
 // sparse.cu
 void launch_node_elem_count(const int32_t* conn, int n_elems, int n_nodes, int32_t* cnt, cudaStream_t s);

@@ -119,6 +119,21 @@ int ikr_fes_create(ikr_fes* out, int32_t n_nodes, const double* coords, int32_t 
  * value of f at the face's single quadrature point (the face centre; rule order = order() = 1). */
 int ikr_fes_add_neumann(ikr_fes fes, int32_t n_faces, const int32_t* face_elem, const int32_t* face_local,
                         const double* traction);
+/* Loads given as functions of the position and the load factor, evaluated on the host:
+ * out[3k .. 3k+2] = f(X[3k .. 3k+2], lambda) for k < n (the reference's std::function<Vector(FieldVector, double)>). */
+typedef void (*ikr_point_fn)(int32_t n, const double* X, double lambda, double* out, void* user);
+/* Replaces skills(neumannBoundaryLoad(patch, f)) with a general f(X, lambda) (loads/traction.hh:21-33, 105-138): the
+ * traction f at each listed face's quadrature point (the face centre, rule order 1).  f is called whenever a force
+ * vector or energy is assembled at a load factor other than the last one (one call per Neumann set with all its
+ * face points); ikr_fes_add_neumann is the faster form for f(X, lambda) = lambda t(X). */
+int ikr_fes_add_neumann_function(ikr_fes fes, int32_t n_faces, const int32_t* face_elem, const int32_t* face_local,
+                                 ikr_point_fn f, void* user);
+/* Replaces skills(volumeLoad<3>(f)) (loads/volume.hh:86-106): body force f(X, lambda) per unit reference volume on
+ * every element, integrated with the element's 2x2x2 Gauss rule, f_I -= N_I b w detJ (and -u.b w detJ in the energy).
+ * f is called with the 8 n_elems Gauss points (element-major; point q = x + 2y + 4z of the element, xi_d =
+ * 1/2 -+ 1/(2 sqrt 3) for bit d of q clear / set) whenever the load factor changes.  Several volume loads add up. */
+int ikr_fes_add_volume_load(ikr_fes fes, ikr_point_fn f, void* user);
+int ikr_fes_clear_volume_loads(ikr_fes fes);
 /* removes every Neumann load added so far (the element set keeps its mesh, material and state) */
 int ikr_fes_clear_neumann(ikr_fes fes);
 /* per-element Lame parameters (n_elems each) replacing the set's single NeoHooke material */

@@ -14,9 +14,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
-_FUSED_PATH = os.path.join(_HERE, "_build", "liboracle_fused.so")
+_UNFUSED_PATH = os.path.join(_HERE, "_build", "liboracle_unfused.so")
 _lib = None
-_lib_fused = None
+_lib_unfused = None
 
 EAS_NONE, EAS_GL, EAS_H, EAS_HT = 0, 1, 2, 3
 DBC_RAW, DBC_REDUCED, DBC_FULL = 0, 1, 2
@@ -36,16 +36,16 @@ def build():
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
 
 
-def lib(fused=False):
-    """The oracle library; fused=True: the same restatement compiled with multiply-adds contracted to fused
-    multiply-adds where the target has them (a second valid FP64 evaluation, for FP64 floors)."""
-    global _lib, _lib_fused
-    if fused:
-        if _lib_fused is None:
-            if not os.path.exists(_FUSED_PATH):
+def lib(unfused=False):
+    """The oracle library; unfused=True: the same restatement compiled without contracting multiply-adds to fused
+    multiply-adds (a second valid FP64 evaluation, for FP64 floors of ill-conditioned quantities)."""
+    global _lib, _lib_unfused
+    if unfused:
+        if _lib_unfused is None:
+            if not os.path.exists(_UNFUSED_PATH):
                 build()
-            _lib_fused = _declare(C.CDLL(_FUSED_PATH))
-        return _lib_fused
+            _lib_unfused = _declare(C.CDLL(_UNFUSED_PATH))
+        return _lib_unfused
     if _lib is None:
         if not os.path.exists(_LIB_PATH):
             build()
@@ -84,11 +84,23 @@ def _declare(L):
                                      C.c_int, C.c_double, dp, dp, ip, dp, dp, dp, C.POINTER(C.c_int),
                                      C.POINTER(C.c_int)]
     L.orc_set_threads.argtypes = [C.c_int]
+    L.orc_add_volume_load.argtypes = [vp, _ORC_POINT_FN, vp]
+    L.orc_add_neumann_function.argtypes = [vp, C.c_int, ip, ip, _ORC_POINT_FN, vp]
     L.orc_constraints_below.argtypes = [vp, ip]
     L.orc_load_step.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp, dp]
     L.orc_path_following_toy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, dp,
                                          dp, ip, dp, dp, C.POINTER(C.c_int)]
     return L
+
+
+_ORC_POINT_FN = C.CFUNCTYPE(None, C.c_int32, C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double), C.c_void_p)
+
+
+def _point_fn(fn):
+    def tramp(n, X, lam, out, _user):
+        x = np.ctypeslib.as_array(X, shape=(n, 3))
+        np.ctypeslib.as_array(out, shape=(n, 3))[:] = np.asarray(fn(x, lam), dtype=np.float64).reshape(n, 3)
+    return _ORC_POINT_FN(tramp)
 
 
 def _p(a, t):
@@ -139,10 +151,11 @@ def path_following_toy(kind=PF_ARC_LENGTH, idbc=False, steps=5, step_size=0.1, t
                 d_steps=ds[: ns.value])
 
 
-def from_problem(p, faithful=False, fused=False):
-    """Oracle twin of an ``ikarus_gb300.problems.Problem`` definition (plain data, no GPU objects); fused: evaluated
-    by the fused-multiply-add build of the oracle."""
-    o = OracleProblem(p.mesh.coords, p.mesh.conn, p.lam, p.mu, p.eas if p.n_eas else EAS_NONE, p.n_eas, fused=fused)
+def from_problem(p, faithful=False, unfused=False):
+    """Oracle twin of an ``ikarus_gb300.problems.Problem`` definition (plain data, no GPU objects); unfused: evaluated
+    by the build of the oracle without fused multiply-adds."""
+    o = OracleProblem(p.mesh.coords, p.mesh.conn, p.lam, p.mu, p.eas if p.n_eas else EAS_NONE, p.n_eas,
+                      unfused=unfused)
     o.set_dirichlet(p.fixed)
     if getattr(p, "material", 0):
         o.set_material(p.material)
@@ -158,13 +171,13 @@ def from_problem(p, faithful=False, fused=False):
 class OracleProblem:
     """One mesh + NeoHooke material + EAS choice, with Dirichlet flags and dead loads."""
 
-    def __init__(self, coords, conn, lam, mu, eas_kind=EAS_NONE, n_alpha=0, fused=False):
+    def __init__(self, coords, conn, lam, mu, eas_kind=EAS_NONE, n_alpha=0, unfused=False):
         self.coords = np.ascontiguousarray(coords, dtype=np.float64)
         self.conn = np.ascontiguousarray(conn, dtype=np.int32)
         self.n_nodes, self.n_elems = self.coords.shape[0], self.conn.shape[0]
         self.n_dofs = 3 * self.n_nodes
         self.n_alpha = n_alpha
-        self._L = L = lib(fused)
+        self._L = L = lib(unfused)
         self.h = L.orc_problem_create(self.n_nodes, _p(self.coords, C.c_double), self.n_elems,
                                       _p(self.conn, C.c_int32), lam, mu, eas_kind, n_alpha)
         if not self.h:
@@ -206,6 +219,21 @@ class OracleProblem:
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(traction, dtype=np.float64), (len(fe), 3)))
         _check(self._L.orc_add_neumann(self.h, len(fe), _p(fe, C.c_int32), _p(fl, C.c_int32), _p(t, C.c_double)),
                "add_neumann")
+
+    def add_volume_load(self, fn):
+        """VolumeLoad with fn(X (n, 3), lambda) -> body forces (n, 3)."""
+        cb = _point_fn(fn)
+        self._cbs = getattr(self, "_cbs", []) + [cb]
+        _check(self._L.orc_add_volume_load(self.h, cb, None), "add_volume_load")
+
+    def add_neumann_function(self, face_elem, face_local, fn):
+        """Neumann faces with a traction function fn(X (n, 3), lambda) -> (n, 3)."""
+        fe = np.ascontiguousarray(face_elem, dtype=np.int32)
+        fl = np.ascontiguousarray(face_local, dtype=np.int32)
+        cb = _point_fn(fn)
+        self._cbs = getattr(self, "_cbs", []) + [cb]
+        _check(self._L.orc_add_neumann_function(self.h, len(fe), _p(fe, C.c_int32), _p(fl, C.c_int32), cb, None),
+               "add_neumann_function")
 
     def add_point_loads(self, dofs, values):
         d = np.ascontiguousarray(dofs, dtype=np.int32)

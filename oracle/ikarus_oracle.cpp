@@ -305,6 +305,13 @@ struct orc_problem {
   std::vector<double> alpha;    // ne*na
   // Neumann faces grouped per element
   std::vector<std::vector<std::pair<int, std::array<double, 3>>>> faces;
+  // loads given as functions f(X, lambda): volume loads on every element, Neumann faces with a function
+  struct PointFn {
+    orc_point_fn f;
+    void* user;
+  };
+  std::vector<PointFn> volume_fns;
+  std::vector<std::vector<std::pair<int, PointFn>>> fn_faces;  // per element: (local face, function)
   std::vector<int32_t> pl_dof;
   std::vector<double> pl_val;
   // inhomogeneous Dirichlet values u_D(lambda) = lambda * idbc_rate on constrained dofs (empty: none)
@@ -611,12 +618,31 @@ void element_internal(const orc_problem& p, int e, const double* u, bool wantK, 
   }
 }
 
-// Dead traction on the element's Neumann faces, 1-point rule (loads/traction.hh:105-138).
+// Dead traction on the element's Neumann faces, 1-point rule (loads/traction.hh:105-138): lambda t for the faces
+// with fixed values, f(X_quadrature point, lambda) for the faces with a function.
 void element_traction(const orc_problem& p, int e, double lambda, double f[ND], const double* u, double* energy) {
-  if (p.faces.empty() || p.faces[e].empty()) return;
+  const bool fixed_faces = !p.faces.empty() && !p.faces[e].empty();
+  const bool fn_faces = !p.fn_faces.empty() && !p.fn_faces[e].empty();
+  if (!fixed_faces && !fn_faces) return;
   double X[NN][3], ue[NN][3];
   gather(p, e, u, X, ue);
-  for (const auto& fc : p.faces[e]) {
+  std::vector<std::pair<int, std::array<double, 3>>> list;
+  if (fixed_faces)
+    for (const auto& fc : p.faces[e])
+      list.push_back({fc.first, {lambda * fc.second[0], lambda * fc.second[1], lambda * fc.second[2]}});
+  if (fn_faces)
+    for (const auto& ff : p.fn_faces[e]) {
+      const int d = ff.first / 2;
+      double xi[3] = {0.5, 0.5, 0.5};
+      xi[d] = (ff.first % 2) ? 1.0 : 0.0;
+      double N[NN], Xq[3] = {0, 0, 0}, t[3];
+      shape_values(xi, N);
+      for (int v = 0; v < NN; ++v)
+        for (int c = 0; c < 3; ++c) Xq[c] += N[v] * X[v][c];
+      ff.second.f(1, Xq, lambda, t, ff.second.user);
+      list.push_back({ff.first, {t[0], t[1], t[2]}});
+    }
+  for (const auto& fc : list) {
     const int lf = fc.first;
     const int d = lf / 2;
     double xi[3] = {0.5, 0.5, 0.5};
@@ -632,7 +658,7 @@ void element_traction(const orc_problem& p, int e, double lambda, double f[ND], 
     }
     const double cr[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
     const double dA = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
-    const double t[3] = {lambda * fc.second[0], lambda * fc.second[1], lambda * fc.second[2]};
+    const double t[3] = {fc.second[0], fc.second[1], fc.second[2]};
     if (f)
       for (int v = 0; v < NN; ++v)
         for (int c = 0; c < 3; ++c) f[3 * v + c] -= N[v] * t[c] * 1.0 * dA;
@@ -641,6 +667,32 @@ void element_traction(const orc_problem& p, int e, double lambda, double f[ND], 
       for (int v = 0; v < NN; ++v)
         for (int c = 0; c < 3; ++c) uv[c] += N[v] * ue[v][c];
       *energy -= (t[0] * uv[0] + t[1] * uv[1] + t[2] * uv[2]) * dA;
+    }
+  }
+}
+
+// VolumeLoad (loads/volume.hh:86-106): f_I -= N_I b(X(xi_q), lambda) w_q detJ(xi_q) over the element's Gauss rule,
+// energy -= u(xi_q) . b w_q detJ (:63-80).
+void element_volume_load(const orc_problem& p, int e, double lambda, double f[ND], const double* u, double* energy) {
+  if (p.volume_fns.empty()) return;
+  double X[NN][3], ue[NN][3];
+  gather(p, e, u, X, ue);
+  const Rule& R = gauss2();
+  for (int q = 0; q < 8; ++q) {
+    Geo g;
+    geometry(X, R.xi[q], g);
+    double N[NN], Xq[3] = {0, 0, 0}, uq[3] = {0, 0, 0};
+    shape_values(R.xi[q], N);
+    for (int v = 0; v < NN; ++v)
+      for (int c = 0; c < 3; ++c) Xq[c] += N[v] * X[v][c], uq[c] += N[v] * ue[v][c];
+    const double wdJ = R.w[q] * g.detJ;
+    for (const auto& vf : p.volume_fns) {
+      double b[3];
+      vf.f(1, Xq, lambda, b, vf.user);
+      if (f)
+        for (int v = 0; v < NN; ++v)
+          for (int c = 0; c < 3; ++c) f[3 * v + c] -= N[v] * b[c] * wdJ;
+      if (energy) *energy -= (uq[0] * b[0] + uq[1] * b[1] + uq[2] * b[2]) * wdJ;
     }
   }
 }
@@ -662,6 +714,7 @@ int element_vector(const orc_problem& p, int e, const double* u, double lambda, 
     }
   }
   element_traction(p, e, lambda, out, nullptr, nullptr);
+  element_volume_load(p, e, lambda, out, nullptr, nullptr);
   return ORC_OK;
 }
 
@@ -1070,6 +1123,21 @@ int orc_set_dirichlet_values(orc_problem* p, const double* rate) {
   p->idbc_rate.assign(rate, rate + p->ndof());
   return ORC_OK;
 }
+int orc_add_volume_load(orc_problem* p, orc_point_fn f, void* user) {
+  if (!p || !f) return ORC_ERR_ARG;
+  p->volume_fns.push_back({f, user});
+  return ORC_OK;
+}
+int orc_add_neumann_function(orc_problem* p, int nf, const int32_t* fe, const int32_t* fl, orc_point_fn f,
+                             void* user) {
+  if (!p || nf < 0 || !f || (nf > 0 && (!fe || !fl))) return ORC_ERR_ARG;
+  if (p->fn_faces.empty()) p->fn_faces.assign(p->ne, {});
+  for (int k = 0; k < nf; ++k) {
+    if (fe[k] < 0 || fe[k] >= p->ne || fl[k] < 0 || fl[k] > 5) return ORC_ERR_ARG;
+    p->fn_faces[fe[k]].push_back({fl[k], {f, user}});
+  }
+  return ORC_OK;
+}
 int orc_add_neumann(orc_problem* p, int nf, const int32_t* fe, const int32_t* fl, const double* t) {
   if (!p || nf < 0) return ORC_ERR_ARG;
   if (p->faces.empty()) p->faces.assign(p->ne, {});
@@ -1125,6 +1193,7 @@ int orc_element_energy(orc_problem* p, int e, const double* u, double lambda, do
   if (!eo.ok) return ORC_ERR_NONPOSITIVE_DETC;
   double en = eo.energy;
   element_traction(*p, e, lambda, nullptr, u, &en);
+  element_volume_load(*p, e, lambda, nullptr, u, &en);
   *energy = en;
   return ORC_OK;
 }

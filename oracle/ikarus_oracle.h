@@ -57,6 +57,13 @@ int orc_set_dirichlet(orc_problem* p, const uint8_t* fixed_dofs);
 int orc_set_dirichlet_values(orc_problem* p, const double* rate);
 int orc_add_neumann(orc_problem* p, int n_faces, const int32_t* face_elem, const int32_t* face_local,
                     const double* traction);
+/* loads given as functions: out[3k..3k+2] = f(X[3k..3k+2], lambda) for k < n */
+typedef void (*orc_point_fn)(int32_t n, const double* X, double lambda, double* out, void* user);
+/* VolumeLoad (loads/volume.hh:86-106): body force f(X, lambda) integrated with the element's Gauss rule */
+int orc_add_volume_load(orc_problem* p, orc_point_fn f, void* user);
+/* Neumann faces with a traction function f(X, lambda) evaluated at the face's quadrature point (the face centre) */
+int orc_add_neumann_function(orc_problem* p, int n_faces, const int32_t* face_elem, const int32_t* face_local,
+                             orc_point_fn f, void* user);
 /* Manipulator-style point loads: after the Dirichlet treatment, R[dof] += lambda * value. */
 int orc_add_point_loads(orc_problem* p, int n, const int32_t* dofs, const double* values);
 /* When set, the tangent moduli are recomputed for every (i,j) node pair of every Gauss point,

@@ -15,8 +15,8 @@ nu = 0.4999:
     agreement of two FP64 implementations (the pressure term carries lambda = 1.7e6 and the static condensation
     cancels lambda-sized terms): the oracle compiled with fused multiply-adds and the oracle compiled without them --
     two equally valid FP64 evaluations of one restatement -- already differ by up to 7.5e-11 on single element
-    matrices (the device, which fuses multiply-adds, differs from the oracle by the same amount on the same
-    element).  There every quantity is bounded by max(1e-12, 2 x that spread), measured here for the same state.
+    matrices (the device differs from the oracle by the same amount on the same element).  There every quantity is
+    bounded by max(1e-12, 2 x the spread of the two oracle builds), measured here for the same state.
 Each measured error is printed beside its bound (and logged by the parity_log fixture).
 """
 import numpy as np
@@ -169,7 +169,7 @@ def smooth_block_field(p, rng, scale):
 def test_config5_eas_block_state_update_element_and_assembly(ikr, parity_log, nu):
     p = problems.eas_block(nu=nu)
     o = oracle.from_problem(p)
-    of = oracle.from_problem(p, fused=True) if nu > 0.49 else None  # second valid FP64 evaluation
+    of = oracle.from_problem(p, unfused=True) if nu > 0.49 else None  # second valid FP64 evaluation
     rng = np.random.default_rng(23)
     du1 = smooth_block_field(p, rng, 2e-4)
     du2 = smooth_block_field(p, rng, 2e-5)
@@ -179,7 +179,7 @@ def test_config5_eas_block_state_update_element_and_assembly(ikr, parity_log, nu
     def bound(spread):  # FP64 floor of an ill-conditioned quantity: twice the spread of the two oracle builds
         if of is None:
             return FP64_RTOL
-        parity_log(f"config5 nu={nu}: oracle with vs without fused multiply-adds", spread, 1.0)
+        parity_log(f"config5 nu={nu}: oracle builds with vs without fused multiply-adds", spread, 1.0)
         return max(FP64_RTOL, 2.0 * spread)
 
     # alpha from the state update at the undeformed state with the increment du1 (updateStateImpl,

@@ -1,0 +1,73 @@
+"""Loads given as functions f(X, lambda) against the oracle's restatement: VolumeLoad (loads/volume.hh:86-106) at the
+element's Gauss points and neumannBoundaryLoad with a general traction function (loads/traction.hh:105-138), alone
+and together with the lambda-linear traction, for element vectors, energies, the assembled force vector at two load
+factors (the functions are re-evaluated when lambda changes) and a load path whose load is not linear in lambda."""
+import numpy as np
+import pytest
+
+import oracle
+from ikarus_gb300 import problems
+from ikarus_gb300.mesh import boundary_faces
+
+pytestmark = pytest.mark.gpu
+FP64_RTOL = 1e-12
+
+
+def rel_err(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(b).max(), 1e-300))
+
+
+def body(X, lam):
+    return np.stack([0.0 * X[:, 0], 0.1 * lam * np.sin(X[:, 0]), -lam ** 2 * (1.0 + X[:, 2])], axis=1)
+
+
+def top(X, lam):
+    return np.stack([0.2 * lam * X[:, 0], 0.0 * X[:, 0], -0.5 * lam ** 3 + 0.1 * X[:, 1]], axis=1)
+
+
+def with_function_loads(p, target):
+    target.add_volume_load(body)
+    fe, fl = boundary_faces(p.mesh, "z+")
+    target.add_neumann_function(fe, fl, top)
+
+
+@pytest.mark.parametrize("eas,n", [(0, 0), (1, 9)])
+def test_function_loads_match_oracle(ikr, eas, n, parity_log):
+    p = problems.cantilever(5, 3, 2, L=4.0, jitter=0.15, seed=4, eas=eas, n_eas=n)
+    fes, asm = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    with_function_loads(p, fes)
+    with_function_loads(p, o)
+    u = 0.01 * np.random.default_rng(3).standard_normal(p.n_dofs) * (1 - p.fixed)
+    for lam in (0.3, 0.8):
+        req = ikr.FERequirements(fes, u, lam)
+        ev = ikr.calculateVector(fes, req)
+        ref = np.array([o.element_vector(e, u, lam) for e in range(p.mesh.n_elems)])
+        assert parity_log(f"function loads eas={eas} lambda={lam}: element vectors", rel_err(ev, ref), FP64_RTOL)
+        R = asm.vector(req, dbc=ikr.DBCOption.Full)
+        assert parity_log(f"function loads eas={eas} lambda={lam}: assembled force", rel_err(R, o.assemble_vector(u, lam)),
+                          FP64_RTOL)
+        if eas == 0:
+            en = ikr.calculateScalar(fes, req)
+            ref_e = np.array([o.element_energy(e, u, lam) for e in range(p.mesh.n_elems)])
+            assert rel_err(en, ref_e) <= FP64_RTOL
+    fes.clear_volume_loads()
+    fes.clear_neumann()
+    assert not asm.vector(ikr.FERequirements(fes), dbc=ikr.DBCOption.Full).any()  # no load left, undeformed
+
+
+def test_load_path_with_loads_not_linear_in_lambda_matches_oracle(ikr, parity_log):
+    p = problems.cantilever(8, 2, 2, traction=(0.0, 0.0, -0.3), load_steps=4, tol=1e-10)
+    fes, asm = problems.build_gpu(p)
+    o = oracle.from_problem(p)
+    with_function_loads(p, fes)
+    with_function_loads(p, o)
+    ref = o.load_control(p.load_steps, tol=p.tol, max_iter=30)
+    req = ikr.FERequirements(fes)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(ikr.NRSettings(tol=p.tol, maxIter=30, linear_rtol=1e-13),
+                                                         ikr.LinearSolver(rtol=1e-13)))
+    info = ikr.LoadControl(nr, p.load_steps).run(req)
+    assert info.success
+    assert [s.iterations for s in info.solverInfos] == list(ref["iterations"])
+    assert parity_log("function loads load path: max|u - u_oracle| / max|u_oracle|",
+                      rel_err(req.globalSolution(), ref["u"]), 1e-8)
