@@ -471,7 +471,10 @@ def finish(args, p, world, t_mixed, t_e2e, t_plain, plain_info, infos, launches,
         {"s_per_load_path": round(t_plain, 4), "newton_iterations": plain_info.totalIterations,
          "cg_iterations": plain_info.totalLinearIterations},
         "mixed": {"newton_iterations": info0.totalIterations, "cg_iterations": info0.totalLinearIterations,
-                  "newton_per_step": newton, "max_rel_diff_vs_plain": rel_diff},
+                  "newton_per_step": newton, "max_rel_diff_vs_plain": rel_diff,
+                  "newton_iterations_as_cuda_graphs": mixed.nr.graph_iterations(),
+                  "fp32_tangent_kernel": {1: "coloured element kernel", 2: "row kernel",
+                                          3: "element blocks + gather"}.get(mixed.asm.tangent_kernel())},
         "speedup_vs_plain_fp64": None if t_plain is None else round(t_plain / t_mixed, 3),
         "e2e": {"value": round(t_e2e, 4), "unit": "s", "h2d_bytes_per_step": 8 * p.n_dofs,
                 "d2h_bytes_per_step": 8 * p.n_dofs},
@@ -483,6 +486,8 @@ def finish(args, p, world, t_mixed, t_e2e, t_plain, plain_info, infos, launches,
                      "cg_iterations_per_launch": round(iters_per_launch, 2), "algorithmic_bytes_per_cg_iteration": bpl,
                      "us_per_cg_iteration": round(spmv_ms * 1e3 / max(spmv_n, 1), 3),
                      "cg_kernel_kind": kind, "l2_keep_fraction": keep,
+                     "traffic_source": "ncu capture of the same kernel kind and L2 keep share, separate run "
+                                       "(profiles/cg_dram_traffic.json)" if traffic is not None else None,
                      "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback"},
         "clocks": clocks.summary(),
     }

@@ -116,7 +116,8 @@ class ControlMessages(enum.IntEnum):  # broadcastermessages.hh:18
 class _NRSettings(C.Structure):
     _fields_ = [("tol", C.c_double), ("max_iter", C.c_int32), ("min_iter", C.c_int32), ("tol_mode", C.c_int32),
                 ("forcing", C.c_int32), ("linear_rtol", C.c_double), ("linear_rtol_min", C.c_double),
-                ("linear_max_iter", C.c_int32), ("refinements", C.c_int32), ("max_backtracks", C.c_int32)]
+                ("linear_max_iter", C.c_int32), ("refinements", C.c_int32), ("max_backtracks", C.c_int32),
+                ("step_graphs", C.c_int32)]
 
 
 class _NRInfo(C.Structure):
@@ -195,6 +196,7 @@ SIGNATURES = {
     "ikr_assembler_add_point_loads": ([_vp, _I, _ip, _dp], C.c_int),
     "ikr_assembler_bind": ([_vp, _vp, _I], C.c_int),
     "ikr_assembler_add_matrix_entries": ([_vp, _I, _ip, _ip, _dp], C.c_int),
+    "ikr_assembler_set_dirichlet_function": ([_vp, _POINT_FN, _POINT_FN, _vp], C.c_int),
     "ikr_assembler_size": ([_vp, _ip], C.c_int),
     "ikr_assembler_reduced_size": ([_vp, _ip], C.c_int),
     "ikr_assembler_constraints_below": ([_vp, _ip], C.c_int),
@@ -216,6 +218,7 @@ SIGNATURES = {
     "ikr_newton_jacobian": ([_vp, _vp], C.c_int),
     "ikr_newton_update": ([_vp, _vp, _dp], C.c_int),
     "ikr_newton_subscribe_logger": ([_vp, _LOG_SINK, _vp], C.c_int),
+    "ikr_newton_graph_iterations": ([_vp, _i64p], C.c_int),
     "ikr_load_control_subscribe_logger": ([_vp, _LOG_SINK, _vp], C.c_int),
     "ikr_path_following_subscribe_logger": ([_vp, _LOG_SINK, _vp], C.c_int),
     "ikr_linear_solver_set_fp64_outer": ([_vp, _I, _D, _I, _I], C.c_int),
@@ -572,6 +575,13 @@ class SparseFlatAssembler:
         v = np.ascontiguousarray(values, dtype=np.float64)
         _err(lib().ikr_assembler_add_point_loads(self.h, len(d), _ptr(d, C.c_int32), _ptr(v)), "point loads")
 
+    def set_dirichlet_function(self, value, derivative):
+        """storeInhomogeneousBoundaryCondition(f): value(X (n, 3), lambda) -> prescribed displacements at every node
+        (nonzero entries are imposed), derivative(X, lambda) -> their lambda-derivative (used at lambda = 1)."""
+        cv, cd = _point_fn(value), _point_fn(derivative)
+        self._dirichlet_cbs = (cv, cd)
+        _err(lib().ikr_assembler_set_dirichlet_function(self.h, cv, cd, None), "set_dirichlet_function")
+
     def add_matrix_entries(self, rows, cols, values):
         """AssemblerManipulator matrix hook: K(row, col) += value after every assembly (springs)."""
         r = np.ascontiguousarray(rows, dtype=np.int32)
@@ -611,7 +621,8 @@ class SparseFlatAssembler:
         return req, DBCOption(self._dbc if dbc is None else dbc)
 
     def set_tangent_kernel(self, path=0):
-        """FP32 displacement-based NeoHooke tangent: 1 coloured element kernel, 2 row kernel, 0 timed choice."""
+        """FP32 displacement-based tangent: 1 coloured element kernel, 2 row kernel, 3 element blocks + gather, 0 timed
+        choice."""
         _err(lib().ikr_assembler_set_tangent_kernel(self.h, int(path)))
 
     def tangent_kernel(self):
@@ -929,11 +940,12 @@ class NRSettings:
     linear_max_iter: int = 100000
     refinements: int = 0
     backtracks: int = 0           # halve a correction that inverts an element (the reference aborts)
+    step_graphs: bool = True      # each Newton iteration as one CUDA graph launch where the configuration allows it
 
     def _c(self):
         return _NRSettings(self.tol, self.maxIter, self.minIter, int(self.relative), int(self.eisenstat_walker),
                            self.linear_rtol, self.linear_rtol_min, self.linear_max_iter, self.refinements,
-                           self.backtracks)
+                           self.backtracks, int(self.step_graphs))
 
 
 @dataclass
@@ -988,6 +1000,12 @@ class NewtonRaphson:
 
     def subscribe_fe_state(self, on=True):
         _err(lib().ikr_newton_subscribe_fe_state(self.h, int(on)))
+
+    def graph_iterations(self):
+        """Newton iterations run as one CUDA graph launch each since creation (NRSettings.step_graphs)."""
+        n = C.c_int64()
+        _err(lib().ikr_newton_graph_iterations(self.h, C.byref(n)))
+        return n.value
 
     def residual(self):
         """residual() (newtonraphson.hh:260-268): f(req) -> force vector with the Full Dirichlet treatment."""

@@ -36,8 +36,12 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
   constexpr bool WANT_K = MODE & kWantK;
   constexpr bool WANT_E = MODE & kWantEnergy;
   constexpr bool ELEM_OUT = MODE & kElemOut;
+  constexpr bool BLOCKS = MODE & kElemBlocks;
   static_assert(!(WANT_R || WANT_E) || std::is_same<KT, double>::value, "residual and energy are FP64");
+  static_assert(!BLOCKS || (WANT_K && std::is_same<KT, float>::value), "element blocks: FP32 tangent only");
   __shared__ KT sh[EPB][8][6];
+  // element blocks: staged per warp (4 elements x 36 blocks x 9 entries) and copied out with 16-byte stores
+  __shared__ __align__(16) KT stage[BLOCKS ? EPB / 4 : 1][BLOCKS ? 4 * kElemBlockCount * 9 : 1];
 
   const int lane = threadIdx.x & 31;
   const int sub = threadIdx.x & 7;
@@ -282,8 +286,9 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const double tv = a.trac[24 * t + 3 * sub + c];
-          f[c] -= a.load_factor * tv;
-          if (WANT_E) psi -= a.load_factor * tv * Ud[c];
+          const double lf = a.load_factor_dev ? *a.load_factor_dev : a.load_factor;
+          f[c] -= lf * tv;
+          if (WANT_E) psi -= lf * tv * Ud[c];
         }
       }
     }
@@ -315,7 +320,24 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
         if (!((fmaskI >> c) & 1)) a.R[3 * node + c] += f[c];
     }
   }
-  if (WANT_K) {
+  if constexpr (BLOCKS) {
+    // lane I's blocks (I, I + d), d = 0..3, and (I, I + 4) for I < 4, into the warp's stage, then the element's 324
+    // values to blk[e] (8 lanes, 16 bytes each per store)
+    KT* st = stage[threadIdx.x >> 5] + (es & 3) * (kElemBlockCount * 9);
+#pragma unroll
+    for (int d = 0; d < 5; ++d) {
+      if (d == 4 && sub >= 4) break;
+      const int pb = d < 4 ? 8 * d + sub : 32 + sub;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) st[pb * 9 + 3 * i + j] = Kacc[d][i][j];
+    }
+    __syncwarp(0xFFu << (lane & ~7));
+    const float4* src4 = reinterpret_cast<const float4*>(st);
+    float4* dst4 = reinterpret_cast<float4*>(static_cast<float*>(a.blk) + (size_t)e * (kElemBlockCount * 9));
+    for (int k = sub; k < kElemBlockCount * 9 / 4; k += 8) dst4[k] = src4[k];
+  } else if (WANT_K) {
     if (ELEM_OUT) {
       double* out = a.elem_mat + 576 * (size_t)li;
 #pragma unroll
@@ -654,7 +676,8 @@ __global__ void __launch_bounds__(EPB * 8) disp_residual_gp_kernel(ElemArgs a, c
     const int t = a.trac_idx[e];
     if (t >= 0) {
 #pragma unroll
-      for (int c = 0; c < 3; ++c) f[c] -= a.load_factor * a.trac[24 * t + 3 * sub + c];
+      for (int c = 0; c < 3; ++c)
+        f[c] -= (a.load_factor_dev ? *a.load_factor_dev : a.load_factor) * a.trac[24 * t + 3 * sub + c];
     }
   }
   if (a.ext) {
@@ -785,6 +808,80 @@ __global__ void stress_at_kernel(ElemArgs a, int e0, int count, const double* __
   o[0] = R[0][0], o[1] = R[1][1], o[2] = R[2][2], o[3] = R[1][2], o[4] = R[0][2], o[5] = R[0][1];
 }
 
+// inverse of the element-to-block map, counted per padded block, filled and sorted per block
+__global__ void tangent_inv_count_kernel(const int32_t* __restrict__ slot, int64_t n, int32_t* __restrict__ cnt) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t < n) atomicAdd(&cnt[slot[t]], 1);
+}
+__global__ void tangent_inv_fill_kernel(const int32_t* __restrict__ slot, int ne, const int32_t* __restrict__ ptr,
+                                        int32_t* __restrict__ cursor, int32_t* __restrict__ inv) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= 64LL * ne) return;
+  const int pair = (int)(t / ne), e = (int)(t % ne);
+  const int b = slot[t];
+  const int code = tangent_block_code(pair >> 3, pair & 7);
+  inv[ptr[b] + atomicAdd(&cursor[b], 1)] = ((e * kElemBlockCount + (code >> 1)) << 1) | (code & 1);
+}
+__global__ void tangent_inv_sort_kernel(const int32_t* __restrict__ ptr, int32_t* __restrict__ inv, int64_t n) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  const int c0 = ptr[b], c1 = ptr[b + 1];
+  for (int i = c0 + 1; i < c1; ++i) {  // at most 8 entries: insertion sort, ascending
+    const int v = inv[i];
+    int j = i - 1;
+    while (j >= c0 && inv[j] > v) {
+      inv[j + 1] = inv[j];
+      --j;
+    }
+    inv[j + 1] = v;
+  }
+}
+
+// One thread per padded block: the sum of its element blocks in ascending order, the Full Dirichlet treatment, and
+// the nine entries written to the entry-interleaved slice (a warp writes 9 x 128 contiguous bytes).
+__global__ void __launch_bounds__(256) tangent_gather_kernel(Bsr A, const int32_t* __restrict__ gslice,
+                                                             const int32_t* __restrict__ ptr,
+                                                             const int32_t* __restrict__ inv,
+                                                             const float* __restrict__ blk,
+                                                             const uint8_t* __restrict__ nf, float* __restrict__ val) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= A.n_padded) return;
+  const int g = (int)(b >> 5), l = (int)(b & 31);
+  const int row = 32 * gslice[g] + l;
+  float acc[9];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) acc[k] = 0.f;
+  const int c0 = ptr[b], c1 = ptr[b + 1];
+  for (int c = c0; c < c1; ++c) {
+    const int code = __ldg(inv + c);
+    const float* src = blk + (size_t)(code >> 1) * 9;
+    float v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = __ldg(src + k);
+    if (code & 1) {
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) acc[3 * i + j] += v[3 * j + i];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc[k] += v[k];
+    }
+  }
+  uint8_t fr = 0, fc = 0;
+  const int col = A.col_sell[b];
+  if (nf && c1 > c0) fr = nf[row], fc = nf[col];
+  float* out = val + (size_t)g * 288 + l;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float v = acc[3 * i + j];
+      if (((fr >> i) | (fc >> j)) & 1) v = (row == col && i == j) ? 1.f : 0.f;  // getMatrixImpl's Full treatment
+      out[32 * (3 * i + j)] = v;
+    }
+}
+
 template <typename KT, int MODE, int EPB, int MAT = 0>
 void launch_disp_epb(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
   const int blocks = (n_list + EPB - 1) / EPB;
@@ -828,8 +925,26 @@ void launch_disp_element(const ElemArgs& a, int mode, bool fp32_tangent, const i
       else launch_disp_t<double, kWantK | kElemOut>(a, list, n_list, e_base, s);
       break;
     case kWantEnergy | kElemOut: launch_disp_t<double, kWantEnergy | kElemOut>(a, list, n_list, e_base, s); break;
+    case kWantK | kElemBlocks: launch_disp_t<float, kWantK | kElemBlocks>(a, list, n_list, e_base, s); break;
     default: break;
   }
+}
+
+void launch_tangent_inverse_count(const int32_t* slot, int n_elems, int32_t* cnt, cudaStream_t s) {
+  const int64_t n = 64LL * n_elems;
+  if (n > 0) tangent_inv_count_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(slot, n, cnt);
+}
+void launch_tangent_inverse_fill(const int32_t* slot, int n_elems, const int32_t* ptr, int32_t* cursor, int32_t* inv,
+                                 int64_t n_padded, cudaStream_t s) {
+  const int64_t n = 64LL * n_elems;
+  if (n > 0) tangent_inv_fill_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(slot, n_elems, ptr, cursor, inv);
+  if (n_padded > 0) tangent_inv_sort_kernel<<<(unsigned)((n_padded + 255) / 256), 256, 0, s>>>(ptr, inv, n_padded);
+}
+void launch_tangent_gather(const Bsr& A, const int32_t* gslice, const int32_t* inv_ptr, const int32_t* inv,
+                           const float* blk, const uint8_t* node_fixed, float* val, cudaStream_t s) {
+  if (A.n_padded > 0)
+    tangent_gather_kernel<<<(unsigned)((A.n_padded + 255) / 256), 256, 0, s>>>(A, gslice, inv_ptr, inv, blk,
+                                                                              node_fixed, val);
 }
 
 void launch_stress_at(const ElemArgs& a, int e0, int count, const double* xi, bool xi_per_elem, int type, double* out,

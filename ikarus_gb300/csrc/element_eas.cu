@@ -600,7 +600,8 @@ __global__ void __launch_bounds__(EasCfg<NA>::EPB * 8) eas_element_kernel(ElemAr
       const int t = a.trac_idx[e];
       if (t >= 0)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) f[c] -= a.load_factor * a.trac[24 * t + 3 * sub + c];
+        for (int c = 0; c < 3; ++c)
+          f[c] -= (a.load_factor_dev ? *a.load_factor_dev : a.load_factor) * a.trac[24 * t + 3 * sub + c];
     }
     if (a.ext) {
 #pragma unroll

@@ -105,15 +105,19 @@ static int choose_epb(ikr_fes f, Pass pass) {
   return best;
 }
 
-void assemble_vector(ikr_asm a, ikr_req r, int dbc) {
+void assemble_vector(ikr_asm a, ikr_req r, int dbc, bool sync) {
   ikr_fes f = a->fes;
-  f->refresh_tractions();
-  f->refresh_function_loads(r->lambda);
+  if (!sync && !(f->epb_r > 0)) fail(IKR_ERR_INVALID_STATE, "residual kernel not tuned before capture");
+  if (sync) {
+    f->refresh_tractions();
+    f->refresh_function_loads(r->lambda);
+  }
   a->R.alloc(a->n);
   CK(cudaMemsetAsync(a->R.p, 0, sizeof(double) * a->n, f->stream));
   ikr::ElemArgs args = f->args();
   args.u = r->u.p;
   args.load_factor = r->lambda;
+  args.load_factor_dev = sync ? nullptr : f->capture_lambda;
   args.node_fixed = (dbc == IKR_DBC_RAW) ? nullptr : a->node_fixed.p;
   args.R = a->R.p;
   if (!f->epb_r) {
@@ -128,24 +132,26 @@ void assemble_vector(ikr_asm a, ikr_req r, int dbc) {
   }
   args.epb = f->epb_r;
   f->launch_coloured(args, ikr::kWantR, false);
-  ikr::launch_vector_finish(a->R.p, nullptr, f->nn, a->pl_dof.p, a->pl_val.p, (int)a->pl_dof.n, r->lambda, f->stream);
+  ikr::launch_vector_finish(a->R.p, nullptr, f->nn, a->pl_dof.p, a->pl_val.p, (int)a->pl_dof.n, r->lambda, f->stream,
+                            args.load_factor_dev);
   if (a->pl_dof.n) count(1);
   a->vector_dbc = dbc;
   if (f->na > 0) f->eas_cache_key = cache_key(r, f);
-  f->check_status();
+  if (sync) f->check_status();
 }
 
-static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc);
+static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc, bool sync);
 
 // The tangent in the assembler's precision; an FP32 tangent with an FP64 twin (dual64) is assembled in FP64 and
-// rounded to FP32 once, so the FP32 CG and the FP64 outer solve see the same tangent.
-void assemble_matrix(ikr_asm a, ikr_req r, int dbc) {
+// rounded to FP32 once, so the FP32 CG and the FP64 outer solve see the same tangent.  sync = false (stream capture):
+// no tuning, no status check.
+void assemble_matrix(ikr_asm a, ikr_req r, int dbc, bool sync) {
   if (a->fp32 && a->dual64) {
     if (!a->nb) a->build_pattern();
     a->val64.alloc(9 * (size_t)a->npad);
     a->fp32 = false;
     try {
-      assemble_matrix_into(a, r, dbc);
+      assemble_matrix_into(a, r, dbc, sync);
     } catch (...) {
       a->fp32 = true;
       throw;
@@ -156,16 +162,17 @@ void assemble_matrix(ikr_asm a, ikr_req r, int dbc) {
     a->k64_stamp = ++a->k_stamp;
     return;
   }
-  assemble_matrix_into(a, r, dbc);
+  assemble_matrix_into(a, r, dbc, sync);
   ++a->k_stamp;
 }
 
-static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc) {
+static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc, bool sync) {
   ikr_fes f = a->fes;
   if (!a->nb) a->build_pattern();
+  const bool timed_path = a->fp32 && f->na == 0;  // the FP32 displacement tangent chooses its kernel by timing
+  if (!sync && !((a->fp32 ? f->epb_k32 : f->epb_k64) > 0 && (!timed_path || a->tan_path > 0)))
+    fail(IKR_ERR_INVALID_STATE, "tangent kernels not tuned before capture");
   const uint8_t* nf = (dbc == IKR_DBC_RAW) ? nullptr : a->node_fixed.p;
-  ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
-  count(nf ? 1 : 0);
   ikr::ElemArgs args = f->args();
   args.u = r->u.p;
   args.load_factor = r->lambda;
@@ -184,21 +191,34 @@ static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc) {
     ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
   }
   args.epb = epb_k;
-  // FP32 displacement-based NeoHooke: the coloured element kernel or the row kernel, whichever is faster
-  const bool row_ok = a->fp32 && f->na == 0 && f->material == 0 && f->n_inst == 0;
-  if (row_ok && a->tan_req) a->tan_path = a->tan_req;
-  if (row_ok && !a->tan_path) {
+  // FP32 displacement-based tangent: the coloured element kernel, the row kernel (NeoHooke on one element set) or
+  // element blocks + gather, whichever is fastest
+  const bool blocks_ok = a->fp32 && f->na == 0;
+  const bool row_ok = blocks_ok && f->material == 0 && f->n_inst == 0;
+  auto element_blocks = [&]() {
+    a->build_gather_map();
+    ikr::ElemArgs t = args;
+    t.blk = a->eblk.p;
+    f->launch_elements(t, ikr::kWantK | ikr::kElemBlocks, true, nullptr, f->ne, 0);
+    ikr::launch_tangent_gather(a->bsr(), a->gslice.p, a->inv_ptr.p, a->inv_idx.p, a->eblk.p, nf,
+                               static_cast<float*>(a->values()), f->stream);
+    count(1);
+  };
+  if (blocks_ok && a->tan_req && (a->tan_req != 2 || row_ok)) a->tan_path = a->tan_req;
+  if (blocks_ok && !a->tan_path) {
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     float best = 1e30f;
-    for (int path : {1, 2}) {
+    for (int path : {1, 2, 3}) {
+      if (path == 2 && !row_ok) continue;
       float t = 1e30f;
       for (int rep = 0; rep < 2; ++rep) {
         ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
         CK(cudaEventRecord(e0, f->stream));
         if (path == 1) f->launch_coloured(args, ikr::kWantK, true);
-        else ikr::launch_row_tangent(args, a->ne_ptr.p, a->ne_elems.p, f->stream);
+        else if (path == 2) ikr::launch_row_tangent(args, a->ne_ptr.p, a->ne_elems.p, f->stream);
+        else element_blocks();
         CK(cudaEventRecord(e1, f->stream));
         CK(cudaEventSynchronize(e1));
         float ms = 0.f;
@@ -212,18 +232,25 @@ static void assemble_matrix_into(ikr_asm a, ikr_req r, int dbc) {
     cudaEventDestroy(e1);
     ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
   }
-  if (row_ok && a->tan_path == 2) {
-    ikr::launch_row_tangent(args, a->ne_ptr.p, a->ne_elems.p, f->stream);
-    count(1);
+  if (blocks_ok && a->tan_path == 3) {
+    element_blocks();  // writes every entry of every slice, Dirichlet treatment included: no reset
   } else {
-    f->launch_coloured(args, ikr::kWantK, a->fp32);
+    // zero values, unit diagonal of the constrained dofs (Full), then the read-modify-write assembly
+    ikr::launch_bsr_reset(a->values(), a->fp32, a->npad, a->diag.p, nf, f->nn, f->stream);
+    count(1);
+    if (row_ok && a->tan_path == 2) {
+      ikr::launch_row_tangent(args, a->ne_ptr.p, a->ne_elems.p, f->stream);
+      count(1);
+    } else {
+      f->launch_coloured(args, ikr::kWantK, a->fp32);
+    }
   }
   if (a->me_idx.n) {  // AssemblerManipulator matrix hooks run after the Dirichlet treatment
     ikr::launch_add_entries(a->values(), a->fp32, a->me_idx.p, a->me_val.p, (int)a->me_idx.n, f->stream);
     count(1);
   }
   a->matrix_dbc = dbc;
-  f->check_status();
+  if (sync) f->check_status();
 }
 
 void ensure_eas_cache(ikr_fes f, ikr_req r) {
@@ -941,9 +968,26 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
     ls->set_launch(use_graphs != 0, chunk_len);
   });
 }
+int ikr_assembler_set_dirichlet_function(ikr_asm a, ikr_point_fn value, ikr_point_fn derivative, void* user) {
+  return guarded([&] {
+    need(a && value && derivative, IKR_ERR_ARG, "null argument");
+    need(a->fes->n_inst == 0, IKR_ERR_NOT_IMPLEMENTED, "the batched solve has no inhomogeneous Dirichlet values");
+    std::vector<double> rate(a->n, 0.0);
+    derivative(a->fes->nn, a->fes->X_h.data(), 1.0, rate.data(), user);
+    for (double v : rate) need(std::isfinite(v), IKR_ERR_ARG, "non-finite Dirichlet derivative");
+    a->idbc_rate.upload(rate.data(), a->n, a->fes->stream);
+    CK(cudaStreamSynchronize(a->fes->stream));
+    a->idbc_value = value;
+    a->idbc_user = user;
+    a->idbc_vals_valid = false;
+    a->has_idbc = true;
+  });
+}
 int ikr_assembler_set_dirichlet_values(ikr_asm a, const double* rate) {
   return guarded([&] {
     need(a, IKR_ERR_ARG, "null argument");
+    a->idbc_value = nullptr;
+    a->idbc_vals_valid = false;
     if (!rate) {
       a->has_idbc = false;
       a->idbc_rate.release();
@@ -985,7 +1029,8 @@ int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t kind, double keep) {
 }
 int ikr_assembler_set_tangent_kernel(ikr_asm a, int32_t path) {
   return guarded([&] {
-    need(a && path >= 0 && path <= 2, IKR_ERR_ARG, "tangent kernel: 0 timed choice, 1 coloured, 2 rows");
+    need(a && path >= 0 && path <= 3, IKR_ERR_ARG,
+         "tangent kernel: 0 timed choice, 1 coloured, 2 rows, 3 element blocks + gather");
     a->tan_req = path;
     a->tan_path = path;
   });
@@ -1098,6 +1143,7 @@ int ikr_nr_settings_default(ikr_nr_settings* s) {
     s->linear_max_iter = 100000;
     s->refinements = 0;
     s->max_backtracks = 0;
+    s->step_graphs = 1;
   });
 }
 int ikr_newton_create(ikr_nr* out, ikr_asm a, ikr_ls ls, const ikr_nr_settings* st) {
@@ -1330,6 +1376,20 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
 
 // the inhomogeneous Dirichlet values at the requirement's load factor (nonlinearsolverfactory.hh:45-52)
 void idbc_sync(ikr_asm a, ikr_req r) {
+  if (a->idbc_value) {  // the value function at this load factor; entries that are nonzero are imposed
+    if (!a->idbc_vals_valid || a->idbc_vals_lambda != r->lambda) {
+      std::vector<double> v(a->n, 0.0);
+      a->idbc_value(a->fes->nn, a->fes->X_h.data(), r->lambda, v.data(), a->idbc_user);
+      a->idbc_vals.upload(v.data(), v.size(), a->fes->stream);
+      CK(cudaStreamSynchronize(a->fes->stream));
+      a->idbc_vals_lambda = r->lambda;
+      a->idbc_vals_valid = true;
+    }
+    ikr::launch_idbc_sync(r->u.p, a->idbc_vals.p, 1.0, 3LL * a->fes->nn, a->fes->stream);
+    count(1);
+    r->version++;
+    return;
+  }
   ikr::launch_idbc_sync(r->u.p, a->idbc_rate.p, r->lambda, 3LL * a->fes->nn, a->fes->stream);
   count(1);
   r->version++;
@@ -1384,11 +1444,6 @@ void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double 
   int64_t lin = 0;
   while ((rnorm > thr && iter < st.max_iter) || iter < st.min_iter) {
     notify(IKR_NLS_ITERATION_STARTED);
-    if (!k_valid) {
-      assemble_matrix(a, r, IKR_DBC_FULL);
-      k_valid = true;
-    }
-    nr->ls->factorize(a);
     // linear tolerance: fixed, or Eisenstat-Walker (choice 2) bounded by the accuracy this step needs
     double eta = st.linear_rtol;
     if (st.forcing == 1) {
@@ -1398,6 +1453,33 @@ void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double 
       eta = std::max(std::max(ew, need_eta), st.linear_rtol_min);
       eta = std::min(eta, st.linear_rtol);
     }
+    if (nr->ls->direct) eta = std::min(eta, nr->ls->rtol);
+    // the whole iteration as one CUDA graph launch where the configuration allows it (newton_graph.cpp)
+    if (!k_valid && step_graph_eligible(nr, r)) {
+      double cnorm = 0.0, rnew = 0.0;
+      const int64_t its = step_graph_iteration(nr, r, eta, &cnorm, &rnew);
+      if (its >= 0) {
+        lin += its;
+        inf.correction_norm = cnorm;
+        notify(IKR_NLS_CORRECTION_UPDATED);
+        notify(IKR_NLS_CORRECTIONNORM_UPDATED);
+        notify(IKR_NLS_SOLUTION_CHANGED);
+        rprev = rnorm;
+        rnorm = rnew;
+        inf.residual_norm = rnorm;
+        notify(IKR_NLS_RESIDUALNORM_UPDATED);
+        ++iter;
+        inf.iterations = iter;
+        notify(IKR_NLS_ITERATION_ENDED);
+        if (!std::isfinite(rnorm)) break;
+        continue;
+      }
+    }
+    if (!k_valid) {
+      assemble_matrix(a, r, IKR_DBC_FULL);
+      k_valid = true;
+    }
+    nr->ls->factorize(a);
     ikr::launch_scale64(nr->rhs.p, a->R.p, -1.0, n, f->stream);
     count(1);
     lin += nr->ls->solve(a, nr->rhs.p, nr->corr.p, eta, st.linear_max_iter, st.refinements);

@@ -147,6 +147,8 @@ struct ikr_fes_s {
   DBuf<double> ext;
   bool ext_dirty = false;
   double ext_lambda = 0.0;
+  // while a Newton iteration is captured as a graph: the device scalar its residual launches read the load factor from
+  const double* capture_lambda = nullptr;
   DBuf<int> status;
   DBuf<double> scratch_out;  // element-level outputs
   DBuf<double> lam_e, mu_e;  // per-element Lame parameters (empty: lam / mu everywhere)
@@ -309,15 +311,50 @@ struct ikr_asm_s {
   std::vector<uint8_t> fixed_h;
   std::vector<int32_t> cb_h;
   DBuf<uint8_t> node_fixed;
-  // inhomogeneous Dirichlet values u_D(lambda) = lambda * idbc_rate on constrained dofs (empty: none)
-  DBuf<double> idbc_rate, idbc_force;
+  // inhomogeneous Dirichlet values u_D(lambda) = lambda * idbc_rate on constrained dofs (empty: none); with a value
+  // function (idbc_value), u_D(lambda) = idbc_value(X_node, lambda) at every node, evaluated on the host for each new
+  // load factor into idbc_vals, and idbc_rate its lambda-derivative at 1 (the IDBC forces)
+  DBuf<double> idbc_rate, idbc_force, idbc_vals;
   bool has_idbc = false;
+  ikr_point_fn idbc_value = nullptr;
+  void* idbc_user = nullptr;
+  double idbc_vals_lambda = 0.0;
+  bool idbc_vals_valid = false;
   // pattern
   int64_t nb = 0, npad = 0;
   int nslices = 0;
   DBuf<int32_t> ne_ptr, ne_elems;  // elements of every node, ascending (row-tangent kernel)
-  // FP32 tangent kernel: 0 = not chosen yet, 1 = coloured element kernel, 2 = row kernel; req = forced choice
+  // FP32 tangent kernel: 0 = not chosen yet, 1 = coloured element kernel, 2 = row kernel, 3 = element blocks +
+  // gather; req = forced choice
   int tan_path = 0, tan_req = 0;
+  // element blocks + gather: the FP32 blocks of every element, the inverse element-to-block map, the slice of every
+  // block column group
+  DBuf<float> eblk;
+  DBuf<int32_t> inv_ptr, inv_idx, gslice;
+  void build_gather_map() {
+    if (inv_idx.p) return;
+    ikr_fes f = fes;
+    cudaStream_t s = f->stream;
+    if (64LL * f->ne * ikr::kElemBlockCount * 2 >= (1LL << 31))
+      fail(IKR_ERR_NOT_IMPLEMENTED, "element-block tangent: too many elements for 32-bit block codes");
+    DBuf<int32_t> cnt, cursor;
+    cnt.alloc(npad);
+    cursor.alloc(npad);
+    CK(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * npad, s));
+    CK(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * npad, s));
+    ikr::launch_tangent_inverse_count(slot.p, f->ne, cnt.p, s);
+    inv_ptr.alloc(npad + 1);
+    ikr::launch_exclusive_scan(cnt.p, inv_ptr.p, (int)npad, s);
+    inv_idx.alloc(64LL * f->ne);
+    ikr::launch_tangent_inverse_fill(slot.p, f->ne, inv_ptr.p, cursor.p, inv_idx.p, npad, s);
+    count(4);
+    std::vector<int32_t> gs(npad / 32);
+    for (int sl = 0; sl < nslices; ++sl)
+      for (int g = slice_off_h[sl]; g < slice_off_h[sl + 1]; ++g) gs[g] = sl;
+    gslice.upload(gs.data(), gs.size(), s);
+    eblk.alloc((size_t)f->ne * ikr::kElemBlockCount * 9);
+    CK(cudaStreamSynchronize(s));
+  }
   DBuf<int32_t> row_ptr, col, diag, slot, slice_off, col_sell;
   std::vector<int32_t> row_ptr_h, col_h, slice_off_h;
   DBuf<double> val64;
@@ -1127,10 +1164,29 @@ struct ControlObserver {
   void* user;
 };
 
+// One Newton iteration captured as a CUDA graph (newton_graph.cpp): tangent assembly, block-Jacobi inverse, the
+// persistent CG, update, residual assembly and both norms; the host writes the CG tolerance and the load factor into
+// `host` before a launch and reads the norms, the CG scalars and the element status from it after.
+struct NewtonStepGraph {
+  cudaGraphExec_t exec = nullptr;
+  std::vector<const void*> key;  // what the captured launches depend on; a change recaptures
+  int64_t launches = 0;          // kernel launches per graph launch
+  bool unsupported = false;      // the capture failed (then the iterations run launch by launch)
+  double* host = nullptr;        // pinned: [0] rtol, [1] lambda, [2] |corr|, [3] |R|, [4 ..] CG scalars, then status
+  DBuf<double> dev;              // [0] rtol, [1] lambda, [2] |corr|, [3] |R|
+  DBuf<double> part;             // partial sums of the two norms
+  ~NewtonStepGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (host) cudaFreeHost(host);
+  }
+};
+
 struct ikr_nr_s {
   ikr_asm asm_ = nullptr;
   ikr_ls ls = nullptr;
   ikr_nr_settings st{};
+  std::unique_ptr<NewtonStepGraph> step_graph;
+  int64_t graph_iterations = 0;  // Newton iterations run as graph launches since creation
   std::vector<Observer> obs;
   std::vector<std::unique_ptr<ListenerBase>> listeners;
   bool fe_state = false;
@@ -1199,11 +1255,17 @@ void predictor_end_step(ikr_lc lc, ikr_req r, int step);
 void need(bool c, int code, const char* msg);
 double device_norm(ikr_fes f, const double* x, int64_t n, DBuf<double>& part, DBuf<double>& out);
 double device_dot(ikr_fes f, const double* x, const double* y, int64_t n, DBuf<double>& part, DBuf<double>& out);
-void assemble_vector(ikr_asm a, ikr_req r, int dbc);
-void assemble_matrix(ikr_asm a, ikr_req r, int dbc);
+// sync = false: capture-safe (the kernels were tuned before; no status read, no host callback)
+void assemble_vector(ikr_asm a, ikr_req r, int dbc, bool sync = true);
+void assemble_matrix(ikr_asm a, ikr_req r, int dbc, bool sync = true);
 void update_state(ikr_fes f, ikr_req r, const double* corr_dev);
 // syncParameterAndGlobalSolution: u = lambda * rate where that value is nonzero
 void idbc_sync(ikr_asm a, ikr_req r);
+// Newton iterations as CUDA graphs (newton_graph.cpp): whether this solve's configuration allows it, and one
+// iteration (tangent at u, solve to rtol, u += correction, residual at u); returns the CG iterations, -1 when the
+// capture was refused (the iteration then runs launch by launch)
+bool step_graph_eligible(ikr_nr nr, ikr_req r);
+int64_t step_graph_iteration(ikr_nr nr, ikr_req r, double rtol, double* corr_norm, double* res_norm);
 // ControlLogger (operators.cpp): a listener and the control observer that feeds it
 std::unique_ptr<ListenerBase> make_control_logger(ikr_log_sink sink, void* user, ControlObserver* obs);
 // Newton-Raphson solve (newtonraphson.hh:193-257); ref_norm > 0 replaces the initial residual norm as the

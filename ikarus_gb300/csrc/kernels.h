@@ -11,6 +11,7 @@ enum ElemMode : int {
   kWantK = 2,       // tangent (FP64 or FP32 arithmetic, see KT)
   kWantEnergy = 4,  // stored energy (FP64, displacement-based only)
   kElemOut = 8,     // write element-level outputs instead of assembling
+  kElemBlocks = 16, // with kWantK: write each element's 36 distinct 3x3 blocks to ElemArgs::blk (gathered afterwards)
 };
 
 enum StatusBits : int {
@@ -37,6 +38,7 @@ struct ElemArgs {
   // current load factor (not scaled by it); nullptr = none
   const double* ext = nullptr;
   double load_factor = 0;
+  const double* load_factor_dev = nullptr;  // when set, the load factor is read here (launches captured in a graph)
   // EAS
   int eas_kind = 0, n_alpha = 0;
   const double* alpha = nullptr;   // n_alpha x n_elems (parameter-major)
@@ -52,6 +54,9 @@ struct ElemArgs {
   double* elem_energy = nullptr;   // element-level: 1 per listed element
   int* status = nullptr;           // StatusBits, OR-ed
   int epb = 32;                    // displacement element kernel: elements per block (16, 32 or 64)
+  // kElemBlocks: 36 blocks x 9 entries per element, element-major; block p = 8 d + I holds (I, I + d mod 8) for
+  // d = 0..3, block 32 + I holds (I, I + 4) for I = 0..3 (tangent_block_code maps a corner pair to its block)
+  void* blk = nullptr;
   // batched solves: the status of an element goes to its instance, inst_status[elem_inst[e]], instead
   const int32_t* elem_inst = nullptr;
   int* inst_status = nullptr;
@@ -83,6 +88,22 @@ void launch_disp_element(const ElemArgs& a, int mode, bool fp32_tangent, const i
                          cudaStream_t s);
 void launch_eas_element(const ElemArgs& a, int mode, bool fp32_tangent, const int32_t* list, int n_list, int e_base,
                         cudaStream_t s);
+// the element's stored block of corner pair (I, J) for kElemBlocks, as (index p << 1) | transposed
+__host__ __device__ __forceinline__ int tangent_block_code(int I, int J) {
+  const int d = (J - I) & 7;
+  if (d < 4) return (8 * d + I) << 1;
+  if (d == 4) return I < 4 ? ((32 + I) << 1) : (((32 + J) << 1) | 1);
+  return ((8 * (8 - d) + J) << 1) | 1;  // (J, I) is stored, transposed
+}
+constexpr int kElemBlockCount = 36;
+// gathered FP32 tangent assembly (element.cu): inverse of the element-to-block map -- for every padded block id the
+// element blocks that add to it, (e * 36 + p) << 1 | transposed, ascending -- and the gather that sums them, applies
+// the Full Dirichlet treatment (node_fixed; unit diagonal) and writes every entry of every slice once
+void launch_tangent_inverse_count(const int32_t* slot, int n_elems, int32_t* cnt, cudaStream_t s);
+void launch_tangent_inverse_fill(const int32_t* slot, int n_elems, const int32_t* ptr, int32_t* cursor, int32_t* inv,
+                                 int64_t n_padded, cudaStream_t s);
+void launch_tangent_gather(const Bsr& A, const int32_t* gslice, const int32_t* inv_ptr, const int32_t* inv,
+                           const float* blk, const uint8_t* node_fixed, float* val, cudaStream_t s);
 // displacement-based NeoHooke FP32 tangent by block rows (thread per node row, no colouring; element.cu);
 // ne_ptr / ne_elems: the elements of every node in ascending order
 void launch_row_tangent(const ElemArgs& a, const int32_t* ne_ptr, const int32_t* ne_elems, cudaStream_t s);
@@ -129,7 +150,8 @@ void launch_bsr_reset(void* val, bool fp32, int64_t n_padded, const int32_t* dia
 // val[idx[k]] += v[k] for n unique value indices (the assembler manipulator's matrix entries)
 void launch_add_entries(void* val, bool fp32, const int64_t* idx, const double* v, int n, cudaStream_t s);
 void launch_vector_finish(double* R, const uint8_t* node_fixed, int n_nodes, const int32_t* pl_dof,
-                          const double* pl_val, int n_pl, double load_factor, cudaStream_t s);
+                          const double* pl_val, int n_pl, double load_factor, cudaStream_t s,
+                          const double* load_factor_dev = nullptr);
 void launch_norm2(const double* x, int64_t n, double* partials, double* out, cudaStream_t s);
 // inhomogeneous Dirichlet values: u[i] = lambda rate[i] where nonzero; R += step F on the free dofs
 void launch_idbc_sync(double* u, const double* rate, double lambda, int64_t n, cudaStream_t s);
@@ -187,6 +209,9 @@ struct PcgWork {
   // withholds its first barrier arrival (every CTA's first wait then runs out and the solve reports the timeout)
   int barrier_polls = 0;
   int withhold_first_arrival = 0;
+  // when set, the init kernel reads the relative tolerance from this device scalar instead of its argument (a solve
+  // captured in a CUDA graph whose tolerance changes from launch to launch)
+  const double* rtol_dev = nullptr;
 };
 void launch_block_jacobi(const Bsr& A, bool fp32, void* minv, bool point_jacobi, cudaStream_t s);
 void launch_pcg_init(const Bsr& A, PcgWork& w, const double* b, double rtol, int max_iter, cudaStream_t s);

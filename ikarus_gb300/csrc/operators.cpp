@@ -212,6 +212,13 @@ int ikr_newton_update(ikr_nr nr, ikr_req r, const double* dx) {
   });
 }
 
+int ikr_newton_graph_iterations(ikr_nr nr, int64_t* n) {
+  return guarded([&] {
+    need(nr && n, IKR_ERR_ARG, "null argument");
+    *n = nr->graph_iterations;
+  });
+}
+
 int ikr_newton_subscribe_logger(ikr_nr nr, ikr_log_sink sink, void* user) {
   return guarded([&] {
     need(nr, IKR_ERR_ARG, "null argument");

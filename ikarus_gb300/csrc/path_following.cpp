@@ -471,6 +471,8 @@ int ikr_path_following_run(ikr_pf pf, ikr_req r, ikr_control_info* info, ikr_nr_
     need(r->fes == f, IKR_ERR_ARG, "requirement of another element set");
     need(f->n_inst == 0 || nr->ls->tag != IKR_SOLVER_GPU_PCG_BATCHED, IKR_ERR_NOT_IMPLEMENTED,
          "path following of batched instances");
+    need(!a->idbc_value, IKR_ERR_NOT_IMPLEMENTED,
+         "path following with Dirichlet values given as a function (use ikr_assembler_set_dirichlet_values)");
     // the load-control and displacement-control subsidiary functions do not handle inhomogeneous Dirichlet values
     // (checkHasNoValidIDBCForceFunction, pathfollowingfunctions.hh:22-26)
     need(!a->has_idbc || pf->kind == IKR_PF_ARC_LENGTH, IKR_ERR_NOT_IMPLEMENTED,

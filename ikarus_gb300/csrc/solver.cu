@@ -125,7 +125,8 @@ __global__ void __launch_bounds__(kThreads) pcg_update_kernel(int n_rows, const 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) pcg_init_kernel(int n_rows, const T* __restrict__ minv,
                                                             const double* __restrict__ b, T* x, T* r, T* z, T* pold,
-                                                            double* part, double* scal, double rtol, int max_iter,
+                                                            double* part, double* scal, double rtol,
+                                                            const double* __restrict__ rtol_dev, int max_iter,
                                                             int coarse) {
   __shared__ double sh[32];
   __shared__ bool last;
@@ -156,7 +157,8 @@ __global__ void __launch_bounds__(kThreads) pcg_init_kernel(int n_rows, const T*
     const double rrs = sum_partials(part + 1, gridDim.x, 2, sh);
     if (threadIdx.x == 0) {
       scal[kBB] = rrs;
-      scal[kTol2] = rtol * rtol * rrs;
+      const double rt = rtol_dev ? *rtol_dev : rtol;  // a captured solve reads its tolerance at run time
+      scal[kTol2] = rt * rt * rrs;
       scal[coarse ? kRzF : kRz] = rzs;
       scal[kBeta] = 0.0;
       scal[kAlpha] = 0.0;
@@ -251,12 +253,12 @@ void launch_pcg_init(const Bsr& A, PcgWork& w, const double* b, double rtol, int
   cudaMemsetAsync(w.scal, 0, sizeof(double) * kNScal, s);  // scalars and tickets start at zero
   if (w.fp32)
     pcg_init_kernel<float><<<w.grid, kThreads, 0, s>>>(w.n_rows, (const float*)w.minv, b, (float*)w.x, (float*)w.r,
-                                                        (float*)w.z, (float*)w.p1, w.part_b, w.scal, rtol, max_iter,
-                                                        w.coarse);
+                                                        (float*)w.z, (float*)w.p1, w.part_b, w.scal, rtol, w.rtol_dev,
+                                                        max_iter, w.coarse);
   else
     pcg_init_kernel<double><<<w.grid, kThreads, 0, s>>>(w.n_rows, (const double*)w.minv, b, (double*)w.x,
                                                          (double*)w.r, (double*)w.z, (double*)w.p1, w.part_b, w.scal,
-                                                         rtol, max_iter, w.coarse);
+                                                         rtol, w.rtol_dev, max_iter, w.coarse);
 }
 
 void launch_pcg_spmv(const Bsr& A, PcgWork& w, int parity, cudaStream_t s) {

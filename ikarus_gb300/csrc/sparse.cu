@@ -182,10 +182,10 @@ __global__ void unit_diag_kernel(T* val, const int32_t* __restrict__ diag, const
 // Manipulator point loads after the Dirichlet treatment (assemblermanipulatorbuildingblocks.hh:110-115):
 // R[dof] += lambda * value, one thread per distinct dof.
 __global__ void point_load_kernel(double* R, const int32_t* __restrict__ dof, const double* __restrict__ val, int n,
-                                  double lf) {
+                                  double lf, const double* __restrict__ lf_dev) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  R[dof[k]] += lf * val[k];
+  R[dof[k]] += (lf_dev ? *lf_dev : lf) * val[k];
 }
 
 // inhomogeneous Dirichlet values: u[i] = lambda rate[i] where that value is nonzero
@@ -329,10 +329,12 @@ void launch_add_entries(void* val, bool fp32, const int64_t* idx, const double* 
 }
 
 void launch_vector_finish(double* R, const uint8_t* node_fixed, int n_nodes, const int32_t* pl_dof,
-                          const double* pl_val, int n_pl, double load_factor, cudaStream_t s) {
+                          const double* pl_val, int n_pl, double load_factor, cudaStream_t s,
+                          const double* load_factor_dev) {
   (void)node_fixed;
   (void)n_nodes;
-  if (n_pl > 0) point_load_kernel<<<blocks_for(n_pl, 128), 128, 0, s>>>(R, pl_dof, pl_val, n_pl, load_factor);
+  if (n_pl > 0)
+    point_load_kernel<<<blocks_for(n_pl, 128), 128, 0, s>>>(R, pl_dof, pl_val, n_pl, load_factor, load_factor_dev);
 }
 void launch_idbc_sync(double* u, const double* rate, double lambda, int64_t n, cudaStream_t s) {
   idbc_sync_kernel<<<kNormGrid, 256, 0, s>>>(u, rate, lambda, n);

@@ -217,6 +217,13 @@ int ikr_assembler_export_csc(ikr_asm a, int32_t dbc_option, int64_t* col_ptr, in
  * every update (nonlinearsolverfactory.hh:45-52); LoadControl also after a step that needed no iteration
  * (loadcontrol.inl:43-44).  Not available in batched solves. */
 int ikr_assembler_set_dirichlet_values(ikr_asm a, const double* rate);
+/* DirichletValues::storeInhomogeneousBoundaryCondition(f) with a general f(x, lambda) (dirichletvalues.hh:213-282):
+ * value(X, lambda) is called on the host with every node position (ikr_point_fn, out: 3 values per node) at each
+ * load factor the prescribed values are imposed at; its entries that are nonzero overwrite the displacement
+ * (nonlinearsolverfactory.hh:45-52).  derivative(X, lambda) = d value / d lambda (the reference differentiates f with
+ * autodiff) is evaluated once at lambda = 1: the IDBC forces K_raw du_D/dlambda stepSize (functionhelper.hh:
+ * 170-184).  LoadControl / NewtonRaphson only: path following returns IKR_ERR_NOT_IMPLEMENTED. */
+int ikr_assembler_set_dirichlet_function(ikr_asm a, ikr_point_fn value, ikr_point_fn derivative, void* user);
 /* the block pattern itself: row_ptr (n_nodes+1), col (n_blocks) */
 int ikr_assembler_block_pattern(ikr_asm a, int32_t* n_rows, int64_t* n_blocks, int32_t* row_ptr, int32_t* col);
 /* ||R|| of the last assembled vector (FP64, deterministic device reduction) */
@@ -271,10 +278,13 @@ int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_le
  * next factorize from timed CG iterations on the assembled tangent and kept for that assembler.  info
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fraction);
-/* no reference counterpart: the kernel of the FP32 displacement-based NeoHooke tangent -- 1: coloured element
- * kernel (8 lanes per element, one launch per colour class), 2: row kernel (a thread per node row adds its row of
- * every adjacent element's tangent, one launch, no colouring), 0 (default): the faster of the two, timed at the
- * first assembly.  Both give the same FP32 tangent up to the order of the FP32 additions. */
+/* no reference counterpart: the kernel of the FP32 displacement-based tangent -- 1: coloured element kernel (8 lanes
+ * per element, one read-modify-write launch per colour class), 2: row kernel (NeoHooke on a set without instances: a
+ * thread per node row adds its row of every adjacent element's tangent, one launch, no colouring), 3: element blocks
+ * + gather (one launch writes every element's 36 distinct FP32 blocks to a scratch array with coalesced stores, a
+ * second sums each matrix block's contributions in a fixed order and writes every slice once, Dirichlet treatment
+ * included; the scratch holds 1.3 KB per element), 0 (default): the fastest, timed at the first assembly.  All give
+ * the same FP32 tangent up to the order of the FP32 additions. */
 int ikr_assembler_set_tangent_kernel(ikr_asm a, int32_t path);
 int ikr_assembler_tangent_kernel(ikr_asm a, int32_t* path);
 /* no reference counterpart: solves with two right-hand sides and one tangent (path following's bordered
@@ -363,6 +373,12 @@ typedef struct ikr_nr_settings {
   int32_t max_backtracks; /* a correction that inverts an element (det C <= 0; the reference aborts) is halved up
                              to this many times before the error is returned (0 = reference behaviour); batched
                              solves halve the correction of the affected instances only */
+  int32_t step_graphs;    /* 1 (default): every Newton iteration after the first of a solver's life -- tangent
+                             assembly, preconditioner, the persistent CG, update, residual assembly and norms -- runs
+                             as one CUDA graph launch with one host synchronisation, where the configuration allows
+                             it (displacement-based elements, persistent CG kind, no backtracking, refinement, coarse
+                             correction, FP64 outer solve or inhomogeneous Dirichlet values); results are identical
+                             to the launch-by-launch iteration; 0: launch by launch */
 } ikr_nr_settings;
 typedef struct ikr_nr_info {   /* NonLinearSolverInformation (solverinfos.hh:20-32) */
   int32_t success;
@@ -396,6 +412,9 @@ int ikr_newton_solve(ikr_nr nr, ikr_req req, double step_size, ikr_nr_info* info
 int ikr_newton_residual(ikr_nr nr, ikr_req req, double* out);
 int ikr_newton_jacobian(ikr_nr nr, ikr_req req);
 int ikr_newton_update(ikr_nr nr, ikr_req req, const double* correction);
+/* no reference counterpart: Newton iterations this solver ran as one CUDA graph launch each (step_graphs), since its
+ * creation */
+int ikr_newton_graph_iterations(ikr_nr nr, int64_t* n);
 /* NonLinearSolverLogger::subscribeTo(nr) */
 int ikr_newton_subscribe_logger(ikr_nr nr, ikr_log_sink sink, void* user);
 /* per instance (batched solves): Newton iterations, final residual norm and convergence of the last solve

@@ -85,6 +85,7 @@ def _declare(L):
                                      C.POINTER(C.c_int)]
     L.orc_set_threads.argtypes = [C.c_int]
     L.orc_add_volume_load.argtypes = [vp, _ORC_POINT_FN, vp]
+    L.orc_set_dirichlet_function.argtypes = [vp, _ORC_POINT_FN, _ORC_POINT_FN, vp]
     L.orc_add_neumann_function.argtypes = [vp, C.c_int, ip, ip, _ORC_POINT_FN, vp]
     L.orc_constraints_below.argtypes = [vp, ip]
     L.orc_load_step.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_double, dp, dp, dp]
@@ -219,6 +220,13 @@ class OracleProblem:
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(traction, dtype=np.float64), (len(fe), 3)))
         _check(self._L.orc_add_neumann(self.h, len(fe), _p(fe, C.c_int32), _p(fl, C.c_int32), _p(t, C.c_double)),
                "add_neumann")
+
+    def set_dirichlet_function(self, value, derivative):
+        """Inhomogeneous Dirichlet values value(X (n, 3), lambda) at every node, lambda-derivative derivative(X,
+        lambda) (used at lambda = 1 for the IDBC forces)."""
+        cv, cd = _point_fn(value), _point_fn(derivative)
+        self._cbs = getattr(self, "_cbs", []) + [cv, cd]
+        _check(self._L.orc_set_dirichlet_function(self.h, cv, cd, None), "set_dirichlet_function")
 
     def add_volume_load(self, fn):
         """VolumeLoad with fn(X (n, 3), lambda) -> body forces (n, 3)."""

@@ -314,8 +314,18 @@ struct orc_problem {
   std::vector<std::vector<std::pair<int, PointFn>>> fn_faces;  // per element: (local face, function)
   std::vector<int32_t> pl_dof;
   std::vector<double> pl_val;
-  // inhomogeneous Dirichlet values u_D(lambda) = lambda * idbc_rate on constrained dofs (empty: none)
+  // inhomogeneous Dirichlet values u_D(lambda) = lambda * idbc_rate on constrained dofs (empty: none); with a value
+  // function, u_D(lambda) = idbc_value(X, lambda) interpolated at every node and idbc_rate its lambda-derivative at 1
   std::vector<double> idbc_rate;
+  orc_point_fn idbc_value = nullptr;
+  void* idbc_user = nullptr;
+  // u_D at the load factor into v (n dofs)
+  void idbc_values(double lambda, std::vector<double>& v) const {
+    v.assign(3 * (size_t)nn, 0.0);
+    if (idbc_value) idbc_value(nn, X.data(), lambda, v.data(), idbc_user);
+    else
+      for (size_t i = 0; i < v.size(); ++i) v[i] = lambda * idbc_rate[i];
+  }
   // pattern caches
   std::vector<std::vector<int32_t>> nodeAdj;
   int ndof() const { return 3 * nn; }
@@ -1112,8 +1122,19 @@ int orc_set_dirichlet(orc_problem* p, const uint8_t* f) {
 }
 // DirichletValues::storeInhomogeneousBoundaryCondition (dirichletvalues.hh:213-222) for prescribed values linear
 // in the load factor: u_D(lambda) = lambda * rate, derivative rate; rate must vanish on free dofs.
+int orc_set_dirichlet_function(orc_problem* p, orc_point_fn value, orc_point_fn derivative, void* user) {
+  if (!p || !value || !derivative) return ORC_ERR_ARG;
+  // storeInhomogeneousBoundaryCondition (dirichletvalues.hh:213-222): the value and its lambda-derivative; the IDBC
+  // force uses the derivative at lambda = 1 interpolated at every node (functionhelper.hh:170-184)
+  p->idbc_rate.assign(3 * (size_t)p->nn, 0.0);
+  derivative(p->nn, p->X.data(), 1.0, p->idbc_rate.data(), user);
+  p->idbc_value = value;
+  p->idbc_user = user;
+  return ORC_OK;
+}
 int orc_set_dirichlet_values(orc_problem* p, const double* rate) {
   if (!p) return ORC_ERR_ARG;
+  p->idbc_value = nullptr;
   if (!rate) {
     p->idbc_rate.clear();
     return ORC_OK;
@@ -1414,12 +1435,12 @@ int orc_load_control(orc_problem* p, int steps, double t0, double t1, double tol
   const bool idbc = !p->idbc_rate.empty();
   // syncParameterAndGlobalSolution with the inhomogeneous values (nonlinearsolverfactory.hh:45-52): entries whose
   // prescribed value is nonzero take it
+  std::vector<double> vd;
   auto sync = [&]() {
     if (!idbc) return;
-    for (int i = 0; i < n; ++i) {
-      const double v = *lambda * p->idbc_rate[i];
-      if (v != 0.0) x[i] = v;
-    }
+    p->idbc_values(*lambda, vd);
+    for (int i = 0; i < n; ++i)
+      if (vd[i] != 0.0) x[i] = vd[i];
   };
   for (int s = 0; s <= steps; ++s) {
     if (s > 0) *lambda += step;  // LoadControl::predictor (loadcontrol.inl:54-57)
@@ -1730,6 +1751,7 @@ int orc_path_following(orc_problem* p, int kind, int steps, double step_size, in
                        const int32_t* controlled, int target_iterations, double tol, int max_iter, int solver,
                        double cg_rtol, double* u, double* lambda, int32_t* iterations, double* res_norms,
                        double* lambdas, double* psi, int* n_solves, int* total_iterations) {
+  if (p && p->idbc_value) return ORC_ERR_NOT_IMPLEMENTED;  // prescribed-value functions: load control only
   if (!p || !u || !lambda || steps <= 0 || kind < 0 || kind > 2) return ORC_ERR_ARG;
   const int n = p->ndof();
   const bool idbc = !p->idbc_rate.empty();

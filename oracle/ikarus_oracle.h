@@ -59,6 +59,10 @@ int orc_add_neumann(orc_problem* p, int n_faces, const int32_t* face_elem, const
                     const double* traction);
 /* loads given as functions: out[3k..3k+2] = f(X[3k..3k+2], lambda) for k < n */
 typedef void (*orc_point_fn)(int32_t n, const double* X, double lambda, double* out, void* user);
+/* inhomogeneous Dirichlet values given as a function (storeInhomogeneousBoundaryCondition, dirichletvalues.hh:213-222):
+ * u_D(lambda) = value(X_node, lambda) at every node (entries that are nonzero are imposed, nonlinearsolverfactory.hh:
+ * 45-52), IDBC forces from derivative(X_node, 1) (functionhelper.hh:170-184); load_control only */
+int orc_set_dirichlet_function(orc_problem* p, orc_point_fn value, orc_point_fn derivative, void* user);
 /* VolumeLoad (loads/volume.hh:86-106): body force f(X, lambda) integrated with the element's Gauss rule */
 int orc_add_volume_load(orc_problem* p, orc_point_fn f, void* user);
 /* Neumann faces with a traction function f(X, lambda) evaluated at the face's quadrature point (the face centre) */

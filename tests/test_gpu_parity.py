@@ -467,11 +467,12 @@ def test_newton_on_a_reduced_binding_gives_the_full_iterates(ikr):
     assert np.abs(u1 - ref["u"]).max() <= 1e-8 * np.abs(ref["u"]).max()
 
 
-@pytest.mark.parametrize("path", [1, 2], ids=["coloured", "rows"])
+@pytest.mark.parametrize("path", [1, 2, 3], ids=["coloured", "rows", "element-blocks"])
 def test_fp32_tangent_kernels_match_oracle(ikr, path):
-    """The two FP32 tangent kernels of the displacement-based NeoHooke element -- coloured element kernel and row
-    kernel (a thread per node row adds its row of every adjacent element's tangent) -- give the oracle's tangent
-    within the FP32 bound, with Full Dirichlet rows and columns; the timed choice picks one of them."""
+    """The three FP32 tangent kernels of the displacement-based NeoHooke element -- coloured element kernel, row
+    kernel (a thread per node row adds its row of every adjacent element's tangent) and element blocks + gather --
+    give the oracle's tangent within the FP32 bound, with Full Dirichlet rows and columns (and Raw without them); the
+    timed choice picks one of them."""
     p = problems.cantilever(5, 3, 2, L=4.0, jitter=0.15, seed=13)
     o = oracle.from_problem(p)
     u = 0.02 * np.random.default_rng(7).standard_normal(p.n_dofs)
@@ -481,7 +482,9 @@ def test_fp32_tangent_kernels_match_oracle(ikr, path):
     K = asm.matrix(req, dbc=ikr.DBCOption.Full).toarray()
     assert asm.tangent_kernel() == path
     assert rel_err(K, o.assemble_matrix_dense(u, 0.3)) <= 2e-6
+    Kraw = asm.matrix(req, dbc=ikr.DBCOption.Raw).toarray()
+    assert rel_err(Kraw, o.assemble_matrix_dense(u, 0.3, oracle.DBC_RAW)) <= 2e-6
     fes2, asm2 = problems.build_gpu(p, precision=1)
     K2 = asm2.matrix(ikr.FERequirements(fes2, u, 0.3), dbc=ikr.DBCOption.Full).toarray()
-    assert asm2.tangent_kernel() in (1, 2)
+    assert asm2.tangent_kernel() in (1, 2, 3)
     assert rel_err(K2, K) <= 2e-6
