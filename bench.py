@@ -83,6 +83,8 @@ def parse():
                     help="config 5: relative tolerance of the FP32 CG inside the FP64 outer solve")
     ap.add_argument("--eas-size", default="64,64,16", help="config 5: elements per direction")
     ap.add_argument("--eas-steps", type=int, default=25, help="config 5: load steps")
+    ap.add_argument("--eas-first-steps", type=int, default=0,
+                    help="config 5: run only the first K of the load steps (a short run for profiling; 0 = all)")
     ap.add_argument("--eas-predictor", type=int, default=1, help="config 5: 0 none, 1 previous increment")
     ap.add_argument("--path-following", type=int, default=0,
                     help="arc-length path of this many steps on the 128x32x32 cantilever instead of the load control")
@@ -793,6 +795,7 @@ def run_eas(args):
     out = {"metric": "time to ||R||/||R0||<1e-8 on every load step (nearly incompressible EAS block)", "unit": "s",
            "higher_is_better": False,
            "config": {"workload": p.name, "elements": p.mesh.n_elems, "dofs": p.n_dofs, "load_steps": p.load_steps,
+                      "steps_run": args.eas_first_steps if 0 < args.eas_first_steps < p.load_steps else p.load_steps,
                       "eas": "GreenLagrange E9", "nu": 0.4999, "predictor": args.eas_predictor,
                       "newton_backtracks": args.backtracks, "mixed_cg_cap": args.eas_cg_cap,
                       "mixed_outer": {"restart": args.eas_restart, "inner_rtol": args.eas_inner_rtol,
@@ -812,7 +815,8 @@ def run_eas(args):
             ls.set_fp64_outer(restart=args.eas_restart, inner_rtol=args.eas_inner_rtol,
                               inner_max_iter=args.eas_cg_cap)
         nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ls))
-        lc = ikr.LoadControl(nr, p.load_steps)
+        k = args.eas_first_steps if 0 < args.eas_first_steps < p.load_steps else p.load_steps
+        lc = ikr.LoadControl(nr, k, (0.0, k / p.load_steps))
         if args.eas_predictor:
             lc.set_predictor(1)
         req = ikr.FERequirements(fes)

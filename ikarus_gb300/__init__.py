@@ -175,6 +175,7 @@ SIGNATURES = {
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
     "ikr_fes_set_material": ([_vp, _I], C.c_int),
+    "ikr_fes_set_hyperelastic": ([_vp, _vp], C.c_int),
     "ikr_assembler_set_dirichlet_values": ([_vp, _dp], C.c_int),
     "ikr_fes_get_alpha": ([_vp, _dp], C.c_int),
     "ikr_fes_set_alpha": ([_vp, _dp], C.c_int),
@@ -351,6 +352,172 @@ class BlatzKo:
         return 0.0
 
 
+# ---- the hyperelastic framework (materials/hyperelastic/) --------------------------------------------------
+HYPER_MAX_TERMS = 4
+
+
+class _HyperelasticC(C.Structure):
+    """ikr_hyperelastic"""
+    _fields_ = [("deviatoric", C.c_int32), ("n_terms", C.c_int32), ("mu", C.c_double * HYPER_MAX_TERMS),
+                ("alpha", C.c_double * HYPER_MAX_TERMS), ("p", C.c_int32 * HYPER_MAX_TERMS),
+                ("q", C.c_int32 * HYPER_MAX_TERMS), ("param", C.c_double), ("volumetric", C.c_int32),
+                ("reserved", C.c_int32), ("K", C.c_double), ("beta", C.c_double)]
+
+
+class PrincipalStretchTags(enum.IntEnum):
+    """materials/tags.hh: the stretches an Ogden function takes"""
+    total = 0
+    deviatoric = 1
+
+
+@dataclass(frozen=True)
+class VolumetricFunction:
+    """VF0..VF12 (volumetric/volumetricfunctions.hh); beta for VF4, VF7, VF10."""
+    index: int
+    beta: float = 0.0
+
+
+def VF0():
+    return VolumetricFunction(0)
+
+
+def VF1():
+    return VolumetricFunction(1)
+
+
+def VF2():
+    return VolumetricFunction(2)
+
+
+def VF3():
+    return VolumetricFunction(3)
+
+
+def VF4(beta):
+    return VolumetricFunction(4, float(beta))
+
+
+def VF5():
+    return VolumetricFunction(5)
+
+
+def VF6():
+    return VolumetricFunction(6)
+
+
+def VF7(beta):
+    return VolumetricFunction(7, float(beta))
+
+
+def VF8():
+    return VolumetricFunction(8)
+
+
+def VF9():
+    return VolumetricFunction(9)
+
+
+def VF10(beta):
+    return VolumetricFunction(10, float(beta))
+
+
+def VF11():
+    return VolumetricFunction(11)
+
+
+def VF12():
+    return VolumetricFunction(12)
+
+
+@dataclass
+class Hyperelastic:
+    """Hyperelastic<Deviatoric<DF>, Volumetric<VF>> (materials/hyperelastic/interface.hh): W(C) = W_dev(lambda_1,
+    lambda_2, lambda_3) + K U(J).  ``deviatoric`` is one of the DEV_* codes below with its parameters; build it with the
+    factories (makeOgden, makeMooneyRivlin, makeYeoh, makeInvariantBased, makeArrudaBoyce, makeGent, makeBlatzKo,
+    makePureVolumetric; hyperelastic/factory.hh)."""
+    deviatoric: int
+    mu: tuple = ()
+    alpha: tuple = ()
+    p: tuple = ()
+    q: tuple = ()
+    param: float = 0.0
+    K: float = 0.0
+    vf: VolumetricFunction = VolumetricFunction(0)
+    kind = 3
+    lambda_ = 0.0
+
+    DEV_NONE, DEV_BLATZKO, DEV_OGDEN_TOTAL, DEV_OGDEN_DEVIATORIC = 0, 1, 2, 3
+    DEV_INVARIANT_BASED, DEV_ARRUDA_BOYCE, DEV_GENT = 4, 5, 6
+
+    def _c(self):
+        h = _HyperelasticC()
+        h.deviatoric, h.n_terms = int(self.deviatoric), max(1, len(self.mu))
+        for name in ("mu", "alpha", "p", "q"):
+            vals = getattr(self, name)
+            if len(vals) > HYPER_MAX_TERMS:
+                raise IkarusError(-1, f"at most {HYPER_MAX_TERMS} terms")
+            for i, v in enumerate(vals):
+                getattr(h, name)[i] = v
+        h.param, h.volumetric, h.K, h.beta = float(self.param), int(self.vf.index), float(self.K), float(self.vf.beta)
+        return h
+
+    def oracle_terms(self):
+        """The plain values of the description (keyword arguments of the oracle's ``hyper``)."""
+        return dict(deviatoric=int(self.deviatoric), mu=list(self.mu), alpha=list(self.alpha), p=list(self.p),
+                    q=list(self.q), param=float(self.param), volumetric=int(self.vf.index), K=float(self.K),
+                    beta=float(self.vf.beta))
+
+    @property
+    def mu0(self):
+        return float(self.mu[0]) if self.mu else 0.0
+
+
+def makeBlatzKo(mu, K=0.0, vf=None):
+    """makeBlatzKo(mu) (factory.hh:34-39); K and vf add a volumetric part as Hyperelastic(dev, vol) would."""
+    return Hyperelastic(Hyperelastic.DEV_BLATZKO, mu=(float(mu),), K=K, vf=vf or VF0())
+
+
+def makeOgden(mu, alpha, K=0.0, vf=None, tag=PrincipalStretchTags.total):
+    """makeOgden<n, tag>(mu, alpha, K, vf) (factory.hh:52-61)."""
+    if len(mu) != len(alpha):
+        raise IkarusError(-1, "Ogden: as many exponents as moduli")
+    dev = Hyperelastic.DEV_OGDEN_TOTAL if tag == PrincipalStretchTags.total else Hyperelastic.DEV_OGDEN_DEVIATORIC
+    return Hyperelastic(dev, mu=tuple(map(float, mu)), alpha=tuple(map(float, alpha)), K=K, vf=vf or VF0())
+
+
+def makeInvariantBased(mu, pex, qex, K=0.0, vf=None):
+    """makeInvariantBased<n>(mu, p, q, K, vf) (factory.hh:74-83): W = sum mu_i (W1 - 3)^p_i (W2 - 3)^q_i."""
+    if not (len(mu) == len(pex) == len(qex)):
+        raise IkarusError(-1, "InvariantBased: as many exponents as coefficients")
+    return Hyperelastic(Hyperelastic.DEV_INVARIANT_BASED, mu=tuple(map(float, mu)), p=tuple(map(int, pex)),
+                        q=tuple(map(int, qex)), K=K, vf=vf or VF0())
+
+
+def makeMooneyRivlin(mu, K=0.0, vf=None):
+    """makeMooneyRivlin(mu, K, vf) (factory.hh:96-102): p = {1, 0}, q = {0, 1}."""
+    return makeInvariantBased(mu, (1, 0), (0, 1), K, vf)
+
+
+def makeYeoh(mu, K=0.0, vf=None):
+    """makeYeoh(mu, K, vf) (factory.hh:115-121): p = {1, 2, 3}, q = {0, 0, 0}."""
+    return makeInvariantBased(mu, (1, 2, 3), (0, 0, 0), K, vf)
+
+
+def makeArrudaBoyce(mu, lambdaM, K=0.0, vf=None):
+    """makeArrudaBoyce({mu, lambdaM}, K, vf) (factory.hh:133-140)."""
+    return Hyperelastic(Hyperelastic.DEV_ARRUDA_BOYCE, mu=(float(mu),), param=float(lambdaM), K=K, vf=vf or VF0())
+
+
+def makeGent(mu, Jm, K=0.0, vf=None):
+    """makeGent({mu, Jm}, K, vf) (factory.hh:152-158)."""
+    return Hyperelastic(Hyperelastic.DEV_GENT, mu=(float(mu),), param=float(Jm), K=K, vf=vf or VF0())
+
+
+def makePureVolumetric(vf, K):
+    """makePureVolumetric(vf, K) (factory.hh:169-174): no deviatoric part."""
+    return Hyperelastic(Hyperelastic.DEV_NONE, K=float(K), vf=vf)
+
+
 # ---- finite elements -------------------------------------------------------------------------------------
 class FiniteElements:
     """All elements of one Q1 hexahedral mesh with skills nonLinearElastic(NeoHooke) [+ eas<ES>(n)]
@@ -364,12 +531,16 @@ class FiniteElements:
         self.n_eas = int(n_eas)
         self.material = material
         h = C.c_void_p()
+        mu = material.mu0 if isinstance(material, Hyperelastic) else material.mu
         _err(lib().ikr_fes_create(C.byref(h), self.n_nodes, _ptr(self.coords), self.n_elems,
-                                  _ptr(self.conn, C.c_int32), material.lambda_, material.mu, int(eas), self.n_eas),
+                                  _ptr(self.conn, C.c_int32), material.lambda_, mu, int(eas), self.n_eas),
              "fes_create")
         self.h = h
         self._load_cbs = []  # ctypes trampolines of function-defined loads (kept alive with the element set)
-        if getattr(material, "kind", 0):
+        if isinstance(material, Hyperelastic):
+            self._hyper = material._c()
+            _err(lib().ikr_fes_set_hyperelastic(self.h, C.byref(self._hyper)), "set_hyperelastic")
+        elif getattr(material, "kind", 0):
             _err(lib().ikr_fes_set_material(self.h, int(material.kind)), "set_material")
 
     def __del__(self):

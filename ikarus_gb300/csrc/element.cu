@@ -20,15 +20,33 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "hyperelastic.cuh"
 #include "kernels.h"
 
 namespace ikr {
 
 namespace {
 
+// B-operator of the Green-Lagrange strain variation w.r.t. a node's displacement (rows 11, 22, 33, 23, 13, 12;
+// easfunctions/displacementgradient.hh:129-146): column a of row (k, l) is dN_l F_ak + dN_k F_al
+template <typename T>
+__device__ __forceinline__ void bop_t(const T F[3][3], const T dN[3], T B[6][3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const T g0 = F[a][0], g1 = F[a][1], g2 = F[a][2];
+    B[0][a] = dN[0] * g0;
+    B[1][a] = dN[1] * g1;
+    B[2][a] = dN[2] * g2;
+    B[3][a] = dN[2] * g1 + dN[1] * g2;
+    B[4][a] = dN[2] * g0 + dN[0] * g2;
+    B[5][a] = dN[1] * g0 + dN[0] * g1;
+  }
+}
+
 // EPB elements per block (8 lanes each): 16, 32 or 64, chosen per element set by timing (host.cpp)
 // MAT 0: NeoHooke (neohooke.hh:78-142); MAT 1: StVenantKirchhoff (svk.hh:63-163); MAT 2: BlatzKo
-// (hyperelastic/deviatoric/blatzko.hh with total stretches and no volumetric part, factory.hh:34-39)
+// (hyperelastic/deviatoric/blatzko.hh with total stretches and no volumetric part, factory.hh:34-39); MAT 3: the
+// hyperelastic framework (hyperelastic/interface.hh, any deviatoric and volumetric function, hyperelastic.cuh)
 template <typename KT, int MODE, int EPB, int MAT = 0>
 __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const int32_t* __restrict__ list, int n_list,
                                                                int e_base) {
@@ -40,6 +58,7 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
   static_assert(!(WANT_R || WANT_E) || std::is_same<KT, double>::value, "residual and energy are FP64");
   static_assert(!BLOCKS || (WANT_K && std::is_same<KT, float>::value), "element blocks: FP32 tangent only");
   __shared__ KT sh[EPB][8][6];
+  __shared__ KT hm[MAT == 3 ? EPB : 1][36];  // hyperelastic: the Gauss point's material moduli (Voigt)
   // element blocks: staged per warp (4 elements x 36 blocks x 9 entries) and copied out with 16-byte stores
   __shared__ __align__(16) KT stage[BLOCKS ? EPB / 4 : 1][BLOCKS ? 4 * kElemBlockCount * 9 : 1];
 
@@ -167,6 +186,73 @@ __global__ void __launch_bounds__(EPB * 8) disp_element_kernel(ElemArgs a, const
 #pragma unroll
             for (int j = 0; j < 3; ++j)
               Kacc[d][i][j] += wl * g[i] * gJ[j] + wm * FFt[i][j] + wu * gJ[i] * g[j] + (i == j ? ws : KT(0));
+        }
+        __syncwarp();
+      }
+      continue;
+    }
+    if constexpr (MAT == 3) {
+      // hyperelastic framework: the material point (S and the Voigt moduli) in FP64 from C = F^T F
+      // (hyper::evaluate; lanes share the moduli, 4-5 entries each), then B_I^T C B_J + (grad N_I . S grad N_J) I
+      // and f_I = B_I^T S with the B-operator of F (nonlinearelastic.hh:294-342) in KT
+      double Cd[3][3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          Cd[i][j] = double(F[0][i]) * double(F[0][j]) + double(F[1][i]) * double(F[1][j]) +
+                     double(F[2][i]) * double(F[2][j]);
+      hyper::Point pt;
+      bad |= hyper::evaluate(a.hyper, Cd, pt, WANT_K);
+      const KT w = KT(kGaussW) * detJ;
+      KT S[3][3];
+#pragma unroll
+      for (int v = 0; v < 6; ++v) {
+        const int i = voigt_a(v), j = voigt_b(v);
+        S[i][j] = S[j][i] = KT(hyper::stress(pt, i, j));
+      }
+      KT SdN[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) SdN[k] = S[k][0] * dN[0] + S[k][1] * dN[1] + S[k][2] * dN[2];
+      if (WANT_R) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) f[i] += double(w * (F[i][0] * SdN[0] + F[i][1] * SdN[1] + F[i][2] * SdN[2]));
+      }
+      if (WANT_E && sub == 0) psi += double(w) * pt.psi;
+      if (WANT_K) {
+        for (int t = sub; t < 36; t += 8)
+          hm[es][t] = KT(hyper::modulus(pt, voigt_a(t / 6), voigt_b(t / 6), voigt_a(t % 6), voigt_b(t % 6)));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) sh[es][sub][k] = dN[k];
+        __syncwarp();
+        KT BI[6][3], CB[6][3];
+        bop_t(F, dN, BI);
+#pragma unroll
+        for (int c = 0; c < 6; ++c)
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            KT acc = KT(0);
+#pragma unroll
+            for (int r = 0; r < 6; ++r) acc += BI[r][i] * hm[es][6 * r + c];
+            CB[c][i] = w * acc;
+          }
+#pragma unroll
+        for (int d = 0; d < 5; ++d) {
+          const int Jn = (sub + d) & 7;
+          KT dNJ[3], BJ[6][3];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) dNJ[k] = sh[es][Jn][k];
+          bop_t(F, dNJ, BJ);
+          const KT kg = w * (SdN[0] * dNJ[0] + SdN[1] * dNJ[1] + SdN[2] * dNJ[2]);
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              KT acc = i == j ? kg : KT(0);
+#pragma unroll
+              for (int c = 0; c < 6; ++c) acc += CB[c][i] * BJ[c][j];
+              Kacc[d][i][j] += acc;
+            }
         }
         __syncwarp();
       }
@@ -551,7 +637,8 @@ __global__ void traction_kernel(const double* __restrict__ X, const int32_t* __r
 // evaluating every Gauss point; the nodal forces w P dN_v of each point are exchanged through shared memory and
 // lane v sums its node's over the points in ascending order.  About a quarter of the FP64 operations of the
 // node-per-lane form, which matters because GB300's FP64 rate bounds this kernel.
-template <int EPB>
+// HYP: the hyperelastic framework's material point (a separate instantiation keeps the other laws' registers)
+template <int EPB, bool HYP>
 __global__ void __launch_bounds__(EPB * 8) disp_residual_gp_kernel(ElemArgs a, const int32_t* __restrict__ list,
                                                                     int n_list, int e_base) {
   __shared__ double fs[EPB][8][8][3];  // [element][Gauss point][node][component]
@@ -613,7 +700,24 @@ __global__ void __launch_bounds__(EPB * 8) disp_residual_gp_kernel(ElemArgs a, c
   int bad = 0;
   const double w = kGaussW * detJ;
   double P[3][3];
-  if (a.material == 1) {
+  if constexpr (HYP) {
+    // P = F S with S of the hyperelastic material point at C = F^T F
+    double Cd[3][3], S[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Cd[i][j] = F[0][i] * F[0][j] + F[1][i] * F[1][j] + F[2][i] * F[2][j];
+    hyper::Point pt;
+    bad |= hyper::evaluate(a.hyper, Cd, pt, false);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[i][j] = hyper::stress(pt, i, j);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) P[i][j] = w * (F[i][0] * S[0][j] + F[i][1] * S[1][j] + F[i][2] * S[2][j]);
+  } else if (a.material == 1) {
     // StVenantKirchhoff: P = F S, S = lambda tr(E) I + 2 mu E, E = (F^T F - I) / 2
     double E[3][3], S[3][3];
 #pragma unroll
@@ -698,7 +802,8 @@ __global__ void __launch_bounds__(EPB * 8) disp_residual_gp_kernel(ElemArgs a, c
 template <int EPB>
 void launch_residual_gp(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
   const int blocks = (n_list + EPB - 1) / EPB;
-  disp_residual_gp_kernel<EPB><<<blocks, EPB * 8, 0, s>>>(a, list, n_list, e_base);
+  if (a.material == 3) disp_residual_gp_kernel<EPB, true><<<blocks, EPB * 8, 0, s>>>(a, list, n_list, e_base);
+  else disp_residual_gp_kernel<EPB, false><<<blocks, EPB * 8, 0, s>>>(a, list, n_list, e_base);
 }
 
 // calculateAt<PK2Stress / kirchhoffStress / cauchyStress> (nonlinearelastic.hh:237-271) of elements
@@ -757,7 +862,15 @@ __global__ void stress_at_kernel(ElemArgs a, int e0, int count, const double* __
     }
   const double lam = a.lam_e ? a.lam_e[e] : a.lam, mu = a.mu_e ? a.mu_e[e] : a.mu;
   double S[3][3];
-  if (a.material == 1) {  // StVenantKirchhoff: S = lambda tr(E) I + 2 mu E with E = (C - I) / 2
+  if (a.material == 3) {  // hyperelastic framework
+    hyper::Point pt;
+    const int bad = hyper::evaluate(a.hyper, C, pt, false);
+    if (bad && a.status) atomicOr(a.status, bad);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S[i][j] = hyper::stress(pt, i, j);
+  } else if (a.material == 1) {  // StVenantKirchhoff: S = lambda tr(E) I + 2 mu E with E = (C - I) / 2
     const double trE = 0.5 * (C[0][0] + C[1][1] + C[2][2] - 3.0);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -892,6 +1005,7 @@ template <typename KT, int MODE>
 void launch_disp_t(const ElemArgs& a, const int32_t* list, int n_list, int e_base, cudaStream_t s) {
   if (a.material == 1) return launch_disp_epb<KT, MODE, 32, 1>(a, list, n_list, e_base, s);  // SVK: one shape
   if (a.material == 2) return launch_disp_epb<KT, MODE, 32, 2>(a, list, n_list, e_base, s);  // BlatzKo: one shape
+  if (a.material == 3) return launch_disp_epb<KT, MODE, 32, 3>(a, list, n_list, e_base, s);  // hyperelastic
   if constexpr ((MODE & kElemOut) == 0) {
     if (a.epb == 16) return launch_disp_epb<KT, MODE, 16>(a, list, n_list, e_base, s);
     if (a.epb == 64) return launch_disp_epb<KT, MODE, 64>(a, list, n_list, e_base, s);

@@ -1011,6 +1011,43 @@ int ikr_fes_set_material(ikr_fes fes, int32_t material) {
     fes->alpha_version++;  // cached EAS condensation data depend on the material
   });
 }
+static_assert(ikr::kHyperMaxTerms == IKR_HYPER_MAX_TERMS, "hyperelastic term count of the C ABI and the kernels");
+int ikr_fes_set_hyperelastic(ikr_fes fes, const ikr_hyperelastic* h) {
+  return guarded([&] {
+    need(fes && h, IKR_ERR_ARG, "null argument");
+    need(h->deviatoric >= IKR_DEV_NONE && h->deviatoric <= IKR_DEV_GENT, IKR_ERR_ARG, "unknown deviatoric function");
+    need(h->volumetric >= 0 && h->volumetric <= 12, IKR_ERR_ARG, "unknown volumetric function");
+    const bool terms = h->deviatoric == IKR_DEV_OGDEN_TOTAL || h->deviatoric == IKR_DEV_OGDEN_DEVIATORIC ||
+                       h->deviatoric == IKR_DEV_INVARIANT_BASED;
+    need(!terms || (h->n_terms >= 1 && h->n_terms <= IKR_HYPER_MAX_TERMS), IKR_ERR_ARG, "n_terms out of range");
+    if (h->deviatoric == IKR_DEV_INVARIANT_BASED)
+      for (int i = 0; i < h->n_terms; ++i) {
+        need(h->p[i] >= 0 && h->q[i] >= 0, IKR_ERR_ARG, "negative invariant exponent");
+        if (h->p[i] == 0 && h->q[i] == 0)
+          fail(IKR_ERR_ARG, "The exponent q%d and the exponent p%d should not be zero at the same time.", i, i);
+      }
+    if (h->deviatoric == IKR_DEV_OGDEN_TOTAL || h->deviatoric == IKR_DEV_OGDEN_DEVIATORIC)
+      for (int i = 0; i < h->n_terms; ++i) need(h->alpha[i] != 0.0, IKR_ERR_ARG, "Ogden exponent zero");
+    need(!(h->deviatoric == IKR_DEV_ARRUDA_BOYCE || h->deviatoric == IKR_DEV_GENT) || h->param > 0.0, IKR_ERR_ARG,
+         "lambdaM / Jm must be positive");
+    ikr::HyperParams hp;
+    hp.dev = h->deviatoric;
+    hp.n = terms ? h->n_terms : 1;
+    for (int i = 0; i < ikr::kHyperMaxTerms; ++i) {
+      hp.mu[i] = h->mu[i];
+      hp.alpha[i] = h->alpha[i];
+      hp.p[i] = h->p[i];
+      hp.q[i] = h->q[i];
+    }
+    hp.param = h->param;
+    hp.vol = h->volumetric;
+    hp.K = h->K;
+    hp.beta = h->beta;
+    fes->hyper = hp;
+    fes->material = IKR_MATERIAL_HYPERELASTIC;
+    fes->alpha_version++;
+  });
+}
 int ikr_fes_kernel_info(ikr_fes fes, int32_t* epb_residual, int32_t* epb_tangent64, int32_t* epb_tangent32) {
   return guarded([&] {
     need(fes, IKR_ERR_ARG, "null argument");

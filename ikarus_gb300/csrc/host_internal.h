@@ -111,6 +111,7 @@ using namespace ikr_host;
 struct ikr_fes_s {
   int nn = 0, ne = 0, na = 0, eas = 0;
   int material = IKR_MATERIAL_NEOHOOKE;
+  ikr::HyperParams hyper;  // the functions of IKR_MATERIAL_HYPERELASTIC
   // elements per block of the displacement element kernel, chosen by timing at the first assembly of each kind
   // (0 = not chosen yet): residual, FP64 tangent, FP32 tangent
   int epb_r = 0, epb_k64 = 0, epb_k32 = 0;
@@ -175,6 +176,7 @@ struct ikr_fes_s {
     a.lam = lam;
     a.mu = mu;
     a.material = material;
+    a.hyper = hyper;
     a.eas_kind = na > 0 ? eas : 0;
     a.n_alpha = na;
     a.alpha = alpha.p;
@@ -278,6 +280,8 @@ struct ikr_fes_s {
         fail(IKR_ERR_NONPOSITIVE_DETC, "Determinant of right Cauchy Green tensor C must be greater than zero");
       if (h & ikr::kStatusSingularD) fail(IKR_ERR_SINGULAR, "EAS matrix D is singular");
       if (h & ikr::kStatusPatternOverflow) fail(IKR_ERR_ARG, "a node couples with more than 128 nodes");
+      if (h & ikr::kStatusMaterialDomain)
+        fail(IKR_ERR_INVALID_STATE, "The material parameter Jm should be greater than (W1 - 3)");
       fail(IKR_ERR_ARG, "device status %d", h);
     }
   }

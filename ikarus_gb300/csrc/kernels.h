@@ -19,6 +19,28 @@ enum StatusBits : int {
   kStatusNonFinite = 2,
   kStatusSingularD = 4,        // EAS D matrix could not be factorised
   kStatusPatternOverflow = 8,  // a node couples with more nodes than the pattern builder supports
+  kStatusMaterialDomain = 16,  // a material evaluated outside its domain (Gent: Jm <= W1 - 3, gent.hh checkJm)
+};
+
+// Hyperelastic<Deviatoric<DF>, Volumetric<VF>> (materials/hyperelastic/): the deviatoric function and its
+// parameters, the volumetric function VF0..VF12 and its factor K (hyperelastic.cuh evaluates them)
+enum HyperDev : int {
+  kDevNone = 0,
+  kDevBlatzKo = 1,           // mu[0]
+  kDevOgdenTotal = 2,        // mu[0..n), alpha[0..n)
+  kDevOgdenDeviatoric = 3,   // mu[0..n), alpha[0..n)
+  kDevInvariantBased = 4,    // mu[0..n), p[0..n), q[0..n)
+  kDevArrudaBoyce = 5,       // mu[0], param = lambdaM
+  kDevGent = 6,              // mu[0], param = Jm
+};
+constexpr int kHyperMaxTerms = 4;
+struct HyperParams {
+  int dev = 0, n = 0;
+  double mu[kHyperMaxTerms] = {0, 0, 0, 0}, alpha[kHyperMaxTerms] = {0, 0, 0, 0};
+  int p[kHyperMaxTerms] = {0, 0, 0, 0}, q[kHyperMaxTerms] = {0, 0, 0, 0};
+  double param = 0;
+  int vol = 0;
+  double K = 0, beta = 0;
 };
 
 struct ElemArgs {
@@ -26,7 +48,8 @@ struct ElemArgs {
   const double* X = nullptr;     // coordinates, n_nodes x 3
   const int32_t* conn = nullptr; // corner-major: conn[v * n_elems + e]
   double lam = 0, mu = 0;        // Lame parameters
-  int material = 0;              // 0 NeoHooke, 1 StVenantKirchhoff
+  int material = 0;              // 0 NeoHooke, 1 StVenantKirchhoff, 2 BlatzKo, 3 hyperelastic framework (hyper)
+  HyperParams hyper;
   const double* lam_e = nullptr;  // per-element Lame parameters (nullptr: lam / mu for every element)
   const double* mu_e = nullptr;
   const double* u = nullptr;     // displacement, 3 * n_nodes (FP64)
@@ -88,6 +111,9 @@ void launch_disp_element(const ElemArgs& a, int mode, bool fp32_tangent, const i
                          cudaStream_t s);
 void launch_eas_element(const ElemArgs& a, int mode, bool fp32_tangent, const int32_t* list, int n_list, int e_base,
                         cudaStream_t s);
+// element_eas_hyper.cu: the same for material 3 (the hyperelastic framework)
+void launch_eas_element_hyper(const ElemArgs& a, int mode, bool fp32_tangent, const int32_t* list, int n_list,
+                              int e_base, cudaStream_t s);
 // the element's stored block of corner pair (I, J) for kElemBlocks, as (index p << 1) | transposed
 __host__ __device__ __forceinline__ int tangent_block_code(int I, int J) {
   const int d = (J - I) & 7;

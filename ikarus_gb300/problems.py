@@ -36,7 +36,8 @@ class Problem:
     t_end: float = 1.0
     tol: float = 1e-10
     relative: bool = False
-    material: int = 0  # 0 NeoHooke, 1 StVenantKirchhoff
+    material: int = 0  # 0 NeoHooke, 1 StVenantKirchhoff, 2 BlatzKo
+    hyper: object = None  # a Hyperelastic law (the hyperelastic framework) instead of ``material``
 
     @property
     def n_dofs(self):
@@ -210,8 +211,8 @@ def build_gpu(p: Problem, precision=0):
     """GPU objects for a problem: (FiniteElements, SparseFlatAssembler)."""
     from . import BlatzKo, FiniteElements, NeoHooke, Precision, SparseFlatAssembler, StVenantKirchhoff
     material = getattr(p, "material", 0)
-    law = {0: lambda: NeoHooke(p.lam, p.mu), 1: lambda: StVenantKirchhoff(p.lam, p.mu),
-           2: lambda: BlatzKo(p.mu)}[material]()
+    law = p.hyper if getattr(p, "hyper", None) is not None else {
+        0: lambda: NeoHooke(p.lam, p.mu), 1: lambda: StVenantKirchhoff(p.lam, p.mu), 2: lambda: BlatzKo(p.mu)}[material]()
     fes = FiniteElements(p.mesh.coords, p.mesh.conn, law, p.eas, p.n_eas)
     if p.face_elem is not None and len(p.face_elem):
         fes.add_neumann(p.face_elem, p.face_local, p.face_traction)

@@ -305,8 +305,43 @@ int ikr_linear_solver_coarse_info(ikr_ls ls, int32_t* out4);
  * neohooke.hh) or StVenantKirchhoff (svk.hh), both with the Lame parameters given at creation, or BlatzKo
  * (makeBlatzKo(mu), hyperelastic/factory.hh:34-39: deviatoric function on the total principal stretches, no
  * volumetric part) with the shear modulus given at creation (the first Lame parameter is not used) */
-enum { IKR_MATERIAL_NEOHOOKE = 0, IKR_MATERIAL_SVK = 1, IKR_MATERIAL_BLATZKO = 2 };
+enum { IKR_MATERIAL_NEOHOOKE = 0, IKR_MATERIAL_SVK = 1, IKR_MATERIAL_BLATZKO = 2, IKR_MATERIAL_HYPERELASTIC = 3 };
 int ikr_fes_set_material(ikr_fes fes, int32_t material);
+/* Hyperelastic<Deviatoric<DF>, Volumetric<VF>> (materials/hyperelastic/interface.hh): a deviatoric function of the
+ * principal stretches plus K U(J) with a volumetric function VF0..VF12 (volumetric/volumetricfunctions.hh).  The
+ * factories of hyperelastic/factory.hh map onto it: makeBlatzKo(mu) = {BLATZKO, mu}; makeOgden<n, tag>(mu, alpha,
+ * K, VF) = {OGDEN_TOTAL or OGDEN_DEVIATORIC, n, mu, alpha}; makeInvariantBased<n>(mu, p, q, K, VF) =
+ * {INVARIANT_BASED, n, mu, p, q}, makeMooneyRivlin(mu) its p = {1, 0}, q = {0, 1} and makeYeoh(mu) its
+ * p = {1, 2, 3}, q = {0, 0, 0}; makeArrudaBoyce({mu, lambdaM}) = {ARRUDA_BOYCE, mu[0], param = lambdaM};
+ * makeGent({mu, Jm}) = {GENT, mu[0], param = Jm}; makePureVolumetric(VF, K) = {NONE}. */
+enum {
+  IKR_DEV_NONE = 0,
+  IKR_DEV_BLATZKO = 1,
+  IKR_DEV_OGDEN_TOTAL = 2,
+  IKR_DEV_OGDEN_DEVIATORIC = 3,
+  IKR_DEV_INVARIANT_BASED = 4,
+  IKR_DEV_ARRUDA_BOYCE = 5,
+  IKR_DEV_GENT = 6
+};
+#define IKR_HYPER_MAX_TERMS 4
+typedef struct ikr_hyperelastic {
+  int32_t deviatoric;                /* IKR_DEV_* */
+  int32_t n_terms;                   /* Ogden / invariant-based terms, 1..IKR_HYPER_MAX_TERMS */
+  double mu[IKR_HYPER_MAX_TERMS];    /* Ogden mu_n, invariant-based C_n, else mu[0] = shear modulus */
+  double alpha[IKR_HYPER_MAX_TERMS]; /* Ogden exponents */
+  int32_t p[IKR_HYPER_MAX_TERMS];    /* invariant-based exponents of (W1 - 3) */
+  int32_t q[IKR_HYPER_MAX_TERMS];    /* invariant-based exponents of (W2 - 3) */
+  double param;                      /* Arruda-Boyce lambdaM, Gent Jm */
+  int32_t volumetric;                /* 0..12: VF0 (none) .. VF12 */
+  int32_t reserved;
+  double K;                          /* Volumetric(K, VF) */
+  double beta;                       /* VF4 / VF7 / VF10 parameter */
+} ikr_hyperelastic;
+/* sets IKR_MATERIAL_HYPERELASTIC with these functions on every element (displacement-based and EAS): residual,
+ * tangent (FP64 material point also under an FP32 tangent), energy and stresses.  IKR_ERR_ARG for an invalid
+ * description (InvariantBased with p_i = q_i = 0 throws in the reference); a Gent element evaluated at
+ * Jm <= W1 - 3 makes the call return IKR_ERR_INVALID_STATE (gent.hh checkJm throws InvalidStateException). */
+int ikr_fes_set_hyperelastic(ikr_fes fes, const ikr_hyperelastic* h);
 /* elements per block the displacement element kernel uses for residual / FP64 tangent / FP32 tangent
  * assembly (16, 32 or 64, chosen by timing at the first assembly of each kind; 0 = not assembled yet; no
  * reference counterpart) */

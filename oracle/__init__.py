@@ -21,7 +21,9 @@ _lib_unfused = None
 EAS_NONE, EAS_GL, EAS_H, EAS_HT = 0, 1, 2, 3
 DBC_RAW, DBC_REDUCED, DBC_FULL = 0, 1, 2
 SOLVER_BANDED_LDLT, SOLVER_CG_JACOBI = 0, 1
-MATERIAL_NEOHOOKE, MATERIAL_SVK, MATERIAL_BLATZKO = 0, 1, 2
+MATERIAL_NEOHOOKE, MATERIAL_SVK, MATERIAL_BLATZKO, MATERIAL_HYPERELASTIC = 0, 1, 2, 3
+DEV_NONE, DEV_BLATZKO, DEV_OGDEN_TOTAL, DEV_OGDEN_DEVIATORIC, DEV_INVARIANT_BASED, DEV_ARRUDA_BOYCE, DEV_GENT = range(7)
+HYPER_MAX_TERMS = 4
 PF_ARC_LENGTH, PF_LOAD_CONTROL, PF_DISPLACEMENT_CONTROL = 0, 1, 2
 ERRORS = {-1: "ARG", -2: "NOT_IMPLEMENTED", -3: "NONPOSITIVE_DETC", -4: "SINGULAR", -5: "NOT_CONVERGED"}
 
@@ -76,6 +78,10 @@ def _declare(L):
     L.orc_assemble_matrix_csc.argtypes = [vp, dp, C.c_double, C.c_int, lp, ip, dp]
     L.orc_set_dirichlet_values.argtypes = [vp, dp]
     L.orc_set_material.argtypes = [vp, C.c_int]
+    L.orc_set_hyperelastic.argtypes = [vp, C.POINTER(OrcHyper)]
+    L.orc_hyper_deviatoric.argtypes = [C.POINTER(OrcHyper), dp, dp]
+    L.orc_hyper_volumetric.argtypes = [C.c_int, C.c_double, C.c_double, dp]
+    L.orc_material_point.argtypes = [C.c_int, C.c_double, C.c_double, C.POINTER(OrcHyper), dp, dp]
     L.orc_calculate_at.argtypes = [vp, C.c_int, dp, C.c_int, dp, dp]
     L.orc_cg_jacobi_csc.argtypes = [C.c_int, lp, ip, dp, dp, dp, C.c_double, C.c_int, C.POINTER(C.c_int)]
     L.orc_load_control.argtypes = [vp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int,
@@ -92,6 +98,60 @@ def _declare(L):
     L.orc_path_following_toy.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_int, dp,
                                          dp, ip, dp, dp, C.POINTER(C.c_int)]
     return L
+
+
+class OrcHyper(C.Structure):
+    """orc_hyper: Hyperelastic<Deviatoric<DF>, Volumetric<VF>> (materials/hyperelastic/interface.hh)."""
+    _fields_ = [("deviatoric", C.c_int32), ("n_terms", C.c_int32), ("mu", C.c_double * HYPER_MAX_TERMS),
+                ("alpha", C.c_double * HYPER_MAX_TERMS), ("p", C.c_int32 * HYPER_MAX_TERMS),
+                ("q", C.c_int32 * HYPER_MAX_TERMS), ("param", C.c_double), ("volumetric", C.c_int32),
+                ("reserved", C.c_int32), ("K", C.c_double), ("beta", C.c_double)]
+
+
+def hyper(deviatoric, mu=(), alpha=(), p=(), q=(), param=0.0, volumetric=0, K=0.0, beta=0.0):
+    """An orc_hyper from plain values (mu: the deviatoric function's moduli or coefficients)."""
+    h = OrcHyper()
+    h.deviatoric, h.n_terms = int(deviatoric), len(mu)
+    for i, v in enumerate(mu):
+        h.mu[i] = v
+    for i, v in enumerate(alpha):
+        h.alpha[i] = v
+    for i, v in enumerate(p):
+        h.p[i] = v
+    for i, v in enumerate(q):
+        h.q[i] = v
+    h.param, h.volumetric, h.K, h.beta = float(param), int(volumetric), float(K), float(beta)
+    return h
+
+
+def _as_hyper(h):
+    return h if isinstance(h, OrcHyper) else hyper(**h)
+
+
+def hyper_deviatoric(h, stretches):
+    """(W, dW/dlambda (3), secondDerivative (3x3)) of the deviatoric function at the principal stretches."""
+    hh = _as_hyper(h)
+    lam = np.ascontiguousarray(stretches, dtype=np.float64)
+    out = np.zeros(13)
+    _check(lib().orc_hyper_deviatoric(C.byref(hh), _p(lam, C.c_double), _p(out, C.c_double)), "hyper_deviatoric")
+    return out[0], out[1:4].copy(), out[4:].reshape(3, 3).copy()
+
+
+def hyper_volumetric(vf, J, beta=0.0):
+    """(U, U', U'') of volumetric function VF<vf> at J."""
+    out = np.zeros(3)
+    _check(lib().orc_hyper_volumetric(int(vf), float(beta), float(J), _p(out, C.c_double)), "hyper_volumetric")
+    return tuple(out)
+
+
+def material_point(material, Cmat, lam=0.0, mu=0.0, h=None, unfused=False):
+    """(psi, S Voigt (6), moduli Voigt (6x6)) of a material law at the right Cauchy-Green tensor C (3x3)."""
+    hh = _as_hyper(h) if h is not None else OrcHyper()
+    c = np.ascontiguousarray(Cmat, dtype=np.float64).reshape(9)
+    out = np.zeros(43)
+    _check(lib(unfused).orc_material_point(int(material), float(lam), float(mu), C.byref(hh), _p(c, C.c_double),
+                                           _p(out, C.c_double)), "material_point")
+    return out[0], out[1:7].copy(), out[7:].reshape(6, 6).copy()
 
 
 _ORC_POINT_FN = C.CFUNCTYPE(None, C.c_int32, C.POINTER(C.c_double), C.c_double, C.POINTER(C.c_double), C.c_void_p)
@@ -158,7 +218,9 @@ def from_problem(p, faithful=False, unfused=False):
     o = OracleProblem(p.mesh.coords, p.mesh.conn, p.lam, p.mu, p.eas if p.n_eas else EAS_NONE, p.n_eas,
                       unfused=unfused)
     o.set_dirichlet(p.fixed)
-    if getattr(p, "material", 0):
+    if getattr(p, "hyper", None) is not None:  # a description with oracle_terms(), or the terms themselves
+        o.set_hyperelastic(p.hyper.oracle_terms() if hasattr(p.hyper, "oracle_terms") else p.hyper)
+    elif getattr(p, "material", 0):
         o.set_material(p.material)
     if p.face_elem is not None and len(p.face_elem):
         o.add_neumann(p.face_elem, p.face_local, p.face_traction)
@@ -205,6 +267,11 @@ class OracleProblem:
     def set_material(self, material):
         """MATERIAL_NEOHOOKE (default) or MATERIAL_SVK for all elements."""
         _check(self._L.orc_set_material(self.h, int(material)), "set_material")
+
+    def set_hyperelastic(self, h):
+        """MATERIAL_HYPERELASTIC with the functions of h (an OrcHyper or the keyword arguments of ``hyper``)."""
+        self._hyper = _as_hyper(h)
+        _check(self._L.orc_set_hyperelastic(self.h, C.byref(self._hyper)), "set_hyperelastic")
 
     def set_dirichlet_values(self, rate):
         """Inhomogeneous Dirichlet values lambda * rate on constrained dofs (None removes them)."""

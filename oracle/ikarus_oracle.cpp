@@ -236,10 +236,347 @@ void blatzko(double mu, const double Ev[6], MatState& m, bool wantTangent = true
     }
 }
 
-void material_law(int material, double lam, double mu, const double Ev[6], MatState& m, bool wantTangent = true) {
+// ---------------------------------------------------------------------------------------------------------------
+// Hyperelastic framework (materials/hyperelastic/): W(C) = W_dev(lambda_1, lambda_2, lambda_3) + K U(J) with the
+// principal stretches lambda_i = sqrt(eig_i(C)).
+// ---------------------------------------------------------------------------------------------------------------
+
+// Deviatoric invariants W1 = I1 I3^-1/3, W2 = I2 I3^-2/3 of the principal stretches with their first and second
+// derivatives (deviatoric/deviatoricinvariants.hh:38-104; invariants I1, I2, I3 materialhelpers.hh:189-201).
+struct DevInv {
+  double W1, W2, d1[3], d2[3], dd1[3][3], dd2[3][3];
+};
+void deviatoric_invariants(const double l[3], DevInv& o) {
+  const double l2[3] = {l[0] * l[0], l[1] * l[1], l[2] * l[2]};
+  const double I1 = l2[0] + l2[1] + l2[2];
+  const double I2 = l2[0] * l2[1] + l2[1] * l2[2] + l2[0] * l2[2];
+  const double I3 = l2[0] * l2[1] * l2[2];
+  const double c1 = std::pow(I3, 1.0 / 3.0), c2 = std::pow(I3, 2.0 / 3.0);
+  o.W1 = I1 * std::pow(I3, -1.0 / 3.0);
+  o.W2 = I2 * std::pow(I3, -2.0 / 3.0);
+  for (int i = 0; i < 3; ++i) {
+    o.d1[i] = 2.0 * (3.0 * l2[i] - I1) / (3.0 * l[i] * c1);
+    o.d2[i] = -2.0 * (3.0 * I3 / l2[i] - I2) / (3.0 * l[i] * c2);
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      if (i == j) {
+        o.dd1[i][i] = (2.0 / 9.0) * (5.0 * I1 - 3.0 * l2[i]) / (l2[i] * c1);
+        o.dd2[i][i] = (2.0 / 9.0) * (15.0 * I3 / l2[i] - I2) / (l2[i] * c2);
+      } else {
+        o.dd1[i][j] = (4.0 / 9.0) * (I1 - 3.0 * (l2[i] + l2[j])) / (l[i] * l[j] * c1);
+        o.dd2[i][j] = (-4.0 / 9.0) * (2.0 * I2 - 3.0 * l2[i] * l2[j]) / (l[i] * l[j] * c2);
+      }
+    }
+}
+
+// x^p m with the reference's conventions for m = 0 and p = 0 (invariantbased.hh powerAndMultiply)
+double pow_times(double x, int p, int m) {
+  if (m == 0) return 0.0;
+  if (p == 0) return m;
+  return std::pow(x, p) * m;
+}
+
+// W, dW/dlambda_i and the "second derivative" d2W/dlambda_i dlambda_j - delta_ij (dW/dlambda_i) / lambda_i that each
+// deviatoric function returns (secondDerivativeImpl of blatzko.hh, ogden.hh, invariantbased.hh, arrudaboyce.hh,
+// gent.hh; the Deviatoric wrapper divides by lambda_i lambda_j, deviatoric/interface.hh:91-118).
+struct DevOut {
+  double W, dW[3], dS[3][3];
+  bool domain_ok;  // Gent: Jm > W1 - 3 (gent.hh checkJm)
+};
+void deviatoric_function(const orc_hyper& h, const double l[3], DevOut& o) {
+  o.W = 0.0;
+  o.domain_ok = true;
+  for (int i = 0; i < 3; ++i) {
+    o.dW[i] = 0.0;
+    for (int j = 0; j < 3; ++j) o.dS[i][j] = 0.0;
+  }
+  const int n = h.n_terms;
+  switch (h.deviatoric) {
+    case ORC_DEV_NONE: return;
+    case ORC_DEV_BLATZKO: {  // blatzko.hh: W = mu/2 (sum lambda_i^-2 + 2 J - 5)
+      const double mu = h.mu[0], J = l[0] * l[1] * l[2];
+      o.W = mu / 2.0 * (1.0 / (l[0] * l[0]) + 1.0 / (l[1] * l[1]) + 1.0 / (l[2] * l[2]) + 2.0 * J - 5.0);
+      for (int i = 0; i < 3; ++i) o.dW[i] = mu * (-1.0 / (l[i] * l[i] * l[i]) + J / l[i]);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          const double li2 = l[i] * l[i];
+          o.dS[i][j] = mu * (i == j ? (1.0 / li2) * (1.0 / li2 - J) + 3.0 / (li2 * li2) : J / (l[i] * l[j]));
+        }
+      return;
+    }
+    case ORC_DEV_OGDEN_TOTAL: {  // ogden.hh: W = sum mu_p / alpha_p (sum_i lambda_i^alpha_p - 3) - mu_p ln J
+      const double lnJ = std::log(l[0] * l[1] * l[2]);
+      for (int p = 0; p < n; ++p) {
+        const double mu = h.mu[p], al = h.alpha[p];
+        double s = 0.0;
+        for (int i = 0; i < 3; ++i) s += std::pow(l[i], al);
+        o.W += mu / al * (s - 3.0) - mu * lnJ;
+        for (int i = 0; i < 3; ++i) {
+          const double la = std::pow(l[i], al);
+          o.dW[i] += mu * (la - 1.0) / l[i];
+          o.dS[i][i] += (-2.0 * mu * (la - 1.0) + mu * la * al) / (l[i] * l[i]);
+        }
+      }
+      return;
+    }
+    case ORC_DEV_OGDEN_DEVIATORIC: {  // ogden.hh with lambda_bar = J^-1/3 lambda (materialhelpers.hh:175-180)
+      const double Jm13 = std::pow(l[0] * l[1] * l[2], -1.0 / 3.0);
+      const double lb[3] = {Jm13 * l[0], Jm13 * l[1], Jm13 * l[2]};
+      double dWdlb[3] = {0.0, 0.0, 0.0}, powsum[ORC_HYPER_MAX_TERMS];
+      for (int p = 0; p < n; ++p) {
+        powsum[p] = 0.0;
+        for (int i = 0; i < 3; ++i) powsum[p] += std::pow(lb[i], h.alpha[p]);
+        o.W += h.mu[p] / h.alpha[p] * (powsum[p] - 3.0);
+        for (int i = 0; i < 3; ++i) dWdlb[i] += h.mu[p] * std::pow(lb[i], h.alpha[p] - 1.0);
+      }
+      const double sum = lb[0] * dWdlb[0] + lb[1] * dWdlb[1] + lb[2] * dWdlb[2];
+      for (int i = 0; i < 3; ++i) o.dW[i] = (lb[i] * dWdlb[i] - sum / 3.0) / l[i];
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+          double v = 0.0;
+          for (int p = 0; p < n; ++p) {
+            const double al = h.alpha[p];
+            if (a == b) v += h.mu[p] * al * (std::pow(lb[a], al) / 3.0 + powsum[p] / 9.0);
+            else v += h.mu[p] * al * (-(std::pow(lb[a], al) + std::pow(lb[b], al)) / 3.0 + powsum[p] / 9.0);
+          }
+          v /= l[a] * l[b];
+          if (a == b) v -= 2.0 / l[a] * o.dW[a];
+          o.dS[a][b] = v;
+        }
+      return;
+    }
+    case ORC_DEV_INVARIANT_BASED: {  // invariantbased.hh: W = sum C_p (W1 - 3)^p_p (W2 - 3)^q_p
+      DevInv d;
+      deviatoric_invariants(l, d);
+      const double W1 = d.W1 - 3.0, W2 = d.W2 - 3.0;
+      for (int p = 0; p < n; ++p) {
+        const int pe = h.p[p], qe = h.q[p];
+        const double c = h.mu[p];
+        const double W1p = std::pow(W1, pe), W2q = std::pow(W2, qe);
+        const double W1pm1p = pow_times(W1, pe - 1, pe), W2qm1q = pow_times(W2, qe - 1, qe);
+        const double W1pm2pp = pow_times(W1, pe - 2, pe * (pe - 1)), W2qm2qq = pow_times(W2, qe - 2, qe * (qe - 1));
+        o.W += c * W1p * W2q;
+        for (int k = 0; k < 3; ++k) o.dW[k] += c * (W1pm1p * W2q * d.d1[k] + W1p * W2qm1q * d.d2[k]);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            const double cross = d.d1[i] * d.d2[j] + d.d1[j] * d.d2[i];
+            double v = (W2qm1q * cross + W2q * d.dd1[i][j]) * W1pm1p * c + W2qm1q * d.dd2[i][j] * W1p * c +
+                       W1pm2pp * W2q * d.d1[i] * d.d1[j] * c + W2qm2qq * W1p * d.d2[i] * d.d2[j] * c;
+            if (i == j) v -= (1.0 / l[i]) * c * (W1pm1p * W2q * d.d1[i] + W1p * W2qm1q * d.d2[i]);
+            o.dS[i][j] += v;
+          }
+      }
+      return;
+    }
+    case ORC_DEV_ARRUDA_BOYCE: {  // arrudaboyce.hh: W = mu sum_p a_p beta^p (W1^(p+1) - 3^(p+1)), beta = lambdaM^-2
+      static const double a[5] = {0.5, 1.0 / 20.0, 11.0 / 1050.0, 19.0 / 7000.0, 519.0 / 673750.0};
+      DevInv d;
+      deviatoric_invariants(l, d);
+      const double mu = h.mu[0], beta = 1.0 / (h.param * h.param), W1 = d.W1;
+      for (int p = 0; p < 5; ++p) {
+        const double f1 = mu * a[p] * std::pow(beta, p);
+        o.W += a[p] * std::pow(beta, p) * (std::pow(W1, p + 1) - std::pow(3.0, p + 1));
+        for (int k = 0; k < 3; ++k) o.dW[k] += f1 * std::pow(W1, p) * d.d1[k] * (p + 1);
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) {
+            double v = f1 * (std::pow(W1, p) * d.dd1[i][j] * (p + 1) + std::pow(W1, p - 1) * d.d1[i] * d.d1[j] * p * (p + 1));
+            if (i == j) v -= d.d1[i] / l[i] * f1 * std::pow(W1, p) * (p + 1);
+            o.dS[i][j] += v;
+          }
+      }
+      o.W *= mu;
+      return;
+    }
+    case ORC_DEV_GENT: {  // gent.hh: W = -mu/2 Jm ln(1 - (W1 - 3) / Jm)
+      DevInv d;
+      deviatoric_invariants(l, d);
+      const double mu = h.mu[0], Jm = h.param, W1 = d.W1;
+      // checkJm: FloatCmp::le(Jm, W1 - 3, 1e-14) throws
+      const double x = W1 - 3.0;
+      if (Jm < x || std::fabs(Jm - x) <= 1e-14 * std::max(std::fabs(Jm), std::fabs(x))) o.domain_ok = false;
+      o.W = -(mu / 2.0) * Jm * std::log(1.0 - (W1 - 3.0) / Jm);
+      for (int k = 0; k < 3; ++k) o.dW[k] = (mu * d.d1[k] * Jm) / (2.0 * (Jm - W1) + 6.0);
+      const double f1 = 1.0 - (W1 - 3.0) / Jm;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double v = (mu / (2.0 * f1)) * (d.dd1[i][j] + (d.d1[i] * d.d1[j] / (f1 * Jm)));
+          if (i == j) v -= (mu / (2.0 * l[i] * f1)) * d.d1[i];
+          o.dS[i][j] = v;
+        }
+      return;
+    }
+    default: o.domain_ok = false;
+  }
+}
+
+// volumetric functions U(J), U'(J), U''(J) (volumetricfunctions.hh VF0..VF12); Volumetric multiplies them by K
+void volumetric_function(int vf, double b, double J, double U[3]) {
+  const double lJ = std::log(J);
+  switch (vf) {
+    case 1: U[0] = 0.5 * (J - 1) * (J - 1), U[1] = J - 1, U[2] = 1; break;
+    case 2:
+      U[0] = 0.25 * ((J - 1) * (J - 1) + lJ * lJ);
+      U[1] = 0.5 * (J - 1 + 1 / J * lJ);
+      U[2] = 1 / (2 * J * J) * (1 + J * J - lJ);
+      break;
+    case 3: U[0] = 0.5 * lJ * lJ, U[1] = 1 / J * lJ, U[2] = 1 / (J * J) * (1 - lJ); break;
+    case 4:
+      U[0] = (1 / (b * b)) * ((1 / std::pow(J, b)) - 1 + b * lJ);
+      U[1] = (1 / b) * ((1 / J) - (1 / std::pow(J, 1 + b)));
+      U[2] = (1 / b) * ((1 / std::pow(J, 2 + b)) * (1 + b - std::pow(J, b)));
+      break;
+    case 5: U[0] = 0.25 * (J * J - 1 - 2 * lJ), U[1] = 0.5 * (J - 1 / J), U[2] = 0.5 * (1 + 1 / (J * J)); break;
+    case 6: U[0] = J - lJ - 1, U[1] = 1 - 1 / J, U[2] = 1 / (J * J); break;
+    case 7:
+      U[0] = std::pow(J, b) * (b * lJ - 1) + 1;
+      U[1] = b * b * (1.0 / std::pow(J, 1.0 - b)) * lJ;
+      U[2] = b * b * std::pow(J, b - 2.0) * (1 + (b - 1) * lJ);
+      break;
+    case 8: U[0] = J * lJ - J + 1, U[1] = lJ, U[2] = 1 / J; break;
+    case 9:
+      U[0] = (1.0 / 32.0) * (J * J - 1 / (J * J)) * (J * J - 1 / (J * J));
+      U[1] = (1.0 / 8.0) * (std::pow(J, 3) - 1.0 / std::pow(J, 5));
+      U[2] = (1.0 / 8.0) * (5.0 * std::pow(J, -6) + 3.0 * J * J);
+      break;
+    case 10:
+      U[0] = (J / b) * (1 - (std::pow(J, -b) / (1 - b))) + (1.0 / (b - 1));
+      U[1] = (1 / b) * (1 - std::pow(J, -b));
+      U[2] = std::pow(J, -1 - b);
+      break;
+    case 11:
+      U[0] = (1.0 / 50.0) * (std::pow(J, 5.0) + std::pow(J, -5.0) - 2.0);
+      U[1] = (1.0 / 10.0) * (std::pow(J, 4.0) - std::pow(J, -6.0));
+      U[2] = (1.0 / 10.0) * (4 * std::pow(J, 3.0) + 6 * std::pow(J, -7.0));
+      break;
+    case 12: U[0] = J - 1, U[1] = 1, U[2] = 0; break;
+    default: U[0] = U[1] = U[2] = 0; break;  // VF0
+  }
+}
+
+// Eigen decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations (Jacobi 1846; Golub & Van Loan,
+// "Matrix Computations", sec. 8.5: the stable choice t = sign(theta) / (|theta| + sqrt(theta^2 + 1))).  The
+// reference calls Eigen's SelfAdjointEigenSolver (materialhelpers.hh:139-152), whose algorithm is not part of the
+// reference; any backward-stable solver gives the same stresses and moduli up to rounding, since these are
+// functions of C alone.  Eigenvalues ascending (as Eigen returns them), eigenvectors in the columns of V.
+void sym_eig3(const double A[3][3], double ev[3], double V[3][3]) {
+  double a[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      a[i][j] = A[i][j];
+      V[i][j] = i == j ? 1.0 : 0.0;
+    }
+  static const int P[3] = {0, 0, 1}, Q[3] = {1, 2, 2};
+  for (int sweep = 0; sweep < 32; ++sweep) {
+    if (a[0][1] == 0.0 && a[0][2] == 0.0 && a[1][2] == 0.0) break;
+    for (int r = 0; r < 3; ++r) {
+      const int p = P[r], q = Q[r];
+      const double apq = a[p][q];
+      if (apq == 0.0) continue;
+      if (std::fabs(a[p][p]) + 100.0 * std::fabs(apq) == std::fabs(a[p][p]) &&
+          std::fabs(a[q][q]) + 100.0 * std::fabs(apq) == std::fabs(a[q][q])) {
+        a[p][q] = a[q][p] = 0.0;  // below the diagonal's resolution
+        continue;
+      }
+      const double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
+      double t = 1.0 / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+      if (std::fabs(theta) > 1e150) t = 0.5 / std::fabs(theta);
+      if (theta < 0.0) t = -t;
+      const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+      const int o = 3 - p - q;  // the third index
+      const double aop = a[o][p], aoq = a[o][q];
+      a[p][p] -= t * apq;
+      a[q][q] += t * apq;
+      a[p][q] = a[q][p] = 0.0;
+      a[o][p] = a[p][o] = c * aop - s * aoq;
+      a[o][q] = a[q][o] = s * aop + c * aoq;
+      for (int k = 0; k < 3; ++k) {
+        const double vkp = V[k][p], vkq = V[k][q];
+        V[k][p] = c * vkp - s * vkq;
+        V[k][q] = s * vkp + c * vkq;
+      }
+    }
+  }
+  for (int i = 0; i < 3; ++i) ev[i] = a[i][i];
+  // ascending order, columns of V along
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2 - i; ++j)
+      if (ev[j] > ev[j + 1]) {
+        std::swap(ev[j], ev[j + 1]);
+        for (int k = 0; k < 3; ++k) std::swap(V[k][j], V[k][j + 1]);
+      }
+}
+
+// Hyperelastic::stressesImpl / tangentModuliImpl / storedEnergyImpl (hyperelastic/interface.hh:106-160, 180-214):
+// S = sum_i (dW_i / lambda_i) N_i (x) N_i + J U' C^-1; moduli = sum_ik L_iikk (N_i N_i)(N_k N_k) +
+// sum_{i != k} L_ikik (N_i N_k)(N_i N_k + N_k N_i) + J (U' + J U'') C^-1 (x) C^-1 - J U' (C^-1 (.) C^-1 sym), with
+// L_iikk = dS_ik / (lambda_i lambda_k) and L_ikik = (S_i - S_k) / (lambda_i^2 - lambda_k^2), or
+// (L_iiii - L_iikk) / 2 for equal stretches (FloatCmp::eq with 1e-8; deviatoric/interface.hh:91-118).
+void hyperelastic(const orc_hyper& h, const double Ev[6], MatState& m, bool wantTangent, bool* domain_ok = nullptr) {
+  double C[3][3];
+  for (int i = 0; i < 3; ++i) C[i][i] = 2.0 * Ev[i] + 1.0;
+  C[1][2] = C[2][1] = Ev[3];
+  C[0][2] = C[2][0] = Ev[4];
+  C[0][1] = C[1][0] = Ev[5];
+  double ev[3], N[3][3];
+  sym_eig3(C, ev, N);
+  const double l[3] = {std::sqrt(ev[0]), std::sqrt(ev[1]), std::sqrt(ev[2])};
+  const double J = l[0] * l[1] * l[2];  // detF from the principal values (interface.hh:245-253)
+  m.ok = J * J > 1e-10 && J > 0.0;
+  DevOut d;
+  deviatoric_function(h, l, d);
+  if (domain_ok) *domain_ok = d.domain_ok;
+  double U[3];
+  volumetric_function(h.volumetric, h.beta, J, U);
+  const double K = h.K;
+  m.psi = d.W + K * U[0];
+  double Ci[3][3];
+  inv3(C, Ci);
+  const double Sp[3] = {d.dW[0] / l[0], d.dW[1] / l[1], d.dW[2] / l[2]};
+  // Voigt dyads of the principal directions: nn[i][v] = N_Ai N_Bi
+  double nn[3][6];
+  for (int v = 0; v < 6; ++v)
+    for (int i = 0; i < 3; ++i) nn[i][v] = N[VA[v]][i] * N[VB[v]][i];
+  const double vs = J * K * U[1];
+  for (int v = 0; v < 6; ++v) m.S[v] = Sp[0] * nn[0][v] + Sp[1] * nn[1][v] + Sp[2] * nn[2][v] + vs * Ci[VA[v]][VB[v]];
+  if (!wantTangent) return;
+  double L[3][3], Lo[3][3];  // L_iikk and, off the diagonal, L_ikik
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) L[i][k] = d.dS[i][k] / (l[i] * l[k]);
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) {
+      if (i == k) {
+        Lo[i][k] = 0.0;
+        continue;
+      }
+      if (std::fabs(l[i] - l[k]) <= 1e-8 * std::max(std::fabs(l[i]), std::fabs(l[k])))
+        Lo[i][k] = 0.5 * (L[i][i] - L[i][k]);
+      else Lo[i][k] = (Sp[i] - Sp[k]) / (l[i] * l[i] - l[k] * l[k]);
+    }
+  const double v1 = J * K * (U[1] + J * U[2]), v2 = J * K * U[1];
+  for (int r = 0; r < 6; ++r)
+    for (int s = 0; s < 6; ++s) {
+      const int A = VA[r], B = VB[r], Cc = VA[s], D = VB[s];
+      double c = 0.0;
+      for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k) {
+          c += L[i][k] * nn[i][r] * nn[k][s];
+          if (i != k) c += Lo[i][k] * N[A][i] * N[B][k] * (N[Cc][i] * N[D][k] + N[Cc][k] * N[D][i]);
+        }
+      c += v1 * Ci[A][B] * Ci[Cc][D] - v2 * (Ci[A][Cc] * Ci[B][D] + Ci[A][D] * Ci[B][Cc]);
+      m.C6[r][s] = c;
+    }
+}
+
+void material_law(int material, double lam, double mu, const orc_hyper* h, const double Ev[6], MatState& m,
+                  bool wantTangent = true) {
   if (material == ORC_MATERIAL_SVK) svk(lam, mu, Ev, m, wantTangent);
   else if (material == ORC_MATERIAL_BLATZKO) blatzko(mu, Ev, m, wantTangent);
-  else neohooke(lam, mu, Ev, m, wantTangent);
+  else if (material == ORC_MATERIAL_HYPERELASTIC) {
+    bool dom = true;
+    hyperelastic(*h, Ev, m, wantTangent, &dom);
+    if (!dom) m.ok = false;
+  } else neohooke(lam, mu, Ev, m, wantTangent);
 }
 
 // Green-Lagrange strain of a displacement gradient, Voigt with doubled shears
@@ -298,7 +635,8 @@ struct orc_problem {
   std::vector<double> X;      // nn*3
   std::vector<int32_t> conn;  // ne*8
   double lam = 0, mu = 0;
-  int material = 0;  // ORC_MATERIAL_NEOHOOKE / ORC_MATERIAL_SVK
+  int material = 0;  // ORC_MATERIAL_*
+  orc_hyper hyper{};  // the functions of ORC_MATERIAL_HYPERELASTIC
   int eas = 0, na = 0;
   bool faithful = false;
   std::vector<uint8_t> fixed;   // n dofs
@@ -480,7 +818,7 @@ void element_internal(const orc_problem& p, int e, const double* u, bool wantK, 
         for (int k = 0; k < na; ++k) Ev[r] += M[r][k] * al[k];
 
     MatState m;
-    material_law(p.material, p.lam, p.mu, Ev, m, true);
+    material_law(p.material, p.lam, p.mu, &p.hyper, Ev, m, true);
     if (!m.ok) out.ok = false;
     out.energy += m.psi * wdJ;
     double Smat[3][3];
@@ -512,7 +850,7 @@ void element_internal(const orc_problem& p, int e, const double* u, bool wantK, 
           MatState mm;
           const MatState* mp = &m;
           if (p.faithful) {  // the reference evaluates the moduli inside the (i,j) loop
-            material_law(p.material, p.lam, p.mu, Ev, mm, true);
+            material_law(p.material, p.lam, p.mu, &p.hyper, Ev, mm, true);
             mp = &mm;
           }
           double CB[6][3];
@@ -1115,6 +1453,60 @@ int orc_set_material(orc_problem* p, int material) {
   p->material = material;
   return ORC_OK;
 }
+
+namespace {
+bool hyper_valid(const orc_hyper* h) {
+  if (!h || h->deviatoric < ORC_DEV_NONE || h->deviatoric > ORC_DEV_GENT) return false;
+  if (h->volumetric < 0 || h->volumetric > 12) return false;
+  const bool terms = h->deviatoric == ORC_DEV_OGDEN_TOTAL || h->deviatoric == ORC_DEV_OGDEN_DEVIATORIC ||
+                     h->deviatoric == ORC_DEV_INVARIANT_BASED;
+  if (terms && (h->n_terms < 1 || h->n_terms > ORC_HYPER_MAX_TERMS)) return false;
+  if (h->deviatoric == ORC_DEV_INVARIANT_BASED)
+    for (int i = 0; i < h->n_terms; ++i)  // checkExponents (invariantbased.hh): p_i = q_i = 0 throws
+      if (h->p[i] < 0 || h->q[i] < 0 || (h->p[i] == 0 && h->q[i] == 0)) return false;
+  if ((h->deviatoric == ORC_DEV_ARRUDA_BOYCE || h->deviatoric == ORC_DEV_GENT) && !(h->param > 0.0)) return false;
+  return true;
+}
+}  // namespace
+
+int orc_set_hyperelastic(orc_problem* p, const orc_hyper* h) {
+  if (!p || !hyper_valid(h)) return ORC_ERR_ARG;
+  p->hyper = *h;
+  p->material = ORC_MATERIAL_HYPERELASTIC;
+  return ORC_OK;
+}
+
+int orc_hyper_deviatoric(const orc_hyper* h, const double* lambda, double* out13) {
+  if (!hyper_valid(h) || !lambda || !out13) return ORC_ERR_ARG;
+  DevOut d;
+  deviatoric_function(*h, lambda, d);
+  out13[0] = d.W;
+  for (int i = 0; i < 3; ++i) out13[1 + i] = d.dW[i];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) out13[4 + 3 * i + j] = d.dS[i][j];
+  return d.domain_ok ? ORC_OK : ORC_ERR_ARG;
+}
+
+int orc_hyper_volumetric(int vf, double beta, double J, double* out3) {
+  if (vf < 0 || vf > 12 || !out3) return ORC_ERR_ARG;
+  volumetric_function(vf, beta, J, out3);
+  return ORC_OK;
+}
+
+int orc_material_point(int material, double lambda, double mu, const orc_hyper* h, const double* C, double* out43) {
+  if (!C || !out43 || material < ORC_MATERIAL_NEOHOOKE || material > ORC_MATERIAL_HYPERELASTIC) return ORC_ERR_ARG;
+  if (material == ORC_MATERIAL_HYPERELASTIC && !hyper_valid(h)) return ORC_ERR_ARG;
+  double Ev[6];
+  for (int i = 0; i < 3; ++i) Ev[i] = 0.5 * (C[4 * i] - 1.0);
+  Ev[3] = C[5], Ev[4] = C[2], Ev[5] = C[1];  // doubled shears 2 E_ij = C_ij
+  MatState m;
+  material_law(material, lambda, mu, h, Ev, m, true);
+  out43[0] = m.psi;
+  for (int v = 0; v < 6; ++v) out43[1 + v] = m.S[v];
+  for (int r = 0; r < 6; ++r)
+    for (int s = 0; s < 6; ++s) out43[7 + 6 * r + s] = m.C6[r][s];
+  return m.ok ? ORC_OK : ORC_ERR_NONPOSITIVE_DETC;
+}
 int orc_set_dirichlet(orc_problem* p, const uint8_t* f) {
   if (!p || !f) return ORC_ERR_ARG;
   for (int i = 0; i < p->ndof(); ++i) p->fixed[i] = f[i] ? 1 : 0;
@@ -1275,7 +1667,7 @@ int orc_calculate_at(orc_problem* p, int e, const double* u, int type, const dou
     }
   }
   MatState m;
-  material_law(p->material, p->lam, p->mu, Ev, m, false);
+  material_law(p->material, p->lam, p->mu, &p->hyper, Ev, m, false);
   if (!m.ok) return ORC_ERR_NONPOSITIVE_DETC;
   if (type == 0) {
     std::copy(m.S, m.S + 6, out6);

@@ -37,7 +37,30 @@ enum {
 enum { ORC_EAS_NONE = 0, ORC_EAS_GL = 1, ORC_EAS_H = 2, ORC_EAS_HT = 3 };
 /* DBCOption (ikarus/assembler/dirichletbcenforcement.hh:8) */
 enum { ORC_DBC_RAW = 0, ORC_DBC_REDUCED = 1, ORC_DBC_FULL = 2 };
-enum { ORC_MATERIAL_NEOHOOKE = 0, ORC_MATERIAL_SVK = 1, ORC_MATERIAL_BLATZKO = 2 };
+enum { ORC_MATERIAL_NEOHOOKE = 0, ORC_MATERIAL_SVK = 1, ORC_MATERIAL_BLATZKO = 2, ORC_MATERIAL_HYPERELASTIC = 3 };
+
+/* Hyperelastic<Deviatoric<DF>, Volumetric<VF>> (materials/hyperelastic/interface.hh): a deviatoric function of the
+ * principal stretches plus K U(J).  Deviatoric functions (hyperelastic/deviatoric/): NoDev, BlatzKo, Ogden with
+ * total or deviatoric stretches, InvariantBased (Mooney-Rivlin, Yeoh), ArrudaBoyce, Gent.  Volumetric functions
+ * VF0..VF12 (hyperelastic/volumetric/volumetricfunctions.hh). */
+enum {
+  ORC_DEV_NONE = 0,
+  ORC_DEV_BLATZKO = 1,           /* mu[0] */
+  ORC_DEV_OGDEN_TOTAL = 2,       /* mu[0..n), alpha[0..n) */
+  ORC_DEV_OGDEN_DEVIATORIC = 3,  /* mu[0..n), alpha[0..n) */
+  ORC_DEV_INVARIANT_BASED = 4,   /* mu[0..n) (the C_pq), p[0..n), q[0..n) */
+  ORC_DEV_ARRUDA_BOYCE = 5,      /* mu[0], param = lambdaM */
+  ORC_DEV_GENT = 6               /* mu[0], param = Jm */
+};
+#define ORC_HYPER_MAX_TERMS 4
+typedef struct orc_hyper {
+  int32_t deviatoric, n_terms;
+  double mu[ORC_HYPER_MAX_TERMS], alpha[ORC_HYPER_MAX_TERMS];
+  int32_t p[ORC_HYPER_MAX_TERMS], q[ORC_HYPER_MAX_TERMS];
+  double param;
+  int32_t volumetric, reserved; /* VF0..VF12 */
+  double K, beta;               /* Volumetric(K, VF), beta of VF4 / VF7 / VF10 */
+} orc_hyper;
 /* linear solvers of the oracle */
 enum { ORC_SOLVER_BANDED_LDLT = 0, ORC_SOLVER_CG_JACOBI = 1 };
 
@@ -49,6 +72,16 @@ void orc_problem_destroy(orc_problem* p);
 /* material law of all elements: NeoHooke (default, neohooke.hh), StVenantKirchhoff (svk.hh) or BlatzKo
  * (makeBlatzKo(mu), hyperelastic/factory.hh:34-39; uses mu only) */
 int orc_set_material(orc_problem* p, int material);
+/* material law ORC_MATERIAL_HYPERELASTIC with these functions (ORC_ERR_ARG for an invalid description) */
+int orc_set_hyperelastic(orc_problem* p, const orc_hyper* h);
+/* deviatoric function at principal stretches lambda[3]: out = {W, dW/dlambda_i (3), secondDerivative (3x3 row-major)},
+ * the three functions of each DF (storedEnergyImpl, firstDerivativeImpl, secondDerivativeImpl) */
+int orc_hyper_deviatoric(const orc_hyper* h, const double* lambda, double* out13);
+/* volumetric function (without K) at J: out = {U, U', U''} */
+int orc_hyper_volumetric(int vf, double beta, double J, double* out3);
+/* material point of any law at the right Cauchy-Green tensor C (3x3 row-major): out = {psi, S Voigt (6),
+ * material moduli Voigt (6x6 row-major)}; ORC_ERR_NONPOSITIVE_DETC when det C fails the check */
+int orc_material_point(int material, double lambda, double mu, const orc_hyper* h, const double* C, double* out43);
 int orc_set_dirichlet(orc_problem* p, const uint8_t* fixed_dofs);
 /* Dead Neumann load on element faces (Dune face numbering: 2d -> xi_d = 0, 2d+1 -> xi_d = 1).
  * traction: 3 values per face = t(X_face_center, lambda = 1); the applied load is lambda * t. */
