@@ -232,6 +232,7 @@ SIGNATURES = {
     "ikr_linear_solver_profile_read": ([_vp, _dp, _i64p], C.c_int),
     "ikr_linear_solver_set_launch": ([_vp, _I, _I], C.c_int),
     "ikr_linear_solver_set_kernel": ([_vp, _I, _D], C.c_int),
+    "ikr_cg_kind_ranges": ([_ip], C.c_int),
     "ikr_linear_solver_kernel_info": ([_vp, _ip, _dp, _dp], C.c_int),
     "ikr_fes_stream": ([_vp, C.POINTER(_vp)], C.c_int),
     "ikr_linear_solver_solve_noalloc": ([_vp, _vp, _vp, _D, _I, _ip], C.c_int),
@@ -1046,8 +1047,16 @@ class LinearSolver:
         """CG iterations per host poll, issued as CUDA graphs or kernel by kernel."""
         _err(lib().ikr_linear_solver_set_launch(self.h, int(use_graphs), int(chunk_len)))
 
+    @staticmethod
+    def kind_ranges():
+        """{"staged", "persistent", "coarse_fused", "count"}: the first CG kind of each family and the number of kinds."""
+        out = (C.c_int32 * 4)()
+        _err(lib().ikr_cg_kind_ranges(out))
+        return dict(zip(("staged", "persistent", "coarse_fused", "count"), list(out)))
+
     def set_kernel(self, spmv_kind=-1, l2_keep_fraction=-1.0):
-        """SpMV kernel (0 direct, 1..4 staged, -1 autotune) and L2 keep fraction (-1 autotune)."""
+        """CG kernel (0 direct-load SpMV, then the staged, persistent and fused-coarse kinds of ``kind_ranges``; -1
+        autotune) and L2 keep fraction (-1 autotune)."""
         _err(lib().ikr_linear_solver_set_kernel(self.h, int(spmv_kind), float(l2_keep_fraction)))
 
     def set_multi_rhs(self, on=True):
@@ -1076,7 +1085,8 @@ class LinearSolver:
     def set_coarse_space(self, n_slabs):
         """Coarse correction of the block-Jacobi CG (0 = off, the default): n_slabs in [1, 128] slabs of equal node
         count along the mesh's longest extent, six rigid-body modes each, A_c = P^T K P rebuilt at every
-        factorize (an additive two-level preconditioner; two-kernel CG forms only)."""
+        factorize (an additive two-level preconditioner; two-kernel CG forms, or with at most 64 slabs the persistent
+        kernel with the correction fused in, which the tuner prefers)."""
         _err(lib().ikr_linear_solver_set_coarse_space(self.h, int(n_slabs)))
 
     def coarse_info(self):

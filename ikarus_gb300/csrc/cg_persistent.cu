@@ -17,97 +17,13 @@
 // gives up sets scal[kDone] = 6, the kernel drains its copies in flight (bounded) and returns.
 #include <mutex>
 
-#include "staging.cuh"
+#include "cg_grid.cuh"
 
 namespace ikr {
 
 namespace {
 
 using namespace cg;
-
-constexpr int kBarrierSpinLimit = 1 << 24;  // polls (with a short sleep) before a grid barrier gives up
-
-// CTA sums of N values: valid in thread 0 only (one __syncthreads; sw holds WARPS x N doubles)
-template <int N>
-__device__ __forceinline__ void cta_reduce(double (&v)[N], double* sw) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-#pragma unroll
-  for (int k = 0; k < N; ++k) {
-    const double s = warp_sum(v[k]);
-    if (lane == 0) sw[warp * N + k] = s;
-  }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      double s = lane < (int)(blockDim.x >> 5) ? sw[lane * N + k] : 0.0;
-      v[k] = warp_sum(s);
-    }
-  }
-}
-
-// Grid-wide sums of N values whose CTA sums are in thread 0: thread 0 publishes them at part[cta * N + k],
-// arrives on the barrier counter and waits (bounded) until `target` arrivals; then warp 0 sums all CTAs'
-// partials with a fixed lane assignment and butterfly order (identical in every CTA) and every thread gets
-// the sums.  Returns false when the wait gave up.
-// WaitCtl: the poll limit, and (tests of the bounded wait only) CTA 0 withholding its arrival at the first barrier,
-// so that every CTA's first wait runs out and the solve ends with the timeout status.
-struct WaitCtl {
-  int polls;
-  int withhold_first;
-};
-
-template <int N>
-__device__ __forceinline__ bool grid_allreduce(double (&v)[N], double* part, unsigned int* count, unsigned int target,
-                                               double* sv, bool* ok_sh, WaitCtl wc) {
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) part[blockIdx.x * N + k] = v[k];
-    __threadfence();
-    if (!(wc.withhold_first && blockIdx.x == 0 && target == gridDim.x)) atomicAdd(count, 1u);
-    bool ok = false;
-    for (int i = 0; i < wc.polls; ++i) {
-      unsigned int c;
-      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(count) : "memory");
-      if (c >= target) {
-        ok = true;
-        break;
-      }
-      if (i > 64) __nanosleep(16);
-    }
-    *ok_sh = ok;
-  }
-  __syncthreads();
-  __threadfence();  // every thread: its later plain loads observe what the other CTAs wrote before arriving
-  if (!*ok_sh) return false;
-  if (threadIdx.x < 32) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      double s = 0.0;
-      for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) s += __ldcg(part + (size_t)i * N + k);
-      s = warp_sum(s);
-      if (threadIdx.x == 0) sv[k] = s;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < N; ++k) v[k] = sv[k];
-  return true;
-}
-
-template <typename T, int CB, int NST, int WARPS>
-struct PersistentCfg {
-  static constexpr int kValBytes = CB * 288 * (int)sizeof(T);
-  static constexpr int kColBytes = CB * 32 * 4;
-  static constexpr int kStageBytes = kValBytes + kColBytes;
-  static constexpr int kSmemBytes = WARPS * NST * kStageBytes;
-  static constexpr int kThreads = WARPS * 32;
-};
-
-// cyclic position in a warp's chunk stream: owned slice j (slice gw + j * nw), first block g, slice end gend
-struct CyclicPos {
-  int j, g, gend;
-};
 
 // the right-hand sides one launch solves together: per RHS its solution, residual, preconditioned residual, the
 // two search-direction buffers (alternating by iteration parity) and its scalar block

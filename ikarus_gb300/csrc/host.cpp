@@ -1056,9 +1056,18 @@ int ikr_fes_kernel_info(ikr_fes fes, int32_t* epb_residual, int32_t* epb_tangent
     if (epb_tangent32) *epb_tangent32 = fes->epb_k32;
   });
 }
+int ikr_cg_kind_ranges(int32_t* out4) {
+  return guarded([&] {
+    need(out4, IKR_ERR_ARG, "null argument");
+    out4[0] = 1;
+    out4[1] = ikr_ls_s::first_persistent_kind();
+    out4[2] = ikr_ls_s::first_coarse_kind();
+    out4[3] = out4[2] + ikr::pcg_coarse_variants();
+  });
+}
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t kind, double keep) {
   return guarded([&] {
-    need(ls && kind >= -1 && kind <= ikr::spmv_staged_variants() + ikr::pcg_persistent_variants() &&
+    need(ls && kind >= -1 && kind <= ikr::spmv_staged_variants() + ikr::pcg_persistent_variants() + ikr::pcg_coarse_variants() &&
              (keep == -1.0 || (keep >= 0.0 && keep < 1.0)),
          IKR_ERR_ARG, "invalid SpMV kernel choice");
     ls->set_kernel(kind, keep);

@@ -516,7 +516,7 @@ struct ikr_ls_s {
     DBuf<float> y4;
     DBuf<int32_t> nodes, chunk_off, agg_chunk, agg_colour;
     std::vector<int32_t> agg_chunk_h;
-    DBuf<double> rpart, gpart, V, W, ainv64, e64;
+    DBuf<double> rpart, gpart, V, W, ainv64, e64, cpart;
     DBuf<float> ainv32, e32;
     std::vector<double> gpart_h, ac, inv, fac;
     std::vector<float> inv32;
@@ -664,12 +664,15 @@ struct ikr_ls_s {
     ikr::launch_block_jacobi(a->bsr(), fp32, w.minv, point_jacobi, a->fes->stream);
     count(1);
     factorized = true;
-    if (tag != IKR_SOLVER_GPU_PCG_BATCHED && tuned_for != a) tune(a);
     w.coarse = 0;
+    if (coarse_req > 0) coarse_operator(a);  // before the tuner: the fused kinds are timed with it
+    if (tag != IKR_SOLVER_GPU_PCG_BATCHED && tuned_for != a) tune(a);
     if (coarse_req > 0) {
-      if (persistent()) fail(IKR_ERR_ARG, "the coarse correction runs with the two-kernel CG kinds only");
-      coarse_operator(a);
+      if (persistent())
+        fail(IKR_ERR_ARG, "the coarse correction runs with the two-kernel CG kinds or the fused coarse kinds only");
       w.coarse = 1;
+    } else if (coarse_fused()) {
+      fail(IKR_ERR_ARG, "the fused coarse CG kinds need a coarse space (set_coarse_space)");
     }
   }
 
@@ -769,6 +772,9 @@ struct ikr_ls_s {
     cudaStream_t s = a->fes->stream;
     const ikr::Bsr A = a->bsr();
     const int S = co.n_slabs, nc = 6 * S, nch = co.C.n_chunks, ncol = co.n_colours;
+    co.cpart.alloc(2 * (size_t)(nc + 2) * w.grid);  // partials of the fused coarse CG (parity, CTA, coarse dof)
+    w.coarse_part = co.cpart.p;
+    w.coarse_part_ctas = w.grid;
     const int64_t n3 = 3LL * a->fes->nn;
     co.V.alloc(6 * (size_t)n3), co.W.alloc(6 * (size_t)n3);
     co.gpart.alloc(36 * (size_t)nch * ncol);
@@ -933,7 +939,28 @@ struct ikr_ls_s {
       }
       return us;
     };
+    // fused coarse kinds: as the persistent kinds, with the coarse part (init leaves r.D^-1 r for it)
+    auto time_coarse = [&](int kind, double keep) {
+      apply(kind, keep);
+      constexpr int kTimed = 160;
+      double us = 1e300;
+      w.coarse = 1;
+      for (int rep = 0; rep < 4; ++rep) {
+        ikr::launch_pcg_init(A, w, b64.p, 0.0, kTimed, s);
+        CK(cudaEventRecord(tev[0], s));
+        CK(ikr::launch_pcg_coarse(A, w, co.C, kind - first_coarse_kind(), s));
+        CK(cudaEventRecord(tev[1], s));
+        CK(cudaEventSynchronize(tev[1]));
+        count(3);
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+        if (rep > 0) us = std::min(us, 1e3 * ms / kTimed);
+      }
+      w.coarse = 0;
+      return us;
+    };
     auto time_kind = [&](int kind, double keep) {
+      if (kind >= first_coarse_kind()) return time_coarse(kind, keep);
       return kind >= first_persistent_kind() ? time_persistent(kind, keep) : time_it(kind, keep);
     };
     int best_kind = spmv_req >= 0 ? spmv_req : 0;
@@ -950,11 +977,26 @@ struct ikr_ls_s {
         const double us = time_persistent(first_persistent_kind() + v, kProbeKeep);
         if (us < best) best = us, best_kind = first_persistent_kind() + v;
       }
+      // with a coarse space the fused kinds are preferred whenever one fits: they replace the two-kernel form's
+      // two extra kernels per iteration (its timed iterations above exclude the coarse part)
+      if (coarse_req > 0) {
+        double best_c = 1e300;
+        for (int v = 0; v < ikr::pcg_coarse_variants(); ++v) {
+          if (!ikr::pcg_coarse_eligible(A, w, co.C, v)) continue;
+          const double us = time_coarse(first_coarse_kind() + v, kProbeKeep);
+          if (us < best_c) best_c = us, best_kind = first_coarse_kind() + v;
+        }
+        if (best_c < 1e300) best = best_c;
+      }
       // the two-kernel CG state was advanced by the persistent trials' inits: restart it for the keep trials
       ikr::launch_pcg_init(A, w, b64.p, 0.0, 1 << 30, s);
       count(2);
+    } else if (best_kind >= first_coarse_kind()) {
+      if (coarse_req <= 0) fail(IKR_ERR_ARG, "the fused coarse CG kinds need a coarse space (set_coarse_space)");
+      if (!ikr::pcg_coarse_eligible(A, w, co.C, best_kind - first_coarse_kind()))
+        fail(IKR_ERR_ARG, "the fused coarse CG variant does not fit this system");
     } else if (best_kind >= first_persistent_kind() && coarse_req > 0) {
-      fail(IKR_ERR_ARG, "the coarse correction runs with the two-kernel CG kinds only (0 .. %d)",
+      fail(IKR_ERR_ARG, "the coarse correction runs with the two-kernel CG kinds (0 .. %d) or the fused coarse kinds",
            first_persistent_kind() - 1);
     } else if (best_kind >= first_persistent_kind() && !ikr::pcg_persistent_eligible(A, w, best_kind - first_persistent_kind())) {
       fail(IKR_ERR_ARG, "the persistent CG variant does not fit this system (too many slices per warp)");
@@ -978,7 +1020,37 @@ struct ikr_ls_s {
   }
 
   static int first_persistent_kind() { return 1 + ikr::spmv_staged_variants(); }
-  bool persistent() const { return w.spmv_kind >= first_persistent_kind(); }
+  static int first_coarse_kind() { return first_persistent_kind() + ikr::pcg_persistent_variants(); }
+  bool persistent() const { return w.spmv_kind >= first_persistent_kind() && w.spmv_kind < first_coarse_kind(); }
+  bool coarse_fused() const { return w.spmv_kind >= first_coarse_kind(); }
+
+  // the whole CG with the coarse correction in one cooperative launch: init, fused kernel, one read of the scalars
+  int solve_coarse_fused(ikr_asm a, const double* b, double* x, double rt, int maxit) {
+    cudaStream_t s = a->fes->stream;
+    const ikr::Bsr A = a->bsr();
+    ikr::launch_pcg_init(A, w, b, rt, maxit, s);
+    count(2);
+    if (profile) CK(cudaEventRecord(tev[0], s));
+    CK(ikr::launch_pcg_coarse(A, w, co.C, w.spmv_kind - first_coarse_kind(), s));
+    count(1);
+    if (profile) CK(cudaEventRecord(tev[1], s));
+    CK(cudaMemcpyAsync(scal_h, scal.p, sizeof(double) * ikr::kNScal, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const double done = scal_h[ikr::kDone];
+    last_iters = (int)scal_h[ikr::kIters];
+    last_rel = scal_h[ikr::kBB] > 0 ? std::sqrt(scal_h[ikr::kRR] / scal_h[ikr::kBB]) : 0.0;
+    if (profile) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, tev[0], tev[1]));
+      prof_ms += ms;
+      prof_n += last_iters;
+    }
+    ikr::launch_pcg_result(w, x, 1.0, s);
+    count(1);
+    if (done == 6.0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the fused coarse CG gave up");
+    if (done == 3.0) fail(IKR_ERR_CG_BREAKDOWN, "CG breakdown (p.Kp zero or not finite) after %d iterations", last_iters);
+    return last_iters;
+  }
 
   // the whole CG in one cooperative launch: init, persistent kernel, one read of the scalars
   int solve_persistent(ikr_asm a, const double* b, double* x, double rt, int maxit) {
@@ -1013,6 +1085,7 @@ struct ikr_ls_s {
   int solve_device(ikr_asm a, const double* b, double* x, double rt, int maxit) {
     if (!factorized || asm_ != a) fail(IKR_ERR_INVALID_STATE, "linear solver not factorized for this assembler");
     if (persistent()) return solve_persistent(a, b, x, rt, maxit);
+    if (coarse_fused()) return solve_coarse_fused(a, b, x, rt, maxit);
     cudaStream_t s = a->fes->stream;
     const ikr::Bsr A = a->bsr();
     build_chunk(s);

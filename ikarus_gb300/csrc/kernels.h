@@ -238,6 +238,10 @@ struct PcgWork {
   // when set, the init kernel reads the relative tolerance from this device scalar instead of its argument (a solve
   // captured in a CUDA graph whose tolerance changes from launch to launch)
   const double* rtol_dev = nullptr;
+  // persistent CG with the coarse correction fused in (cg_coarse.cu): 2 (n_c + 2) partials per CTA for up to
+  // coarse_part_ctas CTAs
+  double* coarse_part = nullptr;
+  int coarse_part_ctas = 0;
 };
 void launch_block_jacobi(const Bsr& A, bool fp32, void* minv, bool point_jacobi, cudaStream_t s);
 void launch_pcg_init(const Bsr& A, PcgWork& w, const double* b, double rtol, int max_iter, cudaStream_t s);
@@ -269,6 +273,12 @@ struct Coarse {
   void* e = nullptr;                   // A_c^-1 P^T r, n_c in the CG's type
 };
 void launch_coarse_correction(const Coarse& C, const PcgWork& w, bool init, cudaStream_t s);
+// cg_coarse.cu: the persistent block-Jacobi CG with the coarse correction in the same cooperative launch (after
+// launch_pcg_init with w.coarse = 1); at most kCoarseFusedMaxDofs coarse dofs (64 slabs)
+constexpr int kCoarseFusedMaxDofs = 384;
+int pcg_coarse_variants();
+bool pcg_coarse_eligible(const Bsr& A, PcgWork& w, const Coarse& C, int variant);
+cudaError_t launch_pcg_coarse(const Bsr& A, PcgWork& w, const Coarse& C, int variant, cudaStream_t s);
 void launch_coarse_probe(const Coarse& C, int colour, double* V, cudaStream_t s);
 void launch_coarse_galerkin(const Coarse& C, const double* W, double* part, cudaStream_t s);
 int pcg_persistent_variants();

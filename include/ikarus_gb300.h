@@ -271,13 +271,18 @@ int ikr_linear_solver_profile_read(ikr_ls ls, double* spmv_ms_total, int64_t* sp
  * (default) or launched kernel by kernel otherwise (for profilers that do not follow graph kernels). */
 int ikr_linear_solver_set_launch(ikr_ls ls, int32_t use_graphs, int32_t chunk_len);
 /* CG kernels (no reference counterpart).  spmv_kind 0 = two kernels per iteration with a direct-load SpMV,
- * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..8 = the
- * whole solve in one persistent cooperative kernel (grid barriers for the two reductions of an iteration;
- * only where every warp's rows fit its registers), -1 = autotune; l2_keep_fraction in [0, 1) = share of the
+ * 1..4 = two kernels with a bulk-copy staged SpMV (chunk size / pipeline depth / warps per block), 5..13 = the
+ * whole solve in one persistent cooperative kernel (5..11: grid barriers for the two reductions of an iteration,
+ * 12..13: one reduction per iteration; only where every warp's rows fit its registers), 14..15 = the persistent
+ * kernel with the coarse correction in the same launch (needs ikr_linear_solver_set_coarse_space; at most 64
+ * slabs), -1 = autotune (with a coarse space: a fused kind whenever one fits); l2_keep_fraction in [0, 1) = share of the
  * matrix the staged kernels keep in L2 across iterations, -1 = autotune.  The choice is made at the
  * next factorize from timed CG iterations on the assembled tangent and kept for that assembler.  info
  * returns the kind and keep fraction in use and the SpMV time per launch the tuner measured (0 if fixed). */
 int ikr_linear_solver_set_kernel(ikr_ls ls, int32_t spmv_kind, double l2_keep_fraction);
+/* the CG kind ranges of this build: out4 = {first staged kind, first persistent kind, first fused coarse kind,
+ * number of kinds} (no reference counterpart) */
+int ikr_cg_kind_ranges(int32_t* out4);
 /* no reference counterpart: the kernel of the FP32 displacement-based tangent -- 1: coloured element kernel (8 lanes
  * per element, one read-modify-write launch per colour class), 2: row kernel (NeoHooke on a set without instances: a
  * thread per node row adds its row of every adjacent element's tangent, one launch, no colouring), 3: element blocks

@@ -64,6 +64,44 @@ def test_coarse_correction_gives_the_same_solution_in_fewer_iterations(ikr, prec
     assert np.all(x1[p.fixed == 1] == 0.0)
 
 
+@pytest.mark.parametrize("precision,rtol,tol_pair", [(0, 1e-12, 1e-9), (1, 1e-5, 1e-3)], ids=["fp64", "fp32"])
+def test_fused_coarse_kernel_matches_the_two_kernel_form(ikr, precision, rtol, tol_pair):
+    """The persistent kernel with the coarse correction in the same launch (cg_coarse.cu) applies the same
+    preconditioner as the two-kernel form (coarse.cu): the same solution to the solve tolerance, about the same
+    iteration count, the requested tolerance reached, bit-identical repeats, and the tuner picks it."""
+    p = problems.cantilever(32, 4, 4, jitter=0.1, seed=3)
+    fes, asm, req, b, x_ref = _system(ikr, p, precision)
+    kinds = ikr.LinearSolver.kind_ranges()
+    ls2 = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=rtol)
+    ls2.set_kernel(1, 0.0)  # a two-kernel (staged) form
+    ls2.set_coarse_space(8)
+    ls2.compute(asm)
+    x2 = ls2.solve(asm, b)
+    it2, _ = ls2.last_info()
+    for variant in range(kinds["coarse_fused"], kinds["count"]):
+        lsf = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=rtol)
+        lsf.set_kernel(variant, 0.45)
+        lsf.set_coarse_space(8)
+        lsf.compute(asm)
+        xf = lsf.solve(asm, b)
+        itf, relf = lsf.last_info()
+        scale = np.abs(x_ref).max()
+        assert np.abs(xf - x2).max() <= tol_pair * scale, variant
+        assert relf <= rtol
+        assert abs(itf - it2) <= max(3, 0.1 * it2), (variant, itf, it2)
+        np.testing.assert_array_equal(lsf.solve(asm, b), xf)
+        assert np.all(xf[p.fixed == 1] == 0.0)
+    lst = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=rtol)
+    lst.set_coarse_space(8)
+    lst.compute(asm)
+    assert lst.kernel_info()[0] >= kinds["coarse_fused"]
+    # a fused kind without a coarse space is an argument error
+    lsb = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi, rtol=rtol)
+    lsb.set_kernel(kinds["coarse_fused"], 0.0)
+    with pytest.raises(ikr.IkarusError):
+        lsb.compute(asm)
+
+
 def test_coarse_correction_with_single_slab_and_many_slabs(ikr):
     """One slab (the six global rigid-body modes) and one slab per node layer, where the clamped layer has no free
     dof and its six modes are dropped."""
