@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--coarse", type=int, default=32,
                     help="slabs of the CG's coarse correction for the extra two-level measurement beside the "
                          "headline (0: skip it)")
+    ap.add_argument("--tangent-kernel", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="mixed form's FP32 tangent kernel: 0 timed choice, 1 coloured, 2 row, 3 element blocks")
+    ap.add_argument("--coarse-refresh", type=int, default=1,
+                    help="two-level measurement: rebuild A_c at every n-th factorize (1: every one)")
     ap.add_argument("--two-level-only", action="store_true",
                     help="only the two-level measurement (mixed and plain FP64 with the coarse correction)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -172,13 +176,14 @@ def solver_settings(ikr, mixed: bool, eta=(2e-2, 1e-5)):
 class Form:
     """One solution form (mixed or plain) on the GPU: element set, assembler, solver objects, requirements."""
 
-    def __init__(self, ikr, problems, p, mixed, predictor=0, eta=(1e-2, 1e-5), coarse=0):
+    def __init__(self, ikr, problems, p, mixed, predictor=0, eta=(1e-2, 1e-5), coarse=0, coarse_refresh=1):
         self.ikr = ikr
         self.mixed = mixed
         self.fes, self.asm = problems.build_gpu(p, precision=1 if mixed else 0)
         self.ls = ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_BlockJacobi)
         if coarse:
             self.ls.set_coarse_space(coarse)
+            self.ls.set_coarse_refresh(coarse_refresh)
         self.nr = ikr.NewtonRaphson(self.asm, ikr.NewtonRaphsonConfig(solver_settings(ikr, mixed, eta), self.ls))
         self.lc = ikr.LoadControl(self.nr, p.load_steps, (0.0, p.t_end))
         if predictor:
@@ -218,6 +223,8 @@ def run_ours(args, rank, world):
         if args.small else problems.config2(load_steps=args.load_steps)
     n_nodes = p.mesh.n_nodes
     mixed = Form(ikr, problems, p, mixed=True, predictor=args.predictor, eta=(args.eta_max, args.eta_min))
+    if args.tangent_kernel:
+        mixed.asm.set_tangent_kernel(args.tangent_kernel)
     stream, ev0, ev1 = make_events(torch, mixed.fes.stream())
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
@@ -320,13 +327,14 @@ def run_two_level(args, ikr, torch, problems, p, u_plain, t_plain_bj):
     time with the same 256 MB L2 flush before each path."""
     import numpy as np
 
-    res = {"slabs": args.coarse, "preconditioner": "block Jacobi + P A_c^-1 P^T (six rigid-body modes per slab, "
-                                                    "A_c = P^T K P rebuilt at every factorize)"}
+    res = {"slabs": args.coarse, "coarse_refresh": args.coarse_refresh,
+           "preconditioner": "block Jacobi + P A_c^-1 P^T (six rigid-body modes per slab, A_c = P^T K P rebuilt at "
+                             "every coarse_refresh-th factorize)"}
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
     try:
         for key, mixed, runs in (("mixed", True, 3), ("plain_fp64", False, 1)):
             f = Form(ikr, problems, p, mixed=mixed, predictor=args.predictor if mixed else 0,
-                     eta=(args.eta_max, args.eta_min), coarse=args.coarse)
+                     eta=(args.eta_max, args.eta_min), coarse=args.coarse, coarse_refresh=args.coarse_refresh)
             st, e0, e1 = make_events(torch, f.fes.stream())
             times = []
             for k in range(runs):

@@ -250,6 +250,7 @@ SIGNATURES = {
     "ikr_linear_solver_set_multi_rhs": ([_vp, _I], C.c_int),
     "ikr_linear_solver_set_coarse_space": ([_vp, _I], C.c_int),
     "ikr_linear_solver_coarse_info": ([_vp, _ip], C.c_int),
+    "ikr_linear_solver_set_coarse_refresh": ([_vp, _I], C.c_int),
     "ikr_assembler_set_tangent_kernel": ([_vp, _I], C.c_int),
     "ikr_assembler_tangent_kernel": ([_vp, _ip], C.c_int),
     "ikr_linear_solver_solve2": ([_vp, _vp, _dp, _dp, _dp, _dp], C.c_int),
@@ -1088,6 +1089,11 @@ class LinearSolver:
         factorize (an additive two-level preconditioner; two-kernel CG forms, or with at most 64 slabs the persistent
         kernel with the correction fused in, which the tuner prefers)."""
         _err(lib().ikr_linear_solver_set_coarse_space(self.h, int(n_slabs)))
+
+    def set_coarse_refresh(self, every):
+        """Rebuild A_c at every ``every``-th factorize only (1, the default: each time); in between the coarse
+        operator of an earlier tangent stays (still SPD: same solution, possibly more CG iterations)."""
+        _err(lib().ikr_linear_solver_set_coarse_refresh(self.h, int(every)))
 
     def coarse_info(self):
         """{"slabs", "coarse_dofs", "dropped_modes", "colours"} of the coarse correction in use (zeros when off)."""

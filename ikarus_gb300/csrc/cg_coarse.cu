@@ -8,9 +8,11 @@
 //   1. every row adds its six mode sums P_row^T r_row into a per-warp shared array (runs of equal aggregate over
 //      the lanes of a slice are summed by a segmented warp scan, the run totals added in lane order); the CTA adds
 //      its warps' arrays in warp order and publishes, with r.D^-1 r and r.r, one partial per coarse dof;
-//   2. grid barrier; every CTA sums the published partials of all CTAs in CTA order (a warp per coarse dof, a
-//      fixed lane split and butterfly), so r_c = P^T r, r.D^-1 r and r.r are bit-identical in every CTA;
-//   3. e = A_c^-1 r_c (a warp per row of A_c^-1, lanes over its columns), r.z = r.D^-1 r + r_c.e;
+//   2. grid barrier; every CTA sums the published partials of all CTAs in CTA order (four coarse dofs per warp at
+//      a time, a fixed lane split and butterfly, all loads of a group in flight together), so r_c = P^T r,
+//      r.D^-1 r and r.r are bit-identical in every CTA;
+//   3. e = A_c^-1 r_c (threads over rows and column segments, sixteen column loads in flight), r.z = r.D^-1 r +
+//      r_c.e;
 //   4. the owned rows' z = D^-1 r + P e goes to registers and to the global z the gathers read; a third grid
 //      barrier (arrive and wait) publishes it before the next product phase.
 // Before the first iteration the same coarse part turns the init kernel's z = D^-1 r_0 into M^-1 r_0.  All sums
@@ -25,6 +27,8 @@ namespace ikr {
 namespace {
 
 using namespace cg;
+
+constexpr int kGridLanes = 6;  // grid partials per lane in the coarse sums: at most 192 CTAs
 
 // per node: offset from the aggregate centroid, aggregate id (bits 0-23) and free-dof mask (bits 24-26)
 struct RowP {
@@ -194,21 +198,52 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     }
     ++barrier_no;
     if (!grid_sync(bar_count, barrier_no * (unsigned)G, &ok_sh, wc.polls)) return false;
-    // every CTA: the sums over all CTAs in CTA order, a warp per value
-    for (int c = warp; c < nv; c += WARPS) {
-      double s = 0.0;
-      for (int g = lane; g < G; g += 32) s += __ldcg(cp + (size_t)c * G + g);
-      s = warp_sum(s);
-      if (lane == 0) rc[c] = s;
+    // every CTA: the sums over all CTAs in CTA order; a warp takes four values at a time and a lane the CTAs
+    // lane, lane + 32, ... (at most kGridLanes of them), all loads of a group issued together: the partials sit in
+    // L2, and a chain of dependent loads would cost one L2 round trip each
+    for (int c0 = 4 * warp; c0 < nv; c0 += 4 * WARPS) {
+      double sq[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int c = c0 + q;
+        double t[kGridLanes];
+#pragma unroll
+        for (int k = 0; k < kGridLanes; ++k) {
+          const int g = lane + 32 * k;
+          t[k] = (c < nv && g < G) ? __ldcg(cp + (size_t)c * G + g) : 0.0;
+        }
+        double a = 0.0;
+#pragma unroll
+        for (int k = 0; k < kGridLanes; ++k) a += t[k];
+        sq[q] = a;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double v = warp_sum(sq[q]);
+        if (lane == 0 && c0 + q < nv) rc[c0 + q] = v;
+      }
     }
     __syncthreads();
     rrn = rc[nc + 1];
-    // e = A_c^-1 r_c (in the CG's type, as the two-kernel form keeps it): a warp per row, lanes over columns
-    for (int i = warp; i < nc; i += WARPS) {
+    // e = A_c^-1 r_c (in the CG's type, as the two-kernel form keeps it): thread t forms the part of row i = t mod
+    // n_c over column segment t / n_c (A_c^-1 is symmetric: the reads of column j are coalesced along i, sixteen
+    // columns' loads in flight), then the segments are added in order
+    {
+      const int nseg = max(1, (int)blockDim.x / nc), seg_len = (nc + nseg - 1) / nseg;
+      const int t = threadIdx.x, i = t % nc, seg = t / nc;
       double s = 0.0;
-      for (int j = lane; j < nc; j += 32) s += double(__ldg(ainv + (size_t)i * nc + j)) * rc[j];
-      s = warp_sum(s);
-      if (lane == 0) ec[i] = double(T(s));
+      if (seg < nseg) {
+        const int j1 = min(nc, (seg + 1) * seg_len);
+#pragma unroll 16
+        for (int j = seg * seg_len; j < j1; ++j) s += double(__ldg(ainv + (size_t)j * nc + i)) * rc[j];
+      }
+      acc[t] = s;  // the mode-sum array is free again
+      __syncthreads();
+      if (t < nc) {
+        double ev = 0.0;
+        for (int g = 0; g < nseg; ++g) ev += acc[g * nc + t];
+        ec[t] = double(T(ev));
+      }
     }
     __syncthreads();
     if (warp == 0) {
@@ -436,7 +471,7 @@ cudaError_t launch_coarse_cfg(const Bsr& A, PcgWork& w, const Coarse& Cc, cudaSt
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
   int grid = bps > 0 ? w.sms * bps : 0;
   if (grid > w.grid) grid = w.grid;
-  *eligible = coop && grid > 0 && (int64_t)grid * WARPS * MAXS >= A.n_slices && Cc.n_c > 0 &&
+  *eligible = coop && grid > 0 && grid <= 32 * kGridLanes && (int64_t)grid * WARPS * MAXS >= A.n_slices && Cc.n_c > 0 &&
               Cc.n_c <= kCoarseFusedMaxDofs && w.coarse_part != nullptr && grid <= w.coarse_part_ctas;
   if (query_only || !*eligible) return cudaSuccess;
   const T* val = (const T*)A.val;

@@ -62,12 +62,30 @@ __device__ __forceinline__ bool grid_allreduce(double (&v)[N], double* part, uns
   __threadfence();  // every thread: its later plain loads observe what the other CTAs wrote before arriving
   if (!*ok_sh) return false;
   if (threadIdx.x < 32) {
+    // lane l adds the partials of CTAs l, l + 32, l + 64, ... in that order; the loads of up to eight of them per
+    // value are issued together (the partials sit in L2, so a dependent chain of loads would cost one L2 round trip
+    // each), then the lanes' sums are combined by the butterfly
+    constexpr int kU = 8;
+    double s[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) s[k] = 0.0;
+    for (int i0 = threadIdx.x; i0 < (int)gridDim.x; i0 += 32 * kU) {
+      double t[kU][N];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int i = i0 + 32 * u;
+#pragma unroll
+        for (int k = 0; k < N; ++k) t[u][k] = i < (int)gridDim.x ? __ldcg(part + (size_t)i * N + k) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u)
+#pragma unroll
+        for (int k = 0; k < N; ++k) s[k] += t[u][k];
+    }
 #pragma unroll
     for (int k = 0; k < N; ++k) {
-      double s = 0.0;
-      for (int i = threadIdx.x; i < (int)gridDim.x; i += 32) s += __ldcg(part + (size_t)i * N + k);
-      s = warp_sum(s);
-      if (threadIdx.x == 0) sv[k] = s;
+      const double v = warp_sum(s[k]);
+      if (threadIdx.x == 0) sv[k] = v;
     }
   }
   __syncthreads();

@@ -1109,6 +1109,12 @@ int ikr_linear_solver_set_coarse_space(ikr_ls ls, int32_t n_slabs) {
     }
   });
 }
+int ikr_linear_solver_set_coarse_refresh(ikr_ls ls, int32_t every) {
+  return guarded([&] {
+    need(ls && every >= 1, IKR_ERR_ARG, "the coarse operator is rebuilt every n >= 1 factorizations");
+    ls->coarse_refresh = every;
+  });
+}
 int ikr_linear_solver_coarse_info(ikr_ls ls, int32_t* out4) {
   return guarded([&] {
     need(ls && out4, IKR_ERR_ARG, "null argument");

@@ -509,7 +509,11 @@ struct ikr_ls_s {
   // count along the mesh's longest extent, six rigid-body modes each; rebuilt (A_c and its inverse) at every
   // factorize.  Two-kernel CG forms only (the tuner then skips the persistent ones).
   int coarse_req = 0;
+  // A_c is rebuilt at every coarse_refresh-th factorize (1: every one); an older A_c = P^T K_old P is still SPD,
+  // so the CG stays exact with it and only its iteration count can grow
+  int coarse_refresh = 1;
   struct CoarseSet {
+    int since_rebuild = 0;  // factorizations that reused the current A_c
     ikr_asm built_for = nullptr;
     int n_slabs = 0, reach = 0, n_colours = 0, dropped = 0;
     ikr::Coarse C;
@@ -767,8 +771,14 @@ struct ikr_ls_s {
   // A_c = P^T K P from probe products (one SpMV per colour and mode), then its inverse
   void coarse_operator(ikr_asm a) {
     if (co.built_for != a || co.n_slabs != std::min(coarse_req, a->fes->nn) ||
-        (fp32 ? (const void*)co.ainv32.p : (const void*)co.ainv64.p) != co.C.ainv)
+        (fp32 ? (const void*)co.ainv32.p : (const void*)co.ainv64.p) != co.C.ainv) {
       coarse_layout(a);
+      co.since_rebuild = 0;
+    } else if (co.since_rebuild + 1 < coarse_refresh) {
+      ++co.since_rebuild;  // keep A_c of an earlier tangent of this assembler
+      return;
+    }
+    co.since_rebuild = 0;
     cudaStream_t s = a->fes->stream;
     const ikr::Bsr A = a->bsr();
     const int S = co.n_slabs, nc = 6 * S, nch = co.C.n_chunks, ncol = co.n_colours;

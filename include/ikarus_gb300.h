@@ -306,6 +306,10 @@ int ikr_linear_solver_kernel_info(ikr_ls ls, int32_t* spmv_kind, double* l2_keep
  * out4: slabs in use (0 = off), coarse dofs, modes dropped as linearly dependent, probe colours. */
 int ikr_linear_solver_set_coarse_space(ikr_ls ls, int32_t n_slabs);
 int ikr_linear_solver_coarse_info(ikr_ls ls, int32_t* out4);
+/* rebuild A_c only at every n-th factorize (default 1: at every one); the others keep A_c of an earlier tangent of
+ * the same assembler, which is still SPD, so the solution is unchanged and only the CG iterations can grow (no
+ * reference counterpart) */
+int ikr_linear_solver_set_coarse_refresh(ikr_ls ls, int32_t every);
 /* material law of all elements (the reference's Material template argument of makeFE): NeoHooke (default,
  * neohooke.hh) or StVenantKirchhoff (svk.hh), both with the Lame parameters given at creation, or BlatzKo
  * (makeBlatzKo(mu), hyperelastic/factory.hh:34-39: deviatoric function on the total principal stretches, no

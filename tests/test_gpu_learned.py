@@ -47,13 +47,22 @@ def _run(ikr, p, fes, asm, theta, kind=0, pred=None, record=False):
     lc = ikr.LoadControl(nr, p.load_steps)
     lc.set_predictor(kind, pred, theta, record)
     info = lc.run(req)
+    hist = None
     if kind:
         # per step: |R| unpredicted, |R| previous increment, |R| learned, kept (0 none, 1 previous, 2 learned)
-        print(np.array2string(lc.predictor_history()[:, 1:5], precision=3))
+        hist = lc.predictor_history()[:, 1:5].copy()
+        print(np.array2string(hist, precision=3))
+    _run.history = hist
     return info, req.globalSolution(), lc.predictor_stats()
 
 
-def test_learned_predictor_saves_newton_iterations(ikr):
+def test_learned_predictor_against_its_fallback(ikr):
+    """The trained predictor is judged against the previous-increment predictor it falls back to: on held-out paths
+    every step keeps the candidate with the smaller FP64 residual (the learned one only where it beats the previous
+    increment), every path reaches the FP64 tolerance, and the Newton iterations of the three predictors are
+    reported.  At this training size (30 paths, 300 snapshots) the network does not beat its fallback measurably:
+    the iteration assertion is that the learned predictor, with its gate, is never worse than the fallback by more
+    than one iteration per path, and strictly better than no predictor."""
     p = problems.learned_cantilever(16, 4, 4, load_steps=10)
     fes, asm = problems.build_gpu(p, precision=1)
     rng = np.random.default_rng(11)
@@ -71,6 +80,12 @@ def test_learned_predictor_saves_newton_iterations(ikr):
         info1, u1, _ = _run(ikr, p, fes, asm, theta, kind=1)
         info2, u2, (acc, rej) = _run(ikr, p, fes, asm, theta, kind=2, pred=pred)
         assert info0.success and info1.success and info2.success
+        h = _run.history
+        for r_prev, r_learned, kept in h[:, 1:4]:
+            if kept == 2:
+                assert r_learned <= r_prev  # the learned candidate is kept only where its FP64 residual is smaller
+            elif kept == 1 and np.isfinite(r_learned) and r_learned > 0:
+                assert r_learned >= r_prev
         # all reach the FP64 tolerance; the converged paths agree
         assert np.abs(u2 - u0).max() <= 1e-5 * np.abs(u0).max()
         plain_its += info0.totalIterations
@@ -80,6 +95,7 @@ def test_learned_predictor_saves_newton_iterations(ikr):
     print(f"Newton iterations over 5 held-out paths: none {plain_its}, previous increment {prev_its}, "
           f"learned {learned_its}")
     assert learned_its < plain_its
+    assert learned_its <= prev_its + 5
 
 
 def test_second_order_extrapolation_predictor_reaches_the_same_path(ikr):
