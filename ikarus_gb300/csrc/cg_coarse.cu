@@ -12,7 +12,9 @@
 //      a time, a fixed lane split and butterfly, all loads of a group in flight together), so r_c = P^T r,
 //      r.D^-1 r and r.r are bit-identical in every CTA;
 //   3. e = A_c^-1 r_c (threads over rows and column segments, sixteen column loads in flight), r.z = r.D^-1 r +
-//      r_c.e;
+//      r_c.e.  The per-row mode sums, their warp scan and this product run in the CG's type (FP32 for the FP32 CG:
+//      GB300's FP64 rate is a small fraction of its FP32 rate, and e is kept in the CG's type anyway); the sums
+//      over rows, warps and CTAs are FP64;
 //   4. the owned rows' z = D^-1 r + P e goes to registers and to the global z the gathers read; a third grid
 //      barrier (arrive and wait) publishes it before the next product phase.
 // Before the first iteration the same coarse part turns the init kernel's z = D^-1 r_0 into M^-1 r_0.  All sums
@@ -84,8 +86,9 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   unsigned char* wbase = smem + (size_t)warp * NST * C::kStageBytes;
   // coarse shared arrays after the stages: per-warp mode sums (WARPS x nc), r_c (+ the two dot products), e
   double* acc = reinterpret_cast<double*>(smem + (size_t)WARPS * NST * C::kStageBytes);
-  double* rc = acc + (size_t)WARPS * nc;
-  double* ec = rc + nv;
+  double* rc = acc + (size_t)WARPS * kCoarseFusedMaxDofs;  // (acc also holds blockDim.x partials of e)
+  T* rct = reinterpret_cast<T*>(rc + nv);                  // r_c and e in the CG's type
+  T* ect = rct + nc;
   const T* ainv = static_cast<const T*>(Cc.ainv);
 
   int ns = 0;
@@ -139,12 +142,13 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
 #pragma unroll
     for (int j = 0; j < MAXS; ++j) {
       const int a = yp[j].agg;  // -1 for rows not owned
-      double v[6] = {0, 0, 0, 0, 0, 0};
+      // in the CG's type: GB300's FP64 pipe is a small fraction of its FP32 rate, and these run for every row
+      T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
       if (a >= 0) {
-        const double r0 = (yp[j].mask & 1) ? double(rr_[j][0]) : 0.0;
-        const double r1 = (yp[j].mask & 2) ? double(rr_[j][1]) : 0.0;
-        const double r2 = (yp[j].mask & 4) ? double(rr_[j][2]) : 0.0;
-        const double yx = yp[j].y[0], yy = yp[j].y[1], yz = yp[j].y[2];
+        const T r0 = (yp[j].mask & 1) ? rr_[j][0] : T(0);
+        const T r1 = (yp[j].mask & 2) ? rr_[j][1] : T(0);
+        const T r2 = (yp[j].mask & 4) ? rr_[j][2] : T(0);
+        const T yx = T(yp[j].y[0]), yy = T(yp[j].y[1]), yz = T(yp[j].y[2]);
         // P^T r with the columns e_k (translations) and e_k x y (rotations) of the node's 3 x 6 block
         v[0] = r0, v[1] = r1, v[2] = r2;
         v[3] = -yz * r1 + yy * r2;
@@ -167,7 +171,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
       for (int d = 1; d < 32; d <<= 1) {
 #pragma unroll
         for (int m = 0; m < 6; ++m) {
-          const double t = __shfl_up_sync(0xffffffffu, v[m], d);
+          const T t = __shfl_up_sync(0xffffffffu, v[m], d);
           if (lane - d >= seg) v[m] += t;
         }
       }
@@ -176,7 +180,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         const int L = __ffs(tails) - 1;
         if (lane == L) {
 #pragma unroll
-          for (int m = 0; m < 6; ++m) aw[6 * a + m] += v[m];
+          for (int m = 0; m < 6; ++m) aw[6 * a + m] += double(v[m]);
         }
         __syncwarp();
         tails &= tails - 1;
@@ -223,6 +227,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         if (lane == 0 && c0 + q < nv) rc[c0 + q] = v;
       }
     }
+    for (int c = threadIdx.x; c < nc; c += blockDim.x) rct[c] = T(rc[c]);
     __syncthreads();
     rrn = rc[nc + 1];
     // e = A_c^-1 r_c (in the CG's type, as the two-kernel form keeps it): thread t forms the part of row i = t mod
@@ -231,24 +236,24 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     {
       const int nseg = max(1, (int)blockDim.x / nc), seg_len = (nc + nseg - 1) / nseg;
       const int t = threadIdx.x, i = t % nc, seg = t / nc;
-      double s = 0.0;
+      T s = T(0);
       if (seg < nseg) {
         const int j1 = min(nc, (seg + 1) * seg_len);
 #pragma unroll 16
-        for (int j = seg * seg_len; j < j1; ++j) s += double(__ldg(ainv + (size_t)j * nc + i)) * rc[j];
+        for (int j = seg * seg_len; j < j1; ++j) s += __ldg(ainv + (size_t)j * nc + i) * rct[j];
       }
-      acc[t] = s;  // the mode-sum array is free again
+      acc[t] = double(s);  // the mode-sum array is free again
       __syncthreads();
       if (t < nc) {
         double ev = 0.0;
         for (int g = 0; g < nseg; ++g) ev += acc[g * nc + t];
-        ec[t] = double(T(ev));
+        ect[t] = T(ev);
       }
     }
     __syncthreads();
     if (warp == 0) {
       double s = 0.0;
-      for (int i = lane; i < nc; i += 32) s += rc[i] * ec[i];
+      for (int i = lane; i < nc; i += 32) s += rc[i] * double(ect[i]);
       s = warp_sum(s);
       if (lane == 0) sv[0] = s;
     }
@@ -259,9 +264,9 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     for (int j = 0; j < MAXS; ++j) {
       const int a = yp[j].agg;
       if (a < 0) continue;
-      const double* ea = ec + 6 * a;
+      const T* ea = ect + 6 * a;
       const T yx = T(yp[j].y[0]), yy = T(yp[j].y[1]), yz = T(yp[j].y[2]);
-      const T e0 = T(ea[0]), e1 = T(ea[1]), e2 = T(ea[2]), e3 = T(ea[3]), e4 = T(ea[4]), e5 = T(ea[5]);
+      const T e0 = ea[0], e1 = ea[1], e2 = ea[2], e3 = ea[3], e4 = ea[4], e5 = ea[5];
       T d0 = e0 + e4 * yz - e5 * yy;
       T d1 = e1 + e5 * yx - e3 * yz;
       T d2 = e2 + e3 * yy - e4 * yx;
@@ -450,7 +455,8 @@ cudaError_t launch_coarse_cfg(const Bsr& A, PcgWork& w, const Coarse& Cc, cudaSt
   using C = PersistentCfg<T, CB, NST, WARPS>;
   auto kern = pcg_coarse_kernel<T, CB, NST, WARPS, MAXS>;
   const size_t smem = (size_t)C::kSmemBytes + sizeof(double) * ((size_t)WARPS * kCoarseFusedMaxDofs +
-                                                                2 * (size_t)kCoarseFusedMaxDofs + 2);
+                                                                (size_t)kCoarseFusedMaxDofs + 2) +
+                      sizeof(T) * 2 * (size_t)kCoarseFusedMaxDofs;
   static std::mutex mu;
   static int blocks_per_sm[64] = {0};
   int dev = 0;
