@@ -43,11 +43,12 @@ __device__ __forceinline__ RowP row_p(const float4* __restrict__ y4, int node) {
   return {{v.x, v.y, v.z}, bits & 0xFFFFFF, (bits >> 24) & 7};
 }
 
-// grid barrier without data: arrive, wait (bounded) until `target` arrivals; false when the wait gave up
+// grid barrier without data: arrive, wait (bounded) until `target` arrivals; false when the wait gave up.  Every
+// thread fences its own global writes before the CTA arrives (they are written by many threads of the CTA).
 __device__ __forceinline__ bool grid_sync(unsigned int* count, unsigned int target, bool* ok_sh, int polls) {
+  __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) {
-    __threadfence();
     atomicAdd(count, 1u);
     bool ok = false;
     for (int i = 0; i < polls; ++i) {
@@ -227,6 +228,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         if (lane == 0 && c0 + q < nv) rc[c0 + q] = v;
       }
     }
+    __syncthreads();
     for (int c = threadIdx.x; c < nc; c += blockDim.x) rct[c] = T(rc[c]);
     __syncthreads();
     rrn = rc[nc + 1];
