@@ -7,14 +7,14 @@
 // the update phase, instead of the two extra kernels per iteration of the two-kernel form:
 //   1. every row adds its six mode sums P_row^T r_row into a per-warp shared array (runs of equal aggregate over
 //      the lanes of a slice are summed by a segmented warp scan, the run totals added in lane order); the CTA adds
-//      its warps' arrays in warp order and publishes, with r.D^-1 r and r.r, one partial per coarse dof;
+//      its warps' arrays in warp order and publishes, with r.D^-1 r and r.r (FP64), one partial per coarse dof;
 //   2. grid barrier; every CTA sums the published partials of all CTAs in CTA order (four coarse dofs per warp at
 //      a time, a fixed lane split and butterfly, all loads of a group in flight together), so r_c = P^T r,
 //      r.D^-1 r and r.r are bit-identical in every CTA;
 //   3. e = A_c^-1 r_c (threads over rows and column segments, sixteen column loads in flight), r.z = r.D^-1 r +
-//      r_c.e.  The per-row mode sums, their warp scan and this product run in the CG's type (FP32 for the FP32 CG:
-//      GB300's FP64 rate is a small fraction of its FP32 rate, and e is kept in the CG's type anyway); the sums
-//      over rows, warps and CTAs are FP64;
+//      r_c.e.  The mode sums (rows, warps, CTAs), their warp scan and this product run in the CG's type (FP32 for
+//      the FP32 CG: GB300's FP64 pipe is a small fraction of its FP32 rate, and e is kept in the CG's type
+//      anyway); r.D^-1 r, r.r and r_c.e are FP64;
 //   4. the owned rows' z = D^-1 r + P e goes to registers and to the global z the gathers read; a third grid
 //      barrier (arrive and wait) publishes it before the next product phase.
 // Before the first iteration the same coarse part turns the init kernel's z = D^-1 r_0 into M^-1 r_0.  All sums
@@ -82,14 +82,16 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   const int nw = G * WARPS;
   const int gw = blockIdx.x * WARPS + warp;
   const int n_slices = A.n_slices;
-  const int nc = Cc.n_c, nv = nc + 2;  // coarse dofs, then r.D^-1 r and r.r
+  const int nc = Cc.n_c, nv = nc + 2;  // r.D^-1 r and r.r, then the coarse dofs
   unsigned int* bar_count = &tickets(scal)[3];
   unsigned char* wbase = smem + (size_t)warp * NST * C::kStageBytes;
   // coarse shared arrays after the stages: per-warp mode sums (WARPS x nc), r_c (+ the two dot products), e
-  double* acc = reinterpret_cast<double*>(smem + (size_t)WARPS * NST * C::kStageBytes);
-  double* rc = acc + (size_t)WARPS * kCoarseFusedMaxDofs;  // (acc also holds blockDim.x partials of e)
-  T* rct = reinterpret_cast<T*>(rc + nv);                  // r_c and e in the CG's type
-  T* ect = rct + nc;
+  // coarse shared arrays after the stages: per-warp mode sums (WARPS x n_c, also the blockDim.x partials of e),
+  // the two FP64 dot products, r_c and e in the CG's type
+  T* accw = reinterpret_cast<T*>(smem + (size_t)WARPS * NST * C::kStageBytes);
+  double* rdot = reinterpret_cast<double*>(accw + (size_t)WARPS * kCoarseFusedMaxDofs);
+  T* rct = reinterpret_cast<T*>(rdot + 2);
+  T* ect = rct + kCoarseFusedMaxDofs;
   const T* ainv = static_cast<const T*>(Cc.ainv);
 
   int ns = 0;
@@ -136,10 +138,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   // The coarse part of z = M^-1 r for the owned rows (zr holds D^-1 r on entry, z = M^-1 r on return, also stored
   // to the global z): returns false when a grid wait gave up.  Sets rzs (r.z), rrn (r.r).
   auto coarse_part = [&](double& rzs, double& rrn) -> bool {
-    for (int i = threadIdx.x; i < WARPS * nc; i += blockDim.x) acc[i] = 0.0;
+    for (int i = threadIdx.x; i < WARPS * nc; i += blockDim.x) accw[i] = T(0);
     __syncthreads();
     double rzf = 0.0, rrl = 0.0;
-    double* aw = acc + (size_t)warp * nc;
+    T* aw = accw + (size_t)warp * nc;
 #pragma unroll
     for (int j = 0; j < MAXS; ++j) {
       const int a = yp[j].agg;  // -1 for rows not owned
@@ -181,86 +183,105 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         const int L = __ffs(tails) - 1;
         if (lane == L) {
 #pragma unroll
-          for (int m = 0; m < 6; ++m) aw[6 * a + m] += double(v[m]);
+          for (int m = 0; m < 6; ++m) aw[6 * a + m] += v[m];
         }
         __syncwarp();
         tails &= tails - 1;
       }
     }
-    // CTA partials: r.D^-1 r, r.r (thread 0) and the mode sums (warps added in order), coarse-dof-major
+    // CTA partials: r.D^-1 r and r.r in FP64 (thread 0), the mode sums (warps added in order) in the CG's type,
+    // coarse-dof-major: per parity 2 G doubles, then n_c G values
     double red[2] = {rzf, rrl};
-    cta_reduce<2>(red, sw);  // ends with warp 0 holding the sums; the __syncthreads inside orders acc
+    cta_reduce<2>(red, sw);  // ends with warp 0 holding the sums; the __syncthreads inside orders accw
     __syncthreads();
-    double* cp = cpart + (size_t)(loop & 1) * nv * G;
+    double* cpd = cpart + (size_t)(loop & 1) * nv * G;
+    T* cpm = reinterpret_cast<T*>(cpd + 2 * (size_t)G);
     for (int c = threadIdx.x; c < nc; c += blockDim.x) {
-      double s = 0.0;
-      for (int w = 0; w < WARPS; ++w) s += acc[(size_t)w * nc + c];
-      cp[(size_t)c * G + blockIdx.x] = s;
+      T sum = T(0);
+      for (int w = 0; w < WARPS; ++w) sum += accw[(size_t)w * nc + c];
+      cpm[(size_t)c * G + blockIdx.x] = sum;
     }
     if (threadIdx.x == 0) {
-      cp[(size_t)nc * G + blockIdx.x] = red[0];
-      cp[(size_t)(nc + 1) * G + blockIdx.x] = red[1];
+      cpd[blockIdx.x] = red[0];
+      cpd[G + blockIdx.x] = red[1];
     }
     ++barrier_no;
     if (!grid_sync(bar_count, barrier_no * (unsigned)G, &ok_sh, wc.polls)) return false;
     // every CTA: the sums over all CTAs in CTA order; a warp takes four values at a time and a lane the CTAs
     // lane, lane + 32, ... (at most kGridLanes of them), all loads of a group issued together: the partials sit in
-    // L2, and a chain of dependent loads would cost one L2 round trip each
+    // L2, and a chain of dependent loads would cost one L2 round trip each.  Value c < 2: the FP64 dot products;
+    // the others: the mode sums in the CG's type
     for (int c0 = 4 * warp; c0 < nv; c0 += 4 * WARPS) {
       double sq[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int c = c0 + q;
-        double t[kGridLanes];
+        if (c < 2) {
+          double t[kGridLanes];
 #pragma unroll
-        for (int k = 0; k < kGridLanes; ++k) {
-          const int g = lane + 32 * k;
-          t[k] = (c < nv && g < G) ? __ldcg(cp + (size_t)c * G + g) : 0.0;
+          for (int k = 0; k < kGridLanes; ++k) {
+            const int g = lane + 32 * k;
+            t[k] = g < G ? __ldcg(cpd + (size_t)c * G + g) : 0.0;
+          }
+          double a = 0.0;
+#pragma unroll
+          for (int k = 0; k < kGridLanes; ++k) a += t[k];
+          sq[q] = a;
+        } else {
+          T t[kGridLanes];
+#pragma unroll
+          for (int k = 0; k < kGridLanes; ++k) {
+            const int g = lane + 32 * k;
+            t[k] = (c < nv && g < G) ? __ldcg(cpm + (size_t)(c - 2) * G + g) : T(0);
+          }
+          T a = T(0);
+#pragma unroll
+          for (int k = 0; k < kGridLanes; ++k) a += t[k];
+          sq[q] = double(warp_sum(a));
         }
-        double a = 0.0;
-#pragma unroll
-        for (int k = 0; k < kGridLanes; ++k) a += t[k];
-        sq[q] = a;
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const double v = warp_sum(sq[q]);
-        if (lane == 0 && c0 + q < nv) rc[c0 + q] = v;
+        const int c = c0 + q;
+        if (c < 2) {
+          const double v = warp_sum(sq[q]);
+          if (lane == 0) rdot[c] = v;
+        } else if (lane == 0 && c < nv) {
+          rct[c - 2] = T(sq[q]);
+        }
       }
     }
     __syncthreads();
-    for (int c = threadIdx.x; c < nc; c += blockDim.x) rct[c] = T(rc[c]);
-    __syncthreads();
-    rrn = rc[nc + 1];
+    rrn = rdot[1];
     // e = A_c^-1 r_c (in the CG's type, as the two-kernel form keeps it): thread t forms the part of row i = t mod
     // n_c over column segment t / n_c (A_c^-1 is symmetric: the reads of column j are coalesced along i, sixteen
     // columns' loads in flight), then the segments are added in order
     {
       const int nseg = max(1, (int)blockDim.x / nc), seg_len = (nc + nseg - 1) / nseg;
       const int t = threadIdx.x, i = t % nc, seg = t / nc;
-      T s = T(0);
+      T sum = T(0);
       if (seg < nseg) {
         const int j1 = min(nc, (seg + 1) * seg_len);
 #pragma unroll 16
-        for (int j = seg * seg_len; j < j1; ++j) s += __ldg(ainv + (size_t)j * nc + i) * rct[j];
+        for (int j = seg * seg_len; j < j1; ++j) sum += __ldg(ainv + (size_t)j * nc + i) * rct[j];
       }
-      acc[t] = double(s);  // the mode-sum array is free again
+      accw[t] = sum;  // the mode-sum array is free again
       __syncthreads();
       if (t < nc) {
-        double ev = 0.0;
-        for (int g = 0; g < nseg; ++g) ev += acc[g * nc + t];
-        ect[t] = T(ev);
+        T ev = T(0);
+        for (int g = 0; g < nseg; ++g) ev += accw[g * nc + t];
+        ect[t] = ev;
       }
     }
     __syncthreads();
     if (warp == 0) {
-      double s = 0.0;
-      for (int i = lane; i < nc; i += 32) s += rc[i] * double(ect[i]);
-      s = warp_sum(s);
-      if (lane == 0) sv[0] = s;
+      double sd = 0.0;
+      for (int i = lane; i < nc; i += 32) sd += double(rct[i]) * double(ect[i]);
+      sd = warp_sum(sd);
+      if (lane == 0) sv[0] = sd;
     }
     __syncthreads();
-    rzs = rc[nc] + sv[0];
+    rzs = rdot[0] + sv[0];
     // z = D^-1 r + P e on the owned rows
 #pragma unroll
     for (int j = 0; j < MAXS; ++j) {
@@ -456,9 +477,7 @@ cudaError_t launch_coarse_cfg(const Bsr& A, PcgWork& w, const Coarse& Cc, cudaSt
                               bool* eligible) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
   auto kern = pcg_coarse_kernel<T, CB, NST, WARPS, MAXS>;
-  const size_t smem = (size_t)C::kSmemBytes + sizeof(double) * ((size_t)WARPS * kCoarseFusedMaxDofs +
-                                                                (size_t)kCoarseFusedMaxDofs + 2) +
-                      sizeof(T) * 2 * (size_t)kCoarseFusedMaxDofs;
+  const size_t smem = (size_t)C::kSmemBytes + sizeof(T) * (size_t)(WARPS + 2) * kCoarseFusedMaxDofs + 2 * sizeof(double);
   static std::mutex mu;
   static int blocks_per_sm[64] = {0};
   int dev = 0;

@@ -1319,7 +1319,7 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   nr->inst_cg_iters.alloc(ni);
   nr->inst_cg_res.alloc(ni);
   std::vector<double> rn(ni), r0(ni), rprev(ni), thr(ni), eta(ni);
-  std::vector<uint8_t> act(ni);
+  std::vector<uint8_t> act(ni), careful(ni, 0);
   std::vector<int32_t> cgit(ni);
   nr->inst_iters.assign(ni, 0);
   nr->inst_conv.assign(ni, 0);
@@ -1355,7 +1355,7 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
         e = std::max(e, 0.5 * thr[i] / std::max(rn[i], 1e-300));
         e = std::min(std::max(e, st.linear_rtol_min), st.linear_rtol);
       }
-      eta[i] = e;
+      eta[i] = careful[i] ? std::min(e, st.linear_rtol_min) : e;
     }
     nr->inst_rtol.upload(eta.data(), ni, s);
     nr->inst_active.upload(act.data(), ni, s);
@@ -1402,6 +1402,28 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
       r->version++;
       assemble_vector(a, r, IKR_DBC_FULL);
       collect_failures();
+    }
+    // an instance that still inverts after the halvings goes back, once per solve, to the state before this
+    // correction and takes its next corrections with the tightest linear tolerance (an inexact direction, not the
+    // load step, is the usual cause in the FP32 form); inverting again takes it out
+    if (st.max_backtracks > 0) {
+      bool any_retry = false;
+      for (int i = 0; i < ni; ++i)
+        if (nr->inst_failed[i] && !failed_before[i] && act[i] && !careful[i]) {
+          nr->inst_failed[i] = 0;
+          careful[i] = 1;
+          step[i] = 0.0;
+          any_retry = true;
+          ++nr->backtracks;
+        }
+      if (any_retry) {
+        nr->inst_step.upload(step.data(), ni, s);
+        ikr::launch_instance_step(r->u.p, nr->u_old.p, nr->corr.p, ni, f->inst_off.p, nr->inst_step.p, s);
+        count(1);
+        r->version++;
+        assemble_vector(a, r, IKR_DBC_FULL);
+        collect_failures();
+      }
     }
     norms();
     for (int i = 0; i < ni; ++i) {

@@ -416,7 +416,9 @@ typedef struct ikr_nr_settings {
   int32_t refinements; /* FP64 iterative-refinement sweeps around an FP32 solve (0 = none) */
   int32_t max_backtracks; /* a correction that inverts an element (det C <= 0; the reference aborts) is halved up
                              to this many times before the error is returned (0 = reference behaviour); batched
-                             solves halve the correction of the affected instances only */
+                             solves halve the correction of the affected instances only, and an instance that still
+                             inverts goes back once per solve to the state before that correction and takes its
+                             next corrections with linear_rtol_min (inverting again takes it out) */
   int32_t step_graphs;    /* 1 (default): every Newton iteration after the first of a solver's life -- tangent
                              assembly, preconditioner, the persistent CG, update, residual assembly and norms -- runs
                              as one CUDA graph launch with one host synchronisation, where the configuration allows
