@@ -59,7 +59,7 @@ def parse():
                          "headline (0: skip it)")
     ap.add_argument("--tangent-kernel", type=int, default=0, choices=[0, 1, 2, 3],
                     help="mixed form's FP32 tangent kernel: 0 timed choice, 1 coloured, 2 row, 3 element blocks")
-    ap.add_argument("--coarse-refresh", type=int, default=1,
+    ap.add_argument("--coarse-refresh", type=int, default=4,
                     help="two-level measurement: rebuild A_c at every n-th factorize (1: every one)")
     ap.add_argument("--two-level-only", action="store_true",
                     help="only the two-level measurement (mixed and plain FP64 with the coarse correction)")
@@ -714,8 +714,10 @@ def run_batched(args):
     out["mixed_vs_plain_max_rel_diff"] = float(diffs.max()) if len(diffs) else None
     # several equilibria exist for the beams loaded far beyond their length: a converged instance may sit on
     # another branch than the plain form's (reported, not averaged away)
-    out["instances_on_another_branch"] = [int(both[k]) for k in np.nonzero(diffs > 1e-6)[0]]
-    out["mixed_vs_plain_max_rel_diff_same_branch"] = float(diffs[diffs <= 1e-6].max()) if (diffs <= 1e-6).any() \
+    # (both stop at ||R|| <= 1e-8 ||R0||, which leaves displacement differences up to ~cond(K) 1e-8; a difference above
+    # 1e-3 of the displacement is another equilibrium)
+    out["instances_on_another_branch"] = [int(both[k]) for k in np.nonzero(diffs > 1e-3)[0]]
+    out["mixed_vs_plain_max_rel_diff_same_branch"] = float(diffs[diffs <= 1e-3].max()) if (diffs <= 1e-3).any() \
         else None
     out["value"] = out["mixed"]["s"]
     out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 3)

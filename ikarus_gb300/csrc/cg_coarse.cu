@@ -74,8 +74,9 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   using C = PersistentCfg<T, CB, NST, WARPS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[WARPS][NST];
-  __shared__ double sw[WARPS * 2];
   __shared__ double sv[2];
+  __shared__ double sdiv[1];
+  __shared__ double sfull[2 * WARPS * 32];
   __shared__ bool ok_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G = gridDim.x;
@@ -192,7 +193,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     // CTA partials: r.D^-1 r and r.r in FP64 (thread 0), the mode sums (warps added in order) in the CG's type,
     // coarse-dof-major: per parity 2 G doubles, then n_c G values
     double red[2] = {rzf, rrl};
-    cta_reduce<2>(red, sw);  // ends with warp 0 holding the sums; the __syncthreads inside orders accw
+    cta_reduce_smem<2>(red, sfull);  // warp 0 holds the sums; the __syncthreads inside orders accw
     __syncthreads();
     double* cpd = cpart + (size_t)(loop & 1) * nv * G;
     T* cpm = reinterpret_cast<T*>(cpd + 2 * (size_t)G);
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     failed = __syncthreads_or(failed);
     if (failed) break;
     double pqa[1] = {pq};
-    cta_reduce<1>(pqa, sw);
+    cta_reduce_smem<1>(pqa, sfull);
     ++barrier_no;
     if (!grid_allreduce<1>(pqa, part_a + (loop & 1) * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh, wc)) {
       failed = true;
@@ -415,7 +416,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
       done = 3.0;
       break;
     }
-    const T alpha = T(rz / pqa[0]);
+    double quo[1];
+    const double rza[1] = {rz};
+    cta_quotients<1>(rza, pqa, quo, sdiv);
+    const T alpha = T(quo[0]);
     // ---- update phase on the owned rows: x, r, z = D^-1 r
 #pragma unroll
     for (int j = 0; j < MAXS; ++j) {
@@ -438,7 +442,12 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
       failed = true;
       break;
     }
-    beta = rzs / rz;
+    {
+      const double na[1] = {rzs}, da[1] = {rz};
+      double ba[1];
+      cta_quotients<1>(na, da, ba, sdiv);
+      beta = ba[0];
+    }
     rz = rzs;
     ++it;
     if (rrs <= tol2) done = 1.0;

@@ -27,6 +27,25 @@ __device__ __forceinline__ void cta_reduce(double (&v)[N], double* sw) {
   }
 }
 
+// CTA sums of N values with the FP64 additions done by one warp: every thread stores its values (sfull holds
+// N x blockDim.x doubles), lane l of warp 0 adds those of threads l, l + 32, ... in order, then a butterfly; valid
+// in warp 0.  A butterfly in every warp would cost each warp five FP64 additions per value, which on GB300's narrow
+// FP64 pipe are several times this.
+template <int N>
+__device__ __forceinline__ void cta_reduce_smem(double (&v)[N], double* sfull) {
+#pragma unroll
+  for (int k = 0; k < N; ++k) sfull[k * blockDim.x + threadIdx.x] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double s = 0.0;
+      for (int i = threadIdx.x; i < (int)blockDim.x; i += 32) s += sfull[k * blockDim.x + i];
+      v[k] = warp_sum(s);
+    }
+  }
+}
+
 // Grid-wide sums of N values whose CTA sums are in thread 0: thread 0 publishes them at part[cta * N + k],
 // arrives on the barrier counter and waits (bounded) until `target` arrivals; then warp 0 sums all CTAs'
 // partials with a fixed lane assignment and butterfly order (identical in every CTA) and every thread gets
@@ -92,6 +111,22 @@ __device__ __forceinline__ bool grid_allreduce(double (&v)[N], double* part, uns
 #pragma unroll
   for (int k = 0; k < N; ++k) v[k] = sv[k];
   return true;
+}
+
+// Quotients num[k] / den[k] formed by thread 0 and read by every thread of the CTA (the same IEEE values): an FP64
+// division is a multi-instruction sequence on GB300's narrow FP64 pipe, and every thread forming it costs microseconds
+// per CG iteration.  A zero or non-finite denominator gives 0.  sq holds N doubles of shared memory; the caller's
+// next CTA barrier orders its reuse.
+template <int N>
+__device__ __forceinline__ void cta_quotients(const double (&num)[N], const double (&den)[N], double (&out)[N],
+                                              double* sq) {
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) sq[k] = (den[k] != 0.0 && isfinite(den[k])) ? num[k] / den[k] : 0.0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; ++k) out[k] = sq[k];
 }
 
 template <typename T, int CB, int NST, int WARPS>

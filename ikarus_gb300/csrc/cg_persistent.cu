@@ -47,8 +47,9 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   using C = PersistentCfg<T, CB, NST, WARPS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[WARPS][NST];
-  __shared__ double sw[WARPS * 2 * NR];
   __shared__ double sv[2 * NR];
+  __shared__ double sdiv[NR];
+  __shared__ double sfull[2 * NR * WARPS * 32];
   __shared__ bool ok_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int G = gridDim.x;
@@ -240,12 +241,14 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     const int par = loop & 1;
     failed = __syncthreads_or(failed);
     if (failed) break;
-    cta_reduce<NR>(pq, sw);
+    cta_reduce_smem<NR>(pq, sfull);
     ++barrier_no;
     if (!grid_allreduce<NR>(pq, part_a + par * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh, wc)) {
       failed = true;
       break;
     }
+    double quo[NR];
+    cta_quotients<NR>(rz, pq, quo, sdiv);
     T alpha[NR];
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
@@ -256,7 +259,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
         act[q] = false;
         continue;
       }
-      alpha[q] = T(rz[q] / pq[q]);
+      alpha[q] = T(quo[q]);
     }
     // ---- update phase on the owned rows
     double red2[2 * NR];
@@ -305,20 +308,24 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       red2[2 * q] = rzn;
       red2[2 * q + 1] = rrn;
     }
-    cta_reduce<2 * NR>(red2, sw);
+    cta_reduce_smem<2 * NR>(red2, sfull);
     ++barrier_no;
     if (!grid_allreduce<2 * NR>(red2, part_b + par * 2 * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh,
                                 wc)) {
       failed = true;
       break;
     }
+    double rzn_all[NR], bq[NR];
+#pragma unroll
+    for (int q = 0; q < NR; ++q) rzn_all[q] = red2[2 * q];
+    cta_quotients<NR>(rzn_all, rz, bq, sdiv);
     all_done = true;
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
       if (act[q]) {
         const double rzs = red2[2 * q];
         rrs[q] = red2[2 * q + 1];
-        beta[q] = rzs / rz[q];
+        beta[q] = bq[q];
         rz[q] = rzs;
         ++it[q];
         if (rrs[q] <= tol2[q]) done[q] = 1.0;
