@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   auto coarse_part = [&](double& rzs, double& rrn) -> bool {
     for (int i = threadIdx.x; i < WARPS * nc; i += blockDim.x) accw[i] = T(0);
     __syncthreads();
-    double rzf = 0.0, rrl = 0.0;
+    T lrz = T(0), lrr = T(0);  // a lane's r.D^-1 r and r.r in the CG's type, converted once
     T* aw = accw + (size_t)warp * nc;
 #pragma unroll
     for (int j = 0; j < MAXS; ++j) {
@@ -164,8 +164,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
           trz += rr_[j][b] * zr[j][b];
           trr += rr_[j][b] * rr_[j][b];
         }
-        rzf += double(trz);
-        rrl += double(trr);
+        lrz += trz;
+        lrr += trr;
       }
       // segmented inclusive scan over runs of equal aggregate (lane order)
       const int ap = __shfl_up_sync(0xffffffffu, a, 1), an = __shfl_down_sync(0xffffffffu, a, 1);
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     }
     // CTA partials: r.D^-1 r and r.r in FP64 (thread 0), the mode sums (warps added in order) in the CG's type,
     // coarse-dof-major: per parity 2 G doubles, then n_c G values
-    double red[2] = {rzf, rrl};
+    double red[2] = {double(lrz), double(lrr)};
     cta_reduce_smem<2>(red, sfull);  // warp 0 holds the sums; the __syncthreads inside orders accw
     __syncthreads();
     double* cpd = cpart + (size_t)(loop & 1) * nv * G;
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
     const T tb = T(beta);
     const T* pold = (it & 1) ? p0 : p1;
     T* pnew = (it & 1) ? p1 : p0;
-    double pq = 0.0;
+    T pql = T(0);  // a lane's p.q in the CG's type, converted once
     // ---- product phase: q = K p_new over the owned slices
 #pragma unroll
     for (int j = 0; j < MAXS; ++j) {
@@ -398,14 +398,14 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
         qr[j][0] = acc3[0], qr[j][1] = acc3[1], qr[j][2] = acc3[2];
         if (row < A.n_rows) {
           store3(pnew, row, n0, n1, n2);
-          pq += double(n0 * acc3[0] + n1 * acc3[1] + n2 * acc3[2]);
+          pql += n0 * acc3[0] + n1 * acc3[1] + n2 * acc3[2];
         }
       }
     }
     // ---- grid reduction of p.q
     failed = __syncthreads_or(failed);
     if (failed) break;
-    double pqa[1] = {pq};
+    double pqa[1] = {double(pql)};
     cta_reduce_smem<1>(pqa, sfull);
     ++barrier_no;
     if (!grid_allreduce<1>(pqa, part_a + (loop & 1) * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh, wc)) {

@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     T* pnew[NR];
     bool act[NR];
     double pq[NR];
+    T pql[NR];  // a lane's p.q in the CG's type, converted once
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
       act[q] = done[q] == 0.0;
@@ -166,6 +167,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       pold[q] = (it[q] & 1) ? V.p0[q] : V.p1[q];
       pnew[q] = (it[q] & 1) ? V.p1[q] : V.p0[q];
       pq[q] = 0.0;
+      pql[q] = T(0);
     }
     // ---- product phase: q = K p_new over the owned slices, every active RHS from the same staged chunk
 #pragma unroll
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
           qr[q][j][0] = acc[q][0], qr[q][j][1] = acc[q][1], qr[q][j][2] = acc[q][2];
           if (row < A.n_rows) {
             store3(pnew[q], row, n0, n1, n2);
-            pq[q] += double(n0 * acc[q][0] + n1 * acc[q][1] + n2 * acc[q][2]);
+            pql[q] += n0 * acc[q][0] + n1 * acc[q][1] + n2 * acc[q][2];
           }
         }
       }
@@ -241,6 +243,8 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     const int par = loop & 1;
     failed = __syncthreads_or(failed);
     if (failed) break;
+#pragma unroll
+    for (int q = 0; q < NR; ++q) pq[q] = double(pql[q]);
     cta_reduce_smem<NR>(pq, sfull);
     ++barrier_no;
     if (!grid_allreduce<NR>(pq, part_a + par * NR * G, bar_count, barrier_no * (unsigned)G, sv, &ok_sh, wc)) {
@@ -265,7 +269,9 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     double red2[2 * NR];
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
-      double rzn = 0.0, rrn = 0.0;
+      // a lane's rows are summed in the CG's type and converted once (FP64 additions and conversions per row would
+      // load GB300's narrow FP64 pipe); the CTA and grid sums above them are FP64
+      T lrz = T(0), lrr = T(0);
       if (act[q]) {
         const T a = alpha[q];
 #pragma unroll
@@ -300,13 +306,13 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
               trz += r1[b] * zv[b];
               trr += r1[b] * r1[b];
             }
-            rzn += double(trz);
-            rrn += double(trr);
+            lrz += trz;
+            lrr += trr;
           }
         }
       }
-      red2[2 * q] = rzn;
-      red2[2 * q + 1] = rrn;
+      red2[2 * q] = double(lrz);
+      red2[2 * q + 1] = double(lrr);
     }
     cta_reduce_smem<2 * NR>(red2, sfull);
     ++barrier_no;
