@@ -699,8 +699,8 @@ def run_batched(args):
                     "newton_iterations_batch": info.totalIterations, "cg_iterations_sum": info.totalLinearIterations,
                     "instances_converged_last_step": int((conv == 1).sum()),
                     "instances_taken_out_element_inversion": int((conv == -1).sum()),
-                    "instances_not_converged": int((conv == 0).sum()),
-                    "taken_out": [int(i) for i in np.nonzero(conv == -1)[0]]}
+                    "instances_taken_out_not_converged": int((conv == -2).sum()),
+                    "taken_out": [int(i) for i in np.nonzero(conv < 0)[0]]}
         finals[key], status[key] = req.globalSolution(), conv.copy()
         del lc, nr, asm, fes
     both = np.nonzero((status["mixed"] == 1) & (status["plain_fp64"] == 1))[0]

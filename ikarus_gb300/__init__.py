@@ -1225,7 +1225,8 @@ class NewtonRaphson:
 
     def instance_info(self):
         """(iterations, residual norms, status) per instance of the last batched solve; status 1 converged,
-        0 not converged, -1 taken out after its elements inverted (det C <= 0)."""
+        -1 taken out after its elements inverted (det C <= 0), -2 taken out still above its tolerance after
+        maxIter (the others go on)."""
         n = self.assembler.fes.n_instances
         it = np.zeros(n, dtype=np.int32)
         rn = np.zeros(n)

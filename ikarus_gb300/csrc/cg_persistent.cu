@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[WARPS][NST];
   __shared__ double sv[2 * NR];
-  __shared__ double sdiv[NR];
+  __shared__ T s_alpha[NR], s_tb[NR];
+  __shared__ int s_dn[NR];
   __shared__ double sfull[2 * NR * WARPS * 32];
   __shared__ bool ok_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -78,8 +79,12 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
   constexpr bool kLean = NR > 1;
   constexpr int XS = kLean ? 1 : MAXS;
   T xr[NR][XS][3], rr_[NR][MAXS][3], zr[NR][XS][3], pr[NR][XS][3], qr[NR][MAXS][3];
-  double rz[NR], tol2[NR], rrs[NR], done[NR], beta[NR];
-  int maxit[NR], it[NR];
+  // The CG scalars are FP64 and thread 0 alone updates them (rz, r.r, beta, the stop decision); the other threads
+  // get the state code, alpha and beta in the CG's type through shared memory (GB300's FP64 pipe is narrow: 512
+  // threads repeating the divisions, comparisons and conversions cost microseconds per iteration)
+  double rz[NR], tol2[NR], rrs[NR], beta[NR];
+  int maxit[NR], it[NR], dn[NR];  // dn: 0 running, 1 converged, 2 iteration cap, 3 breakdown (as scal[kDone])
+  T tbv[NR];
   bool all_done = true;
 #pragma unroll
   for (int q = 0; q < NR; ++q) {
@@ -103,10 +108,11 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     tol2[q] = sc[kTol2];
     maxit[q] = (int)sc[kMaxIt];
     rrs[q] = sc[kRR];
-    done[q] = sc[kDone];
+    dn[q] = (int)sc[kDone];
     it[q] = (int)sc[kIters];
     beta[q] = 0.0;
-    all_done = all_done && done[q] != 0.0;
+    tbv[q] = T(0);
+    all_done = all_done && dn[q] != 0;
   }
 
   if (lane == 0) {
@@ -162,8 +168,8 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     T pql[NR];  // a lane's p.q in the CG's type, converted once
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
-      act[q] = done[q] == 0.0;
-      tb[q] = T(beta[q]);
+      act[q] = dn[q] == 0;
+      tb[q] = tbv[q];
       pold[q] = (it[q] & 1) ? V.p0[q] : V.p1[q];
       pnew[q] = (it[q] & 1) ? V.p1[q] : V.p0[q];
       pq[q] = 0.0;
@@ -251,19 +257,25 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       failed = true;
       break;
     }
-    double quo[NR];
-    cta_quotients<NR>(rz, pq, quo, sdiv);
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int q = 0; q < NR; ++q) {
+        T a = T(0);
+        if (dn[q] == 0) {
+          if (!(fabs(pq[q]) > 0.0) || !isfinite(pq[q])) dn[q] = 3;  // breakdown (negative curvature alone does not stop CG)
+          else a = T(rz[q] / pq[q]);
+        }
+        s_alpha[q] = a;
+        s_dn[q] = dn[q];
+      }
+    }
+    __syncthreads();
     T alpha[NR];
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
-      alpha[q] = T(0);
-      if (!act[q]) continue;
-      if (!(fabs(pq[q]) > 0.0) || !isfinite(pq[q])) {  // breakdown (negative curvature alone does not stop CG)
-        done[q] = 3.0;
-        act[q] = false;
-        continue;
-      }
-      alpha[q] = T(quo[q]);
+      alpha[q] = s_alpha[q];
+      dn[q] = s_dn[q];
+      act[q] = dn[q] == 0;
     }
     // ---- update phase on the owned rows
     double red2[2 * NR];
@@ -321,23 +333,29 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       failed = true;
       break;
     }
-    double rzn_all[NR], bq[NR];
+    if (threadIdx.x == 0) {
 #pragma unroll
-    for (int q = 0; q < NR; ++q) rzn_all[q] = red2[2 * q];
-    cta_quotients<NR>(rzn_all, rz, bq, sdiv);
+      for (int q = 0; q < NR; ++q) {
+        if (act[q]) {
+          const double rzs = red2[2 * q];
+          rrs[q] = red2[2 * q + 1];
+          beta[q] = rzs / rz[q];
+          rz[q] = rzs;
+          if (rrs[q] <= tol2[q]) dn[q] = 1;
+          else if (it[q] + 1 >= maxit[q]) dn[q] = 2;
+        }
+        s_tb[q] = T(beta[q]);
+        s_dn[q] = dn[q];
+      }
+    }
+    __syncthreads();
     all_done = true;
 #pragma unroll
     for (int q = 0; q < NR; ++q) {
-      if (act[q]) {
-        const double rzs = red2[2 * q];
-        rrs[q] = red2[2 * q + 1];
-        beta[q] = bq[q];
-        rz[q] = rzs;
-        ++it[q];
-        if (rrs[q] <= tol2[q]) done[q] = 1.0;
-        else if (it[q] >= maxit[q]) done[q] = 2.0;
-      }
-      all_done = all_done && done[q] != 0.0;
+      if (act[q]) ++it[q];
+      dn[q] = s_dn[q];
+      tbv[q] = s_tb[q];
+      all_done = all_done && dn[q] != 0;
     }
     ++loop;
   }
@@ -363,7 +381,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
       sc[kRR] = rrs[q];
       sc[kRz] = rz[q];
       sc[kBeta] = beta[q];
-      sc[kDone] = failed ? kDoneDeviceTimeout : done[q];
+      sc[kDone] = failed ? kDoneDeviceTimeout : (double)dn[q];
     }
     if (failed && threadIdx.x == 0) V.scal[q][kDone] = kDoneDeviceTimeout;
   }

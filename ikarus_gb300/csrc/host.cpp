@@ -1433,11 +1433,21 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
     }
     ++iter;
   }
+  // an instance still above its tolerance after max_iter is taken out as well (status -2), so that one
+  // instance's failure does not end the others' load path; the solve succeeds when every instance not taken out
+  // converged
   bool ok = true;
   for (int i = 0; i < ni; ++i) {
-    nr->inst_conv[i] = nr->inst_failed[i] ? -1 : (rn[i] <= thr[i] ? 1 : 0);
-    ok = ok && nr->inst_conv[i] != 0;
+    if (nr->inst_failed[i]) {
+      nr->inst_conv[i] = nr->inst_failed[i] == 2 ? -2 : -1;
+    } else if (rn[i] <= thr[i]) {
+      nr->inst_conv[i] = 1;
+    } else {
+      nr->inst_conv[i] = -2;
+      nr->inst_failed[i] = 2;
+    }
   }
+  for (int i = 0; i < ni; ++i) ok = ok && nr->inst_conv[i] != 0;
   nr->inst_res = rn;
   ikr_nr_info inf{};
   inf.success = ok ? 1 : 0;

@@ -464,9 +464,10 @@ int ikr_newton_graph_iterations(ikr_nr nr, int64_t* n);
 /* NonLinearSolverLogger::subscribeTo(nr) */
 int ikr_newton_subscribe_logger(ikr_nr nr, ikr_log_sink sink, void* user);
 /* per instance (batched solves): Newton iterations, final residual norm and convergence of the last solve
- * (1 converged, 0 not converged, -1 taken out after its elements inverted, det C <= 0 -- the reference aborts
- * there; here the other instances go on and the solve succeeds when all instances not taken out converge).
- * Instances taken out stay out for the rest of a LoadControl run. */
+ * (1 converged, -1 taken out after its elements inverted, det C <= 0 -- the reference aborts there --, -2 taken out
+ * because it was still above its tolerance after max_iter -- the reference's LoadControl stops there; here the
+ * other instances go on and the solve succeeds when all instances not taken out converge).  Instances taken out
+ * stay out for the rest of a LoadControl run. */
 int ikr_newton_instance_info(ikr_nr nr, int32_t* iterations, double* residual_norms, int32_t* converged);
 
 /* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
