@@ -75,7 +75,8 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[WARPS][NST];
   __shared__ double sv[2];
-  __shared__ double sdiv[1];
+  __shared__ T s_alpha, s_tb;
+  __shared__ int s_state;
   __shared__ double sfull[2 * WARPS * 32];
   __shared__ bool ok_sh;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -123,7 +124,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   }
   const double tol2 = scal[kTol2];
   const int maxit = (int)scal[kMaxIt];
+  // FP64 scalars: rz, r.r and beta are thread 0's (the others' copies are not updated); every thread keeps the
+  // stop decision, the iteration count and beta in the CG's type
   double rz = 0.0, rrs = scal[kRR], done = scal[kDone], beta = 0.0;
+  T tbv = T(0);
   int it = (int)scal[kIters];
 
   if (lane == 0) {
@@ -347,7 +351,7 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   }
 
   while (done == 0.0 && !failed) {
-    const T tb = T(beta);
+    const T tb = tbv;
     const T* pold = (it & 1) ? p0 : p1;
     T* pnew = (it & 1) ? p1 : p0;
     T pql = T(0);  // a lane's p.q in the CG's type, converted once
@@ -412,14 +416,18 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
       failed = true;
       break;
     }
-    if (!(fabs(pqa[0]) > 0.0) || !isfinite(pqa[0])) {  // breakdown
+    // thread 0 forms alpha (and the breakdown decision) in FP64 and hands it on in the CG's type
+    if (threadIdx.x == 0) {
+      const bool brk = !(fabs(pqa[0]) > 0.0) || !isfinite(pqa[0]);  // breakdown
+      s_state = brk ? 3 : 0;
+      s_alpha = brk ? T(0) : T(rz / pqa[0]);
+    }
+    __syncthreads();
+    if (s_state == 3) {
       done = 3.0;
       break;
     }
-    double quo[1];
-    const double rza[1] = {rz};
-    cta_quotients<1>(rza, pqa, quo, sdiv);
-    const T alpha = T(quo[0]);
+    const T alpha = s_alpha;
     // ---- update phase on the owned rows: x, r, z = D^-1 r
 #pragma unroll
     for (int j = 0; j < MAXS; ++j) {
@@ -442,18 +450,21 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
       failed = true;
       break;
     }
-    {
-      const double na[1] = {rzs}, da[1] = {rz};
-      double ba[1];
-      cta_quotients<1>(na, da, ba, sdiv);
-      beta = ba[0];
+    // thread 0 forms beta and the stop decision (FP64); the others read the decision and beta in the CG's type
+    if (threadIdx.x == 0) {
+      beta = rzs / rz;
+      rz = rzs;
+      s_state = rrs <= tol2 ? 1 : (it + 1 >= maxit ? 2 : 0);
+      s_tb = T(beta);
     }
-    rz = rzs;
+    __syncthreads();
     ++it;
-    if (rrs <= tol2) done = 1.0;
-    else if (it >= maxit) done = 2.0;
+    tbv = s_tb;
     ++loop;
-    if (done != 0.0) break;  // every CTA decides alike (the same sums)
+    if (s_state != 0) {  // every CTA decides alike (the same sums)
+      done = s_state;
+      break;
+    }
     ++barrier_no;
     if (!grid_sync(bar_count, barrier_no * (unsigned)G, &ok_sh, wc.polls)) {
       failed = true;
