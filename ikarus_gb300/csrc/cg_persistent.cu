@@ -25,6 +25,16 @@ namespace {
 
 using namespace cg;
 
+// The block-Jacobi inverses of a CTA's rows in shared memory for the whole solve (they do not change within it), so
+// that the update phase after the first grid barrier of an iteration reads them without an L2 round trip -- where
+// they fit beside the staging buffers.
+template <typename T, int CB, int NST, int WARPS, int MAXS>
+struct MinvShared {
+  static constexpr int kBytes = WARPS * MAXS * 32 * 9 * (int)sizeof(T);
+  static constexpr bool kOn = PersistentCfg<T, CB, NST, WARPS>::kSmemBytes + kBytes <= 200 * 1024;
+  static constexpr int kDynBytes = PersistentCfg<T, CB, NST, WARPS>::kSmemBytes + (kOn ? kBytes : 0);
+};
+
 // the right-hand sides one launch solves together: per RHS its solution, residual, preconditioned residual, the
 // two search-direction buffers (alternating by iteration parity) and its scalar block
 template <typename T, int NR>
@@ -114,6 +124,22 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
     tbv[q] = T(0);
     all_done = all_done && dn[q] != 0;
   }
+
+  using MS = MinvShared<T, CB, NST, WARPS, MAXS>;
+  T* msh = reinterpret_cast<T*>(smem + C::kSmemBytes);  // used when MS::kOn
+  if constexpr (MS::kOn) {
+#pragma unroll
+    for (int j = 0; j < MAXS; ++j) {
+      const int row = 32 * (gw + j * nw) + lane;
+      T* d = msh + ((size_t)(warp * MAXS + j) * 32 + lane) * 9;
+#pragma unroll
+      for (int k = 0; k < 9; ++k) d[k] = (j < ns && row < A.n_rows) ? __ldg(minv + 9 * (int64_t)row + k) : T(0);
+    }
+  }
+  auto minv_of = [&](int j, int row) -> const T* {
+    if constexpr (MS::kOn) return msh + ((size_t)(warp * MAXS + j) * 32 + lane) * 9;
+    return minv + 9 * (int64_t)row;
+  };
 
   if (lane == 0) {
     for (int st = 0; st < NST; ++st) mbar_init(smem_addr(&bars[warp][st]), 1);
@@ -304,11 +330,11 @@ __global__ void __launch_bounds__(WARPS * 32, MINB)
               r1[c] = rr_[q][j][c] - a * qr[q][j][c];
               rr_[q][j][c] = r1[c];
             }
-            const T* m = minv + 9 * (int64_t)row;
+            const T* m = minv_of(j, row);
             T zv[3];
 #pragma unroll
             for (int b = 0; b < 3; ++b) {
-              zv[b] = __ldg(m + 3 * b) * r1[0] + __ldg(m + 3 * b + 1) * r1[1] + __ldg(m + 3 * b + 2) * r1[2];
+              zv[b] = m[3 * b] * r1[0] + m[3 * b + 1] * r1[1] + m[3 * b + 2] * r1[2];
               if constexpr (!kLean) zr[q][j][b] = zv[b];
             }
             store3(V.z[q], row, zv[0], zv[1], zv[2]);
@@ -391,6 +417,7 @@ template <typename T, int CB, int NST, int WARPS, int MAXS, int MINB, int NR>
 cudaError_t launch_persistent(const Bsr& A, PcgWork* const* ws, double* part_a, double* part_b, cudaStream_t s,
                               bool query_only, bool* eligible) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
+  constexpr int kDyn = MinvShared<T, CB, NST, WARPS, MAXS>::kDynBytes;
   auto kern = pcg_persistent_kernel<T, CB, NST, WARPS, MAXS, MINB, NR>;
   static std::mutex mu;
   static int blocks_per_sm[64] = {0};
@@ -402,9 +429,9 @@ cudaError_t launch_persistent(const Bsr& A, PcgWork* const* ws, double* part_a, 
   {
     std::lock_guard<std::mutex> lk(mu);
     if (!blocks_per_sm[dev]) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmemBytes);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kDyn);
       int b = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, C::kThreads, C::kSmemBytes);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, C::kThreads, kDyn);
       blocks_per_sm[dev] = b > 0 ? b : -1;
     }
     bps = blocks_per_sm[dev];
@@ -433,7 +460,7 @@ cudaError_t launch_persistent(const Bsr& A, PcgWork* const* ws, double* part_a, 
   int64_t keep = w.keep_g;
   WaitCtl wc{w.barrier_polls > 0 ? w.barrier_polls : kBarrierSpinLimit, w.withhold_first_arrival};
   void* args[] = {&Acopy, &val, &minv, &V, &part_a, &part_b, &keep, &wc};
-  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(C::kThreads), args, C::kSmemBytes, s);
+  return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(C::kThreads), args, kDyn, s);
 }
 
 template <typename T, int NR>
