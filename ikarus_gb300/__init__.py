@@ -172,6 +172,7 @@ SIGNATURES = {
     "ikr_fes_set_element_materials": ([_vp, _dp, _dp], C.c_int),
     "ikr_fes_set_instances": ([_vp, _I, _ip], C.c_int),
     "ikr_newton_instance_info": ([_vp, _ip, _dp, _ip], C.c_int),
+    "ikr_newton_exclude_instances": ([_vp, _I, C.POINTER(C.c_uint8)], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
     "ikr_fes_set_material": ([_vp, _I], C.c_int),
@@ -1223,10 +1224,18 @@ class NewtonRaphson:
             _err(lib().ikr_newton_update(nr.h, req.h, _ptr(d)), "update")
         return f
 
+    def exclude_instances(self, mask=None):
+        """Keep the instances whose mask entry is true out of the following batched solves (None clears)."""
+        if mask is None:
+            _err(lib().ikr_newton_exclude_instances(self.h, 0, None))
+            return
+        m = np.ascontiguousarray(np.asarray(mask, dtype=bool).astype(np.uint8))
+        _err(lib().ikr_newton_exclude_instances(self.h, len(m), _ptr(m, C.c_uint8)))
+
     def instance_info(self):
         """(iterations, residual norms, status) per instance of the last batched solve; status 1 converged,
         -1 taken out after its elements inverted (det C <= 0), -2 taken out still above its tolerance after
-        maxIter (the others go on)."""
+        maxIter (the others go on), -3 kept out by exclude_instances."""
         n = self.assembler.fes.n_instances
         it = np.zeros(n, dtype=np.int32)
         rn = np.zeros(n)

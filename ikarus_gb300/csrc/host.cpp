@@ -1292,6 +1292,8 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   const int ni = f->n_inst;
   const int64_t n = a->n;
   if ((int)nr->inst_failed.size() != ni) nr->inst_failed.assign(ni, 0);
+  for (int i = 0; i < ni && i < (int)nr->inst_excluded.size(); ++i)
+    if (nr->inst_excluded[i]) nr->inst_failed[i] = 3;  // kept out by the caller
   struct StatusScope {  // per-instance element status for the duration of the solve
     ikr_fes f;
     explicit StatusScope(ikr_fes ff) : f(ff) { f->inst_status_on = true; }
@@ -1439,7 +1441,7 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   bool ok = true;
   for (int i = 0; i < ni; ++i) {
     if (nr->inst_failed[i]) {
-      nr->inst_conv[i] = nr->inst_failed[i] == 2 ? -2 : -1;
+      nr->inst_conv[i] = nr->inst_failed[i] == 3 ? -3 : (nr->inst_failed[i] == 2 ? -2 : -1);
     } else if (rn[i] <= thr[i]) {
       nr->inst_conv[i] = 1;
     } else {
@@ -1626,6 +1628,13 @@ void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double 
 
 extern "C" {
 
+int ikr_newton_exclude_instances(ikr_nr nr, int32_t n, const uint8_t* mask) {
+  return guarded([&] {
+    need(nr && n >= 0 && (n == 0 || mask), IKR_ERR_ARG, "invalid argument");
+    need(n == 0 || n == nr->asm_->fes->n_inst, IKR_ERR_ARG, "one mask entry per instance");
+    nr->inst_excluded.assign(mask, mask + n);
+  });
+}
 int ikr_newton_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info) {
   return guarded([&] {
     need(nr && r, IKR_ERR_ARG, "null argument");

@@ -1284,6 +1284,7 @@ struct ikr_nr_s {
   std::vector<double> inst_res;
   std::vector<int8_t> inst_conv;     // 1 converged, 0 not, -1 taken out after an element inversion
   std::vector<uint8_t> inst_failed;  // inversions seen since the last reset (LoadControl::run, newton_solve)
+  std::vector<uint8_t> inst_excluded;  // instances the caller keeps out of every solve (ikr_newton_exclude_instances)
   DBuf<double> u_old, alpha_old, inst_step;  // backtracking: state before the correction, per-instance steps
   int64_t backtracks = 0;                    // corrections halved since creation
   DBuf<double> inst_norm, inst_rtol;

@@ -465,10 +465,16 @@ int ikr_newton_graph_iterations(ikr_nr nr, int64_t* n);
 int ikr_newton_subscribe_logger(ikr_nr nr, ikr_log_sink sink, void* user);
 /* per instance (batched solves): Newton iterations, final residual norm and convergence of the last solve
  * (1 converged, -1 taken out after its elements inverted, det C <= 0 -- the reference aborts there --, -2 taken out
- * because it was still above its tolerance after max_iter -- the reference's LoadControl stops there; here the
+ * because it was still above its tolerance after max_iter -- the reference's LoadControl stops there --, -3 kept out
+ * by ikr_newton_exclude_instances; here the
  * other instances go on and the solve succeeds when all instances not taken out converge).  Instances taken out
  * stay out for the rest of a LoadControl run. */
 int ikr_newton_instance_info(ikr_nr nr, int32_t* iterations, double* residual_norms, int32_t* converged);
+/* batched solves (no reference counterpart): instances whose mask entry is nonzero take no part in the following
+ * solves (no corrections; their displacement stays as the requirement holds it; status -3 in instance_info), e.g.
+ * to solve again in FP64 only the instances an FP32 run took out.  n = 0 clears the mask; otherwise n must equal
+ * the number of instances. */
+int ikr_newton_exclude_instances(ikr_nr nr, int32_t n, const uint8_t* mask);
 
 /* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
 typedef struct ikr_control_state {   /* ControlRoutineState (controlroutinestate.hh:21-31) */

@@ -64,3 +64,44 @@ def test_an_inverting_instance_is_taken_out_and_the_others_converge(ikr):
         ref = oracle.from_problem(part).load_control(bp.load_steps, tol=1e-8, tol_mode=1)
         ui = u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]]
         assert np.abs(ui - ref["u"]).max() <= 1e-6 * np.abs(ref["u"]).max(), i
+
+
+def test_excluded_instances_take_no_part_and_the_others_are_unchanged(ikr):
+    """ikr_newton_exclude_instances: the excluded instances get no corrections (their displacement stays zero,
+    status -3); the others reach the same solution as without the exclusion (within the FP64 rounding of a
+    different CTA plan), and a following run of only the excluded instances solves them as well -- the FP64 retry
+    the benchmark applies to the instances an FP32 run took out."""
+    bp = problems.batched_cantilevers(n=8, seed=3, nx=(3, 8), nyz=(1, 3), E=(1e3, 1e4), t=(0.1, 0.5), load_steps=3)
+    st = ikr.NRSettings(tol=1e-9, maxIter=30, relative=True, linear_rtol=1e-12)
+
+    def run(exclude=None):
+        fes, asm = problems.build_gpu_batched(bp, precision=0)
+        req = ikr.FERequirements(fes)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+        if exclude is not None:
+            nr.exclude_instances(exclude)
+        info = ikr.LoadControl(nr, bp.load_steps).run(req)
+        return info, nr.instance_info()[2], req.globalSolution()
+
+    info0, conv0, u0 = run()
+    assert info0.success and (conv0 == 1).all()
+    mask = np.zeros(8, dtype=bool)
+    mask[[1, 6]] = True
+    info1, conv1, u1 = run(mask)
+    assert info1.success
+    assert (conv1[mask] == -3).all() and (conv1[~mask] == 1).all()
+    info2, conv2, u2 = run(~mask)
+    assert info2.success and (conv2[mask] == 1).all() and (conv2[~mask] == -3).all()
+    for i in range(8):
+        sl = slice(3 * bp.node_offsets[i], 3 * bp.node_offsets[i + 1])
+        scale = np.abs(u0[sl]).max()
+        if mask[i]:
+            assert not u1[sl].any()
+            assert np.abs(u2[sl] - u0[sl]).max() <= 1e-9 * scale
+        else:
+            assert not u2[sl].any()
+            assert np.abs(u1[sl] - u0[sl]).max() <= 1e-9 * scale
+    with pytest.raises(ikr.IkarusError):
+        fes, asm = problems.build_gpu_batched(bp, precision=0)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+        nr.exclude_instances(np.zeros(5, dtype=bool))
