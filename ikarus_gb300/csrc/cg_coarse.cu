@@ -20,6 +20,7 @@
 // Before the first iteration the same coarse part turns the init kernel's z = D^-1 r_0 into M^-1 r_0.  All sums
 // have a fixed order: a solve is bit-identical run to run.  Every wait is bounded (grid barriers and stage waits
 // give up with scal[kDone] = 6 after their poll limits).
+#include <algorithm>
 #include <mutex>
 
 #include "cg_grid.cuh"
@@ -70,7 +71,8 @@ __device__ __forceinline__ bool grid_sync(unsigned int* count, unsigned int targ
 template <typename T, int CB, int NST, int WARPS, int MAXS>
 __global__ void __launch_bounds__(WARPS * 32, 1)
     pcg_coarse_kernel(Bsr A, const T* __restrict__ val, const T* __restrict__ minv, T* x, const T* r, T* z, T* p0,
-                      T* p1, double* scal, Coarse Cc, double* part_a, double* cpart, int64_t keep_g, WaitCtl wc) {
+                      T* p1, double* scal, Coarse Cc, double* part_a, double* cpart, int64_t keep_g, WaitCtl wc,
+                      int ainv_shared) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[WARPS][NST];
@@ -90,10 +92,11 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   // coarse shared arrays after the stages: per-warp mode sums (WARPS x nc), r_c (+ the two dot products), e
   // coarse shared arrays after the stages: per-warp mode sums (WARPS x n_c, also the blockDim.x partials of e),
   // the two FP64 dot products, r_c and e in the CG's type
-  T* accw = reinterpret_cast<T*>(smem + (size_t)WARPS * NST * C::kStageBytes);
-  double* rdot = reinterpret_cast<double*>(accw + (size_t)WARPS * kCoarseFusedMaxDofs);
-  T* rct = reinterpret_cast<T*>(rdot + 2);
-  T* ect = rct + kCoarseFusedMaxDofs;
+  double* rdot = reinterpret_cast<double*>(smem + (size_t)WARPS * NST * C::kStageBytes);
+  T* accw = reinterpret_cast<T*>(rdot + 2);
+  T* rct = accw + max(WARPS * nc, WARPS * 32);
+  T* ect = rct + nc;
+  T* ainv_s = ect + nc;  // A_c^-1 in shared memory for the whole solve, where it fits (ainv_shared)
   const T* ainv = static_cast<const T*>(Cc.ainv);
 
   int ns = 0;
@@ -130,6 +133,10 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
   T tbv = T(0);
   int it = (int)scal[kIters];
 
+  if (ainv_shared) {
+    for (int k = threadIdx.x; k < nc * nc; k += blockDim.x) ainv_s[k] = __ldg(ainv + k);
+    __syncthreads();
+  }
   if (lane == 0) {
     for (int st = 0; st < NST; ++st) mbar_init(smem_addr(&bars[warp][st]), 1);
     mbar_init_fence();
@@ -267,8 +274,12 @@ __global__ void __launch_bounds__(WARPS * 32, 1)
       T sum = T(0);
       if (seg < nseg) {
         const int j1 = min(nc, (seg + 1) * seg_len);
+        if (ainv_shared) {
+          for (int j = seg * seg_len; j < j1; ++j) sum += ainv_s[(size_t)j * nc + i] * rct[j];
+        } else {
 #pragma unroll 16
-        for (int j = seg * seg_len; j < j1; ++j) sum += __ldg(ainv + (size_t)j * nc + i) * rct[j];
+          for (int j = seg * seg_len; j < j1; ++j) sum += __ldg(ainv + (size_t)j * nc + i) * rct[j];
+        }
       }
       accw[t] = sum;  // the mode-sum array is free again
       __syncthreads();
@@ -497,7 +508,15 @@ cudaError_t launch_coarse_cfg(const Bsr& A, PcgWork& w, const Coarse& Cc, cudaSt
                               bool* eligible) {
   using C = PersistentCfg<T, CB, NST, WARPS>;
   auto kern = pcg_coarse_kernel<T, CB, NST, WARPS, MAXS>;
-  const size_t smem = (size_t)C::kSmemBytes + sizeof(T) * (size_t)(WARPS + 2) * kCoarseFusedMaxDofs + 2 * sizeof(double);
+  // dynamic shared memory: the stages, two FP64 dot products, the per-warp mode sums (also the CTA's e partials), r_c
+  // and e, and A_c^-1 itself where it fits under the budget (one CTA per SM either way)
+  constexpr size_t kBudget = 216 * 1024;
+  const size_t nc = (size_t)Cc.n_c;
+  const size_t base = (size_t)C::kSmemBytes + 2 * sizeof(double) +
+                      sizeof(T) * (std::max(WARPS * nc, (size_t)WARPS * 32) + 2 * nc);
+  const int ainv_shared = base + sizeof(T) * nc * nc <= kBudget ? 1 : 0;
+  const size_t smem = base + (ainv_shared ? sizeof(T) * nc * nc : 0);
+  const size_t smem_max = kBudget;
   static std::mutex mu;
   static int blocks_per_sm[64] = {0};
   int dev = 0;
@@ -507,9 +526,9 @@ cudaError_t launch_coarse_cfg(const Bsr& A, PcgWork& w, const Coarse& Cc, cudaSt
   {
     std::lock_guard<std::mutex> lk(mu);
     if (!blocks_per_sm[dev]) {
-      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
       int b = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, C::kThreads, smem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, C::kThreads, smem_max);
       blocks_per_sm[dev] = b > 0 ? b : -1;
     }
     bps = blocks_per_sm[dev];
@@ -519,7 +538,8 @@ cudaError_t launch_coarse_cfg(const Bsr& A, PcgWork& w, const Coarse& Cc, cudaSt
   int grid = bps > 0 ? w.sms * bps : 0;
   if (grid > w.grid) grid = w.grid;
   *eligible = coop && grid > 0 && grid <= 32 * kGridLanes && (int64_t)grid * WARPS * MAXS >= A.n_slices && Cc.n_c > 0 &&
-              Cc.n_c <= kCoarseFusedMaxDofs && w.coarse_part != nullptr && grid <= w.coarse_part_ctas;
+              Cc.n_c <= kCoarseFusedMaxDofs && w.coarse_part != nullptr && grid <= w.coarse_part_ctas &&
+              smem <= smem_max;
   if (query_only || !*eligible) return cudaSuccess;
   const T* val = (const T*)A.val;
   const T* minv = (const T*)w.minv;
@@ -535,7 +555,8 @@ cudaError_t launch_coarse_cfg(const Bsr& A, PcgWork& w, const Coarse& Cc, cudaSt
   double* cp = w.coarse_part;
   int64_t keep = w.keep_g;
   WaitCtl wc{w.barrier_polls > 0 ? w.barrier_polls : kBarrierSpinLimit, 0};
-  void* args[] = {&Acopy, &val, &minv, &x, &r, &z, &p0, &p1, &scal, &Ccopy, &pa, &cp, &keep, &wc};
+  int ash = ainv_shared;
+  void* args[] = {&Acopy, &val, &minv, &x, &r, &z, &p0, &p1, &scal, &Ccopy, &pa, &cp, &keep, &wc, &ash};
   return cudaLaunchCooperativeKernel((const void*)kern, dim3(grid), dim3(C::kThreads), args, smem, s);
 }
 
