@@ -173,6 +173,7 @@ SIGNATURES = {
     "ikr_fes_set_instances": ([_vp, _I, _ip], C.c_int),
     "ikr_newton_instance_info": ([_vp, _ip, _dp, _ip], C.c_int),
     "ikr_newton_exclude_instances": ([_vp, _I, C.POINTER(C.c_uint8)], C.c_int),
+    "ikr_newton_instance_linear_iterations": ([_vp, _i64p], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
     "ikr_fes_set_material": ([_vp, _I], C.c_int),
@@ -1242,6 +1243,12 @@ class NewtonRaphson:
         cv = np.zeros(n, dtype=np.int32)
         _err(lib().ikr_newton_instance_info(self.h, _ptr(it, C.c_int32), _ptr(rn), _ptr(cv, C.c_int32)))
         return it, rn, cv
+
+    def instance_linear_iterations(self):
+        """CG iterations per instance over the last batched solve."""
+        out = np.zeros(self.assembler.fes.n_instances, dtype=np.int64)
+        _err(lib().ikr_newton_instance_linear_iterations(self.h, _ptr(out, C.c_int64)))
+        return out
 
     def solve(self, req: FERequirements, stepSize: float = 0.0) -> NonLinearSolverInformation:
         info = _NRInfo()

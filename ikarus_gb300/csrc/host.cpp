@@ -1324,7 +1324,20 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   std::vector<uint8_t> act(ni), careful(ni, 0);
   std::vector<int32_t> cgit(ni);
   nr->inst_iters.assign(ni, 0);
+  nr->inst_lin.assign(ni, 0);
   nr->inst_conv.assign(ni, 0);
+  // the observers see the largest residual norm over the instances still in the solve and the batch's Newton
+  // iteration count (newtonraphson.hh:193-257 notifies per iteration; here one iteration serves every instance)
+  ikr_nr_state state{r, INFINITY, INFINITY, 0, r->lambda};
+  auto notify = [&](int msg, int it) {
+    double m = 0.0;
+    for (int i = 0; i < ni; ++i)
+      if (!nr->inst_failed[i] && std::isfinite(rn[i])) m = std::max(m, rn[i]);
+    state.residual_norm = m;
+    state.iterations = it;
+    state.load_factor = r->lambda;
+    for (auto& o : nr->obs) o.cb(msg, &state, o.user);
+  };
   auto norms = [&]() {
     ikr::launch_instance_norms(a->R.p, ni, f->inst_off.p, nr->inst_norm.p, s);
     count(1);
@@ -1339,12 +1352,14 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
     thr[i] = st.tol_mode == 1 ? st.tol * r0[i] : st.tol;
     act[i] = rn[i] > thr[i] && !nr->inst_failed[i];
   }
+  notify(IKR_NLS_INIT, 0);
   if (!a->nb) a->build_pattern();
   nr->ls->setup(a);
   int iter = 0;
   int64_t lin = 0;
   auto any = [&] { return std::any_of(act.begin(), act.end(), [](uint8_t v) { return v != 0; }); };
   while ((any() && iter < st.max_iter) || iter < st.min_iter) {
+    notify(IKR_NLS_ITERATION_STARTED, iter);
     assemble_matrix(a, r, IKR_DBC_FULL);
     collect_failures();
     for (int i = 0; i < ni; ++i)
@@ -1427,13 +1442,17 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
         collect_failures();
       }
     }
+    notify(IKR_NLS_SOLUTION_CHANGED, iter);
     norms();
     for (int i = 0; i < ni; ++i) {
       lin += cgit[i];
+      nr->inst_lin[i] += cgit[i];
       if (act[i]) nr->inst_iters[i]++;
       act[i] = rn[i] > thr[i] && std::isfinite(rn[i]) && !nr->inst_failed[i];
     }
     ++iter;
+    notify(IKR_NLS_RESIDUALNORM_UPDATED, iter);
+    notify(IKR_NLS_ITERATION_ENDED, iter);
   }
   // an instance still above its tolerance after max_iter is taken out as well (status -2), so that one
   // instance's failure does not end the others' load path; the solve succeeds when every instance not taken out
@@ -1457,6 +1476,7 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   inf.correction_norm = 0.0;
   inf.iterations = iter;
   inf.linear_iterations = lin;
+  if (ok) notify(IKR_NLS_FINISHED_SUCESSFULLY, iter);
   if (info) *info = inf;
 }
 
@@ -1628,6 +1648,12 @@ void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double 
 
 extern "C" {
 
+int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations) {
+  return guarded([&] {
+    need(nr && cg_iterations, IKR_ERR_ARG, "null argument");
+    for (size_t i = 0; i < nr->inst_lin.size(); ++i) cg_iterations[i] = nr->inst_lin[i];
+  });
+}
 int ikr_newton_exclude_instances(ikr_nr nr, int32_t n, const uint8_t* mask) {
   return guarded([&] {
     need(nr && n >= 0 && (n == 0 || mask), IKR_ERR_ARG, "invalid argument");

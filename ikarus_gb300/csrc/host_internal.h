@@ -1281,6 +1281,7 @@ struct ikr_nr_s {
   DBuf<double> nrm_part, nrm_out;
   // per-instance state of the last solve (element sets with instances)
   std::vector<int32_t> inst_iters;
+  std::vector<int64_t> inst_lin;  // CG iterations per instance over the solve
   std::vector<double> inst_res;
   std::vector<int8_t> inst_conv;     // 1 converged, 0 not, -1 taken out after an element inversion
   std::vector<uint8_t> inst_failed;  // inversions seen since the last reset (LoadControl::run, newton_solve)

@@ -475,6 +475,10 @@ int ikr_newton_instance_info(ikr_nr nr, int32_t* iterations, double* residual_no
  * to solve again in FP64 only the instances an FP32 run took out.  n = 0 clears the mask; otherwise n must equal
  * the number of instances. */
 int ikr_newton_exclude_instances(ikr_nr nr, int32_t n, const uint8_t* mask);
+/* batched solves (no reference counterpart): CG iterations per instance over the last solve (one value per
+ * instance).  The batched solve notifies the solver's observers like the single-system one, with the largest
+ * residual norm over the instances still in the solve. */
+int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations);
 
 /* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
 typedef struct ikr_control_state {   /* ControlRoutineState (controlroutinestate.hh:21-31) */

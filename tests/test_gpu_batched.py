@@ -105,3 +105,31 @@ def test_excluded_instances_take_no_part_and_the_others_are_unchanged(ikr):
         fes, asm = problems.build_gpu_batched(bp, precision=0)
         nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
         nr.exclude_instances(np.zeros(5, dtype=bool))
+
+
+def test_batched_solve_notifies_observers_and_counts_cg_iterations_per_instance(ikr):
+    """The batched Newton notifies INIT, ITERATION_STARTED/ENDED and FINISHED like the single-system one
+    (newtonraphson.hh:193-257), with the largest residual norm over the instances in the solve; the per-instance
+    CG iteration counts sum to the solve's linear iterations."""
+    bp = problems.batched_cantilevers(n=5, seed=3, nx=(3, 6), nyz=(1, 2), E=(1e3, 1e4), t=(0.1, 0.4), load_steps=2)
+    fes, asm = problems.build_gpu_batched(bp, precision=1)
+    st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                        linear_rtol_min=1e-6)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    M = ikr.NonLinearSolverMessages
+    seen = []
+    nr.subscribe(lambda msg, s: seen.append((msg, s["iterations"], s["residualNorm"])))
+    req = ikr.FERequirements(fes)
+    req.insertParameter(0.5)
+    info = nr.solve(req)
+    assert info.success
+    msgs = [m for m, _, _ in seen]
+    assert msgs[0] == M.INIT and msgs[-1] == M.FINISHED_SUCESSFULLY
+    ended = [(it, rn) for m, it, rn in seen if m == M.ITERATION_ENDED]
+    assert len(ended) == info.iterations == msgs.count(M.ITERATION_STARTED)
+    assert [it for it, _ in ended] == list(range(1, info.iterations + 1))
+    its, rn, conv = nr.instance_info()
+    assert (conv == 1).all()
+    assert ended[-1][1] == pytest.approx(rn.max(), rel=0, abs=0)
+    lin = nr.instance_linear_iterations()
+    assert lin.sum() == info.linearIterations and (lin > 0).all()
