@@ -174,6 +174,8 @@ SIGNATURES = {
     "ikr_newton_instance_info": ([_vp, _ip, _dp, _ip], C.c_int),
     "ikr_newton_exclude_instances": ([_vp, _I, C.POINTER(C.c_uint8)], C.c_int),
     "ikr_newton_instance_linear_iterations": ([_vp, _i64p], C.c_int),
+    "ikr_newton_set_batched_cg": ([_vp, _I, _I], C.c_int),
+    "ikr_newton_batched_cg_launches": ([_vp, _i64p], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
     "ikr_fes_set_material": ([_vp, _I], C.c_int),
@@ -1249,6 +1251,16 @@ class NewtonRaphson:
         out = np.zeros(self.assembler.fes.n_instances, dtype=np.int64)
         _err(lib().ikr_newton_instance_linear_iterations(self.h, _ptr(out, C.c_int64)))
         return out
+
+    def set_batched_cg(self, rows_loop=False, first_chunk=0):
+        """Batched solves: the CG runs as launches of first_chunk (0: 128), then doubling, iterations, re-planned
+        over the instances still running; rows_loop keeps the variant that loops over rows (tests, tuning)."""
+        _err(lib().ikr_newton_set_batched_cg(self.h, int(bool(rows_loop)), int(first_chunk)))
+
+    def batched_cg_launches(self):
+        n = C.c_int64()
+        _err(lib().ikr_newton_batched_cg_launches(self.h, C.byref(n)))
+        return n.value
 
     def solve(self, req: FERequirements, stepSize: float = 0.0) -> NonLinearSolverInformation:
         info = _NRInfo()

@@ -1,17 +1,25 @@
 // Many independent instances of uneven size in one element set: per-instance CG and norms (sm_103a).
 //
 // The instances are disjoint contiguous node ranges of one mesh, so the tangent is block diagonal by instance.
-// batched_pcg_kernel runs the complete block-Jacobi PCG of every instance in one cooperative launch.  Each
-// instance gets a group of CTAs sized to its node count (the host sizes the groups so that all CTAs are
-// co-resident); the CTAs of a group split the instance's block rows into contiguous chunks, one thread per
-// row.  An iteration has two group-wide reductions (p.q, then r.z and r.r): every CTA publishes its partial,
-// arrives on the instance's barrier counter and waits for the group, then sums the group's partials in CTA
-// order, so alpha, beta and the convergence decision are identical in the group's CTAs and run to run.  A
-// one-CTA group needs no global barrier.  p_new = z + beta p_old is formed on the fly for every gathered
-// neighbour (as in the single-system CG), which removes the barrier a separate p update would need.
-// Groups never wait on each other; instances whose Newton iteration has already converged get a zero
-// correction.  Every wait on a barrier is bounded; a wait that gives up marks the instance (iters = -1).
+// batched_pcg_kernel runs the block-Jacobi PCG of many instances in one launch.  Each instance gets a group of CTAs
+// (the host sizes the groups so that all CTAs are co-resident); the CTAs of a group split the instance's block rows
+// into contiguous chunks, one thread per row.  An iteration has two group-wide reductions (p.q, then r.z and r.r):
+// every CTA sums its threads' values (FP64 additions by one warp), publishes the sum, arrives on the instance's
+// barrier counter with release semantics and waits (bounded) for the group; lane b of warp 0 then loads CTA b's sum
+// and the butterfly adds them, so alpha, beta and the convergence decision are identical in the group's CTAs and run
+// to run.  A one-CTA group needs no global barrier.  p_new = z + beta p_old is formed on the fly for every gathered
+// neighbour, which removes the barrier a separate p update would need.
+//
+// The solves of a Newton iteration are latency-bound: a hard instance needs thousands of iterations after the easy
+// ones have converged.  So the host runs a solve as a sequence of launches of at most `chunk` iterations each and
+// re-plans the groups over the instances still running before every launch: the state of every instance (its
+// vectors in the work arrays, rz, r.r, b.b, beta and the iteration count in `st` / `its`) carries over, the CG is
+// continued, not restarted.  When every running instance fits one row per thread (REG), a thread keeps its row's
+// x, r, z, p, q and block-Jacobi inverse in registers for the whole launch; otherwise (GEN) a thread loops over its
+// rows with the state in the work arrays.  Every wait on a barrier is bounded; a wait that gives up ends the
+// instance with flag -1.
 #include "cg_common.cuh"
+#include "cg_grid.cuh"
 
 namespace ikr {
 
@@ -22,184 +30,283 @@ using namespace cg;
 constexpr int kBatchThreads = 256;
 constexpr int kGroupSpinLimit = 1 << 24;
 
-__device__ __forceinline__ double cta_sum(double v, double* sh) {
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double r = (threadIdx.x < (blockDim.x >> 5)) ? sh[threadIdx.x] : 0.0;
-  if (threadIdx.x < 32) r = warp_sum(r);
-  if (threadIdx.x == 0) sh[32] = r;
-  __syncthreads();
-  r = sh[32];
-  __syncthreads();
-  return r;
+// neighbour gathers from the node-padded work vectors; L2: read around L1 (values other CTAs of the group wrote)
+template <bool L2>
+__device__ __forceinline__ V3<float> gather3(const float* v, int node) {
+  const float4* p = reinterpret_cast<const float4*>(v) + node;
+  const float4 a = L2 ? __ldcg(p) : *p;
+  return {a.x, a.y, a.z};
+}
+template <bool L2>
+__device__ __forceinline__ V3<double> gather3(const double* v, int node) {
+  const double2* p = reinterpret_cast<const double2*>(v) + 2 * node;
+  const double2 a = L2 ? __ldcg(p) : *p;
+  const double c = L2 ? __ldcg(v + 4 * node + 2) : v[4 * node + 2];
+  return {a.x, a.y, c};
 }
 
-// group-wide sums of N values per CTA: publish, arrive, wait (bounded), sum the group's partials in CTA order.
-// Partials are double-buffered by `slot` (the two reductions of an iteration alternate), so a CTA that runs
-// ahead never overwrites partials another CTA of the group has still to read.
-template <int N>
-__device__ __forceinline__ bool group_reduce(double (&v)[N], double* part, int first, int size, int slot,
-                                             unsigned int* counter, unsigned int target, double* sh, bool* ok_sh) {
-  double cta[N];
+// q = K (z + tb p_old) on block row `row`; the columns of U blocks are loaded before their vector gathers so that
+// the gathers of U neighbours are in flight together (four in FP32, two in FP64, within the register budget)
+template <typename T, bool L2, int U = sizeof(T) == 4 ? 4 : 2>
+__device__ __forceinline__ V3<T> row_product(const Bsr& A, const T* __restrict__ val, const T* zw, const T* pold, T tb,
+                                             int row) {
+  const int s = row >> 5, l = row & 31;
+  const int gs = __ldg(A.slice_off + s), ge = __ldg(A.slice_off + s + 1);
+  T a0 = T(0), a1 = T(0), a2 = T(0);
+  for (int g0 = gs; g0 < ge; g0 += U) {
+    int c[U];
 #pragma unroll
-  for (int k = 0; k < N; ++k) cta[k] = cta_sum(v[k], sh);
-  if (size == 1) {
+    for (int k = 0; k < U; ++k) c[k] = g0 + k < ge ? __ldg(A.col_sell + 32 * (g0 + k) + l) : -1;
+    V3<T> zv[U], pv[U];
 #pragma unroll
-    for (int k = 0; k < N; ++k) v[k] = cta[k];
-    return true;
+    for (int k = 0; k < U; ++k) {
+      if (c[k] >= 0) {
+        zv[k] = gather3<L2>(zw, c[k]);
+        pv[k] = gather3<L2>(pold, c[k]);
+      } else {
+        zv[k] = {T(0), T(0), T(0)};
+        pv[k] = zv[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      if (c[k] >= 0) {
+        const T* v = val + (int64_t)(g0 + k) * 288 + l;
+        const T x0 = zv[k].x + tb * pv[k].x, x1 = zv[k].y + tb * pv[k].y, x2 = zv[k].z + tb * pv[k].z;
+        a0 += __ldg(v) * x0 + __ldg(v + 32) * x1 + __ldg(v + 64) * x2;
+        a1 += __ldg(v + 96) * x0 + __ldg(v + 128) * x1 + __ldg(v + 160) * x2;
+        a2 += __ldg(v + 192) * x0 + __ldg(v + 224) * x1 + __ldg(v + 256) * x2;
+      }
+    }
   }
-  if (threadIdx.x == 0) {
+  return {a0, a1, a2};
+}
+
+template <typename T>
+__device__ __forceinline__ V3<T> jacobi(const T (&m)[9], const V3<T>& r) {
+  return {m[0] * r.x + m[1] * r.y + m[2] * r.z, m[3] * r.x + m[4] * r.y + m[5] * r.z,
+          m[6] * r.x + m[7] * r.y + m[8] * r.z};
+}
+template <typename T>
+__device__ __forceinline__ void load_minv(const T* __restrict__ minv, int row, T (&m)[9]) {
 #pragma unroll
-    for (int k = 0; k < N; ++k) part[(size_t)(2 * blockIdx.x + slot) * 2 + k] = cta[k];
-    __threadfence();
-    atomicAdd(counter, 1u);
-    bool ok = false;
+  for (int k = 0; k < 9; ++k) m[k] = __ldg(minv + 9 * (int64_t)row + k);
+}
+
+// Group-wide sums of N values: the CTA sum (warp 0 adds the threads' values in order), then, for a group of several
+// CTAs, thread 0 publishes it (part: 2 slots x 2 values per CTA; the reductions of an iteration alternate slots, so a
+// CTA that runs ahead never overwrites a sum another CTA has still to read), arrives with release semantics and polls
+// (bounded) with acquire semantics; lane b < size of warp 0 loads CTA first + b's sum and the butterfly adds them.
+// The sums are valid in warp 0; false (in warp 0) when the wait gave up.
+template <int N>
+__device__ __forceinline__ bool group_sum(double (&v)[N], double* sfull, double* part, int first, int size, int slot,
+                                          unsigned int* counter, unsigned int target) {
+  cta_reduce_smem<N>(v, sfull);
+  if (threadIdx.x >= 32 || size == 1) return true;
+  const int lane = threadIdx.x;
+  int ok = 1;
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) part[((size_t)blockIdx.x * 2 + slot) * 2 + k] = v[k];
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(counter) : "memory");
+    ok = 0;
     for (int i = 0; i < kGroupSpinLimit; ++i) {
       unsigned int c;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(counter) : "memory");
       if (c >= target) {
-        ok = true;
+        ok = 1;
         break;
       }
-      __nanosleep(32);
+      if (i > 32) __nanosleep(32);
     }
-    *ok_sh = ok;
   }
-  __syncthreads();
-  __threadfence();
-  const bool ok = *ok_sh;
-  __syncthreads();
+  __syncwarp();
+  ok = __shfl_sync(0xffffffffu, ok, 0);
   if (!ok) return false;
 #pragma unroll
   for (int k = 0; k < N; ++k) {
-    double s = 0.0;
-    for (int b = 0; b < size; ++b) s += __ldcg(part + (size_t)(2 * (first + b) + slot) * 2 + k);
-    v[k] = s;
+    const double t = lane < size ? __ldcg(part + ((size_t)(first + lane) * 2 + slot) * 2 + k) : 0.0;
+    v[k] = warp_sum(t);
   }
   return true;
 }
 
-// q = K p_new for rows [ra, rb) with p_new = z + beta p_old formed per gathered neighbour and written for the
-// own rows; returns the thread's share of p_new . q.  Neighbour values written by other CTAs of the group are
-// read around L1 (L2_ONLY).
-template <typename T, bool L2_ONLY>
-__device__ __forceinline__ double spmv_rows(const Bsr& A, const T* __restrict__ val, const T* zw, const T* pold,
-                                            T* pnew, T* qw, T tb, int ra, int rb) {
-  auto ld = [](const T* p) { return L2_ONLY ? __ldcg(p) : *p; };
-  double pq = 0.0;
-  for (int row = ra + threadIdx.x; row < rb; row += blockDim.x) {
-    const int s = row >> 5, l = row & 31;
-    T a0 = T(0), a1 = T(0), a2 = T(0);
-    for (int g = A.slice_off[s]; g < A.slice_off[s + 1]; ++g) {
-      const int c = A.col_sell[32 * g + l];
-      const T* v = val + (int64_t)g * 288 + l;
-      const T x0 = ld(zw + 4 * c) + tb * ld(pold + 4 * c);
-      const T x1 = ld(zw + 4 * c + 1) + tb * ld(pold + 4 * c + 1);
-      const T x2 = ld(zw + 4 * c + 2) + tb * ld(pold + 4 * c + 2);
-      a0 += v[0] * x0 + v[32] * x1 + v[64] * x2;
-      a1 += v[96] * x0 + v[128] * x1 + v[160] * x2;
-      a2 += v[192] * x0 + v[224] * x1 + v[256] * x2;
-    }
-    const V3<T> zr = load3rw(zw, row), pr = load3rw(pold, row);
-    const T n0 = zr.x + tb * pr.x, n1 = zr.y + tb * pr.y, n2 = zr.z + tb * pr.z;
-    store3(pnew, row, n0, n1, n2);
-    store3(qw, row, a0, a1, a2);
-    pq += double(n0 * a0 + n1 * a1 + n2 * a2);
-  }
-  return pq;
-}
-
-// work vectors are node-padded (4 values per node) like the global CG's
-template <typename T>
-__global__ void __launch_bounds__(kBatchThreads) batched_pcg_kernel(
-    Bsr A, const T* __restrict__ val, const T* __restrict__ minv, const double* __restrict__ b, double* __restrict__ x_out,
-    const int32_t* __restrict__ node_off, const int32_t* __restrict__ cta_inst, const int32_t* __restrict__ cta_first,
-    const int32_t* __restrict__ cta_size, const uint8_t* __restrict__ active, T* xw, T* rw, T* zw, T* p0, T* p1, T* qw,
-    const double* __restrict__ rtol_inst, int max_iter, int32_t* __restrict__ iters_out,
-    double* __restrict__ relres_out, double* part, unsigned int* counters) {
-  __shared__ double sh[33];
-  __shared__ bool ok_sh;
+// Continues (or, on the first launch of a solve, starts) the PCG of every instance the launch's CTAs serve, for at
+// most `chunk` iterations.  flag per instance on return: 0 still running, 1 finished (r.r <= rtol^2 b.b or max_iter
+// reached), 2 breakdown (p.q not positive and finite; the current iterate stands), -1 a wait gave up.  x_out gets
+// the instance's correction when it finishes.
+template <typename T, bool REG>
+__global__ void __launch_bounds__(kBatchThreads, REG ? 2 : 3) batched_pcg_kernel(
+    Bsr A, const T* __restrict__ val, const T* __restrict__ minv, const double* __restrict__ b,
+    double* __restrict__ x_out, const int32_t* __restrict__ node_off, const int32_t* __restrict__ cta_inst,
+    const int32_t* __restrict__ cta_first, const int32_t* __restrict__ cta_size, T* xw, T* rw, T* zw, T* p0, T* p1,
+    T* qw, const double* __restrict__ rtol_inst, int max_iter, int chunk, int first_launch, double* st,
+    int32_t* its, int32_t* flag, double* __restrict__ relres_out, double* part, unsigned int* counters) {
+  __shared__ double sfull[2 * kBatchThreads];
+  __shared__ T s_alpha, s_tb;
+  __shared__ int s_state;
   const int inst = cta_inst[blockIdx.x];
   const int first = cta_first[blockIdx.x], size = cta_size[blockIdx.x], rank = blockIdx.x - first;
-  const int r0 = node_off[inst], r1 = node_off[inst + 1];
-  // this CTA's contiguous share of the instance's rows
-  const int nr = r1 - r0;
+  const int r0 = node_off[inst], nr = node_off[inst + 1] - r0;
   const int ra = r0 + (int)((int64_t)nr * rank / size), rb = r0 + (int)((int64_t)nr * (rank + 1) / size);
-  const bool lead = rank == 0 && threadIdx.x == 0;
   unsigned int* counter = counters + inst;
   unsigned int bars = 0;
-  if (!active[inst]) {
-    for (int i = 3 * ra + threadIdx.x; i < 3 * rb; i += blockDim.x) x_out[i] = 0.0;
-    if (lead) {
-      iters_out[inst] = 0;
-      relres_out[inst] = 0.0;
-    }
-    return;
-  }
-  // x = 0, r = b, z = M^{-1} r, p_old = 0 (so p_new = z on the first iteration)
-  double init[2] = {0.0, 0.0};  // r.z, r.r
-  for (int row = ra + threadIdx.x; row < rb; row += blockDim.x) {
-    T rv[3], zv[3];
-    for (int c = 0; c < 3; ++c) rv[c] = T(b[3 * row + c]);
-    const T* m = minv + 9 * (int64_t)row;
-    for (int a = 0; a < 3; ++a) zv[a] = m[3 * a] * rv[0] + m[3 * a + 1] * rv[1] + m[3 * a + 2] * rv[2];
-    store3(xw, row, T(0), T(0), T(0));
-    store3(rw, row, rv[0], rv[1], rv[2]);
-    store3(zw, row, zv[0], zv[1], zv[2]);
-    store3(p1, row, T(0), T(0), T(0));
-    for (int c = 0; c < 3; ++c) {
-      init[0] += double(rv[c] * zv[c]);
-      init[1] += double(rv[c]) * double(rv[c]);
-    }
-  }
-  bool ok = group_reduce<2>(init, part, first, size, 0, counter, (++bars) * size, sh, &ok_sh);
-  double rz = init[0];
-  const double bb = init[1];
-  const double tol2 = rtol_inst[inst] * rtol_inst[inst] * bb;
-  double rr = bb;
-  double beta = 0.0;
+  const int row = ra + (int)threadIdx.x;  // REG: the thread's row
+  const bool mine = row < rb;
+  V3<T> xr{}, rv{}, zr{}, pr{}, qr{};
+  T mv[9];
+  if (REG && mine) load_minv(minv, row, mv);
+  // thread 0 owns the FP64 scalars
+  double rz = 0.0, rr = 0.0, bb = 0.0, beta = 0.0, tol2 = 0.0;
   int it = 0;
-  while (ok && it < max_iter && rr > tol2) {
-    const T tb = T(beta);
+  if (first_launch) {  // x = 0, r = b, z = M^-1 r, p_old = 0 (so p_new = z on the first iteration)
+    T lrz = T(0);
+    double lrr = 0.0;
+    for (int rw_ = REG ? row : ra + (int)threadIdx.x; rw_ < rb; rw_ += REG ? rb : (int)blockDim.x) {
+      const V3<T> r_{T(b[3 * rw_]), T(b[3 * rw_ + 1]), T(b[3 * rw_ + 2])};
+      T m[9];
+      if (REG) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) m[k] = mv[k];
+      } else {
+        load_minv(minv, rw_, m);
+      }
+      const V3<T> z_ = jacobi(m, r_);
+      store3(zw, rw_, z_.x, z_.y, z_.z);
+      store3(p1, rw_, T(0), T(0), T(0));
+      if (REG) {
+        rv = r_, zr = z_;
+      } else {
+        store3(xw, rw_, T(0), T(0), T(0));
+        store3(rw, rw_, r_.x, r_.y, r_.z);
+      }
+      lrz += r_.x * z_.x + r_.y * z_.y + r_.z * z_.z;
+      lrr += double(r_.x) * double(r_.x) + double(r_.y) * double(r_.y) + double(r_.z) * double(r_.z);
+    }
+    double v[2] = {double(lrz), lrr};
+    const bool ok = group_sum<2>(v, sfull, part, first, size, 1, counter, (++bars) * size);
+    if (threadIdx.x == 0) {
+      rz = v[0], bb = v[1], rr = v[1];
+      s_state = ok ? 0 : -1;
+    }
+  } else {
+    if (threadIdx.x == 0) {
+      rz = st[4 * inst], rr = st[4 * inst + 1], bb = st[4 * inst + 2], beta = st[4 * inst + 3];
+      s_state = 0;
+    }
+    it = its[inst];
+    if (REG && mine) {
+      xr = load3rw(xw, row), rv = load3rw(rw, row), zr = load3rw(zw, row);
+      pr = load3rw((it & 1) ? p0 : p1, row);
+    }
+  }
+  if (threadIdx.x == 0) {
+    tol2 = rtol_inst[inst] * rtol_inst[inst] * bb;
+    if (s_state == 0 && !(rr > tol2)) s_state = 1;
+    if (s_state == 0 && it >= max_iter) s_state = 1;
+    s_tb = T(beta);
+  }
+  __syncthreads();
+  int state = s_state;
+  const bool l2 = size > 1;
+  for (int k = 0; state == 0 && k < chunk; ++k) {
+    const T tb = s_tb;
     const T* pold = (it & 1) ? p0 : p1;
     T* pnew = (it & 1) ? p1 : p0;
-    // q = K p_new on this CTA's rows (neighbour rows belong to the same instance)
-    double pq[1] = {0.0};
-    if (size > 1) pq[0] = spmv_rows<T, true>(A, val, zw, pold, pnew, qw, tb, ra, rb);
-    else pq[0] = spmv_rows<T, false>(A, val, zw, pold, pnew, qw, tb, ra, rb);
-    ok = group_reduce<1>(pq, part, first, size, 1, counter, (++bars) * size, sh, &ok_sh);
-    if (!ok) break;
-    if (!(fabs(pq[0]) > 0.0) || !isfinite(pq[0])) break;  // breakdown: leave with the current iterate
-    const T alpha = T(rz / pq[0]);
-    double upd[2] = {0.0, 0.0};  // r.z, r.r of the new residual
-    for (int row = ra + threadIdx.x; row < rb; row += blockDim.x) {
-      const V3<T> pv = load3rw(pnew, row), qv = load3rw(qw, row), xv = load3rw(xw, row), rv0 = load3rw(rw, row);
-      store3(xw, row, xv.x + alpha * pv.x, xv.y + alpha * pv.y, xv.z + alpha * pv.z);
-      const T r_[3] = {rv0.x - alpha * qv.x, rv0.y - alpha * qv.y, rv0.z - alpha * qv.z};
-      store3(rw, row, r_[0], r_[1], r_[2]);
-      const T* m = minv + 9 * (int64_t)row;
-      T zv[3];
-      for (int a = 0; a < 3; ++a) zv[a] = m[3 * a] * r_[0] + m[3 * a + 1] * r_[1] + m[3 * a + 2] * r_[2];
-      store3(zw, row, zv[0], zv[1], zv[2]);
-      for (int a = 0; a < 3; ++a) {
-        upd[0] += double(r_[a] * zv[a]);
-        upd[1] += double(r_[a]) * double(r_[a]);
+    T lpq = T(0);
+    if (REG) {
+      if (mine) {
+        qr = l2 ? row_product<T, true>(A, val, zw, pold, tb, row) : row_product<T, false>(A, val, zw, pold, tb, row);
+        pr = {zr.x + tb * pr.x, zr.y + tb * pr.y, zr.z + tb * pr.z};
+        store3(pnew, row, pr.x, pr.y, pr.z);
+        lpq = pr.x * qr.x + pr.y * qr.y + pr.z * qr.z;
+      }
+    } else {
+      for (int r_ = ra + (int)threadIdx.x; r_ < rb; r_ += blockDim.x) {
+        const V3<T> q_ = l2 ? row_product<T, true>(A, val, zw, pold, tb, r_)
+                            : row_product<T, false>(A, val, zw, pold, tb, r_);
+        const V3<T> z_ = load3rw(zw, r_), po = load3rw(pold, r_);
+        const V3<T> pn{z_.x + tb * po.x, z_.y + tb * po.y, z_.z + tb * po.z};
+        store3(pnew, r_, pn.x, pn.y, pn.z);
+        store3(qw, r_, q_.x, q_.y, q_.z);
+        lpq += pn.x * q_.x + pn.y * q_.y + pn.z * q_.z;
       }
     }
-    ok = group_reduce<2>(upd, part, first, size, 0, counter, (++bars) * size, sh, &ok_sh);
-    if (!ok) break;
-    beta = upd[0] / rz;
-    rz = upd[0];
-    rr = upd[1];
+    double v1[1] = {double(lpq)};
+    const bool ok1 = group_sum<1>(v1, sfull, part, first, size, 0, counter, (++bars) * size);
+    if (threadIdx.x == 0) {
+      if (!ok1) {
+        s_state = -1;
+      } else if (!(fabs(v1[0]) > 0.0) || !isfinite(v1[0])) {
+        s_state = 2;  // breakdown: leave with the current iterate
+      } else {
+        s_alpha = T(rz / v1[0]);
+      }
+    }
+    __syncthreads();
+    state = s_state;
+    if (state != 0) break;
+    const T alpha = s_alpha;
+    T lrz = T(0);
+    double lrr = 0.0;
+    if (REG) {
+      if (mine) {
+        xr = {xr.x + alpha * pr.x, xr.y + alpha * pr.y, xr.z + alpha * pr.z};
+        rv = {rv.x - alpha * qr.x, rv.y - alpha * qr.y, rv.z - alpha * qr.z};
+        zr = jacobi(mv, rv);
+        store3(zw, row, zr.x, zr.y, zr.z);
+        lrz = rv.x * zr.x + rv.y * zr.y + rv.z * zr.z;
+        lrr = double(rv.x) * double(rv.x) + double(rv.y) * double(rv.y) + double(rv.z) * double(rv.z);
+      }
+    } else {
+      for (int r_ = ra + (int)threadIdx.x; r_ < rb; r_ += blockDim.x) {
+        const V3<T> pv = load3rw(pnew, r_), qv = load3rw(qw, r_), xv = load3rw(xw, r_), r0v = load3rw(rw, r_);
+        store3(xw, r_, xv.x + alpha * pv.x, xv.y + alpha * pv.y, xv.z + alpha * pv.z);
+        const V3<T> r_n{r0v.x - alpha * qv.x, r0v.y - alpha * qv.y, r0v.z - alpha * qv.z};
+        store3(rw, r_, r_n.x, r_n.y, r_n.z);
+        T m[9];
+        load_minv(minv, r_, m);
+        const V3<T> z_ = jacobi(m, r_n);
+        store3(zw, r_, z_.x, z_.y, z_.z);
+        lrz += r_n.x * z_.x + r_n.y * z_.y + r_n.z * z_.z;
+        lrr += double(r_n.x) * double(r_n.x) + double(r_n.y) * double(r_n.y) + double(r_n.z) * double(r_n.z);
+      }
+    }
+    double v2[2] = {double(lrz), lrr};
+    const bool ok2 = group_sum<2>(v2, sfull, part, first, size, 1, counter, (++bars) * size);
     ++it;
+    if (threadIdx.x == 0) {
+      if (!ok2) {
+        s_state = -1;
+      } else {
+        beta = v2[0] / rz;
+        rz = v2[0];
+        rr = v2[1];
+        s_tb = T(beta);
+        if (!(rr > tol2) || it >= max_iter) s_state = 1;
+      }
+    }
+    __syncthreads();
+    state = s_state;
   }
-  for (int row = ra + threadIdx.x; row < rb; row += blockDim.x) {
-    const V3<T> xv = load3rw(xw, row);
-    x_out[3 * row] = double(xv.x), x_out[3 * row + 1] = double(xv.y), x_out[3 * row + 2] = double(xv.z);
+  if (state == -1) {  // a wait gave up: report it, leave the vectors as they are
+    if (rank == 0 && threadIdx.x == 0) flag[inst] = -1;
+    return;
   }
-  if (lead) {
-    iters_out[inst] = ok ? it : -1;
+  if (REG && mine && state == 0) {  // continued by the next launch
+    store3(xw, row, xr.x, xr.y, xr.z);
+    store3(rw, row, rv.x, rv.y, rv.z);
+  }
+  if (state != 0) {  // finished: the correction of the instance's rows
+    for (int r_ = ra + (int)threadIdx.x; r_ < rb; r_ += blockDim.x) {
+      const V3<T> xv = REG ? xr : load3rw(xw, r_);
+      x_out[3 * r_] = double(xv.x), x_out[3 * r_ + 1] = double(xv.y), x_out[3 * r_ + 2] = double(xv.z);
+    }
+  }
+  if (rank == 0 && threadIdx.x == 0) {
+    st[4 * inst] = rz, st[4 * inst + 1] = rr, st[4 * inst + 2] = bb, st[4 * inst + 3] = beta;
+    its[inst] = it;
+    flag[inst] = state;
     relres_out[inst] = bb > 0.0 ? sqrt(rr / bb) : 0.0;
   }
 }
@@ -211,7 +318,7 @@ __global__ void instance_norms_kernel(const double* __restrict__ x, const int32_
   const int inst = blockIdx.x;
   double s = 0.0;
   for (int i = 3 * node_off[inst] + threadIdx.x; i < 3 * node_off[inst + 1]; i += blockDim.x) s += x[i] * x[i];
-  s = cta_sum(s, sh);
+  s = block_sum_all(s, sh);
   if (threadIdx.x == 0) out[inst] = sqrt(s);
 }
 
@@ -233,39 +340,33 @@ void launch_instance_step(double* u, const double* u_old, const double* corr, in
   instance_step_kernel<<<n_inst, 256, 0, s>>>(u, u_old, corr, node_off, step);
 }
 
-int batched_pcg_capacity(bool fp32, int sms) {
+int batched_pcg_capacity(bool fp32, bool reg, int sms) {
   int b = 0;
-  if (fp32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_pcg_kernel<float>, kBatchThreads, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, batched_pcg_kernel<double>, kBatchThreads, 0);
+  const void* k = fp32 ? (reg ? (const void*)batched_pcg_kernel<float, true> : (const void*)batched_pcg_kernel<float, false>)
+                       : (reg ? (const void*)batched_pcg_kernel<double, true> : (const void*)batched_pcg_kernel<double, false>);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kBatchThreads, 0);
   return b * sms;
 }
 
-cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, const void* minv, const double* b, double* x_out, int n_cta,
-                               const int32_t* node_off, const int32_t* cta_inst, const int32_t* cta_first,
-                               const int32_t* cta_size, const uint8_t* active, void* xw, void* rw, void* zw, void* p0,
-                               void* p1, void* qw, const double* rtol, int max_iter, int32_t* iters, double* relres,
-                               double* part, unsigned int* counters, int n_inst, bool cooperative, cudaStream_t s) {
+int batched_pcg_threads() { return kBatchThreads; }
+
+cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, bool reg, const void* minv, const double* b, double* x_out,
+                               int n_cta, const int32_t* node_off, const int32_t* cta_inst, const int32_t* cta_first,
+                               const int32_t* cta_size, void* xw, void* rw, void* zw, void* p0, void* p1, void* qw,
+                               const double* rtol, int max_iter, int chunk, int first_launch, double* st, int32_t* its,
+                               int32_t* flag, double* relres, double* part, unsigned int* counters, int n_inst,
+                               bool cooperative, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(unsigned int) * n_inst, s);
   if (e != cudaSuccess) return e;
-  if (!cooperative) {  // every group is one CTA: no CTA waits on another, so an ordinary launch will do
-    if (fp32)
-      batched_pcg_kernel<float><<<n_cta, kBatchThreads, 0, s>>>(
-          A, (const float*)A.val, (const float*)minv, b, x_out, node_off, cta_inst, cta_first, cta_size, active,
-          (float*)xw, (float*)rw, (float*)zw, (float*)p0, (float*)p1, (float*)qw, rtol, max_iter, iters, relres, part,
-          counters);
-    else
-      batched_pcg_kernel<double><<<n_cta, kBatchThreads, 0, s>>>(
-          A, (const double*)A.val, (const double*)minv, b, x_out, node_off, cta_inst, cta_first, cta_size, active,
-          (double*)xw, (double*)rw, (double*)zw, (double*)p0, (double*)p1, (double*)qw, rtol, max_iter, iters,
-          relres, part, counters);
-    return cudaGetLastError();
-  }
   Bsr Acopy = A;
   const void* val = A.val;
-  void* args[] = {&Acopy, &val, &minv,  &b,      &x_out,    &node_off, &cta_inst, &cta_first,
-                  &cta_size, &active, &xw, &rw,   &zw,       &p0,       &p1,       &qw,
-                  &rtol,  &max_iter, &iters, &relres, &part, &counters};
-  const void* kern = fp32 ? (const void*)batched_pcg_kernel<float> : (const void*)batched_pcg_kernel<double>;
+  void* args[] = {&Acopy, &val,  &minv, &b,  &x_out, &node_off, &cta_inst, &cta_first, &cta_size,
+                  &xw,    &rw,   &zw,   &p0, &p1,    &qw,       &rtol,     &max_iter,  &chunk,
+                  &first_launch, &st, &its, &flag, &relres, &part, &counters};
+  const void* kern = fp32 ? (reg ? (const void*)batched_pcg_kernel<float, true> : (const void*)batched_pcg_kernel<float, false>)
+                          : (reg ? (const void*)batched_pcg_kernel<double, true> : (const void*)batched_pcg_kernel<double, false>);
+  // a group of one CTA waits on no other CTA: without multi-CTA groups an ordinary launch will do
+  if (!cooperative) return cudaLaunchKernel(kern, dim3(n_cta), dim3(kBatchThreads), args, 0, s);
   return cudaLaunchCooperativeKernel(kern, dim3(n_cta), dim3(kBatchThreads), args, 0, s);
 }
 

@@ -1230,55 +1230,119 @@ int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on) {
 namespace ikr_host {
 // Newton-Raphson over independent instances: every instance runs its own Newton iteration and relative
 // convergence test; one assembly and one batched CG launch (CTA per instance) serve all still-active instances.
-// CTA groups of the batched CG: instance i gets C_i CTAs, C_i ~ its node count, with every group's CTAs
-// co-resident (sum C_i <= the device's resident CTAs of the kernel) and at least 64 rows per CTA; largest
-// instances first.  When every C_i is 1 (or there are more instances than resident CTAs) the launch is an
-// ordinary one.
-static void build_batch_plan(ikr_nr nr, ikr_fes f, bool fp32) {
+// CTA groups of one batched CG launch over the instances in `run`: with one row per thread (REG) instance i gets
+// C_i = ceil(rows_i / threads) CTAs when all groups fit the co-resident CTAs of that variant; otherwise C_i ~ its
+// rows over the smallest rows-per-CTA q (>= 64 rows per CTA) whose groups fit the variant that loops over rows,
+// and when there are more instances than resident CTAs every group is one CTA (an ordinary launch; no CTA waits
+// on another).  Groups are at most 32 CTAs; largest instances first.
+static void plan_batch_launch(ikr_nr nr, ikr_fes f, bool fp32, const std::vector<int>& run) {
   auto& P = nr->plan;
-  if (P.fes == f && P.fp32 == fp32 && P.n_cta > 0) return;
-  const int ni = f->n_inst;
-  const int cap = ikr::batched_pcg_capacity(fp32, num_sms());
-  std::vector<int> nodes(ni), c(ni, 1), order(ni);
-  for (int i = 0; i < ni; ++i) nodes[i] = f->inst_off_h[i + 1] - f->inst_off_h[i], order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nodes[a] > nodes[b]; });
-  auto sizes_for = [&](int64_t q, std::vector<int>& out) {
-    int64_t tot = 0;
-    for (int i = 0; i < ni; ++i) {
-      int64_t ci = (nodes[i] + q - 1) / q;
-      ci = std::min<int64_t>(ci, std::max(1, nodes[i] / 64));
-      ci = std::max<int64_t>(1, std::min<int64_t>(ci, 32));
-      out[i] = (int)ci;
-      tot += ci;
+  const bool reg_allowed = P.rows_loop == 0;
+  const int sms = num_sms();
+  const int threads = ikr::batched_pcg_threads();
+  const int nr_ = (int)run.size();
+  std::vector<int> rows(nr_), c(nr_, 1), order(nr_);
+  for (int k = 0; k < nr_; ++k) rows[k] = f->inst_off_h[run[k] + 1] - f->inst_off_h[run[k]], order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rows[a] > rows[b]; });
+  bool reg = true;
+  int64_t tot = 0;
+  for (int k = 0; k < nr_; ++k) {
+    const int ck = (rows[k] + threads - 1) / threads;
+    reg = reg && ck <= 32;
+    c[k] = std::max(1, ck);
+    tot += c[k];
+  }
+  reg = reg && reg_allowed && tot <= ikr::batched_pcg_capacity(fp32, true, sms);
+  if (!reg) {
+    const int cap = ikr::batched_pcg_capacity(fp32, false, sms);
+    auto sizes_for = [&](int64_t q, std::vector<int>& out) {
+      int64_t t = 0;
+      for (int k = 0; k < nr_; ++k) {
+        int64_t ck = (rows[k] + q - 1) / q;
+        ck = std::min<int64_t>(ck, std::max(1, rows[k] / 64));
+        ck = std::max<int64_t>(1, std::min<int64_t>(ck, 32));
+        out[k] = (int)ck;
+        t += ck;
+      }
+      return t;
+    };
+    std::fill(c.begin(), c.end(), 1);
+    if (nr_ < cap) {
+      int64_t lo = 1, hi = *std::max_element(rows.begin(), rows.end()) + 1;
+      std::vector<int> tmp(nr_);
+      while (lo < hi) {  // smallest rows-per-CTA q whose groups fit the resident CTAs
+        const int64_t mid = (lo + hi) / 2;
+        if (sizes_for(mid, tmp) <= cap) hi = mid;
+        else lo = mid + 1;
+      }
+      sizes_for(lo, c);
     }
-    return tot;
-  };
-  if (ni < cap) {
-    int64_t lo = 1, hi = *std::max_element(nodes.begin(), nodes.end()) + 1;
-    std::vector<int> tmp(ni);
-    while (lo < hi) {  // smallest rows-per-CTA q whose groups fit the resident CTAs
-      const int64_t mid = (lo + hi) / 2;
-      if (sizes_for(mid, tmp) <= cap) hi = mid;
-      else lo = mid + 1;
-    }
-    sizes_for(lo, c);
   }
   std::vector<int32_t> ci, cf, cs;
-  for (int i : order) {
+  for (int k : order) {
     const int first = (int)ci.size();
-    for (int k = 0; k < c[i]; ++k) ci.push_back(i), cf.push_back(first), cs.push_back(c[i]);
+    for (int m = 0; m < c[k]; ++m) ci.push_back(run[k]), cf.push_back(first), cs.push_back(c[k]);
   }
-  P.fes = f;
-  P.fp32 = fp32;
-  P.n_cta = (int)ci.size();
-  P.cooperative = std::any_of(c.begin(), c.end(), [](int v) { return v > 1; });
   cudaStream_t s = f->stream;
-  P.cta_inst.upload(ci.data(), ci.size(), s);
-  P.cta_first.upload(cf.data(), cf.size(), s);
-  P.cta_size.upload(cs.data(), cs.size(), s);
-  P.part.alloc(4 * (size_t)P.n_cta);
+  P.n_cta = (int)ci.size();
+  P.reg = reg;
+  P.cooperative = std::any_of(c.begin(), c.end(), [](int v) { return v > 1; });
+  // the arrays keep their allocation across launches (a plan has at most max(instances, resident CTAs) entries)
+  const size_t cap = (size_t)std::max({f->n_inst, ikr::batched_pcg_capacity(fp32, true, sms),
+                                       ikr::batched_pcg_capacity(fp32, false, sms)});
+  for (auto* b : {&P.cta_inst, &P.cta_first, &P.cta_size})
+    if (b->n < cap) b->alloc(cap);
+  if (P.part.n < 4 * cap) P.part.alloc(4 * cap);
+  CK(cudaMemcpyAsync(P.cta_inst.p, ci.data(), sizeof(int32_t) * ci.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(P.cta_first.p, cf.data(), sizeof(int32_t) * cf.size(), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(P.cta_size.p, cs.data(), sizeof(int32_t) * cs.size(), cudaMemcpyHostToDevice, s));
+}
+
+// The batched CG of one Newton iteration: the instances with act set start their PCG on -R; the solve runs as a
+// sequence of launches of 128, 256, ... (at most 4096) iterations, each re-planned over the instances still
+// running, so that the hard instances that outlast the others get more CTAs and one row per thread.  Instances not
+// in the solve get a zero correction.  cgit: CG iterations per instance (0 for those not in the solve).
+static void batched_cg(ikr_nr nr, ikr_fes f, ikr_asm a, const std::vector<uint8_t>& act, std::vector<int32_t>& cgit) {
+  const int ni = f->n_inst;
+  cudaStream_t s = f->stream;
+  auto& P = nr->plan;
+  ikr::PcgWork& w = nr->ls->w;
+  const ikr_nr_settings& st = nr->st;
+  CK(cudaMemsetAsync(nr->corr.p, 0, sizeof(double) * a->n, s));
+  std::vector<int> run;
+  for (int i = 0; i < ni; ++i)
+    if (act[i]) run.push_back(i);
+  std::fill(cgit.begin(), cgit.end(), 0);
+  if (run.empty()) return;
+  P.st.alloc(4 * (size_t)ni);
+  P.flag.alloc(ni);
   P.counters.alloc(ni);
+  std::vector<int32_t> flag(ni), its(ni);
+  int chunk = std::max(1, P.first_chunk);
+  bool first = true;
+  while (!run.empty()) {
+    plan_batch_launch(nr, f, a->fp32, run);
+    CK(ikr::launch_batched_pcg(a->bsr(), a->fp32, P.reg, w.minv, nr->rhs.p, nr->corr.p, P.n_cta, f->inst_off.p,
+                               P.cta_inst.p, P.cta_first.p, P.cta_size.p, w.x, w.r, w.z, w.p0, w.p1, w.q,
+                               nr->inst_rtol.p, st.linear_max_iter, chunk, first ? 1 : 0, P.st.p,
+                               nr->inst_cg_iters.p, P.flag.p, nr->inst_cg_res.p, P.part.p, P.counters.p, ni,
+                               P.cooperative, s));
+    count(1);
+    ++P.launches;
+    first = false;
+    chunk = std::min(2 * chunk, std::max(chunk, 4096));
+    P.flag.download(flag.data(), ni, s);
+    CK(cudaStreamSynchronize(s));
+    std::vector<int> next;
+    for (int i : run) {
+      if (flag[i] < 0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the batched CG gave up (instance %d)", i);
+      if (flag[i] == 0) next.push_back(i);
+    }
+    run.swap(next);
+  }
+  nr->inst_cg_iters.download(its.data(), ni, s);
   CK(cudaStreamSynchronize(s));
+  for (int i = 0; i < ni; ++i) cgit[i] = act[i] ? its[i] : 0;
 }
 
 // Instances whose elements invert (det C <= 0, or a non-finite state) are taken out of the solve: their element status goes to a
@@ -1317,7 +1381,6 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   nr->rhs.alloc(n);
   nr->inst_norm.alloc(ni);
   nr->inst_rtol.alloc(ni);
-  nr->inst_active.alloc(ni);
   nr->inst_cg_iters.alloc(ni);
   nr->inst_cg_res.alloc(ni);
   std::vector<double> rn(ni), r0(ni), rprev(ni), thr(ni), eta(ni);
@@ -1375,20 +1438,9 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
       eta[i] = careful[i] ? std::min(e, st.linear_rtol_min) : e;
     }
     nr->inst_rtol.upload(eta.data(), ni, s);
-    nr->inst_active.upload(act.data(), ni, s);
     ikr::launch_scale64(nr->rhs.p, a->R.p, -1.0, n, s);
-    ikr::PcgWork& w = nr->ls->w;
-    build_batch_plan(nr, f, a->fp32);
-    const auto& P = nr->plan;
-    CK(ikr::launch_batched_pcg(a->bsr(), a->fp32, w.minv, nr->rhs.p, nr->corr.p, P.n_cta, f->inst_off.p,
-                               P.cta_inst.p, P.cta_first.p, P.cta_size.p, nr->inst_active.p, w.x, w.r, w.z, w.p0, w.p1,
-                               w.q, nr->inst_rtol.p, st.linear_max_iter, nr->inst_cg_iters.p, nr->inst_cg_res.p,
-                               P.part.p, P.counters.p, ni, P.cooperative, s));
-    count(3);
-    nr->inst_cg_iters.download(cgit.data(), ni, s);
-    CK(cudaStreamSynchronize(s));
-    for (int i = 0; i < ni; ++i)
-      if (cgit[i] < 0) fail(IKR_ERR_TIMEOUT, "a bounded wait in the batched CG gave up (instance %d)", i);
+    count(1);
+    batched_cg(nr, f, a, act, cgit);
     std::vector<uint8_t> failed_before(nr->inst_failed);
     if (st.max_backtracks > 0) {
       nr->u_old.alloc(n);
@@ -1652,6 +1704,19 @@ int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations) {
   return guarded([&] {
     need(nr && cg_iterations, IKR_ERR_ARG, "null argument");
     for (size_t i = 0; i < nr->inst_lin.size(); ++i) cg_iterations[i] = nr->inst_lin[i];
+  });
+}
+int ikr_newton_set_batched_cg(ikr_nr nr, int32_t rows_loop, int32_t first_chunk) {
+  return guarded([&] {
+    need(nr && first_chunk >= 0, IKR_ERR_ARG, "invalid argument");
+    nr->plan.rows_loop = rows_loop ? 1 : 0;
+    nr->plan.first_chunk = first_chunk ? first_chunk : 128;
+  });
+}
+int ikr_newton_batched_cg_launches(ikr_nr nr, int64_t* n) {
+  return guarded([&] {
+    need(nr && n, IKR_ERR_ARG, "null argument");
+    *n = nr->plan.launches;
   });
 }
 int ikr_newton_exclude_instances(ikr_nr nr, int32_t n, const uint8_t* mask) {

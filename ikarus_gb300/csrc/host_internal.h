@@ -1289,18 +1289,21 @@ struct ikr_nr_s {
   DBuf<double> u_old, alpha_old, inst_step;  // backtracking: state before the correction, per-instance steps
   int64_t backtracks = 0;                    // corrections halved since creation
   DBuf<double> inst_norm, inst_rtol;
-  DBuf<uint8_t> inst_active;
   DBuf<int32_t> inst_cg_iters;
   DBuf<double> inst_cg_res;
-  // CTA groups of the batched CG (kernels.h launch_batched_pcg), built for one element set and precision
+  // CTA groups of the batched CG (kernels.h launch_batched_pcg), re-planned before every launch over the running instances
   struct BatchPlan {
-    ikr_fes fes = nullptr;
-    bool fp32 = false;
     int n_cta = 0;
+    bool reg = false;
     bool cooperative = false;
     DBuf<int32_t> cta_inst, cta_first, cta_size;
     DBuf<double> part;
     DBuf<unsigned int> counters;
+    DBuf<double> st;             // rz, r.r, b.b, beta per instance between the launches of one solve
+    DBuf<int32_t> flag;          // per instance: 0 running, 1 finished, 2 breakdown, -1 a wait gave up
+    int64_t launches = 0;        // batched CG launches since creation
+    int rows_loop = 0;           // 1: always the variant that loops over rows (tests)
+    int first_chunk = 128;       // iterations of a solve's first launch (doubling for the next ones, at most 4096)
   } plan;
 };
 

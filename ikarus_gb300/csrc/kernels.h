@@ -291,16 +291,21 @@ cudaError_t launch_pcg_persistent2(const Bsr& A, PcgWork& w0, PcgWork& w1, int v
                                    double* part_b, cudaStream_t s);
 
 // batched.cu -- independent instances (disjoint contiguous node ranges) of one element set
-// one cooperative launch runs every active instance's block-Jacobi PCG; instance i is served by the CTAs
-// cta_first[i'] .. + cta_size - 1 listed per CTA (cta_inst, cta_first, cta_size; groups contiguous); inactive
-// instances get a zero correction; xw..qw are node-padded work vectors of the whole set; rtol per instance;
-// part holds 4 doubles per CTA, counters one per instance.  capacity = co-resident CTAs on the device.
-int batched_pcg_capacity(bool fp32, int sms);
-cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, const void* minv, const double* b, double* x_out, int n_cta,
-                               const int32_t* node_off, const int32_t* cta_inst, const int32_t* cta_first,
-                               const int32_t* cta_size, const uint8_t* active, void* xw, void* rw, void* zw, void* p0,
-                               void* p1, void* qw, const double* rtol, int max_iter, int32_t* iters, double* relres,
-                               double* part, unsigned int* counters, int n_inst, bool cooperative, cudaStream_t s);
+// One launch continues (first_launch: starts) the block-Jacobi PCG of the instances its CTAs serve, for at most
+// `chunk` iterations: instance i is served by the CTAs cta_first .. + cta_size - 1 listed per CTA (cta_inst,
+// cta_first, cta_size; groups contiguous).  reg: one row per thread (every group's rows per CTA <=
+// batched_pcg_threads()), the rows' state in registers.  xw..qw are node-padded work vectors of the whole set, rtol
+// per instance; st (4 doubles), its and flag per instance carry the solve between launches (flag 0 running,
+// 1 finished, 2 breakdown, -1 a wait gave up); x_out gets an instance's correction when it finishes.  part holds
+// 4 doubles per CTA, counters one per instance.  capacity = co-resident CTAs of the variant on the device.
+int batched_pcg_capacity(bool fp32, bool reg, int sms);
+int batched_pcg_threads();
+cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, bool reg, const void* minv, const double* b, double* x_out,
+                               int n_cta, const int32_t* node_off, const int32_t* cta_inst, const int32_t* cta_first,
+                               const int32_t* cta_size, void* xw, void* rw, void* zw, void* p0, void* p1, void* qw,
+                               const double* rtol, int max_iter, int chunk, int first_launch, double* st, int32_t* its,
+                               int32_t* flag, double* relres, double* part, unsigned int* counters, int n_inst,
+                               bool cooperative, cudaStream_t s);
 void launch_instance_norms(const double* x, int n_inst, const int32_t* node_off, double* out, cudaStream_t s);
 // u = u_old + step[i] corr on the dofs of instance i (instances with step 1 untouched)
 void launch_instance_step(double* u, const double* u_old, const double* corr, int n_inst, const int32_t* node_off,

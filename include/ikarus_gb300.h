@@ -479,6 +479,12 @@ int ikr_newton_exclude_instances(ikr_nr nr, int32_t n, const uint8_t* mask);
  * instance).  The batched solve notifies the solver's observers like the single-system one, with the largest
  * residual norm over the instances still in the solve. */
 int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations);
+/* batched solves (no reference counterpart): the CG of a Newton iteration runs as launches of first_chunk (0: 128),
+ * then twice as many iterations (at most 4096 unless first_chunk is larger), each re-planned over the instances
+ * still running; rows_loop = 1 keeps the variant that loops over rows even where one row per thread fits (both are
+ * for tests and tuning; the results agree to rounding).  batched_cg_launches: launches since creation. */
+int ikr_newton_set_batched_cg(ikr_nr nr, int32_t rows_loop, int32_t first_chunk);
+int ikr_newton_batched_cg_launches(ikr_nr nr, int64_t* n);
 
 /* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
 typedef struct ikr_control_state {   /* ControlRoutineState (controlroutinestate.hh:21-31) */

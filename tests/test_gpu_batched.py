@@ -133,3 +133,40 @@ def test_batched_solve_notifies_observers_and_counts_cg_iterations_per_instance(
     assert ended[-1][1] == pytest.approx(rn.max(), rel=0, abs=0)
     lin = nr.instance_linear_iterations()
     assert lin.sum() == info.linearIterations and (lin > 0).all()
+
+
+_CHUNK_REF = {}
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("rows_loop,first_chunk", [(False, 0), (True, 0), (False, 3), (True, 5), (False, 1)])
+def test_chunked_and_row_loop_cg_launches_match_the_oracle(ikr, precision, rows_loop, first_chunk, parity_log):
+    """The batched CG continues each instance's PCG across launches of a few iterations, re-planned over the
+    instances still running (first_chunk 1, 3, 5: every solve spans many launches, switching between the
+    one-row-per-thread and the row-loop variants as the running set shrinks); the converged displacements match
+    the oracle's solves as the single-launch runs do (FP64 1e-8 at ||R|| <= 1e-9 ||R0||; mixed 1e-8 at 1e-8)."""
+    bp = problems.batched_cantilevers(n=7, seed=11, nx=(3, 9), nyz=(1, 3), E=(1e3, 1e4), t=(0.1, 0.5), load_steps=3)
+    fes, asm = problems.build_gpu_batched(bp, precision=precision)
+    req = ikr.FERequirements(fes)
+    if precision == 0:
+        st = ikr.NRSettings(tol=1e-9, maxIter=30, relative=True, linear_rtol=1e-12)
+    else:
+        st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                            linear_rtol_min=1e-6)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    nr.set_batched_cg(rows_loop=rows_loop, first_chunk=first_chunk)
+    info = ikr.LoadControl(nr, bp.load_steps).run(req)
+    assert info.success
+    _, _, conv = nr.instance_info()
+    assert (conv == 1).all()
+    if first_chunk:
+        assert nr.batched_cg_launches() > info.totalIterations
+    if "u" not in _CHUNK_REF:
+        _CHUNK_REF["u"] = [oracle.from_problem(part).load_control(bp.load_steps, tol=1e-9, tol_mode=1,
+                                                                   max_iter=30)["u"] for part in bp.parts]
+    u = req.globalSolution()
+    worst = max(np.abs(u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]] - ref).max() / np.abs(ref).max()
+                for i, ref in enumerate(_CHUNK_REF["u"]))
+    form = "FP64" if precision == 0 else "mixed"
+    assert parity_log(f"batched {form}, rows_loop={rows_loop}, first_chunk={first_chunk}: max rel. error vs oracle",
+                      worst, 1e-8)
