@@ -54,7 +54,7 @@ def parse():
                     help="mixed form's Newton predictor: 0 none (the reference's), 1 previous increment (the learned "
                          "predictor's fallback; this single load case has no trained model), 3 second-order "
                          "extrapolation with the previous increment as fallback")
-    ap.add_argument("--coarse", type=int, default=32,
+    ap.add_argument("--coarse", type=int, default=16,
                     help="slabs of the CG's coarse correction for the extra two-level measurement beside the "
                          "headline (0: skip it)")
     ap.add_argument("--tangent-kernel", type=int, default=0, choices=[0, 1, 2, 3],

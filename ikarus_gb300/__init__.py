@@ -1252,10 +1252,11 @@ class NewtonRaphson:
         _err(lib().ikr_newton_instance_linear_iterations(self.h, _ptr(out, C.c_int64)))
         return out
 
-    def set_batched_cg(self, rows_loop=False, first_chunk=0):
+    def set_batched_cg(self, variant=-1, first_chunk=0):
         """Batched solves: the CG runs as launches of first_chunk (0: 128), then doubling, iterations, re-planned
-        over the instances still running; rows_loop keeps the variant that loops over rows (tests, tuning)."""
-        _err(lib().ikr_newton_set_batched_cg(self.h, int(bool(rows_loop)), int(first_chunk)))
+        over the instances still running; variant -1 lets the planner choose per launch, 0 row loop, 1 one row per
+        thread, 2 / 3 four / eight threads per row with the matrix in shared memory (where it fits, else 0)."""
+        _err(lib().ikr_newton_set_batched_cg(self.h, int(variant), int(first_chunk)))
 
     def batched_cg_launches(self):
         n = C.c_int64()

@@ -96,7 +96,8 @@ __device__ __forceinline__ void load_minv(const T* __restrict__ minv, int row, T
 // Group-wide sums of N values: the CTA sum (warp 0 adds the threads' values in order), then, for a group of several
 // CTAs, thread 0 publishes it (part: 2 slots x 2 values per CTA; the reductions of an iteration alternate slots, so a
 // CTA that runs ahead never overwrites a sum another CTA has still to read), arrives with release semantics and polls
-// (bounded) with acquire semantics; lane b < size of warp 0 loads CTA first + b's sum and the butterfly adds them.
+// (bounded) with acquire semantics; lanes of warp 0 load the group's sums (at most 128 CTAs) in a fixed assignment
+// and the butterfly adds them.
 // The sums are valid in warp 0; false (in warp 0) when the wait gave up.
 template <int N>
 __device__ __forceinline__ bool group_sum(double (&v)[N], double* sfull, double* part, int first, int size, int slot,
@@ -123,11 +124,14 @@ __device__ __forceinline__ bool group_sum(double (&v)[N], double* sfull, double*
   __syncwarp();
   ok = __shfl_sync(0xffffffffu, ok, 0);
   if (!ok) return false;
+  double t[4][N];  // lane b adds the sums of CTAs b, b + 32, b + 64, b + 96 (groups of at most 128), loads in flight
 #pragma unroll
-  for (int k = 0; k < N; ++k) {
-    const double t = lane < size ? __ldcg(part + ((size_t)(first + lane) * 2 + slot) * 2 + k) : 0.0;
-    v[k] = warp_sum(t);
-  }
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      t[u][k] = lane + 32 * u < size ? __ldcg(part + ((size_t)(first + lane + 32 * u) * 2 + slot) * 2 + k) : 0.0;
+#pragma unroll
+  for (int k = 0; k < N; ++k) v[k] = warp_sum((t[0][k] + t[1][k]) + (t[2][k] + t[3][k]));
   return true;
 }
 
@@ -311,6 +315,201 @@ __global__ void __launch_bounds__(kBatchThreads, REG ? 2 : 3) batched_pcg_kernel
   }
 }
 
+// The same PCG for groups whose CTAs hold few rows: TPR threads share a row (thread j of the row takes the row's
+// blocks j, j + TPR, ...; the partial products are added by shuffles), and every thread copies its blocks and their
+// columns into shared memory once per launch, so an iteration reads the matrix from shared memory and issues all of a
+// thread's neighbour gathers at once (one L2 round trip).  Thread 0 of a row keeps the row's x, r, z, p and
+// block-Jacobi inverse in registers.  Rows per CTA: kBatchThreads / TPR.  A row's slice may have at most TPR * kU
+// blocks (the host checks).
+template <typename T, int TPR>
+struct SmemCfg {
+  static constexpr int kRows = kBatchThreads / TPR;
+  static constexpr int kU = (27 + TPR - 1) / TPR;  // blocks per thread: a hex node couples to at most 27 nodes
+  static constexpr int kValBytes = 9 * kU * kBatchThreads * (int)sizeof(T);
+  static constexpr int kBytes = kValBytes + kU * kBatchThreads * 4;
+};
+
+template <typename T, int TPR>
+__global__ void __launch_bounds__(kBatchThreads, 2) batched_pcg_smem_kernel(
+    Bsr A, const T* __restrict__ val, const T* __restrict__ minv, const double* __restrict__ b,
+    double* __restrict__ x_out, const int32_t* __restrict__ node_off, const int32_t* __restrict__ cta_inst,
+    const int32_t* __restrict__ cta_first, const int32_t* __restrict__ cta_size, T* xw, T* rw, T* zw, T* p0, T* p1,
+    T* qw, const double* __restrict__ rtol_inst, int max_iter, int chunk, int first_launch, double* st,
+    int32_t* its, int32_t* flag, double* __restrict__ relres_out, double* part, unsigned int* counters) {
+  using C = SmemCfg<T, TPR>;
+  constexpr int kU = C::kU;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  T* sval = reinterpret_cast<T*>(dsm);                       // [9][kU][threads]
+  int32_t* scol = reinterpret_cast<int32_t*>(dsm + C::kValBytes);  // [kU][threads], -1: no block
+  __shared__ double sfull[2 * kBatchThreads];
+  __shared__ T s_alpha, s_tb;
+  __shared__ int s_state;
+  const int inst = cta_inst[blockIdx.x];
+  const int first = cta_first[blockIdx.x], size = cta_size[blockIdx.x], rank = blockIdx.x - first;
+  const int r0 = node_off[inst], nr = node_off[inst + 1] - r0;
+  const int ra = r0 + (int)((int64_t)nr * rank / size), rb = r0 + (int)((int64_t)nr * (rank + 1) / size);
+  unsigned int* counter = counters + inst;
+  unsigned int bars = 0;
+  const int tid = threadIdx.x, j = tid % TPR;
+  const int row = ra + tid / TPR;
+  const bool mine = row < rb, lead = mine && j == 0;
+  // this thread's blocks of its row: slice entries j, j + TPR, ... below the slice width
+  {
+    const int s = mine ? row >> 5 : 0, l = row & 31;
+    const int gs = mine ? __ldg(A.slice_off + s) : 0, w = mine ? __ldg(A.slice_off + s + 1) - gs : 0;
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = j + TPR * u;
+      const bool has = e < w;
+      scol[u * kBatchThreads + tid] = has ? __ldg(A.col_sell + 32 * (gs + e) + l) : -1;
+#pragma unroll
+      for (int k = 0; k < 9; ++k)
+        sval[(k * kU + u) * kBatchThreads + tid] = has ? __ldg(val + (int64_t)(gs + e) * 288 + l + 32 * k) : T(0);
+    }
+  }
+  V3<T> xr{}, rv{}, zr{}, pr{};
+  T mv[9];
+  if (lead) load_minv(minv, row, mv);
+  double rz = 0.0, rr = 0.0, bb = 0.0, beta = 0.0, tol2 = 0.0;  // thread 0's
+  int it = 0;
+  if (first_launch) {
+    T lrz = T(0);
+    double lrr = 0.0;
+    if (lead) {
+      rv = {T(b[3 * row]), T(b[3 * row + 1]), T(b[3 * row + 2])};
+      zr = jacobi(mv, rv);
+      store3(zw, row, zr.x, zr.y, zr.z);
+      store3(p1, row, T(0), T(0), T(0));
+      lrz = rv.x * zr.x + rv.y * zr.y + rv.z * zr.z;
+      lrr = double(rv.x) * double(rv.x) + double(rv.y) * double(rv.y) + double(rv.z) * double(rv.z);
+    }
+    double v[2] = {double(lrz), lrr};
+    const bool ok = group_sum<2>(v, sfull, part, first, size, 1, counter, (++bars) * size);
+    if (tid == 0) {
+      rz = v[0], bb = v[1], rr = v[1];
+      s_state = ok ? 0 : -1;
+    }
+  } else {
+    if (tid == 0) {
+      rz = st[4 * inst], rr = st[4 * inst + 1], bb = st[4 * inst + 2], beta = st[4 * inst + 3];
+      s_state = 0;
+    }
+    it = its[inst];
+    if (lead) {
+      xr = load3rw(xw, row), rv = load3rw(rw, row), zr = load3rw(zw, row);
+      pr = load3rw((it & 1) ? p0 : p1, row);
+    }
+  }
+  if (tid == 0) {
+    tol2 = rtol_inst[inst] * rtol_inst[inst] * bb;
+    if (s_state == 0 && !(rr > tol2)) s_state = 1;
+    if (s_state == 0 && it >= max_iter) s_state = 1;
+    s_tb = T(beta);
+  }
+  __syncthreads();
+  int state = s_state;
+  const bool l2 = size > 1;
+  for (int k = 0; state == 0 && k < chunk; ++k) {
+    const T tb = s_tb;
+    const T* pold = (it & 1) ? p0 : p1;
+    T* pnew = (it & 1) ? p1 : p0;
+    T a0 = T(0), a1 = T(0), a2 = T(0);
+    {
+      int c[kU];
+      V3<T> zv[kU], pv[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) c[u] = scol[u * kBatchThreads + tid];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        if (c[u] >= 0) {
+          zv[u] = l2 ? gather3<true>(zw, c[u]) : gather3<false>(zw, c[u]);
+          pv[u] = l2 ? gather3<true>(pold, c[u]) : gather3<false>(pold, c[u]);
+        } else {
+          zv[u] = {T(0), T(0), T(0)};
+          pv[u] = zv[u];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const T x0 = zv[u].x + tb * pv[u].x, x1 = zv[u].y + tb * pv[u].y, x2 = zv[u].z + tb * pv[u].z;
+        const T* m = sval + u * kBatchThreads + tid;
+        constexpr int P = kU * kBatchThreads;
+        a0 += m[0] * x0 + m[P] * x1 + m[2 * P] * x2;
+        a1 += m[3 * P] * x0 + m[4 * P] * x1 + m[5 * P] * x2;
+        a2 += m[6 * P] * x0 + m[7 * P] * x1 + m[8 * P] * x2;
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < TPR; o <<= 1) {
+      a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+      a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+      a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    T lpq = T(0);
+    if (lead) {
+      pr = {zr.x + tb * pr.x, zr.y + tb * pr.y, zr.z + tb * pr.z};
+      store3(pnew, row, pr.x, pr.y, pr.z);
+      lpq = pr.x * a0 + pr.y * a1 + pr.z * a2;
+    }
+    double v1[1] = {double(lpq)};
+    const bool ok1 = group_sum<1>(v1, sfull, part, first, size, 0, counter, (++bars) * size);
+    if (tid == 0) {
+      if (!ok1) {
+        s_state = -1;
+      } else if (!(fabs(v1[0]) > 0.0) || !isfinite(v1[0])) {
+        s_state = 2;
+      } else {
+        s_alpha = T(rz / v1[0]);
+      }
+    }
+    __syncthreads();
+    state = s_state;
+    if (state != 0) break;
+    const T alpha = s_alpha;
+    T lrz = T(0);
+    double lrr = 0.0;
+    if (lead) {
+      xr = {xr.x + alpha * pr.x, xr.y + alpha * pr.y, xr.z + alpha * pr.z};
+      rv = {rv.x - alpha * a0, rv.y - alpha * a1, rv.z - alpha * a2};
+      zr = jacobi(mv, rv);
+      store3(zw, row, zr.x, zr.y, zr.z);
+      lrz = rv.x * zr.x + rv.y * zr.y + rv.z * zr.z;
+      lrr = double(rv.x) * double(rv.x) + double(rv.y) * double(rv.y) + double(rv.z) * double(rv.z);
+    }
+    double v2[2] = {double(lrz), lrr};
+    const bool ok2 = group_sum<2>(v2, sfull, part, first, size, 1, counter, (++bars) * size);
+    ++it;
+    if (tid == 0) {
+      if (!ok2) {
+        s_state = -1;
+      } else {
+        beta = v2[0] / rz;
+        rz = v2[0];
+        rr = v2[1];
+        s_tb = T(beta);
+        if (!(rr > tol2) || it >= max_iter) s_state = 1;
+      }
+    }
+    __syncthreads();
+    state = s_state;
+  }
+  if (state == -1) {
+    if (rank == 0 && tid == 0) flag[inst] = -1;
+    return;
+  }
+  if (lead && state == 0) {
+    store3(xw, row, xr.x, xr.y, xr.z);
+    store3(rw, row, rv.x, rv.y, rv.z);
+  }
+  if (lead && state != 0) x_out[3 * row] = double(xr.x), x_out[3 * row + 1] = double(xr.y), x_out[3 * row + 2] = double(xr.z);
+  if (rank == 0 && tid == 0) {
+    st[4 * inst] = rz, st[4 * inst + 1] = rr, st[4 * inst + 2] = bb, st[4 * inst + 3] = beta;
+    its[inst] = it;
+    flag[inst] = state;
+    relres_out[inst] = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+  }
+}
+
 // per-instance sum of squares over dof ranges [3 node_off[i], 3 node_off[i+1]); one block per instance
 __global__ void instance_norms_kernel(const double* __restrict__ x, const int32_t* __restrict__ node_off,
                                       double* __restrict__ out) {
@@ -340,17 +539,48 @@ void launch_instance_step(double* u, const double* u_old, const double* corr, in
   instance_step_kernel<<<n_inst, 256, 0, s>>>(u, u_old, corr, node_off, step);
 }
 
-int batched_pcg_capacity(bool fp32, bool reg, int sms) {
+// variants: 0 rows loop (state in the work arrays), 1 one row per thread (state in registers), 2 / 3 four / eight
+// threads per row with the matrix in shared memory
+static const void* batched_kernel(bool fp32, int variant) {
+  if (fp32) {
+    switch (variant) {
+      case 0: return (const void*)batched_pcg_kernel<float, false>;
+      case 1: return (const void*)batched_pcg_kernel<float, true>;
+      case 2: return (const void*)batched_pcg_smem_kernel<float, 4>;
+      default: return (const void*)batched_pcg_smem_kernel<float, 8>;
+    }
+  }
+  switch (variant) {
+    case 0: return (const void*)batched_pcg_kernel<double, false>;
+    case 1: return (const void*)batched_pcg_kernel<double, true>;
+    case 2: return (const void*)batched_pcg_smem_kernel<double, 4>;
+    default: return (const void*)batched_pcg_smem_kernel<double, 8>;
+  }
+}
+
+static int batched_smem_bytes(bool fp32, int variant) {
+  if (variant < 2) return 0;
+  if (fp32) return variant == 2 ? SmemCfg<float, 4>::kBytes : SmemCfg<float, 8>::kBytes;
+  return variant == 2 ? SmemCfg<double, 4>::kBytes : SmemCfg<double, 8>::kBytes;
+}
+
+int batched_pcg_capacity(bool fp32, int variant, int sms) {
+  const void* k = batched_kernel(fp32, variant);
+  const int smem = batched_smem_bytes(fp32, variant);
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return 0;
   int b = 0;
-  const void* k = fp32 ? (reg ? (const void*)batched_pcg_kernel<float, true> : (const void*)batched_pcg_kernel<float, false>)
-                       : (reg ? (const void*)batched_pcg_kernel<double, true> : (const void*)batched_pcg_kernel<double, false>);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kBatchThreads, 0);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kBatchThreads, smem) != cudaSuccess) return 0;
   return b * sms;
 }
 
 int batched_pcg_threads() { return kBatchThreads; }
+int batched_pcg_rows_per_cta(int variant) { return variant == 2 ? kBatchThreads / 4 : (variant == 3 ? kBatchThreads / 8 : kBatchThreads); }
+int batched_pcg_max_width(int variant) {
+  return variant == 2 ? 4 * SmemCfg<float, 4>::kU : (variant == 3 ? 8 * SmemCfg<float, 8>::kU : 1 << 30);
+}
 
-cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, bool reg, const void* minv, const double* b, double* x_out,
+cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, int variant, const void* minv, const double* b, double* x_out,
                                int n_cta, const int32_t* node_off, const int32_t* cta_inst, const int32_t* cta_first,
                                const int32_t* cta_size, void* xw, void* rw, void* zw, void* p0, void* p1, void* qw,
                                const double* rtol, int max_iter, int chunk, int first_launch, double* st, int32_t* its,
@@ -363,11 +593,15 @@ cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, bool reg, const void* mi
   void* args[] = {&Acopy, &val,  &minv, &b,  &x_out, &node_off, &cta_inst, &cta_first, &cta_size,
                   &xw,    &rw,   &zw,   &p0, &p1,    &qw,       &rtol,     &max_iter,  &chunk,
                   &first_launch, &st, &its, &flag, &relres, &part, &counters};
-  const void* kern = fp32 ? (reg ? (const void*)batched_pcg_kernel<float, true> : (const void*)batched_pcg_kernel<float, false>)
-                          : (reg ? (const void*)batched_pcg_kernel<double, true> : (const void*)batched_pcg_kernel<double, false>);
+  const void* kern = batched_kernel(fp32, variant);
+  const int smem = batched_smem_bytes(fp32, variant);
+  if (smem > 48 * 1024) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+  }
   // a group of one CTA waits on no other CTA: without multi-CTA groups an ordinary launch will do
-  if (!cooperative) return cudaLaunchKernel(kern, dim3(n_cta), dim3(kBatchThreads), args, 0, s);
-  return cudaLaunchCooperativeKernel(kern, dim3(n_cta), dim3(kBatchThreads), args, 0, s);
+  if (!cooperative) return cudaLaunchKernel(kern, dim3(n_cta), dim3(kBatchThreads), args, smem, s);
+  return cudaLaunchCooperativeKernel(kern, dim3(n_cta), dim3(kBatchThreads), args, smem, s);
 }
 
 void launch_instance_norms(const double* x, int n_inst, const int32_t* node_off, double* out, cudaStream_t s) {

@@ -1230,31 +1230,47 @@ int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on) {
 namespace ikr_host {
 // Newton-Raphson over independent instances: every instance runs its own Newton iteration and relative
 // convergence test; one assembly and one batched CG launch (CTA per instance) serve all still-active instances.
-// CTA groups of one batched CG launch over the instances in `run`: with one row per thread (REG) instance i gets
-// C_i = ceil(rows_i / threads) CTAs when all groups fit the co-resident CTAs of that variant; otherwise C_i ~ its
-// rows over the smallest rows-per-CTA q (>= 64 rows per CTA) whose groups fit the variant that loops over rows,
-// and when there are more instances than resident CTAs every group is one CTA (an ordinary launch; no CTA waits
-// on another).  Groups are at most 32 CTAs; largest instances first.
-static void plan_batch_launch(ikr_nr nr, ikr_fes f, bool fp32, const std::vector<int>& run) {
+// CTA groups of one batched CG launch over the instances in `run`.  The variants with few rows per CTA go first, as
+// their iterations are the shortest: eight, then four threads per row with the matrix in shared memory, then one row
+// per thread (instance i gets C_i = ceil(rows_i / rows per CTA) CTAs) -- the first whose groups fit the co-resident
+// CTAs of that variant (and at most 128 CTAs per group, rows of at most the variant's blocks).  Otherwise C_i ~ its
+// rows over the smallest rows-per-CTA q (>= 64 rows per CTA) whose groups fit the variant that loops over rows, and
+// when there are more instances than resident CTAs every group is one CTA (an ordinary launch; no CTA waits on
+// another).  Largest instances first.
+static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const std::vector<int>& run) {
   auto& P = nr->plan;
-  const bool reg_allowed = P.rows_loop == 0;
   const int sms = num_sms();
-  const int threads = ikr::batched_pcg_threads();
   const int nr_ = (int)run.size();
-  std::vector<int> rows(nr_), c(nr_, 1), order(nr_);
-  for (int k = 0; k < nr_; ++k) rows[k] = f->inst_off_h[run[k] + 1] - f->inst_off_h[run[k]], order[k] = k;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return rows[a] > rows[b]; });
-  bool reg = true;
-  int64_t tot = 0;
+  std::vector<int> rows(nr_), width(nr_, 0), c(nr_, 1), order(nr_);
   for (int k = 0; k < nr_; ++k) {
-    const int ck = (rows[k] + threads - 1) / threads;
-    reg = reg && ck <= 32;
-    c[k] = std::max(1, ck);
-    tot += c[k];
+    const int r0 = f->inst_off_h[run[k]], r1 = f->inst_off_h[run[k] + 1];
+    rows[k] = r1 - r0, order[k] = k;
+    for (int sl = r0 >> 5; r1 > r0 && sl <= (r1 - 1) >> 5; ++sl)
+      width[k] = std::max(width[k], a->slice_off_h[sl + 1] - a->slice_off_h[sl]);
   }
-  reg = reg && reg_allowed && tot <= ikr::batched_pcg_capacity(fp32, true, sms);
-  if (!reg) {
-    const int cap = ikr::batched_pcg_capacity(fp32, false, sms);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rows[x] > rows[y]; });
+  std::vector<int> cand;
+  if (P.variant >= 0) cand.push_back(P.variant);
+  else cand = {3, 2, 1};
+  int variant = 0;
+  for (int v : cand) {
+    if (v == 0) break;
+    const int rpc = ikr::batched_pcg_rows_per_cta(v), maxw = ikr::batched_pcg_max_width(v);
+    bool fits = true;
+    int64_t tot = 0;
+    for (int k = 0; k < nr_ && fits; ++k) {
+      const int ck = std::max(1, (rows[k] + rpc - 1) / rpc);
+      fits = ck <= 128 && width[k] <= maxw;
+      c[k] = ck;
+      tot += ck;
+    }
+    if (fits && tot <= ikr::batched_pcg_capacity(fp32, v, sms)) {
+      variant = v;
+      break;
+    }
+  }
+  if (variant == 0) {
+    const int cap = ikr::batched_pcg_capacity(fp32, 0, sms);
     auto sizes_for = [&](int64_t q, std::vector<int>& out) {
       int64_t t = 0;
       for (int k = 0; k < nr_; ++k) {
@@ -1285,11 +1301,11 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, bool fp32, const std::vector
   }
   cudaStream_t s = f->stream;
   P.n_cta = (int)ci.size();
-  P.reg = reg;
+  P.cur_variant = variant;
   P.cooperative = std::any_of(c.begin(), c.end(), [](int v) { return v > 1; });
   // the arrays keep their allocation across launches (a plan has at most max(instances, resident CTAs) entries)
-  const size_t cap = (size_t)std::max({f->n_inst, ikr::batched_pcg_capacity(fp32, true, sms),
-                                       ikr::batched_pcg_capacity(fp32, false, sms)});
+  size_t cap = (size_t)f->n_inst;
+  for (int v = 0; v < 4; ++v) cap = std::max(cap, (size_t)ikr::batched_pcg_capacity(fp32, v, sms));
   for (auto* b : {&P.cta_inst, &P.cta_first, &P.cta_size})
     if (b->n < cap) b->alloc(cap);
   if (P.part.n < 4 * cap) P.part.alloc(4 * cap);
@@ -1321,8 +1337,8 @@ static void batched_cg(ikr_nr nr, ikr_fes f, ikr_asm a, const std::vector<uint8_
   int chunk = std::max(1, P.first_chunk);
   bool first = true;
   while (!run.empty()) {
-    plan_batch_launch(nr, f, a->fp32, run);
-    CK(ikr::launch_batched_pcg(a->bsr(), a->fp32, P.reg, w.minv, nr->rhs.p, nr->corr.p, P.n_cta, f->inst_off.p,
+    plan_batch_launch(nr, f, a, a->fp32, run);
+    CK(ikr::launch_batched_pcg(a->bsr(), a->fp32, P.cur_variant, w.minv, nr->rhs.p, nr->corr.p, P.n_cta, f->inst_off.p,
                                P.cta_inst.p, P.cta_first.p, P.cta_size.p, w.x, w.r, w.z, w.p0, w.p1, w.q,
                                nr->inst_rtol.p, st.linear_max_iter, chunk, first ? 1 : 0, P.st.p,
                                nr->inst_cg_iters.p, P.flag.p, nr->inst_cg_res.p, P.part.p, P.counters.p, ni,
@@ -1706,10 +1722,10 @@ int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations) {
     for (size_t i = 0; i < nr->inst_lin.size(); ++i) cg_iterations[i] = nr->inst_lin[i];
   });
 }
-int ikr_newton_set_batched_cg(ikr_nr nr, int32_t rows_loop, int32_t first_chunk) {
+int ikr_newton_set_batched_cg(ikr_nr nr, int32_t variant, int32_t first_chunk) {
   return guarded([&] {
-    need(nr && first_chunk >= 0, IKR_ERR_ARG, "invalid argument");
-    nr->plan.rows_loop = rows_loop ? 1 : 0;
+    need(nr && first_chunk >= 0 && variant >= -1 && variant <= 3, IKR_ERR_ARG, "invalid argument");
+    nr->plan.variant = variant;
     nr->plan.first_chunk = first_chunk ? first_chunk : 128;
   });
 }

@@ -293,14 +293,18 @@ cudaError_t launch_pcg_persistent2(const Bsr& A, PcgWork& w0, PcgWork& w1, int v
 // batched.cu -- independent instances (disjoint contiguous node ranges) of one element set
 // One launch continues (first_launch: starts) the block-Jacobi PCG of the instances its CTAs serve, for at most
 // `chunk` iterations: instance i is served by the CTAs cta_first .. + cta_size - 1 listed per CTA (cta_inst,
-// cta_first, cta_size; groups contiguous).  reg: one row per thread (every group's rows per CTA <=
-// batched_pcg_threads()), the rows' state in registers.  xw..qw are node-padded work vectors of the whole set, rtol
-// per instance; st (4 doubles), its and flag per instance carry the solve between launches (flag 0 running,
-// 1 finished, 2 breakdown, -1 a wait gave up); x_out gets an instance's correction when it finishes.  part holds
-// 4 doubles per CTA, counters one per instance.  capacity = co-resident CTAs of the variant on the device.
-int batched_pcg_capacity(bool fp32, bool reg, int sms);
+// cta_first, cta_size; groups contiguous, at most 128 CTAs).  variant 0: a thread loops over rows with the state in
+// the work arrays; 1: one row per thread (rows per CTA <= batched_pcg_rows_per_cta), the row's state in registers;
+// 2 / 3: four / eight threads per row, the CTA's matrix blocks in shared memory (rows per CTA <=
+// batched_pcg_rows_per_cta, blocks per row <= batched_pcg_max_width).  xw..qw are node-padded work vectors of the
+// whole set, rtol per instance; st (4 doubles), its and flag per instance carry the solve between launches (flag 0
+// running, 1 finished, 2 breakdown, -1 a wait gave up); x_out gets an instance's correction when it finishes.  part
+// holds 4 doubles per CTA, counters one per instance.  capacity = co-resident CTAs of the variant on the device.
+int batched_pcg_capacity(bool fp32, int variant, int sms);
 int batched_pcg_threads();
-cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, bool reg, const void* minv, const double* b, double* x_out,
+int batched_pcg_rows_per_cta(int variant);
+int batched_pcg_max_width(int variant);
+cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, int variant, const void* minv, const double* b, double* x_out,
                                int n_cta, const int32_t* node_off, const int32_t* cta_inst, const int32_t* cta_first,
                                const int32_t* cta_size, void* xw, void* rw, void* zw, void* p0, void* p1, void* qw,
                                const double* rtol, int max_iter, int chunk, int first_launch, double* st, int32_t* its,

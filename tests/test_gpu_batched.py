@@ -139,12 +139,14 @@ _CHUNK_REF = {}
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-@pytest.mark.parametrize("rows_loop,first_chunk", [(False, 0), (True, 0), (False, 3), (True, 5), (False, 1)])
-def test_chunked_and_row_loop_cg_launches_match_the_oracle(ikr, precision, rows_loop, first_chunk, parity_log):
+@pytest.mark.parametrize("variant,first_chunk", [(-1, 0), (0, 0), (1, 0), (2, 0), (3, 0), (-1, 3), (0, 5), (1, 1),
+                                                   (2, 4), (3, 2)])
+def test_chunked_cg_launches_of_every_variant_match_the_oracle(ikr, precision, variant, first_chunk, parity_log):
     """The batched CG continues each instance's PCG across launches of a few iterations, re-planned over the
-    instances still running (first_chunk 1, 3, 5: every solve spans many launches, switching between the
-    one-row-per-thread and the row-loop variants as the running set shrinks); the converged displacements match
-    the oracle's solves as the single-launch runs do (FP64 1e-8 at ||R|| <= 1e-9 ||R0||; mixed 1e-8 at 1e-8)."""
+    instances still running (first_chunk 1..5: every solve spans many launches); every kernel variant (0 row loop,
+    1 one row per thread, 2 / 3 four / eight threads per row with the matrix in shared memory, -1 the planner's
+    choice) gives converged displacements that match the oracle's solves (FP64 1e-8 at ||R|| <= 1e-9 ||R0||; mixed
+    1e-8 at 1e-8)."""
     bp = problems.batched_cantilevers(n=7, seed=11, nx=(3, 9), nyz=(1, 3), E=(1e3, 1e4), t=(0.1, 0.5), load_steps=3)
     fes, asm = problems.build_gpu_batched(bp, precision=precision)
     req = ikr.FERequirements(fes)
@@ -154,7 +156,7 @@ def test_chunked_and_row_loop_cg_launches_match_the_oracle(ikr, precision, rows_
         st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
                             linear_rtol_min=1e-6)
     nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
-    nr.set_batched_cg(rows_loop=rows_loop, first_chunk=first_chunk)
+    nr.set_batched_cg(variant=variant, first_chunk=first_chunk)
     info = ikr.LoadControl(nr, bp.load_steps).run(req)
     assert info.success
     _, _, conv = nr.instance_info()
@@ -168,5 +170,5 @@ def test_chunked_and_row_loop_cg_launches_match_the_oracle(ikr, precision, rows_
     worst = max(np.abs(u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]] - ref).max() / np.abs(ref).max()
                 for i, ref in enumerate(_CHUNK_REF["u"]))
     form = "FP64" if precision == 0 else "mixed"
-    assert parity_log(f"batched {form}, rows_loop={rows_loop}, first_chunk={first_chunk}: max rel. error vs oracle",
+    assert parity_log(f"batched {form}, variant={variant}, first_chunk={first_chunk}: max rel. error vs oracle",
                       worst, 1e-8)
