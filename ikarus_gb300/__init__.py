@@ -176,6 +176,9 @@ SIGNATURES = {
     "ikr_newton_instance_linear_iterations": ([_vp, _i64p], C.c_int),
     "ikr_newton_set_batched_cg": ([_vp, _I, _I], C.c_int),
     "ikr_newton_batched_cg_launches": ([_vp, _i64p], C.c_int),
+    "ikr_newton_set_batched_take_out": ([_vp, _I], C.c_int),
+    "ikr_load_control_set_escalation": ([_vp, _vp, _vp], C.c_int),
+    "ikr_load_control_escalated": ([_vp, _I, _u8p], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
     "ikr_fes_set_material": ([_vp, _I], C.c_int),
@@ -1238,7 +1241,8 @@ class NewtonRaphson:
     def instance_info(self):
         """(iterations, residual norms, status) per instance of the last batched solve; status 1 converged,
         -1 taken out after its elements inverted (det C <= 0), -2 taken out still above its tolerance after
-        maxIter (the others go on), -3 kept out by exclude_instances."""
+        maxIter (the others go on), -3 kept out by exclude_instances, -4 taken out after its CG ran out of iterations
+        (set_batched_take_out)."""
         n = self.assembler.fes.n_instances
         it = np.zeros(n, dtype=np.int32)
         rn = np.zeros(n)
@@ -1257,6 +1261,11 @@ class NewtonRaphson:
         over the instances still running; variant -1 lets the planner choose per launch, 0 row loop, 1 one row per
         thread, 2 / 3 four / eight threads per row with the matrix in shared memory (where it fits, else 0)."""
         _err(lib().ikr_newton_set_batched_cg(self.h, int(variant), int(first_chunk)))
+
+    def set_batched_take_out(self, unsolved_linear=True):
+        """Batched solves: an instance whose CG ends above its tolerance after linear_max_iter is taken out
+        (status -4)."""
+        _err(lib().ikr_newton_set_batched_take_out(self.h, int(bool(unsolved_linear))))
 
     def batched_cg_launches(self):
         n = C.c_int64()
@@ -1306,6 +1315,22 @@ class LoadControl:
         cb = _CTRL_OBS(tramp)
         self._cbs.append(cb)
         _err(lib().ikr_load_control_subscribe(self.h, cb, None), "subscribe")
+
+    def set_escalation(self, solver: "NewtonRaphson" = None, req: "FERequirements" = None):
+        """Batched runs: an instance this run's solver takes out in a load step is solved again from the state at the
+        step's start by `solver` on `req` (a twin element set with the same instances, e.g. FP64) and stays there
+        for the rest of the run; its displacement is copied into the run's requirement at every step end.  No
+        arguments switch it off."""
+        self._esc = (solver, req)
+        _err(lib().ikr_load_control_set_escalation(self.h, solver.h if solver else None, req.h if req else None),
+             "escalation")
+
+    def escalated(self):
+        """Per instance: escalated in the last run."""
+        n = self.nonLinearSolver.assembler.fes.n_instances
+        m = np.zeros(n, dtype=np.uint8)
+        _err(lib().ikr_load_control_escalated(self.h, n, _ptr(m, C.c_uint8)))
+        return m.astype(bool)
 
     def set_predictor(self, kind: int = 0, predictor: "LearnedPredictor" = None, params=None, record=False):
         """Newton predictor of every load step: 0 none (reference), 1 previous increment, 2 learned, 3 second-order

@@ -1372,8 +1372,10 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   const int ni = f->n_inst;
   const int64_t n = a->n;
   if ((int)nr->inst_failed.size() != ni) nr->inst_failed.assign(ni, 0);
-  for (int i = 0; i < ni && i < (int)nr->inst_excluded.size(); ++i)
+  for (int i = 0; i < ni && i < (int)nr->inst_excluded.size(); ++i) {
     if (nr->inst_excluded[i]) nr->inst_failed[i] = 3;  // kept out by the caller
+    else if (nr->inst_failed[i] == 3) nr->inst_failed[i] = 0;  // no longer kept out
+  }
   struct StatusScope {  // per-instance element status for the duration of the solve
     ikr_fes f;
     explicit StatusScope(ikr_fes ff) : f(ff) { f->inst_status_on = true; }
@@ -1457,6 +1459,13 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
     ikr::launch_scale64(nr->rhs.p, a->R.p, -1.0, n, s);
     count(1);
     batched_cg(nr, f, a, act, cgit);
+    if (nr->take_out_unsolved) {  // the CG ran out of iterations above its tolerance: no usable direction
+      std::vector<double> relres(ni);
+      nr->inst_cg_res.download(relres.data(), ni, s);
+      CK(cudaStreamSynchronize(s));
+      for (int i = 0; i < ni; ++i)
+        if (act[i] && cgit[i] >= st.linear_max_iter && !(relres[i] <= eta[i])) nr->inst_failed[i] = 4;
+    }
     std::vector<uint8_t> failed_before(nr->inst_failed);
     if (st.max_backtracks > 0) {
       nr->u_old.alloc(n);
@@ -1528,7 +1537,8 @@ static void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info) {
   bool ok = true;
   for (int i = 0; i < ni; ++i) {
     if (nr->inst_failed[i]) {
-      nr->inst_conv[i] = nr->inst_failed[i] == 3 ? -3 : (nr->inst_failed[i] == 2 ? -2 : -1);
+      const int fl = nr->inst_failed[i];
+      nr->inst_conv[i] = fl == 3 ? -3 : (fl == 2 ? -2 : (fl == 4 ? -4 : -1));
     } else if (rn[i] <= thr[i]) {
       nr->inst_conv[i] = 1;
     } else {
@@ -1735,6 +1745,33 @@ int ikr_newton_batched_cg_launches(ikr_nr nr, int64_t* n) {
     *n = nr->plan.launches;
   });
 }
+int ikr_newton_set_batched_take_out(ikr_nr nr, int32_t unsolved_linear) {
+  return guarded([&] {
+    need(nr, IKR_ERR_ARG, "null argument");
+    nr->take_out_unsolved = unsolved_linear != 0;
+  });
+}
+int ikr_load_control_set_escalation(ikr_lc lc, ikr_nr nr64, ikr_req req64) {
+  return guarded([&] {
+    need(lc, IKR_ERR_ARG, "null argument");
+    need((nr64 == nullptr) == (req64 == nullptr), IKR_ERR_ARG, "give both the solver and its requirement, or neither");
+    if (nr64) {
+      ikr_fes f = lc->nr->asm_->fes, g = nr64->asm_->fes;
+      need(f->n_inst > 0 && g->n_inst == f->n_inst && g->nn == f->nn && g->inst_off_h == f->inst_off_h, IKR_ERR_ARG,
+           "the escalation solver needs an element set with the same instances");
+      need(req64->fes == g, IKR_ERR_ARG, "requirement of another element set");
+      need(nr64 != lc->nr, IKR_ERR_ARG, "the escalation solver must be another solver");
+    }
+    lc->esc_nr = nr64;
+    lc->esc_req = req64;
+  });
+}
+int ikr_load_control_escalated(ikr_lc lc, int32_t n, uint8_t* mask) {
+  return guarded([&] {
+    need(lc && mask, IKR_ERR_ARG, "null argument");
+    for (int i = 0; i < n; ++i) mask[i] = i < (int)lc->escalated.size() ? lc->escalated[i] : 0;
+  });
+}
 int ikr_newton_exclude_instances(ikr_nr nr, int32_t n, const uint8_t* mask) {
   return guarded([&] {
     need(nr && n >= 0 && (n == 0 || mask), IKR_ERR_ARG, "invalid argument");
@@ -1773,6 +1810,66 @@ int ikr_load_control_subscribe(ikr_lc lc, ikr_control_observer cb, void* user) {
     lc->obs.push_back({cb, user});
   });
 }
+// precision escalation of batched load steps (ikr_load_control_set_escalation)
+static void escalation_begin(ikr_lc lc, ikr_req r) {
+  ikr_fes f = r->fes;
+  const int ni = f->n_inst;
+  lc->escalated.assign(ni, 0);
+  lc->esc_nr->inst_failed.assign(ni, 0);
+  lc->esc_nr->inst_excluded.assign(ni, 1);
+  ikr_req e = lc->esc_req;
+  CK(cudaStreamSynchronize(f->stream));
+  CK(cudaMemcpyAsync(e->u.p, r->u.p, sizeof(double) * r->u.n, cudaMemcpyDeviceToDevice, e->fes->stream));
+  CK(cudaStreamSynchronize(e->fes->stream));
+  e->lambda = r->lambda;
+  e->version++;
+}
+
+static void copy_instance(ikr_fes f, double* dst, const double* src, int i, cudaStream_t s) {
+  const int64_t o = 3LL * f->inst_off_h[i], n = 3LL * (f->inst_off_h[i + 1] - f->inst_off_h[i]);
+  CK(cudaMemcpyAsync(dst + o, src + o, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+}
+
+// after the step's solve: the instances the solver took out in this step start again from the state at the step's
+// start in the escalation solver; every escalated instance's step is solved there and copied back
+static void escalation_step(ikr_lc lc, ikr_req r, double step, ikr_nr_info& ni) {
+  ikr_fes f = r->fes;
+  ikr_req e = lc->esc_req;
+  ikr_nr en = lc->esc_nr;
+  const int ni_ = f->n_inst;
+  CK(cudaStreamSynchronize(f->stream));
+  bool any = false;
+  for (int i = 0; i < ni_; ++i) {
+    const int c = lc->nr->inst_conv[i];
+    if (!lc->escalated[i] && (c == -1 || c == -2 || c == -4)) {
+      copy_instance(f, e->u.p, lc->u_start.p, i, e->fes->stream);
+      lc->escalated[i] = 1;
+    }
+    any = any || lc->escalated[i];
+  }
+  if (!any) return;
+  for (int i = 0; i < ni_; ++i) en->inst_excluded[i] = lc->escalated[i] ? 0 : 1;
+  e->lambda = r->lambda;
+  e->version++;
+  ikr_nr_info ei{};
+  nr_solve(en, e, step, &ei);
+  for (int i = 0; i < ni_; ++i)
+    if (lc->escalated[i]) copy_instance(f, r->u.p, e->u.p, i, e->fes->stream);
+  CK(cudaStreamSynchronize(e->fes->stream));
+  r->version++;
+  // the step succeeds when every instance is converged in one of the two solvers or taken out by the escalation
+  // solver too; the batch's Newton and CG iterations add up (the two solves run one after the other)
+  bool ok = true;
+  for (int i = 0; i < ni_; ++i) {
+    if (lc->escalated[i]) ok = ok && en->inst_conv[i] != 0;
+    else ok = ok && lc->nr->inst_conv[i] != 0;
+  }
+  ni.success = ok ? 1 : 0;
+  ni.iterations += ei.iterations;
+  ni.linear_iterations += ei.linear_iterations;
+  ni.residual_norm = std::max(ni.residual_norm, ei.residual_norm);
+}
+
 int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_info* infos, int32_t capacity) {
   return guarded([&] {
     need(lc && r, IKR_ERR_ARG, "null argument");
@@ -1797,6 +1894,8 @@ int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_in
     ikr_nr_info ni{};
     lc->nr->inst_failed.clear();
     nr_solve(lc->nr, r, 0.0, &ni);  // equilibrium check at the initial load factor (loadcontrol.inl:29-34)
+    const bool esc = lc->esc_nr && r->fes->n_inst > 0;
+    if (esc) escalation_begin(lc, r);
     record(ni);
     if (ni.success) {
       cs.step_size = step;
@@ -1806,8 +1905,13 @@ int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_in
         cs.load_step = ls;
         notify(IKR_STEP_STARTED);
         r->lambda += step;  // LoadControl::predictor (loadcontrol.inl:54-57)
+        if (esc) {
+          lc->u_start.alloc(r->u.n);
+          CK(cudaMemcpyAsync(lc->u_start.p, r->u.p, sizeof(double) * r->u.n, cudaMemcpyDeviceToDevice, r->fes->stream));
+        }
         const double ref = predictor_apply(lc, r, ls);  // optional displacement prediction, FP64-gated
         nr_solve(lc->nr, r, step, &ni, ref);
+        if (esc) escalation_step(lc, r, step, ni);
         if (ni.iterations == 0 && lc->nr->asm_->has_idbc) idbc_sync(lc->nr->asm_, r);  // loadcontrol.inl:43-44
         predictor_end_step(lc, r, ls);
         record(ni);

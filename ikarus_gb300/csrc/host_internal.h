@@ -1284,7 +1284,10 @@ struct ikr_nr_s {
   std::vector<int64_t> inst_lin;  // CG iterations per instance over the solve
   std::vector<double> inst_res;
   std::vector<int8_t> inst_conv;     // 1 converged, 0 not, -1 taken out after an element inversion
-  std::vector<uint8_t> inst_failed;  // inversions seen since the last reset (LoadControl::run, newton_solve)
+  std::vector<uint8_t> inst_failed;  // taken out since the last reset (LoadControl::run, newton_solve): 1 inverted,
+                                     // 2 above tolerance after max_iter, 3 kept out by the caller, 4 CG unsolved
+  bool take_out_unsolved = false;    // batched: a CG still above its tolerance after linear_max_iter takes the
+                                     // instance out (status -4)
   std::vector<uint8_t> inst_excluded;  // instances the caller keeps out of every solve (ikr_newton_exclude_instances)
   DBuf<double> u_old, alpha_old, inst_step;  // backtracking: state before the correction, per-instance steps
   int64_t backtracks = 0;                    // corrections halved since creation
@@ -1311,6 +1314,14 @@ struct ikr_lc_s {
   ikr_nr nr = nullptr;
   int steps = 1;
   double t0 = 0, t1 = 1;
+  // batched solves: precision escalation (ikr_load_control_set_escalation).  An instance the solver takes out in a
+  // load step is solved again from the state at the start of that step by esc_nr on esc_req (an FP64 twin of the
+  // element set) and stays there for the rest of the run; its displacement is copied back into the run's requirement
+  // at every step end.
+  ikr_nr esc_nr = nullptr;
+  ikr_req esc_req = nullptr;
+  std::vector<uint8_t> escalated;
+  DBuf<double> u_start;
   std::vector<ControlObserver> obs;
   std::vector<std::unique_ptr<ListenerBase>> listeners;
   // Newton predictor of each load step (the reference only increments the load factor,

@@ -466,7 +466,8 @@ int ikr_newton_subscribe_logger(ikr_nr nr, ikr_log_sink sink, void* user);
 /* per instance (batched solves): Newton iterations, final residual norm and convergence of the last solve
  * (1 converged, -1 taken out after its elements inverted, det C <= 0 -- the reference aborts there --, -2 taken out
  * because it was still above its tolerance after max_iter -- the reference's LoadControl stops there --, -3 kept out
- * by ikr_newton_exclude_instances; here the
+ * by ikr_newton_exclude_instances, -4 taken out after its CG ran out of iterations (ikr_newton_set_batched_take_out);
+ * here the
  * other instances go on and the solve succeeds when all instances not taken out converge).  Instances taken out
  * stay out for the rest of a LoadControl run. */
 int ikr_newton_instance_info(ikr_nr nr, int32_t* iterations, double* residual_norms, int32_t* converged);
@@ -487,6 +488,18 @@ int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations);
  * loop.  For tests and tuning; the results agree to rounding.  batched_cg_launches: launches since creation. */
 int ikr_newton_set_batched_cg(ikr_nr nr, int32_t variant, int32_t first_chunk);
 int ikr_newton_batched_cg_launches(ikr_nr nr, int64_t* n);
+/* batched solves (no reference counterpart): unsolved_linear = 1 takes out an instance whose CG ends above its
+ * tolerance after linear_max_iter (status -4 in instance_info; in FP32 the attainable accuracy of the tangent can lie
+ * above the tolerance, and the direction is then no Newton direction) */
+int ikr_newton_set_batched_take_out(ikr_nr nr, int32_t unsolved_linear);
+/* batched load control (no reference counterpart): precision escalation.  An instance the run's solver takes out in
+ * a load step (-1 inverted, -2 above tolerance after max_iter, -4 CG unsolved) is solved again from the state at the
+ * start of that step by nr64 on req64 -- a solver over a twin element set with the same instances, e.g. in FP64 --
+ * and stays with nr64 for the rest of the run; its displacement is copied into the run's requirement at every step
+ * end.  A step succeeds when every instance converged in one of the two solvers or was taken out by nr64 as well.
+ * nr64 = req64 = NULL switches it off.  escalated: the instances escalated in the last run (one byte each). */
+int ikr_load_control_set_escalation(ikr_lc lc, ikr_nr nr64, ikr_req req64);
+int ikr_load_control_escalated(ikr_lc lc, int32_t n, uint8_t* mask);
 
 /* ---- LoadControl (loadcontrol.hh:29-113, loadcontrol.inl:17-57, controlroutinefactory.hh:38-48) --------- */
 typedef struct ikr_control_state {   /* ControlRoutineState (controlroutinestate.hh:21-31) */

@@ -172,3 +172,83 @@ def test_chunked_cg_launches_of_every_variant_match_the_oracle(ikr, precision, v
     form = "FP64" if precision == 0 else "mixed"
     assert parity_log(f"batched {form}, variant={variant}, first_chunk={first_chunk}: max rel. error vs oracle",
                       worst, 1e-8)
+
+
+def _escalated_run(ikr, bp, primary_settings, take_out=True, observe=None):
+    fes, asm = problems.build_gpu_batched(bp, precision=1)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(primary_settings,
+                                                        ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    nr.set_batched_take_out(take_out)
+    fes64, asm64 = problems.build_gpu_batched(bp, precision=0)
+    nr64 = ikr.NewtonRaphson(asm64, ikr.NewtonRaphsonConfig(
+        ikr.NRSettings(tol=1e-9, maxIter=30, relative=True, linear_rtol=1e-12),
+        ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    req64 = ikr.FERequirements(fes64)
+    lc = ikr.LoadControl(nr, bp.load_steps)
+    lc.set_escalation(nr64, req64)
+    if observe:
+        lc.subscribe(lambda msg, s: observe(msg, s, lc))
+    req = ikr.FERequirements(fes)
+    info = lc.run(req)
+    _, _, conv = nr.instance_info()
+    _, _, conv64 = nr64.instance_info()
+    return info, req.globalSolution(), lc.escalated(), conv, conv64
+
+
+def test_escalation_solves_in_fp64_what_the_fp32_solver_takes_out(ikr, parity_log):
+    """Precision escalation of a batched load control: with a CG capped at 3 iterations every FP32 solve is unsolved
+    (status -4) in the first step, so every instance continues with the FP64 solver from the step's start; the
+    combined solution matches the oracle's solves (1e-8), and the FP32 solver's statuses say why each escalated."""
+    bp = problems.batched_cantilevers(n=5, seed=11, nx=(3, 8), nyz=(1, 3), E=(1e3, 1e4), t=(0.1, 0.5), load_steps=3)
+    st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, linear_rtol=1e-8, linear_max_iter=3)
+    info, u, esc, conv, conv64 = _escalated_run(ikr, bp, st)
+    assert info.success
+    assert esc.all() and (conv == -4).all() and (conv64 == 1).all()
+    worst = 0.0
+    for i, part in enumerate(bp.parts):
+        ref = oracle.from_problem(part).load_control(bp.load_steps, tol=1e-9, tol_mode=1, max_iter=30)["u"]
+        worst = max(worst, np.abs(u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]] - ref).max()
+                    / np.abs(ref).max())
+    assert parity_log("batched escalation (all instances to FP64): max rel. error vs oracle", worst, 1e-8)
+
+
+def test_escalation_mid_run_starts_from_the_step_start(ikr, parity_log):
+    """An FP32 solver allowed 3 Newton iterations per step takes out the instances that need more in some step;
+    each continues in FP64 from the state at the start of that step (the converged state of the step before), and
+    the combined load path matches the oracle's (1e-8) for every instance."""
+    bp = problems.batched_cantilevers(n=8, seed=5, nx=(3, 8), nyz=(1, 3), E=(1e2, 1e4), t=(0.1, 1.0), load_steps=4)
+    st = ikr.NRSettings(tol=1e-8, maxIter=3, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                        linear_rtol_min=1e-6)
+    first_step = {}
+
+    def observe(msg, s, lc):
+        if msg == ikr.ControlMessages.STEP_ENDED and s["loadStep"] >= 0:
+            for i in np.nonzero(lc.escalated())[0]:
+                first_step.setdefault(int(i), s["loadStep"])
+
+    info, u, esc, conv, conv64 = _escalated_run(ikr, bp, st, observe=observe)
+    assert info.success
+    assert ((conv == 1) | (esc & (conv64 == 1))).all()
+    assert set(np.nonzero(esc)[0].tolist()) == set(first_step)
+    worst = 0.0
+    for i, part in enumerate(bp.parts):
+        ref = oracle.from_problem(part).load_control(bp.load_steps, tol=1e-9, tol_mode=1, max_iter=30)["u"]
+        worst = max(worst, np.abs(u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]] - ref).max()
+                    / np.abs(ref).max())
+    assert parity_log(f"batched escalation mid-run (escalated at steps {sorted(first_step.values())}): max rel. "
+                      "error vs oracle", worst, 1e-8)
+
+
+def test_escalated_instance_that_inverts_in_fp64_too_is_taken_out(ikr):
+    """An instance whose elements invert in both precisions ends taken out by the FP64 solver; the others stay
+    with the FP32 solver and converge."""
+    bp = problems.batched_cantilevers(n=6, seed=5, nx=(3, 6), nyz=(1, 2), E=(1e3, 1e3), t=(0.2, 0.3), load_steps=3)
+    bad = 2
+    sel = (bp.face_elem >= bp.elem_offsets[bad]) & (bp.face_elem < bp.elem_offsets[bad + 1])
+    bp.face_traction[sel] *= 1e4
+    st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                        linear_rtol_min=1e-6)
+    info, u, esc, conv, conv64 = _escalated_run(ikr, bp, st)
+    assert info.success
+    assert esc[bad] and conv64[bad] == -1 and conv[bad] in (-1, -4)
+    assert (np.delete(conv, bad) == 1).all() and not np.delete(esc, bad).any()
