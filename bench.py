@@ -658,8 +658,9 @@ def run_spmv_only(args):
 def run_batched(args):
     """512 independent cantilevers (random grids, lengths, materials, tip tractions), 10 load steps, every
     instance to ||R||/||R0|| < 1e-8 on every step: mixed form (FP32 tangent, batched FP32 CG, FP64 residual), alone
-    and with precision escalation of the instances it takes out to FP64, against the plain FP64 form of the same
-    batched method (FP64 tangent and CG to 1e-10).  The value is the escalated form's time."""
+    and with precision escalation of the instances it takes out to FP64 (with its inexact-Newton controls, and with
+    the plain form's settings), against the plain FP64 form of the same batched method (FP64 tangent and CG to
+    1e-10).  The value is the escalated form's time."""
     import numpy as np
     import torch
 
@@ -689,14 +690,13 @@ def run_batched(args):
         if escalate:
             # precision escalation: an instance the FP32 solver takes out in a step (inverted elements, no
             # convergence in maxIter, or a CG that cannot reach its tolerance in FP32) is solved again from the
-            # step's start in FP64 with the same inexact-Newton controls, and stays in FP64
+            # step's start in FP64 and stays in FP64
             nr.set_batched_take_out(True)
             fes64, asm64 = problems.build_gpu_batched(bp, precision=0)
+            # "ew": FP64 with the mixed form's inexact-Newton controls; "plain": the plain FP64 form's settings, so
+            # that an escalated instance is solved from the step's start exactly as the plain form solves it
             nr64 = ikr.NewtonRaphson(asm64, ikr.NewtonRaphsonConfig(
-                ikr.NRSettings(tol=1e-8, maxIter=40, relative=True, eisenstat_walker=True,
-                               linear_rtol=args.batched_eta_max, linear_rtol_min=1e-6, linear_max_iter=20000,
-                               backtracks=args.batched_backtracks),
-                ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+                settings(escalate == "ew"), ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
             req64 = ikr.FERequirements(fes64)
             lc.set_escalation(nr64, req64)
             esc = (fes64, asm64, nr64, req64)
@@ -739,7 +739,8 @@ def run_batched(args):
 
     run_form("mixed", True)
     run_form("plain_fp64", False)
-    run_form("mixed_escalated", True, escalate=True)
+    run_form("mixed_escalated", True, escalate="ew")
+    run_form("mixed_escalated_to_plain", True, escalate="plain")
 
     def compare(a, b):
         both = np.nonzero((status[a] == 1) & (status[b] == 1))[0]
@@ -763,6 +764,8 @@ def run_batched(args):
 
     out["mixed_vs_plain"] = compare("mixed", "plain_fp64")
     out["mixed_escalated_vs_plain"] = compare("mixed_escalated", "plain_fp64")
+    out["mixed_escalated_to_plain_vs_plain"] = compare("mixed_escalated_to_plain", "plain_fp64")
+    out["speedup_escalated_to_plain_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed_escalated_to_plain"]["s"], 3)
     out["value"] = out["mixed_escalated"]["s"]
     out["speedup_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed_escalated"]["s"], 3)
     out["speedup_mixed_alone_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 3)

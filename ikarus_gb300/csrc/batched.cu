@@ -510,6 +510,238 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_pcg_smem_kernel(
   }
 }
 
+// FP32 PCG of one instance per thread-block cluster of kClusterCtas CTAs (rows split across the cluster, one row per
+// thread).  Each CTA keeps its rows' z and the two p buffers in shared memory; neighbours owned by other CTAs are read
+// from their shared memory (distributed shared memory, ld.shared::cluster), and the group sums are exchanged the
+// same way, so an iteration's two reductions are hardware cluster barriers (release / acquire at cluster scope) in
+// place of global atomics and polls.  The CTA's matrix blocks and the owner (CTA rank, local row) of every column
+// are copied to shared memory once per launch.  Clusters never wait on each other, so no co-residency is needed.
+constexpr int kClusterCtas = 16;
+constexpr int kClusterThreads = 192;
+constexpr int kClusterWidth = 27;  // blocks per row (a hex node couples to at most 27 nodes)
+struct ClusterCfg {
+  static constexpr int kValBytes = 9 * kClusterWidth * kClusterThreads * 4;
+  static constexpr int kColBytes = kClusterWidth * kClusterThreads * 4;
+  static constexpr int kVecOff = kValBytes + kColBytes;
+  static constexpr int kBytes = kVecOff + 3 * kClusterThreads * 16;  // z, p0, p1 (float4 per row)
+};
+
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t map_peer(uint32_t local_addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local_addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float4 ld_cluster_f4(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(addr)
+               : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_cluster_f64(uint32_t addr) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+  return v;
+}
+
+// cluster-wide sums of N values: CTA sum (warp 0), published in this CTA's shared slot, cluster barrier, lane k < 16
+// of warp 0 reads CTA k's slot; valid in warp 0
+template <int N>
+__device__ __forceinline__ void cluster_sum(double (&v)[N], double* sfull, double* red, const uint32_t* peer, int slot) {
+  cta_reduce_smem<N>(v, sfull);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) red[2 * slot + k] = v[k];
+  }
+  cluster_sync_all();
+  if (threadIdx.x < 32) {
+    const uint32_t own = (uint32_t)__cvta_generic_to_shared(red + 2 * slot);
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      const double t = threadIdx.x < kClusterCtas ? ld_cluster_f64(map_peer(own + 8 * k, threadIdx.x)) : 0.0;
+      v[k] = warp_sum(t);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kClusterThreads, 1) batched_pcg_cluster_kernel(
+    Bsr A, const float* __restrict__ val, const float* __restrict__ minv, const double* __restrict__ b,
+    double* __restrict__ x_out, const int32_t* __restrict__ node_off, const int32_t* __restrict__ cluster_inst,
+    float* xw, float* rw, float* zw, float* p0, float* p1, const double* __restrict__ rtol_inst, int max_iter,
+    int chunk, int first_launch, double* st, int32_t* its, int32_t* flag, double* __restrict__ relres_out) {
+  using C = ClusterCfg;
+  constexpr int T = kClusterThreads, W = kClusterWidth;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  float* sval = reinterpret_cast<float*>(dsm);                     // [9][W][T]
+  int32_t* scol = reinterpret_cast<int32_t*>(dsm + C::kValBytes);  // [W][T]: owner rank << 16 | local row, -1
+  float4* zs = reinterpret_cast<float4*>(dsm + C::kVecOff);        // [T] own rows' z, then p0, p1
+  __shared__ double sfull[2 * T];
+  __shared__ double red[4];
+  __shared__ uint32_t peer[kClusterCtas];  // shared::cluster address of every CTA's dynamic shared memory
+  __shared__ float s_alpha, s_tb;
+  __shared__ int s_state;
+  const int rank = (int)cluster_ctarank();
+  const int inst = cluster_inst[blockIdx.x / kClusterCtas];
+  const int r0 = node_off[inst], nr = node_off[inst + 1] - r0;
+  auto row_start = [&](int k) { return r0 + (int)((int64_t)nr * k / kClusterCtas); };
+  const int ra = row_start(rank), rb = row_start(rank + 1);
+  const int tid = threadIdx.x, row = ra + tid;
+  const bool mine = row < rb;
+  if (tid < kClusterCtas) peer[tid] = map_peer((uint32_t)__cvta_generic_to_shared(dsm), tid);
+  {  // this row's blocks and the owner of each column
+    const int s = mine ? row >> 5 : 0, l = row & 31;
+    const int gs = mine ? __ldg(A.slice_off + s) : 0, w = mine ? __ldg(A.slice_off + s + 1) - gs : 0;
+    for (int u = 0; u < W; ++u) {
+      int packed = -1;
+      if (u < w) {
+        const int c = __ldg(A.col_sell + 32 * (gs + u) + l);
+        int k = (int)((int64_t)(c - r0) * kClusterCtas / nr);
+        k = max(0, min(k, kClusterCtas - 1));
+        while (k < kClusterCtas - 1 && c >= row_start(k + 1)) ++k;
+        while (k > 0 && c < row_start(k)) --k;
+        packed = (k << 16) | (c - row_start(k));
+      }
+      scol[u * T + tid] = packed;
+#pragma unroll
+      for (int k = 0; k < 9; ++k)
+        sval[(k * W + u) * T + tid] = packed >= 0 ? __ldg(val + (int64_t)(gs + u) * 288 + l + 32 * k) : 0.f;
+    }
+  }
+  V3<float> xr{}, rv{}, zr{}, pr{};
+  float mv[9];
+  if (mine) load_minv(minv, row, mv);
+  double rz = 0.0, rr = 0.0, bb = 0.0, beta = 0.0, tol2 = 0.0;  // thread 0's
+  int it = first_launch ? 0 : its[inst];
+  float lrz = 0.f;
+  double lrr = 0.0;
+  if (mine) {
+    if (first_launch) {  // x = 0, r = b, z = M^-1 r, p_old = 0
+      rv = {float(b[3 * row]), float(b[3 * row + 1]), float(b[3 * row + 2])};
+      zr = jacobi(mv, rv);
+      lrz = rv.x * zr.x + rv.y * zr.y + rv.z * zr.z;
+      lrr = double(rv.x) * double(rv.x) + double(rv.y) * double(rv.y) + double(rv.z) * double(rv.z);
+    } else {
+      xr = load3rw(xw, row), rv = load3rw(rw, row), zr = load3rw(zw, row);
+      pr = load3rw((it & 1) ? p0 : p1, row);
+    }
+    zs[tid] = make_float4(zr.x, zr.y, zr.z, 0.f);
+    zs[T * (1 + ((it & 1) ? 0 : 1)) + tid] = make_float4(pr.x, pr.y, pr.z, 0.f);  // p_old of iteration it
+  }
+  if (first_launch) {
+    double v[2] = {double(lrz), lrr};
+    cluster_sum<2>(v, sfull, red, peer, 1);
+    if (tid == 0) rz = v[0], bb = v[1], rr = v[1];
+  } else {
+    cluster_sync_all();  // every CTA's z and p are in place before the first gathers
+    if (tid == 0) rz = st[4 * inst], rr = st[4 * inst + 1], bb = st[4 * inst + 2], beta = st[4 * inst + 3];
+  }
+  if (tid == 0) {
+    tol2 = rtol_inst[inst] * rtol_inst[inst] * bb;
+    s_state = (!(rr > tol2) || it >= max_iter) ? 1 : 0;
+    s_tb = float(beta);
+  }
+  __syncthreads();
+  int state = s_state;
+  const uint32_t zoff = C::kVecOff;
+  for (int k = 0; state == 0 && k < chunk; ++k) {
+    const float tb = s_tb;
+    const int po = (it & 1) ? 1 : 2, pn = (it & 1) ? 2 : 1;  // p_old / p_new slots (p0 = slot 1, p1 = slot 2)
+    const uint32_t off_z = zoff, off_p = zoff + po * T * 16;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    if (mine) {
+#pragma unroll
+      for (int u0 = 0; u0 < W; u0 += 9) {
+        float4 zv[9], pv[9];
+#pragma unroll
+        for (int u = 0; u < 9; ++u) {
+          const int packed = scol[(u0 + u) * T + tid];
+          if (packed >= 0) {
+            const uint32_t base = peer[packed >> 16] + 16u * (uint32_t)(packed & 0xffff);
+            zv[u] = ld_cluster_f4(base + off_z);
+            pv[u] = ld_cluster_f4(base + off_p);
+          } else {
+            zv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            pv[u] = zv[u];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 9; ++u) {
+          const float x0 = zv[u].x + tb * pv[u].x, x1 = zv[u].y + tb * pv[u].y, x2 = zv[u].z + tb * pv[u].z;
+          const float* m = sval + (u0 + u) * T + tid;
+          constexpr int P = W * T;
+          a0 += m[0] * x0 + m[P] * x1 + m[2 * P] * x2;
+          a1 += m[3 * P] * x0 + m[4 * P] * x1 + m[5 * P] * x2;
+          a2 += m[6 * P] * x0 + m[7 * P] * x1 + m[8 * P] * x2;
+        }
+      }
+    }
+    float lpq = 0.f;
+    if (mine) {
+      pr = {zr.x + tb * pr.x, zr.y + tb * pr.y, zr.z + tb * pr.z};
+      zs[pn * T + tid] = make_float4(pr.x, pr.y, pr.z, 0.f);
+      lpq = pr.x * a0 + pr.y * a1 + pr.z * a2;
+    }
+    double v1[1] = {double(lpq)};
+    cluster_sum<1>(v1, sfull, red, peer, 0);
+    if (tid == 0) {
+      if (!(fabs(v1[0]) > 0.0) || !isfinite(v1[0])) s_state = 2;
+      else s_alpha = float(rz / v1[0]);
+    }
+    __syncthreads();
+    state = s_state;
+    if (state != 0) break;
+    const float alpha = s_alpha;
+    lrz = 0.f;
+    lrr = 0.0;
+    if (mine) {
+      xr = {xr.x + alpha * pr.x, xr.y + alpha * pr.y, xr.z + alpha * pr.z};
+      rv = {rv.x - alpha * a0, rv.y - alpha * a1, rv.z - alpha * a2};
+      zr = jacobi(mv, rv);
+      zs[tid] = make_float4(zr.x, zr.y, zr.z, 0.f);
+      lrz = rv.x * zr.x + rv.y * zr.y + rv.z * zr.z;
+      lrr = double(rv.x) * double(rv.x) + double(rv.y) * double(rv.y) + double(rv.z) * double(rv.z);
+    }
+    double v2[2] = {double(lrz), lrr};
+    cluster_sum<2>(v2, sfull, red, peer, 1);
+    ++it;
+    if (tid == 0) {
+      beta = v2[0] / rz;
+      rz = v2[0];
+      rr = v2[1];
+      s_tb = float(beta);
+      if (!(rr > tol2) || it >= max_iter) s_state = 1;
+    }
+    __syncthreads();
+    state = s_state;
+  }
+  if (mine) {
+    if (state == 0) {  // continued by the next launch: the state the other variants read
+      store3(xw, row, xr.x, xr.y, xr.z);
+      store3(rw, row, rv.x, rv.y, rv.z);
+      store3(zw, row, zr.x, zr.y, zr.z);
+      store3((it & 1) ? p0 : p1, row, pr.x, pr.y, pr.z);
+    } else {
+      x_out[3 * row] = double(xr.x), x_out[3 * row + 1] = double(xr.y), x_out[3 * row + 2] = double(xr.z);
+    }
+  }
+  if (rank == 0 && tid == 0) {
+    st[4 * inst] = rz, st[4 * inst + 1] = rr, st[4 * inst + 2] = bb, st[4 * inst + 3] = beta;
+    its[inst] = it;
+    flag[inst] = state;
+    relres_out[inst] = bb > 0.0 ? sqrt(rr / bb) : 0.0;
+  }
+  cluster_sync_all();  // no CTA leaves while another may still read its shared memory
+}
+
 // per-instance sum of squares over dof ranges [3 node_off[i], 3 node_off[i+1]); one block per instance
 __global__ void instance_norms_kernel(const double* __restrict__ x, const int32_t* __restrict__ node_off,
                                       double* __restrict__ out) {
@@ -575,6 +807,54 @@ int batched_pcg_capacity(bool fp32, int variant, int sms) {
 }
 
 int batched_pcg_threads() { return kBatchThreads; }
+
+int batched_cluster_rows() { return kClusterCtas * kClusterThreads; }
+int batched_cluster_width() { return kClusterWidth; }
+
+static cudaError_t cluster_prepare() {
+  const void* k = (const void*)batched_pcg_cluster_kernel;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, ClusterCfg::kBytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+}
+
+int batched_cluster_capacity() {
+  if (cluster_prepare() != cudaSuccess) return 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kClusterCtas);
+  cfg.blockDim = dim3(kClusterThreads);
+  cfg.dynamicSmemBytes = ClusterCfg::kBytes;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kClusterCtas, at[0].val.clusterDim.y = 1, at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, (const void*)batched_pcg_cluster_kernel, &cfg) != cudaSuccess) return 0;
+  return n;
+}
+
+cudaError_t launch_batched_pcg_cluster(const Bsr& A, const void* minv, const double* b, double* x_out, int n_clusters,
+                                       const int32_t* node_off, const int32_t* cluster_inst, void* xw, void* rw,
+                                       void* zw, void* p0, void* p1, const double* rtol, int max_iter, int chunk,
+                                       int first_launch, double* st, int32_t* its, int32_t* flag, double* relres,
+                                       cudaStream_t s) {
+  cudaError_t e = cluster_prepare();
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kClusterCtas * n_clusters);
+  cfg.blockDim = dim3(kClusterThreads);
+  cfg.dynamicSmemBytes = ClusterCfg::kBytes;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kClusterCtas, at[0].val.clusterDim.y = 1, at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, batched_pcg_cluster_kernel, A, (const float*)A.val, (const float*)minv, b, x_out,
+                            node_off, cluster_inst, (float*)xw, (float*)rw, (float*)zw, (float*)p0, (float*)p1, rtol,
+                            max_iter, chunk, first_launch, st, its, flag, relres);
+}
 int batched_pcg_rows_per_cta(int variant) { return variant == 2 ? kBatchThreads / 4 : (variant == 3 ? kBatchThreads / 8 : kBatchThreads); }
 int batched_pcg_max_width(int variant) {
   return variant == 2 ? 4 * SmemCfg<float, 4>::kU : (variant == 3 ? 8 * SmemCfg<float, 8>::kU : 1 << 30);

@@ -1230,7 +1230,9 @@ int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on) {
 namespace ikr_host {
 // Newton-Raphson over independent instances: every instance runs its own Newton iteration and relative
 // convergence test; one assembly and one batched CG launch (CTA per instance) serve all still-active instances.
-// CTA groups of one batched CG launch over the instances in `run`.  The variants with few rows per CTA go first, as
+// CTA groups of one batched CG launch over the instances in `run`.  In FP32, while every running instance fits one
+// 16-CTA cluster and all their clusters fit the device at once, each instance gets a cluster (variant 4).  Otherwise
+// the variants with few rows per CTA go first, as
 // their iterations are the shortest: eight, then four threads per row with the matrix in shared memory, then one row
 // per thread (instance i gets C_i = ceil(rows_i / rows per CTA) CTAs) -- the first whose groups fit the co-resident
 // CTAs of that variant (and at most 128 CTAs per group, rows of at most the variant's blocks).  Otherwise C_i ~ its
@@ -1249,10 +1251,27 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const 
       width[k] = std::max(width[k], a->slice_off_h[sl + 1] - a->slice_off_h[sl]);
   }
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rows[x] > rows[y]; });
-  std::vector<int> cand;
-  if (P.variant >= 0) cand.push_back(P.variant);
-  else cand = {3, 2, 1};
   int variant = 0;
+  // FP32: one instance per 16-CTA cluster (vectors and sums in distributed shared memory) while the running
+  // instances fit one cluster each and the device holds all their clusters at once
+  if (fp32 && (P.variant == -1 || P.variant == 4)) {
+    bool fits = nr_ <= ikr::batched_cluster_capacity();
+    for (int k = 0; k < nr_ && fits; ++k)
+      fits = rows[k] <= ikr::batched_cluster_rows() && width[k] <= ikr::batched_cluster_width();
+    if (fits) {
+      std::vector<int32_t> ci(run.begin(), run.end());
+      P.n_cta = nr_;
+      P.cur_variant = 4;
+      P.cooperative = false;
+      const size_t cap = (size_t)std::max(f->n_inst, 4 * sms);
+      if (P.cta_inst.n < cap) P.cta_inst.alloc(cap);
+      CK(cudaMemcpyAsync(P.cta_inst.p, ci.data(), sizeof(int32_t) * ci.size(), cudaMemcpyHostToDevice, f->stream));
+      return;
+    }
+  }
+  std::vector<int> cand;
+  if (P.variant >= 0 && P.variant <= 3) cand.push_back(P.variant);
+  else if (P.variant == -1) cand = {3, 2, 1};
   for (int v : cand) {
     if (v == 0) break;
     const int rpc = ikr::batched_pcg_rows_per_cta(v), maxw = ikr::batched_pcg_max_width(v);
@@ -1338,11 +1357,17 @@ static void batched_cg(ikr_nr nr, ikr_fes f, ikr_asm a, const std::vector<uint8_
   bool first = true;
   while (!run.empty()) {
     plan_batch_launch(nr, f, a, a->fp32, run);
-    CK(ikr::launch_batched_pcg(a->bsr(), a->fp32, P.cur_variant, w.minv, nr->rhs.p, nr->corr.p, P.n_cta, f->inst_off.p,
-                               P.cta_inst.p, P.cta_first.p, P.cta_size.p, w.x, w.r, w.z, w.p0, w.p1, w.q,
-                               nr->inst_rtol.p, st.linear_max_iter, chunk, first ? 1 : 0, P.st.p,
-                               nr->inst_cg_iters.p, P.flag.p, nr->inst_cg_res.p, P.part.p, P.counters.p, ni,
-                               P.cooperative, s));
+    if (P.cur_variant == 4)
+      CK(ikr::launch_batched_pcg_cluster(a->bsr(), w.minv, nr->rhs.p, nr->corr.p, P.n_cta, f->inst_off.p,
+                                         P.cta_inst.p, w.x, w.r, w.z, w.p0, w.p1, nr->inst_rtol.p, st.linear_max_iter,
+                                         chunk, first ? 1 : 0, P.st.p, nr->inst_cg_iters.p, P.flag.p,
+                                         nr->inst_cg_res.p, s));
+    else
+      CK(ikr::launch_batched_pcg(a->bsr(), a->fp32, P.cur_variant, w.minv, nr->rhs.p, nr->corr.p, P.n_cta,
+                                 f->inst_off.p, P.cta_inst.p, P.cta_first.p, P.cta_size.p, w.x, w.r, w.z, w.p0, w.p1,
+                                 w.q, nr->inst_rtol.p, st.linear_max_iter, chunk, first ? 1 : 0, P.st.p,
+                                 nr->inst_cg_iters.p, P.flag.p, nr->inst_cg_res.p, P.part.p, P.counters.p, ni,
+                                 P.cooperative, s));
     count(1);
     ++P.launches;
     first = false;
@@ -1734,7 +1759,7 @@ int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations) {
 }
 int ikr_newton_set_batched_cg(ikr_nr nr, int32_t variant, int32_t first_chunk) {
   return guarded([&] {
-    need(nr && first_chunk >= 0 && variant >= -1 && variant <= 3, IKR_ERR_ARG, "invalid argument");
+    need(nr && first_chunk >= 0 && variant >= -1 && variant <= 4, IKR_ERR_ARG, "invalid argument");
     nr->plan.variant = variant;
     nr->plan.first_chunk = first_chunk ? first_chunk : 128;
   });

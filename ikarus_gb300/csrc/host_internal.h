@@ -1297,7 +1297,7 @@ struct ikr_nr_s {
   // CTA groups of the batched CG (kernels.h launch_batched_pcg), re-planned before every launch over the running instances
   struct BatchPlan {
     int n_cta = 0;
-    int cur_variant = 0;         // kernels.h launch_batched_pcg variant of the current plan
+    int cur_variant = 0;         // kernels.h launch_batched_pcg variant of the current plan (4: clusters)
     bool cooperative = false;
     DBuf<int32_t> cta_inst, cta_first, cta_size;
     DBuf<double> part;
@@ -1305,7 +1305,7 @@ struct ikr_nr_s {
     DBuf<double> st;             // rz, r.r, b.b, beta per instance between the launches of one solve
     DBuf<int32_t> flag;          // per instance: 0 running, 1 finished, 2 breakdown, -1 a wait gave up
     int64_t launches = 0;        // batched CG launches since creation
-    int variant = -1;            // -1: the planner's choice; 0..3 that variant where it fits, else the row loop
+    int variant = -1;            // -1: the planner's choice; 0..4 that variant where it fits, else the row loop
     int first_chunk = 128;       // iterations of a solve's first launch (doubling for the next ones, at most 4096)
   } plan;
 };

@@ -310,6 +310,18 @@ cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, int variant, const void*
                                const double* rtol, int max_iter, int chunk, int first_launch, double* st, int32_t* its,
                                int32_t* flag, double* relres, double* part, unsigned int* counters, int n_inst,
                                bool cooperative, cudaStream_t s);
+// FP32 only: one instance per cluster of 16 CTAs (cluster_inst per cluster), at most batched_cluster_rows() rows and
+// batched_cluster_width() blocks per row; vectors and sums through distributed shared memory; same state protocol
+// (st, its, flag, x_out).  capacity: clusters co-resident on the device (more run in waves; clusters never wait on
+// each other).
+int batched_cluster_rows();
+int batched_cluster_width();
+int batched_cluster_capacity();
+cudaError_t launch_batched_pcg_cluster(const Bsr& A, const void* minv, const double* b, double* x_out, int n_clusters,
+                                       const int32_t* node_off, const int32_t* cluster_inst, void* xw, void* rw,
+                                       void* zw, void* p0, void* p1, const double* rtol, int max_iter, int chunk,
+                                       int first_launch, double* st, int32_t* its, int32_t* flag, double* relres,
+                                       cudaStream_t s);
 void launch_instance_norms(const double* x, int n_inst, const int32_t* node_off, double* out, cudaStream_t s);
 // u = u_old + step[i] corr on the dofs of instance i (instances with step 1 untouched)
 void launch_instance_step(double* u, const double* u_old, const double* corr, int n_inst, const int32_t* node_off,
