@@ -1259,8 +1259,8 @@ class NewtonRaphson:
     def set_batched_cg(self, variant=-1, first_chunk=0):
         """Batched solves: the CG runs as launches of first_chunk (0: 128), then doubling, iterations, re-planned
         over the instances still running; variant -1 lets the planner choose per launch, 0 row loop, 1 one row per
-        thread, 2 / 3 four / eight threads per row with the matrix in shared memory, 4 one instance per 16-CTA
-        cluster (FP32; vectors in distributed shared memory) -- where it fits, else 0."""
+        thread, 2 / 3 / 5 four / eight / sixteen threads per row with the matrix in shared memory, 4 one instance per
+        16-CTA cluster (FP32; vectors in distributed shared memory) -- where it fits, else 0."""
         _err(lib().ikr_newton_set_batched_cg(self.h, int(variant), int(first_chunk)))
 
     def set_batched_take_out(self, unsolved_linear=True):

@@ -96,7 +96,7 @@ __device__ __forceinline__ void load_minv(const T* __restrict__ minv, int row, T
 // Group-wide sums of N values: the CTA sum (warp 0 adds the threads' values in order), then, for a group of several
 // CTAs, thread 0 publishes it (part: 2 slots x 2 values per CTA; the reductions of an iteration alternate slots, so a
 // CTA that runs ahead never overwrites a sum another CTA has still to read), arrives with release semantics and polls
-// (bounded) with acquire semantics; lanes of warp 0 load the group's sums (at most 128 CTAs) in a fixed assignment
+// (bounded) with acquire semantics; lanes of warp 0 load the group's sums (at most 256 CTAs) in a fixed assignment
 // and the butterfly adds them.
 // The sums are valid in warp 0; false (in warp 0) when the wait gave up.
 template <int N>
@@ -124,14 +124,15 @@ __device__ __forceinline__ bool group_sum(double (&v)[N], double* sfull, double*
   __syncwarp();
   ok = __shfl_sync(0xffffffffu, ok, 0);
   if (!ok) return false;
-  double t[4][N];  // lane b adds the sums of CTAs b, b + 32, b + 64, b + 96 (groups of at most 128), loads in flight
+  double t[8][N];  // lane b adds the sums of CTAs b, b + 32, ..., b + 224 (groups of at most 256), loads in flight
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < 8; ++u)
 #pragma unroll
     for (int k = 0; k < N; ++k)
       t[u][k] = lane + 32 * u < size ? __ldcg(part + ((size_t)(first + lane + 32 * u) * 2 + slot) * 2 + k) : 0.0;
 #pragma unroll
-  for (int k = 0; k < N; ++k) v[k] = warp_sum((t[0][k] + t[1][k]) + (t[2][k] + t[3][k]));
+  for (int k = 0; k < N; ++k)
+    v[k] = warp_sum(((t[0][k] + t[1][k]) + (t[2][k] + t[3][k])) + ((t[4][k] + t[5][k]) + (t[6][k] + t[7][k])));
   return true;
 }
 
@@ -771,29 +772,36 @@ void launch_instance_step(double* u, const double* u_old, const double* corr, in
   instance_step_kernel<<<n_inst, 256, 0, s>>>(u, u_old, corr, node_off, step);
 }
 
-// variants: 0 rows loop (state in the work arrays), 1 one row per thread (state in registers), 2 / 3 four / eight
-// threads per row with the matrix in shared memory
+// variants: 0 rows loop (state in the work arrays), 1 one row per thread (state in registers), 2 / 3 / 5 four /
+// eight / sixteen threads per row with the matrix in shared memory (4, the cluster kernel, launches separately)
+static int threads_per_row(int variant) { return variant == 2 ? 4 : (variant == 3 ? 8 : (variant == 5 ? 16 : 1)); }
+
 static const void* batched_kernel(bool fp32, int variant) {
   if (fp32) {
     switch (variant) {
       case 0: return (const void*)batched_pcg_kernel<float, false>;
       case 1: return (const void*)batched_pcg_kernel<float, true>;
       case 2: return (const void*)batched_pcg_smem_kernel<float, 4>;
-      default: return (const void*)batched_pcg_smem_kernel<float, 8>;
+      case 3: return (const void*)batched_pcg_smem_kernel<float, 8>;
+      default: return (const void*)batched_pcg_smem_kernel<float, 16>;
     }
   }
   switch (variant) {
     case 0: return (const void*)batched_pcg_kernel<double, false>;
     case 1: return (const void*)batched_pcg_kernel<double, true>;
     case 2: return (const void*)batched_pcg_smem_kernel<double, 4>;
-    default: return (const void*)batched_pcg_smem_kernel<double, 8>;
+    case 3: return (const void*)batched_pcg_smem_kernel<double, 8>;
+    default: return (const void*)batched_pcg_smem_kernel<double, 16>;
   }
 }
 
 static int batched_smem_bytes(bool fp32, int variant) {
-  if (variant < 2) return 0;
-  if (fp32) return variant == 2 ? SmemCfg<float, 4>::kBytes : SmemCfg<float, 8>::kBytes;
-  return variant == 2 ? SmemCfg<double, 4>::kBytes : SmemCfg<double, 8>::kBytes;
+  switch (threads_per_row(variant)) {
+    case 4: return fp32 ? SmemCfg<float, 4>::kBytes : SmemCfg<double, 4>::kBytes;
+    case 8: return fp32 ? SmemCfg<float, 8>::kBytes : SmemCfg<double, 8>::kBytes;
+    case 16: return fp32 ? SmemCfg<float, 16>::kBytes : SmemCfg<double, 16>::kBytes;
+    default: return 0;
+  }
 }
 
 int batched_pcg_capacity(bool fp32, int variant, int sms) {
@@ -855,9 +863,14 @@ cudaError_t launch_batched_pcg_cluster(const Bsr& A, const void* minv, const dou
                             node_off, cluster_inst, (float*)xw, (float*)rw, (float*)zw, (float*)p0, (float*)p1, rtol,
                             max_iter, chunk, first_launch, st, its, flag, relres);
 }
-int batched_pcg_rows_per_cta(int variant) { return variant == 2 ? kBatchThreads / 4 : (variant == 3 ? kBatchThreads / 8 : kBatchThreads); }
+int batched_pcg_rows_per_cta(int variant) { return kBatchThreads / threads_per_row(variant); }
 int batched_pcg_max_width(int variant) {
-  return variant == 2 ? 4 * SmemCfg<float, 4>::kU : (variant == 3 ? 8 * SmemCfg<float, 8>::kU : 1 << 30);
+  switch (threads_per_row(variant)) {
+    case 4: return 4 * SmemCfg<float, 4>::kU;
+    case 8: return 8 * SmemCfg<float, 8>::kU;
+    case 16: return 16 * SmemCfg<float, 16>::kU;
+    default: return 1 << 30;
+  }
 }
 
 cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, int variant, const void* minv, const double* b, double* x_out,

@@ -1235,7 +1235,8 @@ namespace ikr_host {
 // the variants with few rows per CTA go first, as
 // their iterations are the shortest: eight, then four threads per row with the matrix in shared memory, then one row
 // per thread (instance i gets C_i = ceil(rows_i / rows per CTA) CTAs) -- the first whose groups fit the co-resident
-// CTAs of that variant (and at most 128 CTAs per group, rows of at most the variant's blocks).  Otherwise C_i ~ its
+// CTAs of that variant (and at most 256 CTAs per group, rows of at most the variant's blocks); FP64 tries sixteen
+// threads per row first (its iteration is bound by the FP64 pipe: fewer rows per SM).  Otherwise C_i ~ its
 // rows over the smallest rows-per-CTA q (>= 64 rows per CTA) whose groups fit the variant that loops over rows, and
 // when there are more instances than resident CTAs every group is one CTA (an ordinary launch; no CTA waits on
 // another).  Largest instances first.
@@ -1270,8 +1271,8 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const 
     }
   }
   std::vector<int> cand;
-  if (P.variant >= 0 && P.variant <= 3) cand.push_back(P.variant);
-  else if (P.variant == -1) cand = {3, 2, 1};
+  if (P.variant >= 0 && P.variant != 4) cand.push_back(P.variant);
+  else if (P.variant == -1) cand = fp32 ? std::vector<int>{3, 2, 1} : std::vector<int>{5, 3, 2, 1};
   for (int v : cand) {
     if (v == 0) break;
     const int rpc = ikr::batched_pcg_rows_per_cta(v), maxw = ikr::batched_pcg_max_width(v);
@@ -1279,7 +1280,7 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const 
     int64_t tot = 0;
     for (int k = 0; k < nr_ && fits; ++k) {
       const int ck = std::max(1, (rows[k] + rpc - 1) / rpc);
-      fits = ck <= 128 && width[k] <= maxw;
+      fits = ck <= 256 && width[k] <= maxw;
       c[k] = ck;
       tot += ck;
     }
@@ -1759,7 +1760,7 @@ int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations) {
 }
 int ikr_newton_set_batched_cg(ikr_nr nr, int32_t variant, int32_t first_chunk) {
   return guarded([&] {
-    need(nr && first_chunk >= 0 && variant >= -1 && variant <= 4, IKR_ERR_ARG, "invalid argument");
+    need(nr && first_chunk >= 0 && variant >= -1 && variant <= 5, IKR_ERR_ARG, "invalid argument");
     nr->plan.variant = variant;
     nr->plan.first_chunk = first_chunk ? first_chunk : 128;
   });

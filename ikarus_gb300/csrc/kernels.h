@@ -293,9 +293,9 @@ cudaError_t launch_pcg_persistent2(const Bsr& A, PcgWork& w0, PcgWork& w1, int v
 // batched.cu -- independent instances (disjoint contiguous node ranges) of one element set
 // One launch continues (first_launch: starts) the block-Jacobi PCG of the instances its CTAs serve, for at most
 // `chunk` iterations: instance i is served by the CTAs cta_first .. + cta_size - 1 listed per CTA (cta_inst,
-// cta_first, cta_size; groups contiguous, at most 128 CTAs).  variant 0: a thread loops over rows with the state in
+// cta_first, cta_size; groups contiguous, at most 256 CTAs).  variant 0: a thread loops over rows with the state in
 // the work arrays; 1: one row per thread (rows per CTA <= batched_pcg_rows_per_cta), the row's state in registers;
-// 2 / 3: four / eight threads per row, the CTA's matrix blocks in shared memory (rows per CTA <=
+// 2 / 3 / 5: four / eight / sixteen threads per row, the CTA's matrix blocks in shared memory (rows per CTA <=
 // batched_pcg_rows_per_cta, blocks per row <= batched_pcg_max_width).  xw..qw are node-padded work vectors of the
 // whole set, rtol per instance; st (4 doubles), its and flag per instance carry the solve between launches (flag 0
 // running, 1 finished, 2 breakdown, -1 a wait gave up); x_out gets an instance's correction when it finishes.  part

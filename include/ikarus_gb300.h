@@ -483,10 +483,10 @@ int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations);
 /* batched solves (no reference counterpart): the CG of a Newton iteration runs as launches of first_chunk (0: 128),
  * then twice as many iterations (at most 4096 unless first_chunk is larger), each re-planned over the instances
  * still running.  variant -1 lets the planner choose the kernel variant per launch (the first that fits of: in
- * FP32 one instance per 16-CTA thread-block cluster with vectors in distributed shared memory; eight or four threads
- * per row with the matrix in shared memory; one row per thread; rows looped per thread); 0..4 keeps variant 0 (row
- * loop), 1 (one row per thread), 2 (four threads per row), 3 (eight) or 4 (clusters, FP32) where it fits, else the
- * row loop.  For tests and tuning; the results agree to rounding.  batched_cg_launches: launches since creation. */
+ * FP32 one instance per 16-CTA thread-block cluster with vectors in distributed shared memory; sixteen (FP64 only),
+ * eight or four threads per row with the matrix in shared memory; one row per thread; rows looped per thread); 0..5
+ * keeps variant 0 (row loop), 1 (one row per thread), 2 (four threads per row), 3 (eight), 4 (clusters, FP32) or 5
+ * (sixteen threads per row) where it fits, else the row loop.  For tests and tuning; the results agree to rounding.  batched_cg_launches: launches since creation. */
 int ikr_newton_set_batched_cg(ikr_nr nr, int32_t variant, int32_t first_chunk);
 int ikr_newton_batched_cg_launches(ikr_nr nr, int64_t* n);
 /* batched solves (no reference counterpart): unsolved_linear = 1 takes out an instance whose CG ends above its

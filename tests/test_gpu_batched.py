@@ -139,13 +139,13 @@ _CHUNK_REF = {}
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-@pytest.mark.parametrize("variant,first_chunk", [(-1, 0), (0, 0), (1, 0), (2, 0), (3, 0), (4, 0), (-1, 3), (0, 5),
-                                                   (1, 1), (2, 4), (3, 2), (4, 3)])
+@pytest.mark.parametrize("variant,first_chunk", [(-1, 0), (0, 0), (1, 0), (2, 0), (3, 0), (4, 0), (5, 0), (-1, 3),
+                                                   (0, 5), (1, 1), (2, 4), (3, 2), (4, 3), (5, 2)])
 def test_chunked_cg_launches_of_every_variant_match_the_oracle(ikr, precision, variant, first_chunk, parity_log):
     """The batched CG continues each instance's PCG across launches of a few iterations, re-planned over the
     instances still running (first_chunk 1..5: every solve spans many launches); every kernel variant (0 row loop,
-    1 one row per thread, 2 / 3 four / eight threads per row with the matrix in shared memory, 4 one instance per
-    thread-block cluster -- FP32; FP64 runs fall back to the row loop --, -1 the planner's choice) gives converged displacements that match the oracle's solves (FP64 1e-8 at ||R|| <= 1e-9 ||R0||; mixed
+    1 one row per thread, 2 / 3 / 5 four / eight / sixteen threads per row with the matrix in shared memory, 4 one
+    instance per thread-block cluster -- FP32; FP64 runs fall back to the row loop --, -1 the planner's choice) gives converged displacements that match the oracle's solves (FP64 1e-8 at ||R|| <= 1e-9 ||R0||; mixed
     1e-8 at 1e-8)."""
     bp = problems.batched_cantilevers(n=7, seed=11, nx=(3, 9), nyz=(1, 3), E=(1e3, 1e4), t=(0.1, 0.5), load_steps=3)
     fes, asm = problems.build_gpu_batched(bp, precision=precision)
