@@ -1236,7 +1236,8 @@ namespace ikr_host {
 // their iterations are the shortest: eight, then four threads per row with the matrix in shared memory, then one row
 // per thread (instance i gets C_i = ceil(rows_i / rows per CTA) CTAs) -- the first whose groups fit the co-resident
 // CTAs of that variant (and at most 256 CTAs per group, rows of at most the variant's blocks); FP64 tries sixteen
-// threads per row first (its iteration is bound by the FP64 pipe: fewer rows per SM).  Otherwise C_i ~ its
+// threads per row first (its iteration is bound by the FP64 pipe: fewer rows per SM), for groups of at most 64 CTAs.
+// Otherwise C_i ~ its
 // rows over the smallest rows-per-CTA q (>= 64 rows per CTA) whose groups fit the variant that loops over rows, and
 // when there are more instances than resident CTAs every group is one CTA (an ordinary launch; no CTA waits on
 // another).  Largest instances first.
@@ -1278,9 +1279,12 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const 
     const int rpc = ikr::batched_pcg_rows_per_cta(v), maxw = ikr::batched_pcg_max_width(v);
     bool fits = true;
     int64_t tot = 0;
+    // sixteen threads per row pays (FP64) while groups stay small; beyond 64 CTAs the wider group barrier costs more
+    // than the spread FP64 work saves (measured on one 2 673-row instance: 23.3 against 20.5 us per iteration)
+    const int max_group = v == 5 ? 64 : 256;
     for (int k = 0; k < nr_ && fits; ++k) {
       const int ck = std::max(1, (rows[k] + rpc - 1) / rpc);
-      fits = ck <= 256 && width[k] <= maxw;
+      fits = ck <= max_group && width[k] <= maxw;
       c[k] = ck;
       tot += ck;
     }
