@@ -4,10 +4,10 @@
 // batched_pcg_kernel runs the block-Jacobi PCG of many instances in one launch.  Each instance gets a group of CTAs
 // (the host sizes the groups so that all CTAs are co-resident); the CTAs of a group split the instance's block rows
 // into contiguous chunks, one thread per row.  An iteration has two group-wide reductions (p.q, then r.z and r.r):
-// every CTA sums its threads' values (FP64 additions by one warp) and publishes the sum -- FP64: arrival on the
-// instance's barrier counter with release semantics, a bounded wait for the group, then lanes of warp 0 load the
-// CTAs' sums; FP32: the sum as a tagged word, polled directly -- and the butterfly adds them, so alpha, beta and the
-// convergence decision are identical in the group's CTAs and run to run.  A one-CTA group needs no global barrier.  p_new = z + beta p_old is formed on the fly for every gathered
+// every CTA sums its threads' values (FP64 additions by one warp), publishes the sum, arrives on the instance's
+// barrier counter with release semantics and waits (bounded) for the group; lane b of warp 0 then loads CTA b's sum
+// and the butterfly adds them, so alpha, beta and the convergence decision are identical in the group's CTAs and run
+// to run.  A one-CTA group needs no global barrier.  p_new = z + beta p_old is formed on the fly for every gathered
 // neighbour, which removes the barrier a separate p update would need.
 //
 // The solves of a Newton iteration are latency-bound: a hard instance needs thousands of iterations after the easy
@@ -136,84 +136,6 @@ __device__ __forceinline__ bool group_sum(double (&v)[N], double* sfull, double*
   return true;
 }
 
-// The FP32 form's group sums: the CTA sum (FP64, as above) is published as N 64-bit words {tag, FP32 value} with
-// release stores, and lane b of warp 0 polls (acquire, bounded) the words of CTA b until they carry this reduction's
-// tag, so arrival and data arrive in one L2 round trip instead of a counter poll followed by the loads.  The words
-// are zeroed before every launch (tag 0 never matches) and the tag is the launch's reduction number, so a word
-// always belongs to this launch; the slots alternate as above.  Rounding a CTA sum to FP32 costs nothing the FP32
-// vectors have not already lost; the group's sum is formed in FP64 in a fixed order.
-template <int N>
-__device__ __forceinline__ bool group_sum_tagged(double (&v)[N], double* sfull, double* part, int first, int size,
-                                                 int slot, unsigned int tag) {
-  cta_reduce_smem<N>(v, sfull);
-  if (threadIdx.x >= 32 || size == 1) return true;
-  const int lane = threadIdx.x;
-  unsigned long long* words = reinterpret_cast<unsigned long long*>(part);
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      const unsigned long long w =
-          ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(__double2float_rn(v[k]));
-      asm volatile("st.release.gpu.global.b64 [%0], %1;" ::"l"(words + ((size_t)blockIdx.x * 2 + slot) * 2 + k),
-                   "l"(w)
-                   : "memory");
-    }
-  }
-  __syncwarp();
-  float val[8][N];
-  unsigned got = 0;  // bit u * N + k: word (u, k) seen with this tag
-  unsigned need = 0;
-#pragma unroll
-  for (int u = 0; u < 8; ++u)
-#pragma unroll
-    for (int k = 0; k < N; ++k) {
-      val[u][k] = 0.f;
-      if (lane + 32 * u < size) need |= 1u << (u * N + k);
-    }
-  bool ok = false;
-  for (int i = 0; i < kGroupSpinLimit; ++i) {
-#pragma unroll
-    for (int u = 0; u < 8; ++u)
-#pragma unroll
-      for (int k = 0; k < N; ++k) {
-        const unsigned bit = 1u << (u * N + k);
-        if ((need & bit) && !(got & bit)) {
-          unsigned long long w;
-          asm volatile("ld.acquire.gpu.global.b64 %0, [%1];"
-                       : "=l"(w)
-                       : "l"(words + ((size_t)(first + lane + 32 * u) * 2 + slot) * 2 + k)
-                       : "memory");
-          if ((unsigned)(w >> 32) == tag) {
-            val[u][k] = __uint_as_float((unsigned)w);
-            got |= bit;
-          }
-        }
-      }
-    if (__all_sync(0xffffffffu, got == need)) {
-      ok = true;
-      break;
-    }
-    if (i > 32) __nanosleep(32);
-  }
-  if (!ok) return false;
-#pragma unroll
-  for (int k = 0; k < N; ++k) {
-    double t = 0.0;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) t += double(val[u][k]);
-    v[k] = warp_sum(t);
-  }
-  return true;
-}
-
-// the group sums of a kernel over T: tagged words in FP32, the counter in FP64
-template <typename T, int N>
-__device__ __forceinline__ bool group_sum_t(double (&v)[N], double* sfull, double* part, int first, int size, int slot,
-                                            unsigned int* counter, unsigned int bar) {
-  if constexpr (sizeof(T) == 4) return group_sum_tagged<N>(v, sfull, part, first, size, slot, bar);
-  else return group_sum<N>(v, sfull, part, first, size, slot, counter, bar * (unsigned)size);
-}
-
 // Continues (or, on the first launch of a solve, starts) the PCG of every instance the launch's CTAs serve, for at
 // most `chunk` iterations.  flag per instance on return: 0 still running, 1 finished (r.r <= rtol^2 b.b or max_iter
 // reached), 2 breakdown (p.q not positive and finite; the current iterate stands), -1 a wait gave up.  x_out gets
@@ -267,7 +189,7 @@ __global__ void __launch_bounds__(kBatchThreads, REG ? 2 : 3) batched_pcg_kernel
       lrr += double(r_.x) * double(r_.x) + double(r_.y) * double(r_.y) + double(r_.z) * double(r_.z);
     }
     double v[2] = {double(lrz), lrr};
-    const bool ok = group_sum_t<T, 2>(v, sfull, part, first, size, 1, counter, ++bars);
+    const bool ok = group_sum<2>(v, sfull, part, first, size, 1, counter, (++bars) * size);
     if (threadIdx.x == 0) {
       rz = v[0], bb = v[1], rr = v[1];
       s_state = ok ? 0 : -1;
@@ -316,7 +238,7 @@ __global__ void __launch_bounds__(kBatchThreads, REG ? 2 : 3) batched_pcg_kernel
       }
     }
     double v1[1] = {double(lpq)};
-    const bool ok1 = group_sum_t<T, 1>(v1, sfull, part, first, size, 0, counter, ++bars);
+    const bool ok1 = group_sum<1>(v1, sfull, part, first, size, 0, counter, (++bars) * size);
     if (threadIdx.x == 0) {
       if (!ok1) {
         s_state = -1;
@@ -356,7 +278,7 @@ __global__ void __launch_bounds__(kBatchThreads, REG ? 2 : 3) batched_pcg_kernel
       }
     }
     double v2[2] = {double(lrz), lrr};
-    const bool ok2 = group_sum_t<T, 2>(v2, sfull, part, first, size, 1, counter, ++bars);
+    const bool ok2 = group_sum<2>(v2, sfull, part, first, size, 1, counter, (++bars) * size);
     ++it;
     if (threadIdx.x == 0) {
       if (!ok2) {
@@ -463,7 +385,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_pcg_smem_kernel(
       lrr = double(rv.x) * double(rv.x) + double(rv.y) * double(rv.y) + double(rv.z) * double(rv.z);
     }
     double v[2] = {double(lrz), lrr};
-    const bool ok = group_sum_t<T, 2>(v, sfull, part, first, size, 1, counter, ++bars);
+    const bool ok = group_sum<2>(v, sfull, part, first, size, 1, counter, (++bars) * size);
     if (tid == 0) {
       rz = v[0], bb = v[1], rr = v[1];
       s_state = ok ? 0 : -1;
@@ -531,7 +453,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_pcg_smem_kernel(
       lpq = pr.x * a0 + pr.y * a1 + pr.z * a2;
     }
     double v1[1] = {double(lpq)};
-    const bool ok1 = group_sum_t<T, 1>(v1, sfull, part, first, size, 0, counter, ++bars);
+    const bool ok1 = group_sum<1>(v1, sfull, part, first, size, 0, counter, (++bars) * size);
     if (tid == 0) {
       if (!ok1) {
         s_state = -1;
@@ -556,7 +478,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batched_pcg_smem_kernel(
       lrr = double(rv.x) * double(rv.x) + double(rv.y) * double(rv.y) + double(rv.z) * double(rv.z);
     }
     double v2[2] = {double(lrz), lrr};
-    const bool ok2 = group_sum_t<T, 2>(v2, sfull, part, first, size, 1, counter, ++bars);
+    const bool ok2 = group_sum<2>(v2, sfull, part, first, size, 1, counter, (++bars) * size);
     ++it;
     if (tid == 0) {
       if (!ok2) {
@@ -959,10 +881,6 @@ cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, int variant, const void*
                                bool cooperative, cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(counters, 0, sizeof(unsigned int) * n_inst, s);
   if (e != cudaSuccess) return e;
-  if (fp32) {  // the tagged sum words of this launch start with tag 0
-    e = cudaMemsetAsync(part, 0, sizeof(double) * 4 * (size_t)n_cta, s);
-    if (e != cudaSuccess) return e;
-  }
   Bsr Acopy = A;
   const void* val = A.val;
   void* args[] = {&Acopy, &val,  &minv, &b,  &x_out, &node_off, &cta_inst, &cta_first, &cta_size,
