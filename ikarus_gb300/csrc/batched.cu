@@ -18,6 +18,10 @@
 // x, r, z, p, q and block-Jacobi inverse in registers for the whole launch; otherwise (GEN) a thread loops over its
 // rows with the state in the work arrays.  Every wait on a barrier is bounded; a wait that gives up ends the
 // instance with flag -1.
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "cg_common.cuh"
 #include "cg_grid.cuh"
 
@@ -804,15 +808,28 @@ static int batched_smem_bytes(bool fp32, int variant) {
   }
 }
 
-int batched_pcg_capacity(bool fp32, int variant, int sms) {
+// resident CTAs per SM of every variant, queried once per device (the planner asks before every launch)
+static int blocks_per_sm(bool fp32, int variant) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, bool, int>, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_tuple(dev, fp32, variant);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
   const void* k = batched_kernel(fp32, variant);
   const int smem = batched_smem_bytes(fp32, variant);
-  if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-    return 0;
   int b = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kBatchThreads, smem) != cudaSuccess) return 0;
-  return b * sms;
+  if (smem > 48 * 1024 && cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    b = 0;
+  else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, kBatchThreads, smem) != cudaSuccess)
+    b = 0;
+  cache[key] = b;
+  return b;
 }
+
+int batched_pcg_capacity(bool fp32, int variant, int sms) { return blocks_per_sm(fp32, variant) * sms; }
 
 int batched_pcg_threads() { return kBatchThreads; }
 
@@ -826,7 +843,7 @@ static cudaError_t cluster_prepare() {
   return cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
 }
 
-int batched_cluster_capacity() {
+static int cluster_capacity_query() {
   if (cluster_prepare() != cudaSuccess) return 0;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(kClusterCtas);
@@ -840,6 +857,17 @@ int batched_cluster_capacity() {
   int n = 0;
   if (cudaOccupancyMaxActiveClusters(&n, (const void*)batched_pcg_cluster_kernel, &cfg) != cudaSuccess) return 0;
   return n;
+}
+
+int batched_cluster_capacity() {
+  static std::mutex mu;
+  static std::map<int, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  return cache[dev] = cluster_capacity_query();
 }
 
 cudaError_t launch_batched_pcg_cluster(const Bsr& A, const void* minv, const double* b, double* x_out, int n_clusters,
