@@ -721,13 +721,12 @@ def run_batched(args):
                "batched_cg_launches_per_run": nr.batched_cg_launches() // (args.warmup + args.steps)}
         if esc:
             escalated = lc.escalated()
-            _, _, conv64 = esc[2].instance_info()
             rec["escalated_to_fp64"] = int(escalated.sum())
             rec["escalated"] = [int(i) for i in np.nonzero(escalated)[0]]
             rec["escalated_after"] = {"element_inversion": int((escalated & (conv == -1)).sum()),
                                       "no_convergence_in_maxIter": int((escalated & (conv == -2)).sum()),
                                       "cg_unsolved_in_fp32": int((escalated & (conv == -4)).sum())}
-            conv[escalated] = conv64[escalated]
+            conv = lc.instance_status()
         rec.update({"instances_converged_last_step": int((conv == 1).sum()),
                     "instances_taken_out_element_inversion": int((conv == -1).sum()),
                     "instances_taken_out_not_converged": int((conv == -2).sum()),

@@ -179,6 +179,8 @@ SIGNATURES = {
     "ikr_newton_set_batched_take_out": ([_vp, _I], C.c_int),
     "ikr_load_control_set_escalation": ([_vp, _vp, _vp], C.c_int),
     "ikr_load_control_escalated": ([_vp, _I, _u8p], C.c_int),
+    "ikr_load_control_set_escalation_concurrent": ([_vp, _I], C.c_int),
+    "ikr_load_control_instance_status": ([_vp, _I, _ip], C.c_int),
     "ikr_fes_num_colours": ([_vp, _ip], C.c_int),
     "ikr_fes_kernel_info": ([_vp, _ip, _ip, _ip], C.c_int),
     "ikr_fes_set_material": ([_vp, _I], C.c_int),
@@ -1325,6 +1327,19 @@ class LoadControl:
         self._esc = (solver, req)
         _err(lib().ikr_load_control_set_escalation(self.h, solver.h if solver else None, req.h if req else None),
              "escalation")
+
+    def set_escalation_concurrent(self, on=True):
+        """Solve the instances escalated in earlier steps on a second host thread and stream while this run's solver
+        does the step (default), or one after the other."""
+        _err(lib().ikr_load_control_set_escalation_concurrent(self.h, int(bool(on))))
+
+    def instance_status(self):
+        """Per instance: the status of the solver that holds it at the end of the last run (1 converged; -1, -2, -4
+        taken out)."""
+        n = self.nonLinearSolver.assembler.fes.n_instances
+        st = np.zeros(n, dtype=np.int32)
+        _err(lib().ikr_load_control_instance_status(self.h, n, _ptr(st, C.c_int32)))
+        return st
 
     def escalated(self):
         """Per instance: escalated in the last run."""

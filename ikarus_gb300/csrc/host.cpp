@@ -1,6 +1,9 @@
 // Host layer of the GB300-native Newton-Raphson / LoadControl path: the C ABI of include/ikarus_gb300.h.
 // Kernels live in element.cu, element_eas.cu, sparse.cu, solver.cu; shared internals in host_internal.h.
 #include "host_internal.h"
+
+#include <exception>
+#include <thread>
 // ------------------------------------------------------------------------------------------------------------
 namespace ikr_host {
 thread_local std::string g_last_error;
@@ -1254,10 +1257,11 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const 
   }
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rows[x] > rows[y]; });
   int variant = 0;
+  auto share = [&](int cap) { return std::max(1, (int)(cap * P.share)); };
   // FP32: one instance per 16-CTA cluster (vectors and sums in distributed shared memory) while the running
   // instances fit one cluster each and the device holds all their clusters at once
   if (fp32 && (P.variant == -1 || P.variant == 4)) {
-    bool fits = nr_ <= ikr::batched_cluster_capacity();
+    bool fits = nr_ <= share(ikr::batched_cluster_capacity());
     for (int k = 0; k < nr_ && fits; ++k)
       fits = rows[k] <= ikr::batched_cluster_rows() && width[k] <= ikr::batched_cluster_width();
     if (fits) {
@@ -1288,13 +1292,13 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const 
       c[k] = ck;
       tot += ck;
     }
-    if (fits && tot <= ikr::batched_pcg_capacity(fp32, v, sms)) {
+    if (fits && tot <= share(ikr::batched_pcg_capacity(fp32, v, sms))) {
       variant = v;
       break;
     }
   }
   if (variant == 0) {
-    const int cap = ikr::batched_pcg_capacity(fp32, 0, sms);
+    const int cap = share(ikr::batched_pcg_capacity(fp32, 0, sms));
     auto sizes_for = [&](int64_t q, std::vector<int>& out) {
       int64_t t = 0;
       for (int k = 0; k < nr_; ++k) {
@@ -1796,6 +1800,22 @@ int ikr_load_control_set_escalation(ikr_lc lc, ikr_nr nr64, ikr_req req64) {
     lc->esc_req = req64;
   });
 }
+int ikr_load_control_set_escalation_concurrent(ikr_lc lc, int32_t on) {
+  return guarded([&] {
+    need(lc, IKR_ERR_ARG, "null argument");
+    lc->esc_concurrent = on != 0;
+  });
+}
+int ikr_load_control_instance_status(ikr_lc lc, int32_t n, int32_t* status) {
+  return guarded([&] {
+    need(lc && status, IKR_ERR_ARG, "null argument");
+    const auto& conv = lc->nr->inst_conv;
+    for (int i = 0; i < n; ++i) {
+      const bool esc = i < (int)lc->escalated.size() && lc->escalated[i];
+      status[i] = esc ? lc->esc_conv[i] : (i < (int)conv.size() ? conv[i] : 0);
+    }
+  });
+}
 int ikr_load_control_escalated(ikr_lc lc, int32_t n, uint8_t* mask) {
   return guarded([&] {
     need(lc && mask, IKR_ERR_ARG, "null argument");
@@ -1845,6 +1865,7 @@ static void escalation_begin(ikr_lc lc, ikr_req r) {
   ikr_fes f = r->fes;
   const int ni = f->n_inst;
   lc->escalated.assign(ni, 0);
+  lc->esc_conv.assign(ni, 0);
   lc->esc_nr->inst_failed.assign(ni, 0);
   lc->esc_nr->inst_excluded.assign(ni, 1);
   ikr_req e = lc->esc_req;
@@ -1860,44 +1881,87 @@ static void copy_instance(ikr_fes f, double* dst, const double* src, int i, cuda
   CK(cudaMemcpyAsync(dst + o, src + o, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
 }
 
-// after the step's solve: the instances the solver took out in this step start again from the state at the step's
-// start in the escalation solver; every escalated instance's step is solved there and copied back
-static void escalation_step(ikr_lc lc, ikr_req r, double step, ikr_nr_info& ni) {
+// one step of the escalation solver over the instances in `sel` (the others kept out) at load factor lambda
+static ikr_nr_info escalation_solve(ikr_lc lc, double lambda, double step, const std::vector<uint8_t>& sel) {
+  ikr_nr en = lc->esc_nr;
+  ikr_req e = lc->esc_req;
+  const int ni = (int)sel.size();
+  for (int i = 0; i < ni; ++i) en->inst_excluded[i] = sel[i] ? 0 : 1;
+  e->lambda = lambda;
+  e->version++;
+  ikr_nr_info ei{};
+  nr_solve(en, e, step, &ei);
+  for (int i = 0; i < ni; ++i)
+    if (sel[i]) lc->esc_conv[i] = en->inst_conv[i];
+  return ei;
+}
+
+// A load step with escalation.  The instances escalated in earlier steps are solved by the escalation solver --
+// on a second host thread and its own stream, concurrently with the run's solver (esc_concurrent) -- while the run's
+// solver does the step for the others; then the instances the run's solver took out in this step start again from
+// the state at the step's start in the escalation solver, and every escalated instance's displacement is copied back.
+static void escalated_step(ikr_lc lc, ikr_req r, double step, double ref, ikr_nr_info& ni) {
   ikr_fes f = r->fes;
   ikr_req e = lc->esc_req;
-  ikr_nr en = lc->esc_nr;
-  const int ni_ = f->n_inst;
+  const int n_inst = f->n_inst;
+  const std::vector<uint8_t> old = lc->escalated;
+  const bool any_old = std::any_of(old.begin(), old.end(), [](uint8_t v) { return v != 0; });
+  const double lambda = r->lambda;
+  ikr_nr_info e1{}, e2{};
+  if (any_old && lc->esc_concurrent) {
+    std::exception_ptr err;
+    lc->nr->plan.share = 0.5;
+    lc->esc_nr->plan.share = 0.5;
+    std::thread worker([&] {
+      try {
+        e1 = escalation_solve(lc, lambda, step, old);
+      } catch (...) {
+        err = std::current_exception();
+      }
+    });
+    struct Join {  // the worker is joined however the run's solve ends
+      std::thread& t;
+      ikr_lc lc;
+      ~Join() {
+        if (t.joinable()) t.join();
+        lc->nr->plan.share = 1.0;
+        lc->esc_nr->plan.share = 1.0;
+      }
+    } join{worker, lc};
+    nr_solve(lc->nr, r, step, &ni, ref);
+    worker.join();
+    if (err) std::rethrow_exception(err);
+  } else {
+    nr_solve(lc->nr, r, step, &ni, ref);
+    if (any_old) e1 = escalation_solve(lc, lambda, step, old);
+  }
   CK(cudaStreamSynchronize(f->stream));
-  bool any = false;
-  for (int i = 0; i < ni_; ++i) {
+  std::vector<uint8_t> fresh(n_inst, 0);
+  bool any_fresh = false;
+  for (int i = 0; i < n_inst; ++i) {
     const int c = lc->nr->inst_conv[i];
     if (!lc->escalated[i] && (c == -1 || c == -2 || c == -4)) {
       copy_instance(f, e->u.p, lc->u_start.p, i, e->fes->stream);
       lc->escalated[i] = 1;
+      fresh[i] = 1;
+      any_fresh = true;
     }
-    any = any || lc->escalated[i];
   }
-  if (!any) return;
-  for (int i = 0; i < ni_; ++i) en->inst_excluded[i] = lc->escalated[i] ? 0 : 1;
-  e->lambda = r->lambda;
-  e->version++;
-  ikr_nr_info ei{};
-  nr_solve(en, e, step, &ei);
-  for (int i = 0; i < ni_; ++i)
-    if (lc->escalated[i]) copy_instance(f, r->u.p, e->u.p, i, e->fes->stream);
+  if (any_fresh) e2 = escalation_solve(lc, lambda, step, fresh);
+  bool any = false;
+  for (int i = 0; i < n_inst; ++i)
+    if (lc->escalated[i]) copy_instance(f, r->u.p, e->u.p, i, e->fes->stream), any = true;
   CK(cudaStreamSynchronize(e->fes->stream));
+  if (!any) return;
   r->version++;
   // the step succeeds when every instance is converged in one of the two solvers or taken out by the escalation
-  // solver too; the batch's Newton and CG iterations add up (the two solves run one after the other)
+  // solver too; Newton and CG iterations of both solvers add up
   bool ok = true;
-  for (int i = 0; i < ni_; ++i) {
-    if (lc->escalated[i]) ok = ok && en->inst_conv[i] != 0;
-    else ok = ok && lc->nr->inst_conv[i] != 0;
-  }
+  for (int i = 0; i < n_inst; ++i) ok = ok && (lc->escalated[i] ? lc->esc_conv[i] != 0 : lc->nr->inst_conv[i] != 0);
   ni.success = ok ? 1 : 0;
-  ni.iterations += ei.iterations;
-  ni.linear_iterations += ei.linear_iterations;
-  ni.residual_norm = std::max(ni.residual_norm, ei.residual_norm);
+  ni.iterations += e1.iterations + e2.iterations;
+  ni.linear_iterations += e1.linear_iterations + e2.linear_iterations;
+  ni.residual_norm = std::max({ni.residual_norm, any_old ? e1.residual_norm : 0.0, any_fresh ? e2.residual_norm : 0.0});
 }
 
 int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_info* infos, int32_t capacity) {
@@ -1940,8 +2004,8 @@ int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_in
           CK(cudaMemcpyAsync(lc->u_start.p, r->u.p, sizeof(double) * r->u.n, cudaMemcpyDeviceToDevice, r->fes->stream));
         }
         const double ref = predictor_apply(lc, r, ls);  // optional displacement prediction, FP64-gated
-        nr_solve(lc->nr, r, step, &ni, ref);
-        if (esc) escalation_step(lc, r, step, ni);
+        if (esc) escalated_step(lc, r, step, ref, ni);
+        else nr_solve(lc->nr, r, step, &ni, ref);
         if (ni.iterations == 0 && lc->nr->asm_->has_idbc) idbc_sync(lc->nr->asm_, r);  // loadcontrol.inl:43-44
         predictor_end_step(lc, r, ls);
         record(ni);

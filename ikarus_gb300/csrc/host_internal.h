@@ -1306,6 +1306,8 @@ struct ikr_nr_s {
     DBuf<int32_t> flag;          // per instance: 0 running, 1 finished, 2 breakdown, -1 a wait gave up
     int64_t launches = 0;        // batched CG launches since creation
     int variant = -1;            // -1: the planner's choice; 0..4 that variant where it fits, else the row loop
+    double share = 1.0;          // share of the device's co-resident CTAs a plan may use (0.5 while another
+                                 // solver's batched CG runs concurrently)
     int first_chunk = 128;       // iterations of a solve's first launch (doubling for the next ones, at most 4096)
   } plan;
 };
@@ -1321,6 +1323,10 @@ struct ikr_lc_s {
   ikr_nr esc_nr = nullptr;
   ikr_req esc_req = nullptr;
   std::vector<uint8_t> escalated;
+  std::vector<int8_t> esc_conv;  // status of each escalated instance in esc_nr (instance_info codes)
+  bool esc_concurrent = true;    // instances escalated in earlier steps are solved on a second host thread and
+                                 // stream while the run's solver does the step (each planner then uses half of the
+                                 // co-resident CTAs, so both cooperative launches fit the device at once)
   DBuf<double> u_start;
   std::vector<ControlObserver> obs;
   std::vector<std::unique_ptr<ListenerBase>> listeners;

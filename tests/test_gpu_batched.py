@@ -174,7 +174,7 @@ def test_chunked_cg_launches_of_every_variant_match_the_oracle(ikr, precision, v
                       worst, 1e-8)
 
 
-def _escalated_run(ikr, bp, primary_settings, take_out=True, observe=None):
+def _escalated_run(ikr, bp, primary_settings, take_out=True, observe=None, concurrent=True):
     fes, asm = problems.build_gpu_batched(bp, precision=1)
     nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(primary_settings,
                                                         ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
@@ -186,13 +186,17 @@ def _escalated_run(ikr, bp, primary_settings, take_out=True, observe=None):
     req64 = ikr.FERequirements(fes64)
     lc = ikr.LoadControl(nr, bp.load_steps)
     lc.set_escalation(nr64, req64)
+    lc.set_escalation_concurrent(concurrent)
     if observe:
         lc.subscribe(lambda msg, s: observe(msg, s, lc))
     req = ikr.FERequirements(fes)
     info = lc.run(req)
     _, _, conv = nr.instance_info()
-    _, _, conv64 = nr64.instance_info()
-    return info, req.globalSolution(), lc.escalated(), conv, conv64
+    status = lc.instance_status()
+    esc = lc.escalated()
+    assert (status[~esc] == conv[~esc]).all()
+    conv64 = np.where(esc, status, -3)
+    return info, req.globalSolution(), esc, conv, conv64
 
 
 def test_escalation_solves_in_fp64_what_the_fp32_solver_takes_out(ikr, parity_log):
@@ -212,10 +216,12 @@ def test_escalation_solves_in_fp64_what_the_fp32_solver_takes_out(ikr, parity_lo
     assert parity_log("batched escalation (all instances to FP64): max rel. error vs oracle", worst, 1e-8)
 
 
-def test_escalation_mid_run_starts_from_the_step_start(ikr, parity_log):
+@pytest.mark.parametrize("concurrent", [True, False])
+def test_escalation_mid_run_starts_from_the_step_start(ikr, concurrent, parity_log):
     """An FP32 solver allowed 3 Newton iterations per step takes out the instances that need more in some step;
     each continues in FP64 from the state at the start of that step (the converged state of the step before), and
-    the combined load path matches the oracle's (1e-8) for every instance."""
+    the combined load path matches the oracle's (1e-8) for every instance -- with the escalated instances' later
+    steps solved on a second thread and stream while the FP32 solver does the step, and one after the other."""
     bp = problems.batched_cantilevers(n=8, seed=5, nx=(3, 8), nyz=(1, 3), E=(1e2, 1e4), t=(0.1, 1.0), load_steps=4)
     st = ikr.NRSettings(tol=1e-8, maxIter=3, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
                         linear_rtol_min=1e-6)
@@ -226,7 +232,7 @@ def test_escalation_mid_run_starts_from_the_step_start(ikr, parity_log):
             for i in np.nonzero(lc.escalated())[0]:
                 first_step.setdefault(int(i), s["loadStep"])
 
-    info, u, esc, conv, conv64 = _escalated_run(ikr, bp, st, observe=observe)
+    info, u, esc, conv, conv64 = _escalated_run(ikr, bp, st, observe=observe, concurrent=concurrent)
     assert info.success
     assert ((conv == 1) | (esc & (conv64 == 1))).all()
     assert set(np.nonzero(esc)[0].tolist()) == set(first_step)
@@ -235,8 +241,8 @@ def test_escalation_mid_run_starts_from_the_step_start(ikr, parity_log):
         ref = oracle.from_problem(part).load_control(bp.load_steps, tol=1e-9, tol_mode=1, max_iter=30)["u"]
         worst = max(worst, np.abs(u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]] - ref).max()
                     / np.abs(ref).max())
-    assert parity_log(f"batched escalation mid-run (escalated at steps {sorted(first_step.values())}): max rel. "
-                      "error vs oracle", worst, 1e-8)
+    assert parity_log(f"batched escalation mid-run (concurrent={concurrent}, escalated at steps "
+                      f"{sorted(first_step.values())}): max rel. error vs oracle", worst, 1e-8)
 
 
 def test_escalated_instance_that_inverts_in_fp64_too_is_taken_out(ikr):
