@@ -1330,7 +1330,7 @@ class LoadControl:
 
     def set_escalation_concurrent(self, on=True):
         """Solve the instances escalated in earlier steps on a second host thread and stream while this run's solver
-        does the step (default), or one after the other."""
+        does the step, or one after the other (the default: measured faster)."""
         _err(lib().ikr_load_control_set_escalation_concurrent(self.h, int(bool(on))))
 
     def instance_status(self):

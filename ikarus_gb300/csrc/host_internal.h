@@ -1324,7 +1324,7 @@ struct ikr_lc_s {
   ikr_req esc_req = nullptr;
   std::vector<uint8_t> escalated;
   std::vector<int8_t> esc_conv;  // status of each escalated instance in esc_nr (instance_info codes)
-  bool esc_concurrent = true;    // instances escalated in earlier steps are solved on a second host thread and
+  bool esc_concurrent = false;   // instances escalated in earlier steps are solved on a second host thread and
                                  // stream while the run's solver does the step (each planner then uses half of the
                                  // co-resident CTAs, so both cooperative launches fit the device at once)
   DBuf<double> u_start;

@@ -501,9 +501,9 @@ int ikr_newton_set_batched_take_out(ikr_nr nr, int32_t unsolved_linear);
  * nr64 = req64 = NULL switches it off.  escalated: the instances escalated in the last run (one byte each). */
 int ikr_load_control_set_escalation(ikr_lc lc, ikr_nr nr64, ikr_req req64);
 int ikr_load_control_escalated(ikr_lc lc, int32_t n, uint8_t* mask);
-/* on = 1 (default): the instances escalated in earlier steps are solved by nr64 on a second host thread and its own
- * stream while the run's solver does the step (each batched CG plan then takes half of the co-resident CTAs); 0: one
- * after the other.  instance_status: per instance the status of the solver that holds it at the end of the last run
+/* on = 1: the instances escalated in earlier steps are solved by nr64 on a second host thread and its own stream
+ * while the run's solver does the step (each batched CG plan then takes half of the co-resident CTAs); 0 (default):
+ * one after the other, which measured faster (the halved plans cost more than the overlap gains).  instance_status: per instance the status of the solver that holds it at the end of the last run
  * (instance_info codes: 1 converged, -1, -2, -4 taken out). */
 int ikr_load_control_set_escalation_concurrent(ikr_lc lc, int32_t on);
 int ikr_load_control_instance_status(ikr_lc lc, int32_t n, int32_t* status);
