@@ -448,11 +448,12 @@ def finish(args, p, world, t_mixed, t_e2e, t_plain, plain_info, infos, launches,
     tf = os.path.join(ROOT, "profiles", "cg_dram_traffic.json")
     if os.path.exists(tf) and not args.small:
         try:
-            t = json.load(open(tf))
-            if t.get("cg_kernel_kind") == kind and abs(t.get("l2_keep_fraction", -1) - keep) < 1e-9:
-                # DRAM bytes per CG iteration of that kernel and L2 keep share, from one ncu capture
-                traffic = round(t["dram_bytes_per_iteration"] * iters_per_launch)
-        except (OSError, ValueError, KeyError):
+            caps = json.load(open(tf))
+            for t in (caps if isinstance(caps, list) else [caps]):
+                if t.get("cg_kernel_kind") == kind and abs(t.get("l2_keep_fraction", -1) - keep) < 1e-9:
+                    # DRAM bytes per CG iteration of that kernel and L2 keep share, from one ncu capture
+                    traffic = round(t["dram_bytes_per_iteration"] * iters_per_launch)
+        except (OSError, ValueError, KeyError, TypeError):
             traffic = None
 
     info0 = infos[-1]
