@@ -258,3 +258,48 @@ def test_escalated_instance_that_inverts_in_fp64_too_is_taken_out(ikr):
     assert info.success
     assert esc[bad] and conv64[bad] == -1 and conv[bad] in (-1, -4)
     assert (np.delete(conv, bad) == 1).all() and not np.delete(esc, bad).any()
+
+
+def test_escalation_without_failures_changes_nothing_and_bad_twins_are_rejected(ikr):
+    """With nothing taken out the escalated run is the plain run (same displacement bit for bit, nothing escalated);
+    an escalation solver over an element set with other instances, or a requirement of another set, is an ARG
+    error."""
+    bp = problems.batched_cantilevers(n=4, seed=3, nx=(3, 6), nyz=(1, 2), E=(1e3, 1e4), t=(0.1, 0.3), load_steps=2)
+    st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, eisenstat_walker=True, linear_rtol=1e-2,
+                        linear_rtol_min=1e-6)
+
+    def run(with_escalation):
+        fes, asm = problems.build_gpu_batched(bp, precision=1)
+        nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+        lc = ikr.LoadControl(nr, bp.load_steps)
+        keep = None
+        if with_escalation:
+            fes64, asm64 = problems.build_gpu_batched(bp, precision=0)
+            nr64 = ikr.NewtonRaphson(asm64, ikr.NewtonRaphsonConfig(
+                st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+            req64 = ikr.FERequirements(fes64)
+            lc.set_escalation(nr64, req64)
+            keep = (fes64, asm64, nr64, req64)
+        req = ikr.FERequirements(fes)
+        info = lc.run(req)
+        assert info.success
+        esc = lc.escalated() if with_escalation else None
+        return req.globalSolution(), esc, lc.instance_status() if with_escalation else None, keep
+
+    u0, _, _, _ = run(False)
+    u1, esc, status, _ = run(True)
+    assert not esc.any() and (status == 1).all()
+    assert np.array_equal(u0, u1)
+
+    fes, asm = problems.build_gpu_batched(bp, precision=1)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    lc = ikr.LoadControl(nr, bp.load_steps)
+    other = problems.batched_cantilevers(n=3, seed=4, nx=(3, 6), nyz=(1, 2), load_steps=2)
+    fes_o, asm_o = problems.build_gpu_batched(other, precision=0)
+    nr_o = ikr.NewtonRaphson(asm_o, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    with pytest.raises(ikr.IkarusError, match="ARG"):
+        lc.set_escalation(nr_o, ikr.FERequirements(fes_o))
+    fes64, asm64 = problems.build_gpu_batched(bp, precision=0)
+    nr64 = ikr.NewtonRaphson(asm64, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    with pytest.raises(ikr.IkarusError, match="ARG"):
+        lc.set_escalation(nr64, ikr.FERequirements(fes))
