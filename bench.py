@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--two-level-only", action="store_true",
                     help="only the two-level measurement (mixed and plain FP64 with the coarse correction)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cg-kernel", default="",
+                    help="mixed form's CG kernel as kind[:keep] (default: the autotuner's choice)")
     ap.add_argument("--ref-budget", type=float, default=240.0,
                     help="--impl reference: seconds after which no further load step is started (at least one runs)")
     ap.add_argument("--small", action="store_true", help="32x8x8 mesh (profiling runs)")
@@ -225,6 +227,9 @@ def run_ours(args, rank, world):
         if args.small else problems.config2(load_steps=args.load_steps)
     n_nodes = p.mesh.n_nodes
     mixed = Form(ikr, problems, p, mixed=True, predictor=args.predictor, eta=(args.eta_max, args.eta_min))
+    if args.cg_kernel:
+        kind, _, keep = args.cg_kernel.partition(":")
+        mixed.ls.set_kernel(int(kind), float(keep) if keep else -1.0)
     if args.tangent_kernel:
         mixed.asm.set_tangent_kernel(args.tangent_kernel)
     stream, ev0, ev1 = make_events(torch, mixed.fes.stream())
