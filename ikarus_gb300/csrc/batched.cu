@@ -14,10 +14,12 @@
 // ones have converged.  So the host runs a solve as a sequence of launches of at most `chunk` iterations each and
 // re-plans the groups over the instances still running before every launch: the state of every instance (its
 // vectors in the work arrays, rz, r.r, b.b, beta and the iteration count in `st` / `its`) carries over, the CG is
-// continued, not restarted.  When every running instance fits one row per thread (REG), a thread keeps its row's
-// x, r, z, p, q and block-Jacobi inverse in registers for the whole launch; otherwise (GEN) a thread loops over its
-// rows with the state in the work arrays.  Every wait on a barrier is bounded; a wait that gives up ends the
-// instance with flag -1.
+// continued, not restarted.  Kernel variants: batched_pcg_kernel with one row per thread (REG: the row's x, r, z,
+// p, q and block-Jacobi inverse in registers for the whole launch) or with a thread looping over its rows (GEN: the
+// state in the work arrays); batched_pcg_smem_kernel with four, eight or sixteen threads per row and the CTA's
+// matrix blocks in shared memory; and, in FP32, batched_pcg_cluster_kernel with one instance per thread-block
+// cluster and its vectors in distributed shared memory.  Every wait on a global barrier is bounded; a wait that gives
+// up ends the instance with flag -1.
 #include <map>
 #include <mutex>
 #include <tuple>
