@@ -833,7 +833,6 @@ static int blocks_per_sm(bool fp32, int variant) {
 
 int batched_pcg_capacity(bool fp32, int variant, int sms) { return blocks_per_sm(fp32, variant) * sms; }
 
-int batched_pcg_threads() { return kBatchThreads; }
 
 int batched_cluster_rows() { return kClusterCtas * kClusterThreads; }
 int batched_cluster_width() { return kClusterWidth; }

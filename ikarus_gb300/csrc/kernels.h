@@ -301,7 +301,6 @@ cudaError_t launch_pcg_persistent2(const Bsr& A, PcgWork& w0, PcgWork& w1, int v
 // running, 1 finished, 2 breakdown, -1 a wait gave up); x_out gets an instance's correction when it finishes.  part
 // holds 4 doubles per CTA, counters one per instance.  capacity = co-resident CTAs of the variant on the device.
 int batched_pcg_capacity(bool fp32, int variant, int sms);
-int batched_pcg_threads();
 int batched_pcg_rows_per_cta(int variant);
 int batched_pcg_max_width(int variant);
 cudaError_t launch_batched_pcg(const Bsr& A, bool fp32, int variant, const void* minv, const double* b, double* x_out,
