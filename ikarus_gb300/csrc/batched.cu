@@ -330,7 +330,6 @@ __global__ void __launch_bounds__(kBatchThreads, REG ? 2 : 3) batched_pcg_kernel
 // blocks (the host checks).
 template <typename T, int TPR>
 struct SmemCfg {
-  static constexpr int kRows = kBatchThreads / TPR;
   static constexpr int kU = (27 + TPR - 1) / TPR;  // blocks per thread: a hex node couples to at most 27 nodes
   static constexpr int kValBytes = 9 * kU * kBatchThreads * (int)sizeof(T);
   static constexpr int kBytes = kValBytes + kU * kBatchThreads * 4;
