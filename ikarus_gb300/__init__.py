@@ -176,6 +176,7 @@ SIGNATURES = {
     "ikr_newton_instance_linear_iterations": ([_vp, _i64p], C.c_int),
     "ikr_newton_set_batched_cg": ([_vp, _I, _I], C.c_int),
     "ikr_newton_batched_cg_launches": ([_vp, _i64p], C.c_int),
+    "ikr_newton_batched_cg_variant_launches": ([_vp, _i64p], C.c_int),
     "ikr_newton_set_batched_take_out": ([_vp, _I], C.c_int),
     "ikr_load_control_set_escalation": ([_vp, _vp, _vp], C.c_int),
     "ikr_load_control_escalated": ([_vp, _I, _u8p], C.c_int),
@@ -1269,6 +1270,12 @@ class NewtonRaphson:
         """Batched solves: an instance whose CG ends above its tolerance after linear_max_iter is taken out
         (status -4)."""
         _err(lib().ikr_newton_set_batched_take_out(self.h, int(bool(unsolved_linear))))
+
+    def batched_cg_variant_launches(self):
+        """Batched CG launches since creation per kernel variant 0..5."""
+        out = np.zeros(6, dtype=np.int64)
+        _err(lib().ikr_newton_batched_cg_variant_launches(self.h, _ptr(out, C.c_int64)))
+        return out
 
     def batched_cg_launches(self):
         n = C.c_int64()

@@ -1379,6 +1379,7 @@ static void batched_cg(ikr_nr nr, ikr_fes f, ikr_asm a, const std::vector<uint8_
                                  P.cooperative, s));
     count(1);
     ++P.launches;
+    ++P.launches_by_variant[P.cur_variant];
     first = false;
     chunk = std::min(2 * chunk, std::max(chunk, 4096));
     P.flag.download(flag.data(), ni, s);
@@ -1777,6 +1778,12 @@ int ikr_newton_batched_cg_launches(ikr_nr nr, int64_t* n) {
   return guarded([&] {
     need(nr && n, IKR_ERR_ARG, "null argument");
     *n = nr->plan.launches;
+  });
+}
+int ikr_newton_batched_cg_variant_launches(ikr_nr nr, int64_t* by_variant6) {
+  return guarded([&] {
+    need(nr && by_variant6, IKR_ERR_ARG, "null argument");
+    for (int v = 0; v < 6; ++v) by_variant6[v] = nr->plan.launches_by_variant[v];
   });
 }
 int ikr_newton_set_batched_take_out(ikr_nr nr, int32_t unsolved_linear) {

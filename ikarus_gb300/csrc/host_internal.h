@@ -1305,6 +1305,7 @@ struct ikr_nr_s {
     DBuf<double> st;             // rz, r.r, b.b, beta per instance between the launches of one solve
     DBuf<int32_t> flag;          // per instance: 0 running, 1 finished, 2 breakdown, -1 a wait gave up
     int64_t launches = 0;        // batched CG launches since creation
+    int64_t launches_by_variant[6] = {0, 0, 0, 0, 0, 0};
     int variant = -1;            // -1: the planner's choice; 0..4 that variant where it fits, else the row loop
     double share = 1.0;          // share of the device's co-resident CTAs a plan may use (0.5 while another
                                  // solver's batched CG runs concurrently)

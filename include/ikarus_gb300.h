@@ -489,6 +489,8 @@ int ikr_newton_instance_linear_iterations(ikr_nr nr, int64_t* cg_iterations);
  * (sixteen threads per row) where it fits, else the row loop.  For tests and tuning; the results agree to rounding.  batched_cg_launches: launches since creation. */
 int ikr_newton_set_batched_cg(ikr_nr nr, int32_t variant, int32_t first_chunk);
 int ikr_newton_batched_cg_launches(ikr_nr nr, int64_t* n);
+/* the same per kernel variant 0..5 (six values) */
+int ikr_newton_batched_cg_variant_launches(ikr_nr nr, int64_t* by_variant6);
 /* batched solves (no reference counterpart): unsolved_linear = 1 takes out an instance whose CG ends above its
  * tolerance after linear_max_iter (status -4 in instance_info; in FP32 the attainable accuracy of the tangent can lie
  * above the tolerance, and the direction is then no Newton direction) */

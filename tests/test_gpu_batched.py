@@ -170,8 +170,9 @@ def test_chunked_cg_launches_of_every_variant_match_the_oracle(ikr, precision, v
     worst = max(np.abs(u[3 * bp.node_offsets[i]:3 * bp.node_offsets[i + 1]] - ref).max() / np.abs(ref).max()
                 for i, ref in enumerate(_CHUNK_REF["u"]))
     form = "FP64" if precision == 0 else "mixed"
-    assert parity_log(f"batched {form}, variant={variant}, first_chunk={first_chunk}: max rel. error vs oracle",
-                      worst, 1e-8)
+    by = nr.batched_cg_variant_launches().tolist()
+    assert parity_log(f"batched {form}, variant={variant}, first_chunk={first_chunk} (launches per variant {by}): "
+                      "max rel. error vs oracle", worst, 1e-8)
 
 
 def _escalated_run(ikr, bp, primary_settings, take_out=True, observe=None, concurrent=True):
@@ -303,3 +304,26 @@ def test_escalation_without_failures_changes_nothing_and_bad_twins_are_rejected(
     nr64 = ikr.NewtonRaphson(asm64, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
     with pytest.raises(ikr.IkarusError, match="ARG"):
         lc.set_escalation(nr64, ikr.FERequirements(fes))
+
+
+@pytest.mark.parametrize("precision,variant", [(1, 1), (1, 2), (1, 3), (1, 4), (1, 5), (0, 1), (0, 2), (0, 3),
+                                               (0, 5)])
+def test_a_forced_variant_that_fits_is_the_one_launched(ikr, precision, variant):
+    """Three small instances fit every kernel variant (and, in FP32, three clusters of 16 CTAs): forcing a variant
+    launches that variant and no other; the planner's choice (-1) launches one of the fitting variants."""
+    bp = problems.batched_cantilevers(n=3, seed=3, nx=(3, 6), nyz=(1, 2), E=(1e3, 1e4), t=(0.1, 0.3), load_steps=1)
+    fes, asm = problems.build_gpu_batched(bp, precision=precision)
+    st = ikr.NRSettings(tol=1e-8, maxIter=30, relative=True, linear_rtol=1e-8)
+    nr = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    nr.set_batched_cg(variant=variant)
+    req = ikr.FERequirements(fes)
+    req.insertParameter(1.0)
+    assert nr.solve(req).success
+    by = nr.batched_cg_variant_launches()
+    assert by[variant] > 0 and by.sum() == by[variant] == nr.batched_cg_launches()
+    nr2 = ikr.NewtonRaphson(asm, ikr.NewtonRaphsonConfig(st, ikr.LinearSolver(ikr.SolverTypeTag.gpu_PCG_Batched)))
+    req2 = ikr.FERequirements(fes)
+    req2.insertParameter(1.0)
+    assert nr2.solve(req2).success
+    by2 = nr2.batched_cg_variant_launches()
+    assert by2[0] == 0 and by2.sum() > 0
