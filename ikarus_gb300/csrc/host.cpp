@@ -1233,8 +1233,8 @@ int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on) {
 namespace ikr_host {
 // Newton-Raphson over independent instances: every instance runs its own Newton iteration and relative
 // convergence test; one assembly and one batched CG launch (CTA per instance) serve all still-active instances.
-// CTA groups of one batched CG launch over the instances in `run`.  In FP32, while every running instance fits one
-// 16-CTA cluster and all their clusters fit the device at once, each instance gets a cluster (variant 4).  Otherwise
+// CTA groups of one batched CG launch over the instances in `run`.  In FP32, while every running instance has at most
+// 512 rows and all their clusters fit the device at once, each instance gets a 16-CTA cluster (variant 4).  Otherwise
 // the variants with few rows per CTA go first, as
 // their iterations are the shortest: eight, then four threads per row with the matrix in shared memory, then one row
 // per thread (instance i gets C_i = ceil(rows_i / rows per CTA) CTAs) -- the first whose groups fit the co-resident
@@ -1261,9 +1261,13 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const 
   // FP32: one instance per 16-CTA cluster (vectors and sums in distributed shared memory) while the running
   // instances fit one cluster each and the device holds all their clusters at once
   if (fp32 && (P.variant == -1 || P.variant == 4)) {
+    // chosen by the planner only for instances of at most 512 rows: its iteration grows with the rows per CTA (the
+    // distributed-shared-memory gathers of 27 blocks per thread), measured 8.4 us at 297 rows against 9.2 us for
+    // eight threads per row, but 15.2 against 9.2 us at 2 673 rows
+    const int max_rows = P.variant == 4 ? ikr::batched_cluster_rows() : std::min(512, ikr::batched_cluster_rows());
     bool fits = nr_ <= share(ikr::batched_cluster_capacity());
     for (int k = 0; k < nr_ && fits; ++k)
-      fits = rows[k] <= ikr::batched_cluster_rows() && width[k] <= ikr::batched_cluster_width();
+      fits = rows[k] <= max_rows && width[k] <= ikr::batched_cluster_width();
     if (fits) {
       std::vector<int32_t> ci(run.begin(), run.end());
       P.n_cta = nr_;
