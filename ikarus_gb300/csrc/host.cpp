@@ -1907,10 +1907,11 @@ static ikr_nr_info escalation_solve(ikr_lc lc, double lambda, double step, const
   return ei;
 }
 
-// A load step with escalation.  The instances escalated in earlier steps are solved by the escalation solver --
-// on a second host thread and its own stream, concurrently with the run's solver (esc_concurrent) -- while the run's
-// solver does the step for the others; then the instances the run's solver took out in this step start again from
-// the state at the step's start in the escalation solver, and every escalated instance's displacement is copied back.
+// A load step with escalation.  The run's solver does the step for the instances it holds; the instances it takes
+// out in this step start again from the state at the step's start in the escalation solver, which solves them
+// together with the instances escalated in earlier steps -- or, with esc_concurrent, the earlier ones on a second
+// host thread and stream while the run's solver works and the fresh ones after it.  Every escalated instance's
+// displacement is copied back.
 static void escalated_step(ikr_lc lc, ikr_req r, double step, double ref, ikr_nr_info& ni) {
   ikr_fes f = r->fes;
   ikr_req e = lc->esc_req;
@@ -1919,7 +1920,8 @@ static void escalated_step(ikr_lc lc, ikr_req r, double step, double ref, ikr_nr
   const bool any_old = std::any_of(old.begin(), old.end(), [](uint8_t v) { return v != 0; });
   const double lambda = r->lambda;
   ikr_nr_info e1{}, e2{};
-  if (any_old && lc->esc_concurrent) {
+  const bool overlap = any_old && lc->esc_concurrent;
+  if (overlap) {
     std::exception_ptr err;
     lc->nr->plan.share = 0.5;
     lc->esc_nr->plan.share = 0.5;
@@ -1944,21 +1946,21 @@ static void escalated_step(ikr_lc lc, ikr_req r, double step, double ref, ikr_nr
     if (err) std::rethrow_exception(err);
   } else {
     nr_solve(lc->nr, r, step, &ni, ref);
-    if (any_old) e1 = escalation_solve(lc, lambda, step, old);
   }
   CK(cudaStreamSynchronize(f->stream));
-  std::vector<uint8_t> fresh(n_inst, 0);
-  bool any_fresh = false;
+  // one after the other, the step's escalation solve takes the earlier and the fresh instances together (one Newton
+  // loop whose length is the slowest instance's); overlapped, the earlier ones are done and the fresh ones follow
+  std::vector<uint8_t> sel = overlap ? std::vector<uint8_t>(n_inst, 0) : old;
   for (int i = 0; i < n_inst; ++i) {
     const int c = lc->nr->inst_conv[i];
     if (!lc->escalated[i] && (c == -1 || c == -2 || c == -4)) {
       copy_instance(f, e->u.p, lc->u_start.p, i, e->fes->stream);
       lc->escalated[i] = 1;
-      fresh[i] = 1;
-      any_fresh = true;
+      sel[i] = 1;
     }
   }
-  if (any_fresh) e2 = escalation_solve(lc, lambda, step, fresh);
+  const bool any_sel = std::any_of(sel.begin(), sel.end(), [](uint8_t v) { return v != 0; });
+  if (any_sel) e2 = escalation_solve(lc, lambda, step, sel);
   bool any = false;
   for (int i = 0; i < n_inst; ++i)
     if (lc->escalated[i]) copy_instance(f, r->u.p, e->u.p, i, e->fes->stream), any = true;
@@ -1972,7 +1974,7 @@ static void escalated_step(ikr_lc lc, ikr_req r, double step, double ref, ikr_nr
   ni.success = ok ? 1 : 0;
   ni.iterations += e1.iterations + e2.iterations;
   ni.linear_iterations += e1.linear_iterations + e2.linear_iterations;
-  ni.residual_norm = std::max({ni.residual_norm, any_old ? e1.residual_norm : 0.0, any_fresh ? e2.residual_norm : 0.0});
+  ni.residual_norm = std::max({ni.residual_norm, overlap ? e1.residual_norm : 0.0, any_sel ? e2.residual_norm : 0.0});
 }
 
 int ikr_load_control_run(ikr_lc lc, ikr_req r, ikr_control_info* info, ikr_nr_info* infos, int32_t capacity) {
