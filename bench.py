@@ -77,6 +77,9 @@ def parse():
     ap.add_argument("--no-graphs", action="store_true", help="launch CG kernels one by one (for profilers)")
     ap.add_argument("--batched-eta-max", type=float, default=1e-2,
                     help="config 3: mixed form's Eisenstat-Walker upper bound (linear tolerance of the first iteration)")
+    ap.add_argument("--batched-trace", action="store_true",
+                    help="config 3: only the mixed and plain forms, with a per-Newton-iteration trace (wall time, "
+                         "largest per-instance CG count) summarised in the line")
     ap.add_argument("--batched-backtracks", type=int, default=8,
                     help="config 3: halvings of an instance's correction that inverts an element (0: take it out)")
     ap.add_argument("--backtracks", type=int, default=0,
@@ -708,7 +711,26 @@ def run_batched(args):
             esc = (fes64, asm64, nr64, req64)
         stream, ev0, ev1 = make_events(torch, fes.stream())
         times = []
+        trace = []
+        if args.batched_trace:
+            # per batch Newton iteration: wall time (the batched Newton synchronises every iteration) and the largest
+            # per-instance CG count, from the solver's observers
+            t_state = {"t": 0.0, "lin": None}
+
+            def on_nr(msg, s_):
+                if msg == ikr.NonLinearSolverMessages.INIT:
+                    t_state["t"] = time.perf_counter()
+                    t_state["lin"] = np.zeros(len(bp.parts), dtype=np.int64)
+                elif msg == ikr.NonLinearSolverMessages.ITERATION_ENDED:
+                    now = time.perf_counter()
+                    lin = nr.instance_linear_iterations()
+                    d = lin - t_state["lin"]
+                    t_state["lin"] = lin
+                    trace.append((now - t_state["t"], int(d.max()), int((d > 0).sum())))
+                    t_state["t"] = now
+            nr.subscribe(on_nr)
         for k in range(args.warmup + args.steps):
+            trace.clear()
             req.assign(req0)
             torch.cuda.synchronize()
             ev0.record(stream)
@@ -738,14 +760,26 @@ def run_batched(args):
                     "instances_taken_out_not_converged": int((conv == -2).sum()),
                     "instances_taken_out_cg_unsolved": int((conv == -4).sum()),
                     "taken_out": [int(i) for i in np.nonzero(conv != 1)[0]]})
+        if args.batched_trace and trace:
+            tr = np.array(trace, dtype=float)
+            capped = tr[:, 1] >= 0.95 * 20000
+            order = np.argsort(-tr[:, 0])[:5]
+            rec["trace"] = {
+                "newton_iterations": len(tr), "wall_s": round(float(tr[:, 0].sum()), 3),
+                "iterations_with_a_cg_at_its_cap": int(capped.sum()),
+                "wall_s_in_those": round(float(tr[capped, 0].sum()), 3),
+                "us_per_cg_iteration_in_those": round(float(tr[capped, 0].sum() / max(tr[capped, 1].sum(), 1)) * 1e6, 2),
+                "slowest_iterations": [{"s": round(float(tr[k, 0]), 4), "largest_cg": int(tr[k, 1]),
+                                        "instances_in_cg": int(tr[k, 2])} for k in order]}
         out[key] = rec
         finals[key], status[key] = req.globalSolution(), conv
         del lc, nr, asm, fes, esc
 
     run_form("mixed", True)
     run_form("plain_fp64", False)
-    run_form("mixed_escalated", True, escalate="ew")
-    run_form("mixed_escalated_to_plain", True, escalate="plain")
+    if not args.batched_trace:
+        run_form("mixed_escalated", True, escalate="ew")
+        run_form("mixed_escalated_to_plain", True, escalate="plain")
 
     def compare(a, b):
         both = np.nonzero((status[a] == 1) & (status[b] == 1))[0]
@@ -768,6 +802,10 @@ def run_batched(args):
                 else None}
 
     out["mixed_vs_plain"] = compare("mixed", "plain_fp64")
+    if args.batched_trace:
+        out["speedup_mixed_alone_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed"]["s"], 3)
+        print(json.dumps(out))
+        return
     out["mixed_escalated_vs_plain"] = compare("mixed_escalated", "plain_fp64")
     out["mixed_escalated_to_plain_vs_plain"] = compare("mixed_escalated_to_plain", "plain_fp64")
     out["speedup_escalated_to_plain_vs_plain_fp64"] = round(out["plain_fp64"]["s"] / out["mixed_escalated_to_plain"]["s"], 3)
