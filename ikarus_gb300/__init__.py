@@ -177,6 +177,7 @@ SIGNATURES = {
     "ikr_newton_set_batched_cg": ([_vp, _I, _I], C.c_int),
     "ikr_newton_batched_cg_launches": ([_vp, _i64p], C.c_int),
     "ikr_newton_batched_cg_variant_launches": ([_vp, _i64p], C.c_int),
+    "ikr_batched_plan_preview": ([_I, _ip, _ip, _I, _I, _ip, _I, _ip, _ip], C.c_int),
     "ikr_newton_set_batched_take_out": ([_vp, _I], C.c_int),
     "ikr_load_control_set_escalation": ([_vp, _vp, _vp], C.c_int),
     "ikr_load_control_escalated": ([_vp, _I, _u8p], C.c_int),
@@ -315,6 +316,18 @@ def _err(code, what=""):
 
 def _ptr(a, t=C.c_double):
     return a.ctypes.data_as(C.POINTER(t))
+
+
+def batched_plan_preview(rows, widths, fp32=True, variant=-1, caps=(456, 304, 304, 304, 0, 304), cluster_cap=7):
+    """The batched CG's planner on given co-resident capacities (no device needed): (variant, CTAs per instance)."""
+    r = np.ascontiguousarray(rows, dtype=np.int32)
+    w = np.ascontiguousarray(widths, dtype=np.int32)
+    cp = np.ascontiguousarray(caps, dtype=np.int32)
+    v = C.c_int32()
+    out = np.zeros(len(r), dtype=np.int32)
+    _err(lib().ikr_batched_plan_preview(len(r), _ptr(r, C.c_int32), _ptr(w, C.c_int32), int(bool(fp32)), int(variant),
+                                        _ptr(cp, C.c_int32), int(cluster_cap), C.byref(v), _ptr(out, C.c_int32)))
+    return v.value, out
 
 
 def kernel_launches() -> int:

@@ -1233,55 +1233,38 @@ int ikr_newton_subscribe_fe_state(ikr_nr nr, int32_t on) {
 namespace ikr_host {
 // Newton-Raphson over independent instances: every instance runs its own Newton iteration and relative
 // convergence test; one assembly and one batched CG launch (CTA per instance) serve all still-active instances.
-// CTA groups of one batched CG launch over the instances in `run`.  In FP32, while every running instance has at most
-// 512 rows and all their clusters fit the device at once, each instance gets a 16-CTA cluster (variant 4).  Otherwise
-// the variants with few rows per CTA go first, as
-// their iterations are the shortest: eight, then four threads per row with the matrix in shared memory, then one row
-// per thread (instance i gets C_i = ceil(rows_i / rows per CTA) CTAs) -- the first whose groups fit the co-resident
-// CTAs of that variant (and at most 256 CTAs per group, rows of at most the variant's blocks); FP64 tries sixteen
-// threads per row first (its iteration is bound by the FP64 pipe: fewer rows per SM), for groups of at most 64 CTAs.
-// Otherwise C_i ~ its
-// rows over the smallest rows-per-CTA q (>= 64 rows per CTA) whose groups fit the variant that loops over rows, and
-// when there are more instances than resident CTAs every group is one CTA (an ordinary launch; no CTA waits on
-// another).  Largest instances first.
-static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const std::vector<int>& run) {
-  auto& P = nr->plan;
-  const int sms = num_sms();
-  const int nr_ = (int)run.size();
-  std::vector<int> rows(nr_), width(nr_, 0), c(nr_, 1), order(nr_);
-  for (int k = 0; k < nr_; ++k) {
-    const int r0 = f->inst_off_h[run[k]], r1 = f->inst_off_h[run[k] + 1];
-    rows[k] = r1 - r0, order[k] = k;
-    for (int sl = r0 >> 5; r1 > r0 && sl <= (r1 - 1) >> 5; ++sl)
-      width[k] = std::max(width[k], a->slice_off_h[sl + 1] - a->slice_off_h[sl]);
-  }
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rows[x] > rows[y]; });
+struct BatchChoice {
   int variant = 0;
-  auto share = [&](int cap) { return std::max(1, (int)(cap * P.share)); };
+  bool cooperative = false;
+  std::vector<int> ctas;  // CTAs per instance (in the input order); 16 per instance for the cluster variant
+};
+
+// The planner itself, on given co-resident capacities (caps[v]: CTAs of variant v, cluster_cap: 16-CTA clusters),
+// rows and widest slice per running instance; kept free of device calls so that it is tested on the host.
+static BatchChoice choose_batch_plan(const std::vector<int>& rows, const std::vector<int>& width, bool fp32,
+                                     int forced, const int (&caps)[6], int cluster_cap) {
+  const int n = (int)rows.size();
+  BatchChoice out;
+  out.ctas.assign(n, 1);
   // FP32: one instance per 16-CTA cluster (vectors and sums in distributed shared memory) while the running
   // instances fit one cluster each and the device holds all their clusters at once
-  if (fp32 && (P.variant == -1 || P.variant == 4)) {
+  if (fp32 && (forced == -1 || forced == 4)) {
     // chosen by the planner only for instances of at most 512 rows: its iteration grows with the rows per CTA (the
     // distributed-shared-memory gathers of 27 blocks per thread), measured 8.4 us at 297 rows against 9.2 us for
     // eight threads per row, but 15.2 against 9.2 us at 2 673 rows
-    const int max_rows = P.variant == 4 ? ikr::batched_cluster_rows() : std::min(512, ikr::batched_cluster_rows());
-    bool fits = nr_ <= share(ikr::batched_cluster_capacity());
-    for (int k = 0; k < nr_ && fits; ++k)
-      fits = rows[k] <= max_rows && width[k] <= ikr::batched_cluster_width();
+    const int max_rows = forced == 4 ? ikr::batched_cluster_rows() : std::min(512, ikr::batched_cluster_rows());
+    bool fits = n <= cluster_cap;
+    for (int k = 0; k < n && fits; ++k) fits = rows[k] <= max_rows && width[k] <= ikr::batched_cluster_width();
     if (fits) {
-      std::vector<int32_t> ci(run.begin(), run.end());
-      P.n_cta = nr_;
-      P.cur_variant = 4;
-      P.cooperative = false;
-      const size_t cap = (size_t)std::max(f->n_inst, 4 * sms);
-      if (P.cta_inst.n < cap) P.cta_inst.alloc(cap);
-      CK(cudaMemcpyAsync(P.cta_inst.p, ci.data(), sizeof(int32_t) * ci.size(), cudaMemcpyHostToDevice, f->stream));
-      return;
+      out.variant = 4;
+      out.ctas.assign(n, 16);
+      return out;
     }
   }
   std::vector<int> cand;
-  if (P.variant >= 0 && P.variant != 4) cand.push_back(P.variant);
-  else if (P.variant == -1) cand = fp32 ? std::vector<int>{3, 2, 1} : std::vector<int>{5, 3, 2, 1};
+  if (forced >= 0 && forced != 4) cand.push_back(forced);
+  else if (forced == -1) cand = fp32 ? std::vector<int>{3, 2, 1} : std::vector<int>{5, 3, 2, 1};
+  std::vector<int> c(n, 1);
   for (int v : cand) {
     if (v == 0) break;
     const int rpc = ikr::batched_pcg_rows_per_cta(v), maxw = ikr::batched_pcg_max_width(v);
@@ -1290,60 +1273,91 @@ static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const 
     // sixteen threads per row pays (FP64) while groups stay small; beyond 64 CTAs the wider group barrier costs more
     // than the spread FP64 work saves (measured on one 2 673-row instance: 23.3 against 20.5 us per iteration)
     const int max_group = v == 5 ? 64 : 256;
-    for (int k = 0; k < nr_ && fits; ++k) {
+    for (int k = 0; k < n && fits; ++k) {
       const int ck = std::max(1, (rows[k] + rpc - 1) / rpc);
       fits = ck <= max_group && width[k] <= maxw;
       c[k] = ck;
       tot += ck;
     }
-    if (fits && tot <= share(ikr::batched_pcg_capacity(fp32, v, sms))) {
-      variant = v;
-      break;
+    if (fits && tot <= caps[v]) {
+      out.variant = v;
+      out.ctas = c;
+      out.cooperative = std::any_of(c.begin(), c.end(), [](int x) { return x > 1; });
+      return out;
     }
   }
-  if (variant == 0) {
-    const int cap = share(ikr::batched_pcg_capacity(fp32, 0, sms));
-    auto sizes_for = [&](int64_t q, std::vector<int>& out) {
-      int64_t t = 0;
-      for (int k = 0; k < nr_; ++k) {
-        int64_t ck = (rows[k] + q - 1) / q;
-        ck = std::min<int64_t>(ck, std::max(1, rows[k] / 64));
-        ck = std::max<int64_t>(1, std::min<int64_t>(ck, 32));
-        out[k] = (int)ck;
-        t += ck;
-      }
-      return t;
-    };
-    std::fill(c.begin(), c.end(), 1);
-    if (nr_ < cap) {
-      int64_t lo = 1, hi = *std::max_element(rows.begin(), rows.end()) + 1;
-      std::vector<int> tmp(nr_);
-      while (lo < hi) {  // smallest rows-per-CTA q whose groups fit the resident CTAs
-        const int64_t mid = (lo + hi) / 2;
-        if (sizes_for(mid, tmp) <= cap) hi = mid;
-        else lo = mid + 1;
-      }
-      sizes_for(lo, c);
+  // rows looped per thread: C_i ~ rows over the smallest rows-per-CTA q (>= 64 rows per CTA) whose groups fit;
+  // with more instances than resident CTAs every group is one CTA (an ordinary launch; no CTA waits on another)
+  const int cap = caps[0];
+  auto sizes_for = [&](int64_t q, std::vector<int>& o) {
+    int64_t t = 0;
+    for (int k = 0; k < n; ++k) {
+      int64_t ck = (rows[k] + q - 1) / q;
+      ck = std::min<int64_t>(ck, std::max(1, rows[k] / 64));
+      ck = std::max<int64_t>(1, std::min<int64_t>(ck, 32));
+      o[k] = (int)ck;
+      t += ck;
     }
+    return t;
+  };
+  if (n < cap) {
+    int64_t lo = 1, hi = *std::max_element(rows.begin(), rows.end()) + 1;
+    std::vector<int> tmp(n);
+    while (lo < hi) {  // smallest rows-per-CTA q whose groups fit the resident CTAs
+      const int64_t mid = (lo + hi) / 2;
+      if (sizes_for(mid, tmp) <= cap) hi = mid;
+      else lo = mid + 1;
+    }
+    sizes_for(lo, out.ctas);
   }
+  out.cooperative = std::any_of(out.ctas.begin(), out.ctas.end(), [](int x) { return x > 1; });
+  return out;
+}
+
+// CTA groups of one batched CG launch over the instances in `run` (choose_batch_plan on the device's co-resident
+// capacities, a share of them while another solver's batched CG runs concurrently); largest instances first.
+static void plan_batch_launch(ikr_nr nr, ikr_fes f, ikr_asm a, bool fp32, const std::vector<int>& run) {
+  auto& P = nr->plan;
+  const int sms = num_sms();
+  const int nr_ = (int)run.size();
+  std::vector<int> rows(nr_), width(nr_, 0), order(nr_);
+  for (int k = 0; k < nr_; ++k) {
+    const int r0 = f->inst_off_h[run[k]], r1 = f->inst_off_h[run[k] + 1];
+    rows[k] = r1 - r0, order[k] = k;
+    for (int sl = r0 >> 5; r1 > r0 && sl <= (r1 - 1) >> 5; ++sl)
+      width[k] = std::max(width[k], a->slice_off_h[sl + 1] - a->slice_off_h[sl]);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rows[x] > rows[y]; });
+  auto share = [&](int cap) { return std::max(1, (int)(cap * P.share)); };
+  int caps[6];
+  for (int v = 0; v < 6; ++v) caps[v] = v == 4 ? 0 : share(ikr::batched_pcg_capacity(fp32, v, sms));
+  const BatchChoice ch =
+      choose_batch_plan(rows, width, fp32, P.variant, caps, fp32 ? share(ikr::batched_cluster_capacity()) : 0);
   std::vector<int32_t> ci, cf, cs;
-  for (int k : order) {
-    const int first = (int)ci.size();
-    for (int m = 0; m < c[k]; ++m) ci.push_back(run[k]), cf.push_back(first), cs.push_back(c[k]);
+  if (ch.variant == 4) {  // one cluster per instance: the kernel takes the instance of each cluster
+    for (int k : order) ci.push_back(run[k]);
+  } else {
+    for (int k : order) {
+      const int first = (int)ci.size();
+      for (int m = 0; m < ch.ctas[k]; ++m) ci.push_back(run[k]), cf.push_back(first), cs.push_back(ch.ctas[k]);
+    }
   }
   cudaStream_t s = f->stream;
   P.n_cta = (int)ci.size();
-  P.cur_variant = variant;
-  P.cooperative = std::any_of(c.begin(), c.end(), [](int v) { return v > 1; });
+  P.cur_variant = ch.variant;
+  P.cooperative = ch.cooperative;
   // the arrays keep their allocation across launches (a plan has at most max(instances, resident CTAs) entries)
   size_t cap = (size_t)f->n_inst;
-  for (int v = 0; v < 4; ++v) cap = std::max(cap, (size_t)ikr::batched_pcg_capacity(fp32, v, sms));
+  for (int v = 0; v < 6; ++v)
+    if (v != 4) cap = std::max(cap, (size_t)ikr::batched_pcg_capacity(fp32, v, sms));
   for (auto* b : {&P.cta_inst, &P.cta_first, &P.cta_size})
     if (b->n < cap) b->alloc(cap);
   if (P.part.n < 4 * cap) P.part.alloc(4 * cap);
   CK(cudaMemcpyAsync(P.cta_inst.p, ci.data(), sizeof(int32_t) * ci.size(), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(P.cta_first.p, cf.data(), sizeof(int32_t) * cf.size(), cudaMemcpyHostToDevice, s));
-  CK(cudaMemcpyAsync(P.cta_size.p, cs.data(), sizeof(int32_t) * cs.size(), cudaMemcpyHostToDevice, s));
+  if (!cf.empty()) {
+    CK(cudaMemcpyAsync(P.cta_first.p, cf.data(), sizeof(int32_t) * cf.size(), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(P.cta_size.p, cs.data(), sizeof(int32_t) * cs.size(), cudaMemcpyHostToDevice, s));
+  }
 }
 
 // The batched CG of one Newton iteration: the instances with act set start their PCG on -R; the solve runs as a
@@ -1831,6 +1845,19 @@ int ikr_load_control_escalated(ikr_lc lc, int32_t n, uint8_t* mask) {
   return guarded([&] {
     need(lc && mask, IKR_ERR_ARG, "null argument");
     for (int i = 0; i < n; ++i) mask[i] = i < (int)lc->escalated.size() ? lc->escalated[i] : 0;
+  });
+}
+int ikr_batched_plan_preview(int32_t n, const int32_t* rows, const int32_t* widths, int32_t fp32, int32_t variant,
+                             const int32_t* caps6, int32_t cluster_cap, int32_t* out_variant, int32_t* out_ctas) {
+  return guarded([&] {
+    need(n > 0 && rows && widths && caps6 && out_variant && out_ctas && variant >= -1 && variant <= 5, IKR_ERR_ARG,
+         "invalid argument");
+    std::vector<int> r(rows, rows + n), w(widths, widths + n);
+    int caps[6];
+    for (int v = 0; v < 6; ++v) caps[v] = caps6[v];
+    const BatchChoice ch = ikr_host::choose_batch_plan(r, w, fp32 != 0, variant, caps, cluster_cap);
+    *out_variant = ch.variant;
+    for (int k = 0; k < n; ++k) out_ctas[k] = ch.ctas[k];
   });
 }
 int ikr_newton_exclude_instances(ikr_nr nr, int32_t n, const uint8_t* mask) {

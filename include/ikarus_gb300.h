@@ -491,6 +491,12 @@ int ikr_newton_set_batched_cg(ikr_nr nr, int32_t variant, int32_t first_chunk);
 int ikr_newton_batched_cg_launches(ikr_nr nr, int64_t* n);
 /* the same per kernel variant 0..5 (six values) */
 int ikr_newton_batched_cg_variant_launches(ikr_nr nr, int64_t* by_variant6);
+/* the batched CG's planner on given capacities, without a device (tests): n running instances with their rows and
+ * widest slice (blocks), the precision, a forced variant (-1: the planner's choice), the co-resident CTAs of each
+ * variant 0..5 (caps6; entry 4 unused) and the co-resident 16-CTA clusters; gives the variant and the CTAs per
+ * instance (16 per instance for the cluster variant) */
+int ikr_batched_plan_preview(int32_t n, const int32_t* rows, const int32_t* widths, int32_t fp32, int32_t variant,
+                             const int32_t* caps6, int32_t cluster_cap, int32_t* out_variant, int32_t* out_ctas);
 /* batched solves (no reference counterpart): unsolved_linear = 1 takes out an instance whose CG ends above its
  * tolerance after linear_max_iter (status -4 in instance_info; in FP32 the attainable accuracy of the tangent can lie
  * above the tolerance, and the direction is then no Newton direction) */
