@@ -24,7 +24,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", "-I" + os.path.join(CUDA_HOME, "include")]
 
 CU_SOURCES = ["element.cu", "element_eas.cu", "element_eas_hyper.cu", "sparse.cu", "solver.cu", "spmv_staged.cu", "cg_persistent.cu", "cg_coarse.cu", "noalloc.cu", "mlp.cu", "batched.cu", "coarse.cu", "krylov.cu"]
-CPP_SOURCES = ["host.cpp", "predictor.cpp", "path_following.cpp", "krylov.cpp", "operators.cpp", "newton_graph.cpp"]
+CPP_SOURCES = ["host.cpp", "batched_host.cpp", "predictor.cpp", "path_following.cpp", "krylov.cpp", "operators.cpp",
+               "newton_graph.cpp"]
 
 
 def _sources():

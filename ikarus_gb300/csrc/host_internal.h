@@ -1381,4 +1381,15 @@ std::unique_ptr<ListenerBase> make_control_logger(ikr_log_sink sink, void* user,
 // Newton-Raphson solve (newtonraphson.hh:193-257); ref_norm > 0 replaces the initial residual norm as the
 // reference of the relative convergence test
 void nr_solve(ikr_nr nr, ikr_req r, double step_size, ikr_nr_info* info, double ref_norm = 0.0);
+// batched_host.cpp: the batched Newton, the batched CG's planner and the precision escalation of a load control
+struct BatchChoice {
+  int variant = 0;
+  bool cooperative = false;
+  std::vector<int> ctas;  // CTAs per instance (in the input order); 16 per instance for the cluster variant
+};
+BatchChoice choose_batch_plan(const std::vector<int>& rows, const std::vector<int>& width, bool fp32, int forced,
+                              const int (&caps)[6], int cluster_cap);
+void nr_solve_batched(ikr_nr nr, ikr_req r, ikr_nr_info* info);
+void escalation_begin(ikr_lc lc, ikr_req r);
+void escalated_step(ikr_lc lc, ikr_req r, double step, double ref, ikr_nr_info& ni);
 }  // namespace ikr_host
